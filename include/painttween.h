@@ -1,0 +1,296 @@
+/*
+ * painttween.h -- C ABI of the GB300-native offset-field synthesis library
+ * (libpainttween_gb300.so).
+ *
+ * This is the drop-in boundary for PaintTween's per-frame offset-field
+ * synthesis: the PatchMatch-style nearest-neighbour-field optimisation run at
+ * each pyramid level, with offset advection along velocity fields for
+ * animations.  Every entry point below replaces one call of the reference's
+ * C++ namespace `TexSynth` (src/PaintTweenCUDA/texSynth_kernel.h:38-91) or of
+ * the per-frame driver that sequences those calls
+ * (src/PaintTweenCUDA/synthesisFrame.cpp, synthesisProcessor.cpp).  The
+ * reference keeps its state in file-scope globals (texture references,
+ * `__constant__ TsParameters gParams`, `gCurrentBuffer`) and exits the process
+ * on any CUDA error; here all state lives in an opaque context and every call
+ * returns a status code.
+ *
+ * Conventions
+ *  - Host arrays are owned by the caller; device memory is owned by the
+ *    context.  Host pointers are plain row-major arrays of the level size.
+ *  - One context per host thread; a context is bound to one CUDA device and
+ *    one stream (created by pt_create).
+ *  - Image-size buffers are allocated at full (level-0) resolution; level L
+ *    uses the top-left (W>>L) x (H>>L) rectangle, as in the reference
+ *    (src/PaintTweenCUDA/cudaImageBuffer.h:124-129).
+ *  - No call falls back to the CPU: if the CUDA kernels cannot run the call
+ *    returns PT_ERR_CUDA.
+ */
+#ifndef PAINTTWEEN_GB300_H
+#define PAINTTWEEN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PT_ABI_VERSION 1
+#define PT_MAX_STYLES 5 /* NUM_MAX_STYLES, texSynth_interface.h:37 */
+
+typedef enum {
+    PT_OK = 0,
+    PT_ERR_INVALID = 1,     /* bad argument, size or layer */
+    PT_ERR_CUDA = 2,        /* CUDA runtime error (message in pt_last_error) */
+    PT_ERR_OOM = 3,         /* device allocation failed */
+    PT_ERR_STATE = 4,       /* call made before the state it needs exists */
+    PT_ERR_UNSUPPORTED = 5, /* feature outside the implemented path */
+    PT_ERR_TIMEOUT = 6,     /* a bounded device wait gave up */
+    PT_ERR_BUDGET = 7       /* request does not fit the context's HBM budget */
+} pt_status;
+
+/* One offset-field sample; same field order, types and 36-byte size as the
+ * reference's PatchXF (src/PaintTweenCUDA/types.h:94-109). */
+typedef struct {
+    float x, y, theta, hysteresis;
+    int32_t layer;
+    float scaleU, scaleV;
+    float lumShiftY, lumShiftA; /* Luminance luminanceShift {y, a} */
+} pt_patchxf;
+
+/* Pass direction (types.h:122-126). */
+enum { PT_FORWARD = 0, PT_BACKWARD = 1, PT_BIDIRECTIONAL = 2 };
+
+/* Synthesis schemes (types.h:128-134); FMBM and FMBM_RM are implemented. */
+enum { PT_S_FMBM = 0, PT_S_FMBM_RM = 1, PT_S_FBMO = 2, PT_S_TCTF = 3, PT_S_IND = 4 };
+
+/* Random-number mode.
+ *  PT_RNG_REFERENCE: the reference's behaviour -- the random-offset pyramid
+ *    is the glibc srand(frame*level)/rand() sequence of
+ *    SynthesisFrame::createRandomPyramid (synthesisFrame.cpp:66-150), and the
+ *    scatter search uses r = theta = 0 because the reference's randFloat()
+ *    returns an unsigned int (texSynth_util.h:155-163).
+ *  PT_RNG_COUNTER: counter-based hash candidates (seeded, order-independent)
+ *    for both the random pyramid and a real random search. */
+enum { PT_RNG_REFERENCE = 0, PT_RNG_COUNTER = 1 };
+
+/* Field-for-field copy of TsParameters (texSynth_interface.h:79-152); C bools
+ * are int32 here.  The trailing fields are this library's additions. */
+typedef struct {
+    int32_t residualWindowSize; /* patch radius r: taps in [-r, r]^2 */
+    float coherenceWeight;
+    float distTransWeight;
+    float lumShiftWeight;
+    int32_t lumShiftEnable;
+    float inputAnalogyWeight;
+    float canvasOutputWeight;
+    int32_t numStyles;
+    float offsetsHistogramSlope[PT_MAX_STYLES];
+    float offsetsHistogramThreshold[PT_MAX_STYLES];
+    float maxDistortion;
+    float alphaWeight;
+    int32_t transparencyOk;
+    float styleObjIdWeight;
+    int32_t orientationEnabled;
+    int32_t colorspace; /* 0 = RGB (1 = Lab is not implemented) */
+    float coherenceRatioRange;
+    float coherenceAngleRange;
+    int32_t levels;
+    int32_t scatterSamplesCount;
+    float advectionJitter;
+    float timeDerivativeInputWeight;
+    float timeDerivativeOutputWeight;
+    float temporalCoherenceWeight;
+    float hysteresisWeight;
+    int32_t interpolateKeyFrame; /* must be 0: keyframe mode not implemented */
+    int32_t useGuide;
+    int32_t currentInterpolationIndex;
+    int32_t numFrames;
+    int32_t numKeyFrames;
+    int32_t firstKeyIndex;
+    int32_t lastKeyIndex;
+    int32_t distTransCull;
+    float residualWindowScaleU, residualWindowScaleV;
+    int32_t direction; /* PT_FORWARD / PT_BACKWARD / PT_BIDIRECTIONAL */
+    /* --- driver parameters (NLParameters "iterations", "fixupPasses",
+     *     "synthesisScheme", "maxLevel"; GUI/nlParameters.cpp:106-144) --- */
+    int32_t iterations;
+    int32_t fixupPasses;
+    int32_t scheme;
+    int32_t finalLevel;
+    int32_t rngMode;     /* PT_RNG_* */
+    uint32_t rngSeed;    /* seed of PT_RNG_COUNTER */
+    int32_t reserved[6];
+} pt_params;
+
+/* Image layers (TsImageLayer, texSynth_interface.h:53-77, in-scope subset;
+ * the numeric values are the reference's). */
+enum {
+    PT_LAYER_EXEMPLAR_BASE = 0,
+    PT_LAYER_EXEMPLAR_OUTPUT = 1,
+    PT_LAYER_EXEMPLAR_ORIENTATION = 2,
+    PT_LAYER_EXEMPLAR_DIST_TRANS = 3,
+    PT_LAYER_EXEMPLAR_OBJECT_IDS = 4,
+    PT_LAYER_INPUT_COLOR = 5,
+    PT_LAYER_INPUT_ORIENTATION = 6,
+    PT_LAYER_INPUT_DIST_TRANS = 7,
+    PT_LAYER_INPUT_SCALE = 8,
+    PT_LAYER_INPUT_ID = 9,
+    PT_LAYER_INPUT_VEL_B = 11,
+    PT_LAYER_INPUT_VEL_F = 12,
+    PT_LAYER_INPUT_VEL_B_PREVIOUS = 13,
+    PT_LAYER_INPUT_VEL_F_PREVIOUS = 14,
+    PT_LAYER_RANDOM = 21
+};
+
+/* syncBuffers / advect / merge flags (texSynth_kernel.h:79-91). */
+enum {
+    PT_DONT_COPY_OFFSETS = 0x01,
+    PT_DONT_UPDATE_RESIDUAL = 0x10,
+    PT_MERGE_FALLBACK_RANDOM = 0x20,
+    PT_MERGE_FALLBACK_LAST_PASS = 0x40
+};
+enum {
+    PT_ADVECT_IGNORE_RANDOM = 0x1,
+    PT_ADVECT_DO_NOT_CHECK_PREVIOUS = 0x10,
+    PT_ADVECT_CHECK_FRAME_TO_KEY = 0x20,
+    PT_ADVECT_UPDATE_RESIDUAL = 0x80
+};
+
+typedef struct pt_ctx pt_ctx;
+
+/* ---- context ------------------------------------------------------------ */
+
+/* Creates a context on `device` with its own stream.  `hbm_budget_bytes`
+ * caps the device memory the context may allocate (0 = no cap).
+ * Replaces SynthesisProcessor's ownership of WorkingBuffers
+ * (synthesisProcessor.cpp:109,119). */
+pt_status pt_create(int device, size_t hbm_budget_bytes, pt_ctx** out);
+pt_status pt_destroy(pt_ctx* ctx);
+const char* pt_status_string(pt_status s);
+/* Last error message of this context (never NULL). */
+const char* pt_last_error(const pt_ctx* ctx);
+/* ABI version number (PT_ABI_VERSION). */
+int pt_abi_version(void);
+/* Default parameters: NLParameters::getTsDefaultParams
+ * (GUI/nlParameters.cpp:63-104) plus iterations 3, fixupPasses 1,
+ * scheme FMBM_RM (nlParameters.cpp:133-137) and distTransCull 50
+ * (synthesisProcessor.cpp:220). */
+void pt_default_params(pt_params* out);
+/* Device memory currently held by the context, in bytes. */
+size_t pt_device_bytes(const pt_ctx* ctx);
+
+/* ---- configuration (TexSynth::setup / uploadParameters,
+ *      texSynth_kernel.cu:109-123) ---------------------------------------- */
+pt_status pt_set_params(pt_ctx* ctx, const pt_params* params);
+pt_status pt_get_params(const pt_ctx* ctx, pt_params* out);
+
+/* Allocates the image-size working buffers (offsets, residual, canvas,
+ * advected F/B) at image_w x image_h and the style-size histogram at
+ * style_w x (style_h * num_styles); everything is zeroed.
+ * Replaces WorkingBuffers::initialize (workingBuffers.cpp:48-94) and
+ * TexSynth::initialize_images (texSynth_kernel.cu:2120-2126). */
+pt_status pt_initialize(pt_ctx* ctx, int image_w, int image_h,
+                        int style_w, int style_h, int num_styles);
+/* Sizes the exemplar arrays for one pyramid level (w, h = level size).
+ * Replaces TexSynth::initialize_exemplars (texSynth_kernel.cu:2128-2135). */
+pt_status pt_initialize_exemplars(pt_ctx* ctx, int w, int h, int num_styles);
+
+/* Uploads one pyramid level of one layer from host memory; w, h must be the
+ * level size.  `style` selects the exemplar layer (style index).
+ * Replaces TexSynth::uploadImage_{Color4,float,float2,int}
+ * (texSynth_kernel.cu:2143-2253). */
+pt_status pt_upload_image_color4(pt_ctx* ctx, int level, int layer,
+                                 const float* rgba, int w, int h, int style);
+pt_status pt_upload_image_float(pt_ctx* ctx, int level, int layer,
+                                const float* data, int w, int h, int style);
+pt_status pt_upload_image_float2(pt_ctx* ctx, int level, int layer,
+                                 const float* xy, int w, int h);
+pt_status pt_upload_image_int(pt_ctx* ctx, int level, int layer,
+                              const int32_t* data, int w, int h, int style);
+/* Swaps the current/previous frame layers (TexSynth::flipAnimBuffers,
+ * texSynth_kernel.cu:1534-1538). */
+pt_status pt_flip_anim_buffers(pt_ctx* ctx);
+
+/* ---- per-step compute (TexSynth::*, texSynth_kernel.h:58-76) ------------ */
+
+/* Builds the random-offset level from the uploaded input colour/orientation
+ * and exemplar output/orientation, on the device; replaces
+ * SynthesisFrame::createRandomPyramid (synthesisFrame.cpp:66-150). */
+pt_status pt_create_random_level(pt_ctx* ctx, int level, int frame);
+pt_status pt_randomize_offsets(pt_ctx* ctx, int level);          /* :2100 */
+pt_status pt_propagate(pt_ctx* ctx, int level, int jump, int key_index); /* :1306 */
+pt_status pt_scatter(pt_ctx* ctx, int level, int key_index);      /* :1360 */
+pt_status pt_upsample(pt_ctx* ctx, int fine_level);               /* :1513 */
+pt_status pt_advect_offsets(pt_ctx* ctx, int level, int time_step,
+                            int forwards, int op_flags);           /* :1695 */
+pt_status pt_merge_randomly(pt_ctx* ctx, int level, int forwards,
+                            float weight_advected, int force_valid); /* :2003 */
+pt_status pt_merge_using_residual(pt_ctx* ctx, int level, int forwards); /* :1978 */
+pt_status pt_update_residual_cache(pt_ctx* ctx, int level);       /* :1221 */
+pt_status pt_sync_buffers(pt_ctx* ctx, int level, int op_flags);  /* :1240 */
+pt_status pt_reset_advected_buffers(pt_ctx* ctx); /* workingBuffers.cpp:112-116 */
+
+/* ---- state transfer (WorkingBuffers load/getOutput,
+ *      workingBuffers.cpp:118-207) ---------------------------------------- */
+/* Writes the level rectangle of the offsets base buffer (loadOffsets). */
+pt_status pt_load_offsets(pt_ctx* ctx, int level, const pt_patchxf* offsets);
+/* Writes the level rectangle of the residual buffer, rounding each value
+ * through IEEE half precision as the reference's EXR round trip does
+ * (loadResidual reads the half-precision .b channel). */
+pt_status pt_load_residual(pt_ctx* ctx, int level, const float* residual);
+pt_status pt_get_offsets(pt_ctx* ctx, int level, pt_patchxf* out);
+pt_status pt_get_residual(pt_ctx* ctx, int level, float* out);
+/* Stylised output (canvasOutputCache), RGBA float32. */
+pt_status pt_get_output(pt_ctx* ctx, int level, float* out_rgba);
+
+/* ---- working-set level API (pyramids built and kept on the device) ----- */
+
+/* Uploads one style exemplar at level-0 size and builds its pyramid on the
+ * device (2x2 average for colours/DT, structure-tensor average then angle for
+ * orientation, 2x2 majority vote for IDs; downsample.cpp:41-209,
+ * GUI/nlDataAccess.cpp:82-93).  orient_tensor is (xx, xy, yy) per pixel; NULL
+ * orient_tensor/dt/ids mean zero images, as the reference substitutes blank
+ * images for missing elements (GUI/nlDataAccess.cpp:331-341). */
+pt_status pt_set_style(pt_ctx* ctx, int style, int w, int h,
+                       const float* base_rgba, const float* output_rgba,
+                       const float* orient_tensor, const float* dist_trans,
+                       const int32_t* object_ids);
+/* Uploads the inputs of one frame at level-0 size and builds its pyramids on
+ * the device; velocities are averaged and halved per level
+ * (DOWNSAMPLE_SCALE_WITH_LEVELS, downsample.cpp:69-72).  NULL vel/scale mean
+ * zero velocities / unit scale. Frames stay resident until pt_clear_frames. */
+pt_status pt_set_frame(pt_ctx* ctx, int frame, int w, int h,
+                       const float* rgba, const float* orient_tensor,
+                       const float* dist_trans, const int32_t* object_ids,
+                       const float* vel_fwd, const float* vel_bwd,
+                       const float* scale);
+pt_status pt_clear_frames(pt_ctx* ctx);
+
+/* Synthesises one still (renderAnimationFMBM with one frame,
+ * synthesisProcessor.cpp:846-878 -> synthesizeConsecutive,
+ * synthesisFrame.cpp:214-323).  Outputs at level finalLevel; either output
+ * pointer may be NULL. */
+pt_status pt_synthesize_frame(pt_ctx* ctx, int frame, float* out_rgba,
+                              pt_patchxf* out_offsets);
+
+/* Called once per frame with the final stylised output of the animation. */
+typedef void (*pt_frame_callback)(int frame, const float* rgba,
+                                  const pt_patchxf* offsets, int w, int h,
+                                  void* user);
+/* Synthesises frames first..last (all uploaded with pt_set_frame) with the
+ * forward/backward consecutive-pass scheme FMBM(_RM)
+ * (synthesisProcessor.cpp:703-753,846-878). */
+pt_status pt_synthesize_animation(pt_ctx* ctx, int first, int last,
+                                  pt_frame_callback cb, void* user);
+
+/* Number of this library's kernel launches issued so far by the context. */
+uint64_t pt_kernel_launches(const pt_ctx* ctx);
+/* Blocks until the context's stream is idle. */
+pt_status pt_synchronize(pt_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PAINTTWEEN_GB300_H */

@@ -1,0 +1,442 @@
+"""Python side of the CPU oracle (test infrastructure only).
+
+Loads oracle/libpt_oracle.so (the C restatement of the reference's kernels)
+and drives it in the reference's call sequence:
+
+* SynthesisProcessor::renderAnimationFMBM / renderConsecutivePass
+  (src/PaintTweenCUDA/synthesisProcessor.cpp:703-753,846-878)
+* SynthesisFrame::synthesizeConsecutive / propagateAndScatter
+  (src/PaintTweenCUDA/synthesisFrame.cpp:214-323,483-508)
+* the EXR temp-file round trip between levels and passes becomes an
+  in-memory store (offsets exact, residual rounded through half precision as
+  WorkingBuffers::loadResidual reads the half .b channel).
+
+Only tests, __graft_entry__.smoke() and bench.py's CPU baseline may use this
+module, and only as the checker / the timed CPU baseline.
+"""
+import ctypes
+import math
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+from painttween_gb300 import _abi  # noqa: E402  (ABI layout only)
+
+_LIB = None
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        from oracle import build as _build
+        path = _build.build()
+        L = ctypes.CDLL(path)
+        vp, i, f, u32 = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_uint32
+        sig = {
+            "pto_create": (vp, [i, i, i, i, i]),
+            "pto_destroy": (None, [vp]),
+            "pto_set_threads": (None, [vp, i]),
+            "pto_set_params": (None, [vp, ctypes.POINTER(_abi.Params)]),
+            "pto_init_exemplars": (None, [vp, i, i, i]),
+            "pto_upload_exemplar": (None, [vp, i, vp, vp, vp, vp, vp]),
+            "pto_upload_layered": (None, [vp, i, vp, i, i]),
+            "pto_upload_plain": (None, [vp, i, vp, i, i]),
+            "pto_flip": (None, [vp]),
+            "pto_copy_base_to_working": (None, [vp]),
+            "pto_reset_advected": (None, [vp]),
+            "pto_randomize": (None, [vp, i]),
+            "pto_propagate": (None, [vp, i, i]),
+            "pto_scatter": (None, [vp, i]),
+            "pto_update_residual": (None, [vp, i]),
+            "pto_sync": (None, [vp, i, i]),
+            "pto_upsample": (None, [vp, i]),
+            "pto_advect": (None, [vp, i, i, i, i]),
+            "pto_merge_randomly": (None, [vp, i, i, f, i]),
+            "pto_merge_using_residual": (None, [vp, i, i]),
+            "pto_load_offsets": (None, [vp, i, vp]),
+            "pto_load_residual": (None, [vp, i, vp]),
+            "pto_get_offsets": (None, [vp, i, vp]),
+            "pto_get_residual": (None, [vp, i, vp]),
+            "pto_get_output": (None, [vp, i, vp]),
+            "pto_energy_map": (None, [vp, i, vp, vp, vp]),
+            "pto_sinf": (f, [f]), "pto_cosf": (f, [f]),
+            "pto_atan2f": (f, [f, f]), "pto_logf": (f, [f]), "pto_acosf": (f, [f]),
+            "pto_half_roundtrip": (f, [f]),
+            "pto_glibc_stream": (None, [u32, i, vp]),
+            "pto_random_level": (i, [u32, i, i, i, i, i, vp, vp, vp, vp, i, i, i, vp]),
+            "pto_downsample_avg": (None, [vp, i, i, i, f, vp]),
+            "pto_downsample_vote": (None, [vp, i, i, vp]),
+            "pto_tensor_to_angle": (None, [vp, i, vp]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _c(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+# ---------------------------------------------------------------------------
+# pyramids (downsample.cpp:41-209, GUI/nlDataAccess.cpp:82-93)
+# ---------------------------------------------------------------------------
+
+def num_levels(w, h):
+    """ImagePyramid level count, imagePyramid.cpp:86 / downsample.cpp:47."""
+    return int(min(math.floor(math.log2(w)), math.floor(math.log2(h))))
+
+
+def pyramid_avg(img, vel=False):
+    img = _c(img, np.float32)
+    h, w = img.shape[:2]
+    ch = 1 if img.ndim == 2 else img.shape[2]
+    out = [img]
+    for _ in range(1, num_levels(w, h)):
+        cur = out[-1]
+        ch_, cw = cur.shape[:2]
+        dst = np.empty((ch_ >> 1, cw >> 1) + cur.shape[2:], np.float32)
+        lib().pto_downsample_avg(_p(cur), cw, ch_, ch, 1.0 if vel else 0.0, _p(dst))
+        out.append(dst)
+    return out
+
+
+def pyramid_vote(ids):
+    ids = _c(ids, np.int32)
+    h, w = ids.shape
+    out = [ids]
+    for _ in range(1, num_levels(w, h)):
+        cur = out[-1]
+        dst = np.empty((cur.shape[0] >> 1, cur.shape[1] >> 1), np.int32)
+        lib().pto_downsample_vote(_p(cur), cur.shape[1], cur.shape[0], _p(dst))
+        out.append(dst)
+    return out
+
+
+def tensor_to_angle(t3):
+    t3 = _c(t3, np.float32)
+    out = np.empty(t3.shape[:2], np.float32)
+    lib().pto_tensor_to_angle(_p(t3), out.size, _p(out))
+    return out
+
+
+def pyramid_orientation(tensor):
+    return [tensor_to_angle(t) for t in pyramid_avg(tensor)]
+
+
+def style_pyramids(ex):
+    w, h = ex["w"], ex["h"]
+    z = np.zeros((h, w), np.float32)
+    return dict(
+        base=pyramid_avg(ex["base"]), output=pyramid_avg(ex["output"]),
+        orient=pyramid_orientation(ex.get("orient_tensor", np.zeros((h, w, 3), np.float32))),
+        dt=pyramid_avg(ex.get("dist_trans", z)),
+        ids=pyramid_vote(ex.get("object_ids", np.zeros((h, w), np.int32))),
+        w=w, h=h)
+
+
+def frame_pyramids(fr):
+    w, h = fr["w"], fr["h"]
+    return dict(
+        rgba=pyramid_avg(fr["rgba"]),
+        orient=pyramid_orientation(fr["orient_tensor"]),
+        dt=pyramid_avg(fr["dist_trans"]),
+        ids=pyramid_vote(fr["object_ids"]),
+        velf=pyramid_avg(fr.get("vel_fwd", np.zeros((h, w, 2), np.float32)), vel=True),
+        velb=pyramid_avg(fr.get("vel_bwd", np.zeros((h, w, 2), np.float32)), vel=True),
+        scale=pyramid_avg(fr.get("scale", np.ones((h, w, 2), np.float32))),
+        w=w, h=h)
+
+
+def glibc_stream(seed, n):
+    out = np.empty(n, np.int32)
+    lib().pto_glibc_stream(seed & 0xFFFFFFFF, n, _p(out))
+    return out
+
+
+def random_level(seed, level, style_w0, style_h0, img_rgba, img_orient, ex_out, ex_orient,
+                 transparency_ok=False, orientation_enabled=True):
+    """SynthesisFrame::createRandomPyramid for one level (synthesisFrame.cpp:66-150)."""
+    h, w = img_orient.shape
+    ew = ex_orient.shape[1]
+    out = np.empty((h, w, 4), np.float32)
+    lib().pto_random_level(seed & 0xFFFFFFFF, w, h, level, style_w0, style_h0,
+                           _p(_c(img_rgba, np.float32)), _p(_c(img_orient, np.float32)),
+                           _p(_c(ex_out, np.float32)), _p(_c(ex_orient, np.float32)), ew,
+                           int(transparency_ok), int(orientation_enabled), _p(out))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# step-wise oracle with the TexSynth call surface
+# ---------------------------------------------------------------------------
+
+class Oracle:
+    """CPU restatement of TexSynth::* over the reference's buffer model."""
+
+    def __init__(self, W, H, SW, SH, NS=1, threads=1):
+        self.W, self.H, self.SW, self.SH, self.NS = W, H, SW, SH, NS
+        self.h = lib().pto_create(W, H, SW, SH, NS)
+        lib().pto_set_threads(self.h, threads)
+        self.params = _abi.default_params()
+
+    def close(self):
+        if self.h:
+            lib().pto_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_threads(self, n):
+        lib().pto_set_threads(self.h, n)
+
+    def set_params(self, p):
+        self.params = p.copy()
+        lib().pto_set_params(self.h, ctypes.byref(self.params))
+
+    def lw(self, level):
+        return self.W >> level
+
+    def lh(self, level):
+        return self.H >> level
+
+    # --- uploads -----------------------------------------------------------
+    def load_style_level(self, styles, level):
+        """Style::load(level), style.cpp:62-140."""
+        s0 = styles[0]
+        ew, eh = s0["w"] >> level, s0["h"] >> level
+        lib().pto_init_exemplars(self.h, ew, eh, len(styles))
+        self._ex = []
+        for k, s in enumerate(styles):
+            arrs = [_c(s["base"][level], np.float32), _c(s["output"][level], np.float32),
+                    _c(s["orient"][level], np.float32), _c(s["dt"][level], np.float32),
+                    _c(s["ids"][level], np.int32)]
+            lib().pto_upload_exemplar(self.h, k, *[_p(a) for a in arrs])
+            self._ex.append(arrs)
+
+    def load_frame_level(self, fp, level):
+        """SynthesisFrame::loadImages + loadAnimImages, synthesisFrame.cpp:562-656."""
+        L = lib()
+        w, h = self.lw(level), self.lh(level)
+        L.pto_upload_layered(self.h, _abi.LAYER_INPUT_COLOR, _p(_c(fp["rgba"][level], np.float32)), w, h)
+        L.pto_upload_plain(self.h, _abi.LAYER_INPUT_ORIENTATION, _p(_c(fp["orient"][level], np.float32)), w, h)
+        L.pto_upload_plain(self.h, _abi.LAYER_INPUT_ID, _p(_c(fp["ids"][level], np.int32)), w, h)
+        L.pto_upload_layered(self.h, _abi.LAYER_INPUT_VEL_B, _p(_c(fp["velb"][level], np.float32)), w, h)
+        L.pto_upload_layered(self.h, _abi.LAYER_INPUT_VEL_F, _p(_c(fp["velf"][level], np.float32)), w, h)
+        L.pto_upload_layered(self.h, _abi.LAYER_INPUT_DIST_TRANS, _p(_c(fp["dt"][level], np.float32)), w, h)
+        L.pto_upload_plain(self.h, _abi.LAYER_INPUT_SCALE, _p(_c(fp["scale"][level], np.float32)), w, h)
+
+    def upload_random(self, rnd):
+        h, w = rnd.shape[:2]
+        lib().pto_upload_plain(self.h, _abi.LAYER_RANDOM, _p(_c(rnd, np.float32)), w, h)
+
+    def flip(self):
+        lib().pto_flip(self.h)
+
+    def reset_advected(self):
+        lib().pto_reset_advected(self.h)
+
+    # --- TexSynth compute calls (each ends with syncBuffers as the reference's
+    #     host wrappers do) --------------------------------------------------
+    def randomize_offsets(self, level):
+        lib().pto_randomize(self.h, level)
+
+    def propagate(self, level, jump):
+        lib().pto_propagate(self.h, level, jump)
+        lib().pto_sync(self.h, level, 0)
+
+    def scatter(self, level):
+        lib().pto_scatter(self.h, level)
+        lib().pto_sync(self.h, level, 0)
+
+    def upsample(self, level):
+        lib().pto_upsample(self.h, level)
+
+    def advect(self, level, time_step, forwards, flags):
+        lib().pto_advect(self.h, level, time_step, int(forwards), flags)
+
+    def merge_randomly(self, level, forwards, weight=0.5, force=False):
+        lib().pto_merge_randomly(self.h, level, int(forwards), weight, int(force))
+
+    def merge_using_residual(self, level, forwards):
+        lib().pto_merge_using_residual(self.h, level, int(forwards))
+
+    def update_residual(self, level):
+        lib().pto_update_residual(self.h, level)
+
+    def sync(self, level, flags=0):
+        lib().pto_sync(self.h, level, flags)
+
+    # --- state ---------------------------------------------------------------
+    def load_offsets(self, level, offs):
+        lib().pto_load_offsets(self.h, level, _p(np.ascontiguousarray(offs)))
+
+    def load_residual(self, level, res):
+        lib().pto_load_residual(self.h, level, _p(_c(res, np.float32)))
+
+    def get_offsets(self, level):
+        out = np.empty((self.lh(level), self.lw(level)), _abi.PATCH_DTYPE)
+        lib().pto_get_offsets(self.h, level, _p(out))
+        return out
+
+    def get_residual(self, level):
+        out = np.empty((self.lh(level), self.lw(level)), np.float32)
+        lib().pto_get_residual(self.h, level, _p(out))
+        return out
+
+    def get_output(self, level):
+        out = np.empty((self.lh(level), self.lw(level), 4), np.float32)
+        lib().pto_get_output(self.h, level, _p(out))
+        return out
+
+    def energy_map(self, level, offs, f32=True, f64=True):
+        offs = np.ascontiguousarray(offs)
+        o32 = np.empty(offs.shape, np.float32) if f32 else None
+        o64 = np.empty(offs.shape, np.float64) if f64 else None
+        lib().pto_energy_map(self.h, level, _p(offs),
+                             _p(o32) if f32 else None, _p(o64) if f64 else None)
+        return o32, o64
+
+
+# ---------------------------------------------------------------------------
+# the reference's per-frame driver, restated over the oracle
+# ---------------------------------------------------------------------------
+
+class OracleDriver:
+    """renderAnimationFMBM + renderConsecutivePass + synthesizeConsecutive."""
+
+    def __init__(self, params, styles, frames, threads=1):
+        self.user = params.copy()
+        self.styles = [style_pyramids(s) for s in styles]
+        self.frames = {i: frame_pyramids(f) for i, f in enumerate(frames)}
+        f0 = frames[0]
+        self.W, self.H = f0["w"], f0["h"]
+        sw = max(s["w"] for s in styles)
+        sh = max(s["h"] for s in styles)
+        self.o = Oracle(self.W, self.H, sw, sh, len(styles), threads=threads)
+        self.store = {}
+        self.levels = params.levels
+
+    def _update_parameters(self, frame, direction):
+        """SynthesisFrame::updateParameters, synthesisFrame.cpp:522-542."""
+        p = self.user.copy()
+        p.advectionJitter = self.user.advectionJitter * 0.01 if frame % 3 == 0 else 0.0
+        p.direction = direction
+        self.o.set_params(p)
+
+    def _random_level(self, frame, level):
+        """createRandomPyramid (single style)."""
+        fp = self.frames[frame]
+        s = self.styles[0]
+        rnd = random_level(frame * level, level, s["w"], s["h"], fp["rgba"][level],
+                           fp["orient"][level], s["output"][level], s["orient"][level],
+                           bool(self.user.transparencyOk), bool(self.user.orientationEnabled))
+        self.o.upload_random(rnd)
+
+    def _save(self, level, frame, pass_):
+        self.store[(level, frame, pass_)] = (self.o.get_offsets(level), self.o.get_residual(level),
+                                            self.o.get_output(level))
+
+    def _load_offsets(self, level, frame, pass_):
+        self.o.load_offsets(level, self.store[(level, frame, pass_)][0])
+
+    def _load_residual(self, level, frame, pass_):
+        self.o.load_residual(level, self.store[(level, frame, pass_)][1])
+
+    def propagate_and_scatter(self, level, iterations):
+        """synthesisFrame.cpp:483-508."""
+        for itr in range(iterations):
+            j = 128
+            while j > 1:
+                self.o.propagate(level, j)
+                j //= 2
+            self.o.propagate(level, 1)
+            self.o.propagate(level, 1)
+            if itr < iterations - 1:
+                self.o.scatter(level)
+
+    def synthesize_consecutive(self, frame, level, pass_, is_first, forwards, source_pass, first_pass):
+        o = self.o
+        self._update_parameters(frame, _abi.FORWARD if forwards else _abi.BACKWARD)
+        rm = self.user.scheme == _abi.S_FMBM_RM
+        ops = 0 if rm else _abi.ADVECT_UPDATE_RESIDUAL
+        coarsest = level == self.levels - 1
+        if first_pass:
+            self._random_level(frame, level)
+            if is_first:
+                if coarsest:
+                    o.randomize_offsets(level)
+                else:
+                    self._load_offsets(level + 1, frame, source_pass)
+                    o.upsample(level)
+                    o.sync(level)
+            if not is_first and coarsest:
+                o.advect(level, 1, forwards, ops)
+                # copyBaseToWorking
+                self._copy_base_to_working(level)
+            elif not is_first:
+                o.advect(level, 1, forwards, ops | _abi.ADVECT_IGNORE_RANDOM)
+                self._load_offsets(level + 1, frame, source_pass)
+                self._load_residual(level + 1, frame, source_pass)
+                o.upsample(level)
+                o.sync(level)
+                if rm:
+                    o.merge_randomly(level, forwards, 0.5, False)
+                else:
+                    o.merge_using_residual(level, forwards)
+        else:
+            o.advect(level, 1, forwards, ops | _abi.ADVECT_IGNORE_RANDOM)
+            self._load_offsets(level, frame, pass_ - 1)
+            self._load_residual(level, frame, pass_ - 1)
+            o.sync(level, _abi.DONT_COPY_OFFSETS | _abi.DONT_UPDATE_RESIDUAL)
+            if rm:
+                o.merge_randomly(level, forwards, 0.5, False)
+            else:
+                o.merge_using_residual(level, forwards)
+        o.sync(level)
+        self.propagate_and_scatter(level, self.user.iterations)
+        self._save(level, frame, pass_)
+
+    def _copy_base_to_working(self, level):
+        """CudaBufferPair::copyBaseToWorking for the offsets pair."""
+        lib().pto_copy_base_to_working(self.o.h)
+
+    def render(self, first, last):
+        """renderAnimationFMBM, synthesisProcessor.cpp:846-878."""
+        total = self.user.fixupPasses + 1
+        for level in range(self.levels - 1, self.user.finalLevel - 1, -1):
+            self.o.load_style_level(self.styles, level)
+            self.o.reset_advected()
+            for pass_ in range(total):
+                self._render_pass(level, pass_, total - 1, first, last)
+        final_pass = total - 1 if self.user.finalLevel == 0 else 0
+        return {f: self.store[(self.user.finalLevel, f, final_pass)] for f in range(first, last + 1)}
+
+    def _render_pass(self, level, pass_, source_pass, first, last):
+        """renderConsecutivePass, synthesisProcessor.cpp:703-753."""
+        forwards = (pass_ % 2) == 0
+        frames = list(range(first, last + 1)) if forwards else list(range(last, first - 1, -1))
+        if pass_ > 0:
+            self._save(level, frames[0], pass_)
+            frames = frames[1:]
+        for i, f in enumerate(frames):
+            is_first = (i == 0) and (pass_ == 0)
+            if not is_first:
+                self.o.flip()
+            self.o.load_frame_level(self.frames[f], level)
+            self.synthesize_consecutive(f, level, pass_, is_first, forwards, source_pass, pass_ == 0)
+

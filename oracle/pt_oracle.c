@@ -1,0 +1,1370 @@
+/*
+ * pt_oracle.c -- CPU oracle for PaintTween's offset-field synthesis.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
+ * CPU-baseline leg of bench.py may load this library, and only as the checker
+ * (or the timed CPU baseline); the product library never calls it.
+ *
+ * What it is: a scalar C restatement of the reference's hot path
+ * (src/PaintTweenCUDA/texSynth_kernel.cu, texSynth_util.h, cudaImageBuffer.h,
+ * convolution.cu, synthesisFrame.cpp, downsample.cpp), operating on the same
+ * buffer model as the reference: full-resolution buffers whose level-L data
+ * occupies the top-left (W>>L) x (H>>L) rectangle, persistent across levels
+ * and frames.  Every function cites the reference lines it follows.
+ *
+ * Parity status: UNPINNED against the reference itself.  The reference ships
+ * no tests, golden vectors or fixtures for this path, and its CUDA sources do
+ * not compile with the installed CUDA 13 (legacy texture references and
+ * cudaThreadSynchronize are removed), so no reference output can be produced.
+ * The glibc rand() restatement is pinned against the C library's rand().
+ *
+ * Arithmetic contract (shared, by specification, with the CUDA kernels so the
+ * two agree bit for bit): FP32 everywhere the reference uses float, with
+ *  - contraction off (-ffp-contract=off) and fused multiply-adds written out
+ *    with fmaf() at the places listed in the comments;
+ *  - bilinear sampling with exact FP32 weights (the reference uses the
+ *    texture unit's 1.8 fixed-point weights, which no CPU can reproduce);
+ *  - sin/cos/atan2/log/acos from the polynomial routines below (Cody-Waite
+ *    reduction + Taylor series), not from libm, so CPU and GPU agree;
+ *  - double precision exactly where the reference's C++ promotes to double
+ *    (comparisons and sums with M_PI, M_PI_2, 10e-7, 2.828, 0.2126 ...).
+ * An FP64 energy (pto_energy_f64) serves as the accuracy reference.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/painttween.h"
+
+#define ALPHA_THRESHOLD 0.99f /* types.h:39 */
+#define EPSILON_F 0.000001f   /* types.h:38 */
+#define BIG_RESIDUAL ((float)10e30)
+
+/* float -> int conversion with CUDA's cvt.rzi.s32.f32 semantics: truncation,
+ * saturation, NaN -> 0 (plain C conversion is undefined there) */
+static inline int f2i(float v) {
+    if (v != v) return 0;
+    if (v >= 2147483647.0f) return 2147483647;
+    if (v <= -2147483648.0f) return (int)(-2147483647 - 1);
+    return (int)v;
+}
+
+typedef struct { float x, y, z, w; } f4;
+typedef struct { float x, y; } f2;
+
+typedef struct {
+    int W, H;            /* level-0 image size (full-res buffers) */
+    int SW, SH, NS;      /* level-0 style size, number of styles */
+    pt_params p;
+    float gauss[64];     /* unnormalised Gaussian, convolution.cu:37-60 */
+    int cur;             /* gCurrentBuffer */
+    /* image-side layered arrays: 2 layers, full resolution, zero outside the
+     * uploaded level rectangle (texSynth_kernel.cu:2120-2126) */
+    f4* img_base[2];
+    float* img_dt[2];
+    f2* vel_f[2];
+    f2* vel_b[2];
+    /* non-layered level-size arrays (re-initialised per upload) */
+    float* img_orient; int io_w, io_h;
+    f2* img_scale; int is_w, is_h;
+    int32_t* img_ids; int ii_w, ii_h;
+    f4* rnd; int rn_w, rn_h;
+    /* exemplar level arrays: ns layers of ew x eh */
+    int ew, eh, ens;
+    f4* ex_base; f4* ex_out; float* ex_orient; float* ex_dt; int32_t* ex_ids;
+    /* working buffers, full resolution */
+    pt_patchxf* off_base; pt_patchxf* off_work;
+    float* res_base; float* res_work;
+    f4* canvas;
+    float* hist_base; float* hist_work; /* SW x (SH*NS) */
+    pt_patchxf* adv_off[2]; f4* adv_base[2]; f4* adv_out[2];
+    float* adv_res[2]; int32_t* adv_ts[2]; /* [0] = F, [1] = B */
+    int threads;
+} pto;
+
+/* ------------------------------------------------------------------------ */
+/* polynomial elementary functions (shared contract with the CUDA side)     */
+/* ------------------------------------------------------------------------ */
+
+/* sin/cos: k = rint(t*2/pi), r = t - k*pi/2 (two-term Cody-Waite with fma),
+ * Taylor series to r^9 (sin) and r^10 (cos) on |r| <= pi/4. */
+static void pt_sincosf(float t, float* s, float* c) {
+    const float two_over_pi = 0x1.45f306p-1f;
+    const float pio2_hi = 0x1.921fb6p+0f;
+    const float pio2_lo = -0x1.777a5cp-25f;
+    float k = rintf(t * two_over_pi);
+    float r = fmaf(-k, pio2_hi, t);
+    r = fmaf(-k, pio2_lo, r);
+    float r2 = r * r;
+    float ps = fmaf(r2, (float)(1.0 / 362880.0), (float)(-1.0 / 5040.0));
+    ps = fmaf(r2, ps, (float)(1.0 / 120.0));
+    ps = fmaf(r2, ps, (float)(-1.0 / 6.0));
+    ps = ps * r2;
+    float sr = fmaf(r, ps, r);
+    float pc = fmaf(r2, (float)(-1.0 / 3628800.0), (float)(1.0 / 40320.0));
+    pc = fmaf(r2, pc, (float)(-1.0 / 720.0));
+    pc = fmaf(r2, pc, (float)(1.0 / 24.0));
+    pc = fmaf(r2, pc, -0.5f);
+    float cr = fmaf(r2, pc, 1.0f);
+    int q = f2i(k) & 3;
+    switch (q) {
+        case 0: *s = sr; *c = cr; break;
+        case 1: *s = cr; *c = -sr; break;
+        case 2: *s = -sr; *c = -cr; break;
+        default: *s = -cr; *c = sr; break;
+    }
+}
+
+/* atan on [0,1]: for u > tan(pi/8) use atan(u) = pi/4 + atan((u-1)/(u+1));
+ * Taylor series to v^19 on |v| <= tan(pi/8). */
+static float pt_atan01f(float u) {
+    float off = 0.0f;
+    float v = u;
+    if (u > 0x1.a8279ap-2f) { /* 0.41421356 */
+        v = (u - 1.0f) / (u + 1.0f);
+        off = 0x1.921fb6p-1f; /* pi/4 */
+    }
+    float v2 = v * v;
+    float p = (float)(-1.0 / 19.0);
+    p = fmaf(v2, p, (float)(1.0 / 17.0));
+    p = fmaf(v2, p, (float)(-1.0 / 15.0));
+    p = fmaf(v2, p, (float)(1.0 / 13.0));
+    p = fmaf(v2, p, (float)(-1.0 / 11.0));
+    p = fmaf(v2, p, (float)(1.0 / 9.0));
+    p = fmaf(v2, p, (float)(-1.0 / 7.0));
+    p = fmaf(v2, p, (float)(1.0 / 5.0));
+    p = fmaf(v2, p, (float)(-1.0 / 3.0));
+    p = p * v2;
+    return off + fmaf(v, p, v);
+}
+
+static float pt_atan2f(float y, float x) {
+    const float pi = 0x1.921fb6p+1f;
+    const float pio2 = 0x1.921fb6p+0f;
+    float ax = fabsf(x), ay = fabsf(y);
+    if (ax == 0.0f && ay == 0.0f) {
+        float r = signbit(x) ? pi : 0.0f;
+        return signbit(y) ? -r : r;
+    }
+    float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+    float a = pt_atan01f(mn / mx);
+    if (ay > ax) a = pio2 - a;
+    if (signbit(x)) a = pi - a;
+    return signbit(y) ? -a : a;
+}
+
+/* natural log: x = m * 2^e with m in [sqrt(1/2), sqrt(2)),
+ * log(m) = 2 atanh(s), s = (m-1)/(m+1), series to s^11. */
+static float pt_logf(float x) {
+    if (!(x > 0.0f)) return (x == 0.0f) ? -INFINITY : NAN;
+    if (isinf(x)) return x;
+    int e;
+    float m = frexpf(x, &e); /* m in [0.5, 1) */
+    if (m < 0x1.6a09e6p-1f) { m = m * 2.0f; e -= 1; }
+    float s = (m - 1.0f) / (m + 1.0f);
+    float s2 = s * s;
+    float p = (float)(1.0 / 11.0);
+    p = fmaf(s2, p, (float)(1.0 / 9.0));
+    p = fmaf(s2, p, (float)(1.0 / 7.0));
+    p = fmaf(s2, p, (float)(1.0 / 5.0));
+    p = fmaf(s2, p, (float)(1.0 / 3.0));
+    p = p * s2;
+    float lm = 2.0f * fmaf(s, p, s);
+    float fe = (float)e;
+    return fmaf(fe, 0x1.62e430p-1f, fmaf(fe, -0x1.05c610p-29f, lm));
+}
+
+/* asin on [0, 1/2] by its Taylor series (12 terms). */
+static float pt_asin_small(float x) {
+    static const double c[12] = {
+        1.0 / 6.0, 3.0 / 40.0, 15.0 / 336.0, 105.0 / 3456.0, 945.0 / 42240.0,
+        10395.0 / 599040.0, 135135.0 / 9676800.0, 2027025.0 / 175472640.0,
+        34459425.0 / 3530096640.0, 654729075.0 / 78033715200.0,
+        13749310575.0 / 1880240947200.0, 316234143225.0 / 49049763430400.0};
+    float z = x * x;
+    float p = (float)c[11];
+    for (int i = 10; i >= 0; --i) p = fmaf(z, p, (float)c[i]);
+    p = p * z;
+    return fmaf(x, p, x);
+}
+
+static float pt_acosf(float x) {
+    const float pi = 0x1.921fb6p+1f;
+    const float pio2 = 0x1.921fb6p+0f;
+    if (!(fabsf(x) <= 1.0f)) return NAN;
+    if (fabsf(x) <= 0.5f) return pio2 - pt_asin_small(x);
+    float t = sqrtf((1.0f - fabsf(x)) * 0.5f);
+    float a = 2.0f * pt_asin_small(t);
+    return (x > 0.0f) ? a : pi - a;
+}
+
+/* IEEE binary16 round trip (round to nearest even), the EXR half channel. */
+static float pt_half_roundtrip(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    uint32_t sign = u & 0x80000000u;
+    uint32_t a = u & 0x7fffffffu;
+    uint16_t h;
+    if (a >= 0x7f800000u) {
+        h = (uint16_t)((a > 0x7f800000u) ? 0x7e00 : 0x7c00);
+    } else if (a >= 0x477ff000u) { /* >= 65520 rounds to inf */
+        h = 0x7c00;
+    } else if (a < 0x38800000u) { /* subnormal or zero half */
+        float af;
+        memcpy(&af, &a, 4);
+        float scaled = af * 16777216.0f; /* 2^24: half subnormal unit */
+        h = (uint16_t)rintf(scaled);
+    } else {
+        uint32_t mant = a & 0x007fffffu;
+        int32_t exp = (int32_t)(a >> 23) - 127 + 15;
+        uint32_t hm = mant >> 13;
+        uint32_t rest = mant & 0x1fffu;
+        uint32_t hv = ((uint32_t)exp << 10) | hm;
+        if (rest > 0x1000u || (rest == 0x1000u && (hv & 1u))) hv += 1;
+        h = (uint16_t)hv;
+    }
+    /* back to float */
+    uint32_t he = (h >> 10) & 0x1f, hmant = h & 0x3ff;
+    float out;
+    if (he == 0) {
+        out = (float)hmant / 16777216.0f;
+    } else if (he == 31) {
+        out = hmant ? NAN : INFINITY;
+    } else {
+        uint32_t bits = ((he - 15 + 127) << 23) | (hmant << 13);
+        memcpy(&out, &bits, 4);
+    }
+    return sign ? -out : out;
+}
+
+/* ------------------------------------------------------------------------ */
+/* fetches                                                                  */
+/* ------------------------------------------------------------------------ */
+
+static inline int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+static inline int lvl_w(const pto* o, int level) { return o->W >> level; }
+static inline int lvl_h(const pto* o, int level) { return o->H >> level; }
+static inline int in_rect(const pto* o, int x, int y, int level, int border) {
+    /* CudaImageBufferDevice::inBounds, cudaImageBuffer.h:117-120 */
+    return x >= border && y >= border && x < lvl_w(o, level) - border &&
+           y < lvl_h(o, level) - border;
+}
+
+/* integer coordinate of a point-filtered fetch at unnormalised u (+0.5 as
+ * PYRAMID_FETCH adds, cudaImagePyramid.h:102,108), clamp addressing */
+static inline int point_index(float u, int n) {
+    float f = floorf(u + 0.5f);
+    f = fminf(fmaxf(f, -1.0f), (float)n);
+    return clampi((int)f, 0, n - 1);
+}
+
+typedef struct { int x0, x1, y0, y1; float w00, w10, w01, w11; } bl_t;
+
+/* bilinear footprint at unnormalised (u,v) with clamp to (n x m) */
+static inline bl_t bl_setup(float u, float v, int n, int m) {
+    bl_t b;
+    float xs = u + 0.5f, ys = v + 0.5f;
+    float xb = xs - 0.5f, yb = ys - 0.5f;
+    float fx = floorf(xb), fy = floorf(yb);
+    float a = xb - fx, c = yb - fy;
+    fx = fminf(fmaxf(fx, -1.0f), (float)n);
+    fy = fminf(fmaxf(fy, -1.0f), (float)m);
+    int ix = (int)fx, iy = (int)fy;
+    b.x0 = clampi(ix, 0, n - 1); b.x1 = clampi(ix + 1, 0, n - 1);
+    b.y0 = clampi(iy, 0, m - 1); b.y1 = clampi(iy + 1, 0, m - 1);
+    float oa = 1.0f - a, oc = 1.0f - c;
+    b.w00 = oa * oc; b.w10 = a * oc; b.w01 = oa * c; b.w11 = a * c;
+    return b;
+}
+static inline float bl1(const bl_t* b, float t00, float t10, float t01, float t11) {
+    float r = t00 * b->w00;
+    r = fmaf(t10, b->w10, r);
+    r = fmaf(t01, b->w01, r);
+    r = fmaf(t11, b->w11, r);
+    return r;
+}
+static inline f4 bl4(const bl_t* b, f4 a, f4 c, f4 d, f4 e) {
+    f4 r;
+    r.x = bl1(b, a.x, c.x, d.x, e.x);
+    r.y = bl1(b, a.y, c.y, d.y, e.y);
+    r.z = bl1(b, a.z, c.z, d.z, e.z);
+    r.w = bl1(b, a.w, c.w, d.w, e.w);
+    return r;
+}
+
+static inline int ex_layer(const pto* o, int layer) { return clampi(layer, 0, o->ens - 1); }
+
+static inline void ex_sample2(const pto* o, float u, float v, int layer, f4* base, f4* out) {
+    bl_t b = bl_setup(u, v, o->ew, o->eh);
+    size_t L = (size_t)ex_layer(o, layer) * o->ew * o->eh;
+    const f4* B = o->ex_base + L;
+    const f4* O = o->ex_out + L;
+    size_t i00 = (size_t)b.y0 * o->ew + b.x0, i10 = (size_t)b.y0 * o->ew + b.x1;
+    size_t i01 = (size_t)b.y1 * o->ew + b.x0, i11 = (size_t)b.y1 * o->ew + b.x1;
+    *base = bl4(&b, B[i00], B[i10], B[i01], B[i11]);
+    *out = bl4(&b, O[i00], O[i10], O[i01], O[i11]);
+}
+static inline f4 ex_sample_out(const pto* o, float u, float v, int layer) {
+    bl_t b = bl_setup(u, v, o->ew, o->eh);
+    const f4* O = o->ex_out + (size_t)ex_layer(o, layer) * o->ew * o->eh;
+    return bl4(&b, O[(size_t)b.y0 * o->ew + b.x0], O[(size_t)b.y0 * o->ew + b.x1],
+               O[(size_t)b.y1 * o->ew + b.x0], O[(size_t)b.y1 * o->ew + b.x1]);
+}
+static inline float ex_sample_dt(const pto* o, float u, float v, int layer) {
+    bl_t b = bl_setup(u, v, o->ew, o->eh);
+    const float* D = o->ex_dt + (size_t)ex_layer(o, layer) * o->ew * o->eh;
+    return bl1(&b, D[(size_t)b.y0 * o->ew + b.x0], D[(size_t)b.y0 * o->ew + b.x1],
+               D[(size_t)b.y1 * o->ew + b.x0], D[(size_t)b.y1 * o->ew + b.x1]);
+}
+static inline float ex_texel_dt(const pto* o, int x, int y, int layer) {
+    x = clampi(x, 0, o->ew - 1); y = clampi(y, 0, o->eh - 1);
+    return o->ex_dt[(size_t)ex_layer(o, layer) * o->ew * o->eh + (size_t)y * o->ew + x];
+}
+static inline float ex_point_orient(const pto* o, float u, float v, int layer) {
+    int x = point_index(u, o->ew), y = point_index(v, o->eh);
+    return o->ex_orient[(size_t)ex_layer(o, layer) * o->ew * o->eh + (size_t)y * o->ew + x];
+}
+static inline int ex_point_id(const pto* o, float u, float v, int layer) {
+    int x = point_index(u, o->ew), y = point_index(v, o->eh);
+    return o->ex_ids[(size_t)ex_layer(o, layer) * o->ew * o->eh + (size_t)y * o->ew + x];
+}
+
+/* image-side layered arrays: full-resolution extent */
+static inline f4 img_texel(const pto* o, int layer, int x, int y) {
+    x = clampi(x, 0, o->W - 1); y = clampi(y, 0, o->H - 1);
+    return o->img_base[layer][(size_t)y * o->W + x];
+}
+static inline float dt_texel(const pto* o, int layer, int x, int y) {
+    x = clampi(x, 0, o->W - 1); y = clampi(y, 0, o->H - 1);
+    return o->img_dt[layer][(size_t)y * o->W + x];
+}
+static inline f2 vel_texel(const f2* v, const pto* o, int x, int y) {
+    x = clampi(x, 0, o->W - 1); y = clampi(y, 0, o->H - 1);
+    return v[(size_t)y * o->W + x];
+}
+static inline f2 vel_bilinear(const f2* v, const pto* o, float u, float w) {
+    bl_t b = bl_setup(u, w, o->W, o->H);
+    f2 a = v[(size_t)b.y0 * o->W + b.x0], c = v[(size_t)b.y0 * o->W + b.x1];
+    f2 d = v[(size_t)b.y1 * o->W + b.x0], e = v[(size_t)b.y1 * o->W + b.x1];
+    f2 r;
+    r.x = bl1(&b, a.x, c.x, d.x, e.x);
+    r.y = bl1(&b, a.y, c.y, d.y, e.y);
+    return r;
+}
+static inline f4 img_bilinear(const pto* o, int layer, float u, float w) {
+    bl_t b = bl_setup(u, w, o->W, o->H);
+    const f4* B = o->img_base[layer];
+    return bl4(&b, B[(size_t)b.y0 * o->W + b.x0], B[(size_t)b.y0 * o->W + b.x1],
+               B[(size_t)b.y1 * o->W + b.x0], B[(size_t)b.y1 * o->W + b.x1]);
+}
+/* non-layered level-size arrays, integer coordinates */
+static inline float orient_texel(const pto* o, int x, int y) {
+    x = clampi(x, 0, o->io_w - 1); y = clampi(y, 0, o->io_h - 1);
+    return o->img_orient[(size_t)y * o->io_w + x];
+}
+static inline f2 scale_texel(const pto* o, int x, int y) {
+    x = clampi(x, 0, o->is_w - 1); y = clampi(y, 0, o->is_h - 1);
+    return o->img_scale[(size_t)y * o->is_w + x];
+}
+static inline int id_texel(const pto* o, int x, int y) {
+    x = clampi(x, 0, o->ii_w - 1); y = clampi(y, 0, o->ii_h - 1);
+    return o->img_ids[(size_t)y * o->ii_w + x];
+}
+static inline f4 rnd_texel(const pto* o, int x, int y) {
+    x = clampi(x, 0, o->rn_w - 1); y = clampi(y, 0, o->rn_h - 1);
+    return o->rnd[(size_t)y * o->rn_w + x];
+}
+
+/* ------------------------------------------------------------------------ */
+/* device-function restatements                                             */
+/* ------------------------------------------------------------------------ */
+
+static inline int image_culled(const pto* o, int x, int y) {
+    /* isImagePixelCulled, texSynth_kernel.cu:176-186 */
+    return dt_texel(o, o->cur, x, y) > (float)o->p.distTransCull;
+}
+
+/* screenToExemplarAngle, texSynth_kernel.cu:425-436 */
+static inline float screen_to_exemplar_angle(const pto* o, int x, int y, float ex, float ey, int layer) {
+    if (o->p.orientationEnabled) {
+        float theta = ex_point_orient(o, ex, ey, layer) - orient_texel(o, x, y);
+        if ((double)theta > M_PI_2) return (float)((double)theta - M_PI);
+        if ((double)theta < -M_PI_2) return (float)(M_PI + (double)theta);
+        return theta;
+    }
+    return 0.0f;
+}
+
+/* screenToExemplarBasis, texSynth_util.h:95-104 */
+static inline void basis(float angle, float su, float sv, f2* b0, f2* b1) {
+    float s, c;
+    pt_sincosf(angle, &s, &c);
+    b1->x = -s * sv;
+    b1->y = c * sv;
+    b0->x = c * su;
+    b0->y = s * su;
+}
+
+/* calculateNewExemplarCoord, texSynth_util.h:106-118: e + (i*b0 + j*b1) */
+static inline void new_coord(float i, float j, float ex, float ey, f2 b0, f2 b1, float* ox, float* oy) {
+    *ox = ex + fmaf(i, b0.x, j * b1.x);
+    *oy = ey + fmaf(i, b0.y, j * b1.y);
+}
+
+/* clampToExemplar(float*), texSynth_util.h:50-57 */
+static inline void clamp_to_exemplar(float* x, float* y, int w, int h) {
+    if (*x < 0) *x = 0;
+    if (*y < 0) *y = 0;
+    if (*x >= w) *x = (float)(w - 1);
+    if (*y >= h) *y = (float)(h - 1);
+}
+
+/* sumSquaredDiff with alpha weight, texSynth_util.h:68-75 */
+static inline float ssd_a(f4 a, f4 b, float alpha) {
+    float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z, dw = a.w - b.w;
+    float s = dx * dx;
+    s = fmaf(dy, dy, s);
+    s = fmaf(dz, dz, s);
+    s = fmaf(alpha * dw, dw, s);
+    return s;
+}
+/* sumSquaredDiff without alpha weight, texSynth_util.h:59-66 */
+static inline float ssd(f4 a, f4 b) {
+    float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z, dw = a.w - b.w;
+    float s = dx * dx;
+    s = fmaf(dy, dy, s);
+    s = fmaf(dz, dz, s);
+    s = fmaf(dw, dw, s);
+    return s;
+}
+static inline f4 sub4(f4 a, f4 b) { f4 r = {a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w}; return r; }
+
+/* per-pixel values that calculateResidual recomputes for every candidate
+ * but that do not depend on the candidate (texSynth_kernel.cu:545-561) */
+typedef struct {
+    int validF, validB;      /* advected centre hysteresis > 0 */
+    pt_patchxf prevF, prevB;
+    f2 fb0, fb1, bb0, bb1;
+    float hyst;              /* hysteresisTerm if validF else 0 */
+    int temporalF, temporalB;
+} pixctx;
+
+/* hysteresisTerm, texSynth_kernel.cu:506-535 */
+static float hysteresis_term(const pto* o, int x, int y, int level) {
+    float maxD = o->p.maxDistortion / ldexpf(1.0f, level);
+    const f2* v = (o->p.direction == PT_FORWARD) ? o->vel_b[o->cur] : o->vel_f[o->cur];
+    f2 d00 = vel_texel(v, o, x, y), d10 = vel_texel(v, o, x + 1, y);
+    f2 d01 = vel_texel(v, o, x, y + 1), d11 = vel_texel(v, o, x + 1, y + 1);
+    float maxX = fmaxf(d00.x, fmaxf(d01.x, fmaxf(d10.x, d11.x)));
+    float maxY = fmaxf(d00.y, fmaxf(d01.y, fmaxf(d10.y, d11.y)));
+    float minX = fminf(d00.x, fminf(d01.x, fminf(d10.x, d11.x)));
+    float minY = fminf(d00.y, fminf(d01.y, fminf(d10.y, d11.y)));
+    if ((maxX - minX) < maxD && (maxY - minY) < maxD) return o->p.hysteresisWeight;
+    return 0.0f;
+}
+
+static void make_pixctx(const pto* o, int x, int y, int level, pixctx* pc) {
+    size_t i = (size_t)y * o->W + x;
+    pc->prevF = o->adv_off[0][i];
+    pc->prevB = o->adv_off[1][i];
+    pc->validF = pc->prevF.hysteresis > 0;
+    pc->validB = pc->prevB.hysteresis > 0;
+    int td = (o->p.timeDerivativeInputWeight > 0.f || o->p.timeDerivativeOutputWeight > 0.f ||
+              o->p.temporalCoherenceWeight > 0.f);
+    pc->temporalF = (o->p.direction == PT_FORWARD || o->p.direction == PT_BIDIRECTIONAL) && pc->validF && td;
+    pc->temporalB = (o->p.direction == PT_BACKWARD || o->p.direction == PT_BIDIRECTIONAL) && pc->validB && td;
+    if (pc->temporalF) {
+        float a = screen_to_exemplar_angle(o, x, y, pc->prevF.x, pc->prevF.y, pc->prevF.layer);
+        basis(a, o->p.residualWindowScaleU * pc->prevF.scaleU, o->p.residualWindowScaleV * pc->prevF.scaleV,
+              &pc->fb0, &pc->fb1);
+    }
+    if (pc->temporalB) {
+        float a = screen_to_exemplar_angle(o, x, y, pc->prevB.x, pc->prevB.y, pc->prevB.layer);
+        basis(a, o->p.residualWindowScaleU * pc->prevB.scaleU, o->p.residualWindowScaleV * pc->prevB.scaleV,
+              &pc->bb0, &pc->bb1);
+    }
+    pc->hyst = pc->validF ? hysteresis_term(o, x, y, level) : 0.0f;
+}
+
+/* timeDerivativeTerms, texSynth_kernel.cu:438-469 */
+static float time_derivative(const pto* o, int dir, const pt_patchxf* prev, f2 pb0, f2 pb1,
+                             f4 base, f4 tb, f4 canvas, f4 to, int x, int y, int i, int j) {
+    size_t k = (size_t)(y + j) * o->W + (x + i);
+    f4 pbase = o->adv_base[dir][k], pout = o->adv_out[dir][k];
+    float px, py;
+    new_coord((float)i, (float)j, prev->x, prev->y, pb0, pb1, &px, &py);
+    f4 peb, peo;
+    ex_sample2(o, px, py, prev->layer, &peb, &peo);
+    float r = ssd(sub4(base, pbase), sub4(tb, peb)) * o->p.timeDerivativeInputWeight;
+    r = fmaf(ssd(sub4(canvas, pout), sub4(to, peo)), o->p.timeDerivativeOutputWeight, r);
+    r = fmaf(ssd(pout, to), o->p.temporalCoherenceWeight, r);
+    return r;
+}
+
+/* coherenceTerm, texSynth_kernel.cu:377-423 */
+static float coherence_term(const pto* o, int x, int y, int i, int j, float tcx, float tcy,
+                            float tx, float ty, int level) {
+    const pt_patchxf* co = &o->off_base[(size_t)(y + j) * o->W + (x + i)];
+    float dx = co->x - tcx, dy = co->y - tcy;
+    float distEx = fmaf(dy, dy, dx * dx) * (float)(1 << level);
+    float distIm = (float)(i * i + j * j) * (float)(1 << level);
+    float R = o->p.coherenceRatioRange;
+    float ratio = fmaxf(1.0f / R, fminf(distEx / distIm, R));
+    float lr = pt_logf(ratio);
+    float lR = pt_logf(R);
+    float Z = lR * lR;
+    float Er = (lr * lr) / Z;
+    float tdx = tx - tcx, tdy = ty - tcy;
+    float lt = sqrtf(fmaf(tdy, tdy, tdx * tdx));
+    float dtx = (lt > 1e-4f) ? tdx * (1.0f / lt) : 1.0f;
+    float dty = (lt > 1e-4f) ? tdy * (1.0f / lt) : 0.0f;
+    float lc = sqrtf(fmaf(dy, dy, dx * dx));
+    float dcx = (lc > 1e-4f) ? dx * (1.0f / lc) : 1.0f;
+    float dcy = (lc > 1e-4f) ? dy * (1.0f / lc) : 0.0f;
+    float d = fmaf(dty, dcy, dtx * dcx);
+    float angle = fmaxf(-1.0f, fminf(pt_acosf(d), 1.0f));
+    double ar = (double)o->p.coherenceAngleRange * M_PI;
+    float Ea = (float)(fmin((double)angle, ar) / ar);
+    return 1.0f - (1.0f - Er) * (1.0f - Ea);
+}
+
+/* calculateResidual, texSynth_kernel.cu:537-659 (FP32 contract) */
+static float energy_f32(const pto* o, int x, int y, int level, const pt_patchxf* t, const pixctx* pc) {
+    const pt_params* P = &o->p;
+    const int r = P->residualWindowSize;
+    float sumW = 0.0f, sum = 0.0f;
+    if (pc->validF) sum = sum - pc->hyst;
+    f2 b0, b1;
+    basis(t->theta, P->residualWindowScaleU * t->scaleU, P->residualWindowScaleV * t->scaleV, &b0, &b1);
+    const int hw = (o->SW) >> level;
+    const int hh = (o->SH * o->NS) >> level;
+    for (int i = -r; i <= r; i++) {
+        for (int j = -r; j <= r; j++) {
+            if (!in_rect(o, x + i, y + j, level, 0)) continue;
+            size_t k = (size_t)(y + j) * o->W + (x + i);
+            f4 base = o->img_base[o->cur][k];
+            f4 canvas = o->canvas[k];
+            float tx, ty;
+            new_coord((float)i, (float)j, t->x, t->y, b0, b1, &tx, &ty);
+            if (tx >= (float)hw) tx -= (float)hw; else if (tx < 0) tx += (float)hw;
+            if (ty >= (float)hh) ty -= (float)hh; else if (ty < 0) ty += (float)hh;
+            f4 tb, to;
+            ex_sample2(o, tx, ty, t->layer, &tb, &to);
+            float res = ssd_a(base, tb, P->alphaWeight) * P->inputAnalogyWeight;
+            if (pc->temporalF && o->adv_off[0][k].hysteresis > 0)
+                res = res + time_derivative(o, 0, &pc->prevF, pc->fb0, pc->fb1, base, tb, canvas, to, x, y, i, j);
+            if (pc->temporalB && o->adv_off[1][k].hysteresis > 0)
+                res = res + time_derivative(o, 1, &pc->prevB, pc->bb0, pc->bb1, base, tb, canvas, to, x, y, i, j);
+            if (i == 0 && j == 0) {
+                if (P->distTransWeight > 0.f) {
+                    float de = ex_sample_dt(o, tx, ty, t->layer) / t->scaleV;
+                    float di = dt_texel(o, o->cur, x, y);
+                    float diff = fminf(fmaxf(fabsf(de - di), 0.0f), 10.0f);
+                    res = res + diff * P->distTransWeight;
+                }
+                { /* histogramTerm, :486-495 */
+                    int L = clampi(t->layer, 0, PT_MAX_STYLES - 1);
+                    float sh = (float)(hh / P->numStyles);
+                    int hx = f2i(tx), hy = f2i(ty + sh * (float)t->layer);
+                    hx = clampi(hx, 0, o->SW - 1);
+                    hy = clampi(hy, 0, o->SH * o->NS - 1);
+                    float h = o->hist_base[(size_t)hy * o->SW + hx];
+                    float thr = P->offsetsHistogramThreshold[L];
+                    res = res + ((h > thr) ? (h - thr) * P->offsetsHistogramSlope[L] : 0.0f);
+                }
+                if (P->styleObjIdWeight > 0.f) {
+                    int imgID = id_texel(o, x, y);
+                    int styleID = ex_point_id(o, tx, ty, t->layer);
+                    res = res + ((imgID != styleID) ? P->styleObjIdWeight : 0.0f);
+                }
+            } else {
+                res = fmaf(ssd_a(canvas, to, P->alphaWeight), P->canvasOutputWeight, res);
+                if (P->coherenceWeight > 0.f) {
+                    float c = coherence_term(o, x, y, i, j, t->x, t->y, tx, ty, level);
+                    res = fmaf(c, P->coherenceWeight, res);
+                }
+            }
+            float w = o->gauss[i + r] * o->gauss[j + r];
+            sum = fmaf(res, w, sum);
+            sumW = sumW + w;
+        }
+    }
+    if (sumW < EPSILON_F) return BIG_RESIDUAL;
+    return sum / sumW;
+}
+
+/* test_offset + isExemplarPixelCulled, texSynth_kernel.cu:200-205,695-721 */
+static float test_offset(const pto* o, int x, int y, const pt_patchxf* t, int level, float image_alpha,
+                         const pixctx* pc) {
+    float dte = ex_texel_dt(o, f2i(t->x), f2i(t->y), t->layer);
+    if (!((double)dte > (double)o->p.distTransCull * 1.25)) {
+        if (!o->p.transparencyOk) {
+            float ea = ex_sample_out(o, t->x, t->y, t->layer).w;
+            if (ea < ALPHA_THRESHOLD && image_alpha > ALPHA_THRESHOLD) return BIG_RESIDUAL;
+        }
+        return energy_f32(o, x, y, level, t, pc);
+    }
+    return BIG_RESIDUAL;
+}
+
+static inline pt_patchxf patch(float x, float y, float th, float h, int layer, float su, float sv) {
+    pt_patchxf p;
+    p.x = x; p.y = y; p.theta = th; p.hysteresis = h; p.layer = layer;
+    p.scaleU = su; p.scaleV = sv; p.lumShiftY = 0.f; p.lumShiftA = 0.f;
+    return p;
+}
+
+/* calculatePropagateOffset, texSynth_kernel.cu:956-982 */
+static pt_patchxf propagate_offset(const pto* o, const pt_patchxf* src, int tx, int ty, int x, int y) {
+    /* pixelWrap with the level-0 size, cudaImageBuffer.h:81-87 */
+    int wx = (int)((float)tx - (float)o->W * floorf((float)tx / (float)o->W));
+    int wy = (int)((float)ty - (float)o->H * floorf((float)ty / (float)o->H));
+    pt_patchxf t = src[(size_t)wy * o->W + wx];
+    f2 sc = scale_texel(o, tx, ty);
+    f2 b0, b1;
+    basis(t.theta, o->p.residualWindowScaleU * sc.x, o->p.residualWindowScaleV * sc.y, &b0, &b1);
+    float ex, ey;
+    new_coord((float)x - (float)tx, (float)y - (float)ty, t.x, t.y, b0, b1, &ex, &ey);
+    clamp_to_exemplar(&ex, &ey, o->ew, o->eh);
+    float ang = screen_to_exemplar_angle(o, x, y, ex, ey, t.layer);
+    f2 s2 = scale_texel(o, x, y);
+    return patch(ex, ey, ang, 0.0f, t.layer, s2.x, s2.y);
+}
+
+/* ------------------------------------------------------------------------ */
+/* kernels                                                                  */
+/* ------------------------------------------------------------------------ */
+
+#define FOR_RECT(o, level)                                     \
+    _Pragma("omp parallel for schedule(dynamic, 4) num_threads(o->threads)") \
+    for (int y = 0; y < lvl_h(o, level); y++)                  \
+        for (int x = 0; x < lvl_w(o, level); x++)
+
+/* propagate_kernel, texSynth_kernel.cu:1112-1219 (advected candidates at
+ * :1184-1216 are rebuilt with hysteresis 0 at :981 and never tested) */
+void pto_propagate(pto* o, int level, int jump) {
+    const pt_patchxf* base = o->off_base;
+    pt_patchxf* work = o->off_work;
+    FOR_RECT(o, level) {
+        size_t k = (size_t)y * o->W + x;
+        if (image_culled(o, x, y)) { work[k] = patch(0, 0, 0, 0, 0, 1.f, 1.f); continue; }
+        float best = o->res_base[k];
+        float ia = o->img_base[o->cur][k].w;
+        pt_patchxf ow = base[k];
+        pixctx pc;
+        make_pixctx(o, x, y, level, &pc);
+        for (int c = 0; c < 4; c++) {
+            int tx = x, ty = y;
+            if (c == 0) tx = x + jump;
+            else if (c == 1) tx = x - jump;
+            else if (c == 2) ty = y + jump;
+            else ty = y - jump;
+            pt_patchxf t = propagate_offset(o, base, tx, ty, x, y);
+            float r = test_offset(o, x, y, &t, level, ia, &pc);
+            if (r < best) { ow = t; best = r; }
+        }
+        work[k] = ow;
+    }
+}
+
+/* scatter_kernel + averageOffset, texSynth_kernel.cu:841-952; the reference's
+ * randFloat() returns unsigned int 0 (texSynth_util.h:155-163), so every
+ * candidate is (best.x + 0.9*dist, best.y). */
+void pto_scatter(pto* o, int level) {
+    const pt_patchxf* base = o->off_base;
+    pt_patchxf* work = o->off_work;
+    FOR_RECT(o, level) {
+        size_t k = (size_t)y * o->W + x;
+        if (image_culled(o, x, y)) continue;
+        pt_patchxf off = base[k];
+        float cached = o->res_base[k];
+        float best = (float)((double)cached + 10e-7);
+        pt_patchxf ow = off;
+        float ia = o->img_base[o->cur][k].w;
+        float dist = (float)(o->ew > o->eh ? o->ew : o->eh);
+        const float closest = 10.f, factor = 0.9f;
+        f2 sc = scale_texel(o, x, y);
+        pixctx pc;
+        make_pixctx(o, x, y, level, &pc);
+        for (int i = 0; i < o->p.scatterSamplesCount && dist * factor >= closest; i++) {
+            float dmin = dist * factor;
+            float ex = ow.x + dmin;
+            float ey = ow.y + 0.0f;
+            clamp_to_exemplar(&ex, &ey, o->ew, o->eh);
+            float ang = screen_to_exemplar_angle(o, x, y, ex, ey, 0);
+            pt_patchxf t = patch(ex, ey, ang, 0.0f, 0, sc.x, sc.y);
+            float r = test_offset(o, x, y, &t, level, ia, &pc);
+            if (r < best) { ow = t; best = r; }
+            dist *= factor;
+        }
+        /* averageOffset(offsets, x, y, level, 0) */
+        pt_patchxf avg = patch(0, 0, 0, 1.f, 0, 1.f, 1.f);
+        int n = 0;
+        for (int i = -1; i <= 1; i++)
+            for (int j = -1; j <= 1; j++) {
+                if (!in_rect(o, x + i, y + j, level, 0) || (i == 0 && j == 0)) continue;
+                const pt_patchxf* nb = &base[(size_t)(y + j) * o->W + (x + i)];
+                if (nb->layer != 0) continue;
+                avg.x = avg.x + nb->x;
+                avg.y = avg.y + nb->y;
+                n++;
+            }
+        avg.x = avg.x / (float)n;
+        avg.y = avg.y / (float)n;
+        avg.theta = screen_to_exemplar_angle(o, x, y, avg.x, avg.y, 0);
+        float r = test_offset(o, x, y, &avg, level, ia, &pc);
+        if (r < best) { ow = avg; best = r; }
+        if (best < cached) work[k] = ow;
+    }
+}
+
+/* updateResidualCache_kernel, texSynth_kernel.cu:661-693 */
+void pto_update_residual(pto* o, int level) {
+    FOR_RECT(o, level) {
+        size_t k = (size_t)y * o->W + x;
+        if (image_culled(o, x, y)) { o->res_base[k] = 0.0f; continue; }
+        pixctx pc;
+        make_pixctx(o, x, y, level, &pc);
+        o->res_base[k] = energy_f32(o, x, y, level, &o->off_base[k], &pc);
+    }
+}
+
+/* offsetsToOutput, texSynth_kernel.cu:263-274 */
+static void offsets_to_output(pto* o, int level) {
+    FOR_RECT(o, level) {
+        size_t k = (size_t)y * o->W + x;
+        const pt_patchxf* p = &o->off_base[k];
+        f4 c = ex_sample_out(o, p->x, p->y, p->layer);
+        c.x = c.x + p->lumShiftY; c.y = c.y + p->lumShiftY; c.z = c.z + p->lumShiftY;
+        c.w = c.w + p->lumShiftA;
+        o->canvas[k] = c;
+    }
+}
+
+/* separable Gaussian, convolution.cu:76-210 (normalised weights, zero
+ * apron); the smoothed histogram is input to histogramTerm. */
+static void conv_pass(pto* o, const float* src, float* dst, int w, int h, int rows, const float* kern, int r) {
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            float s = 0.0f;
+            for (int j = -r; j <= r; j++) {
+                int xx = rows ? x + j : x, yy = rows ? y : y + j;
+                float v = (xx >= 0 && xx < w && yy >= 0 && yy < h) ? src[(size_t)yy * o->SW + xx] : 0.0f;
+                s = fmaf(kern[r - j], v, s);
+            }
+            dst[(size_t)y * o->SW + x] = s;
+        }
+}
+
+/* syncBuffers, texSynth_kernel.cu:1240-1303 (distance-transform, velocity
+ * and ribbon caches are display-only and not kept) */
+void pto_sync(pto* o, int level, int flags) {
+    if (!(flags & PT_DONT_COPY_OFFSETS))
+        memcpy(o->off_base, o->off_work, sizeof(pt_patchxf) * (size_t)o->W * o->H);
+    int hist = 0;
+    for (int i = 0; i < o->p.numStyles && i < PT_MAX_STYLES; i++)
+        hist = hist || (o->p.offsetsHistogramSlope[i] > 0.0f);
+    if (hist) {
+        size_t n = (size_t)o->SW * o->SH * o->NS;
+        memset(o->hist_base, 0, n * sizeof(float));
+        memset(o->hist_work, 0, n * sizeof(float));
+        /* calculateOffsetsHistogram adds nothing (:258 is commented out) */
+        int r = o->p.residualWindowSize;
+        float kern[64];
+        float sigma = (float)r / 3.0f, s2 = sigma * sigma;
+        for (int i = 0; i <= r; i++) {
+            float wgt = expf(-(float)(i * i) / (2.f * s2));
+            wgt = wgt / (sqrtf(2.f * (float)M_PI) * sigma);
+            kern[r + i] = wgt; kern[r - i] = wgt;
+        }
+        int w = o->SW >> level, h = (o->SH * o->NS) >> level;
+        /* convolutionRowsGPU(dst = working, src = base), then
+         * convolutionColumnsGPU(dst = base, src = working) */
+        conv_pass(o, o->hist_base, o->hist_work, w, h, 1, kern, r);
+        conv_pass(o, o->hist_work, o->hist_base, w, h, 0, kern, r);
+    }
+    offsets_to_output(o, level);
+    if (!(flags & PT_DONT_UPDATE_RESIDUAL)) pto_update_residual(o, level);
+}
+
+/* copyRandomKernel + randomizeOffsets, texSynth_kernel.cu:2044-2059,2100-2109 */
+void pto_randomize(pto* o, int level) {
+    FOR_RECT(o, level) {
+        f4 r = rnd_texel(o, x, y);
+        o->off_work[(size_t)y * o->W + x] = patch(r.x, r.y, r.z, 0.f, f2i(r.w), 1.f, 1.f);
+    }
+    pto_sync(o, level, 0);
+}
+
+/* offsetUpsampleNearest, texSynth_kernel.cu:1403-1417 */
+static f2 upsample_nearest(const pto* o, const pt_patchxf* c, float dx, float dy) {
+    f2 b0, b1;
+    basis(c->theta, 1.0f, 1.0f, &b0, &b1);
+    float ix, iy;
+    new_coord(dx, dy, c->x, c->y, b0, b1, &ix, &iy);
+    clamp_to_exemplar(&ix, &iy, o->ew, o->eh);
+    f2 r = {fmaf(ix, 2.0f, 0.5f), fmaf(iy, 2.0f, 0.5f)};
+    return r;
+}
+
+/* upsampleBilinearKernel + TexSynth::upsample, texSynth_kernel.cu:1453-1532.
+ * Border pixels keep the working buffer's content; the residual working
+ * buffer's border is modelled as equal to the base residual. */
+void pto_upsample(pto* o, int level) {
+    const pt_patchxf* base = o->off_base;
+    pt_patchxf* work = o->off_work;
+    for (size_t k = 0; k < (size_t)o->W * o->H; k++) o->res_work[k] = o->res_base[k];
+    _Pragma("omp parallel for schedule(dynamic, 4) num_threads(o->threads)")
+    for (int y = 1; y < lvl_h(o, level) - 1; y++)
+        for (int x = 1; x < lvl_w(o, level) - 1; x++) {
+            float cx = (float)((double)x - 0.5) / 2.0f;
+            float cy = (float)((double)y - 0.5) / 2.0f;
+            int lcx = (int)floorf(cx), lcy = (int)floorf(cy);
+            const pt_patchxf* o00 = &base[(size_t)lcy * o->W + lcx];
+            const pt_patchxf* o10 = &base[(size_t)lcy * o->W + lcx + 1];
+            const pt_patchxf* o01 = &base[(size_t)(lcy + 1) * o->W + lcx];
+            const pt_patchxf* o11 = &base[(size_t)(lcy + 1) * o->W + lcx + 1];
+            float a = cx - (float)lcx, b = cy - (float)lcy;
+            float w00 = (1 - a) * (1 - b), w10 = a * (1 - b), w01 = (1 - a) * b, w11 = a * b;
+            float ix = w00 * o00->x; ix = fmaf(w10, o10->x, ix); ix = fmaf(w01, o01->x, ix); ix = fmaf(w11, o11->x, ix);
+            float iy = w00 * o00->y; iy = fmaf(w10, o10->y, iy); iy = fmaf(w01, o01->y, iy); iy = fmaf(w11, o11->y, iy);
+            f2 up = {fmaf(ix, 2.0f, 0.5f), fmaf(iy, 2.0f, 0.5f)};
+            const pt_patchxf* cs[4] = {o00, o10, o01, o11};
+            int far = 0;
+            for (int q = 0; q < 4; q++) {
+                float dx = ix - cs[q]->x, dy = iy - cs[q]->y;
+                if (fmaf(dy, dy, dx * dx) > 16.0f) far = 1;
+            }
+            if (far) {
+                int rcx = (int)roundf(cx), rcy = (int)roundf(cy);
+                const pt_patchxf* c = &base[(size_t)rcy * o->W + rcx];
+                up = upsample_nearest(o, c, cx - (float)rcx, cy - (float)rcy);
+            }
+            int layer = o00->layer;
+            float rw = o->res_base[(size_t)lcy * o->W + lcx];
+            float ang = screen_to_exemplar_angle(o, x, y, up.x, up.y, layer);
+            f2 sc = scale_texel(o, x, y);
+            work[(size_t)y * o->W + x] = patch(up.x, up.y, ang, 0.0f, layer, sc.x, sc.y);
+            o->res_work[(size_t)y * o->W + x] = rw;
+        }
+    memcpy(o->off_base, o->off_work, sizeof(pt_patchxf) * (size_t)o->W * o->H);
+    memcpy(o->res_base, o->res_work, sizeof(float) * (size_t)o->W * o->H);
+}
+
+/* calculateTranslatedPosition + advectKernel + TexSynth::advectOffsets,
+ * texSynth_kernel.cu:1540-1726 (keyframe ribbons not in scope) */
+void pto_advect(pto* o, int level, int time_step, int forwards, int flags) {
+    int d = forwards ? 0 : 1;
+    int prev = (o->cur + 1) % 2;
+    pt_patchxf* dst = o->adv_off[d];
+    FOR_RECT(o, level) {
+        size_t k = (size_t)y * o->W + x;
+        if (image_culled(o, x, y)) {
+            f4 z = {0, 0, 0, 0};
+            o->adv_base[d][k] = z; o->adv_out[d][k] = z;
+            dst[k] = patch(0, 0, 0, 0, 0, 1.f, 1.f);
+            continue;
+        }
+        f4 rnd = rnd_texel(o, x, y);
+        f4 fr = {rnd.x - floorf(rnd.x), rnd.y - floorf(rnd.y), rnd.z - floorf(rnd.z), rnd.w - floorf(rnd.w)};
+        pt_patchxf out = patch(0, 0, 0, 0, 0, 1.f, 1.f);
+        int valid = 0;
+        float tx = 0, ty = 0;
+        if (!(flags & PT_ADVECT_DO_NOT_CHECK_PREVIOUS)) {
+            f2 fw, bk;
+            if (forwards) {
+                bk = vel_texel(o->vel_b[o->cur], o, x, y);
+                tx = (float)x + bk.x; ty = (float)y + bk.y;
+                fw = vel_bilinear(o->vel_f[prev], o, tx, ty);
+            } else {
+                fw = vel_texel(o->vel_f[o->cur], o, x, y);
+                tx = (float)x + fw.x; ty = (float)y + fw.y;
+                bk = vel_bilinear(o->vel_b[prev], o, tx, ty);
+            }
+            fw.x = -fw.x; fw.y = -fw.y;
+            float ddx = fw.x - bk.x, ddy = fw.y - bk.y;
+            float dist = sqrtf(fmaf(ddy, ddy, ddx * ddx));
+            float cxf = fminf(fmaxf(ceilf(tx), -2.f), 1e9f), cyf = fminf(fmaxf(ceilf(ty), -2.f), 1e9f);
+            float fxf = fminf(fmaxf(floorf(tx), -2.f), 1e9f), fyf = fminf(fmaxf(floorf(ty), -2.f), 1e9f);
+            valid = in_rect(o, f2i(cxf), f2i(cyf), level, 0) && in_rect(o, f2i(fxf), f2i(fyf), level, 0) &&
+                    (dist < (float)(1.414 * 2));
+            if (valid) {
+                /* isImagePixelCulledPreviousFrame(tx, ty, level, 8.0), :188-198 */
+                float pd = dt_texel(o, prev, f2i(tx), f2i(ty));
+                if (pd > ((float)o->p.distTransCull - 8.0f)) valid = 0;
+            }
+        }
+        if (valid) {
+            int rtx = (int)roundf(tx), rty = (int)roundf(ty);
+            const pt_patchxf* nx = &o->off_base[(size_t)rty * o->W + rtx];
+            f2 b0, b1;
+            basis(nx->theta, 1.0f, 1.0f, &b0, &b1);
+            float ix, iy;
+            new_coord(tx - (float)rtx, ty - (float)rty, nx->x, nx->y, b0, b1, &ix, &iy);
+            clamp_to_exemplar(&ix, &iy, o->ew, o->eh);
+            f4 color = o->img_base[o->cur][k];
+            f4 pcol = img_bilinear(o, prev, tx, ty);
+            out.x = ix; out.y = iy; out.theta = nx->theta;
+            if (o->p.lumShiftEnable) {
+                float dr = color.x - pcol.x, dg = color.y - pcol.y, db = color.z - pcol.z;
+                float ly = (float)(0.2126 * dr + 0.7152 * dg + 0.0722 * db);
+                out.lumShiftY = nx->lumShiftY + ly;
+            } else {
+                out.lumShiftY = 0.f;
+            }
+            out.lumShiftA = 0.f;
+            out.layer = nx->layer;
+            out.hysteresis = 1;
+            o->adv_base[d][k] = pcol;
+            o->adv_out[d][k] = ex_sample_out(o, out.x, out.y, out.layer);
+            o->adv_ts[d][k] = time_step;
+        }
+        if (out.hysteresis == 0) {
+            out = patch(rnd.x, rnd.y, rnd.z, 0.0f, f2i(rnd.w), 1.f, 1.f);
+            f4 z = {0, 0, 0, 0};
+            o->adv_base[d][k] = z; o->adv_out[d][k] = z;
+            o->adv_ts[d][k] = -1;
+        }
+        float J = o->p.advectionJitter;
+        out.x = fmaf(fr.x, J, out.x * (1 - J));
+        out.y = fmaf(fr.y, J, out.y * (1 - J));
+        out.theta = screen_to_exemplar_angle(o, x, y, out.x, out.y, out.layer);
+        dst[k] = out;
+    }
+    memcpy(o->off_base, dst, sizeof(pt_patchxf) * (size_t)o->W * o->H);
+    pto_sync(o, level, PT_DONT_COPY_OFFSETS | PT_DONT_UPDATE_RESIDUAL);
+    if (flags & PT_ADVECT_UPDATE_RESIDUAL) pto_update_residual(o, level);
+    memcpy(o->adv_res[d], o->res_base, sizeof(float) * (size_t)o->W * o->H);
+}
+
+/* mergeRandomlyKernel + TexSynth::mergeRandomly, texSynth_kernel.cu:1891-1936,
+ * 2003-2024.  Frame-to-key ribbons are never uploaded outside keyframe mode,
+ * so both ribbon fetches read zero and both count as valid. */
+void pto_merge_randomly(pto* o, int level, int forwards, float weight, int force) {
+    int d = forwards ? 0 : 1;
+    FOR_RECT(o, level) {
+        size_t k = (size_t)y * o->W + x;
+        pt_patchxf a = o->adv_off[d][k], u = o->off_base[k];
+        f4 rnd = rnd_texel(o, x, y);
+        float r = forwards ? rnd.x - floorf(rnd.x) : rnd.y - floorf(rnd.y);
+        int av = a.hysteresis > 0;
+        o->off_work[k] = ((av || force) && r < weight) ? a : u;
+    }
+    pto_sync(o, level, 0);
+}
+
+/* mergeUsingResidualKernel, texSynth_kernel.cu:1856-1889,1978-2001 */
+void pto_merge_using_residual(pto* o, int level, int forwards) {
+    int d = forwards ? 0 : 1;
+    FOR_RECT(o, level) {
+        size_t k = (size_t)y * o->W + x;
+        pt_patchxf r;
+        if (o->adv_res[d][k] < o->res_base[k]) { r = o->adv_off[d][k]; r.hysteresis = 1.f; }
+        else { r = o->off_base[k]; r.hysteresis = 0.f; }
+        o->off_work[k] = r;
+    }
+    pto_sync(o, level, 0);
+}
+
+/* ------------------------------------------------------------------------ */
+/* FP64 energy (accuracy reference; exact bilinear, libm sin/cos)           */
+/* ------------------------------------------------------------------------ */
+
+typedef struct { double x, y, z, w; } d4;
+
+static d4 ex_sample_d(const pto* o, const f4* arr, double u, double v, int layer) {
+    double fx = floor(u), fy = floor(v);
+    double a = u - fx, c = v - fy;
+    fx = fmin(fmax(fx, -1.0), (double)o->ew);
+    fy = fmin(fmax(fy, -1.0), (double)o->eh);
+    int ix = (int)fx, iy = (int)fy;
+    int x0 = clampi(ix, 0, o->ew - 1), x1 = clampi(ix + 1, 0, o->ew - 1);
+    int y0 = clampi(iy, 0, o->eh - 1), y1 = clampi(iy + 1, 0, o->eh - 1);
+    const f4* A = arr + (size_t)ex_layer(o, layer) * o->ew * o->eh;
+    f4 t00 = A[(size_t)y0 * o->ew + x0], t10 = A[(size_t)y0 * o->ew + x1];
+    f4 t01 = A[(size_t)y1 * o->ew + x0], t11 = A[(size_t)y1 * o->ew + x1];
+    double w00 = (1 - a) * (1 - c), w10 = a * (1 - c), w01 = (1 - a) * c, w11 = a * c;
+    d4 r;
+    r.x = t00.x * w00 + t10.x * w10 + t01.x * w01 + t11.x * w11;
+    r.y = t00.y * w00 + t10.y * w10 + t01.y * w01 + t11.y * w11;
+    r.z = t00.z * w00 + t10.z * w10 + t01.z * w01 + t11.z * w11;
+    r.w = t00.w * w00 + t10.w * w10 + t01.w * w01 + t11.w * w11;
+    return r;
+}
+
+/* calculateResidual in double precision for the non-temporal terms
+ * (inputAnalogy, canvasOutput, DT, histogram (zero), objectID).  The sample
+ * positions are the reference's float positions (basis, offset + i*b0 + j*b1
+ * and the one-period wrap are float arithmetic in the reference); bilinear
+ * filtering, the SSDs, the Gaussian weights and the sums are in double. */
+static double energy_f64(const pto* o, int x, int y, int level, const pt_patchxf* t) {
+    const pt_params* P = &o->p;
+    const int r = P->residualWindowSize;
+    double sumW = 0, sum = 0;
+    f2 fb0, fb1;
+    basis(t->theta, P->residualWindowScaleU * t->scaleU, P->residualWindowScaleV * t->scaleV, &fb0, &fb1);
+    const int hw = (o->SW) >> level, hh = (o->SH * o->NS) >> level;
+    double sigma = r / 3.0;
+    for (int i = -r; i <= r; i++)
+        for (int j = -r; j <= r; j++) {
+            if (!in_rect(o, x + i, y + j, level, 0)) continue;
+            size_t k = (size_t)(y + j) * o->W + (x + i);
+            f4 base = o->img_base[o->cur][k];
+            f4 canvas = o->canvas[k];
+            float ftx, fty;
+            new_coord((float)i, (float)j, t->x, t->y, fb0, fb1, &ftx, &fty);
+            if (ftx >= (float)hw) ftx -= (float)hw; else if (ftx < 0) ftx += (float)hw;
+            if (fty >= (float)hh) fty -= (float)hh; else if (fty < 0) fty += (float)hh;
+            double tx = ftx, ty = fty;
+            d4 tb = ex_sample_d(o, o->ex_base, tx, ty, t->layer);
+            d4 to = ex_sample_d(o, o->ex_out, tx, ty, t->layer);
+            double dx = base.x - tb.x, dy = base.y - tb.y, dz = base.z - tb.z, dw = base.w - tb.w;
+            double res = (dx * dx + dy * dy + dz * dz + (double)P->alphaWeight * dw * dw) * P->inputAnalogyWeight;
+            if (i == 0 && j == 0) {
+                if (P->distTransWeight > 0.f) {
+                    /* bilinear DT in double */
+                    double fx = floor(tx), fy = floor(ty), a = tx - fx, cc = ty - fy;
+                    int ix = (int)fmin(fmax(fx, -1.0), (double)o->ew), iy = (int)fmin(fmax(fy, -1.0), (double)o->eh);
+                    const float* D = o->ex_dt + (size_t)ex_layer(o, t->layer) * o->ew * o->eh;
+                    int x0 = clampi(ix, 0, o->ew - 1), x1 = clampi(ix + 1, 0, o->ew - 1);
+                    int y0 = clampi(iy, 0, o->eh - 1), y1 = clampi(iy + 1, 0, o->eh - 1);
+                    double de = D[(size_t)y0 * o->ew + x0] * (1 - a) * (1 - cc) + D[(size_t)y0 * o->ew + x1] * a * (1 - cc) +
+                                D[(size_t)y1 * o->ew + x0] * (1 - a) * cc + D[(size_t)y1 * o->ew + x1] * a * cc;
+                    de /= t->scaleV;
+                    double di = dt_texel(o, o->cur, x, y);
+                    double diff = fmin(fmax(fabs(de - di), 0.0), 10.0);
+                    res += diff * P->distTransWeight;
+                }
+                {
+                    int L = clampi(t->layer, 0, PT_MAX_STYLES - 1);
+                    if (0.0 > P->offsetsHistogramThreshold[L])
+                        res += (0.0 - P->offsetsHistogramThreshold[L]) * P->offsetsHistogramSlope[L];
+                }
+                if (P->styleObjIdWeight > 0.f) {
+                    int imgID = id_texel(o, x, y);
+                    int styleID = ex_point_id(o, (float)tx, (float)ty, t->layer);
+                    if (imgID != styleID) res += P->styleObjIdWeight;
+                }
+            } else {
+                double ex = canvas.x - to.x, ey = canvas.y - to.y, ez = canvas.z - to.z, ea = canvas.w - to.w;
+                res += (ex * ex + ey * ey + ez * ez + (double)P->alphaWeight * ea * ea) * P->canvasOutputWeight;
+            }
+            double wi = exp(-(double)(i * i) / (2 * sigma * sigma)), wj = exp(-(double)(j * j) / (2 * sigma * sigma));
+            double w = wi * wj;
+            sum += res * w;
+            sumW += w;
+        }
+    if (sumW < 1e-6) return 1e31;
+    return sum / sumW;
+}
+
+/* ------------------------------------------------------------------------ */
+/* public C interface of the oracle (ctypes)                                */
+/* ------------------------------------------------------------------------ */
+
+static void* zalloc(size_t n) { return calloc(1, n ? n : 1); }
+
+pto* pto_create(int W, int H, int SW, int SH, int NS) {
+    pto* o = (pto*)zalloc(sizeof(pto));
+    o->W = W; o->H = H; o->SW = SW; o->SH = SH; o->NS = NS;
+    o->threads = 1;
+    size_t n = (size_t)W * H;
+    for (int l = 0; l < 2; l++) {
+        o->img_base[l] = (f4*)zalloc(n * sizeof(f4));
+        o->img_dt[l] = (float*)zalloc(n * sizeof(float));
+        o->vel_f[l] = (f2*)zalloc(n * sizeof(f2));
+        o->vel_b[l] = (f2*)zalloc(n * sizeof(f2));
+        o->adv_off[l] = (pt_patchxf*)zalloc(n * sizeof(pt_patchxf));
+        o->adv_base[l] = (f4*)zalloc(n * sizeof(f4));
+        o->adv_out[l] = (f4*)zalloc(n * sizeof(f4));
+        o->adv_res[l] = (float*)zalloc(n * sizeof(float));
+        o->adv_ts[l] = (int32_t*)zalloc(n * sizeof(int32_t));
+    }
+    o->off_base = (pt_patchxf*)zalloc(n * sizeof(pt_patchxf));
+    o->off_work = (pt_patchxf*)zalloc(n * sizeof(pt_patchxf));
+    o->res_base = (float*)zalloc(n * sizeof(float));
+    o->res_work = (float*)zalloc(n * sizeof(float));
+    o->canvas = (f4*)zalloc(n * sizeof(f4));
+    size_t hn = (size_t)SW * SH * NS;
+    o->hist_base = (float*)zalloc(hn * sizeof(float));
+    o->hist_work = (float*)zalloc(hn * sizeof(float));
+    return o;
+}
+
+void pto_destroy(pto* o) {
+    if (!o) return;
+    for (int l = 0; l < 2; l++) {
+        free(o->img_base[l]); free(o->img_dt[l]); free(o->vel_f[l]); free(o->vel_b[l]);
+        free(o->adv_off[l]); free(o->adv_base[l]); free(o->adv_out[l]); free(o->adv_res[l]); free(o->adv_ts[l]);
+    }
+    free(o->off_base); free(o->off_work); free(o->res_base); free(o->res_work); free(o->canvas);
+    free(o->hist_base); free(o->hist_work);
+    free(o->img_orient); free(o->img_scale); free(o->img_ids); free(o->rnd);
+    free(o->ex_base); free(o->ex_out); free(o->ex_orient); free(o->ex_dt); free(o->ex_ids);
+    free(o);
+}
+
+void pto_set_threads(pto* o, int n) { o->threads = n < 1 ? 1 : n; }
+
+/* TexSynth::setup: unnormalised Gaussian of radius r, convolution.cu:37-60 */
+void pto_set_params(pto* o, const pt_params* p) {
+    o->p = *p;
+    int r = p->residualWindowSize;
+    float sigma = (float)r / 3.0f, s2 = sigma * sigma;
+    for (int i = 0; i <= r && i < 32; i++) {
+        float w = expf(-(float)(i * i) / (2.f * s2));
+        o->gauss[r + i] = w; o->gauss[r - i] = w;
+    }
+}
+
+void pto_init_exemplars(pto* o, int ew, int eh, int ns) {
+    free(o->ex_base); free(o->ex_out); free(o->ex_orient); free(o->ex_dt); free(o->ex_ids);
+    size_t n = (size_t)ew * eh * ns;
+    o->ew = ew; o->eh = eh; o->ens = ns;
+    o->ex_base = (f4*)zalloc(n * sizeof(f4));
+    o->ex_out = (f4*)zalloc(n * sizeof(f4));
+    o->ex_orient = (float*)zalloc(n * sizeof(float));
+    o->ex_dt = (float*)zalloc(n * sizeof(float));
+    o->ex_ids = (int32_t*)zalloc(n * sizeof(int32_t));
+}
+
+void pto_upload_exemplar(pto* o, int style, const float* base, const float* out, const float* orient,
+                         const float* dt, const int32_t* ids) {
+    size_t n = (size_t)o->ew * o->eh, off = n * style;
+    memcpy(o->ex_base + off, base, n * sizeof(f4));
+    memcpy(o->ex_out + off, out, n * sizeof(f4));
+    memcpy(o->ex_orient + off, orient, n * sizeof(float));
+    memcpy(o->ex_dt + off, dt, n * sizeof(float));
+    memcpy(o->ex_ids + off, ids, n * sizeof(int32_t));
+}
+
+/* layered uploads into the current layer's top-left rectangle (or the
+ * previous layer for VEL_*_PREVIOUS), texSynth_kernel.cu:2143-2253 */
+void pto_upload_layered(pto* o, int which, const float* data, int w, int h) {
+    int prev = (o->cur + 1) % 2;
+    for (int y = 0; y < h; y++) {
+        size_t dst = (size_t)y * o->W;
+        switch (which) {
+            case PT_LAYER_INPUT_COLOR: memcpy(o->img_base[o->cur] + dst, data + (size_t)y * w * 4, w * sizeof(f4)); break;
+            case PT_LAYER_INPUT_DIST_TRANS: memcpy(o->img_dt[o->cur] + dst, data + (size_t)y * w, w * sizeof(float)); break;
+            case PT_LAYER_INPUT_VEL_B: memcpy(o->vel_b[o->cur] + dst, data + (size_t)y * w * 2, w * sizeof(f2)); break;
+            case PT_LAYER_INPUT_VEL_F: memcpy(o->vel_f[o->cur] + dst, data + (size_t)y * w * 2, w * sizeof(f2)); break;
+            case PT_LAYER_INPUT_VEL_B_PREVIOUS: memcpy(o->vel_b[prev] + dst, data + (size_t)y * w * 2, w * sizeof(f2)); break;
+            case PT_LAYER_INPUT_VEL_F_PREVIOUS: memcpy(o->vel_f[prev] + dst, data + (size_t)y * w * 2, w * sizeof(f2)); break;
+            default: break;
+        }
+    }
+}
+
+void pto_upload_plain(pto* o, int which, const void* data, int w, int h) {
+    size_t n = (size_t)w * h;
+    switch (which) {
+        case PT_LAYER_INPUT_ORIENTATION:
+            free(o->img_orient); o->img_orient = (float*)zalloc(n * 4); memcpy(o->img_orient, data, n * 4);
+            o->io_w = w; o->io_h = h; break;
+        case PT_LAYER_INPUT_SCALE:
+            free(o->img_scale); o->img_scale = (f2*)zalloc(n * 8); memcpy(o->img_scale, data, n * 8);
+            o->is_w = w; o->is_h = h; break;
+        case PT_LAYER_INPUT_ID:
+            free(o->img_ids); o->img_ids = (int32_t*)zalloc(n * 4); memcpy(o->img_ids, data, n * 4);
+            o->ii_w = w; o->ii_h = h; break;
+        case PT_LAYER_RANDOM:
+            free(o->rnd); o->rnd = (f4*)zalloc(n * 16); memcpy(o->rnd, data, n * 16);
+            o->rn_w = w; o->rn_h = h; break;
+        default: break;
+    }
+}
+
+void pto_flip(pto* o) { o->cur = (o->cur + 1) % 2; }
+/* CudaBufferPair::copyBaseToWorking, cudaImageBuffer.h:335-337 */
+void pto_copy_base_to_working(pto* o) {
+    memcpy(o->off_work, o->off_base, sizeof(pt_patchxf) * (size_t)o->W * o->H);
+}
+void pto_reset_advected(pto* o) {
+    size_t n = (size_t)o->W * o->H;
+    for (int l = 0; l < 2; l++) {
+        memset(o->adv_off[l], 0, n * sizeof(pt_patchxf)); memset(o->adv_base[l], 0, n * sizeof(f4));
+        memset(o->adv_out[l], 0, n * sizeof(f4)); memset(o->adv_res[l], 0, n * sizeof(float));
+        memset(o->adv_ts[l], 0, n * sizeof(int32_t));
+    }
+}
+
+/* WorkingBuffers::loadOffsets / loadResidual, workingBuffers.cpp:166-207 */
+void pto_load_offsets(pto* o, int level, const pt_patchxf* src) {
+    int w = lvl_w(o, level), h = lvl_h(o, level);
+    for (int y = 0; y < h; y++) memcpy(o->off_base + (size_t)y * o->W, src + (size_t)y * w, w * sizeof(pt_patchxf));
+}
+void pto_load_residual(pto* o, int level, const float* src) {
+    int w = lvl_w(o, level), h = lvl_h(o, level);
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) o->res_base[(size_t)y * o->W + x] = pt_half_roundtrip(src[(size_t)y * w + x]);
+}
+void pto_get_offsets(const pto* o, int level, pt_patchxf* dst) {
+    int w = lvl_w(o, level), h = lvl_h(o, level);
+    for (int y = 0; y < h; y++) memcpy(dst + (size_t)y * w, o->off_base + (size_t)y * o->W, w * sizeof(pt_patchxf));
+}
+void pto_get_residual(const pto* o, int level, float* dst) {
+    int w = lvl_w(o, level), h = lvl_h(o, level);
+    for (int y = 0; y < h; y++) memcpy(dst + (size_t)y * w, o->res_base + (size_t)y * o->W, w * sizeof(float));
+}
+void pto_get_output(const pto* o, int level, float* dst) {
+    int w = lvl_w(o, level), h = lvl_h(o, level);
+    for (int y = 0; y < h; y++) memcpy(dst + (size_t)y * w * 4, o->canvas + (size_t)y * o->W, w * sizeof(f4));
+}
+
+/* Energy of given offsets at every level pixel, using the current canvas:
+ * FP32 contract (out32) and FP64 (out64); culled pixels give 0. */
+void pto_energy_map(const pto* o, int level, const pt_patchxf* offs, float* out32, double* out64) {
+    int w = lvl_w(o, level), h = lvl_h(o, level);
+    _Pragma("omp parallel for schedule(dynamic, 4) num_threads(o->threads)")
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            const pt_patchxf* t = &offs[(size_t)y * w + x];
+            if (image_culled(o, x, y)) {
+                if (out32) out32[(size_t)y * w + x] = 0.f;
+                if (out64) out64[(size_t)y * w + x] = 0.0;
+                continue;
+            }
+            if (out32) {
+                pixctx pc;
+                make_pixctx(o, x, y, level, &pc);
+                out32[(size_t)y * w + x] = energy_f32(o, x, y, level, t, &pc);
+            }
+            if (out64) out64[(size_t)y * w + x] = energy_f64(o, x, y, level, t);
+        }
+}
+
+/* polynomial functions exported for tests against libm */
+float pto_sinf(float t) { float s, c; pt_sincosf(t, &s, &c); return s; }
+float pto_cosf(float t) { float s, c; pt_sincosf(t, &s, &c); return c; }
+float pto_atan2f(float y, float x) { return pt_atan2f(y, x); }
+float pto_logf(float x) { return pt_logf(x); }
+float pto_acosf(float x) { return pt_acosf(x); }
+float pto_half_roundtrip(float x) { return pt_half_roundtrip(x); }
+
+/* ------------------------------------------------------------------------ */
+/* glibc rand() restatement and the random-offset pyramid                   */
+/* ------------------------------------------------------------------------ */
+
+/* glibc's TYPE_3 additive feedback generator behind srand()/rand():
+ * r[0] = seed (0 -> 1); r[i] = 16807 r[i-1] mod (2^31-1) for i < 31 (Schrage);
+ * r[i] = r[i-31] for 31 <= i < 34; r[i] = r[i-31] + r[i-3] (mod 2^32) after;
+ * outputs r[i] >> 1 for i >= 344. */
+typedef struct { uint32_t r[34]; int pos; } pto_glibc;
+
+static void glibc_srand(pto_glibc* g, uint32_t seed) {
+    int32_t word = (int32_t)seed;
+    if (seed == 0) word = 1;
+    uint32_t r[344];
+    r[0] = (uint32_t)word;
+    for (int i = 1; i < 31; i++) {
+        int32_t hi = word / 127773, lo = word % 127773;
+        word = 16807 * lo - 2836 * hi;
+        if (word < 0) word += 2147483647;
+        r[i] = (uint32_t)word;
+    }
+    for (int i = 31; i < 34; i++) r[i] = r[i - 31];
+    for (int i = 34; i < 344; i++) r[i] = r[i - 31] + r[i - 3];
+    for (int i = 0; i < 34; i++) g->r[i] = r[310 + i];
+    g->pos = 0;
+}
+static uint32_t glibc_rand(pto_glibc* g) {
+    /* ring of the last 34 values; new = value 31 back + value 3 back */
+    uint32_t v = g->r[(g->pos + 3) % 34] + g->r[(g->pos + 31) % 34];
+    g->r[g->pos] = v;
+    g->pos = (g->pos + 1) % 34;
+    return v >> 1;
+}
+
+void pto_glibc_stream(uint32_t seed, int n, int32_t* out) {
+    pto_glibc g;
+    glibc_srand(&g, seed);
+    for (int i = 0; i < n; i++) out[i] = (int32_t)glibc_rand(&g);
+}
+
+/* SynthesisFrame::createRandomPyramid for one level, synthesisFrame.cpp:66-150
+ * (single style, no keyframes).  img_rgba/img_orient: level-size input;
+ * ex_out_rgba/ex_orient: level-size exemplar; style_w0/h0: level-0 style
+ * size.  Returns the number of pixels that needed a retry. */
+int pto_random_level(uint32_t seed, int w, int h, int level, int style_w0, int style_h0,
+                     const float* img_rgba, const float* img_orient, const float* ex_out_rgba,
+                     const float* ex_orient, int ew, int transparency_ok, int orientation_enabled,
+                     float* out) {
+    pto_glibc g;
+    glibc_srand(&g, seed);
+    int retried = 0;
+    int mx = (style_w0 >> level) - 1, my = (style_h0 >> level) - 1;
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            int ox, oy, trial = 0;
+            float ia = img_rgba[((size_t)y * w + x) * 4 + 3];
+            do {
+                ox = (int)(glibc_rand(&g) % (uint32_t)mx);
+                oy = (int)(glibc_rand(&g) % (uint32_t)my);
+                trial++;
+            } while (!transparency_ok && ia > ALPHA_THRESHOLD &&
+                     ex_out_rgba[((size_t)oy * ew + ox) * 4 + 3] < ALPHA_THRESHOLD && trial < 50);
+            if (trial > 1) retried++;
+            float orient = orientation_enabled ? img_orient[(size_t)y * w + x] - ex_orient[(size_t)oy * ew + ox] : 0.f;
+            float rx = (float)glibc_rand(&g) / (float)2147483647;
+            float ry = (float)glibc_rand(&g) / (float)2147483647;
+            float* p = out + ((size_t)y * w + x) * 4;
+            p[0] = (float)ox + rx; p[1] = (float)oy + ry; p[2] = orient; p[3] = 0.0f;
+        }
+    return retried;
+}
+
+/* ------------------------------------------------------------------------ */
+/* pyramid construction, downsample.cpp:41-209, imageIO.h:136-139           */
+/* ------------------------------------------------------------------------ */
+
+/* downsampleAverage: ((((0 + p00) + p01) + p10) + p11) * 0.25 (* 0.5) */
+void pto_downsample_avg(const float* src, int w, int h, int ch, float vel_scale, float* dst) {
+    int lw = w >> 1, lh = h >> 1;
+    for (int y = 0; y < lh; y++)
+        for (int x = 0; x < lw; x++)
+            for (int c = 0; c < ch; c++) {
+                float s = 0.0f;
+                s = s + src[((size_t)(2 * y) * w + 2 * x) * ch + c];
+                s = s + src[((size_t)(2 * y) * w + 2 * x + 1) * ch + c];
+                s = s + src[((size_t)(2 * y + 1) * w + 2 * x) * ch + c];
+                s = s + src[((size_t)(2 * y + 1) * w + 2 * x + 1) * ch + c];
+                s = s * 0.25f;
+                if (vel_scale) s = s * 0.5f;
+                dst[((size_t)y * lw + x) * ch + c] = s;
+            }
+}
+
+/* downsampleVote: most frequent of the 2x2 values; ties go to the smallest
+ * value (the reference's tie order is QHash iteration order, unspecified) */
+void pto_downsample_vote(const int32_t* src, int w, int h, int32_t* dst) {
+    int lw = w >> 1, lh = h >> 1;
+    for (int y = 0; y < lh; y++)
+        for (int x = 0; x < lw; x++) {
+            int32_t v[4] = {src[(size_t)(2 * y) * w + 2 * x], src[(size_t)(2 * y) * w + 2 * x + 1],
+                            src[(size_t)(2 * y + 1) * w + 2 * x], src[(size_t)(2 * y + 1) * w + 2 * x + 1]};
+            int32_t best = v[0];
+            int bestc = -1;
+            for (int i = 0; i < 4; i++) {
+                int c = 0;
+                for (int j = 0; j < 4; j++) c += (v[j] == v[i]);
+                if (c > bestc || (c == bestc && v[i] < best)) { bestc = c; best = v[i]; }
+            }
+            dst[(size_t)y * lw + x] = best;
+        }
+}
+
+/* strucTensorToAngle, imageIO.h:136-139, on (xx, xy, yy) triples */
+void pto_tensor_to_angle(const float* t3, int n, float* out) {
+    for (int i = 0; i < n; i++) {
+        float xx = t3[3 * i], xy = t3[3 * i + 1], yy = t3[3 * i + 2];
+        float a2 = pt_atan2f((float)(2.0 * (double)xy), xx - yy);
+        float angle = (float)(0.5 * (double)a2 + M_PI_2);
+        out[i] = ((double)angle >= M_PI_2) ? (float)((double)angle - M_PI) : angle;
+    }
+}

@@ -1,0 +1,1380 @@
+// pt_context.cpp -- host side of libpainttween_gb300: the context, device
+// buffers, the C ABI of include/painttween.h and the per-frame driver.
+//
+// Buffer model.  As in the reference (src/PaintTweenCUDA/cudaImageBuffer.h,
+// workingBuffers.cpp:48-94) the image-size buffers are full resolution and a
+// level uses the top-left (W>>L) x (H>>L) rectangle.  The reference keeps a
+// base/working pair for the offsets and copies working -> base after every
+// Jacobi pass (copyWorkingToBase, :332-334).  Here the pair is two physical
+// buffers with a copy-on-write alias: after a sync the logical base and
+// working buffers are the same physical buffer, and the next writer of
+// "working" takes the other one (writing every level pixel it would otherwise
+// have left unchanged).  This removes the per-pass full-buffer copy while
+// keeping the reference's observable state.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "painttween.h"
+#include "pt_internal.h"
+
+using ptk::AdvView;
+using ptk::Arr;
+using ptk::ConvKernel;
+using ptk::ExView;
+using ptk::ImgView;
+using ptk::Params;
+using ptk::PatchPlanes;
+
+namespace {
+
+int level_count(int w, int h) {
+    // ImagePyramid level count, imagePyramid.cpp:86
+    return (int)std::min(std::floor(std::log2((float)w)), std::floor(std::log2((float)h)));
+}
+
+struct ExLevel {  // one exemplar pyramid level, all styles
+    float4* bo = nullptr;
+    float* orient = nullptr;
+    float* dt = nullptr;
+    int* ids = nullptr;
+    int w = 0, h = 0;
+    int transparent = -1;  // -1 unknown, 0/1
+};
+
+struct FrameLevel {
+    float4* rgba = nullptr;
+    float* orient = nullptr;
+    float* dt = nullptr;
+    int* ids = nullptr;
+    float2* velf = nullptr;
+    float2* velb = nullptr;
+    float2* scale = nullptr;
+    int w = 0, h = 0;
+};
+
+struct StoreEntry {
+    pt_patchxf* offs = nullptr;
+    float* res = nullptr;
+    float4* canvas = nullptr;
+    int w = 0, h = 0;
+};
+
+}  // namespace
+
+struct pt_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    size_t budget = 0, allocated = 0;
+    std::string err;
+    std::map<void*, size_t> allocs;
+
+    pt_params params{};
+    bool have_params = false;
+    float gauss[2 * ptk::kMaxRadius + 1] = {0};
+    ConvKernel hist_kernel{};
+
+    int W = 0, H = 0, SW = 0, SH = 0, NS = 0;
+    bool initialized = false;
+
+    PatchPlanes off[2]{};
+    int base_i = 0, work_i = 0;
+    float* res[2] = {nullptr, nullptr};
+    int res_i = 0;
+    float4* canvas = nullptr;
+    float* hist[2] = {nullptr, nullptr};  // [0] base, [1] working
+    AdvView adv[2]{};
+
+    // storage behind the step-wise uploads
+    float4* up_base[2] = {nullptr, nullptr};
+    float* up_dt[2] = {nullptr, nullptr};
+    float2* up_velf[2] = {nullptr, nullptr};
+    float2* up_velb[2] = {nullptr, nullptr};
+    float* up_orient = nullptr;
+    float2* up_scale = nullptr;
+    int* up_ids = nullptr;
+    float4* rnd = nullptr;
+    ImgView img{};
+
+    ExLevel up_ex;     // exemplar storage of the step-wise API
+    ExLevel* ex = nullptr;
+    size_t ex_cap = 0;  // texels (w*h*ns) allocated in up_ex
+
+    // staging
+    void* stage = nullptr;
+    size_t stage_bytes = 0;
+    uint32_t* states = nullptr;
+    size_t states_cap = 0;
+    int* flag = nullptr;
+
+    // resident working set
+    std::vector<ExLevel> style_levels;
+    std::vector<int> style_set;
+    std::map<int, std::vector<FrameLevel>> frames;
+    std::map<std::tuple<int, int, int>, StoreEntry> store;
+
+    uint64_t launches = 0;
+    uint32_t pass_counter = 0;
+    std::map<int, std::vector<uint32_t>> jump_cache;  // M^(4w)
+};
+
+// ---------------------------------------------------------------------------
+// errors and allocation
+// ---------------------------------------------------------------------------
+
+static pt_status fail(pt_ctx* c, pt_status s, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    c->err = buf;
+    return s;
+}
+
+#define CU(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return fail(c, PT_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+#define LN(call)              \
+    do {                              \
+        CU(call);                     \
+        c->launches++;                \
+    } while (0)
+
+#define TRY(expr)                      \
+    do {                               \
+        pt_status s_ = (expr);         \
+        if (s_ != PT_OK) return s_;    \
+    } while (0)
+
+static pt_status dalloc(pt_ctx* c, void** p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) bytes = 16;
+    if (c->budget && c->allocated + bytes > c->budget)
+        return fail(c, PT_ERR_BUDGET, "allocation of %zu bytes exceeds the HBM budget (%zu of %zu used)", bytes,
+                    c->allocated, c->budget);
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, PT_ERR_OOM, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    }
+    c->allocated += bytes;
+    c->allocs[*p] = bytes;
+    e = cudaMemsetAsync(*p, 0, bytes, c->stream);
+    if (e != cudaSuccess) return fail(c, PT_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));
+    return PT_OK;
+}
+template <class T>
+static pt_status dalloc_t(pt_ctx* c, T** p, size_t count) {
+    void* v = nullptr;
+    pt_status s = dalloc(c, &v, count * sizeof(T));
+    *p = (T*)v;
+    return s;
+}
+static void dfree(pt_ctx* c, void* p) {
+    if (!p) return;
+    auto it = c->allocs.find(p);
+    if (it != c->allocs.end()) {
+        c->allocated -= it->second;
+        c->allocs.erase(it);
+    }
+    cudaFree(p);
+}
+template <class T>
+static void dfree_t(pt_ctx* c, T*& p) {
+    dfree(c, (void*)p);
+    p = nullptr;
+}
+
+static pt_status ensure_stage(pt_ctx* c, size_t bytes) {
+    if (c->stage_bytes >= bytes) return PT_OK;
+    dfree(c, c->stage);
+    c->stage = nullptr;
+    c->stage_bytes = 0;
+    TRY(dalloc(c, &c->stage, bytes));
+    c->stage_bytes = bytes;
+    return PT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// kernel parameters
+// ---------------------------------------------------------------------------
+
+static PatchPlanes base_planes(pt_ctx* c) { return c->off[c->base_i]; }
+
+static Params make_params(pt_ctx* c, int level) {
+    Params P;
+    memset(&P, 0, sizeof(P));
+    const pt_params& p = c->params;
+    P.W = c->W;
+    P.H = c->H;
+    P.level = level;
+    P.lw = c->W >> level;
+    P.lh = c->H >> level;
+    P.r = p.residualWindowSize;
+    for (int i = 0; i < 2 * P.r + 1; i++) P.gauss[i] = c->gauss[i];
+    P.scaleWU = p.residualWindowScaleU;
+    P.scaleWV = p.residualWindowScaleV;
+    P.alphaWeight = p.alphaWeight;
+    P.inputAnalogyWeight = p.inputAnalogyWeight;
+    P.canvasOutputWeight = p.canvasOutputWeight;
+    P.distTransWeight = p.distTransWeight;
+    P.styleObjIdWeight = p.styleObjIdWeight;
+    P.coherenceWeight = p.coherenceWeight;
+    P.coherenceRatioRange = p.coherenceRatioRange;
+    P.coherenceAngleRange = p.coherenceAngleRange;
+    P.tdIn = p.timeDerivativeInputWeight;
+    P.tdOut = p.timeDerivativeOutputWeight;
+    P.tc = p.temporalCoherenceWeight;
+    P.maxDistortion = p.maxDistortion;
+    P.hysteresisWeight = p.hysteresisWeight;
+    for (int i = 0; i < PT_MAX_STYLES; i++) {
+        P.histThreshold[i] = p.offsetsHistogramThreshold[i];
+        P.histSlope[i] = p.offsetsHistogramSlope[i];
+    }
+    P.jitter = p.advectionJitter;
+    P.numStyles = p.numStyles > 0 ? p.numStyles : 1;
+    P.transparencyOk = p.transparencyOk;
+    P.orientationEnabled = p.orientationEnabled;
+    P.lumShiftEnable = p.lumShiftEnable;
+    P.distTransCull = p.distTransCull;
+    P.direction = p.direction;
+    P.scatterSamples = p.scatterSamplesCount;
+    P.rngMode = p.rngMode;
+    P.rngSeed = p.rngSeed;
+    P.histPitch = c->SW;
+    P.histRows = c->SH * c->NS;
+    P.histW = c->SW >> level;
+    P.histH = (c->SH * c->NS) >> level;
+    P.hist = c->hist[0];
+    if (c->ex) {
+        P.ex.bo = c->ex->bo;
+        P.ex.orient = c->ex->orient;
+        P.ex.dt = c->ex->dt;
+        P.ex.ids = c->ex->ids;
+        P.ex.w = c->ex->w;
+        P.ex.h = c->ex->h;
+        P.ex.ns = c->NS;
+    }
+    P.img = c->img;
+    P.off = base_planes(c);
+    P.res = c->res[c->res_i];
+    P.canvas = c->canvas;
+    P.adv[0] = c->adv[0];
+    P.adv[1] = c->adv[1];
+    return P;
+}
+
+static pt_status check_ready(pt_ctx* c, int level, bool need_ex = true, bool need_img = true) {
+    if (!c->initialized) return fail(c, PT_ERR_STATE, "pt_initialize has not been called");
+    if (!c->have_params) return fail(c, PT_ERR_STATE, "pt_set_params has not been called");
+    if (level < 0 || (c->W >> level) < 1 || (c->H >> level) < 1)
+        return fail(c, PT_ERR_INVALID, "level %d out of range", level);
+    if (need_ex && (!c->ex || !c->ex->bo)) return fail(c, PT_ERR_STATE, "no exemplar level loaded");
+    if (need_img) {
+        const ImgView& I = c->img;
+        int lw = c->W >> level, lh = c->H >> level;
+        if (!I.base[I.cur].p || I.base[I.cur].w != lw || I.base[I.cur].h != lh)
+            return fail(c, PT_ERR_STATE, "input colour of level %d not uploaded", level);
+        if (!I.dt[I.cur].p || I.dt[I.cur].w != lw || I.dt[I.cur].h != lh)
+            return fail(c, PT_ERR_STATE, "input distance transform of level %d not uploaded", level);
+        if (!I.orient.p || !I.scale.p || !I.ids.p)
+            return fail(c, PT_ERR_STATE, "input orientation/scale/ids not uploaded");
+    }
+    return PT_OK;
+}
+
+// copy-on-write helpers for the offsets pair
+static PatchPlanes writable_work(pt_ctx* c, bool* was_aliased) {
+    if (was_aliased) *was_aliased = (c->work_i == c->base_i);
+    if (c->work_i == c->base_i) c->work_i = 1 - c->base_i;
+    return c->off[c->work_i];
+}
+static pt_status copy_planes_full(pt_ctx* c, PatchPlanes dst, PatchPlanes src) {
+    size_t n = (size_t)c->W * c->H;
+    CU(cudaMemcpyAsync(dst.A, src.A, n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
+    CU(cudaMemcpyAsync(dst.B, src.B, n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
+    CU(cudaMemcpyAsync(dst.C, src.C, n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+    return PT_OK;
+}
+// base about to be partly overwritten: give it its own buffer first
+static pt_status base_for_partial_write(pt_ctx* c, PatchPlanes* out) {
+    if (c->base_i == c->work_i) {
+        int nb = 1 - c->work_i;
+        TRY(copy_planes_full(c, c->off[nb], c->off[c->work_i]));
+        c->base_i = nb;
+    }
+    *out = c->off[c->base_i];
+    return PT_OK;
+}
+// base about to be overwritten on the whole level rectangle
+static PatchPlanes base_for_full_write(pt_ctx* c) {
+    if (c->base_i == c->work_i) c->base_i = 1 - c->work_i;
+    return c->off[c->base_i];
+}
+
+// ---------------------------------------------------------------------------
+// syncBuffers and friends
+// ---------------------------------------------------------------------------
+
+static bool histogram_on(pt_ctx* c) {
+    for (int i = 0; i < c->params.numStyles && i < PT_MAX_STYLES; i++)
+        if (c->params.offsetsHistogramSlope[i] > 0.0f) return true;
+    return false;
+}
+
+static pt_status do_residual(pt_ctx* c, int level) {
+    Params P = make_params(c, level);
+    LN(pt::launch_residual(P, c->res[c->res_i], c->stream));
+    return PT_OK;
+}
+
+// TexSynth::syncBuffers, texSynth_kernel.cu:1240-1303
+static pt_status do_sync(pt_ctx* c, int level, int flags) {
+    if (!(flags & PT_DONT_COPY_OFFSETS)) c->base_i = c->work_i;
+    if (histogram_on(c)) {
+        size_t hn = (size_t)c->SW * c->SH * c->NS * sizeof(float);
+        CU(cudaMemsetAsync(c->hist[0], 0, hn, c->stream));
+        CU(cudaMemsetAsync(c->hist[1], 0, hn, c->stream));
+        // calculateOffsetsHistogram adds nothing (its atomicAdd is commented
+        // out at :258); rows base -> working, columns working -> base.
+        int hw = c->SW >> level, hh = (c->SH * c->NS) >> level;
+        LN(pt::launch_conv(c->hist[0], c->hist[1], hw, hh, c->SW, 1, c->hist_kernel, c->stream));
+        LN(pt::launch_conv(c->hist[1], c->hist[0], hw, hh, c->SW, 0, c->hist_kernel, c->stream));
+    }
+    Params P = make_params(c, level);
+    LN(pt::launch_canvas(P, c->canvas, c->stream));
+    if (!(flags & PT_DONT_UPDATE_RESIDUAL)) TRY(do_residual(c, level));
+    return PT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// glibc random(): seeding and jump-ahead (row-parallel random levels)
+// ---------------------------------------------------------------------------
+
+// state of the TYPE_3 generator after srand(seed): the 31 values
+// r[313..343] that produce the first output r[344] >> 1
+static void glibc_state(uint32_t seed, uint32_t out[31]) {
+    int32_t word = (int32_t)seed;
+    if (seed == 0) word = 1;
+    std::vector<uint32_t> r(344);
+    r[0] = (uint32_t)word;
+    for (int i = 1; i < 31; i++) {
+        int32_t hi = word / 127773, lo = word % 127773;
+        word = 16807 * lo - 2836 * hi;
+        if (word < 0) word += 2147483647;
+        r[i] = (uint32_t)word;
+    }
+    for (int i = 31; i < 34; i++) r[i] = r[i - 31];
+    for (int i = 34; i < 344; i++) r[i] = r[i - 31] + r[i - 3];
+    for (int i = 0; i < 31; i++) out[i] = r[313 + i];
+}
+
+// 31x31 matrices over Z/2^32, row-major
+static void matmul31(const uint32_t* a, const uint32_t* b, uint32_t* out) {
+    for (int i = 0; i < 31; i++)
+        for (int j = 0; j < 31; j++) {
+            uint32_t s = 0;
+            for (int k = 0; k < 31; k++) s += a[i * 31 + k] * b[k * 31 + j];
+            out[i * 31 + j] = s;
+        }
+}
+static std::vector<uint32_t> step_power(uint64_t n) {
+    // one step: s'[i] = s[i+1] (i < 30), s'[30] = s[0] + s[28]
+    std::vector<uint32_t> M(961, 0), R(961, 0), T(961);
+    for (int i = 0; i < 30; i++) M[i * 31 + i + 1] = 1;
+    M[30 * 31 + 0] = 1;
+    M[30 * 31 + 28] += 1;
+    for (int i = 0; i < 31; i++) R[i * 31 + i] = 1;
+    while (n) {
+        if (n & 1) { matmul31(R.data(), M.data(), T.data()); R.swap(T); }
+        matmul31(M.data(), M.data(), T.data());
+        M.swap(T);
+        n >>= 1;
+    }
+    return R;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+// The public functions below take their C linkage from the declarations in
+// painttween.h.
+
+int pt_abi_version(void) { return PT_ABI_VERSION; }
+
+const char* pt_status_string(pt_status s) {
+    switch (s) {
+        case PT_OK: return "PT_OK";
+        case PT_ERR_INVALID: return "PT_ERR_INVALID";
+        case PT_ERR_CUDA: return "PT_ERR_CUDA";
+        case PT_ERR_OOM: return "PT_ERR_OOM";
+        case PT_ERR_STATE: return "PT_ERR_STATE";
+        case PT_ERR_UNSUPPORTED: return "PT_ERR_UNSUPPORTED";
+        case PT_ERR_TIMEOUT: return "PT_ERR_TIMEOUT";
+        case PT_ERR_BUDGET: return "PT_ERR_BUDGET";
+    }
+    return "PT_ERR_UNKNOWN";
+}
+
+const char* pt_last_error(const pt_ctx* c) { return c ? c->err.c_str() : "null context"; }
+size_t pt_device_bytes(const pt_ctx* c) { return c ? c->allocated : 0; }
+uint64_t pt_kernel_launches(const pt_ctx* c) { return c ? c->launches : 0; }
+
+void pt_default_params(pt_params* p) {
+    memset(p, 0, sizeof(*p));
+    p->residualWindowSize = 4;
+    p->inputAnalogyWeight = 1.0f;
+    p->canvasOutputWeight = 1.0f;
+    p->orientationEnabled = 1;
+    p->numStyles = 1;
+    p->maxDistortion = 4.0f;
+    p->alphaWeight = 1.0f;
+    p->coherenceRatioRange = 2.0f;
+    p->coherenceAngleRange = 0.25f;
+    p->levels = 4;
+    p->scatterSamplesCount = 25;
+    p->timeDerivativeInputWeight = 1.f;
+    p->timeDerivativeOutputWeight = 1.f;
+    p->temporalCoherenceWeight = 0.2f;
+    p->distTransCull = 50;
+    p->residualWindowScaleU = 1;
+    p->residualWindowScaleV = 1;
+    p->firstKeyIndex = -1;
+    p->lastKeyIndex = -1;
+    p->direction = PT_BIDIRECTIONAL;
+    p->iterations = 3;
+    p->fixupPasses = 1;
+    p->scheme = PT_S_FMBM_RM;
+    p->finalLevel = 0;
+    p->rngMode = PT_RNG_REFERENCE;
+}
+
+pt_status pt_create(int device, size_t budget, pt_ctx** out) {
+    if (!out) return PT_ERR_INVALID;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+        cudaGetLastError();
+        return PT_ERR_CUDA;
+    }
+    if (cudaSetDevice(device) != cudaSuccess) return PT_ERR_CUDA;
+    pt_ctx* c = new pt_ctx();
+    c->device = device;
+    c->budget = budget;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return PT_ERR_CUDA;
+    }
+    pt_default_params(&c->params);
+    if (dalloc_t(c, &c->flag, 4) != PT_OK) {
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return PT_ERR_OOM;
+    }
+    *out = c;
+    return PT_OK;
+}
+
+static void free_frames(pt_ctx* c) {
+    for (auto& kv : c->frames)
+        for (auto& L : kv.second) {
+            dfree_t(c, L.rgba); dfree_t(c, L.orient); dfree_t(c, L.dt); dfree_t(c, L.ids);
+            dfree_t(c, L.velf); dfree_t(c, L.velb); dfree_t(c, L.scale);
+        }
+    c->frames.clear();
+}
+static void free_store(pt_ctx* c) {
+    for (auto& kv : c->store) {
+        dfree_t(c, kv.second.offs);
+        dfree_t(c, kv.second.res);
+        dfree_t(c, kv.second.canvas);
+    }
+    c->store.clear();
+}
+
+pt_status pt_destroy(pt_ctx* c) {
+    if (!c) return PT_ERR_INVALID;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (auto& kv : c->allocs) cudaFree(kv.first);
+    c->allocs.clear();
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return PT_OK;
+}
+
+pt_status pt_synchronize(pt_ctx* c) {
+    if (!c) return PT_ERR_INVALID;
+    CU(cudaStreamSynchronize(c->stream));
+    return PT_OK;
+}
+
+pt_status pt_set_params(pt_ctx* c, const pt_params* p) {
+    if (!c || !p) return PT_ERR_INVALID;
+    if (p->residualWindowSize < 0 || p->residualWindowSize > ptk::kMaxRadius)
+        return fail(c, PT_ERR_INVALID, "residualWindowSize %d outside [0, %d]", p->residualWindowSize,
+                    ptk::kMaxRadius);
+    if (p->interpolateKeyFrame) return fail(c, PT_ERR_UNSUPPORTED, "keyframe interpolation is not implemented");
+    if (p->colorspace != 0) return fail(c, PT_ERR_UNSUPPORTED, "only the RGB colour space is implemented");
+    if (p->numStyles < 1 || p->numStyles > PT_MAX_STYLES) return fail(c, PT_ERR_INVALID, "numStyles out of range");
+    if (p->rngMode != PT_RNG_REFERENCE && p->rngMode != PT_RNG_COUNTER)
+        return fail(c, PT_ERR_INVALID, "unknown rngMode");
+    c->params = *p;
+    c->have_params = true;
+    // TexSynth::setup: unnormalised Gaussian with sigma = r/3
+    // (allocateGaussianKernel(..., normalize=false), convolution.cu:37-60)
+    int r = p->residualWindowSize;
+    float sigma = (float)r / 3.0f, s2 = sigma * sigma;
+    c->hist_kernel.r = r;
+    for (int i = 0; i <= r; i++) {
+        float w = expf(-(float)(i * i) / (2.f * s2));
+        c->gauss[r + i] = w;
+        c->gauss[r - i] = w;
+        float wn = w / (sqrtf(2.f * (float)M_PI) * sigma);  // normalised copy for the histogram
+        c->hist_kernel.w[r + i] = wn;
+        c->hist_kernel.w[r - i] = wn;
+    }
+    return PT_OK;
+}
+
+pt_status pt_get_params(const pt_ctx* c, pt_params* out) {
+    if (!c || !out) return PT_ERR_INVALID;
+    *out = c->params;
+    return PT_OK;
+}
+
+static pt_status alloc_planes(pt_ctx* c, PatchPlanes* p, size_t n) {
+    TRY(dalloc_t(c, &p->A, n));
+    TRY(dalloc_t(c, &p->B, n));
+    TRY(dalloc_t(c, &p->C, n));
+    return PT_OK;
+}
+static void free_planes(pt_ctx* c, PatchPlanes* p) {
+    dfree_t(c, p->A);
+    dfree_t(c, p->B);
+    dfree_t(c, p->C);
+}
+
+pt_status pt_initialize(pt_ctx* c, int iw, int ih, int sw, int sh, int ns) {
+    if (!c) return PT_ERR_INVALID;
+    if (iw < 2 || ih < 2 || sw < 2 || sh < 2 || ns < 1 || ns > PT_MAX_STYLES)
+        return fail(c, PT_ERR_INVALID, "bad sizes %dx%d style %dx%dx%d", iw, ih, sw, sh, ns);
+    CU(cudaSetDevice(c->device));
+    if (c->initialized && iw == c->W && ih == c->H && sw == c->SW && sh == c->SH && ns == c->NS) return PT_OK;
+    // release the image-size state
+    for (int i = 0; i < 2; i++) {
+        free_planes(c, &c->off[i]);
+        dfree_t(c, c->res[i]);
+        dfree_t(c, c->hist[i]);
+        free_planes(c, &c->adv[i].off);
+        dfree_t(c, c->adv[i].base); dfree_t(c, c->adv[i].out); dfree_t(c, c->adv[i].res); dfree_t(c, c->adv[i].ts);
+        dfree_t(c, c->up_base[i]); dfree_t(c, c->up_dt[i]); dfree_t(c, c->up_velf[i]); dfree_t(c, c->up_velb[i]);
+    }
+    dfree_t(c, c->canvas); dfree_t(c, c->up_orient); dfree_t(c, c->up_scale); dfree_t(c, c->up_ids);
+    dfree_t(c, c->rnd);
+    free_store(c);
+    c->initialized = false;
+    c->W = iw; c->H = ih; c->SW = sw; c->SH = sh; c->NS = ns;
+    size_t n = (size_t)iw * ih;
+    for (int i = 0; i < 2; i++) {
+        TRY(alloc_planes(c, &c->off[i], n));
+        TRY(dalloc_t(c, &c->res[i], n));
+        TRY(dalloc_t(c, &c->hist[i], (size_t)sw * sh * ns));
+        TRY(alloc_planes(c, &c->adv[i].off, n));
+        TRY(dalloc_t(c, &c->adv[i].base, n));
+        TRY(dalloc_t(c, &c->adv[i].out, n));
+        TRY(dalloc_t(c, &c->adv[i].res, n));
+        TRY(dalloc_t(c, &c->adv[i].ts, n));
+    }
+    TRY(dalloc_t(c, &c->canvas, n));
+    c->base_i = c->work_i = 0;
+    c->res_i = 0;
+    memset(&c->img, 0, sizeof(c->img));
+    c->initialized = true;
+    return PT_OK;
+}
+
+// zero the working state (the reference starts each synthesis from freshly
+// memset buffers, cudaImageBuffer.h:154-162)
+static pt_status reset_working(pt_ctx* c) {
+    size_t n = (size_t)c->W * c->H;
+    for (int i = 0; i < 2; i++) {
+        CU(cudaMemsetAsync(c->off[i].A, 0, n * sizeof(float4), c->stream));
+        CU(cudaMemsetAsync(c->off[i].B, 0, n * sizeof(float4), c->stream));
+        CU(cudaMemsetAsync(c->off[i].C, 0, n * sizeof(float), c->stream));
+        CU(cudaMemsetAsync(c->res[i], 0, n * sizeof(float), c->stream));
+        CU(cudaMemsetAsync(c->hist[i], 0, (size_t)c->SW * c->SH * c->NS * sizeof(float), c->stream));
+    }
+    CU(cudaMemsetAsync(c->canvas, 0, n * sizeof(float4), c->stream));
+    c->base_i = c->work_i = 0;
+    c->res_i = 0;
+    c->pass_counter = 0;
+    return pt_reset_advected_buffers(c);
+}
+
+pt_status pt_reset_advected_buffers(pt_ctx* c) {
+    if (!c || !c->initialized) return PT_ERR_STATE;
+    size_t n = (size_t)c->W * c->H;
+    for (int i = 0; i < 2; i++) {
+        CU(cudaMemsetAsync(c->adv[i].off.A, 0, n * sizeof(float4), c->stream));
+        CU(cudaMemsetAsync(c->adv[i].off.B, 0, n * sizeof(float4), c->stream));
+        CU(cudaMemsetAsync(c->adv[i].off.C, 0, n * sizeof(float), c->stream));
+        CU(cudaMemsetAsync(c->adv[i].base, 0, n * sizeof(float4), c->stream));
+        CU(cudaMemsetAsync(c->adv[i].out, 0, n * sizeof(float4), c->stream));
+        CU(cudaMemsetAsync(c->adv[i].res, 0, n * sizeof(float), c->stream));
+        CU(cudaMemsetAsync(c->adv[i].ts, 0, n * sizeof(int), c->stream));
+    }
+    return PT_OK;
+}
+
+pt_status pt_initialize_exemplars(pt_ctx* c, int w, int h, int ns) {
+    if (!c) return PT_ERR_INVALID;
+    if (!c->initialized) return fail(c, PT_ERR_STATE, "pt_initialize has not been called");
+    if (w < 2 || h < 2 || ns != c->NS) return fail(c, PT_ERR_INVALID, "bad exemplar size %dx%dx%d", w, h, ns);
+    size_t n = (size_t)w * h * ns;
+    if (n > c->ex_cap) {
+        dfree_t(c, c->up_ex.bo); dfree_t(c, c->up_ex.orient); dfree_t(c, c->up_ex.dt); dfree_t(c, c->up_ex.ids);
+        TRY(dalloc_t(c, &c->up_ex.bo, 2 * n));
+        TRY(dalloc_t(c, &c->up_ex.orient, n));
+        TRY(dalloc_t(c, &c->up_ex.dt, n));
+        TRY(dalloc_t(c, &c->up_ex.ids, n));
+        c->ex_cap = n;
+    }
+    c->up_ex.w = w;
+    c->up_ex.h = h;
+    c->up_ex.transparent = -1;
+    c->ex = &c->up_ex;
+    return PT_OK;
+}
+
+// Host-to-device copy that has finished reading `src` on return, so callers
+// may reuse or free their host buffer at once (the reference's uploads are
+// synchronous as well).
+static pt_status h2d(pt_ctx* c, void* dst, const void* src, size_t bytes) {
+    CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return PT_OK;
+}
+
+pt_status pt_upload_image_color4(pt_ctx* c, int level, int layer, const float* rgba, int w, int h, int style) {
+    if (!c || !rgba) return PT_ERR_INVALID;
+    if (!c->initialized) return fail(c, PT_ERR_STATE, "pt_initialize has not been called");
+    size_t n = (size_t)w * h;
+    if (layer == PT_LAYER_EXEMPLAR_BASE || layer == PT_LAYER_EXEMPLAR_OUTPUT) {
+        if (!c->ex || c->ex != &c->up_ex || w != c->up_ex.w || h != c->up_ex.h || style < 0 || style >= c->NS)
+            return fail(c, PT_ERR_INVALID, "exemplar upload %dx%d style %d does not match pt_initialize_exemplars", w,
+                        h, style);
+        TRY(ensure_stage(c, n * sizeof(float4)));
+        TRY(h2d(c, c->stage, rgba, n * sizeof(float4)));
+        LN(pt::launch_interleave((const float4*)c->stage, (int)n, c->up_ex.bo + 2 * n * style,
+                                 layer == PT_LAYER_EXEMPLAR_OUTPUT ? 1 : 0, c->stream));
+        if (layer == PT_LAYER_EXEMPLAR_OUTPUT) c->up_ex.transparent = -1;
+        return PT_OK;
+    }
+    if (level < 0 || w != (c->W >> level) || h != (c->H >> level))
+        return fail(c, PT_ERR_INVALID, "image upload %dx%d does not match level %d", w, h, level);
+    int cur = c->img.cur;
+    if (layer == PT_LAYER_INPUT_COLOR) {
+        if (!c->up_base[cur]) TRY(dalloc_t(c, &c->up_base[cur], (size_t)c->W * c->H));
+        TRY(h2d(c, c->up_base[cur], rgba, n * sizeof(float4)));
+        c->img.base[cur] = Arr<float4>{c->up_base[cur], w, h};
+        return PT_OK;
+    }
+    if (layer == PT_LAYER_RANDOM) {
+        if (!c->rnd) TRY(dalloc_t(c, &c->rnd, (size_t)c->W * c->H));
+        TRY(h2d(c, c->rnd, rgba, n * sizeof(float4)));
+        c->img.rnd = Arr<float4>{c->rnd, w, h};
+        return PT_OK;
+    }
+    return fail(c, PT_ERR_UNSUPPORTED, "colour layer %d not supported", layer);
+}
+
+pt_status pt_upload_image_float(pt_ctx* c, int level, int layer, const float* data, int w, int h, int style) {
+    if (!c || !data) return PT_ERR_INVALID;
+    if (!c->initialized) return fail(c, PT_ERR_STATE, "pt_initialize has not been called");
+    size_t n = (size_t)w * h;
+    if (layer == PT_LAYER_EXEMPLAR_ORIENTATION || layer == PT_LAYER_EXEMPLAR_DIST_TRANS) {
+        if (!c->ex || c->ex != &c->up_ex || w != c->up_ex.w || h != c->up_ex.h || style < 0 || style >= c->NS)
+            return fail(c, PT_ERR_INVALID, "exemplar upload does not match pt_initialize_exemplars");
+        float* dst = (layer == PT_LAYER_EXEMPLAR_ORIENTATION ? c->up_ex.orient : c->up_ex.dt) + n * style;
+        return h2d(c, dst, data, n * sizeof(float));
+    }
+    if (level < 0 || w != (c->W >> level) || h != (c->H >> level))
+        return fail(c, PT_ERR_INVALID, "image upload %dx%d does not match level %d", w, h, level);
+    int cur = c->img.cur;
+    if (layer == PT_LAYER_INPUT_ORIENTATION) {
+        if (!c->up_orient) TRY(dalloc_t(c, &c->up_orient, (size_t)c->W * c->H));
+        TRY(h2d(c, c->up_orient, data, n * sizeof(float)));
+        c->img.orient = Arr<float>{c->up_orient, w, h};
+        return PT_OK;
+    }
+    if (layer == PT_LAYER_INPUT_DIST_TRANS) {
+        if (!c->up_dt[cur]) TRY(dalloc_t(c, &c->up_dt[cur], (size_t)c->W * c->H));
+        TRY(h2d(c, c->up_dt[cur], data, n * sizeof(float)));
+        c->img.dt[cur] = Arr<float>{c->up_dt[cur], w, h};
+        return PT_OK;
+    }
+    return fail(c, PT_ERR_UNSUPPORTED, "float layer %d not supported", layer);
+}
+
+pt_status pt_upload_image_float2(pt_ctx* c, int level, int layer, const float* xy, int w, int h) {
+    if (!c || !xy) return PT_ERR_INVALID;
+    if (!c->initialized) return fail(c, PT_ERR_STATE, "pt_initialize has not been called");
+    if (level < 0 || w != (c->W >> level) || h != (c->H >> level))
+        return fail(c, PT_ERR_INVALID, "image upload %dx%d does not match level %d", w, h, level);
+    size_t n = (size_t)w * h;
+    int cur = c->img.cur, prev = 1 - c->img.cur;
+    float2** store = nullptr;
+    Arr<float2>* slot = nullptr;
+    switch (layer) {
+        case PT_LAYER_INPUT_VEL_B: store = &c->up_velb[cur]; slot = &c->img.velb[cur]; break;
+        case PT_LAYER_INPUT_VEL_F: store = &c->up_velf[cur]; slot = &c->img.velf[cur]; break;
+        case PT_LAYER_INPUT_VEL_B_PREVIOUS: store = &c->up_velb[prev]; slot = &c->img.velb[prev]; break;
+        case PT_LAYER_INPUT_VEL_F_PREVIOUS: store = &c->up_velf[prev]; slot = &c->img.velf[prev]; break;
+        case PT_LAYER_INPUT_SCALE: store = &c->up_scale; slot = &c->img.scale; break;
+        default: return fail(c, PT_ERR_UNSUPPORTED, "float2 layer %d not supported", layer);
+    }
+    if (!*store) TRY(dalloc_t(c, store, (size_t)c->W * c->H));
+    TRY(h2d(c, *store, xy, n * sizeof(float2)));
+    *slot = Arr<float2>{*store, w, h};
+    return PT_OK;
+}
+
+pt_status pt_upload_image_int(pt_ctx* c, int level, int layer, const int32_t* data, int w, int h, int style) {
+    if (!c || !data) return PT_ERR_INVALID;
+    if (!c->initialized) return fail(c, PT_ERR_STATE, "pt_initialize has not been called");
+    size_t n = (size_t)w * h;
+    if (layer == PT_LAYER_EXEMPLAR_OBJECT_IDS) {
+        if (!c->ex || c->ex != &c->up_ex || w != c->up_ex.w || h != c->up_ex.h || style < 0 || style >= c->NS)
+            return fail(c, PT_ERR_INVALID, "exemplar upload does not match pt_initialize_exemplars");
+        return h2d(c, c->up_ex.ids + n * style, data, n * sizeof(int));
+    }
+    if (layer == PT_LAYER_INPUT_ID) {
+        if (level < 0 || w != (c->W >> level) || h != (c->H >> level))
+            return fail(c, PT_ERR_INVALID, "image upload %dx%d does not match level %d", w, h, level);
+        if (!c->up_ids) TRY(dalloc_t(c, &c->up_ids, (size_t)c->W * c->H));
+        TRY(h2d(c, c->up_ids, data, n * sizeof(int)));
+        c->img.ids = Arr<int>{c->up_ids, w, h};
+        return PT_OK;
+    }
+    return fail(c, PT_ERR_UNSUPPORTED, "int layer %d not supported", layer);
+}
+
+pt_status pt_flip_anim_buffers(pt_ctx* c) {
+    if (!c) return PT_ERR_INVALID;
+    c->img.cur = 1 - c->img.cur;
+    return PT_OK;
+}
+
+// --- per-step compute --------------------------------------------------------
+
+static pt_status ensure_transparency_known(pt_ctx* c) {
+    if (c->ex->transparent >= 0) return PT_OK;
+    CU(cudaMemsetAsync(c->flag, 0, sizeof(int), c->stream));
+    LN(pt::launch_any_transparent(c->ex->bo, (size_t)c->ex->w * c->ex->h, c->flag, c->stream));
+    int f = 0;
+    CU(cudaMemcpyAsync(&f, c->flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    c->ex->transparent = f ? 1 : 0;
+    return PT_OK;
+}
+
+pt_status pt_create_random_level(pt_ctx* c, int level, int frame) {
+    if (!c) return PT_ERR_INVALID;
+    TRY(check_ready(c, level));
+    int lw = c->W >> level, lh = c->H >> level;
+    int mx = (c->SW >> level) - 1, my = (c->SH >> level) - 1;
+    if (mx < 1 || my < 1) return fail(c, PT_ERR_INVALID, "style too small for level %d", level);
+    if (!c->rnd) TRY(dalloc_t(c, &c->rnd, (size_t)c->W * c->H));
+    ExView ex{c->ex->bo, c->ex->orient, c->ex->dt, c->ex->ids, c->ex->w, c->ex->h, c->NS};
+    const ImgView& I = c->img;
+    int mode;
+    uint32_t seed = (uint32_t)(frame * level);
+    if (c->params.rngMode == PT_RNG_COUNTER) {
+        mode = 2;
+        seed = c->params.rngSeed ^ (0x9E3779B9u * (uint32_t)(frame + 1)) ^ (0x85EBCA6Bu * (uint32_t)(level + 1));
+    } else {
+        TRY(ensure_transparency_known(c));
+        mode = (c->params.transparencyOk || !c->ex->transparent) ? 0 : 1;
+        uint32_t s0[31];
+        glibc_state(seed, s0);
+        size_t need = mode == 0 ? (size_t)lh * 31 : 31;
+        if (need > c->states_cap) {
+            dfree_t(c, c->states);
+            TRY(dalloc_t(c, &c->states, need));
+            c->states_cap = need;
+        }
+        std::vector<uint32_t> host(need);
+        if (mode == 0) {
+            auto it = c->jump_cache.find(lw);
+            if (it == c->jump_cache.end()) it = c->jump_cache.emplace(lw, step_power(4ull * (uint64_t)lw)).first;
+            const std::vector<uint32_t>& A = it->second;
+            std::vector<uint32_t> s(s0, s0 + 31), t(31);
+            for (int y = 0; y < lh; y++) {
+                memcpy(&host[(size_t)y * 31], s.data(), 31 * sizeof(uint32_t));
+                for (int i = 0; i < 31; i++) {
+                    uint32_t acc = 0;
+                    for (int k = 0; k < 31; k++) acc += A[i * 31 + k] * s[k];
+                    t[i] = acc;
+                }
+                s.swap(t);
+            }
+        } else {
+            memcpy(host.data(), s0, sizeof(s0));
+        }
+        CU(cudaMemcpyAsync(c->states, host.data(), need * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
+        CU(cudaStreamSynchronize(c->stream));  // host vector goes out of scope
+    }
+    LN(pt::launch_random_level(mode, lw, lh, mx, my, c->params.transparencyOk, c->params.orientationEnabled,
+                               I.base[I.cur], I.orient, ex, c->rnd, c->states, seed, c->stream));
+    c->img.rnd = Arr<float4>{c->rnd, lw, lh};
+    return PT_OK;
+}
+
+pt_status pt_randomize_offsets(pt_ctx* c, int level) {
+    if (!c) return PT_ERR_INVALID;
+    TRY(check_ready(c, level));
+    if (!c->img.rnd.p) return fail(c, PT_ERR_STATE, "no random level");
+    PatchPlanes work = writable_work(c, nullptr);
+    Params P = make_params(c, level);
+    LN(pt::launch_random_offsets(P, work, c->stream));
+    return do_sync(c, level, 0);
+}
+
+pt_status pt_propagate(pt_ctx* c, int level, int jump, int key_index) {
+    if (!c) return PT_ERR_INVALID;
+    TRY(check_ready(c, level));
+    if (key_index >= 0) return fail(c, PT_ERR_UNSUPPORTED, "keyframe propagation is not implemented");
+    PatchPlanes work = writable_work(c, nullptr);
+    Params P = make_params(c, level);
+    LN(pt::launch_propagate(P, work, jump, c->stream));
+    return do_sync(c, level, 0);
+}
+
+pt_status pt_scatter(pt_ctx* c, int level, int key_index) {
+    if (!c) return PT_ERR_INVALID;
+    TRY(check_ready(c, level));
+    if (key_index >= 0) return fail(c, PT_ERR_UNSUPPORTED, "keyframe scatter is not implemented");
+    bool aliased = false;
+    PatchPlanes work = writable_work(c, &aliased);
+    Params P = make_params(c, level);
+    LN(pt::launch_scatter(P, work, aliased ? 1 : 0, c->pass_counter++, c->stream));
+    return do_sync(c, level, 0);
+}
+
+pt_status pt_upsample(pt_ctx* c, int fine_level) {
+    if (!c) return PT_ERR_INVALID;
+    TRY(check_ready(c, fine_level));
+    bool aliased = false;
+    PatchPlanes old_base = base_planes(c);
+    PatchPlanes work = writable_work(c, &aliased);
+    Params P = make_params(c, fine_level);
+    float* res_out = c->res[1 - c->res_i];
+    LN(pt::launch_upsample(P, work, old_base, aliased ? 1 : 0, res_out, c->stream));
+    c->res_i = 1 - c->res_i;
+    c->base_i = c->work_i;  // copyWorkingToBase for offsets and residual
+    return PT_OK;
+}
+
+pt_status pt_advect_offsets(pt_ctx* c, int level, int time_step, int forwards, int flags) {
+    if (!c) return PT_ERR_INVALID;
+    TRY(check_ready(c, level));
+    if (flags & PT_ADVECT_CHECK_FRAME_TO_KEY)
+        return fail(c, PT_ERR_UNSUPPORTED, "frame-to-key ribbons are not implemented");
+    if (!c->img.rnd.p) return fail(c, PT_ERR_STATE, "no random level");
+    int d = forwards ? 0 : 1;
+    Params P = make_params(c, level);
+    LN(pt::launch_advect(P, d, forwards ? 1 : 0, time_step, flags, c->stream));
+    PatchPlanes dst = base_for_full_write(c);
+    P = make_params(c, level);
+    LN(pt::launch_copy_patch(P, dst, c->adv[d].off, c->stream));
+    TRY(do_sync(c, level, PT_DONT_COPY_OFFSETS | PT_DONT_UPDATE_RESIDUAL));
+    if (flags & PT_ADVECT_UPDATE_RESIDUAL) TRY(do_residual(c, level));
+    P = make_params(c, level);
+    LN(pt::launch_copy_float(P, c->adv[d].res, c->res[c->res_i], c->stream));
+    return PT_OK;
+}
+
+pt_status pt_merge_randomly(pt_ctx* c, int level, int forwards, float weight, int force_valid) {
+    if (!c) return PT_ERR_INVALID;
+    TRY(check_ready(c, level));
+    if (!c->img.rnd.p) return fail(c, PT_ERR_STATE, "no random level");
+    PatchPlanes work = writable_work(c, nullptr);
+    Params P = make_params(c, level);
+    LN(pt::launch_merge_random(P, forwards ? 0 : 1, forwards ? 1 : 0, weight, force_valid ? 1 : 0, work, c->stream));
+    return do_sync(c, level, 0);
+}
+
+pt_status pt_merge_using_residual(pt_ctx* c, int level, int forwards) {
+    if (!c) return PT_ERR_INVALID;
+    TRY(check_ready(c, level));
+    PatchPlanes work = writable_work(c, nullptr);
+    Params P = make_params(c, level);
+    LN(pt::launch_merge_residual(P, forwards ? 0 : 1, work, c->stream));
+    return do_sync(c, level, 0);
+}
+
+pt_status pt_update_residual_cache(pt_ctx* c, int level) {
+    if (!c) return PT_ERR_INVALID;
+    TRY(check_ready(c, level));
+    return do_residual(c, level);
+}
+
+pt_status pt_sync_buffers(pt_ctx* c, int level, int flags) {
+    if (!c) return PT_ERR_INVALID;
+    TRY(check_ready(c, level));
+    return do_sync(c, level, flags);
+}
+
+// --- state transfer ------------------------------------------------------------
+
+pt_status pt_load_offsets(pt_ctx* c, int level, const pt_patchxf* offs) {
+    if (!c || !offs) return PT_ERR_INVALID;
+    TRY(check_ready(c, level, false, false));
+    size_t n = (size_t)(c->W >> level) * (c->H >> level);
+    TRY(ensure_stage(c, n * sizeof(pt_patchxf)));
+    TRY(h2d(c, c->stage, offs, n * sizeof(pt_patchxf)));
+    PatchPlanes dst;
+    TRY(base_for_partial_write(c, &dst));
+    Params P = make_params(c, level);
+    LN(pt::launch_unpack_patch(P, (const pt_patchxf*)c->stage, dst, c->stream));
+    return PT_OK;
+}
+
+pt_status pt_load_residual(pt_ctx* c, int level, const float* res) {
+    if (!c || !res) return PT_ERR_INVALID;
+    TRY(check_ready(c, level, false, false));
+    size_t n = (size_t)(c->W >> level) * (c->H >> level);
+    TRY(ensure_stage(c, n * sizeof(float)));
+    TRY(h2d(c, c->stage, res, n * sizeof(float)));
+    Params P = make_params(c, level);
+    LN(pt::launch_load_residual(P, (const float*)c->stage, c->res[c->res_i], c->stream));
+    return PT_OK;
+}
+
+pt_status pt_get_offsets(pt_ctx* c, int level, pt_patchxf* out) {
+    if (!c || !out) return PT_ERR_INVALID;
+    TRY(check_ready(c, level, false, false));
+    size_t n = (size_t)(c->W >> level) * (c->H >> level);
+    TRY(ensure_stage(c, n * sizeof(pt_patchxf)));
+    Params P = make_params(c, level);
+    LN(pt::launch_pack_patch(P, base_planes(c), (pt_patchxf*)c->stage, c->stream));
+    CU(cudaMemcpyAsync(out, c->stage, n * sizeof(pt_patchxf), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return PT_OK;
+}
+
+static pt_status get_plane(pt_ctx* c, int level, const float* src, int ch, float* out) {
+    TRY(check_ready(c, level, false, false));
+    size_t n = (size_t)(c->W >> level) * (c->H >> level) * ch;
+    TRY(ensure_stage(c, n * sizeof(float)));
+    Params P = make_params(c, level);
+    LN(pt::launch_gather_level(P, src, ch, (float*)c->stage, c->stream));
+    CU(cudaMemcpyAsync(out, c->stage, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return PT_OK;
+}
+
+pt_status pt_get_residual(pt_ctx* c, int level, float* out) {
+    if (!c || !out) return PT_ERR_INVALID;
+    return get_plane(c, level, c->res[c->res_i], 1, out);
+}
+
+pt_status pt_get_output(pt_ctx* c, int level, float* out) {
+    if (!c || !out) return PT_ERR_INVALID;
+    return get_plane(c, level, (const float*)c->canvas, 4, out);
+}
+
+// --- resident pyramids ----------------------------------------------------------
+
+// builds the float pyramid of `ch` channels from a device level-0 array;
+// returns per-level device arrays (level 0 is `src` itself)
+static pt_status build_avg(pt_ctx* c, float* src, int w, int h, int ch, int vel, int nlev, std::vector<float*>& out) {
+    out.assign(nlev, nullptr);
+    out[0] = src;
+    for (int l = 1; l < nlev; l++) {
+        int pw = w >> (l - 1), ph = h >> (l - 1);
+        TRY(dalloc_t(c, &out[l], (size_t)(pw >> 1) * (ph >> 1) * ch));
+        LN(pt::launch_down_avg(out[l - 1], pw, ph, ch, vel, out[l], c->stream));
+    }
+    return PT_OK;
+}
+static pt_status build_vote(pt_ctx* c, int* src, int w, int h, int nlev, std::vector<int*>& out) {
+    out.assign(nlev, nullptr);
+    out[0] = src;
+    for (int l = 1; l < nlev; l++) {
+        int pw = w >> (l - 1), ph = h >> (l - 1);
+        TRY(dalloc_t(c, &out[l], (size_t)(pw >> 1) * (ph >> 1)));
+        LN(pt::launch_down_vote(out[l - 1], pw, ph, out[l], c->stream));
+    }
+    return PT_OK;
+}
+template <class T>
+static pt_status upload_or_fill(pt_ctx* c, T** dst, const void* src, size_t n, int ch, float fill) {
+    TRY(dalloc_t(c, dst, n * ch));
+    if (src) return h2d(c, *dst, src, n * ch * sizeof(T));
+    if (fill != 0.0f) {
+        std::vector<T> tmp(n * ch, (T)fill);
+        TRY(h2d(c, *dst, tmp.data(), n * ch * sizeof(T)));
+        CU(cudaStreamSynchronize(c->stream));
+    }
+    return PT_OK;
+}
+static pt_status orientation_pyramid(pt_ctx* c, const float* tensor, int w, int h, int nlev, std::vector<float*>& out) {
+    float* t0 = nullptr;
+    TRY(upload_or_fill(c, &t0, tensor, (size_t)w * h, 3, 0.0f));
+    std::vector<float*> tens;
+    TRY(build_avg(c, t0, w, h, 3, 0, nlev, tens));
+    out.assign(nlev, nullptr);
+    for (int l = 0; l < nlev; l++) {
+        int n = (w >> l) * (h >> l);
+        TRY(dalloc_t(c, &out[l], (size_t)n));
+        LN(pt::launch_tensor_angle(tens[l], n, out[l], c->stream));
+    }
+    CU(cudaStreamSynchronize(c->stream));
+    for (auto p : tens) dfree_t(c, p);
+    return PT_OK;
+}
+
+pt_status pt_set_style(pt_ctx* c, int style, int w, int h, const float* base, const float* output,
+                       const float* orient_tensor, const float* dist_trans, const int32_t* ids) {
+    if (!c || !base || !output) return PT_ERR_INVALID;
+    if (!c->initialized) return fail(c, PT_ERR_STATE, "pt_initialize has not been called");
+    if (style < 0 || style >= c->NS) return fail(c, PT_ERR_INVALID, "style %d out of range", style);
+    if (w != c->SW || h != c->SH)
+        return fail(c, PT_ERR_UNSUPPORTED, "style %dx%d differs from the initialized style size %dx%d", w, h, c->SW,
+                    c->SH);
+    int nlev = level_count(w, h);
+    if ((int)c->style_levels.size() != nlev) {
+        for (auto& L : c->style_levels) {
+            dfree_t(c, L.bo); dfree_t(c, L.orient); dfree_t(c, L.dt); dfree_t(c, L.ids);
+        }
+        c->style_levels.assign(nlev, ExLevel());
+        for (int l = 0; l < nlev; l++) {
+            ExLevel& L = c->style_levels[l];
+            L.w = w >> l;
+            L.h = h >> l;
+            size_t n = (size_t)L.w * L.h * c->NS;
+            TRY(dalloc_t(c, &L.bo, 2 * n));
+            TRY(dalloc_t(c, &L.orient, n));
+            TRY(dalloc_t(c, &L.dt, n));
+            TRY(dalloc_t(c, &L.ids, n));
+        }
+        c->style_set.assign(c->NS, 0);
+    }
+    size_t n0 = (size_t)w * h;
+    float *b0 = nullptr, *o0 = nullptr, *d0 = nullptr;
+    int* i0 = nullptr;
+    TRY(upload_or_fill(c, &b0, base, n0, 4, 0.f));
+    TRY(upload_or_fill(c, &o0, output, n0, 4, 0.f));
+    TRY(upload_or_fill(c, &d0, dist_trans, n0, 1, 0.f));
+    TRY(upload_or_fill(c, &i0, ids, n0, 1, 0.f));
+    std::vector<float*> pb, po, pd, por;
+    std::vector<int*> pi;
+    TRY(build_avg(c, b0, w, h, 4, 0, nlev, pb));
+    TRY(build_avg(c, o0, w, h, 4, 0, nlev, po));
+    TRY(build_avg(c, d0, w, h, 1, 0, nlev, pd));
+    TRY(build_vote(c, i0, w, h, nlev, pi));
+    TRY(orientation_pyramid(c, orient_tensor, w, h, nlev, por));
+    for (int l = 0; l < nlev; l++) {
+        ExLevel& L = c->style_levels[l];
+        size_t n = (size_t)L.w * L.h;
+        LN(pt::launch_interleave((const float4*)pb[l], (int)n, L.bo + 2 * n * style, 0, c->stream));
+        LN(pt::launch_interleave((const float4*)po[l], (int)n, L.bo + 2 * n * style, 1, c->stream));
+        CU(cudaMemcpyAsync(L.orient + n * style, por[l], n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+        CU(cudaMemcpyAsync(L.dt + n * style, pd[l], n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+        CU(cudaMemcpyAsync(L.ids + n * style, pi[l], n * sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
+        L.transparent = -1;
+    }
+    CU(cudaStreamSynchronize(c->stream));
+    for (int l = 0; l < nlev; l++) {
+        dfree_t(c, pb[l]); dfree_t(c, po[l]); dfree_t(c, pd[l]); dfree_t(c, pi[l]); dfree_t(c, por[l]);
+    }
+    c->style_set[style] = 1;
+    return PT_OK;
+}
+
+pt_status pt_set_frame(pt_ctx* c, int frame, int w, int h, const float* rgba, const float* orient_tensor,
+                       const float* dist_trans, const int32_t* ids, const float* vel_fwd, const float* vel_bwd,
+                       const float* scale) {
+    if (!c || !rgba) return PT_ERR_INVALID;
+    if (!c->initialized) return fail(c, PT_ERR_STATE, "pt_initialize has not been called");
+    if (w != c->W || h != c->H) return fail(c, PT_ERR_INVALID, "frame %dx%d differs from image size", w, h);
+    auto it = c->frames.find(frame);
+    if (it != c->frames.end()) {
+        for (auto& L : it->second) {
+            dfree_t(c, L.rgba); dfree_t(c, L.orient); dfree_t(c, L.dt); dfree_t(c, L.ids);
+            dfree_t(c, L.velf); dfree_t(c, L.velb); dfree_t(c, L.scale);
+        }
+        c->frames.erase(it);
+    }
+    int nlev = level_count(w, h);
+    size_t n0 = (size_t)w * h;
+    float *c0, *d0, *vf0, *vb0, *s0;
+    int* i0;
+    TRY(upload_or_fill(c, &c0, rgba, n0, 4, 0.f));
+    TRY(upload_or_fill(c, &d0, dist_trans, n0, 1, 0.f));
+    TRY(upload_or_fill(c, &i0, ids, n0, 1, 0.f));
+    TRY(upload_or_fill(c, &vf0, vel_fwd, n0, 2, 0.f));
+    TRY(upload_or_fill(c, &vb0, vel_bwd, n0, 2, 0.f));
+    TRY(upload_or_fill(c, &s0, scale, n0, 2, 1.f));
+    std::vector<float*> pc, pd, pvf, pvb, ps, por;
+    std::vector<int*> pi;
+    TRY(build_avg(c, c0, w, h, 4, 0, nlev, pc));
+    TRY(build_avg(c, d0, w, h, 1, 0, nlev, pd));
+    TRY(build_avg(c, vf0, w, h, 2, 1, nlev, pvf));
+    TRY(build_avg(c, vb0, w, h, 2, 1, nlev, pvb));
+    TRY(build_avg(c, s0, w, h, 2, 0, nlev, ps));
+    TRY(build_vote(c, i0, w, h, nlev, pi));
+    TRY(orientation_pyramid(c, orient_tensor, w, h, nlev, por));
+    std::vector<FrameLevel> lv(nlev);
+    for (int l = 0; l < nlev; l++) {
+        FrameLevel& L = lv[l];
+        L.w = w >> l;
+        L.h = h >> l;
+        L.rgba = (float4*)pc[l];
+        L.dt = pd[l];
+        L.velf = (float2*)pvf[l];
+        L.velb = (float2*)pvb[l];
+        L.scale = (float2*)ps[l];
+        L.ids = pi[l];
+        L.orient = por[l];
+    }
+    c->frames[frame] = std::move(lv);
+    return PT_OK;
+}
+
+pt_status pt_clear_frames(pt_ctx* c) {
+    if (!c) return PT_ERR_INVALID;
+    CU(cudaStreamSynchronize(c->stream));
+    free_frames(c);
+    return PT_OK;
+}
+
+// --- driver -------------------------------------------------------------------
+
+// Style::load(level), style.cpp:62-140 (a pointer switch to the resident level)
+static pt_status bind_style_level(pt_ctx* c, int level) {
+    if (level >= (int)c->style_levels.size()) return fail(c, PT_ERR_INVALID, "style pyramid too shallow");
+    for (int s = 0; s < c->NS; s++)
+        if (!c->style_set[s]) return fail(c, PT_ERR_STATE, "style %d not set", s);
+    c->ex = &c->style_levels[level];
+    return PT_OK;
+}
+
+// SynthesisFrame::loadImages + loadAnimImages, synthesisFrame.cpp:562-656
+static pt_status bind_frame_level(pt_ctx* c, int frame, int level) {
+    auto it = c->frames.find(frame);
+    if (it == c->frames.end()) return fail(c, PT_ERR_STATE, "frame %d not set", frame);
+    if (level >= (int)it->second.size()) return fail(c, PT_ERR_INVALID, "frame pyramid too shallow");
+    const FrameLevel& L = it->second[level];
+    int cur = c->img.cur;
+    c->img.base[cur] = Arr<float4>{L.rgba, L.w, L.h};
+    c->img.dt[cur] = Arr<float>{L.dt, L.w, L.h};
+    c->img.velf[cur] = Arr<float2>{L.velf, L.w, L.h};
+    c->img.velb[cur] = Arr<float2>{L.velb, L.w, L.h};
+    c->img.orient = Arr<float>{L.orient, L.w, L.h};
+    c->img.scale = Arr<float2>{L.scale, L.w, L.h};
+    c->img.ids = Arr<int>{L.ids, L.w, L.h};
+    return PT_OK;
+}
+
+static pt_status store_save(pt_ctx* c, int level, int frame, int pass, bool with_canvas) {
+    StoreEntry& e = c->store[std::make_tuple(level, frame, pass)];
+    int lw = c->W >> level, lh = c->H >> level;
+    size_t n = (size_t)lw * lh;
+    if (!e.offs || e.w != lw || e.h != lh) {
+        dfree_t(c, e.offs); dfree_t(c, e.res); dfree_t(c, e.canvas);
+        TRY(dalloc_t(c, &e.offs, n));
+        TRY(dalloc_t(c, &e.res, n));
+        e.w = lw;
+        e.h = lh;
+    }
+    Params P = make_params(c, level);
+    LN(pt::launch_pack_patch(P, base_planes(c), e.offs, c->stream));
+    LN(pt::launch_gather_level(P, c->res[c->res_i], 1, e.res, c->stream));
+    if (with_canvas) {
+        if (!e.canvas) TRY(dalloc_t(c, &e.canvas, n));
+        LN(pt::launch_gather_level(P, (const float*)c->canvas, 4, (float*)e.canvas, c->stream));
+    }
+    return PT_OK;
+}
+
+static pt_status store_load_offsets(pt_ctx* c, int level, int frame, int pass) {
+    auto it = c->store.find(std::make_tuple(level, frame, pass));
+    if (it == c->store.end()) return fail(c, PT_ERR_STATE, "no saved offsets for level %d frame %d pass %d", level, frame, pass);
+    PatchPlanes dst;
+    TRY(base_for_partial_write(c, &dst));
+    Params P = make_params(c, level);
+    LN(pt::launch_unpack_patch(P, it->second.offs, dst, c->stream));
+    return PT_OK;
+}
+static pt_status store_load_residual(pt_ctx* c, int level, int frame, int pass) {
+    auto it = c->store.find(std::make_tuple(level, frame, pass));
+    if (it == c->store.end()) return fail(c, PT_ERR_STATE, "no saved residual");
+    Params P = make_params(c, level);
+    LN(pt::launch_load_residual(P, it->second.res, c->res[c->res_i], c->stream));
+    return PT_OK;
+}
+
+// SynthesisFrame::propagateAndScatter, synthesisFrame.cpp:483-508
+static pt_status propagate_and_scatter(pt_ctx* c, int level, int iterations) {
+    for (int itr = 0; itr < iterations; itr++) {
+        for (int j = 128; j > 1; j /= 2) TRY(pt_propagate(c, level, j, -1));
+        TRY(pt_propagate(c, level, 1, -1));
+        TRY(pt_propagate(c, level, 1, -1));
+        if (itr < iterations - 1) TRY(pt_scatter(c, level, -1));
+    }
+    return PT_OK;
+}
+
+// SynthesisFrame::synthesizeConsecutive, synthesisFrame.cpp:214-323
+static pt_status synthesize_consecutive(pt_ctx* c, const pt_params& user, int frame, int level, int pass,
+                                        bool is_first, bool forwards, int source_pass, bool first_pass,
+                                        bool save_canvas) {
+    pt_params p = user;  // SynthesisFrame::updateParameters, :522-542
+    p.advectionJitter = (frame % 3 == 0) ? user.advectionJitter * 0.01f : 0.0f;
+    p.direction = forwards ? PT_FORWARD : PT_BACKWARD;
+    TRY(pt_set_params(c, &p));
+    bool rm = user.scheme == PT_S_FMBM_RM;
+    int ops = rm ? 0 : PT_ADVECT_UPDATE_RESIDUAL;
+    bool coarsest = level == user.levels - 1;
+    if (first_pass) {
+        TRY(pt_create_random_level(c, level, frame));
+        if (is_first) {
+            if (coarsest) {
+                TRY(pt_randomize_offsets(c, level));
+            } else {
+                TRY(store_load_offsets(c, level + 1, frame, source_pass));
+                TRY(pt_upsample(c, level));
+                TRY(do_sync(c, level, 0));
+            }
+        }
+        if (!is_first && coarsest) {
+            TRY(pt_advect_offsets(c, level, 1, forwards, ops));
+            c->work_i = c->base_i;  // copyBaseToWorking
+        } else if (!is_first) {
+            TRY(pt_advect_offsets(c, level, 1, forwards, ops | PT_ADVECT_IGNORE_RANDOM));
+            TRY(store_load_offsets(c, level + 1, frame, source_pass));
+            TRY(store_load_residual(c, level + 1, frame, source_pass));
+            TRY(pt_upsample(c, level));
+            TRY(do_sync(c, level, 0));
+            if (rm) TRY(pt_merge_randomly(c, level, forwards, 0.5f, 0));
+            else TRY(pt_merge_using_residual(c, level, forwards));
+        }
+    } else {
+        TRY(pt_advect_offsets(c, level, 1, forwards, ops | PT_ADVECT_IGNORE_RANDOM));
+        TRY(store_load_offsets(c, level, frame, pass - 1));
+        TRY(store_load_residual(c, level, frame, pass - 1));
+        TRY(do_sync(c, level, PT_DONT_COPY_OFFSETS | PT_DONT_UPDATE_RESIDUAL));
+        if (rm) TRY(pt_merge_randomly(c, level, forwards, 0.5f, 0));
+        else TRY(pt_merge_using_residual(c, level, forwards));
+    }
+    TRY(do_sync(c, level, 0));
+    TRY(propagate_and_scatter(c, level, user.iterations));
+    return store_save(c, level, frame, pass, save_canvas);
+}
+
+// SynthesisProcessor::renderAnimationFMBM + renderConsecutivePass,
+// synthesisProcessor.cpp:703-753,846-878
+static pt_status render_fmbm(pt_ctx* c, int first, int last) {
+    const pt_params user = c->params;
+    if (user.scheme != PT_S_FMBM && user.scheme != PT_S_FMBM_RM)
+        return fail(c, PT_ERR_UNSUPPORTED, "only the FMBM schemes are implemented");
+    if (user.levels < 1 || user.finalLevel < 0 || user.finalLevel >= user.levels)
+        return fail(c, PT_ERR_INVALID, "bad levels/finalLevel");
+    for (int f = first; f <= last; f++)
+        if (!c->frames.count(f)) return fail(c, PT_ERR_STATE, "frame %d not set", f);
+    TRY(reset_working(c));
+    c->img.cur = 0;
+    free_store(c);
+    const int total = user.fixupPasses + 1;
+    const int final_pass = (user.finalLevel == 0) ? total - 1 : 0;
+    for (int level = user.levels - 1; level >= user.finalLevel; level--) {
+        TRY(bind_style_level(c, level));
+        TRY(pt_reset_advected_buffers(c));
+        for (int pass = 0; pass < total; pass++) {
+            bool forwards = (pass % 2) == 0;
+            std::vector<int> fr;
+            if (forwards) for (int f = first; f <= last; f++) fr.push_back(f);
+            else for (int f = last; f >= first; f--) fr.push_back(f);
+            bool save_canvas = (level == user.finalLevel && pass == final_pass);
+            if (pass > 0) {
+                TRY(store_save(c, level, fr[0], pass, save_canvas));
+                fr.erase(fr.begin());
+            }
+            for (size_t i = 0; i < fr.size(); i++) {
+                bool is_first = (i == 0) && (pass == 0);
+                if (!is_first) TRY(pt_flip_anim_buffers(c));
+                TRY(bind_frame_level(c, fr[i], level));
+                TRY(synthesize_consecutive(c, user, fr[i], level, pass, is_first, forwards, total - 1, pass == 0,
+                                           save_canvas));
+            }
+        }
+        // the coarser level's saved state is no longer needed
+        if (level + 1 < user.levels) {
+            for (auto it = c->store.begin(); it != c->store.end();) {
+                if (std::get<0>(it->first) == level + 1) {
+                    dfree_t(c, it->second.offs); dfree_t(c, it->second.res); dfree_t(c, it->second.canvas);
+                    it = c->store.erase(it);
+                } else {
+                    ++it;
+                }
+            }
+        }
+    }
+    c->params = user;
+    return PT_OK;
+}
+
+static pt_status fetch_final(pt_ctx* c, int frame, float* out_rgba, pt_patchxf* out_offsets) {
+    const int total = c->params.fixupPasses + 1;
+    const int final_pass = (c->params.finalLevel == 0) ? total - 1 : 0;
+    auto it = c->store.find(std::make_tuple(c->params.finalLevel, frame, final_pass));
+    if (it == c->store.end()) return fail(c, PT_ERR_STATE, "no final output for frame %d", frame);
+    size_t n = (size_t)it->second.w * it->second.h;
+    if (out_rgba)
+        CU(cudaMemcpyAsync(out_rgba, it->second.canvas, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
+    if (out_offsets)
+        CU(cudaMemcpyAsync(out_offsets, it->second.offs, n * sizeof(pt_patchxf), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return PT_OK;
+}
+
+pt_status pt_synthesize_frame(pt_ctx* c, int frame, float* out_rgba, pt_patchxf* out_offsets) {
+    if (!c) return PT_ERR_INVALID;
+    if (!c->initialized || !c->have_params) return fail(c, PT_ERR_STATE, "context not initialized");
+    CU(cudaSetDevice(c->device));
+    TRY(render_fmbm(c, frame, frame));
+    return fetch_final(c, frame, out_rgba, out_offsets);
+}
+
+pt_status pt_synthesize_animation(pt_ctx* c, int first, int last, pt_frame_callback cb, void* user) {
+    if (!c || last < first) return PT_ERR_INVALID;
+    if (!c->initialized || !c->have_params) return fail(c, PT_ERR_STATE, "context not initialized");
+    CU(cudaSetDevice(c->device));
+    TRY(render_fmbm(c, first, last));
+    if (cb) {
+        int lw = c->W >> c->params.finalLevel, lh = c->H >> c->params.finalLevel;
+        std::vector<float> rgba((size_t)lw * lh * 4);
+        std::vector<pt_patchxf> offs((size_t)lw * lh);
+        for (int f = first; f <= last; f++) {
+            TRY(fetch_final(c, f, rgba.data(), offs.data()));
+            cb(f, rgba.data(), offs.data(), lw, lh, user);
+        }
+    }
+    return PT_OK;
+}

@@ -1,0 +1,303 @@
+// pt_device.cuh -- device-side data views and arithmetic for the offset-field
+// synthesis kernels (sm_103a).
+//
+// Arithmetic contract.  All kernels are compiled with -fmad=false, so no
+// multiply-add is fused unless written as fmaf(); the places that use fmaf()
+// and the operation order of every sum are fixed, which makes the results
+// reproducible on any IEEE FP32 machine.  Bilinear sampling uses exact FP32
+// weights (the reference samples through the texture unit, whose 1.8
+// fixed-point weights are a property of the hardware), sin/cos/atan2/log/acos
+// come from the polynomial routines below, and double precision is used
+// exactly where the reference's C++ promotes to double.
+#pragma once
+
+#include <cstdint>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "painttween.h"
+#include "pt_types.h"
+
+namespace ptk {
+
+constexpr float kAlphaThreshold = 0.99f;  // types.h:39
+constexpr float kEpsilon = 0.000001f;     // types.h:38
+constexpr float kBigResidual = (float)10e30;
+
+// ---------------------------------------------------------------------------
+// polynomial elementary functions
+// ---------------------------------------------------------------------------
+
+// k = rint(t*2/pi); r = t - k*pi/2 (two-term Cody-Waite, fused);
+// Taylor series of sin to r^9 and cos to r^10 on |r| <= pi/4.
+__device__ __forceinline__ void sincos_poly(float t, float* s, float* c) {
+    const float two_over_pi = 0x1.45f306p-1f;
+    const float pio2_hi = 0x1.921fb6p+0f;
+    const float pio2_lo = -0x1.777a5cp-25f;
+    float k = rintf(t * two_over_pi);
+    float r = fmaf(-k, pio2_hi, t);
+    r = fmaf(-k, pio2_lo, r);
+    float r2 = r * r;
+    float ps = fmaf(r2, (float)(1.0 / 362880.0), (float)(-1.0 / 5040.0));
+    ps = fmaf(r2, ps, (float)(1.0 / 120.0));
+    ps = fmaf(r2, ps, (float)(-1.0 / 6.0));
+    ps = ps * r2;
+    float sr = fmaf(r, ps, r);
+    float pc = fmaf(r2, (float)(-1.0 / 3628800.0), (float)(1.0 / 40320.0));
+    pc = fmaf(r2, pc, (float)(-1.0 / 720.0));
+    pc = fmaf(r2, pc, (float)(1.0 / 24.0));
+    pc = fmaf(r2, pc, -0.5f);
+    float cr = fmaf(r2, pc, 1.0f);
+    int q = ((int)k) & 3;  // cvt.rzi saturates, NaN -> 0
+    if (q == 0) { *s = sr; *c = cr; }
+    else if (q == 1) { *s = cr; *c = -sr; }
+    else if (q == 2) { *s = -sr; *c = -cr; }
+    else { *s = -cr; *c = sr; }
+}
+
+// atan on [0,1]: atan(u) = pi/4 + atan((u-1)/(u+1)) above tan(pi/8);
+// Taylor series to v^19.
+__device__ __forceinline__ float atan01_poly(float u) {
+    float off = 0.0f;
+    float v = u;
+    if (u > 0x1.a8279ap-2f) {
+        v = (u - 1.0f) / (u + 1.0f);
+        off = 0x1.921fb6p-1f;
+    }
+    float v2 = v * v;
+    float p = (float)(-1.0 / 19.0);
+    p = fmaf(v2, p, (float)(1.0 / 17.0));
+    p = fmaf(v2, p, (float)(-1.0 / 15.0));
+    p = fmaf(v2, p, (float)(1.0 / 13.0));
+    p = fmaf(v2, p, (float)(-1.0 / 11.0));
+    p = fmaf(v2, p, (float)(1.0 / 9.0));
+    p = fmaf(v2, p, (float)(-1.0 / 7.0));
+    p = fmaf(v2, p, (float)(1.0 / 5.0));
+    p = fmaf(v2, p, (float)(-1.0 / 3.0));
+    p = p * v2;
+    return off + fmaf(v, p, v);
+}
+
+__device__ __forceinline__ float atan2_poly(float y, float x) {
+    const float pi = 0x1.921fb6p+1f;
+    const float pio2 = 0x1.921fb6p+0f;
+    float ax = fabsf(x), ay = fabsf(y);
+    if (ax == 0.0f && ay == 0.0f) {
+        float r = signbit(x) ? pi : 0.0f;
+        return signbit(y) ? -r : r;
+    }
+    float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+    float a = atan01_poly(mn / mx);
+    if (ay > ax) a = pio2 - a;
+    if (signbit(x)) a = pi - a;
+    return signbit(y) ? -a : a;
+}
+
+// log(x) = e ln2 + 2 atanh((m-1)/(m+1)), m in [sqrt(1/2), sqrt(2)).
+__device__ __forceinline__ float log_poly(float x) {
+    if (!(x > 0.0f)) return (x == 0.0f) ? -INFINITY : NAN;
+    if (isinf(x)) return x;
+    int e;
+    float m = frexpf(x, &e);
+    if (m < 0x1.6a09e6p-1f) { m = m * 2.0f; e -= 1; }
+    float s = (m - 1.0f) / (m + 1.0f);
+    float s2 = s * s;
+    float p = (float)(1.0 / 11.0);
+    p = fmaf(s2, p, (float)(1.0 / 9.0));
+    p = fmaf(s2, p, (float)(1.0 / 7.0));
+    p = fmaf(s2, p, (float)(1.0 / 5.0));
+    p = fmaf(s2, p, (float)(1.0 / 3.0));
+    p = p * s2;
+    float lm = 2.0f * fmaf(s, p, s);
+    float fe = (float)e;
+    return fmaf(fe, 0x1.62e430p-1f, fmaf(fe, -0x1.05c610p-29f, lm));
+}
+
+// asin on [0, 1/2], Taylor series with 12 terms.
+__device__ __forceinline__ float asin_small_poly(float x) {
+    const double c[12] = {
+        1.0 / 6.0, 3.0 / 40.0, 15.0 / 336.0, 105.0 / 3456.0, 945.0 / 42240.0,
+        10395.0 / 599040.0, 135135.0 / 9676800.0, 2027025.0 / 175472640.0,
+        34459425.0 / 3530096640.0, 654729075.0 / 78033715200.0,
+        13749310575.0 / 1880240947200.0, 316234143225.0 / 49049763430400.0};
+    float z = x * x;
+    float p = (float)c[11];
+#pragma unroll
+    for (int i = 10; i >= 0; --i) p = fmaf(z, p, (float)c[i]);
+    p = p * z;
+    return fmaf(x, p, x);
+}
+
+__device__ __forceinline__ float acos_poly(float x) {
+    const float pi = 0x1.921fb6p+1f;
+    const float pio2 = 0x1.921fb6p+0f;
+    if (!(fabsf(x) <= 1.0f)) return NAN;
+    if (fabsf(x) <= 0.5f) return pio2 - asin_small_poly(x);
+    float t = sqrtf((1.0f - fabsf(x)) * 0.5f);
+    float a = 2.0f * asin_small_poly(t);
+    return (x > 0.0f) ? a : pi - a;
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+__device__ __forceinline__ float4 f4(float x, float y, float z, float w) { return make_float4(x, y, z, w); }
+
+// ---------------------------------------------------------------------------
+// data views
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ Patch load_patch(const PatchPlanes& p, size_t k) {
+    float4 a = __ldg(p.A + k);
+    float4 b = __ldg(p.B + k);
+    Patch r;
+    r.x = a.x; r.y = a.y; r.theta = a.z; r.layer = __float_as_int(a.w);
+    r.hyst = b.x; r.su = b.y; r.sv = b.z; r.lumy = b.w;
+    r.luma = __ldg(p.C + k);
+    return r;
+}
+__device__ __forceinline__ void store_patch(const PatchPlanes& p, size_t k, const Patch& v) {
+    p.A[k] = f4(v.x, v.y, v.theta, __int_as_float(v.layer));
+    p.B[k] = f4(v.hyst, v.su, v.sv, v.lumy);
+    p.C[k] = v.luma;
+}
+__device__ __forceinline__ Patch make_patch(float x, float y, float th, float h, int layer, float su, float sv) {
+    Patch p;
+    p.x = x; p.y = y; p.theta = th; p.hyst = h; p.layer = layer;
+    p.su = su; p.sv = sv; p.lumy = 0.f; p.luma = 0.f;
+    return p;
+}
+
+// --- fetches ----------------------------------------------------------------
+
+template <class T>
+__device__ __forceinline__ T zero_of();
+template <> __device__ __forceinline__ float zero_of<float>() { return 0.0f; }
+template <> __device__ __forceinline__ float2 zero_of<float2>() { return make_float2(0.f, 0.f); }
+template <> __device__ __forceinline__ float4 zero_of<float4>() { return make_float4(0.f, 0.f, 0.f, 0.f); }
+
+// layered image array texel at integer (x, y)
+template <class T>
+__device__ __forceinline__ T lay_texel(const Arr<T>& a, const Params& P, int x, int y) {
+    x = clampi(x, 0, P.W - 1);
+    y = clampi(y, 0, P.H - 1);
+    if (x >= a.w || y >= a.h) return zero_of<T>();
+    return __ldg(a.p + (size_t)y * a.w + x);
+}
+// level-size array texel at integer (x, y), clamp addressing
+template <class T>
+__device__ __forceinline__ T lvl_texel(const Arr<T>& a, int x, int y) {
+    x = clampi(x, 0, a.w - 1);
+    y = clampi(y, 0, a.h - 1);
+    return __ldg(a.p + (size_t)y * a.w + x);
+}
+
+// point-filtered index at unnormalised u (+0.5), clamp to [0, n-1]
+__device__ __forceinline__ int point_index(float u, int n) {
+    float f = floorf(u + 0.5f);
+    f = fminf(fmaxf(f, -1.0f), (float)n);
+    return clampi((int)f, 0, n - 1);
+}
+
+struct Bl {
+    int x0, x1, y0, y1;
+    float w00, w10, w01, w11;
+};
+__device__ __forceinline__ Bl bl_setup(float u, float v, int n, int m) {
+    Bl b;
+    float xs = u + 0.5f, ys = v + 0.5f;
+    float xb = xs - 0.5f, yb = ys - 0.5f;
+    float fx = floorf(xb), fy = floorf(yb);
+    float a = xb - fx, c = yb - fy;
+    fx = fminf(fmaxf(fx, -1.0f), (float)n);
+    fy = fminf(fmaxf(fy, -1.0f), (float)m);
+    int ix = (int)fx, iy = (int)fy;
+    b.x0 = clampi(ix, 0, n - 1); b.x1 = clampi(ix + 1, 0, n - 1);
+    b.y0 = clampi(iy, 0, m - 1); b.y1 = clampi(iy + 1, 0, m - 1);
+    float oa = 1.0f - a, oc = 1.0f - c;
+    b.w00 = oa * oc; b.w10 = a * oc; b.w01 = oa * c; b.w11 = a * c;
+    return b;
+}
+__device__ __forceinline__ float bl1(const Bl& b, float t00, float t10, float t01, float t11) {
+    float r = t00 * b.w00;
+    r = fmaf(t10, b.w10, r);
+    r = fmaf(t01, b.w01, r);
+    r = fmaf(t11, b.w11, r);
+    return r;
+}
+__device__ __forceinline__ float4 bl4(const Bl& b, float4 a, float4 c, float4 d, float4 e) {
+    return f4(bl1(b, a.x, c.x, d.x, e.x), bl1(b, a.y, c.y, d.y, e.y),
+              bl1(b, a.z, c.z, d.z, e.z), bl1(b, a.w, c.w, d.w, e.w));
+}
+
+__device__ __forceinline__ int ex_layer(const ExView& e, int layer) { return clampi(layer, 0, e.ns - 1); }
+
+// exemplar base and output at unnormalised (u, v), one footprint
+__device__ __forceinline__ void ex_sample2(const ExView& e, float u, float v, int layer, float4* base, float4* out) {
+    Bl b = bl_setup(u, v, e.w, e.h);
+    const float4* L = e.bo + (size_t)ex_layer(e, layer) * e.w * e.h * 2;
+    const float4* r0 = L + (size_t)b.y0 * e.w * 2;
+    const float4* r1 = L + (size_t)b.y1 * e.w * 2;
+    float4 b00 = __ldg(r0 + 2 * b.x0), o00 = __ldg(r0 + 2 * b.x0 + 1);
+    float4 b10 = __ldg(r0 + 2 * b.x1), o10 = __ldg(r0 + 2 * b.x1 + 1);
+    float4 b01 = __ldg(r1 + 2 * b.x0), o01 = __ldg(r1 + 2 * b.x0 + 1);
+    float4 b11 = __ldg(r1 + 2 * b.x1), o11 = __ldg(r1 + 2 * b.x1 + 1);
+    *base = bl4(b, b00, b10, b01, b11);
+    *out = bl4(b, o00, o10, o01, o11);
+}
+__device__ __forceinline__ float4 ex_sample_out(const ExView& e, float u, float v, int layer) {
+    Bl b = bl_setup(u, v, e.w, e.h);
+    const float4* L = e.bo + (size_t)ex_layer(e, layer) * e.w * e.h * 2;
+    const float4* r0 = L + (size_t)b.y0 * e.w * 2;
+    const float4* r1 = L + (size_t)b.y1 * e.w * 2;
+    return bl4(b, __ldg(r0 + 2 * b.x0 + 1), __ldg(r0 + 2 * b.x1 + 1),
+               __ldg(r1 + 2 * b.x0 + 1), __ldg(r1 + 2 * b.x1 + 1));
+}
+__device__ __forceinline__ float ex_sample_out_alpha(const ExView& e, float u, float v, int layer) {
+    Bl b = bl_setup(u, v, e.w, e.h);
+    const float* L = (const float*)(e.bo + (size_t)ex_layer(e, layer) * e.w * e.h * 2);
+    const float* r0 = L + (size_t)b.y0 * e.w * 8;
+    const float* r1 = L + (size_t)b.y1 * e.w * 8;
+    return bl1(b, __ldg(r0 + 8 * b.x0 + 7), __ldg(r0 + 8 * b.x1 + 7),
+               __ldg(r1 + 8 * b.x0 + 7), __ldg(r1 + 8 * b.x1 + 7));
+}
+__device__ __forceinline__ float ex_sample_dt(const ExView& e, float u, float v, int layer) {
+    Bl b = bl_setup(u, v, e.w, e.h);
+    const float* D = e.dt + (size_t)ex_layer(e, layer) * e.w * e.h;
+    return bl1(b, __ldg(D + (size_t)b.y0 * e.w + b.x0), __ldg(D + (size_t)b.y0 * e.w + b.x1),
+               __ldg(D + (size_t)b.y1 * e.w + b.x0), __ldg(D + (size_t)b.y1 * e.w + b.x1));
+}
+__device__ __forceinline__ float ex_texel_dt(const ExView& e, int x, int y, int layer) {
+    x = clampi(x, 0, e.w - 1); y = clampi(y, 0, e.h - 1);
+    return __ldg(e.dt + (size_t)ex_layer(e, layer) * e.w * e.h + (size_t)y * e.w + x);
+}
+__device__ __forceinline__ float ex_point_orient(const ExView& e, float u, float v, int layer) {
+    int x = point_index(u, e.w), y = point_index(v, e.h);
+    return __ldg(e.orient + (size_t)ex_layer(e, layer) * e.w * e.h + (size_t)y * e.w + x);
+}
+__device__ __forceinline__ int ex_point_id(const ExView& e, float u, float v, int layer) {
+    int x = point_index(u, e.w), y = point_index(v, e.h);
+    return __ldg(e.ids + (size_t)ex_layer(e, layer) * e.w * e.h + (size_t)y * e.w + x);
+}
+
+// layered image array bilinear at unnormalised (u, v): clamp at level-0 size,
+// zero outside the level rectangle
+template <class T>
+__device__ __forceinline__ T lay_bilinear(const Arr<T>& a, const Params& P, float u, float v);
+template <>
+__device__ __forceinline__ float2 lay_bilinear<float2>(const Arr<float2>& a, const Params& P, float u, float v) {
+    Bl b = bl_setup(u, v, P.W, P.H);
+    float2 t00 = lay_texel(a, P, b.x0, b.y0), t10 = lay_texel(a, P, b.x1, b.y0);
+    float2 t01 = lay_texel(a, P, b.x0, b.y1), t11 = lay_texel(a, P, b.x1, b.y1);
+    return make_float2(bl1(b, t00.x, t10.x, t01.x, t11.x), bl1(b, t00.y, t10.y, t01.y, t11.y));
+}
+template <>
+__device__ __forceinline__ float4 lay_bilinear<float4>(const Arr<float4>& a, const Params& P, float u, float v) {
+    Bl b = bl_setup(u, v, P.W, P.H);
+    return bl4(b, lay_texel(a, P, b.x0, b.y0), lay_texel(a, P, b.x1, b.y0),
+               lay_texel(a, P, b.x0, b.y1), lay_texel(a, P, b.x1, b.y1));
+}
+
+__device__ __forceinline__ bool in_rect(const Params& P, int x, int y, int border = 0) {
+    return x >= border && y >= border && x < P.lw - border && y < P.lh - border;
+}
+
+}  // namespace ptk

@@ -1,0 +1,43 @@
+// pt_internal.h -- launchers shared by the kernel and host translation units.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "pt_types.h"
+
+namespace pt {
+using ptk::Arr;
+using ptk::ConvKernel;
+using ptk::ExView;
+using ptk::Params;
+using ptk::PatchPlanes;
+
+cudaError_t launch_propagate(const Params& P, PatchPlanes work, int jump, cudaStream_t s);
+cudaError_t launch_scatter(const Params& P, PatchPlanes work, int write_all, uint32_t pass_id, cudaStream_t s);
+cudaError_t launch_residual(const Params& P, float* out, cudaStream_t s);
+cudaError_t launch_canvas(const Params& P, float4* canvas, cudaStream_t s);
+cudaError_t launch_random_offsets(const Params& P, PatchPlanes work, cudaStream_t s);
+cudaError_t launch_upsample(const Params& P, PatchPlanes work, PatchPlanes border_src, int copy_border,
+                            float* res_out, cudaStream_t s);
+cudaError_t launch_advect(const Params& P, int d, int forwards, int time_step, int flags, cudaStream_t s);
+cudaError_t launch_merge_random(const Params& P, int d, int forwards, float weight, int force, PatchPlanes work,
+                                cudaStream_t s);
+cudaError_t launch_merge_residual(const Params& P, int d, PatchPlanes work, cudaStream_t s);
+cudaError_t launch_conv(const float* src, float* dst, int w, int h, int pitch, int rows, const ConvKernel& kw,
+                        cudaStream_t s);
+cudaError_t launch_copy_patch(const Params& P, PatchPlanes dst, PatchPlanes src, cudaStream_t s);
+cudaError_t launch_copy_float(const Params& P, float* dst, const float* src, cudaStream_t s);
+cudaError_t launch_unpack_patch(const Params& P, const pt_patchxf* src, PatchPlanes dst, cudaStream_t s);
+cudaError_t launch_pack_patch(const Params& P, PatchPlanes src, pt_patchxf* dst, cudaStream_t s);
+cudaError_t launch_load_residual(const Params& P, const float* src, float* dst, cudaStream_t s);
+cudaError_t launch_gather_level(const Params& P, const float* src, int ch, float* dst, cudaStream_t s);
+cudaError_t launch_down_avg(const float* src, int w, int h, int ch, int vel, float* dst, cudaStream_t s);
+cudaError_t launch_down_vote(const int* src, int w, int h, int* dst, cudaStream_t s);
+cudaError_t launch_tensor_angle(const float* t3, int n, float* out, cudaStream_t s);
+cudaError_t launch_interleave(const float4* src, int n, float4* bo, int which, cudaStream_t s);
+cudaError_t launch_random_level(int mode, int w, int h, int mx, int my, int transparencyOk, int orientationEnabled,
+                                Arr<float4> img, Arr<float> iorient, ExView ex, float4* out,
+                                const uint32_t* states, uint32_t seed, cudaStream_t s);
+cudaError_t launch_any_transparent(const float4* bo, size_t n, int* flag, cudaStream_t s);
+}  // namespace pt

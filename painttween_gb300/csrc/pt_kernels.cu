@@ -1,0 +1,893 @@
+// pt_kernels.cu -- sm_103a kernels of the offset-field synthesis.
+//
+// Each kernel restates one kernel of the reference
+// (src/PaintTweenCUDA/texSynth_kernel.cu, convolution.cu) or one host-side
+// pyramid step (downsample.cpp, synthesisFrame.cpp:66-150) with the same
+// per-pixel semantics, over the buffer model described in pt_device.cuh.
+#include "pt_device.cuh"
+#include "pt_internal.h"
+
+namespace ptk {
+
+// ---------------------------------------------------------------------------
+// energy (calculateResidual and its terms, texSynth_kernel.cu:377-721)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ bool image_culled(const Params& P, int x, int y) {
+    // isImagePixelCulled, :176-186
+    return lay_texel(P.img.dt[P.img.cur], P, x, y) > (float)P.distTransCull;
+}
+
+// screenToExemplarAngle, :425-436
+__device__ __forceinline__ float screen_to_exemplar_angle(const Params& P, int x, int y, float ex, float ey,
+                                                          int layer) {
+    if (P.orientationEnabled) {
+        float theta = ex_point_orient(P.ex, ex, ey, layer) - lvl_texel(P.img.orient, x, y);
+        if ((double)theta > 1.57079632679489661923) return (float)((double)theta - 3.14159265358979323846);
+        if ((double)theta < -1.57079632679489661923) return (float)(3.14159265358979323846 + (double)theta);
+        return theta;
+    }
+    return 0.0f;
+}
+
+// screenToExemplarBasis, texSynth_util.h:95-104
+__device__ __forceinline__ void basis(float angle, float su, float sv, float2* b0, float2* b1) {
+    float s, c;
+    sincos_poly(angle, &s, &c);
+    b1->x = -s * sv;
+    b1->y = c * sv;
+    b0->x = c * su;
+    b0->y = s * su;
+}
+
+// calculateNewExemplarCoord, texSynth_util.h:106-118
+__device__ __forceinline__ void new_coord(float i, float j, float ex, float ey, float2 b0, float2 b1, float* ox,
+                                          float* oy) {
+    *ox = ex + fmaf(i, b0.x, j * b1.x);
+    *oy = ey + fmaf(i, b0.y, j * b1.y);
+}
+
+// clampToExemplar(float*), texSynth_util.h:50-57
+__device__ __forceinline__ void clamp_to_exemplar(float* x, float* y, int w, int h) {
+    if (*x < 0) *x = 0;
+    if (*y < 0) *y = 0;
+    if (*x >= w) *x = (float)(w - 1);
+    if (*y >= h) *y = (float)(h - 1);
+}
+
+__device__ __forceinline__ float ssd_a(float4 a, float4 b, float alpha) {
+    float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z, dw = a.w - b.w;
+    float s = dx * dx;
+    s = fmaf(dy, dy, s);
+    s = fmaf(dz, dz, s);
+    s = fmaf(alpha * dw, dw, s);
+    return s;
+}
+__device__ __forceinline__ float ssd(float4 a, float4 b) {
+    float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z, dw = a.w - b.w;
+    float s = dx * dx;
+    s = fmaf(dy, dy, s);
+    s = fmaf(dz, dz, s);
+    s = fmaf(dw, dw, s);
+    return s;
+}
+__device__ __forceinline__ float4 sub4(float4 a, float4 b) { return f4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
+
+struct PixCtx {
+    bool validF, validB, temporalF, temporalB;
+    Patch prevF, prevB;
+    float2 fb0, fb1, bb0, bb1;
+    float hyst;
+};
+
+// hysteresisTerm, :506-535
+__device__ float hysteresis_term(const Params& P, int x, int y) {
+    float maxD = P.maxDistortion / ldexpf(1.0f, P.level);
+    const Arr<float2>& v = (P.direction == PT_FORWARD) ? P.img.velb[P.img.cur] : P.img.velf[P.img.cur];
+    float2 d00 = lay_texel(v, P, x, y), d10 = lay_texel(v, P, x + 1, y);
+    float2 d01 = lay_texel(v, P, x, y + 1), d11 = lay_texel(v, P, x + 1, y + 1);
+    float maxX = fmaxf(d00.x, fmaxf(d01.x, fmaxf(d10.x, d11.x)));
+    float maxY = fmaxf(d00.y, fmaxf(d01.y, fmaxf(d10.y, d11.y)));
+    float minX = fminf(d00.x, fminf(d01.x, fminf(d10.x, d11.x)));
+    float minY = fminf(d00.y, fminf(d01.y, fminf(d10.y, d11.y)));
+    if ((maxX - minX) < maxD && (maxY - minY) < maxD) return P.hysteresisWeight;
+    return 0.0f;
+}
+
+__device__ void make_pixctx(const Params& P, int x, int y, PixCtx* pc) {
+    size_t k = (size_t)y * P.W + x;
+    pc->prevF = load_patch(P.adv[0].off, k);
+    pc->prevB = load_patch(P.adv[1].off, k);
+    pc->validF = pc->prevF.hyst > 0;
+    pc->validB = pc->prevB.hyst > 0;
+    bool td = (P.tdIn > 0.f || P.tdOut > 0.f || P.tc > 0.f);
+    pc->temporalF = (P.direction == PT_FORWARD || P.direction == PT_BIDIRECTIONAL) && pc->validF && td;
+    pc->temporalB = (P.direction == PT_BACKWARD || P.direction == PT_BIDIRECTIONAL) && pc->validB && td;
+    if (pc->temporalF) {
+        float a = screen_to_exemplar_angle(P, x, y, pc->prevF.x, pc->prevF.y, pc->prevF.layer);
+        basis(a, P.scaleWU * pc->prevF.su, P.scaleWV * pc->prevF.sv, &pc->fb0, &pc->fb1);
+    }
+    if (pc->temporalB) {
+        float a = screen_to_exemplar_angle(P, x, y, pc->prevB.x, pc->prevB.y, pc->prevB.layer);
+        basis(a, P.scaleWU * pc->prevB.su, P.scaleWV * pc->prevB.sv, &pc->bb0, &pc->bb1);
+    }
+    pc->hyst = pc->validF ? hysteresis_term(P, x, y) : 0.0f;
+}
+
+// timeDerivativeTerms, :438-469
+__device__ float time_derivative(const Params& P, int d, const Patch& prev, float2 pb0, float2 pb1, float4 base,
+                                 float4 tb, float4 canvas, float4 to, size_t k, int i, int j) {
+    float4 pbase = __ldg(P.adv[d].base + k), pout = __ldg(P.adv[d].out + k);
+    float px, py;
+    new_coord((float)i, (float)j, prev.x, prev.y, pb0, pb1, &px, &py);
+    float4 peb, peo;
+    ex_sample2(P.ex, px, py, prev.layer, &peb, &peo);
+    float r = ssd(sub4(base, pbase), sub4(tb, peb)) * P.tdIn;
+    r = fmaf(ssd(sub4(canvas, pout), sub4(to, peo)), P.tdOut, r);
+    r = fmaf(ssd(pout, to), P.tc, r);
+    return r;
+}
+
+// coherenceTerm, :377-423
+__device__ float coherence_term(const Params& P, int x, int y, int i, int j, float tcx, float tcy, float tx,
+                                float ty) {
+    float4 ca = __ldg(P.off.A + (size_t)(y + j) * P.W + (x + i));
+    float dx = ca.x - tcx, dy = ca.y - tcy;
+    float distEx = fmaf(dy, dy, dx * dx) * (float)(1 << P.level);
+    float distIm = (float)(i * i + j * j) * (float)(1 << P.level);
+    float R = P.coherenceRatioRange;
+    float ratio = fmaxf(1.0f / R, fminf(distEx / distIm, R));
+    float lr = log_poly(ratio);
+    float lR = log_poly(R);
+    float Z = lR * lR;
+    float Er = (lr * lr) / Z;
+    float tdx = tx - tcx, tdy = ty - tcy;
+    float lt = sqrtf(fmaf(tdy, tdy, tdx * tdx));
+    float dtx = (lt > 1e-4f) ? tdx * (1.0f / lt) : 1.0f;
+    float dty = (lt > 1e-4f) ? tdy * (1.0f / lt) : 0.0f;
+    float lc = sqrtf(fmaf(dy, dy, dx * dx));
+    float dcx = (lc > 1e-4f) ? dx * (1.0f / lc) : 1.0f;
+    float dcy = (lc > 1e-4f) ? dy * (1.0f / lc) : 0.0f;
+    float d = fmaf(dty, dcy, dtx * dcx);
+    float angle = fmaxf(-1.0f, fminf(acos_poly(d), 1.0f));
+    double ar = (double)P.coherenceAngleRange * 3.14159265358979323846;
+    float Ea = (float)(fmin((double)angle, ar) / ar);
+    return 1.0f - (1.0f - Er) * (1.0f - Ea);
+}
+
+__device__ __forceinline__ int f2i(float v) { return (int)v; }  // cvt.rzi: saturating, NaN -> 0
+
+// calculateResidual, :537-659
+__device__ float energy(const Params& P, int x, int y, const Patch& t, const PixCtx& pc) {
+    const int r = P.r;
+    float sumW = 0.0f, sum = 0.0f;
+    if (pc.validF) sum = sum - pc.hyst;
+    float2 b0, b1;
+    basis(t.theta, P.scaleWU * t.su, P.scaleWV * t.sv, &b0, &b1);
+    const float hw = (float)P.histW, hh = (float)P.histH;
+    const float4* imgb = P.img.base[P.img.cur].p;
+    const int imgw = P.img.base[P.img.cur].w;
+    for (int i = -r; i <= r; i++) {
+        for (int j = -r; j <= r; j++) {
+            if (!in_rect(P, x + i, y + j)) continue;
+            size_t k = (size_t)(y + j) * P.W + (x + i);
+            float4 base = __ldg(imgb + (size_t)(y + j) * imgw + (x + i));
+            float4 canvas = __ldg(P.canvas + k);
+            float tx, ty;
+            new_coord((float)i, (float)j, t.x, t.y, b0, b1, &tx, &ty);
+            if (tx >= hw) tx -= hw; else if (tx < 0) tx += hw;
+            if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
+            float4 tb, to;
+            ex_sample2(P.ex, tx, ty, t.layer, &tb, &to);
+            float res = ssd_a(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
+            if (pc.temporalF && __ldg(&P.adv[0].off.B[k].x) > 0)
+                res = res + time_derivative(P, 0, pc.prevF, pc.fb0, pc.fb1, base, tb, canvas, to, k, i, j);
+            if (pc.temporalB && __ldg(&P.adv[1].off.B[k].x) > 0)
+                res = res + time_derivative(P, 1, pc.prevB, pc.bb0, pc.bb1, base, tb, canvas, to, k, i, j);
+            if (i == 0 && j == 0) {
+                if (P.distTransWeight > 0.f) {
+                    float de = ex_sample_dt(P.ex, tx, ty, t.layer) / t.sv;
+                    float di = lay_texel(P.img.dt[P.img.cur], P, x, y);
+                    float diff = fminf(fmaxf(fabsf(de - di), 0.0f), 10.0f);
+                    res = res + diff * P.distTransWeight;
+                }
+                {  // histogramTerm, :486-495
+                    int L = clampi(t.layer, 0, PT_MAX_STYLES - 1);
+                    float sh = (float)(P.histH / P.numStyles);
+                    int hx = clampi(f2i(tx), 0, P.histPitch - 1);
+                    int hy = clampi(f2i(ty + sh * (float)t.layer), 0, P.histRows - 1);
+                    float h = __ldg(P.hist + (size_t)hy * P.histPitch + hx);
+                    float thr = P.histThreshold[L];
+                    res = res + ((h > thr) ? (h - thr) * P.histSlope[L] : 0.0f);
+                }
+                if (P.styleObjIdWeight > 0.f) {
+                    int imgID = lvl_texel(P.img.ids, x, y);
+                    int styleID = ex_point_id(P.ex, tx, ty, t.layer);
+                    res = res + ((imgID != styleID) ? P.styleObjIdWeight : 0.0f);
+                }
+            } else {
+                res = fmaf(ssd_a(canvas, to, P.alphaWeight), P.canvasOutputWeight, res);
+                if (P.coherenceWeight > 0.f) {
+                    float c = coherence_term(P, x, y, i, j, t.x, t.y, tx, ty);
+                    res = fmaf(c, P.coherenceWeight, res);
+                }
+            }
+            float w = P.gauss[i + r] * P.gauss[j + r];
+            sum = fmaf(res, w, sum);
+            sumW = sumW + w;
+        }
+    }
+    if (sumW < kEpsilon) return kBigResidual;
+    return sum / sumW;
+}
+
+// test_offset + isExemplarPixelCulled, :200-205,695-721
+__device__ float test_offset(const Params& P, int x, int y, const Patch& t, float image_alpha, const PixCtx& pc) {
+    float dte = ex_texel_dt(P.ex, f2i(t.x), f2i(t.y), t.layer);
+    if (!((double)dte > (double)P.distTransCull * 1.25)) {
+        if (!P.transparencyOk) {
+            float ea = ex_sample_out_alpha(P.ex, t.x, t.y, t.layer);
+            if (ea < kAlphaThreshold && image_alpha > kAlphaThreshold) return kBigResidual;
+        }
+        return energy(P, x, y, t, pc);
+    }
+    return kBigResidual;
+}
+
+// calculatePropagateOffset, :956-982 (pixelWrap with the level-0 size,
+// cudaImageBuffer.h:81-87)
+__device__ Patch propagate_offset(const Params& P, int tx, int ty, int x, int y) {
+    int wx = (int)((float)tx - (float)P.W * floorf((float)tx / (float)P.W));
+    int wy = (int)((float)ty - (float)P.H * floorf((float)ty / (float)P.H));
+    size_t kk = (size_t)wy * P.W + wx;
+    float4 a = __ldg(P.off.A + kk);
+    float2 sc = lvl_texel(P.img.scale, tx, ty);
+    float2 b0, b1;
+    basis(a.z, P.scaleWU * sc.x, P.scaleWV * sc.y, &b0, &b1);
+    float ex, ey;
+    new_coord((float)x - (float)tx, (float)y - (float)ty, a.x, a.y, b0, b1, &ex, &ey);
+    clamp_to_exemplar(&ex, &ey, P.ex.w, P.ex.h);
+    int layer = __float_as_int(a.w);
+    float ang = screen_to_exemplar_angle(P, x, y, ex, ey, layer);
+    float2 s2 = lvl_texel(P.img.scale, x, y);
+    return make_patch(ex, ey, ang, 0.0f, layer, s2.x, s2.y);
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+
+#define PIXEL_XY                                        \
+    const int x = blockIdx.x * blockDim.x + threadIdx.x; \
+    const int y = blockIdx.y * blockDim.y + threadIdx.y; \
+    if (!in_rect(P, x, y)) return;                      \
+    const size_t k = (size_t)y * P.W + x;
+
+// propagate_kernel, :1112-1219 (advected candidates are dead code, :981)
+__global__ void __launch_bounds__(128) k_propagate(const Params P, PatchPlanes work, int jump) {
+    PIXEL_XY
+    if (image_culled(P, x, y)) {
+        store_patch(work, k, make_patch(0, 0, 0, 0, 0, 1.f, 1.f));
+        return;
+    }
+    float best = __ldg(P.res + k);
+    float ia = lay_texel(P.img.base[P.img.cur], P, x, y).w;
+    Patch ow = load_patch(P.off, k);
+    PixCtx pc;
+    make_pixctx(P, x, y, &pc);
+#pragma unroll 1
+    for (int c = 0; c < 4; c++) {
+        int tx = x, ty = y;
+        if (c == 0) tx = x + jump;
+        else if (c == 1) tx = x - jump;
+        else if (c == 2) ty = y + jump;
+        else ty = y - jump;
+        Patch t = propagate_offset(P, tx, ty, x, y);
+        float r = test_offset(P, x, y, t, ia, pc);
+        if (r < best) { ow = t; best = r; }
+    }
+    store_patch(work, k, ow);
+}
+
+// scatter_kernel + averageOffset, :841-952.  REFERENCE mode: randFloat()
+// returns unsigned int 0 (texSynth_util.h:155-163), so candidate i is
+// (best.x + 0.9*dist_i, best.y).  COUNTER mode draws r and theta in [0, 1)
+// and [0, 2pi) from a counter-based hash.  write_all: the working buffer
+// aliases base, so unchanged pixels are written too.
+__device__ __forceinline__ uint32_t hash32(uint32_t a) {
+    a ^= a >> 16; a *= 0x7feb352dU; a ^= a >> 15; a *= 0x846ca68bU; a ^= a >> 16;
+    return a;
+}
+__device__ __forceinline__ float counter_u01(uint32_t seed, uint32_t level, uint32_t x, uint32_t y, uint32_t n) {
+    uint32_t h = hash32(seed ^ hash32(level * 0x9E3779B9U ^ hash32(x * 0x85EBCA6BU ^ hash32(y * 0xC2B2AE35U ^ n))));
+    return (float)(h >> 8) * (1.0f / 16777216.0f);
+}
+
+__global__ void __launch_bounds__(128) k_scatter(const Params P, PatchPlanes work, int write_all, uint32_t pass_id) {
+    PIXEL_XY
+    Patch off = load_patch(P.off, k);
+    if (image_culled(P, x, y)) {
+        if (write_all) store_patch(work, k, off);
+        return;
+    }
+    float cached = __ldg(P.res + k);
+    float best = (float)((double)cached + 10e-7);
+    Patch ow = off;
+    float ia = lay_texel(P.img.base[P.img.cur], P, x, y).w;
+    float dist = (float)(P.ex.w > P.ex.h ? P.ex.w : P.ex.h);
+    const float closest = 10.f, factor = 0.9f;
+    float2 sc = lvl_texel(P.img.scale, x, y);
+    PixCtx pc;
+    make_pixctx(P, x, y, &pc);
+#pragma unroll 1
+    for (int i = 0; i < P.scatterSamples && dist * factor >= closest; i++) {
+        float dmin = dist * factor;
+        float ex, ey;
+        if (P.rngMode == PT_RNG_COUNTER) {
+            float rr = counter_u01(P.rngSeed, pass_id, x, y, 2 * i);
+            float th = counter_u01(P.rngSeed, pass_id, x, y, 2 * i + 1) * 6.28318530717958647692f;
+            float s, c;
+            sincos_poly(th, &s, &c);
+            float len = fmaf(rr, dist - dmin, dmin);
+            ex = fmaf(c, len, ow.x);
+            ey = fmaf(s, len, ow.y);
+        } else {
+            ex = ow.x + dmin;
+            ey = ow.y + 0.0f;
+        }
+        clamp_to_exemplar(&ex, &ey, P.ex.w, P.ex.h);
+        float ang = screen_to_exemplar_angle(P, x, y, ex, ey, 0);
+        Patch t = make_patch(ex, ey, ang, 0.0f, 0, sc.x, sc.y);
+        float r = test_offset(P, x, y, t, ia, pc);
+        if (r < best) { ow = t; best = r; }
+        dist *= factor;
+    }
+    Patch avg = make_patch(0, 0, 0, 1.f, 0, 1.f, 1.f);
+    int n = 0;
+    for (int i = -1; i <= 1; i++)
+        for (int j = -1; j <= 1; j++) {
+            if (!in_rect(P, x + i, y + j) || (i == 0 && j == 0)) continue;
+            float4 nb = __ldg(P.off.A + (size_t)(y + j) * P.W + (x + i));
+            if (__float_as_int(nb.w) != 0) continue;
+            avg.x = avg.x + nb.x;
+            avg.y = avg.y + nb.y;
+            n++;
+        }
+    avg.x = avg.x / (float)n;
+    avg.y = avg.y / (float)n;
+    avg.theta = screen_to_exemplar_angle(P, x, y, avg.x, avg.y, 0);
+    float r = test_offset(P, x, y, avg, ia, pc);
+    if (r < best) { ow = avg; best = r; }
+    if (best < cached) store_patch(work, k, ow);
+    else if (write_all) store_patch(work, k, off);
+}
+
+// updateResidualCache_kernel, :661-693
+__global__ void __launch_bounds__(128) k_residual(const Params P, float* out) {
+    PIXEL_XY
+    if (image_culled(P, x, y)) { out[k] = 0.0f; return; }
+    PixCtx pc;
+    make_pixctx(P, x, y, &pc);
+    Patch t = load_patch(P.off, k);
+    out[k] = energy(P, x, y, t, pc);
+}
+
+// offsetsToOutput, :263-274
+__global__ void k_canvas(const Params P, float4* canvas) {
+    PIXEL_XY
+    float4 a = __ldg(P.off.A + k);
+    float lumy = __ldg(&P.off.B[k].w), luma = __ldg(P.off.C + k);
+    float4 c = ex_sample_out(P.ex, a.x, a.y, __float_as_int(a.w));
+    canvas[k] = f4(c.x + lumy, c.y + lumy, c.z + lumy, c.w + luma);
+}
+
+// copyRandomKernel, :2044-2059
+__global__ void k_random_offsets(const Params P, PatchPlanes work) {
+    PIXEL_XY
+    float4 r = lvl_texel(P.img.rnd, x, y);
+    store_patch(work, k, make_patch(r.x, r.y, r.z, 0.f, f2i(r.w), 1.f, 1.f));
+}
+
+// offsetUpsampleNearest, :1403-1417
+__device__ float2 upsample_nearest(const Params& P, const Patch& c, float dx, float dy) {
+    float2 b0, b1;
+    basis(c.theta, 1.0f, 1.0f, &b0, &b1);
+    float ix, iy;
+    new_coord(dx, dy, c.x, c.y, b0, b1, &ix, &iy);
+    clamp_to_exemplar(&ix, &iy, P.ex.w, P.ex.h);
+    return make_float2(fmaf(ix, 2.0f, 0.5f), fmaf(iy, 2.0f, 0.5f));
+}
+
+// upsampleBilinearKernel + TexSynth::upsample, :1453-1532.  Border pixels
+// keep the working buffer's content (border_src); residual border keeps the
+// base residual.
+__global__ void k_upsample(const Params P, PatchPlanes work, PatchPlanes border_src, int copy_border,
+                           float* res_out) {
+    PIXEL_XY
+    if (!in_rect(P, x, y, 1)) {
+        if (copy_border) store_patch(work, k, load_patch(border_src, k));
+        res_out[k] = __ldg(P.res + k);
+        return;
+    }
+    float cx = (float)((double)x - 0.5) / 2.0f;
+    float cy = (float)((double)y - 0.5) / 2.0f;
+    int lcx = (int)floorf(cx), lcy = (int)floorf(cy);
+    float4 o00 = __ldg(P.off.A + (size_t)lcy * P.W + lcx);
+    float4 o10 = __ldg(P.off.A + (size_t)lcy * P.W + lcx + 1);
+    float4 o01 = __ldg(P.off.A + (size_t)(lcy + 1) * P.W + lcx);
+    float4 o11 = __ldg(P.off.A + (size_t)(lcy + 1) * P.W + lcx + 1);
+    float a = cx - (float)lcx, b = cy - (float)lcy;
+    float w00 = (1 - a) * (1 - b), w10 = a * (1 - b), w01 = (1 - a) * b, w11 = a * b;
+    float ix = w00 * o00.x; ix = fmaf(w10, o10.x, ix); ix = fmaf(w01, o01.x, ix); ix = fmaf(w11, o11.x, ix);
+    float iy = w00 * o00.y; iy = fmaf(w10, o10.y, iy); iy = fmaf(w01, o01.y, iy); iy = fmaf(w11, o11.y, iy);
+    float2 up = make_float2(fmaf(ix, 2.0f, 0.5f), fmaf(iy, 2.0f, 0.5f));
+    bool far = false;
+    {
+        float dx, dy;
+        dx = ix - o00.x; dy = iy - o00.y; far |= fmaf(dy, dy, dx * dx) > 16.0f;
+        dx = ix - o10.x; dy = iy - o10.y; far |= fmaf(dy, dy, dx * dx) > 16.0f;
+        dx = ix - o01.x; dy = iy - o01.y; far |= fmaf(dy, dy, dx * dx) > 16.0f;
+        dx = ix - o11.x; dy = iy - o11.y; far |= fmaf(dy, dy, dx * dx) > 16.0f;
+    }
+    if (far) {
+        int rcx = (int)roundf(cx), rcy = (int)roundf(cy);
+        Patch c = load_patch(P.off, (size_t)rcy * P.W + rcx);
+        up = upsample_nearest(P, c, cx - (float)rcx, cy - (float)rcy);
+    }
+    int layer = __float_as_int(o00.w);
+    float rw = __ldg(P.res + (size_t)lcy * P.W + lcx);
+    float ang = screen_to_exemplar_angle(P, x, y, up.x, up.y, layer);
+    float2 sc = lvl_texel(P.img.scale, x, y);
+    store_patch(work, k, make_patch(up.x, up.y, ang, 0.0f, layer, sc.x, sc.y));
+    res_out[k] = rw;
+}
+
+// calculateTranslatedPosition + advectKernel, :1540-1693
+__global__ void k_advect(const Params P, int d, int forwards, int time_step, int flags) {
+    PIXEL_XY
+    const AdvView& A = P.adv[d];
+    const int cur = P.img.cur, prev = (P.img.cur + 1) % 2;
+    if (image_culled(P, x, y)) {
+        A.base[k] = f4(0, 0, 0, 0);
+        A.out[k] = f4(0, 0, 0, 0);
+        store_patch(A.off, k, make_patch(0, 0, 0, 0, 0, 1.f, 1.f));
+        return;
+    }
+    float4 rnd = lvl_texel(P.img.rnd, x, y);
+    float4 fr = f4(rnd.x - floorf(rnd.x), rnd.y - floorf(rnd.y), rnd.z - floorf(rnd.z), rnd.w - floorf(rnd.w));
+    Patch out = make_patch(0, 0, 0, 0, 0, 1.f, 1.f);
+    bool valid = false;
+    float tx = 0, ty = 0;
+    if (!(flags & PT_ADVECT_DO_NOT_CHECK_PREVIOUS)) {
+        float2 fw, bk;
+        if (forwards) {
+            bk = lay_texel(P.img.velb[cur], P, x, y);
+            tx = (float)x + bk.x; ty = (float)y + bk.y;
+            fw = lay_bilinear(P.img.velf[prev], P, tx, ty);
+        } else {
+            fw = lay_texel(P.img.velf[cur], P, x, y);
+            tx = (float)x + fw.x; ty = (float)y + fw.y;
+            bk = lay_bilinear(P.img.velb[prev], P, tx, ty);
+        }
+        fw.x = -fw.x; fw.y = -fw.y;
+        float ddx = fw.x - bk.x, ddy = fw.y - bk.y;
+        float dist = sqrtf(fmaf(ddy, ddy, ddx * ddx));
+        float cxf = fminf(fmaxf(ceilf(tx), -2.f), 1e9f), cyf = fminf(fmaxf(ceilf(ty), -2.f), 1e9f);
+        float fxf = fminf(fmaxf(floorf(tx), -2.f), 1e9f), fyf = fminf(fmaxf(floorf(ty), -2.f), 1e9f);
+        valid = in_rect(P, f2i(cxf), f2i(cyf)) && in_rect(P, f2i(fxf), f2i(fyf)) && (dist < (float)(1.414 * 2));
+        if (valid) {
+            float pd = lay_texel(P.img.dt[prev], P, f2i(tx), f2i(ty));
+            if (pd > ((float)P.distTransCull - 8.0f)) valid = false;
+        }
+    }
+    if (valid) {
+        int rtx = (int)roundf(tx), rty = (int)roundf(ty);
+        Patch nx = load_patch(P.off, (size_t)rty * P.W + rtx);
+        float2 b0, b1;
+        basis(nx.theta, 1.0f, 1.0f, &b0, &b1);
+        float ix, iy;
+        new_coord(tx - (float)rtx, ty - (float)rty, nx.x, nx.y, b0, b1, &ix, &iy);
+        clamp_to_exemplar(&ix, &iy, P.ex.w, P.ex.h);
+        float4 color = lay_texel(P.img.base[cur], P, x, y);
+        float4 pcol = lay_bilinear(P.img.base[prev], P, tx, ty);
+        out.x = ix; out.y = iy; out.theta = nx.theta;
+        if (P.lumShiftEnable) {
+            float dr = color.x - pcol.x, dg = color.y - pcol.y, db = color.z - pcol.z;
+            float ly = (float)(0.2126 * (double)dr + 0.7152 * (double)dg + 0.0722 * (double)db);
+            out.lumy = nx.lumy + ly;
+        } else {
+            out.lumy = 0.f;
+        }
+        out.luma = 0.f;
+        out.layer = nx.layer;
+        out.hyst = 1;
+        A.base[k] = pcol;
+        A.out[k] = ex_sample_out(P.ex, out.x, out.y, out.layer);
+        A.ts[k] = time_step;
+    }
+    if (out.hyst == 0) {
+        out = make_patch(rnd.x, rnd.y, rnd.z, 0.0f, f2i(rnd.w), 1.f, 1.f);
+        A.base[k] = f4(0, 0, 0, 0);
+        A.out[k] = f4(0, 0, 0, 0);
+        A.ts[k] = -1;
+    }
+    float J = P.jitter;
+    out.x = fmaf(fr.x, J, out.x * (1 - J));
+    out.y = fmaf(fr.y, J, out.y * (1 - J));
+    out.theta = screen_to_exemplar_angle(P, x, y, out.x, out.y, out.layer);
+    store_patch(A.off, k, out);
+}
+
+// mergeRandomlyKernel, :1891-1936 (frame-to-key ribbons are unbound outside
+// keyframe mode: both read as valid, so the ribbon clause is false)
+__global__ void k_merge_random(const Params P, int d, int forwards, float weight, int force, PatchPlanes work) {
+    PIXEL_XY
+    float4 rnd = lvl_texel(P.img.rnd, x, y);
+    float r = forwards ? rnd.x - floorf(rnd.x) : rnd.y - floorf(rnd.y);
+    bool av = __ldg(&P.adv[d].off.B[k].x) > 0;
+    const PatchPlanes& src = ((av || force) && r < weight) ? P.adv[d].off : P.off;
+    store_patch(work, k, load_patch(src, k));
+}
+
+// mergeUsingResidualKernel, :1856-1889
+__global__ void k_merge_residual(const Params P, int d, PatchPlanes work) {
+    PIXEL_XY
+    Patch r;
+    if (__ldg(P.adv[d].res + k) < __ldg(P.res + k)) { r = load_patch(P.adv[d].off, k); r.hyst = 1.f; }
+    else { r = load_patch(P.off, k); r.hyst = 0.f; }
+    store_patch(work, k, r);
+}
+
+// separable Gaussian over the histogram, convolution.cu:76-210 (normalised
+// weights, zero apron): rows (rows=1) or columns (rows=0)
+__global__ void k_conv(const float* src, float* dst, int w, int h, int pitch, int rows, ConvKernel kw) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    float s = 0.0f;
+    const int r = kw.r;
+    for (int j = -r; j <= r; j++) {
+        int xx = rows ? x + j : x, yy = rows ? y : y + j;
+        float v = (xx >= 0 && xx < w && yy >= 0 && yy < h) ? __ldg(src + (size_t)yy * pitch + xx) : 0.0f;
+        s = fmaf(kw.w[r - j], v, s);
+    }
+    dst[(size_t)y * pitch + x] = s;
+}
+
+// copies of the level rectangle
+__global__ void k_copy_patch(const Params P, PatchPlanes dst, PatchPlanes src) {
+    PIXEL_XY
+    dst.A[k] = __ldg(src.A + k);
+    dst.B[k] = __ldg(src.B + k);
+    dst.C[k] = __ldg(src.C + k);
+}
+__global__ void k_copy_float(const Params P, float* dst, const float* src) {
+    PIXEL_XY
+    dst[k] = __ldg(src + k);
+}
+
+// PatchXF records <-> planes, and the half-precision residual round trip
+__global__ void k_unpack_patch(const Params P, const pt_patchxf* src, PatchPlanes dst) {
+    PIXEL_XY
+    pt_patchxf v = src[(size_t)y * P.lw + x];
+    Patch p;
+    p.x = v.x; p.y = v.y; p.theta = v.theta; p.hyst = v.hysteresis; p.layer = v.layer;
+    p.su = v.scaleU; p.sv = v.scaleV; p.lumy = v.lumShiftY; p.luma = v.lumShiftA;
+    store_patch(dst, k, p);
+}
+__global__ void k_pack_patch(const Params P, PatchPlanes src, pt_patchxf* dst) {
+    PIXEL_XY
+    Patch p = load_patch(src, k);
+    pt_patchxf v;
+    v.x = p.x; v.y = p.y; v.theta = p.theta; v.hysteresis = p.hyst; v.layer = p.layer;
+    v.scaleU = p.su; v.scaleV = p.sv; v.lumShiftY = p.lumy; v.lumShiftA = p.luma;
+    dst[(size_t)y * P.lw + x] = v;
+}
+__global__ void k_load_residual(const Params P, const float* src, float* dst) {
+    PIXEL_XY
+    dst[k] = __half2float(__float2half_rn(src[(size_t)y * P.lw + x]));
+}
+__global__ void k_gather_level(const Params P, const float* src, int ch, float* dst) {
+    PIXEL_XY
+    for (int c = 0; c < ch; c++) dst[((size_t)y * P.lw + x) * ch + c] = __ldg(src + k * ch + c);
+}
+
+// ---------------------------------------------------------------------------
+// pyramid construction (downsample.cpp:41-209, imageIO.h:136-139)
+// ---------------------------------------------------------------------------
+
+__global__ void k_down_avg(const float* src, int w, int h, int ch, int vel, float* dst) {
+    int lw = w >> 1, lh = h >> 1;
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= lw || y >= lh) return;
+    for (int c = 0; c < ch; c++) {
+        float s = 0.0f;
+        s = s + __ldg(src + ((size_t)(2 * y) * w + 2 * x) * ch + c);
+        s = s + __ldg(src + ((size_t)(2 * y) * w + 2 * x + 1) * ch + c);
+        s = s + __ldg(src + ((size_t)(2 * y + 1) * w + 2 * x) * ch + c);
+        s = s + __ldg(src + ((size_t)(2 * y + 1) * w + 2 * x + 1) * ch + c);
+        s = s * 0.25f;
+        if (vel) s = s * 0.5f;
+        dst[((size_t)y * lw + x) * ch + c] = s;
+    }
+}
+
+// majority vote of the 2x2 values; ties go to the smallest value
+__global__ void k_down_vote(const int* src, int w, int h, int* dst) {
+    int lw = w >> 1, lh = h >> 1;
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= lw || y >= lh) return;
+    int v[4] = {__ldg(src + (size_t)(2 * y) * w + 2 * x), __ldg(src + (size_t)(2 * y) * w + 2 * x + 1),
+                __ldg(src + (size_t)(2 * y + 1) * w + 2 * x), __ldg(src + (size_t)(2 * y + 1) * w + 2 * x + 1)};
+    int best = v[0], bestc = -1;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        int c = 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) c += (v[j] == v[i]);
+        if (c > bestc || (c == bestc && v[i] < best)) { bestc = c; best = v[i]; }
+    }
+    dst[(size_t)y * lw + x] = best;
+}
+
+__global__ void k_tensor_angle(const float* t3, int n, float* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float xx = __ldg(t3 + 3 * i), xy = __ldg(t3 + 3 * i + 1), yy = __ldg(t3 + 3 * i + 2);
+    float a2 = atan2_poly((float)(2.0 * (double)xy), xx - yy);
+    float angle = (float)(0.5 * (double)a2 + 1.57079632679489661923);
+    out[i] = ((double)angle >= 1.57079632679489661923) ? (float)((double)angle - 3.14159265358979323846) : angle;
+}
+
+// base/output interleaving of one exemplar layer
+__global__ void k_interleave(const float4* src, int n, float4* bo, int which) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    bo[2 * (size_t)i + which] = __ldg(src + i);
+}
+
+// ---------------------------------------------------------------------------
+// random-offset level (SynthesisFrame::createRandomPyramid,
+// synthesisFrame.cpp:66-150)
+// ---------------------------------------------------------------------------
+
+struct RandParams {
+    int w, h, mx, my;
+    int transparencyOk, orientationEnabled;
+    Arr<float4> img;     // level-size input colour (alpha)
+    Arr<float> iorient;  // level-size input orientation
+    ExView ex;           // exemplar level (style 0)
+    float4* out;
+};
+
+__device__ __forceinline__ float4 random_texel(const RandParams& R, int x, int y, uint32_t d0, uint32_t d1,
+                                                uint32_t d2, uint32_t d3) {
+    int ox = (int)((d0 >> 1) % (uint32_t)R.mx);
+    int oy = (int)((d1 >> 1) % (uint32_t)R.my);
+    float orient = R.orientationEnabled
+                       ? __ldg(R.iorient.p + (size_t)y * R.iorient.w + x) - __ldg(R.ex.orient + (size_t)oy * R.ex.w + ox)
+                       : 0.f;
+    float rx = (float)(d2 >> 1) / (float)2147483647;
+    float ry = (float)(d3 >> 1) / (float)2147483647;
+    return f4((float)ox + rx, (float)oy + ry, orient, 0.0f);
+}
+
+// One thread per row: the glibc additive-feedback state at the row start is
+// precomputed on the host (jump-ahead by a 31x31 matrix power over Z/2^32);
+// each thread then steps the recurrence r[i] = r[i-31] + r[i-3] in a
+// shared-memory ring.  Valid when no pixel retries (no exemplar texel with
+// alpha < 0.99, or transparency allowed).
+__global__ void k_glibc_rows(const RandParams R, const uint32_t* row_states) {
+    extern __shared__ uint32_t ring_all[];
+    int y = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t* ring = ring_all + threadIdx.x;  // stride blockDim.x: conflict-free
+    const int S = blockDim.x;
+    if (y >= R.h) return;
+    for (int i = 0; i < 31; i++) ring[i * S] = row_states[(size_t)y * 31 + i];
+    int head = 0;
+    int h28 = 28;
+    for (int x = 0; x < R.w; x++) {
+        uint32_t d[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            uint32_t v = ring[head * S] + ring[h28 * S];
+            ring[head * S] = v;
+            head = (head == 30) ? 0 : head + 1;
+            h28 = (h28 == 30) ? 0 : h28 + 1;
+            d[q] = v;
+        }
+        R.out[(size_t)y * R.w + x] = random_texel(R, x, y, d[0], d[1], d[2], d[3]);
+    }
+}
+
+// Exact serial version (one thread) with the reference's retry loop for
+// opaque pixels that drew a transparent exemplar texel.
+__global__ void k_glibc_serial(const RandParams R, const uint32_t* state31) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    uint32_t ring[31];
+    for (int i = 0; i < 31; i++) ring[i] = state31[i];
+    int head = 0;
+    auto next = [&]() -> uint32_t {
+        int h28 = head + 28;
+        if (h28 >= 31) h28 -= 31;
+        uint32_t v = ring[head] + ring[h28];
+        ring[head] = v;
+        head = (head == 30) ? 0 : head + 1;
+        return v;
+    };
+    for (int y = 0; y < R.h; y++)
+        for (int x = 0; x < R.w; x++) {
+            float ia = __ldg(R.img.p + (size_t)y * R.img.w + x).w;
+            uint32_t d0, d1;
+            int trial = 0;
+            bool again;
+            do {
+                d0 = next();
+                d1 = next();
+                trial++;
+                int ox = (int)((d0 >> 1) % (uint32_t)R.mx), oy = (int)((d1 >> 1) % (uint32_t)R.my);
+                float ea = __ldg(R.ex.bo + ((size_t)oy * R.ex.w + ox) * 2 + 1).w;
+                again = !R.transparencyOk && ia > kAlphaThreshold && ea < kAlphaThreshold && trial < 50;
+            } while (again);
+            uint32_t d2 = next(), d3 = next();
+            R.out[(size_t)y * R.w + x] = random_texel(R, x, y, d0, d1, d2, d3);
+        }
+}
+
+// counter-based random level: four hashed draws per pixel and trial
+__global__ void k_counter_random(const RandParams R, uint32_t seed) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= R.w || y >= R.h) return;
+    float ia = __ldg(R.img.p + (size_t)y * R.img.w + x).w;
+    uint32_t base = hash32(seed ^ hash32(x * 0x85EBCA6BU ^ hash32(y * 0xC2B2AE35U)));
+    uint32_t d0, d1;
+    int trial = 0;
+    bool again;
+    do {
+        d0 = hash32(base + 4u * trial);
+        d1 = hash32(base + 4u * trial + 1u);
+        trial++;
+        int ox = (int)((d0 >> 1) % (uint32_t)R.mx), oy = (int)((d1 >> 1) % (uint32_t)R.my);
+        float ea = __ldg(R.ex.bo + ((size_t)oy * R.ex.w + ox) * 2 + 1).w;
+        again = !R.transparencyOk && ia > kAlphaThreshold && ea < kAlphaThreshold && trial < 50;
+    } while (again);
+    uint32_t d2 = hash32(base + 0x40000000u), d3 = hash32(base + 0x40000001u);
+    R.out[(size_t)y * R.w + x] = random_texel(R, x, y, d0, d1, d2, d3);
+}
+
+// any exemplar output texel with alpha < 0.99 (decides whether the random
+// level can be drawn row-parallel)
+__global__ void k_any_transparent(const float4* bo, size_t n, int* flag) {
+    size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    for (; i < n; i += (size_t)gridDim.x * blockDim.x)
+        if (__ldg(bo + 2 * i + 1).w < kAlphaThreshold) { atomicOr(flag, 1); return; }
+}
+
+}  // namespace ptk
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+
+namespace pt {
+
+using namespace ptk;
+
+static inline dim3 grid2(int w, int h, dim3 b) { return dim3((w + b.x - 1) / b.x, (h + b.y - 1) / b.y); }
+static const dim3 kPix(32, 4);
+
+#define LAUNCH_CHECK() return cudaGetLastError()
+
+cudaError_t launch_propagate(const Params& P, PatchPlanes work, int jump, cudaStream_t s) {
+    k_propagate<<<grid2(P.lw, P.lh, kPix), kPix, 0, s>>>(P, work, jump);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_scatter(const Params& P, PatchPlanes work, int write_all, uint32_t pass_id, cudaStream_t s) {
+    k_scatter<<<grid2(P.lw, P.lh, kPix), kPix, 0, s>>>(P, work, write_all, pass_id);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_residual(const Params& P, float* out, cudaStream_t s) {
+    k_residual<<<grid2(P.lw, P.lh, kPix), kPix, 0, s>>>(P, out);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_canvas(const Params& P, float4* canvas, cudaStream_t s) {
+    k_canvas<<<grid2(P.lw, P.lh, kPix), kPix, 0, s>>>(P, canvas);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_random_offsets(const Params& P, PatchPlanes work, cudaStream_t s) {
+    k_random_offsets<<<grid2(P.lw, P.lh, kPix), kPix, 0, s>>>(P, work);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_upsample(const Params& P, PatchPlanes work, PatchPlanes border_src, int copy_border,
+                            float* res_out, cudaStream_t s) {
+    k_upsample<<<grid2(P.lw, P.lh, kPix), kPix, 0, s>>>(P, work, border_src, copy_border, res_out);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_advect(const Params& P, int d, int forwards, int time_step, int flags, cudaStream_t s) {
+    k_advect<<<grid2(P.lw, P.lh, kPix), kPix, 0, s>>>(P, d, forwards, time_step, flags);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_merge_random(const Params& P, int d, int forwards, float weight, int force, PatchPlanes work,
+                                cudaStream_t s) {
+    k_merge_random<<<grid2(P.lw, P.lh, kPix), kPix, 0, s>>>(P, d, forwards, weight, force, work);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_merge_residual(const Params& P, int d, PatchPlanes work, cudaStream_t s) {
+    k_merge_residual<<<grid2(P.lw, P.lh, kPix), kPix, 0, s>>>(P, d, work);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_conv(const float* src, float* dst, int w, int h, int pitch, int rows, const ConvKernel& kw,
+                        cudaStream_t s) {
+    dim3 b(32, 4);
+    k_conv<<<grid2(w, h, b), b, 0, s>>>(src, dst, w, h, pitch, rows, kw);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_copy_patch(const Params& P, PatchPlanes dst, PatchPlanes src, cudaStream_t s) {
+    k_copy_patch<<<grid2(P.lw, P.lh, kPix), kPix, 0, s>>>(P, dst, src);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_copy_float(const Params& P, float* dst, const float* src, cudaStream_t s) {
+    k_copy_float<<<grid2(P.lw, P.lh, kPix), kPix, 0, s>>>(P, dst, src);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_unpack_patch(const Params& P, const pt_patchxf* src, PatchPlanes dst, cudaStream_t s) {
+    k_unpack_patch<<<grid2(P.lw, P.lh, kPix), kPix, 0, s>>>(P, src, dst);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_pack_patch(const Params& P, PatchPlanes src, pt_patchxf* dst, cudaStream_t s) {
+    k_pack_patch<<<grid2(P.lw, P.lh, kPix), kPix, 0, s>>>(P, src, dst);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_load_residual(const Params& P, const float* src, float* dst, cudaStream_t s) {
+    k_load_residual<<<grid2(P.lw, P.lh, kPix), kPix, 0, s>>>(P, src, dst);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_gather_level(const Params& P, const float* src, int ch, float* dst, cudaStream_t s) {
+    k_gather_level<<<grid2(P.lw, P.lh, kPix), kPix, 0, s>>>(P, src, ch, dst);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_down_avg(const float* src, int w, int h, int ch, int vel, float* dst, cudaStream_t s) {
+    dim3 b(32, 4);
+    k_down_avg<<<grid2(w >> 1, h >> 1, b), b, 0, s>>>(src, w, h, ch, vel, dst);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_down_vote(const int* src, int w, int h, int* dst, cudaStream_t s) {
+    dim3 b(32, 4);
+    k_down_vote<<<grid2(w >> 1, h >> 1, b), b, 0, s>>>(src, w, h, dst);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_tensor_angle(const float* t3, int n, float* out, cudaStream_t s) {
+    k_tensor_angle<<<(n + 255) / 256, 256, 0, s>>>(t3, n, out);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_interleave(const float4* src, int n, float4* bo, int which, cudaStream_t s) {
+    k_interleave<<<(n + 255) / 256, 256, 0, s>>>(src, n, bo, which);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_random_level(int mode, int w, int h, int mx, int my, int transparencyOk, int orientationEnabled,
+                                Arr<float4> img, Arr<float> iorient, ExView ex, float4* out,
+                                const uint32_t* states, uint32_t seed, cudaStream_t s) {
+    RandParams R;
+    R.w = w; R.h = h; R.mx = mx; R.my = my;
+    R.transparencyOk = transparencyOk; R.orientationEnabled = orientationEnabled;
+    R.img = img; R.iorient = iorient; R.ex = ex; R.out = out;
+    if (mode == 0) {  // row-parallel glibc
+        const int tb = 64;
+        k_glibc_rows<<<(h + tb - 1) / tb, tb, tb * 31 * sizeof(uint32_t), s>>>(R, states);
+    } else if (mode == 1) {  // serial glibc
+        k_glibc_serial<<<1, 1, 0, s>>>(R, states);
+    } else {
+        dim3 b(32, 4);
+        k_counter_random<<<grid2(w, h, b), b, 0, s>>>(R, seed);
+    }
+    LAUNCH_CHECK();
+}
+cudaError_t launch_any_transparent(const float4* bo, size_t n, int* flag, cudaStream_t s) {
+    k_any_transparent<<<152 * 4, 256, 0, s>>>(bo, n, flag);
+    LAUNCH_CHECK();
+}
+
+}  // namespace pt

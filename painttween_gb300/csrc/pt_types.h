@@ -1,0 +1,107 @@
+// pt_types.h -- plain data structures shared by host and device code.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "painttween.h"
+
+namespace ptk {
+
+constexpr int kMaxRadius = 15;  // taps per axis <= 31
+
+// Offset field in three planes (SoA of the 36-byte PatchXF):
+//   A = (x, y, theta, layer as int bits), B = (hysteresis, scaleU, scaleV,
+//   lumShift.y), C = lumShift.a.  Full-resolution, pitch = image width.
+struct Patch {
+    float x, y, theta, hyst;
+    int layer;
+    float su, sv, lumy, luma;
+};
+
+struct PatchPlanes {
+    float4* A;
+    float4* B;
+    float* C;
+};
+
+// One exemplar pyramid level: ns styles of w x h texels; base and output are
+// interleaved per texel (32 bytes: base RGBA, output RGBA) so one bilinear
+// footprint of both images is four 32-byte sectors.
+struct ExView {
+    const float4* bo;
+    const float* orient;
+    const float* dt;
+    const int* ids;
+    int w, h, ns;
+};
+
+// A 2-D array of one pyramid level.  Image-side "layered" inputs (colour,
+// DT, velocities) are addressed with clamp at the level-0 size and read zero
+// outside the level rectangle, like the reference's full-resolution layered
+// textures holding the level in the top-left corner; the other inputs clamp
+// at their own size.
+template <class T>
+struct Arr {
+    const T* p;
+    int w, h;
+};
+
+struct ImgView {
+    Arr<float4> base[2];
+    Arr<float> dt[2];
+    Arr<float2> velf[2];
+    Arr<float2> velb[2];
+    Arr<float> orient;
+    Arr<float2> scale;
+    Arr<int> ids;
+    Arr<float4> rnd;
+    int cur;
+};
+
+struct AdvView {
+    PatchPlanes off;
+    float4* base;
+    float4* out;
+    float* res;
+    int* ts;
+};
+
+struct Params {
+    int W, H;            // level-0 image size == buffer pitch / height
+    int level, lw, lh;   // level and its size
+    int r;               // patch radius
+    float gauss[2 * kMaxRadius + 1];
+    float scaleWU, scaleWV;
+    float alphaWeight, inputAnalogyWeight, canvasOutputWeight;
+    float distTransWeight, styleObjIdWeight, coherenceWeight;
+    float coherenceRatioRange, coherenceAngleRange;
+    float tdIn, tdOut, tc;
+    float maxDistortion, hysteresisWeight;
+    float histThreshold[PT_MAX_STYLES], histSlope[PT_MAX_STYLES];
+    float jitter;
+    int numStyles;
+    int transparencyOk, orientationEnabled, lumShiftEnable;
+    int distTransCull;
+    int direction;
+    int scatterSamples;
+    int rngMode;
+    uint32_t rngSeed;
+    int histW, histH;          // histogram level size (style w, style h * ns) >> level
+    int histPitch, histRows;   // histogram buffer size at level 0
+    const float* hist;
+    ExView ex;
+    ImgView img;
+    PatchPlanes off;           // offsets base
+    const float* res;          // residual base
+    const float4* canvas;
+    AdvView adv[2];            // [0] = forward, [1] = backward
+};
+
+struct ConvKernel {
+    int r;
+    float w[2 * kMaxRadius + 1];
+};
+
+}  // namespace ptk

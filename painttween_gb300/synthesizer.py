@@ -1,0 +1,232 @@
+"""Python mirror of the reference's synthesizer interface for the offset-field
+synthesis path, over the C ABI of libpainttween_gb300.
+
+* `TexSynth` -- the step-wise calls of the reference's `namespace TexSynth`
+  (src/PaintTweenCUDA/texSynth_kernel.h:38-91) with the same names, argument
+  meaning and call order; errors raise `PaintTweenError` instead of exiting.
+* `Synthesizer` -- the working-set level: a style exemplar plus per-frame
+  image, orientation, distance-transform, object-ID and velocity inputs,
+  "synthesize frame" and "synthesize animation"
+  (GUI/nlSynthesizer.h:52-75, SynthesisProcessor::renderAnimationFMBM).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _abi
+from ._lib import lib
+
+
+class PaintTweenError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s: %s" % (_abi.status_name(status), message))
+        self.status = status
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _c(a, dtype):
+    return None if a is None else np.ascontiguousarray(a, dtype=dtype)
+
+
+class TexSynth:
+    """One synthesis context on one GPU (pt_create)."""
+
+    def __init__(self, device=0, hbm_budget=0):
+        h = ctypes.c_void_p()
+        st = lib().pt_create(device, hbm_budget, ctypes.byref(h))
+        if st != _abi.PT_OK:
+            raise PaintTweenError(st, "pt_create(device=%d) failed" % device)
+        self.h = h
+        self.W = self.H = 0
+        self.params = _abi.default_params()
+
+    # -- plumbing ------------------------------------------------------------
+    def _check(self, st, what):
+        if st != _abi.PT_OK:
+            msg = lib().pt_last_error(self.h) if self.h else b""
+            raise PaintTweenError(st, "%s: %s" % (what, (msg or b"").decode(errors="replace")))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().pt_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def kernel_launches(self):
+        return int(lib().pt_kernel_launches(self.h))
+
+    @property
+    def device_bytes(self):
+        return int(lib().pt_device_bytes(self.h))
+
+    def synchronize(self):
+        self._check(lib().pt_synchronize(self.h), "pt_synchronize")
+
+    # -- configuration (TexSynth::setup / uploadParameters) ----------------------
+    def set_params(self, params):
+        self.params = params.copy()
+        self._check(lib().pt_set_params(self.h, ctypes.byref(self.params)), "pt_set_params")
+
+    def initialize(self, image_w, image_h, style_w, style_h, num_styles=1):
+        self._check(lib().pt_initialize(self.h, image_w, image_h, style_w, style_h, num_styles), "pt_initialize")
+        self.W, self.H = image_w, image_h
+
+    def initialize_exemplars(self, w, h, num_styles=1):
+        self._check(lib().pt_initialize_exemplars(self.h, w, h, num_styles), "pt_initialize_exemplars")
+
+    def upload_image_color4(self, level, layer, rgba, style=0):
+        a = _c(rgba, np.float32)
+        self._check(lib().pt_upload_image_color4(self.h, level, layer, _p(a), a.shape[1], a.shape[0], style),
+                    "pt_upload_image_color4")
+
+    def upload_image_float(self, level, layer, data, style=0):
+        a = _c(data, np.float32)
+        self._check(lib().pt_upload_image_float(self.h, level, layer, _p(a), a.shape[1], a.shape[0], style),
+                    "pt_upload_image_float")
+
+    def upload_image_float2(self, level, layer, xy):
+        a = _c(xy, np.float32)
+        self._check(lib().pt_upload_image_float2(self.h, level, layer, _p(a), a.shape[1], a.shape[0]),
+                    "pt_upload_image_float2")
+
+    def upload_image_int(self, level, layer, data, style=0):
+        a = _c(data, np.int32)
+        self._check(lib().pt_upload_image_int(self.h, level, layer, _p(a), a.shape[1], a.shape[0], style),
+                    "pt_upload_image_int")
+
+    def flip_anim_buffers(self):
+        self._check(lib().pt_flip_anim_buffers(self.h), "pt_flip_anim_buffers")
+
+    # -- compute (TexSynth::*) ---------------------------------------------------
+    def create_random_level(self, level, frame):
+        self._check(lib().pt_create_random_level(self.h, level, frame), "pt_create_random_level")
+
+    def randomize_offsets(self, level):
+        self._check(lib().pt_randomize_offsets(self.h, level), "pt_randomize_offsets")
+
+    def propagate(self, level, jump, key_index=-1):
+        self._check(lib().pt_propagate(self.h, level, jump, key_index), "pt_propagate")
+
+    def scatter(self, level, key_index=-1):
+        self._check(lib().pt_scatter(self.h, level, key_index), "pt_scatter")
+
+    def upsample(self, fine_level):
+        self._check(lib().pt_upsample(self.h, fine_level), "pt_upsample")
+
+    def advect_offsets(self, level, time_step, forwards, op_flags=0):
+        self._check(lib().pt_advect_offsets(self.h, level, time_step, int(forwards), op_flags), "pt_advect_offsets")
+
+    def merge_randomly(self, level, forwards, weight_advected=0.5, force_valid=False):
+        self._check(lib().pt_merge_randomly(self.h, level, int(forwards), weight_advected, int(force_valid)),
+                    "pt_merge_randomly")
+
+    def merge_using_residual(self, level, forwards):
+        self._check(lib().pt_merge_using_residual(self.h, level, int(forwards)), "pt_merge_using_residual")
+
+    def update_residual_cache(self, level):
+        self._check(lib().pt_update_residual_cache(self.h, level), "pt_update_residual_cache")
+
+    def sync_buffers(self, level, op_flags=0):
+        self._check(lib().pt_sync_buffers(self.h, level, op_flags), "pt_sync_buffers")
+
+    def reset_advected_buffers(self):
+        self._check(lib().pt_reset_advected_buffers(self.h), "pt_reset_advected_buffers")
+
+    # -- state transfer ------------------------------------------------------------
+    def load_offsets(self, level, offsets):
+        a = np.ascontiguousarray(offsets, dtype=_abi.PATCH_DTYPE)
+        self._check(lib().pt_load_offsets(self.h, level, _p(a)), "pt_load_offsets")
+
+    def load_residual(self, level, residual):
+        a = _c(residual, np.float32)
+        self._check(lib().pt_load_residual(self.h, level, _p(a)), "pt_load_residual")
+
+    def get_offsets(self, level):
+        out = np.empty((self.H >> level, self.W >> level), _abi.PATCH_DTYPE)
+        self._check(lib().pt_get_offsets(self.h, level, _p(out)), "pt_get_offsets")
+        return out
+
+    def get_residual(self, level):
+        out = np.empty((self.H >> level, self.W >> level), np.float32)
+        self._check(lib().pt_get_residual(self.h, level, _p(out)), "pt_get_residual")
+        return out
+
+    def get_output(self, level):
+        out = np.empty((self.H >> level, self.W >> level, 4), np.float32)
+        self._check(lib().pt_get_output(self.h, level, _p(out)), "pt_get_output")
+        return out
+
+
+FRAME_CB = ctypes.CFUNCTYPE(None, ctypes.c_int, ctypes.POINTER(ctypes.c_float), ctypes.c_void_p,
+                            ctypes.c_int, ctypes.c_int, ctypes.c_void_p)
+
+
+class Synthesizer(TexSynth):
+    """Working-set API: resident style and frame pyramids on the device."""
+
+    def setup(self, params, image_w, image_h, style_w, style_h, num_styles=1):
+        self.initialize(image_w, image_h, style_w, style_h, num_styles)
+        self.set_params(params)
+
+    def set_style(self, style, base, output, orient_tensor=None, dist_trans=None, object_ids=None):
+        b, o = _c(base, np.float32), _c(output, np.float32)
+        h, w = b.shape[:2]
+        self._check(lib().pt_set_style(self.h, style, w, h, _p(b), _p(o), _p(_c(orient_tensor, np.float32)),
+                                       _p(_c(dist_trans, np.float32)), _p(_c(object_ids, np.int32))),
+                    "pt_set_style")
+
+    def set_frame(self, frame, rgba, orient_tensor=None, dist_trans=None, object_ids=None, vel_fwd=None,
+                  vel_bwd=None, scale=None):
+        c = _c(rgba, np.float32)
+        h, w = c.shape[:2]
+        self._check(lib().pt_set_frame(self.h, frame, w, h, _p(c), _p(_c(orient_tensor, np.float32)),
+                                       _p(_c(dist_trans, np.float32)), _p(_c(object_ids, np.int32)),
+                                       _p(_c(vel_fwd, np.float32)), _p(_c(vel_bwd, np.float32)),
+                                       _p(_c(scale, np.float32))), "pt_set_frame")
+
+    def set_frame_dict(self, frame, fr):
+        self.set_frame(frame, fr["rgba"], fr.get("orient_tensor"), fr.get("dist_trans"), fr.get("object_ids"),
+                       fr.get("vel_fwd"), fr.get("vel_bwd"), fr.get("scale"))
+
+    def clear_frames(self):
+        self._check(lib().pt_clear_frames(self.h), "pt_clear_frames")
+
+    def _final_shape(self):
+        fl = self.params.finalLevel
+        return self.H >> fl, self.W >> fl
+
+    def synthesize_frame(self, frame):
+        h, w = self._final_shape()
+        rgba = np.empty((h, w, 4), np.float32)
+        offs = np.empty((h, w), _abi.PATCH_DTYPE)
+        self._check(lib().pt_synthesize_frame(self.h, frame, _p(rgba), _p(offs)), "pt_synthesize_frame")
+        return rgba, offs
+
+    def synthesize_animation(self, first, last):
+        results = {}
+
+        def cb(frame, rgba, offs, w, h, user):
+            a = np.ctypeslib.as_array(rgba, shape=(h, w, 4)).copy()
+            o = np.frombuffer(ctypes.string_at(offs, w * h * _abi.PATCH_DTYPE.itemsize),
+                              dtype=_abi.PATCH_DTYPE).reshape(h, w).copy()
+            results[frame] = (a, o)
+
+        cfn = FRAME_CB(cb)
+        self._check(lib().pt_synthesize_animation(self.h, first, last, ctypes.cast(cfn, ctypes.c_void_p), None),
+                    "pt_synthesize_animation")
+        return results

@@ -1,0 +1,39 @@
+"""Writes the committed fixtures of tests/golden.
+
+glibc_rand.npz: the C library's own rand() output after srand(seed) for the
+seeds createRandomPyramid uses (frame * level) -- produced by libc itself,
+not by the restatement.
+still48.npz: the oracle's result for a 48x48 still (r2, 3 levels, 2
+iterations), a regression lock of the oracle.
+"""
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+
+def main():
+    libc = ctypes.CDLL("libc.so.6")
+    vec = {}
+    for seed in (0, 1, 2, 4, 6, 12, 23, 46, 69, 92):
+        libc.srand(seed)
+        vec["seed_%d" % seed] = np.array([libc.rand() for _ in range(512)], np.int32)
+    np.savez_compressed(os.path.join(HERE, "glibc_rand.npz"), **vec)
+
+    from oracle import oracle as O
+    from painttween_gb300 import _abi, synthetic
+    p = _abi.default_params()
+    p.residualWindowSize, p.levels, p.iterations = 2, 3, 2
+    ex = synthetic.make_exemplar(48, 48, seed=101)
+    fr = synthetic.make_still(48, 48, 3, seed=102)
+    offs, res, out = O.OracleDriver(p, [ex], [fr], threads=4).render(0, 0)[0]
+    np.savez_compressed(os.path.join(HERE, "still48.npz"), offsets=offs, residual=res, output=out,
+                        ex_seed=101, fr_seed=102)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,324 @@
+"""Parity of the CUDA kernels (through the C ABI) with the CPU oracle.
+
+Integer and index work (random levels, offsets' layers, the pyramid
+indexing) and, by the shared FP32 arithmetic contract, the floating-point
+offsets, residuals and outputs are compared bit for bit.  The energy is also
+checked against the FP64 oracle within 1e-5 relative.
+"""
+import numpy as np
+import pytest
+
+from painttween_gb300 import Synthesizer, _abi, synthetic
+from oracle import oracle as O
+
+from _harness import Pair, assert_array_equal, assert_offsets_equal, config_params
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(gpu_lib):
+    return gpu_lib
+
+
+def _still_steps(pair, level, frame=0):
+    pair.load_style(level)
+    pair.load_frame(frame, level)
+    pair.random_level(frame, level)
+
+
+def test_random_level_and_randomize_bit_exact():
+    pair = Pair(64, 48, 64, 64, config_params())
+    try:
+        for level in (2, 1, 0):
+            _still_steps(pair, level, 0)
+            pair.both("randomize_offsets", level)
+            pair.compare(level, "randomize L%d" % level)
+    finally:
+        pair.close()
+
+
+@pytest.mark.parametrize("jump", [1, 2, 8, 128])
+def test_propagate_bit_exact(jump):
+    pair = Pair(64, 64, 64, 64, config_params())
+    try:
+        _still_steps(pair, 1)
+        pair.both("randomize_offsets", 1)
+        for _ in range(2):
+            pair.both("propagate", 1, jump)
+            pair.compare(1, "propagate jump %d" % jump)
+    finally:
+        pair.close()
+
+
+def test_scatter_bit_exact():
+    pair = Pair(64, 64, 64, 64, config_params())
+    try:
+        _still_steps(pair, 0)
+        pair.both("randomize_offsets", 0)
+        pair.both("propagate", 0, 4)
+        pair.both("scatter", 0)
+        pair.compare(0, "scatter")
+        pair.both("scatter", 0)
+        pair.compare(0, "scatter 2")
+    finally:
+        pair.close()
+
+
+def test_upsample_bit_exact_odd_sizes():
+    # odd sizes: the upsample reads one coarse row/column past the coarse
+    # rectangle (texSynth_kernel.cu:1468-1474)
+    pair = Pair(67, 45, 64, 64, config_params())
+    try:
+        _still_steps(pair, 1)
+        pair.both("randomize_offsets", 1)
+        pair.both("propagate", 1, 2)
+        _still_steps(pair, 0)
+        pair.both("upsample", 0)
+        pair.compare(0, "upsample", residual=True, output=False)
+        pair.both("sync", 0, 0)
+        pair.compare(0, "upsample+sync")
+    finally:
+        pair.close()
+
+
+@pytest.mark.parametrize("forwards", [True, False])
+def test_advect_and_merge_bit_exact(forwards):
+    p = config_params()
+    pair = Pair(64, 64, 64, 64, p, frames=3)
+    try:
+        level = 0
+        pair.load_style(level)
+        pair.both("reset_advected")
+        f0, f1 = (0, 1) if forwards else (2, 1)
+        pair.load_frame(f0, level)
+        pair.random_level(f0, level)
+        pair.both("randomize_offsets", level)
+        pair.both("propagate", level, 2)
+        pair.flip()
+        pair.load_frame(f1, level)
+        pair.random_level(f1, level)
+        pair.both("advect", level, 1, forwards, 0)
+        pair.compare(level, "advect")
+        pair.both("merge_randomly", level, forwards, 0.5, False)
+        pair.compare(level, "merge randomly")
+        pair.both("advect", level, 1, forwards, _abi.ADVECT_UPDATE_RESIDUAL)
+        pair.both("merge_using_residual", level, forwards)
+        pair.compare(level, "merge using residual")
+        # temporal terms active now (advected hysteresis > 0)
+        q = p.copy()
+        q.direction = _abi.FORWARD if forwards else _abi.BACKWARD
+        q.hysteresisWeight = 0.5
+        pair.set_params(q)
+        pair.both("propagate", level, 1)
+        pair.compare(level, "propagate with temporal terms")
+        pair.both("scatter", level)
+        pair.compare(level, "scatter with temporal terms")
+    finally:
+        pair.close()
+
+
+def test_all_energy_terms_bit_exact():
+    p = config_params(r=3)
+    p.distTransWeight = 1.0
+    p.styleObjIdWeight = 1.0
+    p.coherenceWeight = 0.5
+    p.offsetsHistogramSlope[0] = 1.0
+    p.offsetsHistogramThreshold[0] = -0.25  # makes the (always-empty) histogram term non-zero
+    ex = synthetic.make_exemplar(64, 64, seed=5)
+    ex["dist_trans"] = np.random.default_rng(3).uniform(0, 80, (64, 64)).astype(np.float32)
+    pair = Pair(64, 64, 64, 64, p, style=ex)
+    try:
+        _still_steps(pair, 0)
+        pair.both("randomize_offsets", 0)
+        pair.compare(0, "randomize (all terms)")
+        pair.both("propagate", 0, 4)
+        pair.compare(0, "propagate (all terms)")
+        pair.both("scatter", 0)
+        pair.compare(0, "scatter (all terms)")
+    finally:
+        pair.close()
+
+
+def test_transparent_exemplar_serial_random_level():
+    # transparent exemplar texels force the reference's retry loop; the GPU
+    # then draws the glibc sequence serially
+    ex = synthetic.make_exemplar(64, 64, seed=9)
+    ex["output"][:, :20, 3] = 0.2
+    ex["base"][:, :20, 3] = 0.2
+    pair = Pair(48, 48, 64, 64, config_params(), style=ex)
+    try:
+        for level in (1, 0):
+            _still_steps(pair, level)
+            pair.both("randomize_offsets", level)
+            pair.compare(level, "randomize transparent L%d" % level)
+    finally:
+        pair.close()
+
+
+def test_load_offsets_residual_half_roundtrip():
+    pair = Pair(32, 32, 32, 32, config_params())
+    try:
+        _still_steps(pair, 0)
+        pair.both("randomize_offsets", 0)
+        offs = pair.o.get_offsets(0)
+        offs["lumShiftA"] = 0.125
+        offs["lumShiftY"] = -0.25
+        res = np.random.default_rng(0).uniform(0, 70000, (32, 32)).astype(np.float32)
+        for side in (pair.o, pair.g):
+            side.load_offsets(0, offs)
+            side.load_residual(0, res)
+        assert_array_equal(pair.g.get_residual(0), pair.o.get_residual(0), "half residual")
+        assert_array_equal(pair.g.get_residual(0), res.astype(np.float16).astype(np.float32), "half vs numpy")
+        pair.both("sync", 0, _abi.DONT_COPY_OFFSETS | _abi.DONT_UPDATE_RESIDUAL)
+        pair.compare(0, "loaded offsets")
+    finally:
+        pair.close()
+
+
+def test_energy_matches_fp64_oracle():
+    """Per-pixel patch distance of the CUDA residual vs the FP64 oracle."""
+    pair = Pair(64, 64, 64, 64, config_params(r=3))
+    try:
+        _still_steps(pair, 0)
+        pair.both("randomize_offsets", 0)
+        pair.both("propagate", 0, 8)
+        offs = pair.g.get_offsets(0)
+        g = pair.g.get_residual(0).astype(np.float64)
+        _, e64 = pair.o.energy_map(0, offs, f32=False, f64=True)
+        mask = e64 > 0
+        rel = np.abs(g[mask] - e64[mask]) / np.maximum(np.abs(e64[mask]), 1e-3)
+        assert rel.max() <= 1e-5, rel.max()
+    finally:
+        pair.close()
+
+
+def _driver_pair(W, H, EW, EH, p, frames, seed):
+    ex = synthetic.make_exemplar(EW, EH, seed=seed)
+    clip = synthetic.make_clip(W, H, 3, frames, seed=seed + 1)
+    s = Synthesizer(device=0)
+    s.setup(p, W, H, EW, EH, 1)
+    s.set_style(0, ex["base"], ex["output"], ex["orient_tensor"], ex["dist_trans"], ex["object_ids"])
+    for i, fr in enumerate(clip):
+        s.set_frame_dict(i, fr)
+    d = O.OracleDriver(p, [ex], clip, threads=8)
+    return s, d
+
+
+def test_still_synthesis_driver_bit_exact():
+    p = config_params(r=2, levels=3, iterations=3)
+    s, d = _driver_pair(96, 80, 64, 64, p, 1, seed=21)
+    try:
+        rgba, offs = s.synthesize_frame(0)
+        ref = d.render(0, 0)[0]
+        assert_offsets_equal(offs, ref[0], 0.999, "still offsets")
+        assert np.abs(rgba - ref[2]).max() <= 1e-6
+        psnr = 10 * np.log10(1.0 / max(np.mean((rgba - ref[2]) ** 2), 1e-20))
+        assert psnr >= 40
+    finally:
+        s.close()
+
+
+def test_animation_driver_bit_exact():
+    p = config_params(r=2, levels=3, iterations=2)
+    p.temporalCoherenceWeight = 0.5
+    s, d = _driver_pair(64, 64, 64, 64, p, 4, seed=31)
+    try:
+        got = s.synthesize_animation(0, 3)
+        ref = d.render(0, 3)
+        for f in range(4):
+            assert_offsets_equal(got[f][1], ref[f][0], 0.999, "frame %d offsets" % f)
+            assert np.abs(got[f][0] - ref[f][2]).max() <= 1e-6
+    finally:
+        s.close()
+
+
+def test_animation_scheme_fmbm_residual_merge():
+    p = config_params(r=2, levels=2, iterations=2)
+    p.scheme = _abi.S_FMBM
+    s, d = _driver_pair(48, 48, 64, 64, p, 3, seed=41)
+    try:
+        got = s.synthesize_animation(0, 2)
+        ref = d.render(0, 2)
+        for f in range(3):
+            assert_offsets_equal(got[f][1], ref[f][0], 0.999, "FMBM frame %d" % f)
+    finally:
+        s.close()
+
+
+def test_still_config_256_full_size():
+    """The 256x256 still configuration at full size (r2, 3 levels, 4
+    iterations) against the oracle."""
+    cfg = synthetic.config("still256")
+    p = cfg["params"]
+    s, d = _driver_pair(cfg["w"], cfg["h"], cfg["ew"], cfg["eh"], p, 1, seed=7)
+    try:
+        rgba, offs = s.synthesize_frame(0)
+        ref = d.render(0, 0)[0]
+        assert_offsets_equal(offs, ref[0], 0.999, "still256 offsets")
+        psnr = 10 * np.log10(1.0 / max(np.mean((rgba - ref[2]) ** 2), 1e-20))
+        assert psnr >= 40
+    finally:
+        s.close()
+
+
+def test_determinism_and_residual_consistency_large():
+    """Size-independent properties on a larger frame: two runs are identical,
+    offsets stay inside the exemplar, and the stored residual equals a fresh
+    recomputation."""
+    p = config_params(r=3, levels=4, iterations=2)
+    ex = synthetic.make_exemplar(256, 256, seed=3)
+    fr = synthetic.make_still(640, 360, 6, seed=4)
+    outs = []
+    for _ in range(2):
+        s = Synthesizer(device=0)
+        s.setup(p, 640, 360, 256, 256, 1)
+        s.set_style(0, ex["base"], ex["output"], ex["orient_tensor"], ex["dist_trans"], ex["object_ids"])
+        s.set_frame_dict(0, fr)
+        outs.append(s.synthesize_frame(0))
+        res_before = s.get_residual(0)
+        s.update_residual_cache(0)
+        assert_array_equal(s.get_residual(0), res_before, "residual recomputation")
+        s.close()
+    assert_offsets_equal(outs[0][1], outs[1][1], 1.0, "repeat run")
+    o = outs[0][1]
+    active = o["hysteresis"] >= 0
+    assert np.isfinite(o["x"][active]).all()
+    assert (o["x"] >= 0).all() and (o["x"] <= 256).all() and (o["y"] >= 0).all() and (o["y"] <= 256).all()
+
+
+def test_counter_rng_mode_runs_and_is_deterministic():
+    p = config_params(r=2, levels=3, iterations=2)
+    p.rngMode = _abi.RNG_COUNTER
+    p.rngSeed = 1234
+    ex = synthetic.make_exemplar(64, 64, seed=2)
+    fr = synthetic.make_still(64, 64, 3, seed=3)
+    res = []
+    for _ in range(2):
+        s = Synthesizer(device=0)
+        s.setup(p, 64, 64, 64, 64, 1)
+        s.set_style(0, ex["base"], ex["output"], ex["orient_tensor"], ex["dist_trans"], ex["object_ids"])
+        s.set_frame_dict(0, fr)
+        res.append(s.synthesize_frame(0)[1])
+        s.close()
+    assert_offsets_equal(res[0], res[1], 1.0, "counter mode repeat")
+
+
+def test_errors_are_status_codes():
+    from painttween_gb300 import PaintTweenError, TexSynth
+    t = TexSynth(device=0)
+    with pytest.raises(PaintTweenError):
+        t.propagate(0, 1)  # before initialize
+    t.initialize(32, 32, 32, 32, 1)
+    with pytest.raises(PaintTweenError):
+        t.upload_image_color4(0, _abi.LAYER_INPUT_COLOR, np.zeros((10, 10, 4), np.float32))
+    p = config_params()
+    p.interpolateKeyFrame = 1
+    with pytest.raises(PaintTweenError):
+        t.set_params(p)
+    t.close()
+    tb = TexSynth(device=0, hbm_budget=1 << 20)
+    with pytest.raises(PaintTweenError) as e:
+        tb.initialize(1024, 1024, 256, 256, 1)
+    assert e.value.status == 7  # PT_ERR_BUDGET
+    tb.close()

@@ -1,0 +1,142 @@
+"""CPU tests of the oracle: pinned pieces (glibc rand, IEEE half), accuracy of
+the polynomial elementary functions, pyramid construction, and the
+committed golden fixtures."""
+import ctypes
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from painttween_gb300 import _abi, synthetic
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_glibc_stream_matches_libc_rand():
+    """The restated TYPE_3 generator reproduces the C library's rand()."""
+    libc = ctypes.CDLL("libc.so.6")
+    for seed in (0, 1, 2, 3, 17, 96, 1 << 20):
+        libc.srand(seed)
+        ref = np.array([libc.rand() for _ in range(2000)], np.int32)
+        assert (O.glibc_stream(seed, 2000) == ref).all(), seed
+
+
+def test_glibc_stream_matches_committed_vectors():
+    g = np.load(os.path.join(GOLDEN, "glibc_rand.npz"))
+    for key in g.files:
+        seed = int(key.split("_")[1])
+        assert (O.glibc_stream(seed, g[key].size) == g[key]).all(), key
+
+
+def test_half_roundtrip_matches_numpy():
+    rng = np.random.default_rng(0)
+    v = np.concatenate([rng.normal(0, 1, 20000) * 10.0 ** rng.integers(-9, 6, 20000),
+                        [0.0, -0.0, 65504.0, 65519.9, 65520.0, 1e31, 6.1e-5, 5.96e-8, 2.98e-8, 1e-9]]).astype(np.float32)
+    lib = O.lib()
+    got = np.array([lib.pto_half_roundtrip(float(x)) for x in v], np.float32)
+    ref = v.astype(np.float16).astype(np.float32)
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
+def test_polynomial_functions_accuracy():
+    lib = O.lib()
+    t = np.linspace(-9.0, 9.0, 4001).astype(np.float32)
+    s = np.array([lib.pto_sinf(float(x)) for x in t])
+    c = np.array([lib.pto_cosf(float(x)) for x in t])
+    assert np.abs(s - np.sin(t.astype(np.float64))).max() < 2.5e-7
+    assert np.abs(c - np.cos(t.astype(np.float64))).max() < 2.5e-7
+    assert lib.pto_sinf(0.0) == 0.0 and lib.pto_cosf(0.0) == 1.0
+    rng = np.random.default_rng(1)
+    ys, xs = rng.normal(size=2000).astype(np.float32), rng.normal(size=2000).astype(np.float32)
+    a = np.array([lib.pto_atan2f(float(y), float(x)) for y, x in zip(ys, xs)])
+    assert np.abs(a - np.arctan2(ys.astype(np.float64), xs.astype(np.float64))).max() < 5e-7
+    assert lib.pto_atan2f(0.0, 0.0) == 0.0
+    xl = np.exp(rng.uniform(-20, 20, 2000)).astype(np.float32)
+    lg = np.array([lib.pto_logf(float(x)) for x in xl])
+    assert np.abs(lg - np.log(xl.astype(np.float64))).max() < 5e-6
+    xc = rng.uniform(-1, 1, 2000).astype(np.float32)
+    ac = np.array([lib.pto_acosf(float(x)) for x in xc])
+    assert np.abs(ac - np.arccos(xc.astype(np.float64))).max() < 1e-6
+    assert math.isnan(lib.pto_acosf(1.5))
+
+
+def test_pyramids():
+    rng = np.random.default_rng(2)
+    img = rng.random((37, 50, 4), dtype=np.float32)
+    pyr = O.pyramid_avg(img)
+    assert len(pyr) == 5 and pyr[1].shape == (18, 25, 4)
+    a = img[0:36:2, 0:50:2] + img[0:36:2, 1:50:2]
+    b = a + img[1:36:2, 0:50:2]
+    ref = ((b + img[1:36:2, 1:50:2]) * np.float32(0.25)).astype(np.float32)
+    assert np.array_equal(pyr[1], ref)
+    vel = O.pyramid_avg(img[..., :2], vel=True)
+    assert np.array_equal(vel[1], ref[..., :2] * np.float32(0.5))
+    ids = np.array([[1, 2, 3, 3], [2, 1, 3, 4]], np.int32)
+    v = O.pyramid_vote(np.tile(ids, (2, 2)))
+    assert v[1][0, 0] == 1 and v[1][0, 1] == 3  # 2-2 tie -> smaller id; 3 wins
+    ang = O.tensor_to_angle(np.array([[[1.0, 0.0, 0.0], [0.0, 0.0, 1.0], [0.5, 0.5, 0.5]]], np.float32))
+    assert np.allclose(ang, [[-np.pi / 2, 0.0, -np.pi / 4]], atol=1e-6)
+
+
+def test_random_level_uses_rand_sequence():
+    """createRandomPyramid draws (x, y, fx, fy) per pixel in scan order."""
+    h, w = 3, 5
+    img = np.ones((h, w, 4), np.float32)
+    orient = np.zeros((h, w), np.float32)
+    ex_out = np.ones((16, 16, 4), np.float32)
+    ex_or = np.zeros((16, 16), np.float32)
+    rnd = O.random_level(7 * 2, 2, 64, 64, img, orient, ex_out, ex_or)
+    s = O.glibc_stream(14, 4 * w * h).reshape(h, w, 4)
+    assert np.array_equal(rnd[..., 0], (s[..., 0] % 15).astype(np.float32) + s[..., 2].astype(np.float32) / np.float32(2147483647))
+    assert np.array_equal(rnd[..., 1], (s[..., 1] % 15).astype(np.float32) + s[..., 3].astype(np.float32) / np.float32(2147483647))
+
+
+def test_oracle_still_matches_golden_fixture():
+    """Regression lock of the oracle on a small still (fixture written by
+    tests/golden/make_golden.py)."""
+    g = np.load(os.path.join(GOLDEN, "still48.npz"))
+    p = _abi.default_params()
+    p.residualWindowSize, p.levels, p.iterations = 2, 3, 2
+    ex = synthetic.make_exemplar(48, 48, seed=int(g["ex_seed"]))
+    fr = synthetic.make_still(48, 48, 3, seed=int(g["fr_seed"]))
+    d = O.OracleDriver(p, [ex], [fr], threads=4)
+    offs, res, out = d.render(0, 0)[0]
+    assert np.array_equal(offs.view(np.uint8), g["offsets"].view(np.uint8))
+    assert np.array_equal(res, g["residual"])
+    assert np.array_equal(out, g["output"])
+
+
+def test_energy_fp32_close_to_fp64():
+    p = _abi.default_params()
+    p.residualWindowSize, p.levels, p.iterations = 3, 2, 2
+    ex = synthetic.make_exemplar(48, 48, seed=4)
+    fr = synthetic.make_still(48, 48, 3, seed=5)
+    d = O.OracleDriver(p, [ex], [fr], threads=4)
+    offs = d.render(0, 0)[0][0]
+    e32, e64 = d.o.energy_map(0, offs)
+    m = e64 > 0
+    rel = np.abs(e32[m] - e64[m]) / np.maximum(e64[m], 1e-3)
+    assert rel.max() < 1e-5
+
+
+def test_oracle_openmp_threads_agree():
+    p = _abi.default_params()
+    p.residualWindowSize, p.levels, p.iterations = 2, 2, 2
+    ex = synthetic.make_exemplar(32, 32, seed=8)
+    fr = synthetic.make_still(40, 32, 2, seed=9)
+    a = O.OracleDriver(p, [ex], [fr], threads=1).render(0, 0)[0][0]
+    b = O.OracleDriver(p, [ex], [fr], threads=4).render(0, 0)[0][0]
+    assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+def test_animation_oracle_runs():
+    p = _abi.default_params()
+    p.residualWindowSize, p.levels, p.iterations = 2, 2, 1
+    ex = synthetic.make_exemplar(32, 32, seed=1)
+    clip = synthetic.make_clip(32, 32, 2, 3, seed=2)
+    res = O.OracleDriver(p, [ex], clip, threads=4).render(0, 2)
+    assert sorted(res) == [0, 1, 2]
+    for f in res:
+        assert np.isfinite(res[f][2]).all()
