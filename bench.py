@@ -1,0 +1,410 @@
+#!/usr/bin/env python3
+"""Benchmark: 1080p stylised frames/s of PaintTween's offset-field synthesis.
+
+Workload (one "step"): the 24-frame 1920x1080 clip with a 1024x1024 exemplar
+(6 moving discs, 4 object IDs), patch radius 3, 5 pyramid levels, 6
+iterations per level, histogram term on, forward + backward consecutive
+passes (FMBM_RM) -- synthesised end to end by the CUDA library.
+
+  value  frames/s with the frame pyramids already resident in HBM (device
+         time from CUDA events on the library's stream, max over ranks)
+  e2e    frames/s through the C ABI with host buffers: every step uploads
+         the 24 frames (H2D, pyramids built on the device) and reads back
+         every frame's output and offsets (D2H)
+  roofline  the dominant kernel (propagate) from per-launch CUDA events and
+         counted patch-distance evaluations of the same timed steps
+  cpu_baseline  the CPU oracle (a scalar C restatement of the reference's
+         kernels; the reference has no CPU path) on a bounded sample
+
+`--impl reference` times that CPU restatement alone (the reference's CUDA
+code cannot be built with CUDA 13), each step one bounded sample.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from painttween_gb300 import _abi, synthetic  # noqa: E402
+
+WORKLOAD = "clip1080p"
+METRIC = "1080p stylized frames/s"
+UNIT = "frames/s"
+
+# DRAM bytes per patch-distance evaluation of the propagate kernel, from the
+# ncu capture summarised in profiles/propagate_clip1080p.md (None until a
+# capture exists).
+PROPAGATE_DRAM_BYTES_PER_EVAL = None
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Replicas only: each rank synthesises its own clip on its own GPU; a
+    gloo group supplies the barrier and the max over ranks."""
+
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def max(self, v):
+        if self.ws == 1:
+            return v
+        import torch
+        t = torch.tensor([float(v)])
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.td.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# inputs and the analytic evaluation count of the schedule
+# ---------------------------------------------------------------------------
+
+def make_inputs(cfg, frames, seed=2026):
+    ex = synthetic.make_exemplar(cfg["ew"], cfg["eh"], seed=seed)
+    clip = synthetic.make_clip(cfg["w"], cfg["h"], cfg["discs"], frames, seed=seed + 1)
+    return ex, clip
+
+
+def active_pixels(clip, levels, cull):
+    """Non-culled pixels (image DT <= cull) per frame and level, with the DT
+    pyramid built like the reference (2x2 average)."""
+    out = []
+    for fr in clip:
+        dt = fr["dist_trans"].astype(np.float32)
+        per = []
+        for lv in range(levels):
+            per.append(int((dt <= np.float32(cull)).sum()))
+            h, w = dt.shape
+            a = dt[0:h - h % 2:2, 0:w - w % 2:2] + dt[0:h - h % 2:2, 1:w - w % 2:2]
+            a = a + dt[1:h - h % 2:2, 0:w - w % 2:2]
+            dt = ((a + dt[1:h - h % 2:2, 1:w - w % 2:2]) * np.float32(0.25)).astype(np.float32)
+        out.append(per)
+    return out
+
+
+def scatter_samples(ew, eh, count=25):
+    """Candidates of the scatter chain: dist = 0.9^i * max(w, h) (float32)
+    while 0.9 * dist >= 10, at most scatterSamplesCount."""
+    f = np.float32
+    dist, n = f(max(ew, eh)), 0
+    while n < count and f(dist * f(0.9)) >= f(10.0):
+        dist = f(dist * f(0.9))
+        n += 1
+    return n
+
+
+def evals_per_step(p, cfg, act, frames):
+    """Patch-distance evaluations of one clip synthesis (exemplar DT 0 and
+    alpha 1: no candidate is rejected before evaluation)."""
+    total = 0
+    it = p.iterations
+    for lv in range(p.levels):
+        s = scatter_samples(cfg["ew"] >> lv, cfg["eh"] >> lv, p.scatterSamplesCount)
+        per_px = it * 9 * (4 + 1) + (it - 1) * ((s + 1) + 1)  # propagates/scatters + their syncs
+        for f in range(frames):
+            a = act[f][lv]
+            # pass 0: random/upsample sync + (merge sync) + final sync
+            extra0 = 2 if (f == 0) else (3 if lv < p.levels - 1 else 1)
+            total += a * (per_px + extra0)
+            if f != frames - 1:  # pass 1 (backward): merge sync + final sync
+                total += a * (per_px + 2)
+    return total
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU arms
+# ---------------------------------------------------------------------------
+
+def cpu_sample(cfg, p, ex, clip, threads, passes=1):
+    """The CPU oracle on one level-0 propagate pass (jump 8) of frame 0 at
+    full size; returns (evaluations/s, description)."""
+    from oracle import oracle as O
+    o = O.Oracle(cfg["w"], cfg["h"], cfg["ew"], cfg["eh"], 1, threads=threads)
+    q = p.copy()
+    q.direction = _abi.FORWARD
+    o.set_params(q)
+    sp = O.style_pyramids(ex)
+    fp = O.frame_pyramids(clip[0])
+    o.load_style_level([sp], 0)
+    o.load_frame_level(fp, 0)
+    rnd = O.random_level(0, 0, cfg["ew"], cfg["eh"], fp["rgba"][0], fp["orient"][0], sp["output"][0],
+                         sp["orient"][0])
+    o.upload_random(rnd)
+    o.randomize_offsets(0)
+    act = int((fp["dt"][0] <= np.float32(p.distTransCull)).sum())
+    lib = O.lib()
+    t0 = time.perf_counter()
+    for _ in range(passes):
+        lib.pto_propagate(o.h, 0, 8)
+    dt = time.perf_counter() - t0
+    o.close()
+    evals = 4 * act * passes
+    desc = ("%d level-0 propagate pass(es) (4 candidates x %d active pixels, r=%d) of frame 0 of the "
+            "1920x1080 clip" % (passes, act, p.residualWindowSize))
+    return evals / dt, desc, dt
+
+
+def run_reference(args, dist):
+    cfg = synthetic.config(WORKLOAD)
+    p = cfg["params"]
+    frames = args.frames or cfg["frames"]
+    if dist.rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    ex, clip = make_inputs(cfg, frames)
+    act = active_pixels(clip, p.levels, p.distTransCull)
+    per_step_evals = evals_per_step(p, cfg, act, frames)
+    rates = []
+    for i in range(args.warmup + args.steps):
+        rate, desc, _ = cpu_sample(cfg, p, ex, clip, threads)
+        if i >= args.warmup:
+            rates.append(rate)
+    rate = float(np.mean(rates))
+    fps = rate / (per_step_evals / frames)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": fps, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * frames / fps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "frames": frames, "image": "1920x1080", "exemplar": "1024x1024",
+                   "patch_radius": p.residualWindowSize, "levels": p.levels, "iterations": p.iterations},
+        "cpu_baseline": {"value": fps, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": desc + "; frames/s = evaluations/s / evaluations per frame of the schedule"},
+        "e2e": {"value": fps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "evals_per_s": rate,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+
+def run_ours(args, dist):
+    from painttween_gb300 import Synthesizer
+    from painttween_gb300 import build as B
+    B.build()
+    cfg = synthetic.config(WORKLOAD)
+    p = cfg["params"]
+    frames = args.frames or cfg["frames"]
+    device = dist.local
+    ex, clip = make_inputs(cfg, frames, seed=2026 + dist.rank)
+    s = Synthesizer(device=device)
+    s.setup(p, cfg["w"], cfg["h"], cfg["ew"], cfg["eh"], 1)
+    s.set_style(0, ex["base"], ex["output"], ex["orient_tensor"], ex["dist_trans"], ex["object_ids"])
+    for i, fr in enumerate(clip):
+        s.set_frame_dict(i, fr)
+
+    def render():
+        s._check(__import__("painttween_gb300._lib", fromlist=["lib"]).lib().pt_synthesize_animation(
+            s.h, 0, frames - 1, None, None), "pt_synthesize_animation")
+
+    for _ in range(args.warmup):
+        render()
+    s.synchronize()
+    dist.barrier()
+
+    clocks = Clocks(device)
+    clocks.start()
+    s.set_profiling(True)
+    l0 = s.kernel_launches
+    times = []
+    for _ in range(args.steps):
+        s.timer_record(0)
+        render()
+        s.timer_record(1)
+        times.append(s.timer_elapsed(0, 1))
+    launches = s.kernel_launches - l0
+    stats = {k: s.kernel_stats(k) for k in range(4)}
+    s.set_profiling(False)
+    ck = clocks.stop()
+    total_ms = dist.max(sum(times))
+    dist.barrier()
+
+    # end to end through the C ABI with host buffers
+    e2e_times = []
+    h2d = sum(fr[k].nbytes for fr in clip for k in ("rgba", "orient_tensor", "dist_trans", "object_ids",
+                                                       "vel_fwd", "vel_bwd", "scale"))
+    h, w = cfg["h"] >> p.finalLevel, cfg["w"] >> p.finalLevel
+    d2h = frames * h * w * (16 + 36)
+    for _ in range(args.e2e_steps):
+        s.synchronize()
+        t0 = time.perf_counter()
+        s.timer_record(2)
+        for i, fr in enumerate(clip):
+            s.set_frame_dict(i, fr)
+        out = s.synthesize_animation(0, frames - 1)
+        s.timer_record(3)
+        e2e_times.append(max(s.timer_elapsed(2, 3), 1000.0 * (time.perf_counter() - t0)))
+        assert len(out) == frames
+    e2e_ms = dist.max(float(np.mean(e2e_times)) * args.steps) if e2e_times else None
+
+    # roofline of the dominant kernel (propagate)
+    st = stats[_abi.KERNEL_PROPAGATE]
+    r = p.residualWindowSize
+    K = (2 * r + 1) ** 2
+    bytes_per_eval = 32 * K + 16
+    flops_per_eval = 84 * K + 40
+    avg_launch_s = st["total_ms"] / max(st["launches"], 1) / 1000.0
+    evals_per_launch = st["energy_evals"] / max(st["launches"], 1)
+    achieved = evals_per_launch * bytes_per_eval / avg_launch_s / 1e9
+    hbm, peak_kind = peaks()
+    sm_mhz = (ck or {}).get("sm_mhz") or 1900.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fp32_achieved = evals_per_launch * flops_per_eval / avg_launch_s / 1e12
+    traffic = (None if PROPAGATE_DRAM_BYTES_PER_EVAL is None
+               else PROPAGATE_DRAM_BYTES_PER_EVAL * evals_per_launch)
+    kernel_share = st["total_ms"] / max(sum(v["total_ms"] for v in stats.values()), 1e-9)
+
+    value = dist.ws * frames * args.steps / (total_ms / 1000.0)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "frames": frames, "image": "%dx%d" % (cfg["w"], cfg["h"]),
+                   "exemplar": "%dx%d" % (cfg["ew"], cfg["eh"]), "patch_radius": r, "levels": p.levels,
+                   "iterations": p.iterations, "scheme": "FMBM_RM", "histogram": True,
+                   "parallelism": "replicas" if dist.ws > 1 else "single",
+                   "l2": "inputs larger than L2 (%.1f GB of resident frame pyramids per step)"
+                         % (s.device_bytes / 1e9)},
+        "e2e": ({"value": dist.ws * frames * args.steps / (e2e_ms / 1000.0), "unit": UNIT,
+                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)} if e2e_ms else None),
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": "k_propagate", "bytes_per_eval": bytes_per_eval,
+                     "evals_per_launch": evals_per_launch, "avg_launch_ms": avg_launch_s * 1000.0,
+                     "time_share": kernel_share,
+                     "fp32": {"achieved_tflops": fp32_achieved, "peak_tflops": fp32_peak,
+                              "frac": fp32_achieved / fp32_peak, "flops_per_eval": flops_per_eval,
+                              "peak_kind": "nominal 152 SM x 128 lanes x 2 at the sampled SM clock"}},
+        "kernels": {name: stats[k] for k, name in enumerate(["propagate", "scatter", "residual", "canvas"])},
+    }
+    if ck:
+        line["clocks"] = ck
+    if dist.rank == 0 and dist.ws == 1 and not args.no_cpu_baseline:
+        act = active_pixels(clip, p.levels, p.distTransCull)
+        per_frame = evals_per_step(p, cfg, act, frames) / frames
+        counted = sum(v["energy_evals"] for v in stats.values()) / (frames * args.steps)
+        threads = os.cpu_count() or 1
+        rate, desc, _ = cpu_sample(cfg, p, ex, clip, threads)
+        line["cpu_baseline"] = {"value": rate / per_frame, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": desc + "; frames/s = evaluations/s / evaluations per frame",
+                                "evals_per_s": rate}
+        line["evals_per_frame"] = {"schedule": per_frame, "counted": counted}
+    s.close()
+    if dist.rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--frames", type=int, default=0, help="override the clip length (testing only)")
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            return run_reference(args, dist)
+        return run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

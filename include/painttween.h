@@ -286,6 +286,29 @@ pt_status pt_synthesize_animation(pt_ctx* ctx, int first, int last,
 
 /* Number of this library's kernel launches issued so far by the context. */
 uint64_t pt_kernel_launches(const pt_ctx* ctx);
+
+/* ---- measurement (no counterpart in the reference, which has no GPU
+ *      timers; its Stats/ScopeTimer are host wall clocks, stats.h:41-182) -- */
+#define PT_TIMER_SLOTS 16
+/* Records CUDA event `slot` (0..15) on the context's stream. */
+pt_status pt_timer_record(pt_ctx* ctx, int slot);
+/* Waits for both events and returns the time between them in ms. */
+pt_status pt_timer_elapsed(pt_ctx* ctx, int slot_a, int slot_b, float* ms);
+
+/* Kernels whose launches are timed when profiling is on. */
+enum { PT_KERNEL_PROPAGATE = 0, PT_KERNEL_SCATTER = 1, PT_KERNEL_RESIDUAL = 2,
+       PT_KERNEL_CANVAS = 3, PT_KERNEL_COUNT = 4 };
+typedef struct {
+    uint64_t launches;        /* launches since profiling was switched on */
+    double total_ms;          /* sum of per-launch CUDA-event durations */
+    uint64_t energy_evals;    /* patch-distance evaluations performed */
+    uint64_t taps;            /* taps summed over those evaluations */
+} pt_kernel_stats;
+/* Switches per-launch event timing and patch-distance counting on or off
+ * (and clears the statistics). */
+pt_status pt_set_profiling(pt_ctx* ctx, int on);
+/* Statistics of one kernel (waits for the stream). */
+pt_status pt_get_kernel_stats(pt_ctx* ctx, int kernel, pt_kernel_stats* out);
 /* Blocks until the context's stream is idle. */
 pt_status pt_synchronize(pt_ctx* ctx);
 

@@ -58,6 +58,10 @@ SIGNATURES = {
     "pt_synthesize_animation": (_I, [_VP, _I, _I, _VP, _VP]),
     "pt_kernel_launches": (ctypes.c_uint64, [_VP]),
     "pt_synchronize": (_I, [_VP]),
+    "pt_timer_record": (_I, [_VP, _I]),
+    "pt_timer_elapsed": (_I, [_VP, _I, _I, ctypes.POINTER(ctypes.c_float)]),
+    "pt_set_profiling": (_I, [_VP, _I]),
+    "pt_get_kernel_stats": (_I, [_VP, _I, ctypes.POINTER(_abi.KernelStats)]),
 }
 
 

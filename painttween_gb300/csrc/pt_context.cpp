@@ -122,6 +122,13 @@ struct pt_ctx {
 
     uint64_t launches = 0;
     uint32_t pass_counter = 0;
+
+    // measurement
+    cudaEvent_t timers[PT_TIMER_SLOTS] = {};
+    bool profiling = false;
+    unsigned long long* counters = nullptr;  // [kernel][evals, taps]
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pairs[PT_KERNEL_COUNT];
     std::map<int, std::vector<uint32_t>> jump_cache;  // M^(4w)
 };
 
@@ -334,10 +341,42 @@ static bool histogram_on(pt_ctx* c) {
     return false;
 }
 
+// ---------------------------------------------------------------------------
+// profiled launches: an event pair around the launch and the kernel's own
+// evaluation counters
+// ---------------------------------------------------------------------------
+
+static cudaEvent_t pool_event(pt_ctx* c) {
+    if (!c->ev_pool.empty()) {
+        cudaEvent_t e = c->ev_pool.back();
+        c->ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+template <class F>
+static pt_status profiled(pt_ctx* c, int kernel, Params& P, F&& launch) {
+    if (!c->profiling) {
+        LN(launch(P));
+        return PT_OK;
+    }
+    P.counters = c->counters + 2 * kernel;
+    cudaEvent_t a = pool_event(c), b = pool_event(c);
+    if (!a || !b) return fail(c, PT_ERR_CUDA, "cudaEventCreate failed");
+    CU(cudaEventRecord(a, c->stream));
+    LN(launch(P));
+    CU(cudaEventRecord(b, c->stream));
+    c->ev_pairs[kernel].push_back(std::make_pair(a, b));
+    return PT_OK;
+}
+
 static pt_status do_residual(pt_ctx* c, int level) {
     Params P = make_params(c, level);
-    LN(pt::launch_residual(P, c->res[c->res_i], c->stream));
-    return PT_OK;
+    float* out = c->res[c->res_i];
+    return profiled(c, PT_KERNEL_RESIDUAL, P, [&](const Params& Q) { return pt::launch_residual(Q, out, c->stream); });
 }
 
 // TexSynth::syncBuffers, texSynth_kernel.cu:1240-1303
@@ -354,7 +393,7 @@ static pt_status do_sync(pt_ctx* c, int level, int flags) {
         LN(pt::launch_conv(c->hist[1], c->hist[0], hw, hh, c->SW, 0, c->hist_kernel, c->stream));
     }
     Params P = make_params(c, level);
-    LN(pt::launch_canvas(P, c->canvas, c->stream));
+    TRY(profiled(c, PT_KERNEL_CANVAS, P, [&](const Params& Q) { return pt::launch_canvas(Q, c->canvas, c->stream); }));
     if (!(flags & PT_DONT_UPDATE_RESIDUAL)) TRY(do_residual(c, level));
     return PT_OK;
 }
@@ -509,6 +548,11 @@ pt_status pt_destroy(pt_ctx* c) {
     if (!c) return PT_ERR_INVALID;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    for (auto& e : c->timers)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : c->ev_pool) cudaEventDestroy(e);
+    for (auto& v : c->ev_pairs)
+        for (auto& pr : v) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
     for (auto& kv : c->allocs) cudaFree(kv.first);
     c->allocs.clear();
     cudaStreamDestroy(c->stream);
@@ -860,7 +904,8 @@ pt_status pt_propagate(pt_ctx* c, int level, int jump, int key_index) {
     if (key_index >= 0) return fail(c, PT_ERR_UNSUPPORTED, "keyframe propagation is not implemented");
     PatchPlanes work = writable_work(c, nullptr);
     Params P = make_params(c, level);
-    LN(pt::launch_propagate(P, work, jump, c->stream));
+    TRY(profiled(c, PT_KERNEL_PROPAGATE, P,
+                 [&](const Params& Q) { return pt::launch_propagate(Q, work, jump, c->stream); }));
     return do_sync(c, level, 0);
 }
 
@@ -871,7 +916,10 @@ pt_status pt_scatter(pt_ctx* c, int level, int key_index) {
     bool aliased = false;
     PatchPlanes work = writable_work(c, &aliased);
     Params P = make_params(c, level);
-    LN(pt::launch_scatter(P, work, aliased ? 1 : 0, c->pass_counter++, c->stream));
+    uint32_t pass_id = c->pass_counter++;
+    TRY(profiled(c, PT_KERNEL_SCATTER, P, [&](const Params& Q) {
+        return pt::launch_scatter(Q, work, aliased ? 1 : 0, pass_id, c->stream);
+    }));
     return do_sync(c, level, 0);
 }
 
@@ -1161,6 +1209,62 @@ pt_status pt_clear_frames(pt_ctx* c) {
     if (!c) return PT_ERR_INVALID;
     CU(cudaStreamSynchronize(c->stream));
     free_frames(c);
+    return PT_OK;
+}
+
+// --- measurement ----------------------------------------------------------------
+
+pt_status pt_timer_record(pt_ctx* c, int slot) {
+    if (!c || slot < 0 || slot >= PT_TIMER_SLOTS) return PT_ERR_INVALID;
+    if (!c->timers[slot]) CU(cudaEventCreate(&c->timers[slot]));
+    CU(cudaEventRecord(c->timers[slot], c->stream));
+    return PT_OK;
+}
+
+pt_status pt_timer_elapsed(pt_ctx* c, int a, int b, float* ms) {
+    if (!c || !ms || a < 0 || b < 0 || a >= PT_TIMER_SLOTS || b >= PT_TIMER_SLOTS) return PT_ERR_INVALID;
+    if (!c->timers[a] || !c->timers[b]) return fail(c, PT_ERR_STATE, "timer slot not recorded");
+    CU(cudaEventSynchronize(c->timers[b]));
+    CU(cudaEventElapsedTime(ms, c->timers[a], c->timers[b]));
+    return PT_OK;
+}
+
+static void clear_profile(pt_ctx* c) {
+    for (auto& v : c->ev_pairs) {
+        for (auto& pr : v) {
+            c->ev_pool.push_back(pr.first);
+            c->ev_pool.push_back(pr.second);
+        }
+        v.clear();
+    }
+}
+
+pt_status pt_set_profiling(pt_ctx* c, int on) {
+    if (!c) return PT_ERR_INVALID;
+    CU(cudaStreamSynchronize(c->stream));
+    clear_profile(c);
+    if (!c->counters) TRY(dalloc_t(c, &c->counters, 2 * PT_KERNEL_COUNT));
+    CU(cudaMemsetAsync(c->counters, 0, 2 * PT_KERNEL_COUNT * sizeof(unsigned long long), c->stream));
+    c->profiling = on != 0;
+    return PT_OK;
+}
+
+pt_status pt_get_kernel_stats(pt_ctx* c, int kernel, pt_kernel_stats* out) {
+    if (!c || !out || kernel < 0 || kernel >= PT_KERNEL_COUNT) return PT_ERR_INVALID;
+    CU(cudaStreamSynchronize(c->stream));
+    memset(out, 0, sizeof(*out));
+    for (auto& pr : c->ev_pairs[kernel]) {
+        float ms = 0.f;
+        CU(cudaEventElapsedTime(&ms, pr.first, pr.second));
+        out->total_ms += ms;
+        out->launches++;
+    }
+    if (c->counters) {
+        unsigned long long h[2] = {0, 0};
+        CU(cudaMemcpy(h, c->counters + 2 * kernel, sizeof(h), cudaMemcpyDeviceToHost));
+        out->energy_evals = h[0];
+        out->taps = h[1];
+    }
     return PT_OK;
 }
 

@@ -221,6 +221,25 @@ __device__ float energy(const Params& P, int x, int y, const Patch& t, const Pix
     return sum / sumW;
 }
 
+// profiling: one patch-distance evaluation and its in-rectangle taps,
+// aggregated over the lanes that are active at this point
+__device__ __forceinline__ unsigned lane_id() {
+    unsigned l;
+    asm volatile("mov.u32 %0, %%laneid;" : "=r"(l));
+    return l;
+}
+__device__ __forceinline__ void count_eval(const Params& P, int x, int y) {
+    int x0 = max(x - P.r, 0), x1 = min(x + P.r, P.lw - 1);
+    int y0 = max(y - P.r, 0), y1 = min(y + P.r, P.lh - 1);
+    unsigned taps = (unsigned)((x1 - x0 + 1) * (y1 - y0 + 1));
+    unsigned mask = __activemask();
+    unsigned tsum = __reduce_add_sync(mask, taps);
+    if (lane_id() == (unsigned)(__ffs(mask) - 1)) {
+        atomicAdd(&P.counters[0], (unsigned long long)__popc(mask));
+        atomicAdd(&P.counters[1], (unsigned long long)tsum);
+    }
+}
+
 // test_offset + isExemplarPixelCulled, :200-205,695-721
 __device__ float test_offset(const Params& P, int x, int y, const Patch& t, float image_alpha, const PixCtx& pc) {
     float dte = ex_texel_dt(P.ex, f2i(t.x), f2i(t.y), t.layer);
@@ -229,6 +248,7 @@ __device__ float test_offset(const Params& P, int x, int y, const Patch& t, floa
             float ea = ex_sample_out_alpha(P.ex, t.x, t.y, t.layer);
             if (ea < kAlphaThreshold && image_alpha > kAlphaThreshold) return kBigResidual;
         }
+        if (P.counters) count_eval(P, x, y);
         return energy(P, x, y, t, pc);
     }
     return kBigResidual;
@@ -369,6 +389,7 @@ __global__ void __launch_bounds__(128) k_residual(const Params P, float* out) {
     PixCtx pc;
     make_pixctx(P, x, y, &pc);
     Patch t = load_patch(P.off, k);
+    if (P.counters) count_eval(P, x, y);
     out[k] = energy(P, x, y, t, pc);
 }
 

@@ -77,6 +77,23 @@ class TexSynth:
     def synchronize(self):
         self._check(lib().pt_synchronize(self.h), "pt_synchronize")
 
+    # -- measurement (CUDA events on the context's stream) -----------------------
+    def timer_record(self, slot):
+        self._check(lib().pt_timer_record(self.h, slot), "pt_timer_record")
+
+    def timer_elapsed(self, a, b):
+        ms = ctypes.c_float()
+        self._check(lib().pt_timer_elapsed(self.h, a, b, ctypes.byref(ms)), "pt_timer_elapsed")
+        return ms.value
+
+    def set_profiling(self, on):
+        self._check(lib().pt_set_profiling(self.h, int(on)), "pt_set_profiling")
+
+    def kernel_stats(self, kernel):
+        st = _abi.KernelStats()
+        self._check(lib().pt_get_kernel_stats(self.h, kernel, ctypes.byref(st)), "pt_get_kernel_stats")
+        return dict(launches=st.launches, total_ms=st.total_ms, energy_evals=st.energy_evals, taps=st.taps)
+
     # -- configuration (TexSynth::setup / uploadParameters) ----------------------
     def set_params(self, params):
         self.params = params.copy()

@@ -169,7 +169,9 @@ def test_load_offsets_residual_half_roundtrip():
             side.load_offsets(0, offs)
             side.load_residual(0, res)
         assert_array_equal(pair.g.get_residual(0), pair.o.get_residual(0), "half residual")
-        assert_array_equal(pair.g.get_residual(0), res.astype(np.float16).astype(np.float32), "half vs numpy")
+        with np.errstate(over="ignore"):
+            half = res.astype(np.float16).astype(np.float32)
+        assert_array_equal(pair.g.get_residual(0), half, "half vs numpy")
         pair.both("sync", 0, _abi.DONT_COPY_OFFSETS | _abi.DONT_UPDATE_RESIDUAL)
         pair.compare(0, "loaded offsets")
     finally:
@@ -282,9 +284,12 @@ def test_determinism_and_residual_consistency_large():
         s.close()
     assert_offsets_equal(outs[0][1], outs[1][1], 1.0, "repeat run")
     o = outs[0][1]
-    active = o["hysteresis"] >= 0
-    assert np.isfinite(o["x"][active]).all()
-    assert (o["x"] >= 0).all() and (o["x"] <= 256).all() and (o["y"] >= 0).all() and (o["y"] <= 256).all()
+    assert np.isfinite(o["x"]).all() and np.isfinite(o["y"]).all()
+    # offsetUpsampleNearest clamps in coarse coordinates to the fine exemplar
+    # size before doubling (texSynth_kernel.cu:1411-1414), so coordinates can
+    # reach 2 * (w - 1) + 0.5
+    assert (o["x"] >= 0).all() and (o["x"] <= 2 * 255 + 0.5).all()
+    assert (o["y"] >= 0).all() and (o["y"] <= 2 * 255 + 0.5).all()
 
 
 def test_counter_rng_mode_runs_and_is_deterministic():
