@@ -307,6 +307,11 @@ typedef struct {
 /* Switches per-launch event timing and patch-distance counting on or off
  * (and clears the statistics). */
 pt_status pt_set_profiling(pt_ctx* ctx, int on);
+/* Selects the kernels of the patch-distance passes: 1 (default) = the tiled
+ * shared-memory kernels where an instantiation exists (patch radius 2-4, no
+ * coherence term, one temporal direction), 0 = the generic kernels
+ * everywhere.  Both compute identical results. */
+pt_status pt_set_tiled_kernels(pt_ctx* ctx, int on);
 /* Statistics of one kernel (waits for the stream). */
 pt_status pt_get_kernel_stats(pt_ctx* ctx, int kernel, pt_kernel_stats* out);
 /* Blocks until the context's stream is idle. */

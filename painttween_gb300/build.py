@@ -42,14 +42,14 @@ def build(force=False, verbose=False):
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(BUILD, exist_ok=True)
     inc = ["-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
-    k_obj = os.path.join(BUILD, "pt_kernels.o")
+    cu_files = sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
+    objs = [os.path.join(BUILD, f[:-3] + ".o") for f in cu_files]
     h_obj = os.path.join(BUILD, "pt_context.o")
-    jobs = [
-        [nvcc, ARCH, "-lineinfo", "-O3", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
-         "--expt-relaxed-constexpr"] + inc + ["-c", os.path.join(CSRC, "pt_kernels.cu"), "-o", k_obj],
-        ["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function",
-         "-I" + os.path.join(cuda, "include")] + inc + ["-c", os.path.join(CSRC, "pt_context.cpp"), "-o", h_obj],
-    ]
+    jobs = [[nvcc, ARCH, "-lineinfo", "-O3", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
+             "--expt-relaxed-constexpr"] + inc + ["-c", os.path.join(CSRC, f), "-o", o]
+            for f, o in zip(cu_files, objs)]
+    jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function",
+                 "-I" + os.path.join(cuda, "include")] + inc + ["-c", os.path.join(CSRC, "pt_context.cpp"), "-o", h_obj])
     procs = []
     for cmd in jobs:
         if verbose:
@@ -64,7 +64,8 @@ def build(force=False, verbose=False):
             print(out.decode(errors="replace"))
     if failed:
         raise RuntimeError("painttween_gb300 build failed:\n" + "\n".join(failed))
-    link = [nvcc, ARCH, "-shared", "-o", LIB + ".tmp", k_obj, h_obj, "-lcudart_static", "-lrt", "-lpthread", "-ldl"]
+    link = [nvcc, ARCH, "-shared", "-o", LIB + ".tmp"] + objs + [h_obj, "-lcudart_static", "-lrt", "-lpthread",
+                                                                "-ldl"]
     if verbose:
         print(" ".join(link))
     subprocess.check_call(link)

@@ -122,6 +122,8 @@ struct pt_ctx {
 
     uint64_t launches = 0;
     uint32_t pass_counter = 0;
+    bool adv_written[2] = {false, false};  // advected F/B written since the last reset
+    bool use_tiled = true;                 // tiled kernels where an instantiation exists
 
     // measurement
     cudaEvent_t timers[PT_TIMER_SLOTS] = {};
@@ -373,10 +375,45 @@ static pt_status profiled(pt_ctx* c, int kernel, Params& P, F&& launch) {
     return PT_OK;
 }
 
+// Temporal mode of the tiled kernels: which advected buffer can make the
+// temporal terms of calculateResidual active (texSynth_kernel.cu:610-627).
+// Returns -1 when both can (bidirectional), which the tiled kernels do not
+// cover.
+static int temporal_mode(pt_ctx* c) {
+    const pt_params& p = c->params;
+    bool td = p.timeDerivativeInputWeight > 0.f || p.timeDerivativeOutputWeight > 0.f ||
+              p.temporalCoherenceWeight > 0.f;
+    bool f = td && c->adv_written[0] && (p.direction == PT_FORWARD || p.direction == PT_BIDIRECTIONAL);
+    bool b = td && c->adv_written[1] && (p.direction == PT_BACKWARD || p.direction == PT_BIDIRECTIONAL);
+    if (f && b) return -1;
+    return f ? 1 : (b ? 2 : 0);
+}
+
+// launches the tiled kernel of `kind` if one is instantiated for this
+// configuration; *done = false otherwise (the generic kernel is used)
+static cudaError_t launch_tiled(pt_ctx* c, int kind, const Params& P, PatchPlanes work, int arg, uint32_t pass_id,
+                                float* out, bool* done) {
+    *done = false;
+    if (!c->use_tiled || c->params.coherenceWeight > 0.f) return cudaSuccess;
+    int tm = temporal_mode(c);
+    if (tm < 0) return cudaSuccess;
+    *done = true;
+    switch (P.r) {
+        case 2: return pt::launch_tiled_2(kind, tm, P, work, arg, pass_id, out, c->stream);
+        case 3: return pt::launch_tiled_3(kind, tm, P, work, arg, pass_id, out, c->stream);
+        case 4: return pt::launch_tiled_4(kind, tm, P, work, arg, pass_id, out, c->stream);
+        default: *done = false; return cudaSuccess;
+    }
+}
+
 static pt_status do_residual(pt_ctx* c, int level) {
     Params P = make_params(c, level);
     float* out = c->res[c->res_i];
-    return profiled(c, PT_KERNEL_RESIDUAL, P, [&](const Params& Q) { return pt::launch_residual(Q, out, c->stream); });
+    return profiled(c, PT_KERNEL_RESIDUAL, P, [&](const Params& Q) {
+        bool done = false;
+        cudaError_t e = launch_tiled(c, 2, Q, PatchPlanes{}, 0, 0, out, &done);
+        return done ? e : pt::launch_residual(Q, out, c->stream);
+    });
 }
 
 // TexSynth::syncBuffers, texSynth_kernel.cu:1240-1303
@@ -671,6 +708,7 @@ static pt_status reset_working(pt_ctx* c) {
 
 pt_status pt_reset_advected_buffers(pt_ctx* c) {
     if (!c || !c->initialized) return PT_ERR_STATE;
+    c->adv_written[0] = c->adv_written[1] = false;
     size_t n = (size_t)c->W * c->H;
     for (int i = 0; i < 2; i++) {
         CU(cudaMemsetAsync(c->adv[i].off.A, 0, n * sizeof(float4), c->stream));
@@ -904,8 +942,11 @@ pt_status pt_propagate(pt_ctx* c, int level, int jump, int key_index) {
     if (key_index >= 0) return fail(c, PT_ERR_UNSUPPORTED, "keyframe propagation is not implemented");
     PatchPlanes work = writable_work(c, nullptr);
     Params P = make_params(c, level);
-    TRY(profiled(c, PT_KERNEL_PROPAGATE, P,
-                 [&](const Params& Q) { return pt::launch_propagate(Q, work, jump, c->stream); }));
+    TRY(profiled(c, PT_KERNEL_PROPAGATE, P, [&](const Params& Q) {
+        bool done = false;
+        cudaError_t e = launch_tiled(c, 0, Q, work, jump, 0, nullptr, &done);
+        return done ? e : pt::launch_propagate(Q, work, jump, c->stream);
+    }));
     return do_sync(c, level, 0);
 }
 
@@ -918,7 +959,9 @@ pt_status pt_scatter(pt_ctx* c, int level, int key_index) {
     Params P = make_params(c, level);
     uint32_t pass_id = c->pass_counter++;
     TRY(profiled(c, PT_KERNEL_SCATTER, P, [&](const Params& Q) {
-        return pt::launch_scatter(Q, work, aliased ? 1 : 0, pass_id, c->stream);
+        bool done = false;
+        cudaError_t e = launch_tiled(c, 1, Q, work, aliased ? 1 : 0, pass_id, nullptr, &done);
+        return done ? e : pt::launch_scatter(Q, work, aliased ? 1 : 0, pass_id, c->stream);
     }));
     return do_sync(c, level, 0);
 }
@@ -946,6 +989,7 @@ pt_status pt_advect_offsets(pt_ctx* c, int level, int time_step, int forwards, i
     int d = forwards ? 0 : 1;
     Params P = make_params(c, level);
     LN(pt::launch_advect(P, d, forwards ? 1 : 0, time_step, flags, c->stream));
+    c->adv_written[d] = true;
     PatchPlanes dst = base_for_full_write(c);
     P = make_params(c, level);
     LN(pt::launch_copy_patch(P, dst, c->adv[d].off, c->stream));
@@ -1246,6 +1290,12 @@ pt_status pt_set_profiling(pt_ctx* c, int on) {
     if (!c->counters) TRY(dalloc_t(c, &c->counters, 2 * PT_KERNEL_COUNT));
     CU(cudaMemsetAsync(c->counters, 0, 2 * PT_KERNEL_COUNT * sizeof(unsigned long long), c->stream));
     c->profiling = on != 0;
+    return PT_OK;
+}
+
+pt_status pt_set_tiled_kernels(pt_ctx* c, int on) {
+    if (!c) return PT_ERR_INVALID;
+    c->use_tiled = on != 0;
     return PT_OK;
 }
 

@@ -1,0 +1,391 @@
+// pt_energy.cuh -- the tiled patch-distance kernels (propagate, scatter,
+// residual) for a compile-time patch radius R and temporal mode TM.
+//
+// Same per-pixel semantics and the same FP32 arithmetic, operation by
+// operation, as the generic kernels in pt_kernels.cu (which restate
+// calculateResidual and its callers, src/PaintTweenCUDA/texSynth_kernel.cu:
+// 537-952), organised for sm_103a:
+//  * a block owns a 32 x 8 pixel tile; the pixel-side inputs of every tap
+//    (input colour, canvas, and for temporal passes the advected colours and
+//    validity) are staged once into shared memory with an R-pixel halo;
+//  * the (2R+1)^2 tap loop is fully unrolled and straight-line: taps outside
+//    the level rectangle are evaluated and then discarded by selects, which
+//    leaves the sums exactly as skipping them would;
+//  * an exemplar texel is 32 bytes (base RGBA, output RGBA), one sector per
+//    texel of the bilinear footprint; when a candidate's whole footprint lies inside the
+//    exemplar (decided for the whole warp), the wrap and clamp steps -- which
+//    are then no-ops -- are left out.
+#pragma once
+
+#include "pt_common.cuh"
+#include "pt_internal.h"
+
+namespace ptk {
+
+constexpr int kTileW = 32;
+constexpr int kTileH = 8;
+constexpr int kTileThreads = kTileW * kTileH;
+
+enum { TM_NONE = 0, TM_FWD = 1, TM_BWD = 2 };
+
+template <int R, int TM>
+struct TileSmem {
+    static constexpr int TW = kTileW + 2 * R;
+    static constexpr int TH = kTileH + 2 * R;
+    static constexpr int N = TW * TH;
+    float4 base[N];
+    float4 canvas[N];
+    float4 pbase[TM ? N : 1];
+    float4 pout[TM ? N : 1];
+    float phys[TM ? N : 1];
+};
+
+// one exemplar texel (base, output): 32 contiguous bytes, one sector
+__device__ __forceinline__ void ld_texel(const float4* p, float4* b, float4* o) {
+    *b = __ldg(p);
+    *o = __ldg(p + 1);
+}
+
+// bilinear base+output at (u, v) of one exemplar layer; FAST: the footprint
+// is known to be inside [0, w-1] x [0, h-1] (no clamping needed)
+template <bool FAST>
+__device__ __forceinline__ void sample2(const float4* L, int w, int h, float u, float v, float4* base, float4* out) {
+    float xs = u + 0.5f, ys = v + 0.5f;
+    float xb = xs - 0.5f, yb = ys - 0.5f;
+    float fx = floorf(xb), fy = floorf(yb);
+    float a = xb - fx, c = yb - fy;
+    int x0, x1, y0, y1;
+    if (FAST) {
+        x0 = (int)fx; y0 = (int)fy; x1 = x0 + 1; y1 = y0 + 1;
+    } else {
+        fx = fminf(fmaxf(fx, -1.0f), (float)w);
+        fy = fminf(fmaxf(fy, -1.0f), (float)h);
+        int ix = (int)fx, iy = (int)fy;
+        x0 = clampi(ix, 0, w - 1); x1 = clampi(ix + 1, 0, w - 1);
+        y0 = clampi(iy, 0, h - 1); y1 = clampi(iy + 1, 0, h - 1);
+    }
+    float oa = 1.0f - a, oc = 1.0f - c;
+    Bl bw;
+    bw.w00 = oa * oc; bw.w10 = a * oc; bw.w01 = oa * c; bw.w11 = a * c;
+    float4 b00, o00, b10, o10, b01, o01, b11, o11;
+    const float4* r0 = L + (size_t)y0 * w * 2;
+    const float4* r1 = L + (size_t)y1 * w * 2;
+    ld_texel(r0 + 2 * x0, &b00, &o00);
+    ld_texel(r0 + 2 * x1, &b10, &o10);
+    ld_texel(r1 + 2 * x0, &b01, &o01);
+    ld_texel(r1 + 2 * x1, &b11, &o11);
+    *base = bl4(bw, b00, b10, b01, b11);
+    *out = bl4(bw, o00, o10, o01, o11);
+}
+
+struct Cand {
+    float x, y, theta, su, sv;
+    int layer;
+};
+
+// per-pixel state of the tiled kernels
+struct PixT {
+    int x, y;          // level coordinates
+    int sidx;          // shared-memory index of the pixel
+    int imin, imax, jmin, jmax;  // taps inside the level rectangle
+    bool hyst_on;      // advected-F centre valid (hysteresis term subtracted)
+    float hyst;
+    bool temporal;     // temporal terms of direction TM apply at this pixel
+    Patch prev;        // advected offset at the pixel (direction TM)
+    float2 pb0, pb1;   // its basis
+    bool prev_fast;    // its footprint is inside the exemplar
+};
+
+// does the footprint of a patch at (x, y) with basis (b0, b1) stay inside
+// [1, w-3] x [1, h-3] (so every tap's 2x2 texels are in range and no wrap
+// applies, since the wrap period is at least the exemplar size)
+template <int R>
+__device__ __forceinline__ bool footprint_inside(float x, float y, float2 b0, float2 b1, int w, int h) {
+    float bx = (float)R * (fabsf(b0.x) + fabsf(b1.x)) + 1.0f;
+    float by = (float)R * (fabsf(b0.y) + fabsf(b1.y)) + 1.0f;
+    return (x - bx >= 0.0f) && (x + bx <= (float)(w - 2)) && (y - by >= 0.0f) && (y + by <= (float)(h - 2));
+}
+
+template <int R, int TM, bool FAST, bool FASTP>
+__device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
+                                             const Cand& c, float2 b0, float2 b1, float sum0) {
+    constexpr int TW = TileSmem<R, TM>::TW;
+    const float4* L = P.ex.bo + (size_t)ex_layer(P.ex, c.layer) * P.ex.w * P.ex.h * 2;
+    const float4* LP = nullptr;
+    if (TM) LP = P.ex.bo + (size_t)ex_layer(P.ex, px.prev.layer) * P.ex.w * P.ex.h * 2;
+    const float hw = (float)P.histW, hh = (float)P.histH;
+    float sum = sum0, sumW = 0.0f;
+#pragma unroll
+    for (int i = -R; i <= R; i++) {
+#pragma unroll
+        for (int j = -R; j <= R; j++) {
+            const bool valid = (i >= px.imin) && (i <= px.imax) && (j >= px.jmin) && (j <= px.jmax);
+            const int s = px.sidx + j * TW + i;
+            float4 base = T.base[s];
+            float4 canvas = T.canvas[s];
+            float tx = c.x + fmaf((float)i, b0.x, (float)j * b1.x);
+            float ty = c.y + fmaf((float)i, b0.y, (float)j * b1.y);
+            if (!FAST) {
+                if (tx >= hw) tx -= hw; else if (tx < 0) tx += hw;
+                if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
+            }
+            float4 tb, to;
+            sample2<FAST>(L, P.ex.w, P.ex.h, tx, ty, &tb, &to);
+            float res = ssd_a(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
+            if (TM) {
+                if (px.temporal) {
+                    float4 pbase = T.pbase[s], pout = T.pout[s];
+                    float ptx = px.prev.x + fmaf((float)i, px.pb0.x, (float)j * px.pb1.x);
+                    float pty = px.prev.y + fmaf((float)i, px.pb0.y, (float)j * px.pb1.y);
+                    float4 peb, peo;
+                    sample2<FASTP>(LP, P.ex.w, P.ex.h, ptx, pty, &peb, &peo);
+                    float r = ssd(sub4(base, pbase), sub4(tb, peb)) * P.tdIn;
+                    r = fmaf(ssd(sub4(canvas, pout), sub4(to, peo)), P.tdOut, r);
+                    r = fmaf(ssd(pout, to), P.tc, r);
+                    res = (T.phys[s] > 0) ? res + r : res;
+                }
+            }
+            if (i == 0 && j == 0) {
+                if (P.distTransWeight > 0.f) {
+                    float de = ex_sample_dt(P.ex, tx, ty, c.layer) / c.sv;
+                    float di = lay_texel(P.img.dt[P.img.cur], P, px.x, px.y);
+                    float diff = fminf(fmaxf(fabsf(de - di), 0.0f), 10.0f);
+                    res = res + diff * P.distTransWeight;
+                }
+                {
+                    int Lh = clampi(c.layer, 0, PT_MAX_STYLES - 1);
+                    float sh = (float)(P.histH / P.numStyles);
+                    int hx = clampi((int)tx, 0, P.histPitch - 1);
+                    int hy = clampi((int)(ty + sh * (float)c.layer), 0, P.histRows - 1);
+                    float h = __ldg(P.hist + (size_t)hy * P.histPitch + hx);
+                    float thr = P.histThreshold[Lh];
+                    res = res + ((h > thr) ? (h - thr) * P.histSlope[Lh] : 0.0f);
+                }
+                if (P.styleObjIdWeight > 0.f) {
+                    int imgID = lvl_texel(P.img.ids, px.x, px.y);
+                    int styleID = ex_point_id(P.ex, tx, ty, c.layer);
+                    res = res + ((imgID != styleID) ? P.styleObjIdWeight : 0.0f);
+                }
+            } else {
+                res = fmaf(ssd_a(canvas, to, P.alphaWeight), P.canvasOutputWeight, res);
+            }
+            const float w = P.gauss[i + R] * P.gauss[j + R];
+            sum = valid ? fmaf(res, w, sum) : sum;
+            sumW = valid ? sumW + w : sumW;
+        }
+    }
+    if (sumW < kEpsilon) return kBigResidual;
+    return sum / sumW;
+}
+
+// one call per candidate (kept out of line: the three kernels share it)
+template <int R, int TM>
+__device__ __noinline__ float energy_tiled(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
+                                           const Cand& c) {
+    float sum0 = 0.0f;
+    if (px.hyst_on) sum0 = sum0 - px.hyst;
+    float2 b0, b1;
+    basis(c.theta, P.scaleWU * c.su, P.scaleWV * c.sv, &b0, &b1);
+    bool fast = footprint_inside<R>(c.x, c.y, b0, b1, P.ex.w, P.ex.h);
+    fast = __all_sync(__activemask(), fast);
+    if (TM) {
+        if (fast && px.prev_fast) return energy_taps<R, TM, true, true>(P, T, px, c, b0, b1, sum0);
+        return energy_taps<R, TM, false, false>(P, T, px, c, b0, b1, sum0);
+    }
+    if (fast) return energy_taps<R, TM, true, true>(P, T, px, c, b0, b1, sum0);
+    return energy_taps<R, TM, false, false>(P, T, px, c, b0, b1, sum0);
+}
+
+// test_offset + isExemplarPixelCulled, texSynth_kernel.cu:200-205,695-721
+template <int R, int TM>
+__device__ __forceinline__ float test_offset_tiled(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
+                                                   const Cand& c, float image_alpha) {
+    float dte = ex_texel_dt(P.ex, (int)c.x, (int)c.y, c.layer);
+    if (!((double)dte > (double)P.distTransCull * 1.25)) {
+        if (!P.transparencyOk) {
+            float ea = ex_sample_out_alpha(P.ex, c.x, c.y, c.layer);
+            if (ea < kAlphaThreshold && image_alpha > kAlphaThreshold) return kBigResidual;
+        }
+        if (P.counters) count_eval(P, px.x, px.y);
+        return energy_tiled<R, TM>(P, T, px, c);
+    }
+    return kBigResidual;
+}
+
+// Stages the tile (and halo) of the pixel-side inputs and fills the
+// per-pixel state.  Returns false for threads whose pixel is outside the
+// level rectangle.
+template <int R, int TM>
+__device__ __forceinline__ bool stage_tile(const Params& P, TileSmem<R, TM>& T, PixT* px) {
+    constexpr int TW = TileSmem<R, TM>::TW, N = TileSmem<R, TM>::N;
+    const int tid = threadIdx.x + threadIdx.y * kTileW;
+    const int x0 = blockIdx.x * kTileW - R, y0 = blockIdx.y * kTileH - R;
+    const Arr<float4>& ib = P.img.base[P.img.cur];
+    for (int q = tid; q < N; q += kTileThreads) {
+        int gx = clampi(x0 + q % TW, 0, P.lw - 1);
+        int gy = clampi(y0 + q / TW, 0, P.lh - 1);
+        size_t k = (size_t)gy * P.W + gx;
+        T.base[q] = __ldg(ib.p + (size_t)gy * ib.w + gx);
+        T.canvas[q] = __ldg(P.canvas + k);
+        if (TM) {
+            const AdvView& A = P.adv[TM == TM_FWD ? 0 : 1];
+            T.pbase[q] = __ldg(A.base + k);
+            T.pout[q] = __ldg(A.out + k);
+            T.phys[q] = __ldg(&A.off.B[k].x);
+        }
+    }
+    __syncthreads();
+    const int x = blockIdx.x * kTileW + threadIdx.x, y = blockIdx.y * kTileH + threadIdx.y;
+    if (x >= P.lw || y >= P.lh) return false;
+    px->x = x;
+    px->y = y;
+    px->sidx = (threadIdx.y + R) * TW + threadIdx.x + R;
+    px->imin = max(-R, -x); px->imax = min(R, P.lw - 1 - x);
+    px->jmin = max(-R, -y); px->jmax = min(R, P.lh - 1 - y);
+    const size_t k = (size_t)y * P.W + x;
+    px->hyst_on = false;
+    px->hyst = 0.0f;
+    if (P.hysteresisWeight != 0.0f) {
+        px->hyst_on = __ldg(&P.adv[0].off.B[k].x) > 0;
+        if (px->hyst_on) px->hyst = hysteresis_term(P, x, y);
+    }
+    px->temporal = false;
+    px->prev_fast = false;
+    if (TM) {
+        px->prev = load_patch(P.adv[TM == TM_FWD ? 0 : 1].off, k);
+        bool td = (P.tdIn > 0.f || P.tdOut > 0.f || P.tc > 0.f);
+        px->temporal = td && px->prev.hyst > 0;
+        if (px->temporal) {
+            float a = screen_to_exemplar_angle(P, x, y, px->prev.x, px->prev.y, px->prev.layer);
+            basis(a, P.scaleWU * px->prev.su, P.scaleWV * px->prev.sv, &px->pb0, &px->pb1);
+            px->prev_fast = footprint_inside<R>(px->prev.x, px->prev.y, px->pb0, px->pb1, P.ex.w, P.ex.h);
+        }
+    }
+    return true;
+}
+
+// propagate_kernel, texSynth_kernel.cu:1112-1219
+template <int R, int TM>
+__global__ void __launch_bounds__(kTileThreads, 2) kt_propagate(const Params P, PatchPlanes work, int jump) {
+    __shared__ TileSmem<R, TM> T;
+    PixT px;
+    if (!stage_tile<R, TM>(P, T, &px)) return;
+    const int x = px.x, y = px.y;
+    const size_t k = (size_t)y * P.W + x;
+    if (image_culled(P, x, y)) {
+        store_patch(work, k, make_patch(0, 0, 0, 0, 0, 1.f, 1.f));
+        return;
+    }
+    float best = __ldg(P.res + k);
+    float ia = T.base[px.sidx].w;
+    Patch ow = load_patch(P.off, k);
+#pragma unroll 1
+    for (int cdx = 0; cdx < 4; cdx++) {
+        int tx = x, ty = y;
+        if (cdx == 0) tx = x + jump;
+        else if (cdx == 1) tx = x - jump;
+        else if (cdx == 2) ty = y + jump;
+        else ty = y - jump;
+        Patch t = propagate_offset(P, tx, ty, x, y);
+        Cand c{t.x, t.y, t.theta, t.su, t.sv, t.layer};
+        float r = test_offset_tiled<R, TM>(P, T, px, c, ia);
+        if (r < best) { ow = t; best = r; }
+    }
+    store_patch(work, k, ow);
+}
+
+// scatter_kernel + averageOffset, texSynth_kernel.cu:841-952
+template <int R, int TM>
+__global__ void __launch_bounds__(kTileThreads, 2) kt_scatter(const Params P, PatchPlanes work, int write_all,
+                                                             uint32_t pass_id) {
+    __shared__ TileSmem<R, TM> T;
+    PixT px;
+    if (!stage_tile<R, TM>(P, T, &px)) return;
+    const int x = px.x, y = px.y;
+    const size_t k = (size_t)y * P.W + x;
+    Patch off = load_patch(P.off, k);
+    if (image_culled(P, x, y)) {
+        if (write_all) store_patch(work, k, off);
+        return;
+    }
+    float cached = __ldg(P.res + k);
+    float best = (float)((double)cached + 10e-7);
+    Patch ow = off;
+    float ia = T.base[px.sidx].w;
+    float dist = (float)(P.ex.w > P.ex.h ? P.ex.w : P.ex.h);
+    const float closest = 10.f, factor = 0.9f;
+    float2 sc = lvl_texel(P.img.scale, x, y);
+#pragma unroll 1
+    for (int i = 0; i < P.scatterSamples && dist * factor >= closest; i++) {
+        float dmin = dist * factor;
+        float ex, ey;
+        if (P.rngMode == PT_RNG_COUNTER) {
+            float rr = counter_u01(P.rngSeed, pass_id, x, y, 2 * i);
+            float th = counter_u01(P.rngSeed, pass_id, x, y, 2 * i + 1) * 6.28318530717958647692f;
+            float s, c;
+            sincos_poly(th, &s, &c);
+            float len = fmaf(rr, dist - dmin, dmin);
+            ex = fmaf(c, len, ow.x);
+            ey = fmaf(s, len, ow.y);
+        } else {
+            ex = ow.x + dmin;
+            ey = ow.y + 0.0f;
+        }
+        clamp_to_exemplar(&ex, &ey, P.ex.w, P.ex.h);
+        float ang = screen_to_exemplar_angle(P, x, y, ex, ey, 0);
+        Cand c{ex, ey, ang, sc.x, sc.y, 0};
+        float r = test_offset_tiled<R, TM>(P, T, px, c, ia);
+        if (r < best) { ow = make_patch(ex, ey, ang, 0.0f, 0, sc.x, sc.y); best = r; }
+        dist *= factor;
+    }
+    Patch avg = make_patch(0, 0, 0, 1.f, 0, 1.f, 1.f);
+    int n = 0;
+    for (int i = -1; i <= 1; i++)
+        for (int j = -1; j <= 1; j++) {
+            if (!in_rect(P, x + i, y + j) || (i == 0 && j == 0)) continue;
+            float4 nb = __ldg(P.off.A + (size_t)(y + j) * P.W + (x + i));
+            if (__float_as_int(nb.w) != 0) continue;
+            avg.x = avg.x + nb.x;
+            avg.y = avg.y + nb.y;
+            n++;
+        }
+    avg.x = avg.x / (float)n;
+    avg.y = avg.y / (float)n;
+    avg.theta = screen_to_exemplar_angle(P, x, y, avg.x, avg.y, 0);
+    Cand c{avg.x, avg.y, avg.theta, avg.su, avg.sv, 0};
+    float r = test_offset_tiled<R, TM>(P, T, px, c, ia);
+    if (r < best) { ow = avg; best = r; }
+    if (best < cached) store_patch(work, k, ow);
+    else if (write_all) store_patch(work, k, off);
+}
+
+// updateResidualCache_kernel, texSynth_kernel.cu:661-693
+template <int R, int TM>
+__global__ void __launch_bounds__(kTileThreads, 2) kt_residual(const Params P, float* out) {
+    __shared__ TileSmem<R, TM> T;
+    PixT px;
+    if (!stage_tile<R, TM>(P, T, &px)) return;
+    const size_t k = (size_t)px.y * P.W + px.x;
+    if (image_culled(P, px.x, px.y)) { out[k] = 0.0f; return; }
+    Patch t = load_patch(P.off, k);
+    Cand c{t.x, t.y, t.theta, t.su, t.sv, t.layer};
+    if (P.counters) count_eval(P, px.x, px.y);
+    out[k] = energy_tiled<R, TM>(P, T, px, c);
+}
+
+template <int R>
+cudaError_t launch_tiled_r(int kind, int tm, const Params& P, PatchPlanes work, int arg, uint32_t pass_id, float* out,
+                           cudaStream_t s) {
+    dim3 b(kTileW, kTileH), g((P.lw + kTileW - 1) / kTileW, (P.lh + kTileH - 1) / kTileH);
+#define PT_TILED_DISPATCH(TMV)                                                                   \
+    if (kind == 0) kt_propagate<R, TMV><<<g, b, 0, s>>>(P, work, arg);                          \
+    else if (kind == 1) kt_scatter<R, TMV><<<g, b, 0, s>>>(P, work, arg, pass_id);              \
+    else kt_residual<R, TMV><<<g, b, 0, s>>>(P, out);
+    if (tm == TM_NONE) { PT_TILED_DISPATCH(TM_NONE) }
+    else if (tm == TM_FWD) { PT_TILED_DISPATCH(TM_FWD) }
+    else { PT_TILED_DISPATCH(TM_BWD) }
+#undef PT_TILED_DISPATCH
+    return cudaGetLastError();
+}
+
+}  // namespace ptk

@@ -40,4 +40,14 @@ cudaError_t launch_random_level(int mode, int w, int h, int mx, int my, int tran
                                 Arr<float4> img, Arr<float> iorient, ExView ex, float4* out,
                                 const uint32_t* states, uint32_t seed, cudaStream_t s);
 cudaError_t launch_any_transparent(const float4* bo, size_t n, int* flag, cudaStream_t s);
+
+// tiled patch-distance kernels for patch radius 2, 3, 4 (pt_tiled_r*.cu):
+// kind 0 = propagate (arg = jump), 1 = scatter (arg = write_all),
+// 2 = residual (into out); tm 0 = no temporal terms, 1 = forward, 2 = backward
+cudaError_t launch_tiled_2(int kind, int tm, const Params& P, PatchPlanes work, int arg, uint32_t pass_id, float* out,
+                           cudaStream_t s);
+cudaError_t launch_tiled_3(int kind, int tm, const Params& P, PatchPlanes work, int arg, uint32_t pass_id, float* out,
+                           cudaStream_t s);
+cudaError_t launch_tiled_4(int kind, int tm, const Params& P, PatchPlanes work, int arg, uint32_t pass_id, float* out,
+                           cudaStream_t s);
 }  // namespace pt

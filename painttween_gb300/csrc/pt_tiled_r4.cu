@@ -1,0 +1,9 @@
+// pt_tiled_r4.cu -- tiled patch-distance kernels instantiated for patch radius 4.
+#include "pt_energy.cuh"
+
+namespace pt {
+cudaError_t launch_tiled_4(int kind, int tm, const Params& P, PatchPlanes work, int arg, uint32_t pass_id, float* out,
+                           cudaStream_t s) {
+    return ptk::launch_tiled_r<4>(kind, tm, P, work, arg, pass_id, out, s);
+}
+}  // namespace pt

@@ -86,6 +86,9 @@ class TexSynth:
         self._check(lib().pt_timer_elapsed(self.h, a, b, ctypes.byref(ms)), "pt_timer_elapsed")
         return ms.value
 
+    def set_tiled_kernels(self, on):
+        self._check(lib().pt_set_tiled_kernels(self.h, int(on)), "pt_set_tiled_kernels")
+
     def set_profiling(self, on):
         self._check(lib().pt_set_profiling(self.h, int(on)), "pt_set_profiling")
 

@@ -327,3 +327,32 @@ def test_errors_are_status_codes():
         tb.initialize(1024, 1024, 256, 256, 1)
     assert e.value.status == 7  # PT_ERR_BUDGET
     tb.close()
+
+
+@pytest.mark.parametrize("r", [1, 2, 3, 4])
+def test_tiled_and_generic_kernels_identical(r):
+    """The tiled shared-memory kernels (patch radius 2-4) and the generic
+    kernels give bit-identical animations, including the temporal terms of
+    both pass directions; radius 1 runs the generic kernels in both cases."""
+    p = config_params(r=r, levels=2, iterations=2)
+    p.temporalCoherenceWeight = 0.5
+    p.hysteresisWeight = 0.25
+    p.distTransWeight = 0.5
+    ex = synthetic.make_exemplar(64, 64, seed=50 + r)
+    clip = synthetic.make_clip(72, 56, 3, 3, seed=60 + r)
+    outs = []
+    for tiled in (True, False):
+        s = Synthesizer(device=0)
+        s.setup(p, 72, 56, 64, 64, 1)
+        s.set_tiled_kernels(tiled)
+        s.set_style(0, ex["base"], ex["output"], ex["orient_tensor"], ex["dist_trans"], ex["object_ids"])
+        for i, fr in enumerate(clip):
+            s.set_frame_dict(i, fr)
+        outs.append(s.synthesize_animation(0, 2))
+        s.close()
+    for f in range(3):
+        assert_offsets_equal(outs[0][f][1], outs[1][f][1], 1.0, "tiled vs generic frame %d" % f)
+        assert_array_equal(outs[0][f][0], outs[1][f][0], "tiled vs generic output frame %d" % f)
+    ref = O.OracleDriver(p, [ex], clip, threads=8).render(0, 2)
+    for f in range(3):
+        assert_offsets_equal(outs[0][f][1], ref[f][0], 0.999, "tiled vs oracle frame %d" % f)
