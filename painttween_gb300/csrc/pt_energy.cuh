@@ -115,7 +115,7 @@ __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, 
     if (TM) LP = P.ex.bo + (size_t)ex_layer(P.ex, px.prev.layer) * P.ex.w * P.ex.h * 2;
     const float hw = (float)P.histW, hh = (float)P.histH;
     float sum = sum0, sumW = 0.0f;
-#pragma unroll
+#pragma unroll 1
     for (int i = -R; i <= R; i++) {
 #pragma unroll
         for (int j = -R; j <= R; j++) {
@@ -178,9 +178,8 @@ __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, 
     return sum / sumW;
 }
 
-// one call per candidate (kept out of line: the three kernels share it)
 template <int R, int TM>
-__device__ __noinline__ float energy_tiled(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
+__device__ __forceinline__ float energy_tiled(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
                                            const Cand& c) {
     float sum0 = 0.0f;
     if (px.hyst_on) sum0 = sum0 - px.hyst;
@@ -279,6 +278,12 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate(const Params P, 
     float best = __ldg(P.res + k);
     float ia = T.base[px.sidx].w;
     Patch ow = load_patch(P.off, k);
+    // A candidate bit-identical to one already evaluated for this pixel has
+    // the same energy, which the strict "<" test then rejects: skipping it
+    // leaves the result unchanged.
+    // keys of the candidates evaluated so far (x, y, theta bits and layer)
+    uint32_t s0x = 0, s0y = 0, s0t = 0, s1x = 0, s1y = 0, s1t = 0, s2x = 0, s2y = 0, s2t = 0;
+    int s0l = -1, s1l = -1, s2l = -1;
 #pragma unroll 1
     for (int cdx = 0; cdx < 4; cdx++) {
         int tx = x, ty = y;
@@ -287,6 +292,14 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate(const Params P, 
         else if (cdx == 2) ty = y + jump;
         else ty = y - jump;
         Patch t = propagate_offset(P, tx, ty, x, y);
+        uint32_t kx = __float_as_uint(t.x), ky = __float_as_uint(t.y), kt = __float_as_uint(t.theta);
+        bool dup = (cdx > 0 && kx == s0x && ky == s0y && kt == s0t && t.layer == s0l) ||
+                   (cdx > 1 && kx == s1x && ky == s1y && kt == s1t && t.layer == s1l) ||
+                   (cdx > 2 && kx == s2x && ky == s2y && kt == s2t && t.layer == s2l);
+        if (cdx == 0) { s0x = kx; s0y = ky; s0t = kt; s0l = t.layer; }
+        else if (cdx == 1) { s1x = kx; s1y = ky; s1t = kt; s1l = t.layer; }
+        else if (cdx == 2) { s2x = kx; s2y = ky; s2t = kt; s2l = t.layer; }
+        if (dup) continue;
         Cand c{t.x, t.y, t.theta, t.su, t.sv, t.layer};
         float r = test_offset_tiled<R, TM>(P, T, px, c, ia);
         if (r < best) { ow = t; best = r; }
@@ -315,6 +328,10 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter(const Params P, Pa
     float dist = (float)(P.ex.w > P.ex.h ? P.ex.w : P.ex.h);
     const float closest = 10.f, factor = 0.9f;
     float2 sc = lvl_texel(P.img.scale, x, y);
+    // the chain often clamps several candidates to the same exemplar
+    // position; an exact repeat of the previous evaluated candidate has the
+    // same energy and is rejected by the strict "<" test, so it is skipped
+    uint32_t lastx = 0xffffffffu, lasty = 0xffffffffu;
 #pragma unroll 1
     for (int i = 0; i < P.scatterSamples && dist * factor >= closest; i++) {
         float dmin = dist * factor;
@@ -332,6 +349,12 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter(const Params P, Pa
             ey = ow.y + 0.0f;
         }
         clamp_to_exemplar(&ex, &ey, P.ex.w, P.ex.h);
+        if (__float_as_uint(ex) == lastx && __float_as_uint(ey) == lasty) {
+            dist *= factor;
+            continue;
+        }
+        lastx = __float_as_uint(ex);
+        lasty = __float_as_uint(ey);
         float ang = screen_to_exemplar_angle(P, x, y, ex, ey, 0);
         Cand c{ex, ey, ang, sc.x, sc.y, 0};
         float r = test_offset_tiled<R, TM>(P, T, px, c, ia);
