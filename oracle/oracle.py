@@ -51,6 +51,8 @@ def lib():
             "pto_randomize": (None, [vp, i]),
             "pto_propagate": (None, [vp, i, i]),
             "pto_scatter": (None, [vp, i]),
+            "pto_scatter_pass": (None, [vp, i, u32]),
+            "pto_counter_random_level": (None, [u32, i, i, i, i, i, vp, vp, vp, vp, i, i, i, vp]),
             "pto_update_residual": (None, [vp, i]),
             "pto_sync": (None, [vp, i, i]),
             "pto_upsample": (None, [vp, i]),
@@ -158,6 +160,24 @@ def frame_pyramids(fr):
         w=w, h=h)
 
 
+def counter_random_level(seed, level, style_w0, style_h0, img_rgba, img_orient, ex_out, ex_orient,
+                         transparency_ok=False, orientation_enabled=True):
+    """The PT_RNG_COUNTER random level (hashed draws, reference retry rule)."""
+    h, w = img_orient.shape
+    ew = ex_orient.shape[1]
+    out = np.empty((h, w, 4), np.float32)
+    lib().pto_counter_random_level(seed & 0xFFFFFFFF, w, h, level, style_w0, style_h0,
+                                   _p(_c(img_rgba, np.float32)), _p(_c(img_orient, np.float32)),
+                                   _p(_c(ex_out, np.float32)), _p(_c(ex_orient, np.float32)), ew,
+                                   int(transparency_ok), int(orientation_enabled), _p(out))
+    return out
+
+
+def counter_seed(rng_seed, frame, level):
+    """Seed of one random level in PT_RNG_COUNTER mode."""
+    return (rng_seed ^ ((0x9E3779B9 * (frame + 1)) & 0xFFFFFFFF) ^ ((0x85EBCA6B * (level + 1)) & 0xFFFFFFFF)) & 0xFFFFFFFF
+
+
 def glibc_stream(seed, n):
     out = np.empty(n, np.int32)
     lib().pto_glibc_stream(seed & 0xFFFFFFFF, n, _p(out))
@@ -189,6 +209,7 @@ class Oracle:
         self.h = lib().pto_create(W, H, SW, SH, NS)
         lib().pto_set_threads(self.h, threads)
         self.params = _abi.default_params()
+        self.pass_counter = 0
 
     def close(self):
         if self.h:
@@ -260,7 +281,8 @@ class Oracle:
         lib().pto_sync(self.h, level, 0)
 
     def scatter(self, level):
-        lib().pto_scatter(self.h, level)
+        lib().pto_scatter_pass(self.h, level, self.pass_counter)
+        self.pass_counter += 1
         lib().pto_sync(self.h, level, 0)
 
     def upsample(self, level):
@@ -342,9 +364,12 @@ class OracleDriver:
         """createRandomPyramid (single style)."""
         fp = self.frames[frame]
         s = self.styles[0]
-        rnd = random_level(frame * level, level, s["w"], s["h"], fp["rgba"][level],
-                           fp["orient"][level], s["output"][level], s["orient"][level],
-                           bool(self.user.transparencyOk), bool(self.user.orientationEnabled))
+        args = (level, s["w"], s["h"], fp["rgba"][level], fp["orient"][level], s["output"][level],
+                s["orient"][level], bool(self.user.transparencyOk), bool(self.user.orientationEnabled))
+        if self.user.rngMode == _abi.RNG_COUNTER:
+            rnd = counter_random_level(counter_seed(self.user.rngSeed, frame, level), *args)
+        else:
+            rnd = random_level(frame * level, *args)
         self.o.upload_random(rnd)
 
     def _save(self, level, frame, pass_):

@@ -241,6 +241,17 @@ static float pt_half_roundtrip(float f) {
     return sign ? -out : out;
 }
 
+/* counter-based hash of the PT_RNG_COUNTER mode (an integer mixing
+ * function: xor-shift / multiply rounds) */
+static inline uint32_t hash32(uint32_t a) {
+    a ^= a >> 16; a *= 0x7feb352dU; a ^= a >> 15; a *= 0x846ca68bU; a ^= a >> 16;
+    return a;
+}
+static inline float counter_u01(uint32_t seed, uint32_t pass, uint32_t x, uint32_t y, uint32_t n) {
+    uint32_t h = hash32(seed ^ hash32(pass * 0x9E3779B9U ^ hash32(x * 0x85EBCA6BU ^ hash32(y * 0xC2B2AE35U ^ n))));
+    return (float)(h >> 8) * (1.0f / 16777216.0f);
+}
+
 /* ------------------------------------------------------------------------ */
 /* fetches                                                                  */
 /* ------------------------------------------------------------------------ */
@@ -675,7 +686,9 @@ void pto_propagate(pto* o, int level, int jump) {
 /* scatter_kernel + averageOffset, texSynth_kernel.cu:841-952; the reference's
  * randFloat() returns unsigned int 0 (texSynth_util.h:155-163), so every
  * candidate is (best.x + 0.9*dist, best.y). */
-void pto_scatter(pto* o, int level) {
+void pto_scatter_pass(pto* o, int level, uint32_t pass_id);
+void pto_scatter(pto* o, int level) { pto_scatter_pass(o, level, 0); }
+void pto_scatter_pass(pto* o, int level, uint32_t pass_id) {
     const pt_patchxf* base = o->off_base;
     pt_patchxf* work = o->off_work;
     FOR_RECT(o, level) {
@@ -693,8 +706,21 @@ void pto_scatter(pto* o, int level) {
         make_pixctx(o, x, y, level, &pc);
         for (int i = 0; i < o->p.scatterSamplesCount && dist * factor >= closest; i++) {
             float dmin = dist * factor;
-            float ex = ow.x + dmin;
-            float ey = ow.y + 0.0f;
+            float ex, ey;
+            if (o->p.rngMode == PT_RNG_COUNTER) {
+                /* opt-in mode: radius in [dmin, dist), angle in [0, 2pi) */
+                float rr = counter_u01(o->p.rngSeed, pass_id, (uint32_t)x, (uint32_t)y, 2u * (uint32_t)i);
+                float th = counter_u01(o->p.rngSeed, pass_id, (uint32_t)x, (uint32_t)y, 2u * (uint32_t)i + 1u) *
+                           6.28318530717958647692f;
+                float s, cth;
+                pt_sincosf(th, &s, &cth);
+                float len = fmaf(rr, dist - dmin, dmin);
+                ex = fmaf(cth, len, ow.x);
+                ey = fmaf(s, len, ow.y);
+            } else {
+                ex = ow.x + dmin;
+                ey = ow.y + 0.0f;
+            }
             clamp_to_exemplar(&ex, &ey, o->ew, o->eh);
             float ang = screen_to_exemplar_angle(o, x, y, ex, ey, 0);
             pt_patchxf t = patch(ex, ey, ang, 0.0f, 0, sc.x, sc.y);
@@ -1317,6 +1343,37 @@ int pto_random_level(uint32_t seed, int w, int h, int level, int style_w0, int s
             p[0] = (float)ox + rx; p[1] = (float)oy + ry; p[2] = orient; p[3] = 0.0f;
         }
     return retried;
+}
+
+/* PT_RNG_COUNTER random level: four hashed draws per pixel and trial, with
+ * the reference's retry rule for opaque pixels on transparent texels */
+void pto_counter_random_level(uint32_t seed, int w, int h, int level, int style_w0, int style_h0,
+                              const float* img_rgba, const float* img_orient, const float* ex_out_rgba,
+                              const float* ex_orient, int ew, int transparency_ok, int orientation_enabled,
+                              float* out) {
+    int mx = (style_w0 >> level) - 1, my = (style_h0 >> level) - 1;
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            float ia = img_rgba[((size_t)y * w + x) * 4 + 3];
+            uint32_t base = hash32(seed ^ hash32((uint32_t)x * 0x85EBCA6BU ^ hash32((uint32_t)y * 0xC2B2AE35U)));
+            uint32_t d0, d1;
+            int trial = 0, again, ox, oy;
+            do {
+                d0 = hash32(base + 4u * (uint32_t)trial);
+                d1 = hash32(base + 4u * (uint32_t)trial + 1u);
+                trial++;
+                ox = (int)((d0 >> 1) % (uint32_t)mx);
+                oy = (int)((d1 >> 1) % (uint32_t)my);
+                again = !transparency_ok && ia > ALPHA_THRESHOLD &&
+                        ex_out_rgba[((size_t)oy * ew + ox) * 4 + 3] < ALPHA_THRESHOLD && trial < 50;
+            } while (again);
+            uint32_t d2 = hash32(base + 0x40000000u), d3 = hash32(base + 0x40000001u);
+            float orient = orientation_enabled ? img_orient[(size_t)y * w + x] - ex_orient[(size_t)oy * ew + ox] : 0.f;
+            float rx = (float)(d2 >> 1) / (float)2147483647;
+            float ry = (float)(d3 >> 1) / (float)2147483647;
+            float* p = out + ((size_t)y * w + x) * 4;
+            p[0] = (float)ox + rx; p[1] = (float)oy + ry; p[2] = orient; p[3] = 0.0f;
+        }
 }
 
 /* ------------------------------------------------------------------------ */
