@@ -40,8 +40,9 @@ int level_count(int w, int h) {
     return (int)std::min(std::floor(std::log2((float)w)), std::floor(std::log2((float)h)));
 }
 
-struct ExLevel {  // one exemplar pyramid level, all styles
-    float4* bo = nullptr;
+struct ExLevel {  // one exemplar pyramid level, all styles (base and output planes)
+    float4* base = nullptr;
+    float4* out = nullptr;
     float* orient = nullptr;
     float* dt = nullptr;
     int* ids = nullptr;
@@ -268,7 +269,8 @@ static Params make_params(pt_ctx* c, int level) {
     P.histH = (c->SH * c->NS) >> level;
     P.hist = c->hist[0];
     if (c->ex) {
-        P.ex.bo = c->ex->bo;
+        P.ex.base = c->ex->base;
+        P.ex.out = c->ex->out;
         P.ex.orient = c->ex->orient;
         P.ex.dt = c->ex->dt;
         P.ex.ids = c->ex->ids;
@@ -290,7 +292,7 @@ static pt_status check_ready(pt_ctx* c, int level, bool need_ex = true, bool nee
     if (!c->have_params) return fail(c, PT_ERR_STATE, "pt_set_params has not been called");
     if (level < 0 || (c->W >> level) < 1 || (c->H >> level) < 1)
         return fail(c, PT_ERR_INVALID, "level %d out of range", level);
-    if (need_ex && (!c->ex || !c->ex->bo)) return fail(c, PT_ERR_STATE, "no exemplar level loaded");
+    if (need_ex && (!c->ex || !c->ex->base)) return fail(c, PT_ERR_STATE, "no exemplar level loaded");
     if (need_img) {
         const ImgView& I = c->img;
         int lw = c->W >> level, lh = c->H >> level;
@@ -728,8 +730,10 @@ pt_status pt_initialize_exemplars(pt_ctx* c, int w, int h, int ns) {
     if (w < 2 || h < 2 || ns != c->NS) return fail(c, PT_ERR_INVALID, "bad exemplar size %dx%dx%d", w, h, ns);
     size_t n = (size_t)w * h * ns;
     if (n > c->ex_cap) {
-        dfree_t(c, c->up_ex.bo); dfree_t(c, c->up_ex.orient); dfree_t(c, c->up_ex.dt); dfree_t(c, c->up_ex.ids);
-        TRY(dalloc_t(c, &c->up_ex.bo, 2 * n));
+        dfree_t(c, c->up_ex.base); dfree_t(c, c->up_ex.out);
+        dfree_t(c, c->up_ex.orient); dfree_t(c, c->up_ex.dt); dfree_t(c, c->up_ex.ids);
+        TRY(dalloc_t(c, &c->up_ex.base, n));
+        TRY(dalloc_t(c, &c->up_ex.out, n));
         TRY(dalloc_t(c, &c->up_ex.orient, n));
         TRY(dalloc_t(c, &c->up_ex.dt, n));
         TRY(dalloc_t(c, &c->up_ex.ids, n));
@@ -759,10 +763,8 @@ pt_status pt_upload_image_color4(pt_ctx* c, int level, int layer, const float* r
         if (!c->ex || c->ex != &c->up_ex || w != c->up_ex.w || h != c->up_ex.h || style < 0 || style >= c->NS)
             return fail(c, PT_ERR_INVALID, "exemplar upload %dx%d style %d does not match pt_initialize_exemplars", w,
                         h, style);
-        TRY(ensure_stage(c, n * sizeof(float4)));
-        TRY(h2d(c, c->stage, rgba, n * sizeof(float4)));
-        LN(pt::launch_interleave((const float4*)c->stage, (int)n, c->up_ex.bo + 2 * n * style,
-                                 layer == PT_LAYER_EXEMPLAR_OUTPUT ? 1 : 0, c->stream));
+        float4* plane = (layer == PT_LAYER_EXEMPLAR_OUTPUT) ? c->up_ex.out : c->up_ex.base;
+        TRY(h2d(c, plane + n * style, rgba, n * sizeof(float4)));
         if (layer == PT_LAYER_EXEMPLAR_OUTPUT) c->up_ex.transparent = -1;
         return PT_OK;
     }
@@ -866,7 +868,7 @@ pt_status pt_flip_anim_buffers(pt_ctx* c) {
 static pt_status ensure_transparency_known(pt_ctx* c) {
     if (c->ex->transparent >= 0) return PT_OK;
     CU(cudaMemsetAsync(c->flag, 0, sizeof(int), c->stream));
-    LN(pt::launch_any_transparent(c->ex->bo, (size_t)c->ex->w * c->ex->h, c->flag, c->stream));
+    LN(pt::launch_any_transparent(c->ex->out, (size_t)c->ex->w * c->ex->h, c->flag, c->stream));
     int f = 0;
     CU(cudaMemcpyAsync(&f, c->flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));
@@ -881,7 +883,7 @@ pt_status pt_create_random_level(pt_ctx* c, int level, int frame) {
     int mx = (c->SW >> level) - 1, my = (c->SH >> level) - 1;
     if (mx < 1 || my < 1) return fail(c, PT_ERR_INVALID, "style too small for level %d", level);
     if (!c->rnd) TRY(dalloc_t(c, &c->rnd, (size_t)c->W * c->H));
-    ExView ex{c->ex->bo, c->ex->orient, c->ex->dt, c->ex->ids, c->ex->w, c->ex->h, c->NS};
+    ExView ex{c->ex->base, c->ex->out, c->ex->orient, c->ex->dt, c->ex->ids, c->ex->w, c->ex->h, c->NS};
     const ImgView& I = c->img;
     int mode;
     uint32_t seed = (uint32_t)(frame * level);
@@ -1152,7 +1154,7 @@ pt_status pt_set_style(pt_ctx* c, int style, int w, int h, const float* base, co
     int nlev = level_count(w, h);
     if ((int)c->style_levels.size() != nlev) {
         for (auto& L : c->style_levels) {
-            dfree_t(c, L.bo); dfree_t(c, L.orient); dfree_t(c, L.dt); dfree_t(c, L.ids);
+            dfree_t(c, L.base); dfree_t(c, L.out); dfree_t(c, L.orient); dfree_t(c, L.dt); dfree_t(c, L.ids);
         }
         c->style_levels.assign(nlev, ExLevel());
         for (int l = 0; l < nlev; l++) {
@@ -1160,7 +1162,8 @@ pt_status pt_set_style(pt_ctx* c, int style, int w, int h, const float* base, co
             L.w = w >> l;
             L.h = h >> l;
             size_t n = (size_t)L.w * L.h * c->NS;
-            TRY(dalloc_t(c, &L.bo, 2 * n));
+            TRY(dalloc_t(c, &L.base, n));
+            TRY(dalloc_t(c, &L.out, n));
             TRY(dalloc_t(c, &L.orient, n));
             TRY(dalloc_t(c, &L.dt, n));
             TRY(dalloc_t(c, &L.ids, n));
@@ -1184,8 +1187,8 @@ pt_status pt_set_style(pt_ctx* c, int style, int w, int h, const float* base, co
     for (int l = 0; l < nlev; l++) {
         ExLevel& L = c->style_levels[l];
         size_t n = (size_t)L.w * L.h;
-        LN(pt::launch_interleave((const float4*)pb[l], (int)n, L.bo + 2 * n * style, 0, c->stream));
-        LN(pt::launch_interleave((const float4*)po[l], (int)n, L.bo + 2 * n * style, 1, c->stream));
+        CU(cudaMemcpyAsync(L.base + n * style, pb[l], n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
+        CU(cudaMemcpyAsync(L.out + n * style, po[l], n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
         CU(cudaMemcpyAsync(L.orient + n * style, por[l], n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
         CU(cudaMemcpyAsync(L.dt + n * style, pd[l], n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
         CU(cudaMemcpyAsync(L.ids + n * style, pi[l], n * sizeof(int), cudaMemcpyDeviceToDevice, c->stream));

@@ -233,31 +233,29 @@ __device__ __forceinline__ int ex_layer(const ExView& e, int layer) { return cla
 // exemplar base and output at unnormalised (u, v), one footprint
 __device__ __forceinline__ void ex_sample2(const ExView& e, float u, float v, int layer, float4* base, float4* out) {
     Bl b = bl_setup(u, v, e.w, e.h);
-    const float4* L = e.bo + (size_t)ex_layer(e, layer) * e.w * e.h * 2;
-    const float4* r0 = L + (size_t)b.y0 * e.w * 2;
-    const float4* r1 = L + (size_t)b.y1 * e.w * 2;
-    float4 b00 = __ldg(r0 + 2 * b.x0), o00 = __ldg(r0 + 2 * b.x0 + 1);
-    float4 b10 = __ldg(r0 + 2 * b.x1), o10 = __ldg(r0 + 2 * b.x1 + 1);
-    float4 b01 = __ldg(r1 + 2 * b.x0), o01 = __ldg(r1 + 2 * b.x0 + 1);
-    float4 b11 = __ldg(r1 + 2 * b.x1), o11 = __ldg(r1 + 2 * b.x1 + 1);
+    const size_t L = (size_t)ex_layer(e, layer) * e.w * e.h;
+    const size_t r0 = L + (size_t)b.y0 * e.w, r1 = L + (size_t)b.y1 * e.w;
+    float4 b00 = __ldg(e.base + r0 + b.x0), b10 = __ldg(e.base + r0 + b.x1);
+    float4 b01 = __ldg(e.base + r1 + b.x0), b11 = __ldg(e.base + r1 + b.x1);
+    float4 o00 = __ldg(e.out + r0 + b.x0), o10 = __ldg(e.out + r0 + b.x1);
+    float4 o01 = __ldg(e.out + r1 + b.x0), o11 = __ldg(e.out + r1 + b.x1);
     *base = bl4(b, b00, b10, b01, b11);
     *out = bl4(b, o00, o10, o01, o11);
 }
 __device__ __forceinline__ float4 ex_sample_out(const ExView& e, float u, float v, int layer) {
     Bl b = bl_setup(u, v, e.w, e.h);
-    const float4* L = e.bo + (size_t)ex_layer(e, layer) * e.w * e.h * 2;
-    const float4* r0 = L + (size_t)b.y0 * e.w * 2;
-    const float4* r1 = L + (size_t)b.y1 * e.w * 2;
-    return bl4(b, __ldg(r0 + 2 * b.x0 + 1), __ldg(r0 + 2 * b.x1 + 1),
-               __ldg(r1 + 2 * b.x0 + 1), __ldg(r1 + 2 * b.x1 + 1));
+    const size_t L = (size_t)ex_layer(e, layer) * e.w * e.h;
+    const size_t r0 = L + (size_t)b.y0 * e.w, r1 = L + (size_t)b.y1 * e.w;
+    return bl4(b, __ldg(e.out + r0 + b.x0), __ldg(e.out + r0 + b.x1), __ldg(e.out + r1 + b.x0),
+               __ldg(e.out + r1 + b.x1));
 }
 __device__ __forceinline__ float ex_sample_out_alpha(const ExView& e, float u, float v, int layer) {
     Bl b = bl_setup(u, v, e.w, e.h);
-    const float* L = (const float*)(e.bo + (size_t)ex_layer(e, layer) * e.w * e.h * 2);
-    const float* r0 = L + (size_t)b.y0 * e.w * 8;
-    const float* r1 = L + (size_t)b.y1 * e.w * 8;
-    return bl1(b, __ldg(r0 + 8 * b.x0 + 7), __ldg(r0 + 8 * b.x1 + 7),
-               __ldg(r1 + 8 * b.x0 + 7), __ldg(r1 + 8 * b.x1 + 7));
+    const float* L = (const float*)(e.out + (size_t)ex_layer(e, layer) * e.w * e.h);
+    const float* r0 = L + (size_t)b.y0 * e.w * 4;
+    const float* r1 = L + (size_t)b.y1 * e.w * 4;
+    return bl1(b, __ldg(r0 + 4 * b.x0 + 3), __ldg(r0 + 4 * b.x1 + 3),
+               __ldg(r1 + 4 * b.x0 + 3), __ldg(r1 + 4 * b.x1 + 3));
 }
 __device__ __forceinline__ float ex_sample_dt(const ExView& e, float u, float v, int layer) {
     Bl b = bl_setup(u, v, e.w, e.h);

@@ -40,16 +40,12 @@ struct TileSmem {
     float phys[TM ? N : 1];
 };
 
-// one exemplar texel (base, output): 32 contiguous bytes, one sector
-__device__ __forceinline__ void ld_texel(const float4* p, float4* b, float4* o) {
-    *b = __ldg(p);
-    *o = __ldg(p + 1);
-}
-
-// bilinear base+output at (u, v) of one exemplar layer; FAST: the footprint
-// is known to be inside [0, w-1] x [0, h-1] (no clamping needed)
+// bilinear base+output at (u, v) of one exemplar layer (LB: base plane,
+// LO: output plane); FAST: the footprint is known to be inside
+// [0, w-1] x [0, h-1] (no clamping needed)
 template <bool FAST>
-__device__ __forceinline__ void sample2(const float4* L, int w, int h, float u, float v, float4* base, float4* out) {
+__device__ __forceinline__ void sample2(const float4* LB, const float4* LO, int w, int h, float u, float v,
+                                        float4* base, float4* out) {
     float xs = u + 0.5f, ys = v + 0.5f;
     float xb = xs - 0.5f, yb = ys - 0.5f;
     float fx = floorf(xb), fy = floorf(yb);
@@ -67,13 +63,11 @@ __device__ __forceinline__ void sample2(const float4* L, int w, int h, float u, 
     float oa = 1.0f - a, oc = 1.0f - c;
     Bl bw;
     bw.w00 = oa * oc; bw.w10 = a * oc; bw.w01 = oa * c; bw.w11 = a * c;
-    float4 b00, o00, b10, o10, b01, o01, b11, o11;
-    const float4* r0 = L + (size_t)y0 * w * 2;
-    const float4* r1 = L + (size_t)y1 * w * 2;
-    ld_texel(r0 + 2 * x0, &b00, &o00);
-    ld_texel(r0 + 2 * x1, &b10, &o10);
-    ld_texel(r1 + 2 * x0, &b01, &o01);
-    ld_texel(r1 + 2 * x1, &b11, &o11);
+    const size_t r0 = (size_t)y0 * w, r1 = (size_t)y1 * w;
+    float4 b00 = __ldg(LB + r0 + x0), b10 = __ldg(LB + r0 + x1);
+    float4 b01 = __ldg(LB + r1 + x0), b11 = __ldg(LB + r1 + x1);
+    float4 o00 = __ldg(LO + r0 + x0), o10 = __ldg(LO + r0 + x1);
+    float4 o01 = __ldg(LO + r1 + x0), o11 = __ldg(LO + r1 + x1);
     *base = bl4(bw, b00, b10, b01, b11);
     *out = bl4(bw, o00, o10, o01, o11);
 }
@@ -110,9 +104,11 @@ template <int R, int TM, bool FAST, bool FASTP>
 __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
                                              const Cand& c, float2 b0, float2 b1, float sum0) {
     constexpr int TW = TileSmem<R, TM>::TW;
-    const float4* L = P.ex.bo + (size_t)ex_layer(P.ex, c.layer) * P.ex.w * P.ex.h * 2;
-    const float4* LP = nullptr;
-    if (TM) LP = P.ex.bo + (size_t)ex_layer(P.ex, px.prev.layer) * P.ex.w * P.ex.h * 2;
+    const size_t lsz = (size_t)P.ex.w * P.ex.h;
+    const size_t lo = (size_t)ex_layer(P.ex, c.layer) * lsz;
+    const float4* LB = P.ex.base + lo;
+    const float4* LO = P.ex.out + lo;
+    const size_t lp = TM ? (size_t)ex_layer(P.ex, px.prev.layer) * lsz : 0;
     const float hw = (float)P.histW, hh = (float)P.histH;
     float sum = sum0, sumW = 0.0f;
 #pragma unroll 1
@@ -130,7 +126,7 @@ __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, 
                 if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
             }
             float4 tb, to;
-            sample2<FAST>(L, P.ex.w, P.ex.h, tx, ty, &tb, &to);
+            sample2<FAST>(LB, LO, P.ex.w, P.ex.h, tx, ty, &tb, &to);
             float res = ssd_a(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
             if (TM) {
                 if (px.temporal) {
@@ -138,7 +134,7 @@ __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, 
                     float ptx = px.prev.x + fmaf((float)i, px.pb0.x, (float)j * px.pb1.x);
                     float pty = px.prev.y + fmaf((float)i, px.pb0.y, (float)j * px.pb1.y);
                     float4 peb, peo;
-                    sample2<FASTP>(LP, P.ex.w, P.ex.h, ptx, pty, &peb, &peo);
+                    sample2<FASTP>(P.ex.base + lp, P.ex.out + lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo);
                     float r = ssd(sub4(base, pbase), sub4(tb, peb)) * P.tdIn;
                     r = fmaf(ssd(sub4(canvas, pout), sub4(to, peo)), P.tdOut, r);
                     r = fmaf(ssd(pout, to), P.tc, r);
@@ -261,6 +257,188 @@ __device__ __forceinline__ bool stage_tile(const Params& P, TileSmem<R, TM>& T, 
         }
     }
     return true;
+}
+
+// Up to four candidates of one pixel evaluated in one tap loop: the
+// pixel-side reads and, for temporal passes, the previous-frame exemplar
+// sample of each tap (both independent of the candidate) are done once per
+// tap; every candidate keeps its own sums in the reference's tap order, so
+// each energy is bit-identical to a separate evaluation.
+template <int R, int TM, bool FAST, bool FASTP>
+__device__ __forceinline__ void energy4_taps(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
+                                             const Cand* c, const float2* b0, const float2* b1, int n,
+                                             float* sum, float* sumW) {
+    constexpr int TW = TileSmem<R, TM>::TW;
+    const size_t lsz = (size_t)P.ex.w * P.ex.h;
+    size_t lo[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) lo[k] = (size_t)ex_layer(P.ex, c[k].layer) * lsz;
+    const size_t lp = TM ? (size_t)ex_layer(P.ex, px.prev.layer) * lsz : 0;
+    const float hw = (float)P.histW, hh = (float)P.histH;
+#pragma unroll 1
+    for (int i = -R; i <= R; i++) {
+#pragma unroll 1
+        for (int j = -R; j <= R; j++) {
+            const bool valid = (i >= px.imin) && (i <= px.imax) && (j >= px.jmin) && (j <= px.jmax);
+            const int s = px.sidx + j * TW + i;
+            const float4 base = T.base[s];
+            const float4 canvas = T.canvas[s];
+            float4 pbase, pout, peb, peo;
+            bool tvalid = false;
+            if (TM) {
+                if (px.temporal) {
+                    pbase = T.pbase[s];
+                    pout = T.pout[s];
+                    float ptx = px.prev.x + fmaf((float)i, px.pb0.x, (float)j * px.pb1.x);
+                    float pty = px.prev.y + fmaf((float)i, px.pb0.y, (float)j * px.pb1.y);
+                    sample2<FASTP>(P.ex.base + lp, P.ex.out + lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo);
+                    tvalid = T.phys[s] > 0;
+                }
+            }
+            const float w = P.gauss[i + R] * P.gauss[j + R];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                if (k < n) {
+                    float tx = c[k].x + fmaf((float)i, b0[k].x, (float)j * b1[k].x);
+                    float ty = c[k].y + fmaf((float)i, b0[k].y, (float)j * b1[k].y);
+                    if (!FAST) {
+                        if (tx >= hw) tx -= hw; else if (tx < 0) tx += hw;
+                        if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
+                    }
+                    float4 tb, to;
+                    sample2<FAST>(P.ex.base + lo[k], P.ex.out + lo[k], P.ex.w, P.ex.h, tx, ty, &tb, &to);
+                    float res = ssd_a(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
+                    if (TM) {
+                        if (px.temporal) {
+                            float r = ssd(sub4(base, pbase), sub4(tb, peb)) * P.tdIn;
+                            r = fmaf(ssd(sub4(canvas, pout), sub4(to, peo)), P.tdOut, r);
+                            r = fmaf(ssd(pout, to), P.tc, r);
+                            res = tvalid ? res + r : res;
+                        }
+                    }
+                    if (i == 0 && j == 0) {
+                        if (P.distTransWeight > 0.f) {
+                            float de = ex_sample_dt(P.ex, tx, ty, c[k].layer) / c[k].sv;
+                            float di = lay_texel(P.img.dt[P.img.cur], P, px.x, px.y);
+                            float diff = fminf(fmaxf(fabsf(de - di), 0.0f), 10.0f);
+                            res = res + diff * P.distTransWeight;
+                        }
+                        {
+                            int Lh = clampi(c[k].layer, 0, PT_MAX_STYLES - 1);
+                            float sh = (float)(P.histH / P.numStyles);
+                            int hx = clampi((int)tx, 0, P.histPitch - 1);
+                            int hy = clampi((int)(ty + sh * (float)c[k].layer), 0, P.histRows - 1);
+                            float h = __ldg(P.hist + (size_t)hy * P.histPitch + hx);
+                            float thr = P.histThreshold[Lh];
+                            res = res + ((h > thr) ? (h - thr) * P.histSlope[Lh] : 0.0f);
+                        }
+                        if (P.styleObjIdWeight > 0.f) {
+                            int imgID = lvl_texel(P.img.ids, px.x, px.y);
+                            int styleID = ex_point_id(P.ex, tx, ty, c[k].layer);
+                            res = res + ((imgID != styleID) ? P.styleObjIdWeight : 0.0f);
+                        }
+                    } else {
+                        res = fmaf(ssd_a(canvas, to, P.alphaWeight), P.canvasOutputWeight, res);
+                    }
+                    sum[k] = valid ? fmaf(res, w, sum[k]) : sum[k];
+                    sumW[k] = valid ? sumW[k] + w : sumW[k];
+                }
+            }
+        }
+    }
+}
+
+// energies of n <= 4 candidates (kBigResidual where sumW < eps)
+template <int R, int TM>
+__device__ __forceinline__ void energy4(const Params& P, const TileSmem<R, TM>& T, const PixT& px, const Cand* c,
+                                        int n, float* out) {
+    float2 b0[4], b1[4];
+    float sum[4], sumW[4];
+    bool fast = true;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        sum[k] = 0.0f;
+        if (px.hyst_on) sum[k] = sum[k] - px.hyst;
+        sumW[k] = 0.0f;
+        b0[k] = make_float2(0.f, 0.f);
+        b1[k] = make_float2(0.f, 0.f);
+        if (k < n) {
+            basis(c[k].theta, P.scaleWU * c[k].su, P.scaleWV * c[k].sv, &b0[k], &b1[k]);
+            fast = fast && footprint_inside<R>(c[k].x, c[k].y, b0[k], b1[k], P.ex.w, P.ex.h);
+        }
+    }
+    if (TM) fast = fast && (!px.temporal || px.prev_fast);
+    fast = __all_sync(__activemask(), fast);
+    if (fast) energy4_taps<R, TM, true, true>(P, T, px, c, b0, b1, n, sum, sumW);
+    else energy4_taps<R, TM, false, false>(P, T, px, c, b0, b1, n, sum, sumW);
+#pragma unroll
+    for (int k = 0; k < 4; k++) out[k] = (sumW[k] < kEpsilon) ? kBigResidual : sum[k] / sumW[k];
+}
+
+// propagate_kernel with the four jump candidates evaluated together
+template <int R, int TM>
+__global__ void __launch_bounds__(kTileThreads, 2) kt_propagate4(const Params P, PatchPlanes work, int jump) {
+    __shared__ TileSmem<R, TM> T;
+    PixT px;
+    if (!stage_tile<R, TM>(P, T, &px)) return;
+    const int x = px.x, y = px.y;
+    const size_t k = (size_t)y * P.W + x;
+    if (image_culled(P, x, y)) {
+        store_patch(work, k, make_patch(0, 0, 0, 0, 0, 1.f, 1.f));
+        return;
+    }
+    float best = __ldg(P.res + k);
+    float ia = T.base[px.sidx].w;
+    Patch ow = load_patch(P.off, k);
+    // the four candidates in the reference's order; a candidate that repeats
+    // an earlier one, or that test_offset rejects before the energy, keeps
+    // its fixed outcome
+    Patch cand[4];
+    float res[4];
+    int slot[4];
+    Cand ev[4];
+    int n = 0;
+#pragma unroll
+    for (int cdx = 0; cdx < 4; cdx++) {
+        int tx = x, ty = y;
+        if (cdx == 0) tx = x + jump;
+        else if (cdx == 1) tx = x - jump;
+        else if (cdx == 2) ty = y + jump;
+        else ty = y - jump;
+        cand[cdx] = propagate_offset(P, tx, ty, x, y);
+        slot[cdx] = -1;
+        res[cdx] = kBigResidual;
+        bool dup = false;
+#pragma unroll
+        for (int q = 0; q < cdx; q++)
+            dup |= __float_as_uint(cand[q].x) == __float_as_uint(cand[cdx].x) &&
+                   __float_as_uint(cand[q].y) == __float_as_uint(cand[cdx].y) &&
+                   __float_as_uint(cand[q].theta) == __float_as_uint(cand[cdx].theta) &&
+                   cand[q].layer == cand[cdx].layer;
+        if (dup) { slot[cdx] = -2; continue; }
+        const Patch& t = cand[cdx];
+        float dte = ex_texel_dt(P.ex, (int)t.x, (int)t.y, t.layer);
+        if ((double)dte > (double)P.distTransCull * 1.25) continue;
+        if (!P.transparencyOk) {
+            float ea = ex_sample_out_alpha(P.ex, t.x, t.y, t.layer);
+            if (ea < kAlphaThreshold && ia > kAlphaThreshold) continue;
+        }
+        if (P.counters) count_eval(P, x, y);
+        ev[n] = Cand{t.x, t.y, t.theta, t.su, t.sv, t.layer};
+        slot[cdx] = n;
+        n++;
+    }
+    float e[4];
+    energy4<R, TM>(P, T, px, ev, n, e);
+#pragma unroll
+    for (int cdx = 0; cdx < 4; cdx++) {
+        if (slot[cdx] == -2) continue;  // repeat: same energy, rejected by "<"
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if (slot[cdx] == q) res[cdx] = e[q];
+        if (res[cdx] < best) { ow = cand[cdx]; best = res[cdx]; }
+    }
+    store_patch(work, k, ow);
 }
 
 // propagate_kernel, texSynth_kernel.cu:1112-1219
@@ -401,7 +579,8 @@ cudaError_t launch_tiled_r(int kind, int tm, const Params& P, PatchPlanes work, 
                            cudaStream_t s) {
     dim3 b(kTileW, kTileH), g((P.lw + kTileW - 1) / kTileW, (P.lh + kTileH - 1) / kTileH);
 #define PT_TILED_DISPATCH(TMV)                                                                   \
-    if (kind == 0) kt_propagate<R, TMV><<<g, b, 0, s>>>(P, work, arg);                          \
+    if (kind == 0) kt_propagate4<R, TMV><<<g, b, 0, s>>>(P, work, arg);                         \
+    else if (kind == 3) kt_propagate<R, TMV><<<g, b, 0, s>>>(P, work, arg);                     \
     else if (kind == 1) kt_scatter<R, TMV><<<g, b, 0, s>>>(P, work, arg, pass_id);              \
     else kt_residual<R, TMV><<<g, b, 0, s>>>(P, out);
     if (tm == TM_NONE) { PT_TILED_DISPATCH(TM_NONE) }

@@ -35,11 +35,10 @@ cudaError_t launch_gather_level(const Params& P, const float* src, int ch, float
 cudaError_t launch_down_avg(const float* src, int w, int h, int ch, int vel, float* dst, cudaStream_t s);
 cudaError_t launch_down_vote(const int* src, int w, int h, int* dst, cudaStream_t s);
 cudaError_t launch_tensor_angle(const float* t3, int n, float* out, cudaStream_t s);
-cudaError_t launch_interleave(const float4* src, int n, float4* bo, int which, cudaStream_t s);
 cudaError_t launch_random_level(int mode, int w, int h, int mx, int my, int transparencyOk, int orientationEnabled,
                                 Arr<float4> img, Arr<float> iorient, ExView ex, float4* out,
                                 const uint32_t* states, uint32_t seed, cudaStream_t s);
-cudaError_t launch_any_transparent(const float4* bo, size_t n, int* flag, cudaStream_t s);
+cudaError_t launch_any_transparent(const float4* out, size_t n, int* flag, cudaStream_t s);
 
 // tiled patch-distance kernels for patch radius 2, 3, 4 (pt_tiled_r*.cu):
 // kind 0 = propagate (arg = jump), 1 = scatter (arg = write_all),

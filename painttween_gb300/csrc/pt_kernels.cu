@@ -394,13 +394,6 @@ __global__ void k_tensor_angle(const float* t3, int n, float* out) {
     out[i] = ((double)angle >= 1.57079632679489661923) ? (float)((double)angle - 3.14159265358979323846) : angle;
 }
 
-// base/output interleaving of one exemplar layer
-__global__ void k_interleave(const float4* src, int n, float4* bo, int which) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    bo[2 * (size_t)i + which] = __ldg(src + i);
-}
-
 // ---------------------------------------------------------------------------
 // random-offset level (SynthesisFrame::createRandomPyramid,
 // synthesisFrame.cpp:66-150)
@@ -481,7 +474,7 @@ __global__ void k_glibc_serial(const RandParams R, const uint32_t* state31) {
                 d1 = next();
                 trial++;
                 int ox = (int)((d0 >> 1) % (uint32_t)R.mx), oy = (int)((d1 >> 1) % (uint32_t)R.my);
-                float ea = __ldg(R.ex.bo + ((size_t)oy * R.ex.w + ox) * 2 + 1).w;
+                float ea = __ldg(R.ex.out + (size_t)oy * R.ex.w + ox).w;
                 again = !R.transparencyOk && ia > kAlphaThreshold && ea < kAlphaThreshold && trial < 50;
             } while (again);
             uint32_t d2 = next(), d3 = next();
@@ -504,7 +497,7 @@ __global__ void k_counter_random(const RandParams R, uint32_t seed) {
         d1 = hash32(base + 4u * trial + 1u);
         trial++;
         int ox = (int)((d0 >> 1) % (uint32_t)R.mx), oy = (int)((d1 >> 1) % (uint32_t)R.my);
-        float ea = __ldg(R.ex.bo + ((size_t)oy * R.ex.w + ox) * 2 + 1).w;
+        float ea = __ldg(R.ex.out + (size_t)oy * R.ex.w + ox).w;
         again = !R.transparencyOk && ia > kAlphaThreshold && ea < kAlphaThreshold && trial < 50;
     } while (again);
     uint32_t d2 = hash32(base + 0x40000000u), d3 = hash32(base + 0x40000001u);
@@ -513,10 +506,10 @@ __global__ void k_counter_random(const RandParams R, uint32_t seed) {
 
 // any exemplar output texel with alpha < 0.99 (decides whether the random
 // level can be drawn row-parallel)
-__global__ void k_any_transparent(const float4* bo, size_t n, int* flag) {
+__global__ void k_any_transparent(const float4* out, size_t n, int* flag) {
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     for (; i < n; i += (size_t)gridDim.x * blockDim.x)
-        if (__ldg(bo + 2 * i + 1).w < kAlphaThreshold) { atomicOr(flag, 1); return; }
+        if (__ldg(out + i).w < kAlphaThreshold) { atomicOr(flag, 1); return; }
 }
 
 }  // namespace ptk
@@ -616,10 +609,6 @@ cudaError_t launch_tensor_angle(const float* t3, int n, float* out, cudaStream_t
     k_tensor_angle<<<(n + 255) / 256, 256, 0, s>>>(t3, n, out);
     LAUNCH_CHECK();
 }
-cudaError_t launch_interleave(const float4* src, int n, float4* bo, int which, cudaStream_t s) {
-    k_interleave<<<(n + 255) / 256, 256, 0, s>>>(src, n, bo, which);
-    LAUNCH_CHECK();
-}
 cudaError_t launch_random_level(int mode, int w, int h, int mx, int my, int transparencyOk, int orientationEnabled,
                                 Arr<float4> img, Arr<float> iorient, ExView ex, float4* out,
                                 const uint32_t* states, uint32_t seed, cudaStream_t s) {
@@ -638,8 +627,8 @@ cudaError_t launch_random_level(int mode, int w, int h, int mx, int my, int tran
     }
     LAUNCH_CHECK();
 }
-cudaError_t launch_any_transparent(const float4* bo, size_t n, int* flag, cudaStream_t s) {
-    k_any_transparent<<<152 * 4, 256, 0, s>>>(bo, n, flag);
+cudaError_t launch_any_transparent(const float4* out, size_t n, int* flag, cudaStream_t s) {
+    k_any_transparent<<<152 * 4, 256, 0, s>>>(out, n, flag);
     LAUNCH_CHECK();
 }
 

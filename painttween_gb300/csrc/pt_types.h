@@ -26,11 +26,12 @@ struct PatchPlanes {
     float* C;
 };
 
-// One exemplar pyramid level: ns styles of w x h texels; base and output are
-// interleaved per texel (32 bytes: base RGBA, output RGBA) so one bilinear
-// footprint of both images is four 32-byte sectors.
+// One exemplar pyramid level: ns styles of w x h texels, base and output
+// colours in two planes (16-byte texels), so that the gathers of neighbouring
+// pixels, which sample neighbouring texels, share cache lines.
 struct ExView {
-    const float4* bo;
+    const float4* base;
+    const float4* out;
     const float* orient;
     const float* dt;
     const int* ids;
