@@ -560,6 +560,140 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter(const Params P, Pa
     else if (write_all) store_patch(work, k, off);
 }
 
+// scatter_kernel with the chain evaluated in speculative batches: the next
+// (up to) four distinct chain candidates for the current best offset are
+// evaluated together; they are then accepted in chain order, and after an
+// acceptance the rest of the batch (built from the old best) is discarded
+// and the chain continues from the next index.  The decisions, and so the
+// result, are those of the one-by-one chain.
+template <int R, int TM>
+__global__ void __launch_bounds__(kTileThreads, 2) kt_scatter4(const Params P, PatchPlanes work, int write_all,
+                                                              uint32_t pass_id) {
+    __shared__ TileSmem<R, TM> T;
+    PixT px;
+    if (!stage_tile<R, TM>(P, T, &px)) return;
+    const int x = px.x, y = px.y;
+    const size_t k = (size_t)y * P.W + x;
+    Patch off = load_patch(P.off, k);
+    if (image_culled(P, x, y)) {
+        if (write_all) store_patch(work, k, off);
+        return;
+    }
+    float cached = __ldg(P.res + k);
+    float best = (float)((double)cached + 10e-7);
+    Patch ow = off;
+    float ia = T.base[px.sidx].w;
+    const float closest = 10.f, factor = 0.9f;
+    float2 sc = lvl_texel(P.img.scale, x, y);
+    float dist = (float)(P.ex.w > P.ex.h ? P.ex.w : P.ex.h);
+    int i = 0;
+    uint32_t lastx = 0xffffffffu, lasty = 0xffffffffu;
+#pragma unroll 1
+    while (true) {
+        Cand c[4];
+        float dnext[4];
+        int inext[4];
+        bool pre[4];   // rejected by test_offset before the energy
+        int n = 0;
+        int j = i;
+        float d = dist;
+        uint32_t lx = lastx, ly = lasty;
+#pragma unroll 1
+        while (n < 4 && j < P.scatterSamples && d * factor >= closest) {
+            float dmin = d * factor;
+            float ex, ey;
+            if (P.rngMode == PT_RNG_COUNTER) {
+                float rr = counter_u01(P.rngSeed, pass_id, x, y, 2 * j);
+                float th = counter_u01(P.rngSeed, pass_id, x, y, 2 * j + 1) * 6.28318530717958647692f;
+                float s, cc;
+                sincos_poly(th, &s, &cc);
+                float len = fmaf(rr, d - dmin, dmin);
+                ex = fmaf(cc, len, ow.x);
+                ey = fmaf(s, len, ow.y);
+            } else {
+                ex = ow.x + dmin;
+                ey = ow.y + 0.0f;
+            }
+            clamp_to_exemplar(&ex, &ey, P.ex.w, P.ex.h);
+            j++;
+            d *= factor;
+            if (__float_as_uint(ex) == lx && __float_as_uint(ey) == ly) continue;  // repeat: rejected by "<"
+            lx = __float_as_uint(ex);
+            ly = __float_as_uint(ey);
+            float ang = screen_to_exemplar_angle(P, x, y, ex, ey, 0);
+            c[n] = Cand{ex, ey, ang, sc.x, sc.y, 0};
+            dnext[n] = d;
+            inext[n] = j;
+            float dte = ex_texel_dt(P.ex, (int)ex, (int)ey, 0);
+            pre[n] = (double)dte > (double)P.distTransCull * 1.25;
+            if (!pre[n] && !P.transparencyOk) {
+                float ea = ex_sample_out_alpha(P.ex, ex, ey, 0);
+                pre[n] = ea < kAlphaThreshold && ia > kAlphaThreshold;
+            }
+            n++;
+        }
+        if (n == 0) break;
+        // evaluate the candidates that reach the energy (compacted)
+        Cand evc[4];
+        int m = 0;
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if (q < n && !pre[q]) { evc[m] = c[q]; m++; }
+        if (P.counters)
+            for (int q = 0; q < m; q++) count_eval(P, x, y);
+        float e[4];
+        energy4<R, TM>(P, T, px, evc, m, e);
+        int accepted = -1, mi = 0;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if (q < n && accepted < 0) {
+                float r = kBigResidual;
+                if (!pre[q]) {
+#pragma unroll
+                    for (int t = 0; t < 4; t++)
+                        if (t == mi) r = e[t];
+                    mi++;
+                }
+                if (r < best) {
+                    ow = make_patch(c[q].x, c[q].y, c[q].theta, 0.0f, 0, sc.x, sc.y);
+                    best = r;
+                    accepted = q;
+                }
+            }
+        }
+        if (accepted >= 0) {
+            i = inext[accepted];
+            dist = dnext[accepted];
+            lastx = __float_as_uint(c[accepted].x);
+            lasty = __float_as_uint(c[accepted].y);
+        } else {
+            i = j;
+            dist = d;
+            lastx = lx;
+            lasty = ly;
+        }
+    }
+    Patch avg = make_patch(0, 0, 0, 1.f, 0, 1.f, 1.f);
+    int nn = 0;
+    for (int a = -1; a <= 1; a++)
+        for (int b = -1; b <= 1; b++) {
+            if (!in_rect(P, x + a, y + b) || (a == 0 && b == 0)) continue;
+            float4 nb = __ldg(P.off.A + (size_t)(y + b) * P.W + (x + a));
+            if (__float_as_int(nb.w) != 0) continue;
+            avg.x = avg.x + nb.x;
+            avg.y = avg.y + nb.y;
+            nn++;
+        }
+    avg.x = avg.x / (float)nn;
+    avg.y = avg.y / (float)nn;
+    avg.theta = screen_to_exemplar_angle(P, x, y, avg.x, avg.y, 0);
+    Cand ca{avg.x, avg.y, avg.theta, avg.su, avg.sv, 0};
+    float r = test_offset_tiled<R, TM>(P, T, px, ca, ia);
+    if (r < best) { ow = avg; best = r; }
+    if (best < cached) store_patch(work, k, ow);
+    else if (write_all) store_patch(work, k, off);
+}
+
 // updateResidualCache_kernel, texSynth_kernel.cu:661-693
 template <int R, int TM>
 __global__ void __launch_bounds__(kTileThreads, 2) kt_residual(const Params P, float* out) {
@@ -581,7 +715,8 @@ cudaError_t launch_tiled_r(int kind, int tm, const Params& P, PatchPlanes work, 
 #define PT_TILED_DISPATCH(TMV)                                                                   \
     if (kind == 0) kt_propagate4<R, TMV><<<g, b, 0, s>>>(P, work, arg);                         \
     else if (kind == 3) kt_propagate<R, TMV><<<g, b, 0, s>>>(P, work, arg);                     \
-    else if (kind == 1) kt_scatter<R, TMV><<<g, b, 0, s>>>(P, work, arg, pass_id);              \
+    else if (kind == 1) kt_scatter4<R, TMV><<<g, b, 0, s>>>(P, work, arg, pass_id);             \
+    else if (kind == 4) kt_scatter<R, TMV><<<g, b, 0, s>>>(P, work, arg, pass_id);              \
     else kt_residual<R, TMV><<<g, b, 0, s>>>(P, out);
     if (tm == TM_NONE) { PT_TILED_DISPATCH(TM_NONE) }
     else if (tm == TM_FWD) { PT_TILED_DISPATCH(TM_FWD) }
