@@ -264,15 +264,15 @@ __device__ __forceinline__ bool stage_tile(const Params& P, TileSmem<R, TM>& T, 
 // sample of each tap (both independent of the candidate) are done once per
 // tap; every candidate keeps its own sums in the reference's tap order, so
 // each energy is bit-identical to a separate evaluation.
-template <int R, int TM, bool FAST, bool FASTP>
-__device__ __forceinline__ void energy4_taps(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
+template <int R, int TM, int NC, bool FASTP>
+__device__ __forceinline__ void energyN_taps(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
                                              const Cand* c, const float2* b0, const float2* b1, int n,
-                                             float* sum, float* sumW) {
+                                             const bool* fast, float* sum, float* sumW) {
     constexpr int TW = TileSmem<R, TM>::TW;
     const size_t lsz = (size_t)P.ex.w * P.ex.h;
-    size_t lo[4];
+    size_t lo[NC];
 #pragma unroll
-    for (int k = 0; k < 4; k++) lo[k] = (size_t)ex_layer(P.ex, c[k].layer) * lsz;
+    for (int k = 0; k < NC; k++) lo[k] = (size_t)ex_layer(P.ex, c[k].layer) * lsz;
     const size_t lp = TM ? (size_t)ex_layer(P.ex, px.prev.layer) * lsz : 0;
     const float hw = (float)P.histW, hh = (float)P.histH;
 #pragma unroll 1
@@ -297,16 +297,18 @@ __device__ __forceinline__ void energy4_taps(const Params& P, const TileSmem<R, 
             }
             const float w = P.gauss[i + R] * P.gauss[j + R];
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
+            for (int k = 0; k < NC; k++) {
                 if (k < n) {
                     float tx = c[k].x + fmaf((float)i, b0[k].x, (float)j * b1[k].x);
                     float ty = c[k].y + fmaf((float)i, b0[k].y, (float)j * b1[k].y);
-                    if (!FAST) {
+                    float4 tb, to;
+                    if (fast[k]) {  // warp-uniform: footprint inside the exemplar
+                        sample2<true>(P.ex.base + lo[k], P.ex.out + lo[k], P.ex.w, P.ex.h, tx, ty, &tb, &to);
+                    } else {
                         if (tx >= hw) tx -= hw; else if (tx < 0) tx += hw;
                         if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
+                        sample2<false>(P.ex.base + lo[k], P.ex.out + lo[k], P.ex.w, P.ex.h, tx, ty, &tb, &to);
                     }
-                    float4 tb, to;
-                    sample2<FAST>(P.ex.base + lo[k], P.ex.out + lo[k], P.ex.w, P.ex.h, tx, ty, &tb, &to);
                     float res = ssd_a(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
                     if (TM) {
                         if (px.temporal) {
@@ -348,36 +350,44 @@ __device__ __forceinline__ void energy4_taps(const Params& P, const TileSmem<R, 
     }
 }
 
-// energies of n <= 4 candidates (kBigResidual where sumW < eps)
-template <int R, int TM>
-__device__ __forceinline__ void energy4(const Params& P, const TileSmem<R, TM>& T, const PixT& px, const Cand* c,
+// energies of n <= NC candidates (kBigResidual where sumW < eps)
+template <int R, int TM, int NC>
+__device__ __forceinline__ void energyN(const Params& P, const TileSmem<R, TM>& T, const PixT& px, const Cand* c,
                                         int n, float* out) {
-    float2 b0[4], b1[4];
-    float sum[4], sumW[4];
-    bool fast = true;
+    float2 b0[NC], b1[NC];
+    float sum[NC], sumW[NC];
+    bool fast[NC];
+    const unsigned mask = __activemask();
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
+    for (int k = 0; k < NC; k++) {
         sum[k] = 0.0f;
         if (px.hyst_on) sum[k] = sum[k] - px.hyst;
         sumW[k] = 0.0f;
         b0[k] = make_float2(0.f, 0.f);
         b1[k] = make_float2(0.f, 0.f);
+        bool f = true;
         if (k < n) {
             basis(c[k].theta, P.scaleWU * c[k].su, P.scaleWV * c[k].sv, &b0[k], &b1[k]);
-            fast = fast && footprint_inside<R>(c[k].x, c[k].y, b0[k], b1[k], P.ex.w, P.ex.h);
+            f = footprint_inside<R>(c[k].x, c[k].y, b0[k], b1[k], P.ex.w, P.ex.h);
         }
+        fast[k] = __all_sync(mask, f);
     }
-    if (TM) fast = fast && (!px.temporal || px.prev_fast);
-    fast = __all_sync(__activemask(), fast);
-    if (fast) energy4_taps<R, TM, true, true>(P, T, px, c, b0, b1, n, sum, sumW);
-    else energy4_taps<R, TM, false, false>(P, T, px, c, b0, b1, n, sum, sumW);
+    bool fastp = true;
+    if (TM) fastp = __all_sync(mask, !px.temporal || px.prev_fast);
+    if (fastp) energyN_taps<R, TM, NC, true>(P, T, px, c, b0, b1, n, fast, sum, sumW);
+    else energyN_taps<R, TM, NC, false>(P, T, px, c, b0, b1, n, fast, sum, sumW);
 #pragma unroll
-    for (int k = 0; k < 4; k++) out[k] = (sumW[k] < kEpsilon) ? kBigResidual : sum[k] / sumW[k];
+    for (int k = 0; k < NC; k++) out[k] = (sumW[k] < kEpsilon) ? kBigResidual : sum[k] / sumW[k];
 }
 
 // propagate_kernel with the four jump candidates evaluated together
+// self_res: the pixel's cached residual (the energy of its current offset
+// under the current canvas, which a residual update after the previous pass
+// would have stored) is evaluated here, in the same tap loop, instead of
+// being read from the residual buffer.
 template <int R, int TM>
-__global__ void __launch_bounds__(kTileThreads, 2) kt_propagate4(const Params P, PatchPlanes work, int jump) {
+__global__ void __launch_bounds__(kTileThreads, 2) kt_propagate4(const Params P, PatchPlanes work, int jump,
+                                                                int self_res) {
     __shared__ TileSmem<R, TM> T;
     PixT px;
     if (!stage_tile<R, TM>(P, T, &px)) return;
@@ -387,17 +397,21 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate4(const Params P,
         store_patch(work, k, make_patch(0, 0, 0, 0, 0, 1.f, 1.f));
         return;
     }
-    float best = __ldg(P.res + k);
     float ia = T.base[px.sidx].w;
     Patch ow = load_patch(P.off, k);
-    // the four candidates in the reference's order; a candidate that repeats
-    // an earlier one, or that test_offset rejects before the energy, keeps
-    // its fixed outcome
+    // slot 0: the current offset when self_res; then the four candidates in
+    // the reference's order; a candidate that repeats an earlier one, or
+    // that test_offset rejects before the energy, keeps its fixed outcome
     Patch cand[4];
     float res[4];
     int slot[4];
-    Cand ev[4];
+    Cand ev[5];
     int n = 0;
+    if (self_res) {
+        ev[0] = Cand{ow.x, ow.y, ow.theta, ow.su, ow.sv, ow.layer};
+        if (P.counters) count_eval(P, x, y);
+        n = 1;
+    }
 #pragma unroll
     for (int cdx = 0; cdx < 4; cdx++) {
         int tx = x, ty = y;
@@ -428,13 +442,14 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate4(const Params P,
         slot[cdx] = n;
         n++;
     }
-    float e[4];
-    energy4<R, TM>(P, T, px, ev, n, e);
+    float e[5];
+    energyN<R, TM, 5>(P, T, px, ev, n, e);
+    float best = self_res ? e[0] : __ldg(P.res + k);
 #pragma unroll
     for (int cdx = 0; cdx < 4; cdx++) {
         if (slot[cdx] == -2) continue;  // repeat: same energy, rejected by "<"
 #pragma unroll
-        for (int q = 0; q < 4; q++)
+        for (int q = 0; q < 5; q++)
             if (slot[cdx] == q) res[cdx] = e[q];
         if (res[cdx] < best) { ow = cand[cdx]; best = res[cdx]; }
     }
@@ -568,7 +583,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter(const Params P, Pa
 // result, are those of the one-by-one chain.
 template <int R, int TM>
 __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter4(const Params P, PatchPlanes work, int write_all,
-                                                              uint32_t pass_id) {
+                                                              uint32_t pass_id, int self_res) {
     __shared__ TileSmem<R, TM> T;
     PixT px;
     if (!stage_tile<R, TM>(P, T, &px)) return;
@@ -579,7 +594,10 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter4(const Params P, P
         if (write_all) store_patch(work, k, off);
         return;
     }
-    float cached = __ldg(P.res + k);
+    // with self_res the cached residual (energy of the current offset) is
+    // evaluated in the first batch, ahead of the chain candidates
+    bool need_self = self_res != 0;
+    float cached = need_self ? 0.0f : __ldg(P.res + k);
     float best = (float)((double)cached + 10e-7);
     Patch ow = off;
     float ia = T.base[px.sidx].w;
@@ -594,12 +612,13 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter4(const Params P, P
         float dnext[4];
         int inext[4];
         bool pre[4];   // rejected by test_offset before the energy
+        const int cap = need_self ? 3 : 4;
         int n = 0;
         int j = i;
         float d = dist;
         uint32_t lx = lastx, ly = lasty;
 #pragma unroll 1
-        while (n < 4 && j < P.scatterSamples && d * factor >= closest) {
+        while (n < cap && j < P.scatterSamples && d * factor >= closest) {
             float dmin = d * factor;
             float ex, ey;
             if (P.rngMode == PT_RNG_COUNTER) {
@@ -632,18 +651,30 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter4(const Params P, P
             }
             n++;
         }
-        if (n == 0) break;
-        // evaluate the candidates that reach the energy (compacted)
+        if (n == 0 && !need_self) break;
+        // evaluate the candidates that reach the energy (compacted), after
+        // the current offset when its energy is still needed
         Cand evc[4];
         int m = 0;
+        if (need_self) {
+            evc[0] = Cand{off.x, off.y, off.theta, off.su, off.sv, off.layer};
+            m = 1;
+        }
 #pragma unroll
         for (int q = 0; q < 4; q++)
             if (q < n && !pre[q]) { evc[m] = c[q]; m++; }
         if (P.counters)
             for (int q = 0; q < m; q++) count_eval(P, x, y);
         float e[4];
-        energy4<R, TM>(P, T, px, evc, m, e);
+        energyN<R, TM, 4>(P, T, px, evc, m, e);
         int accepted = -1, mi = 0;
+        if (need_self) {
+            cached = e[0];
+            best = (float)((double)cached + 10e-7);
+            mi = 1;
+            need_self = false;
+            if (n == 0) break;
+        }
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             if (q < n && accepted < 0) {
@@ -710,12 +741,12 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_residual(const Params P, f
 
 template <int R>
 cudaError_t launch_tiled_r(int kind, int tm, const Params& P, PatchPlanes work, int arg, uint32_t pass_id, float* out,
-                           cudaStream_t s) {
+                           int self_res, cudaStream_t s) {
     dim3 b(kTileW, kTileH), g((P.lw + kTileW - 1) / kTileW, (P.lh + kTileH - 1) / kTileH);
 #define PT_TILED_DISPATCH(TMV)                                                                   \
-    if (kind == 0) kt_propagate4<R, TMV><<<g, b, 0, s>>>(P, work, arg);                         \
+    if (kind == 0) kt_propagate4<R, TMV><<<g, b, 0, s>>>(P, work, arg, self_res);               \
     else if (kind == 3) kt_propagate<R, TMV><<<g, b, 0, s>>>(P, work, arg);                     \
-    else if (kind == 1) kt_scatter4<R, TMV><<<g, b, 0, s>>>(P, work, arg, pass_id);             \
+    else if (kind == 1) kt_scatter4<R, TMV><<<g, b, 0, s>>>(P, work, arg, pass_id, self_res);   \
     else if (kind == 4) kt_scatter<R, TMV><<<g, b, 0, s>>>(P, work, arg, pass_id);              \
     else kt_residual<R, TMV><<<g, b, 0, s>>>(P, out);
     if (tm == TM_NONE) { PT_TILED_DISPATCH(TM_NONE) }
