@@ -400,15 +400,15 @@ static bool tiled_usable(pt_ctx* c) {
 // launches the tiled kernel of `kind` if one is instantiated for this
 // configuration; *done = false otherwise (the generic kernel is used)
 static cudaError_t launch_tiled(pt_ctx* c, int kind, const Params& P, PatchPlanes work, int arg, uint32_t pass_id,
-                                float* out, int self_res, bool* done) {
+                                float* out, bool* done) {
     *done = false;
     if (!tiled_usable(c)) return cudaSuccess;
     int tm = temporal_mode(c);
     *done = true;
     switch (P.r) {
-        case 2: return pt::launch_tiled_2(kind, tm, P, work, arg, pass_id, out, self_res, c->stream);
-        case 3: return pt::launch_tiled_3(kind, tm, P, work, arg, pass_id, out, self_res, c->stream);
-        case 4: return pt::launch_tiled_4(kind, tm, P, work, arg, pass_id, out, self_res, c->stream);
+        case 2: return pt::launch_tiled_2(kind, tm, P, work, arg, pass_id, out, c->stream);
+        case 3: return pt::launch_tiled_3(kind, tm, P, work, arg, pass_id, out, c->stream);
+        case 4: return pt::launch_tiled_4(kind, tm, P, work, arg, pass_id, out, c->stream);
         default: *done = false; return cudaSuccess;
     }
 }
@@ -418,7 +418,7 @@ static pt_status do_residual(pt_ctx* c, int level) {
     float* out = c->res[c->res_i];
     return profiled(c, PT_KERNEL_RESIDUAL, P, [&](const Params& Q) {
         bool done = false;
-        cudaError_t e = launch_tiled(c, 2, Q, PatchPlanes{}, 0, 0, out, 0, &done);
+        cudaError_t e = launch_tiled(c, 2, Q, PatchPlanes{}, 0, 0, out, &done);
         return done ? e : pt::launch_residual(Q, out, c->stream);
     });
 }
@@ -943,26 +943,25 @@ pt_status pt_randomize_offsets(pt_ctx* c, int level) {
     return do_sync(c, level, 0);
 }
 
-// one propagate pass into the working buffer; with self_res the kernel
-// evaluates each pixel's cached residual itself (tiled kernels only)
-static pt_status propagate_pass(pt_ctx* c, int level, int jump, int self_res) {
+// one propagate pass into the working buffer
+static pt_status propagate_pass(pt_ctx* c, int level, int jump) {
     PatchPlanes work = writable_work(c, nullptr);
     Params P = make_params(c, level);
     return profiled(c, PT_KERNEL_PROPAGATE, P, [&](const Params& Q) {
         bool done = false;
-        cudaError_t e = launch_tiled(c, 0, Q, work, jump, 0, nullptr, self_res, &done);
+        cudaError_t e = launch_tiled(c, 0, Q, work, jump, 0, nullptr, &done);
         return done ? e : pt::launch_propagate(Q, work, jump, c->stream);
     });
 }
 
-static pt_status scatter_pass(pt_ctx* c, int level, int self_res) {
+static pt_status scatter_pass(pt_ctx* c, int level) {
     bool aliased = false;
     PatchPlanes work = writable_work(c, &aliased);
     Params P = make_params(c, level);
     uint32_t pass_id = c->pass_counter++;
     return profiled(c, PT_KERNEL_SCATTER, P, [&](const Params& Q) {
         bool done = false;
-        cudaError_t e = launch_tiled(c, 1, Q, work, aliased ? 1 : 0, pass_id, nullptr, self_res, &done);
+        cudaError_t e = launch_tiled(c, 1, Q, work, aliased ? 1 : 0, pass_id, nullptr, &done);
         return done ? e : pt::launch_scatter(Q, work, aliased ? 1 : 0, pass_id, c->stream);
     });
 }
@@ -971,7 +970,7 @@ pt_status pt_propagate(pt_ctx* c, int level, int jump, int key_index) {
     if (!c) return PT_ERR_INVALID;
     TRY(check_ready(c, level));
     if (key_index >= 0) return fail(c, PT_ERR_UNSUPPORTED, "keyframe propagation is not implemented");
-    TRY(propagate_pass(c, level, jump, 0));
+    TRY(propagate_pass(c, level, jump));
     return do_sync(c, level, 0);
 }
 
@@ -979,7 +978,7 @@ pt_status pt_scatter(pt_ctx* c, int level, int key_index) {
     if (!c) return PT_ERR_INVALID;
     TRY(check_ready(c, level));
     if (key_index >= 0) return fail(c, PT_ERR_UNSUPPORTED, "keyframe scatter is not implemented");
-    TRY(scatter_pass(c, level, 0));
+    TRY(scatter_pass(c, level));
     return do_sync(c, level, 0);
 }
 
@@ -1402,30 +1401,14 @@ static pt_status store_load_residual(pt_ctx* c, int level, int frame, int pass) 
     return PT_OK;
 }
 
-// SynthesisFrame::propagateAndScatter, synthesisFrame.cpp:483-508.  Every
-// pass of the reference ends with syncBuffers, whose residual update is only
-// read by the next pass (as each pixel's cached residual): when the tiled
-// kernels run, that next pass evaluates it itself, so the per-pass residual
-// launch is left out and the buffer is filled once after the last pass.
+// SynthesisFrame::propagateAndScatter, synthesisFrame.cpp:483-508
 static pt_status propagate_and_scatter(pt_ctx* c, int level, int iterations) {
-    const bool fused = tiled_usable(c);
-    const int self_res = fused ? 1 : 0;
-    const int sync_flags = fused ? PT_DONT_UPDATE_RESIDUAL : 0;
     for (int itr = 0; itr < iterations; itr++) {
-        for (int j = 128; j > 1; j /= 2) {
-            TRY(propagate_pass(c, level, j, self_res));
-            TRY(do_sync(c, level, sync_flags));
-        }
-        for (int q = 0; q < 2; q++) {
-            TRY(propagate_pass(c, level, 1, self_res));
-            TRY(do_sync(c, level, sync_flags));
-        }
-        if (itr < iterations - 1) {
-            TRY(scatter_pass(c, level, self_res));
-            TRY(do_sync(c, level, sync_flags));
-        }
+        for (int j = 128; j > 1; j /= 2) TRY(pt_propagate(c, level, j, -1));
+        TRY(pt_propagate(c, level, 1, -1));
+        TRY(pt_propagate(c, level, 1, -1));
+        if (itr < iterations - 1) TRY(pt_scatter(c, level, -1));
     }
-    if (fused) TRY(do_residual(c, level));
     return PT_OK;
 }
 

@@ -381,13 +381,8 @@ __device__ __forceinline__ void energyN(const Params& P, const TileSmem<R, TM>& 
 }
 
 // propagate_kernel with the four jump candidates evaluated together
-// self_res: the pixel's cached residual (the energy of its current offset
-// under the current canvas, which a residual update after the previous pass
-// would have stored) is evaluated here, in the same tap loop, instead of
-// being read from the residual buffer.
 template <int R, int TM>
-__global__ void __launch_bounds__(kTileThreads, 2) kt_propagate4(const Params P, PatchPlanes work, int jump,
-                                                                int self_res) {
+__global__ void __launch_bounds__(kTileThreads, 2) kt_propagate4(const Params P, PatchPlanes work, int jump) {
     __shared__ TileSmem<R, TM> T;
     PixT px;
     if (!stage_tile<R, TM>(P, T, &px)) return;
@@ -397,21 +392,17 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate4(const Params P,
         store_patch(work, k, make_patch(0, 0, 0, 0, 0, 1.f, 1.f));
         return;
     }
+    float best = __ldg(P.res + k);
     float ia = T.base[px.sidx].w;
     Patch ow = load_patch(P.off, k);
-    // slot 0: the current offset when self_res; then the four candidates in
-    // the reference's order; a candidate that repeats an earlier one, or
-    // that test_offset rejects before the energy, keeps its fixed outcome
+    // the four candidates in the reference's order; a candidate that repeats
+    // an earlier one, or that test_offset rejects before the energy, keeps
+    // its fixed outcome
     Patch cand[4];
     float res[4];
     int slot[4];
-    Cand ev[5];
+    Cand ev[4];
     int n = 0;
-    if (self_res) {
-        ev[0] = Cand{ow.x, ow.y, ow.theta, ow.su, ow.sv, ow.layer};
-        if (P.counters) count_eval(P, x, y);
-        n = 1;
-    }
 #pragma unroll
     for (int cdx = 0; cdx < 4; cdx++) {
         int tx = x, ty = y;
@@ -442,60 +433,15 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate4(const Params P,
         slot[cdx] = n;
         n++;
     }
-    float e[5];
-    energyN<R, TM, 5>(P, T, px, ev, n, e);
-    float best = self_res ? e[0] : __ldg(P.res + k);
+    float e[4];
+    energyN<R, TM, 4>(P, T, px, ev, n, e);
 #pragma unroll
     for (int cdx = 0; cdx < 4; cdx++) {
         if (slot[cdx] == -2) continue;  // repeat: same energy, rejected by "<"
 #pragma unroll
-        for (int q = 0; q < 5; q++)
+        for (int q = 0; q < 4; q++)
             if (slot[cdx] == q) res[cdx] = e[q];
         if (res[cdx] < best) { ow = cand[cdx]; best = res[cdx]; }
-    }
-    store_patch(work, k, ow);
-}
-
-// propagate_kernel, texSynth_kernel.cu:1112-1219
-template <int R, int TM>
-__global__ void __launch_bounds__(kTileThreads, 2) kt_propagate(const Params P, PatchPlanes work, int jump) {
-    __shared__ TileSmem<R, TM> T;
-    PixT px;
-    if (!stage_tile<R, TM>(P, T, &px)) return;
-    const int x = px.x, y = px.y;
-    const size_t k = (size_t)y * P.W + x;
-    if (image_culled(P, x, y)) {
-        store_patch(work, k, make_patch(0, 0, 0, 0, 0, 1.f, 1.f));
-        return;
-    }
-    float best = __ldg(P.res + k);
-    float ia = T.base[px.sidx].w;
-    Patch ow = load_patch(P.off, k);
-    // A candidate bit-identical to one already evaluated for this pixel has
-    // the same energy, which the strict "<" test then rejects: skipping it
-    // leaves the result unchanged.
-    // keys of the candidates evaluated so far (x, y, theta bits and layer)
-    uint32_t s0x = 0, s0y = 0, s0t = 0, s1x = 0, s1y = 0, s1t = 0, s2x = 0, s2y = 0, s2t = 0;
-    int s0l = -1, s1l = -1, s2l = -1;
-#pragma unroll 1
-    for (int cdx = 0; cdx < 4; cdx++) {
-        int tx = x, ty = y;
-        if (cdx == 0) tx = x + jump;
-        else if (cdx == 1) tx = x - jump;
-        else if (cdx == 2) ty = y + jump;
-        else ty = y - jump;
-        Patch t = propagate_offset(P, tx, ty, x, y);
-        uint32_t kx = __float_as_uint(t.x), ky = __float_as_uint(t.y), kt = __float_as_uint(t.theta);
-        bool dup = (cdx > 0 && kx == s0x && ky == s0y && kt == s0t && t.layer == s0l) ||
-                   (cdx > 1 && kx == s1x && ky == s1y && kt == s1t && t.layer == s1l) ||
-                   (cdx > 2 && kx == s2x && ky == s2y && kt == s2t && t.layer == s2l);
-        if (cdx == 0) { s0x = kx; s0y = ky; s0t = kt; s0l = t.layer; }
-        else if (cdx == 1) { s1x = kx; s1y = ky; s1t = kt; s1l = t.layer; }
-        else if (cdx == 2) { s2x = kx; s2y = ky; s2t = kt; s2l = t.layer; }
-        if (dup) continue;
-        Cand c{t.x, t.y, t.theta, t.su, t.sv, t.layer};
-        float r = test_offset_tiled<R, TM>(P, T, px, c, ia);
-        if (r < best) { ow = t; best = r; }
     }
     store_patch(work, k, ow);
 }
@@ -575,156 +521,6 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter(const Params P, Pa
     else if (write_all) store_patch(work, k, off);
 }
 
-// scatter_kernel with the chain evaluated in speculative batches: the next
-// (up to) four distinct chain candidates for the current best offset are
-// evaluated together; they are then accepted in chain order, and after an
-// acceptance the rest of the batch (built from the old best) is discarded
-// and the chain continues from the next index.  The decisions, and so the
-// result, are those of the one-by-one chain.
-template <int R, int TM>
-__global__ void __launch_bounds__(kTileThreads, 2) kt_scatter4(const Params P, PatchPlanes work, int write_all,
-                                                              uint32_t pass_id, int self_res) {
-    __shared__ TileSmem<R, TM> T;
-    PixT px;
-    if (!stage_tile<R, TM>(P, T, &px)) return;
-    const int x = px.x, y = px.y;
-    const size_t k = (size_t)y * P.W + x;
-    Patch off = load_patch(P.off, k);
-    if (image_culled(P, x, y)) {
-        if (write_all) store_patch(work, k, off);
-        return;
-    }
-    // with self_res the cached residual (energy of the current offset) is
-    // evaluated in the first batch, ahead of the chain candidates
-    bool need_self = self_res != 0;
-    float cached = need_self ? 0.0f : __ldg(P.res + k);
-    float best = (float)((double)cached + 10e-7);
-    Patch ow = off;
-    float ia = T.base[px.sidx].w;
-    const float closest = 10.f, factor = 0.9f;
-    float2 sc = lvl_texel(P.img.scale, x, y);
-    float dist = (float)(P.ex.w > P.ex.h ? P.ex.w : P.ex.h);
-    int i = 0;
-    uint32_t lastx = 0xffffffffu, lasty = 0xffffffffu;
-#pragma unroll 1
-    while (true) {
-        Cand c[4];
-        float dnext[4];
-        int inext[4];
-        bool pre[4];   // rejected by test_offset before the energy
-        const int cap = need_self ? 3 : 4;
-        int n = 0;
-        int j = i;
-        float d = dist;
-        uint32_t lx = lastx, ly = lasty;
-#pragma unroll 1
-        while (n < cap && j < P.scatterSamples && d * factor >= closest) {
-            float dmin = d * factor;
-            float ex, ey;
-            if (P.rngMode == PT_RNG_COUNTER) {
-                float rr = counter_u01(P.rngSeed, pass_id, x, y, 2 * j);
-                float th = counter_u01(P.rngSeed, pass_id, x, y, 2 * j + 1) * 6.28318530717958647692f;
-                float s, cc;
-                sincos_poly(th, &s, &cc);
-                float len = fmaf(rr, d - dmin, dmin);
-                ex = fmaf(cc, len, ow.x);
-                ey = fmaf(s, len, ow.y);
-            } else {
-                ex = ow.x + dmin;
-                ey = ow.y + 0.0f;
-            }
-            clamp_to_exemplar(&ex, &ey, P.ex.w, P.ex.h);
-            j++;
-            d *= factor;
-            if (__float_as_uint(ex) == lx && __float_as_uint(ey) == ly) continue;  // repeat: rejected by "<"
-            lx = __float_as_uint(ex);
-            ly = __float_as_uint(ey);
-            float ang = screen_to_exemplar_angle(P, x, y, ex, ey, 0);
-            c[n] = Cand{ex, ey, ang, sc.x, sc.y, 0};
-            dnext[n] = d;
-            inext[n] = j;
-            float dte = ex_texel_dt(P.ex, (int)ex, (int)ey, 0);
-            pre[n] = (double)dte > (double)P.distTransCull * 1.25;
-            if (!pre[n] && !P.transparencyOk) {
-                float ea = ex_sample_out_alpha(P.ex, ex, ey, 0);
-                pre[n] = ea < kAlphaThreshold && ia > kAlphaThreshold;
-            }
-            n++;
-        }
-        if (n == 0 && !need_self) break;
-        // evaluate the candidates that reach the energy (compacted), after
-        // the current offset when its energy is still needed
-        Cand evc[4];
-        int m = 0;
-        if (need_self) {
-            evc[0] = Cand{off.x, off.y, off.theta, off.su, off.sv, off.layer};
-            m = 1;
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-            if (q < n && !pre[q]) { evc[m] = c[q]; m++; }
-        if (P.counters)
-            for (int q = 0; q < m; q++) count_eval(P, x, y);
-        float e[4];
-        energyN<R, TM, 4>(P, T, px, evc, m, e);
-        int accepted = -1, mi = 0;
-        if (need_self) {
-            cached = e[0];
-            best = (float)((double)cached + 10e-7);
-            mi = 1;
-            need_self = false;
-            if (n == 0) break;
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            if (q < n && accepted < 0) {
-                float r = kBigResidual;
-                if (!pre[q]) {
-#pragma unroll
-                    for (int t = 0; t < 4; t++)
-                        if (t == mi) r = e[t];
-                    mi++;
-                }
-                if (r < best) {
-                    ow = make_patch(c[q].x, c[q].y, c[q].theta, 0.0f, 0, sc.x, sc.y);
-                    best = r;
-                    accepted = q;
-                }
-            }
-        }
-        if (accepted >= 0) {
-            i = inext[accepted];
-            dist = dnext[accepted];
-            lastx = __float_as_uint(c[accepted].x);
-            lasty = __float_as_uint(c[accepted].y);
-        } else {
-            i = j;
-            dist = d;
-            lastx = lx;
-            lasty = ly;
-        }
-    }
-    Patch avg = make_patch(0, 0, 0, 1.f, 0, 1.f, 1.f);
-    int nn = 0;
-    for (int a = -1; a <= 1; a++)
-        for (int b = -1; b <= 1; b++) {
-            if (!in_rect(P, x + a, y + b) || (a == 0 && b == 0)) continue;
-            float4 nb = __ldg(P.off.A + (size_t)(y + b) * P.W + (x + a));
-            if (__float_as_int(nb.w) != 0) continue;
-            avg.x = avg.x + nb.x;
-            avg.y = avg.y + nb.y;
-            nn++;
-        }
-    avg.x = avg.x / (float)nn;
-    avg.y = avg.y / (float)nn;
-    avg.theta = screen_to_exemplar_angle(P, x, y, avg.x, avg.y, 0);
-    Cand ca{avg.x, avg.y, avg.theta, avg.su, avg.sv, 0};
-    float r = test_offset_tiled<R, TM>(P, T, px, ca, ia);
-    if (r < best) { ow = avg; best = r; }
-    if (best < cached) store_patch(work, k, ow);
-    else if (write_all) store_patch(work, k, off);
-}
-
 // updateResidualCache_kernel, texSynth_kernel.cu:661-693
 template <int R, int TM>
 __global__ void __launch_bounds__(kTileThreads, 2) kt_residual(const Params P, float* out) {
@@ -741,13 +537,11 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_residual(const Params P, f
 
 template <int R>
 cudaError_t launch_tiled_r(int kind, int tm, const Params& P, PatchPlanes work, int arg, uint32_t pass_id, float* out,
-                           int self_res, cudaStream_t s) {
+                           cudaStream_t s) {
     dim3 b(kTileW, kTileH), g((P.lw + kTileW - 1) / kTileW, (P.lh + kTileH - 1) / kTileH);
 #define PT_TILED_DISPATCH(TMV)                                                                   \
-    if (kind == 0) kt_propagate4<R, TMV><<<g, b, 0, s>>>(P, work, arg, self_res);               \
-    else if (kind == 3) kt_propagate<R, TMV><<<g, b, 0, s>>>(P, work, arg);                     \
-    else if (kind == 1) kt_scatter4<R, TMV><<<g, b, 0, s>>>(P, work, arg, pass_id, self_res);   \
-    else if (kind == 4) kt_scatter<R, TMV><<<g, b, 0, s>>>(P, work, arg, pass_id);              \
+    if (kind == 0) kt_propagate4<R, TMV><<<g, b, 0, s>>>(P, work, arg);                         \
+    else if (kind == 1) kt_scatter<R, TMV><<<g, b, 0, s>>>(P, work, arg, pass_id);              \
     else kt_residual<R, TMV><<<g, b, 0, s>>>(P, out);
     if (tm == TM_NONE) { PT_TILED_DISPATCH(TM_NONE) }
     else if (tm == TM_FWD) { PT_TILED_DISPATCH(TM_FWD) }

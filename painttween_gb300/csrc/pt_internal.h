@@ -42,12 +42,11 @@ cudaError_t launch_any_transparent(const float4* out, size_t n, int* flag, cudaS
 
 // tiled patch-distance kernels for patch radius 2, 3, 4 (pt_tiled_r*.cu):
 // kind 0 = propagate (arg = jump), 1 = scatter (arg = write_all),
-// 2 = residual (into out); tm 0 = no temporal terms, 1 = forward, 2 = backward;
-// self_res: propagate/scatter evaluate the cached residual themselves
+// 2 = residual (into out); tm 0 = no temporal terms, 1 = forward, 2 = backward
 cudaError_t launch_tiled_2(int kind, int tm, const Params& P, PatchPlanes work, int arg, uint32_t pass_id, float* out,
-                           int self_res, cudaStream_t s);
+                           cudaStream_t s);
 cudaError_t launch_tiled_3(int kind, int tm, const Params& P, PatchPlanes work, int arg, uint32_t pass_id, float* out,
-                           int self_res, cudaStream_t s);
+                           cudaStream_t s);
 cudaError_t launch_tiled_4(int kind, int tm, const Params& P, PatchPlanes work, int arg, uint32_t pass_id, float* out,
-                           int self_res, cudaStream_t s);
+                           cudaStream_t s);
 }  // namespace pt

@@ -36,6 +36,10 @@ __global__ void __launch_bounds__(128) k_propagate(const Params P, PatchPlanes w
     Patch ow = load_patch(P.off, k);
     PixCtx pc;
     make_pixctx(P, x, y, &pc);
+    // an exact repeat of an earlier candidate has the same energy and is
+    // rejected by the strict "<" test: it is not evaluated again
+    uint32_t s0x = 0, s0y = 0, s0t = 0, s1x = 0, s1y = 0, s1t = 0, s2x = 0, s2y = 0, s2t = 0;
+    int s0l = -1, s1l = -1, s2l = -1;
 #pragma unroll 1
     for (int c = 0; c < 4; c++) {
         int tx = x, ty = y;
@@ -44,6 +48,14 @@ __global__ void __launch_bounds__(128) k_propagate(const Params P, PatchPlanes w
         else if (c == 2) ty = y + jump;
         else ty = y - jump;
         Patch t = propagate_offset(P, tx, ty, x, y);
+        uint32_t kx = __float_as_uint(t.x), ky = __float_as_uint(t.y), kt = __float_as_uint(t.theta);
+        bool dup = (c > 0 && kx == s0x && ky == s0y && kt == s0t && t.layer == s0l) ||
+                   (c > 1 && kx == s1x && ky == s1y && kt == s1t && t.layer == s1l) ||
+                   (c > 2 && kx == s2x && ky == s2y && kt == s2t && t.layer == s2l);
+        if (c == 0) { s0x = kx; s0y = ky; s0t = kt; s0l = t.layer; }
+        else if (c == 1) { s1x = kx; s1y = ky; s1t = kt; s1l = t.layer; }
+        else if (c == 2) { s2x = kx; s2y = ky; s2t = kt; s2l = t.layer; }
+        if (dup) continue;
         float r = test_offset(P, x, y, t, ia, pc);
         if (r < best) { ow = t; best = r; }
     }
@@ -71,6 +83,7 @@ __global__ void __launch_bounds__(128) k_scatter(const Params P, PatchPlanes wor
     float2 sc = lvl_texel(P.img.scale, x, y);
     PixCtx pc;
     make_pixctx(P, x, y, &pc);
+    uint32_t lastx = 0xffffffffu, lasty = 0xffffffffu;  // exact repeats are not re-evaluated
 #pragma unroll 1
     for (int i = 0; i < P.scatterSamples && dist * factor >= closest; i++) {
         float dmin = dist * factor;
@@ -88,6 +101,12 @@ __global__ void __launch_bounds__(128) k_scatter(const Params P, PatchPlanes wor
             ey = ow.y + 0.0f;
         }
         clamp_to_exemplar(&ex, &ey, P.ex.w, P.ex.h);
+        if (__float_as_uint(ex) == lastx && __float_as_uint(ey) == lasty) {
+            dist *= factor;
+            continue;
+        }
+        lastx = __float_as_uint(ex);
+        lasty = __float_as_uint(ey);
         float ang = screen_to_exemplar_angle(P, x, y, ex, ey, 0);
         Patch t = make_patch(ex, ey, ang, 0.0f, 0, sc.x, sc.y);
         float r = test_offset(P, x, y, t, ia, pc);

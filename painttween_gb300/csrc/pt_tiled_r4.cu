@@ -3,7 +3,7 @@
 
 namespace pt {
 cudaError_t launch_tiled_4(int kind, int tm, const Params& P, PatchPlanes work, int arg, uint32_t pass_id, float* out,
-                           int self_res, cudaStream_t s) {
-    return ptk::launch_tiled_r<4>(kind, tm, P, work, arg, pass_id, out, self_res, s);
+                           cudaStream_t s) {
+    return ptk::launch_tiled_r<4>(kind, tm, P, work, arg, pass_id, out, s);
 }
 }  // namespace pt
