@@ -332,15 +332,21 @@ def run_ours(args, dist):
     st = stats[_abi.KERNEL_PROPAGATE]
     r = p.residualWindowSize
     K = (2 * r + 1) ** 2
-    bytes_per_eval = 32 * K + 16
-    flops_per_eval = 84 * K + 40
-    avg_launch_s = st["total_ms"] / max(st["launches"], 1) / 1000.0
-    evals_per_launch = st["energy_evals"] / max(st["launches"], 1)
-    achieved = evals_per_launch * bytes_per_eval / avg_launch_s / 1e9
+    # algorithmic work per evaluation: 2 exemplar float4 samples per tap
+    # (32 B, ~84 flops) + 16 B at the centre; temporal taps add 2 samples and
+    # 3 SSDs (+32 B, +84 flops)
+    n_launch = max(st["launches"], 1)
+    evals_per_launch = st["energy_evals"] / n_launch
+    bytes_per_launch = (32 * st["taps"] + 16 * st["energy_evals"] + 32 * st["temporal_taps"]) / n_launch
+    flops_per_launch = (84 * st["taps"] + 40 * st["energy_evals"] + 84 * st["temporal_taps"]) / n_launch
+    bytes_per_eval = bytes_per_launch / max(evals_per_launch, 1)
+    flops_per_eval = flops_per_launch / max(evals_per_launch, 1)
+    avg_launch_s = st["total_ms"] / n_launch / 1000.0
+    achieved = bytes_per_launch / avg_launch_s / 1e9
     hbm, peak_kind = peaks()
     sm_mhz = (ck or {}).get("sm_mhz") or 1900.0
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-    fp32_achieved = evals_per_launch * flops_per_eval / avg_launch_s / 1e12
+    fp32_achieved = flops_per_launch / avg_launch_s / 1e12
     traffic = (None if PROPAGATE_DRAM_BYTES_PER_EVAL is None
                else PROPAGATE_DRAM_BYTES_PER_EVAL * evals_per_launch)
     kernel_share = st["total_ms"] / max(sum(v["total_ms"] for v in stats.values()), 1e-9)
@@ -361,7 +367,8 @@ def run_ours(args, dist):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "k_propagate", "bytes_per_eval": bytes_per_eval,
+                     "kernel": "propagate", "bytes_per_eval": bytes_per_eval,
+                     "temporal_tap_fraction": st["temporal_taps"] / max(st["taps"], 1),
                      "evals_per_launch": evals_per_launch, "avg_launch_ms": avg_launch_s * 1000.0,
                      "time_share": kernel_share,
                      "fp32": {"achieved_tflops": fp32_achieved, "peak_tflops": fp32_peak,

@@ -244,6 +244,15 @@ pt_status pt_get_residual(pt_ctx* ctx, int level, float* out);
 /* Stylised output (canvasOutputCache), RGBA float32. */
 pt_status pt_get_output(pt_ctx* ctx, int level, float* out_rgba);
 
+/* Separable normalised Gaussian blur (sigma = radius / 3, zero outside the
+ * image) of one float image: convolutionRowsGPU followed by
+ * convolutionColumnsGPU (convolution.h:36-44, convolution.cu:63-210), the
+ * smoothing the reference applies to its offsets histogram.  src and dst are
+ * device pointers with a row pitch of `pitch` floats; the row-pass result is
+ * kept in the context's scratch buffer.  Runs on the context's stream. */
+pt_status pt_convolve_separable(pt_ctx* ctx, const float* src_dev, float* dst_dev, int w, int h, int pitch,
+                                int radius);
+
 /* ---- working-set level API (pyramids built and kept on the device) ----- */
 
 /* Uploads one style exemplar at level-0 size and builds its pyramid on the
@@ -303,6 +312,7 @@ typedef struct {
     double total_ms;          /* sum of per-launch CUDA-event durations */
     uint64_t energy_evals;    /* patch-distance evaluations performed */
     uint64_t taps;            /* taps summed over those evaluations */
+    uint64_t temporal_taps;   /* taps of evaluations with temporal terms */
 } pt_kernel_stats;
 /* Switches per-launch event timing and patch-distance counting on or off
  * (and clears the statistics). */

@@ -73,6 +73,7 @@ def lib():
             "pto_downsample_avg": (None, [vp, i, i, i, f, vp]),
             "pto_downsample_vote": (None, [vp, i, i, vp]),
             "pto_tensor_to_angle": (None, [vp, i, vp]),
+            "pto_convolve_separable": (None, [vp, vp, i, i, i]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -122,6 +123,14 @@ def pyramid_vote(ids):
         dst = np.empty((cur.shape[0] >> 1, cur.shape[1] >> 1), np.int32)
         lib().pto_downsample_vote(_p(cur), cur.shape[1], cur.shape[0], _p(dst))
         out.append(dst)
+    return out
+
+
+def convolve_separable(img, radius):
+    """convolutionRowsGPU + convolutionColumnsGPU (normalised Gaussian)."""
+    img = _c(img, np.float32)
+    out = np.empty_like(img)
+    lib().pto_convolve_separable(_p(img), _p(out), img.shape[1], img.shape[0], radius)
     return out
 
 

@@ -787,6 +787,33 @@ static void conv_pass(pto* o, const float* src, float* dst, int w, int h, int ro
         }
 }
 
+/* convolutionRowsGPU + convolutionColumnsGPU on one w x h image (pitch w) */
+void pto_convolve_separable(const float* src, float* dst, int w, int h, int r) {
+    float kern[64];
+    float sigma = (float)r / 3.0f, s2 = sigma * sigma;
+    for (int i = 0; i <= r; i++) {
+        float wgt = expf(-(float)(i * i) / (2.f * s2));
+        wgt = wgt / (sqrtf(2.f * (float)M_PI) * sigma);
+        kern[r + i] = wgt; kern[r - i] = wgt;
+    }
+    float* tmp = (float*)malloc(sizeof(float) * (size_t)w * h);
+    for (int pass = 0; pass < 2; pass++) {
+        const float* s = pass ? tmp : src;
+        float* d = pass ? dst : tmp;
+        for (int y = 0; y < h; y++)
+            for (int x = 0; x < w; x++) {
+                float acc = 0.0f;
+                for (int j = -r; j <= r; j++) {
+                    int xx = pass ? x : x + j, yy = pass ? y + j : y;
+                    float v = (xx >= 0 && xx < w && yy >= 0 && yy < h) ? s[(size_t)yy * w + xx] : 0.0f;
+                    acc = fmaf(kern[r - j], v, acc);
+                }
+                d[(size_t)y * w + x] = acc;
+            }
+    }
+    free(tmp);
+}
+
 /* syncBuffers, texSynth_kernel.cu:1240-1303 (distance-transform, velocity
  * and ribbon caches are display-only and not kept) */
 void pto_sync(pto* o, int level, int flags) {

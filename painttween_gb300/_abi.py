@@ -162,7 +162,8 @@ KERNEL_PROPAGATE, KERNEL_SCATTER, KERNEL_RESIDUAL, KERNEL_CANVAS = 0, 1, 2, 3
 class KernelStats(ctypes.Structure):
     """pt_kernel_stats (include/painttween.h)."""
     _fields_ = [("launches", ctypes.c_uint64), ("total_ms", ctypes.c_double),
-                ("energy_evals", ctypes.c_uint64), ("taps", ctypes.c_uint64)]
+                ("energy_evals", ctypes.c_uint64), ("taps", ctypes.c_uint64),
+                ("temporal_taps", ctypes.c_uint64)]
 
 
 def status_name(s):

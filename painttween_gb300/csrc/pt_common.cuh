@@ -223,15 +223,17 @@ static __device__ __forceinline__ unsigned lane_id() {
     asm volatile("mov.u32 %0, %%laneid;" : "=r"(l));
     return l;
 }
-static __device__ __forceinline__ void count_eval(const Params& P, int x, int y) {
+static __device__ __forceinline__ void count_eval(const Params& P, int x, int y, bool temporal) {
     int x0 = max(x - P.r, 0), x1 = min(x + P.r, P.lw - 1);
     int y0 = max(y - P.r, 0), y1 = min(y + P.r, P.lh - 1);
     unsigned taps = (unsigned)((x1 - x0 + 1) * (y1 - y0 + 1));
     unsigned mask = __activemask();
     unsigned tsum = __reduce_add_sync(mask, taps);
+    unsigned ttsum = __reduce_add_sync(mask, temporal ? taps : 0u);
     if (lane_id() == (unsigned)(__ffs(mask) - 1)) {
         atomicAdd(&P.counters[0], (unsigned long long)__popc(mask));
         atomicAdd(&P.counters[1], (unsigned long long)tsum);
+        atomicAdd(&P.counters[2], (unsigned long long)ttsum);
     }
 }
 
@@ -243,7 +245,7 @@ static __device__ float test_offset(const Params& P, int x, int y, const Patch& 
             float ea = ex_sample_out_alpha(P.ex, t.x, t.y, t.layer);
             if (ea < kAlphaThreshold && image_alpha > kAlphaThreshold) return kBigResidual;
         }
-        if (P.counters) count_eval(P, x, y);
+        if (P.counters) count_eval(P, x, y, pc.temporalF || pc.temporalB);
         return energy(P, x, y, t, pc);
     }
     return kBigResidual;

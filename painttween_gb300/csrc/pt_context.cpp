@@ -111,6 +111,8 @@ struct pt_ctx {
     // staging
     void* stage = nullptr;
     size_t stage_bytes = 0;
+    float* conv_scratch = nullptr;
+    size_t conv_scratch_elems = 0;
     uint32_t* states = nullptr;
     size_t states_cap = 0;
     int* flag = nullptr;
@@ -129,7 +131,7 @@ struct pt_ctx {
     // measurement
     cudaEvent_t timers[PT_TIMER_SLOTS] = {};
     bool profiling = false;
-    unsigned long long* counters = nullptr;  // [kernel][evals, taps]
+    unsigned long long* counters = nullptr;  // [kernel][evals, taps, temporal taps]
     std::vector<cudaEvent_t> ev_pool;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pairs[PT_KERNEL_COUNT];
     std::map<int, std::vector<uint32_t>> jump_cache;  // M^(4w)
@@ -367,7 +369,7 @@ static pt_status profiled(pt_ctx* c, int kernel, Params& P, F&& launch) {
         LN(launch(P));
         return PT_OK;
     }
-    P.counters = c->counters + 2 * kernel;
+    P.counters = c->counters + 3 * kernel;
     cudaEvent_t a = pool_event(c), b = pool_event(c);
     if (!a || !b) return fail(c, PT_ERR_CUDA, "cudaEventCreate failed");
     CU(cudaEventRecord(a, c->stream));
@@ -1106,6 +1108,38 @@ pt_status pt_get_output(pt_ctx* c, int level, float* out) {
     return get_plane(c, level, (const float*)c->canvas, 4, out);
 }
 
+// normalised Gaussian of radius r (allocateGaussianKernel(..., normalize=true),
+// convolution.cu:37-60)
+static void normalized_gaussian(int r, ConvKernel* k) {
+    float sigma = (float)r / 3.0f, s2 = sigma * sigma;
+    k->r = r;
+    for (int i = 0; i <= r; i++) {
+        float w = expf(-(float)(i * i) / (2.f * s2));
+        w = w / (sqrtf(2.f * (float)M_PI) * sigma);
+        k->w[r + i] = w;
+        k->w[r - i] = w;
+    }
+}
+
+pt_status pt_convolve_separable(pt_ctx* c, const float* src, float* dst, int w, int h, int pitch, int radius) {
+    if (!c || !src || !dst) return PT_ERR_INVALID;
+    if (w < 1 || h < 1 || pitch < w || radius < 1 || radius > ptk::kMaxRadius)
+        return fail(c, PT_ERR_INVALID, "bad convolution size %dx%d pitch %d radius %d", w, h, pitch, radius);
+    CU(cudaSetDevice(c->device));
+    size_t n = (size_t)pitch * h;
+    if (n > c->conv_scratch_elems) {
+        dfree_t(c, c->conv_scratch);
+        c->conv_scratch_elems = 0;
+        TRY(dalloc_t(c, &c->conv_scratch, n));
+        c->conv_scratch_elems = n;
+    }
+    ConvKernel k;
+    normalized_gaussian(radius, &k);
+    LN(pt::launch_conv(src, c->conv_scratch, w, h, pitch, 1, k, c->stream));
+    LN(pt::launch_conv(c->conv_scratch, dst, w, h, pitch, 0, k, c->stream));
+    return PT_OK;
+}
+
 // --- resident pyramids ----------------------------------------------------------
 
 // builds the float pyramid of `ch` channels from a device level-0 array;
@@ -1304,8 +1338,8 @@ pt_status pt_set_profiling(pt_ctx* c, int on) {
     if (!c) return PT_ERR_INVALID;
     CU(cudaStreamSynchronize(c->stream));
     clear_profile(c);
-    if (!c->counters) TRY(dalloc_t(c, &c->counters, 2 * PT_KERNEL_COUNT));
-    CU(cudaMemsetAsync(c->counters, 0, 2 * PT_KERNEL_COUNT * sizeof(unsigned long long), c->stream));
+    if (!c->counters) TRY(dalloc_t(c, &c->counters, 3 * PT_KERNEL_COUNT));
+    CU(cudaMemsetAsync(c->counters, 0, 3 * PT_KERNEL_COUNT * sizeof(unsigned long long), c->stream));
     c->profiling = on != 0;
     return PT_OK;
 }
@@ -1327,10 +1361,11 @@ pt_status pt_get_kernel_stats(pt_ctx* c, int kernel, pt_kernel_stats* out) {
         out->launches++;
     }
     if (c->counters) {
-        unsigned long long h[2] = {0, 0};
-        CU(cudaMemcpy(h, c->counters + 2 * kernel, sizeof(h), cudaMemcpyDeviceToHost));
+        unsigned long long h[3] = {0, 0, 0};
+        CU(cudaMemcpy(h, c->counters + 3 * kernel, sizeof(h), cudaMemcpyDeviceToHost));
         out->energy_evals = h[0];
         out->taps = h[1];
+        out->temporal_taps = h[2];
     }
     return PT_OK;
 }

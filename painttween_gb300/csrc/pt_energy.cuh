@@ -201,7 +201,7 @@ __device__ __forceinline__ float test_offset_tiled(const Params& P, const TileSm
             float ea = ex_sample_out_alpha(P.ex, c.x, c.y, c.layer);
             if (ea < kAlphaThreshold && image_alpha > kAlphaThreshold) return kBigResidual;
         }
-        if (P.counters) count_eval(P, px.x, px.y);
+        if (P.counters) count_eval(P, px.x, px.y, px.temporal);
         return energy_tiled<R, TM>(P, T, px, c);
     }
     return kBigResidual;
@@ -428,7 +428,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate4(const Params P,
             float ea = ex_sample_out_alpha(P.ex, t.x, t.y, t.layer);
             if (ea < kAlphaThreshold && ia > kAlphaThreshold) continue;
         }
-        if (P.counters) count_eval(P, x, y);
+        if (P.counters) count_eval(P, x, y, px.temporal);
         ev[n] = Cand{t.x, t.y, t.theta, t.su, t.sv, t.layer};
         slot[cdx] = n;
         n++;
@@ -531,7 +531,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_residual(const Params P, f
     if (image_culled(P, px.x, px.y)) { out[k] = 0.0f; return; }
     Patch t = load_patch(P.off, k);
     Cand c{t.x, t.y, t.theta, t.su, t.sv, t.layer};
-    if (P.counters) count_eval(P, px.x, px.y);
+    if (P.counters) count_eval(P, px.x, px.y, px.temporal);
     out[k] = energy_tiled<R, TM>(P, T, px, c);
 }
 

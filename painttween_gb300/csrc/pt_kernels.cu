@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(128) k_residual(const Params P, float* out) {
     PixCtx pc;
     make_pixctx(P, x, y, &pc);
     Patch t = load_patch(P.off, k);
-    if (P.counters) count_eval(P, x, y);
+    if (P.counters) count_eval(P, x, y, pc.temporalF || pc.temporalB);
     out[k] = energy(P, x, y, t, pc);
 }
 

@@ -98,7 +98,7 @@ struct Params {
     const float* res;          // residual base
     const float4* canvas;
     AdvView adv[2];            // [0] = forward, [1] = backward
-    unsigned long long* counters;  // profiling: [0] energy evaluations, [1] taps (null = off)
+    unsigned long long* counters;  // profiling: energy evaluations, taps, temporal taps (null = off)
 };
 
 struct ConvKernel {

@@ -95,7 +95,8 @@ class TexSynth:
     def kernel_stats(self, kernel):
         st = _abi.KernelStats()
         self._check(lib().pt_get_kernel_stats(self.h, kernel, ctypes.byref(st)), "pt_get_kernel_stats")
-        return dict(launches=st.launches, total_ms=st.total_ms, energy_evals=st.energy_evals, taps=st.taps)
+        return dict(launches=st.launches, total_ms=st.total_ms, energy_evals=st.energy_evals, taps=st.taps,
+                    temporal_taps=st.temporal_taps)
 
     # -- configuration (TexSynth::setup / uploadParameters) ----------------------
     def set_params(self, params):
@@ -166,6 +167,11 @@ class TexSynth:
 
     def reset_advected_buffers(self):
         self._check(lib().pt_reset_advected_buffers(self.h), "pt_reset_advected_buffers")
+
+    def convolve_separable(self, src_dev, dst_dev, w, h, pitch, radius):
+        """Gaussian blur of a device float image (device pointers as ints)."""
+        self._check(lib().pt_convolve_separable(self.h, ctypes.c_void_p(src_dev), ctypes.c_void_p(dst_dev), w, h,
+                                                pitch, radius), "pt_convolve_separable")
 
     # -- state transfer ------------------------------------------------------------
     def load_offsets(self, level, offsets):

@@ -372,3 +372,21 @@ def test_tiled_and_generic_kernels_identical(r):
     ref = O.OracleDriver(p, [ex], clip, threads=8).render(0, 2)
     for f in range(3):
         assert_offsets_equal(outs[0][f][1], ref[f][0], 0.999, "tiled vs oracle frame %d" % f)
+
+
+@pytest.mark.parametrize("radius", [1, 3, 7])
+def test_convolve_separable_matches_oracle(radius):
+    """Separable Gaussian (convolutionRowsGPU + convolutionColumnsGPU) on a
+    device image, against the oracle bit for bit."""
+    torch = pytest.importorskip("torch")
+    from painttween_gb300 import TexSynth
+    rng = np.random.default_rng(radius)
+    img = rng.uniform(0, 5, (70, 93)).astype(np.float32)
+    ref = O.convolve_separable(img, radius)
+    src = torch.from_numpy(img).cuda()
+    dst = torch.zeros_like(src)
+    t = TexSynth(device=0)
+    t.convolve_separable(src.data_ptr(), dst.data_ptr(), 93, 70, 93, radius)
+    t.synchronize()
+    t.close()
+    assert_array_equal(dst.cpu().numpy(), ref, "separable Gaussian r=%d" % radius)
