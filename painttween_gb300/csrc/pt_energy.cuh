@@ -41,17 +41,16 @@ struct TileSmem {
 };
 
 // bilinear base+output at (u, v) of one exemplar layer (LB: base plane,
-// LO: output plane); FAST: the footprint is known to be inside
-// [0, w-1] x [0, h-1] (no clamping needed)
-template <bool FAST>
+// LO: output plane); fast (warp-uniform): the footprint is known to be
+// inside [0, w-1] x [0, h-1], so the clamps are no-ops and are skipped
 __device__ __forceinline__ void sample2(const float4* LB, const float4* LO, int w, int h, float u, float v,
-                                        float4* base, float4* out) {
+                                        float4* base, float4* out, bool fast) {
     float xs = u + 0.5f, ys = v + 0.5f;
     float xb = xs - 0.5f, yb = ys - 0.5f;
     float fx = floorf(xb), fy = floorf(yb);
     float a = xb - fx, c = yb - fy;
     int x0, x1, y0, y1;
-    if (FAST) {
+    if (fast) {
         x0 = (int)fx; y0 = (int)fy; x1 = x0 + 1; y1 = y0 + 1;
     } else {
         fx = fminf(fmaxf(fx, -1.0f), (float)w);
@@ -100,9 +99,9 @@ __device__ __forceinline__ bool footprint_inside(float x, float y, float2 b0, fl
     return (x - bx >= 0.0f) && (x + bx <= (float)(w - 2)) && (y - by >= 0.0f) && (y + by <= (float)(h - 2));
 }
 
-template <int R, int TM, bool FAST, bool FASTP>
+template <int R, int TM>
 __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
-                                             const Cand& c, float2 b0, float2 b1, float sum0) {
+                                             const Cand& c, float2 b0, float2 b1, float sum0, bool fast, bool fastp) {
     constexpr int TW = TileSmem<R, TM>::TW;
     const size_t lsz = (size_t)P.ex.w * P.ex.h;
     const size_t lo = (size_t)ex_layer(P.ex, c.layer) * lsz;
@@ -121,12 +120,12 @@ __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, 
             float4 canvas = T.canvas[s];
             float tx = c.x + fmaf((float)i, b0.x, (float)j * b1.x);
             float ty = c.y + fmaf((float)i, b0.y, (float)j * b1.y);
-            if (!FAST) {
+            if (!fast) {
                 if (tx >= hw) tx -= hw; else if (tx < 0) tx += hw;
                 if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
             }
             float4 tb, to;
-            sample2<FAST>(LB, LO, P.ex.w, P.ex.h, tx, ty, &tb, &to);
+            sample2(LB, LO, P.ex.w, P.ex.h, tx, ty, &tb, &to, fast);
             float res = ssd_a(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
             if (TM) {
                 if (px.temporal) {
@@ -134,7 +133,7 @@ __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, 
                     float ptx = px.prev.x + fmaf((float)i, px.pb0.x, (float)j * px.pb1.x);
                     float pty = px.prev.y + fmaf((float)i, px.pb0.y, (float)j * px.pb1.y);
                     float4 peb, peo;
-                    sample2<FASTP>(P.ex.base + lp, P.ex.out + lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo);
+                    sample2(P.ex.base + lp, P.ex.out + lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo, fastp);
                     float r = ssd(sub4(base, pbase), sub4(tb, peb)) * P.tdIn;
                     r = fmaf(ssd(sub4(canvas, pout), sub4(to, peo)), P.tdOut, r);
                     r = fmaf(ssd(pout, to), P.tc, r);
@@ -181,14 +180,10 @@ __device__ __forceinline__ float energy_tiled(const Params& P, const TileSmem<R,
     if (px.hyst_on) sum0 = sum0 - px.hyst;
     float2 b0, b1;
     basis(c.theta, P.scaleWU * c.su, P.scaleWV * c.sv, &b0, &b1);
-    bool fast = footprint_inside<R>(c.x, c.y, b0, b1, P.ex.w, P.ex.h);
-    fast = __all_sync(__activemask(), fast);
-    if (TM) {
-        if (fast && px.prev_fast) return energy_taps<R, TM, true, true>(P, T, px, c, b0, b1, sum0);
-        return energy_taps<R, TM, false, false>(P, T, px, c, b0, b1, sum0);
-    }
-    if (fast) return energy_taps<R, TM, true, true>(P, T, px, c, b0, b1, sum0);
-    return energy_taps<R, TM, false, false>(P, T, px, c, b0, b1, sum0);
+    const unsigned mask = __activemask();
+    bool fast = __all_sync(mask, footprint_inside<R>(c.x, c.y, b0, b1, P.ex.w, P.ex.h));
+    bool fastp = TM ? __all_sync(mask, !px.temporal || px.prev_fast) : true;
+    return energy_taps<R, TM>(P, T, px, c, b0, b1, sum0, fast, fastp);
 }
 
 // test_offset + isExemplarPixelCulled, texSynth_kernel.cu:200-205,695-721
@@ -264,10 +259,10 @@ __device__ __forceinline__ bool stage_tile(const Params& P, TileSmem<R, TM>& T, 
 // sample of each tap (both independent of the candidate) are done once per
 // tap; every candidate keeps its own sums in the reference's tap order, so
 // each energy is bit-identical to a separate evaluation.
-template <int R, int TM, int NC, bool FASTP>
+template <int R, int TM, int NC>
 __device__ __forceinline__ void energyN_taps(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
                                              const Cand* c, const float2* b0, const float2* b1, int n,
-                                             const bool* fast, float* sum, float* sumW) {
+                                             bool fast, bool fastp, float* sum, float* sumW) {
     constexpr int TW = TileSmem<R, TM>::TW;
     const size_t lsz = (size_t)P.ex.w * P.ex.h;
     size_t lo[NC];
@@ -291,7 +286,7 @@ __device__ __forceinline__ void energyN_taps(const Params& P, const TileSmem<R, 
                     pout = T.pout[s];
                     float ptx = px.prev.x + fmaf((float)i, px.pb0.x, (float)j * px.pb1.x);
                     float pty = px.prev.y + fmaf((float)i, px.pb0.y, (float)j * px.pb1.y);
-                    sample2<FASTP>(P.ex.base + lp, P.ex.out + lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo);
+                    sample2(P.ex.base + lp, P.ex.out + lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo, fastp);
                     tvalid = T.phys[s] > 0;
                 }
             }
@@ -301,14 +296,12 @@ __device__ __forceinline__ void energyN_taps(const Params& P, const TileSmem<R, 
                 if (k < n) {
                     float tx = c[k].x + fmaf((float)i, b0[k].x, (float)j * b1[k].x);
                     float ty = c[k].y + fmaf((float)i, b0[k].y, (float)j * b1[k].y);
-                    float4 tb, to;
-                    if (fast[k]) {  // warp-uniform: footprint inside the exemplar
-                        sample2<true>(P.ex.base + lo[k], P.ex.out + lo[k], P.ex.w, P.ex.h, tx, ty, &tb, &to);
-                    } else {
+                    if (!fast) {
                         if (tx >= hw) tx -= hw; else if (tx < 0) tx += hw;
                         if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
-                        sample2<false>(P.ex.base + lo[k], P.ex.out + lo[k], P.ex.w, P.ex.h, tx, ty, &tb, &to);
                     }
+                    float4 tb, to;
+                    sample2(P.ex.base + lo[k], P.ex.out + lo[k], P.ex.w, P.ex.h, tx, ty, &tb, &to, fast);
                     float res = ssd_a(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
                     if (TM) {
                         if (px.temporal) {
@@ -356,8 +349,7 @@ __device__ __forceinline__ void energyN(const Params& P, const TileSmem<R, TM>& 
                                         int n, float* out) {
     float2 b0[NC], b1[NC];
     float sum[NC], sumW[NC];
-    bool fast[NC];
-    const unsigned mask = __activemask();
+    bool f = true;
 #pragma unroll
     for (int k = 0; k < NC; k++) {
         sum[k] = 0.0f;
@@ -365,17 +357,15 @@ __device__ __forceinline__ void energyN(const Params& P, const TileSmem<R, TM>& 
         sumW[k] = 0.0f;
         b0[k] = make_float2(0.f, 0.f);
         b1[k] = make_float2(0.f, 0.f);
-        bool f = true;
         if (k < n) {
             basis(c[k].theta, P.scaleWU * c[k].su, P.scaleWV * c[k].sv, &b0[k], &b1[k]);
-            f = footprint_inside<R>(c[k].x, c[k].y, b0[k], b1[k], P.ex.w, P.ex.h);
+            f = f && footprint_inside<R>(c[k].x, c[k].y, b0[k], b1[k], P.ex.w, P.ex.h);
         }
-        fast[k] = __all_sync(mask, f);
     }
-    bool fastp = true;
-    if (TM) fastp = __all_sync(mask, !px.temporal || px.prev_fast);
-    if (fastp) energyN_taps<R, TM, NC, true>(P, T, px, c, b0, b1, n, fast, sum, sumW);
-    else energyN_taps<R, TM, NC, false>(P, T, px, c, b0, b1, n, fast, sum, sumW);
+    const unsigned mask = __activemask();
+    const bool fast = __all_sync(mask, f);
+    const bool fastp = TM ? __all_sync(mask, !px.temporal || px.prev_fast) : true;
+    energyN_taps<R, TM, NC>(P, T, px, c, b0, b1, n, fast, fastp, sum, sumW);
 #pragma unroll
     for (int k = 0; k < NC; k++) out[k] = (sumW[k] < kEpsilon) ? kBigResidual : sum[k] / sumW[k];
 }
@@ -467,38 +457,45 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter(const Params P, Pa
     float dist = (float)(P.ex.w > P.ex.h ? P.ex.w : P.ex.h);
     const float closest = 10.f, factor = 0.9f;
     float2 sc = lvl_texel(P.img.scale, x, y);
-    // the chain often clamps several candidates to the same exemplar
-    // position; an exact repeat of the previous evaluated candidate has the
-    // same energy and is rejected by the strict "<" test, so it is skipped
+    // Each lane advances along its chain to the next candidate that needs
+    // an energy (an exact repeat of the previous evaluated candidate has the
+    // same energy and is rejected by the strict "<" test, so it is skipped);
+    // the warp then evaluates the lanes' candidates together.
     uint32_t lastx = 0xffffffffu, lasty = 0xffffffffu;
+    int i = 0;
 #pragma unroll 1
-    for (int i = 0; i < P.scatterSamples && dist * factor >= closest; i++) {
-        float dmin = dist * factor;
-        float ex, ey;
-        if (P.rngMode == PT_RNG_COUNTER) {
-            float rr = counter_u01(P.rngSeed, pass_id, x, y, 2 * i);
-            float th = counter_u01(P.rngSeed, pass_id, x, y, 2 * i + 1) * 6.28318530717958647692f;
-            float s, c;
-            sincos_poly(th, &s, &c);
-            float len = fmaf(rr, dist - dmin, dmin);
-            ex = fmaf(c, len, ow.x);
-            ey = fmaf(s, len, ow.y);
-        } else {
-            ex = ow.x + dmin;
-            ey = ow.y + 0.0f;
-        }
-        clamp_to_exemplar(&ex, &ey, P.ex.w, P.ex.h);
-        if (__float_as_uint(ex) == lastx && __float_as_uint(ey) == lasty) {
+    while (true) {
+        bool have = false;
+        float ex = 0.f, ey = 0.f;
+#pragma unroll 1
+        while (i < P.scatterSamples && dist * factor >= closest) {
+            float dmin = dist * factor;
+            if (P.rngMode == PT_RNG_COUNTER) {
+                float rr = counter_u01(P.rngSeed, pass_id, x, y, 2 * i);
+                float th = counter_u01(P.rngSeed, pass_id, x, y, 2 * i + 1) * 6.28318530717958647692f;
+                float s, c;
+                sincos_poly(th, &s, &c);
+                float len = fmaf(rr, dist - dmin, dmin);
+                ex = fmaf(c, len, ow.x);
+                ey = fmaf(s, len, ow.y);
+            } else {
+                ex = ow.x + dmin;
+                ey = ow.y + 0.0f;
+            }
+            clamp_to_exemplar(&ex, &ey, P.ex.w, P.ex.h);
+            i++;
             dist *= factor;
-            continue;
+            if (__float_as_uint(ex) == lastx && __float_as_uint(ey) == lasty) continue;
+            lastx = __float_as_uint(ex);
+            lasty = __float_as_uint(ey);
+            have = true;
+            break;
         }
-        lastx = __float_as_uint(ex);
-        lasty = __float_as_uint(ey);
+        if (!have) break;
         float ang = screen_to_exemplar_angle(P, x, y, ex, ey, 0);
         Cand c{ex, ey, ang, sc.x, sc.y, 0};
         float r = test_offset_tiled<R, TM>(P, T, px, c, ia);
         if (r < best) { ow = make_patch(ex, ey, ang, 0.0f, 0, sc.x, sc.y); best = r; }
-        dist *= factor;
     }
     Patch avg = make_patch(0, 0, 0, 1.f, 0, 1.f, 1.f);
     int n = 0;
