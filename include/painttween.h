@@ -253,6 +253,30 @@ pt_status pt_get_output(pt_ctx* ctx, int level, float* out_rgba);
 pt_status pt_convolve_separable(pt_ctx* ctx, const float* src_dev, float* dst_dev, int w, int h, int pitch,
                                 int radius);
 
+/* Allocation-free variant of pt_convolve_separable, for callers that cannot
+ * allocate device memory when they call it (a plugin host that owns all
+ * device memory through its own pool and forbids cudaMalloc in its frame
+ * callbacks, or a process whose memory a framework's caching allocator
+ * holds).  It has no counterpart in the reference.
+ *  - No context: the caller passes device pointers to its input and output
+ *    (row pitch `pitch` floats) and the CUDA stream to run on (NULL = the
+ *    default stream); the current device is used.
+ *  - The row-pass intermediate lives in a fixed array of
+ *    PT_NOALLOC_MAX_PIXELS floats (4 MiB) in the library's device memory,
+ *    which every GPU that loads the library holds until the process exits.
+ *    pitch * h above that limit returns PT_ERR_INVALID.  Nothing is
+ *    allocated or freed by the call.
+ *  - The first call on a device looks up the array's device address (once
+ *    per device); make that first call outside any stream capture.
+ *  - All calls share the one array and it keeps the last call's contents:
+ *    calls that overlap on the GPU (different streams, or different host
+ *    threads on one device) race on it and must be serialised by the caller.
+ *    No element needs clearing: the column pass reads only what the row
+ *    pass of the same call wrote. */
+#define PT_NOALLOC_MAX_PIXELS (1 << 20)
+pt_status pt_convolve_separable_noalloc(const float* src_dev, float* dst_dev, int w, int h, int pitch, int radius,
+                                        void* stream);
+
 /* ---- working-set level API (pyramids built and kept on the device) ----- */
 
 /* Uploads one style exemplar at level-0 size and builds its pyramid on the
