@@ -99,9 +99,13 @@ __device__ __forceinline__ bool footprint_inside(float x, float y, float2 b0, fl
     return (x - bx >= 0.0f) && (x + bx <= (float)(w - 2)) && (y - by >= 0.0f) && (y + by <= (float)(h - 2));
 }
 
+// One body for both cases: the single-candidate kernels (scatter in
+// particular) are instruction-cache bound, and a second, compile-time fast
+// copy of this loop measured slower there.
 template <int R, int TM>
 __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
-                                             const Cand& c, float2 b0, float2 b1, float sum0, bool fast, bool fastp) {
+                                             const Cand& c, float2 b0, float2 b1, float sum0, bool fast,
+                                             bool fastp) {
     constexpr int TW = TileSmem<R, TM>::TW;
     const size_t lsz = (size_t)P.ex.w * P.ex.h;
     const size_t lo = (size_t)ex_layer(P.ex, c.layer) * lsz;
@@ -259,10 +263,14 @@ __device__ __forceinline__ bool stage_tile(const Params& P, TileSmem<R, TM>& T, 
 // sample of each tap (both independent of the candidate) are done once per
 // tap; every candidate keeps its own sums in the reference's tap order, so
 // each energy is bit-identical to a separate evaluation.
-template <int R, int TM, int NC>
+// AF: every footprint of the warp is inside the exemplar; fast and fastp
+// are then true at compile time and no wrap/clamp code is emitted.  The
+// multi-candidate loop runs long enough per call that this second copy pays.
+template <int R, int TM, int NC, bool AF>
 __device__ __forceinline__ void energyN_taps(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
                                              const Cand* c, const float2* b0, const float2* b1, int n,
-                                             bool fast, bool fastp, float* sum, float* sumW) {
+                                             bool fast_, bool fastp_, float* sum, float* sumW) {
+    const bool fast = AF || fast_, fastp = AF || fastp_;
     constexpr int TW = TileSmem<R, TM>::TW;
     const size_t lsz = (size_t)P.ex.w * P.ex.h;
     size_t lo[NC];
@@ -365,7 +373,8 @@ __device__ __forceinline__ void energyN(const Params& P, const TileSmem<R, TM>& 
     const unsigned mask = __activemask();
     const bool fast = __all_sync(mask, f);
     const bool fastp = TM ? __all_sync(mask, !px.temporal || px.prev_fast) : true;
-    energyN_taps<R, TM, NC>(P, T, px, c, b0, b1, n, fast, fastp, sum, sumW);
+    if (fast && fastp) energyN_taps<R, TM, NC, true>(P, T, px, c, b0, b1, n, true, true, sum, sumW);
+    else energyN_taps<R, TM, NC, false>(P, T, px, c, b0, b1, n, fast, fastp, sum, sumW);
 #pragma unroll
     for (int k = 0; k < NC; k++) out[k] = (sumW[k] < kEpsilon) ? kBigResidual : sum[k] / sumW[k];
 }
@@ -387,9 +396,11 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate4(const Params P,
     Patch ow = load_patch(P.off, k);
     // the four candidates in the reference's order; a candidate that repeats
     // an earlier one, or that test_offset rejects before the energy, keeps
-    // its fixed outcome
-    Patch cand[4];
-    float res[4];
+    // its fixed outcome.  Only the keys and the evaluated candidates stay
+    // live across the tap loop; the winner is rebuilt afterwards (the
+    // construction is deterministic).
+    uint32_t kx[4], ky[4], kt[4];
+    int kl[4];
     int slot[4];
     Cand ev[4];
     int n = 0;
@@ -400,18 +411,17 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate4(const Params P,
         else if (cdx == 1) tx = x - jump;
         else if (cdx == 2) ty = y + jump;
         else ty = y - jump;
-        cand[cdx] = propagate_offset(P, tx, ty, x, y);
+        Patch t = propagate_offset(P, tx, ty, x, y);
+        kx[cdx] = __float_as_uint(t.x);
+        ky[cdx] = __float_as_uint(t.y);
+        kt[cdx] = __float_as_uint(t.theta);
+        kl[cdx] = t.layer;
         slot[cdx] = -1;
-        res[cdx] = kBigResidual;
         bool dup = false;
 #pragma unroll
         for (int q = 0; q < cdx; q++)
-            dup |= __float_as_uint(cand[q].x) == __float_as_uint(cand[cdx].x) &&
-                   __float_as_uint(cand[q].y) == __float_as_uint(cand[cdx].y) &&
-                   __float_as_uint(cand[q].theta) == __float_as_uint(cand[cdx].theta) &&
-                   cand[q].layer == cand[cdx].layer;
+            dup |= kx[q] == kx[cdx] && ky[q] == ky[cdx] && kt[q] == kt[cdx] && kl[q] == kl[cdx];
         if (dup) { slot[cdx] = -2; continue; }
-        const Patch& t = cand[cdx];
         float dte = ex_texel_dt(P.ex, (int)t.x, (int)t.y, t.layer);
         if ((double)dte > (double)P.distTransCull * 1.25) continue;
         if (!P.transparencyOk) {
@@ -425,13 +435,23 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate4(const Params P,
     }
     float e[4];
     energyN<R, TM, 4>(P, T, px, ev, n, e);
+    int win = -1;
 #pragma unroll
     for (int cdx = 0; cdx < 4; cdx++) {
-        if (slot[cdx] == -2) continue;  // repeat: same energy, rejected by "<"
+        if (slot[cdx] < 0) continue;  // repeat (same energy, rejected by "<") or rejected early (1e31)
+        float r = kBigResidual;
 #pragma unroll
         for (int q = 0; q < 4; q++)
-            if (slot[cdx] == q) res[cdx] = e[q];
-        if (res[cdx] < best) { ow = cand[cdx]; best = res[cdx]; }
+            if (slot[cdx] == q) r = e[q];
+        if (r < best) { best = r; win = cdx; }
+    }
+    if (win >= 0) {
+        int tx = x, ty = y;
+        if (win == 0) tx = x + jump;
+        else if (win == 1) tx = x - jump;
+        else if (win == 2) ty = y + jump;
+        else ty = y - jump;
+        ow = propagate_offset(P, tx, ty, x, y);
     }
     store_patch(work, k, ow);
 }
