@@ -39,10 +39,12 @@ WORKLOAD = "clip1080p"
 METRIC = "1080p stylized frames/s"
 UNIT = "frames/s"
 
-# DRAM bytes per patch-distance evaluation of the propagate kernel, from the
-# ncu capture summarised in profiles/propagate_clip1080p.md (None until a
-# capture exists).
-PROPAGATE_DRAM_BYTES_PER_EVAL = None
+# DRAM bytes (read + write) per level pixel of one kt_propagate4 launch: the
+# ncu capture of a level-0 temporal launch of this workload (1920x1080 level,
+# 293.3 MB read + 94.5 MB written) summarised in
+# profiles/kt_energy_kernels_clip1080p.md.  The exemplar planes stay in L2,
+# so DRAM traffic follows the staged pixel-side planes, i.e. the level area.
+PROPAGATE_DRAM_BYTES_PER_PIXEL = (293.295104e6 + 94.506496e6) / (1920 * 1080)
 
 
 def peaks():
@@ -347,8 +349,10 @@ def run_ours(args, dist):
     sm_mhz = (ck or {}).get("sm_mhz") or 1900.0
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
     fp32_achieved = flops_per_launch / avg_launch_s / 1e12
-    traffic = (None if PROPAGATE_DRAM_BYTES_PER_EVAL is None
-               else PROPAGATE_DRAM_BYTES_PER_EVAL * evals_per_launch)
+    # every level runs the same propagate passes, so the average launch covers
+    # the mean level area
+    level_px = float(np.mean([(cfg["w"] >> lv) * (cfg["h"] >> lv) for lv in range(p.levels)]))
+    traffic = PROPAGATE_DRAM_BYTES_PER_PIXEL * level_px
     kernel_share = st["total_ms"] / max(sum(v["total_ms"] for v in stats.values()), 1e-9)
 
     value = dist.ws * frames * args.steps / (total_ms / 1000.0)

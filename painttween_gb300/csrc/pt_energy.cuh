@@ -477,12 +477,34 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter(const Params P, Pa
     float dist = (float)(P.ex.w > P.ex.h ? P.ex.w : P.ex.h);
     const float closest = 10.f, factor = 0.9f;
     float2 sc = lvl_texel(P.img.scale, x, y);
+    // averageOffset of the base field (texSynth_kernel.cu:841-861): it does
+    // not depend on the chain, so it is formed first and tested last
+    Patch avg = make_patch(0, 0, 0, 1.f, 0, 1.f, 1.f);
+    {
+        int n = 0;
+        for (int i = -1; i <= 1; i++)
+            for (int j = -1; j <= 1; j++) {
+                if (!in_rect(P, x + i, y + j) || (i == 0 && j == 0)) continue;
+                float4 nb = __ldg(P.off.A + (size_t)(y + j) * P.W + (x + i));
+                if (__float_as_int(nb.w) != 0) continue;
+                avg.x = avg.x + nb.x;
+                avg.y = avg.y + nb.y;
+                n++;
+            }
+        avg.x = avg.x / (float)n;
+        avg.y = avg.y / (float)n;
+        avg.theta = screen_to_exemplar_angle(P, x, y, avg.x, avg.y, 0);
+    }
     // Each lane advances along its chain to the next candidate that needs
     // an energy (an exact repeat of the previous evaluated candidate has the
     // same energy and is rejected by the strict "<" test, so it is skipped);
-    // the warp then evaluates the lanes' candidates together.
+    // after the chain it takes the average offset.  The warp evaluates the
+    // lanes' candidates together through one call site of the energy, so
+    // lanes at different points of their chains still run converged and the
+    // tap loop is emitted once.
     uint32_t lastx = 0xffffffffu, lasty = 0xffffffffu;
     int i = 0;
+    bool avg_pending = true;
 #pragma unroll 1
     while (true) {
         bool have = false;
@@ -511,29 +533,21 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter(const Params P, Pa
             have = true;
             break;
         }
-        if (!have) break;
-        float ang = screen_to_exemplar_angle(P, x, y, ex, ey, 0);
-        Cand c{ex, ey, ang, sc.x, sc.y, 0};
-        float r = test_offset_tiled<R, TM>(P, T, px, c, ia);
-        if (r < best) { ow = make_patch(ex, ey, ang, 0.0f, 0, sc.x, sc.y); best = r; }
-    }
-    Patch avg = make_patch(0, 0, 0, 1.f, 0, 1.f, 1.f);
-    int n = 0;
-    for (int i = -1; i <= 1; i++)
-        for (int j = -1; j <= 1; j++) {
-            if (!in_rect(P, x + i, y + j) || (i == 0 && j == 0)) continue;
-            float4 nb = __ldg(P.off.A + (size_t)(y + j) * P.W + (x + i));
-            if (__float_as_int(nb.w) != 0) continue;
-            avg.x = avg.x + nb.x;
-            avg.y = avg.y + nb.y;
-            n++;
+        Cand c;
+        if (have) {
+            c = Cand{ex, ey, screen_to_exemplar_angle(P, x, y, ex, ey, 0), sc.x, sc.y, 0};
+        } else if (avg_pending) {
+            c = Cand{avg.x, avg.y, avg.theta, avg.su, avg.sv, 0};
+            avg_pending = false;
+        } else {
+            break;
         }
-    avg.x = avg.x / (float)n;
-    avg.y = avg.y / (float)n;
-    avg.theta = screen_to_exemplar_angle(P, x, y, avg.x, avg.y, 0);
-    Cand c{avg.x, avg.y, avg.theta, avg.su, avg.sv, 0};
-    float r = test_offset_tiled<R, TM>(P, T, px, c, ia);
-    if (r < best) { ow = avg; best = r; }
+        float r = test_offset_tiled<R, TM>(P, T, px, c, ia);
+        if (r < best) {
+            ow = have ? make_patch(c.x, c.y, c.theta, 0.0f, 0, sc.x, sc.y) : avg;
+            best = r;
+        }
+    }
     if (best < cached) store_patch(work, k, ow);
     else if (write_all) store_patch(work, k, off);
 }
