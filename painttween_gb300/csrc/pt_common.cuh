@@ -68,6 +68,34 @@ static __device__ __forceinline__ float ssd(float4 a, float4 b) {
 }
 static __device__ __forceinline__ float4 sub4(float4 a, float4 b) { return f4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
 
+// The same three functions with the channel differences formed two channels
+// at a time by the packed f32x2 add (a + (-b) is a - b exactly, per
+// component, in round-to-nearest); the sums of squares keep the scalar order
+// x, y, z, w, so results are bit-identical.  Used where they measured faster
+// (the single-candidate tap loop); the four-candidate loop keeps the scalar
+// forms, which need fewer registers there.
+static __device__ __forceinline__ float4 sub4p(float4 a, float4 b) {
+    float2 l = __fadd2_rn(make_float2(a.x, a.y), make_float2(-b.x, -b.y));
+    float2 h = __fadd2_rn(make_float2(a.z, a.w), make_float2(-b.z, -b.w));
+    return f4(l.x, l.y, h.x, h.y);
+}
+static __device__ __forceinline__ float ssd_ap(float4 a, float4 b, float alpha) {
+    const float4 d = sub4p(a, b);
+    float s = d.x * d.x;
+    s = fmaf(d.y, d.y, s);
+    s = fmaf(d.z, d.z, s);
+    s = fmaf(alpha * d.w, d.w, s);
+    return s;
+}
+static __device__ __forceinline__ float ssdp(float4 a, float4 b) {
+    const float4 d = sub4p(a, b);
+    float s = d.x * d.x;
+    s = fmaf(d.y, d.y, s);
+    s = fmaf(d.z, d.z, s);
+    s = fmaf(d.w, d.w, s);
+    return s;
+}
+
 struct PixCtx {
     bool validF, validB, temporalF, temporalB;
     Patch prevF, prevB;
@@ -223,17 +251,22 @@ static __device__ __forceinline__ unsigned lane_id() {
     asm volatile("mov.u32 %0, %%laneid;" : "=r"(l));
     return l;
 }
-static __device__ __forceinline__ void count_eval(const Params& P, int x, int y, bool temporal) {
+// profiling counters: one evaluation and (with_taps) its taps; the tiled
+// kernels count the taps they actually process after the tap loop
+static __device__ __forceinline__ void count_eval(const Params& P, int x, int y, bool temporal,
+                                                  bool with_taps = true) {
     int x0 = max(x - P.r, 0), x1 = min(x + P.r, P.lw - 1);
     int y0 = max(y - P.r, 0), y1 = min(y + P.r, P.lh - 1);
-    unsigned taps = (unsigned)((x1 - x0 + 1) * (y1 - y0 + 1));
+    unsigned taps = with_taps ? (unsigned)((x1 - x0 + 1) * (y1 - y0 + 1)) : 0u;
     unsigned mask = __activemask();
     unsigned tsum = __reduce_add_sync(mask, taps);
     unsigned ttsum = __reduce_add_sync(mask, temporal ? taps : 0u);
     if (lane_id() == (unsigned)(__ffs(mask) - 1)) {
         atomicAdd(&P.counters[0], (unsigned long long)__popc(mask));
-        atomicAdd(&P.counters[1], (unsigned long long)tsum);
-        atomicAdd(&P.counters[2], (unsigned long long)ttsum);
+        if (with_taps) {
+            atomicAdd(&P.counters[1], (unsigned long long)tsum);
+            atomicAdd(&P.counters[2], (unsigned long long)ttsum);
+        }
     }
 }
 

@@ -255,6 +255,15 @@ static Params make_params(pt_ctx* c, int level) {
         P.histThreshold[i] = p.offsetsHistogramThreshold[i];
         P.histSlope[i] = p.offsetsHistogramSlope[i];
     }
+    // A candidate's partial patch sum can only grow when every weight that
+    // scales a per-tap term is non-negative (NaN weights fail the test).
+    {
+        bool nonneg = P.alphaWeight >= 0.f && P.inputAnalogyWeight >= 0.f && P.canvasOutputWeight >= 0.f &&
+                      P.tdIn >= 0.f && P.tdOut >= 0.f && P.tc >= 0.f;
+        for (int i = 0; i < PT_MAX_STYLES; i++) nonneg = nonneg && P.histSlope[i] >= 0.f;
+        for (int i = 0; i < 2 * P.r + 1; i++) nonneg = nonneg && P.gauss[i] >= 0.f;
+        P.earlyExit = nonneg ? 1 : 0;
+    }
     P.jitter = p.advectionJitter;
     P.numStyles = p.numStyles > 0 ? p.numStyles : 1;
     P.transparencyOk = p.transparencyOk;

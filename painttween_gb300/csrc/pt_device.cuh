@@ -227,6 +227,21 @@ __device__ __forceinline__ float4 bl4(const Bl& b, float4 a, float4 c, float4 d,
     return f4(bl1(b, a.x, c.x, d.x, e.x), bl1(b, a.y, c.y, d.y, e.y),
               bl1(b, a.z, c.z, d.z, e.z), bl1(b, a.w, c.w, d.w, e.w));
 }
+// bl4 with two channels per packed f32x2 multiply-add (each component
+// rounds exactly as bl1)
+__device__ __forceinline__ float4 bl4p(const Bl& b, float4 a, float4 c, float4 d, float4 e) {
+    const float2 w00 = make_float2(b.w00, b.w00), w10 = make_float2(b.w10, b.w10);
+    const float2 w01 = make_float2(b.w01, b.w01), w11 = make_float2(b.w11, b.w11);
+    float2 l = __fmul2_rn(make_float2(a.x, a.y), w00);
+    float2 h = __fmul2_rn(make_float2(a.z, a.w), w00);
+    l = __ffma2_rn(make_float2(c.x, c.y), w10, l);
+    h = __ffma2_rn(make_float2(c.z, c.w), w10, h);
+    l = __ffma2_rn(make_float2(d.x, d.y), w01, l);
+    h = __ffma2_rn(make_float2(d.z, d.w), w01, h);
+    l = __ffma2_rn(make_float2(e.x, e.y), w11, l);
+    h = __ffma2_rn(make_float2(e.z, e.w), w11, h);
+    return f4(l.x, l.y, h.x, h.y);
+}
 
 __device__ __forceinline__ int ex_layer(const ExView& e, int layer) { return clampi(layer, 0, e.ns - 1); }
 

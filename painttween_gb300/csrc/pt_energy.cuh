@@ -43,6 +43,7 @@ struct TileSmem {
 // bilinear base+output at (u, v) of one exemplar layer (LB: base plane,
 // LO: output plane); fast (warp-uniform): the footprint is known to be
 // inside [0, w-1] x [0, h-1], so the clamps are no-ops and are skipped
+template <bool PK>
 __device__ __forceinline__ void sample2(const float4* LB, const float4* LO, int w, int h, float u, float v,
                                         float4* base, float4* out, bool fast) {
     float xs = u + 0.5f, ys = v + 0.5f;
@@ -67,8 +68,8 @@ __device__ __forceinline__ void sample2(const float4* LB, const float4* LO, int 
     float4 b01 = __ldg(LB + r1 + x0), b11 = __ldg(LB + r1 + x1);
     float4 o00 = __ldg(LO + r0 + x0), o10 = __ldg(LO + r0 + x1);
     float4 o01 = __ldg(LO + r1 + x0), o11 = __ldg(LO + r1 + x1);
-    *base = bl4(bw, b00, b10, b01, b11);
-    *out = bl4(bw, o00, o10, o01, o11);
+    *base = PK ? bl4p(bw, b00, b10, b01, b11) : bl4(bw, b00, b10, b01, b11);
+    *out = PK ? bl4p(bw, o00, o10, o01, o11) : bl4(bw, o00, o10, o01, o11);
 }
 
 struct Cand {
@@ -87,6 +88,7 @@ struct PixT {
     Patch prev;        // advected offset at the pixel (direction TM)
     float2 pb0, pb1;   // its basis
     bool prev_fast;    // its footprint is inside the exemplar
+    float sumW;        // sum of the valid taps' weights, in tap order (the same for every candidate)
 };
 
 // does the footprint of a patch at (x, y) with basis (b0, b1) stay inside
@@ -99,13 +101,46 @@ __device__ __forceinline__ bool footprint_inside(float x, float y, float2 b0, fl
     return (x - bx >= 0.0f) && (x + bx <= (float)(w - 2)) && (y - by >= 0.0f) && (y + by <= (float)(h - 2));
 }
 
+// Early exit.  When every per-tap term is >= 0 (Params::earlyExit), the
+// running sum of a candidate never decreases (each fmaf adds a non-negative
+// product and rounding is monotone), and the final energy is that sum divided
+// by the pixel's constant tap-weight sum.  Once the running sum reaches
+// thr2 = best * sumW rounded up, the energy is >= best whatever the remaining
+// taps add, so the reference's strict "<" test rejects the candidate: its
+// remaining taps are skipped and it returns +inf, which every caller rejects
+// the same way.  A candidate that is still below thr2 at the end returns
+// exactly sum / sumW.  A NaN thr2 (no early exit, or best = kNoBest) never
+// stops a sum, so the energy is computed in full, NaN and inf included.
+constexpr float kNoBest = __builtin_nanf("");
+__device__ __forceinline__ float exit_threshold(const Params& P, const PixT& px, float best) {
+    return (P.earlyExit && px.sumW >= kEpsilon) ? __fmul_ru(best, px.sumW) : kNoBest;
+}
+
+// taps a loop processed before it stopped: the valid taps of its first
+// `cols` columns
+template <int R>
+__device__ __forceinline__ unsigned taps_done(const PixT& px, int cols) {
+    const int last = min(-R + cols - 1, px.imax);
+    return last < px.imin ? 0u : (unsigned)((last - px.imin + 1) * (px.jmax - px.jmin + 1));
+}
+
+__device__ __forceinline__ void count_taps(const Params& P, unsigned taps, bool temporal) {
+    unsigned mask = __activemask();
+    unsigned tsum = __reduce_add_sync(mask, taps);
+    unsigned ttsum = __reduce_add_sync(mask, temporal ? taps : 0u);
+    if (lane_id() == (unsigned)(__ffs(mask) - 1)) {
+        atomicAdd(&P.counters[1], (unsigned long long)tsum);
+        atomicAdd(&P.counters[2], (unsigned long long)ttsum);
+    }
+}
+
 // One body for both cases: the single-candidate kernels (scatter in
 // particular) are instruction-cache bound, and a second, compile-time fast
 // copy of this loop measured slower there.
 template <int R, int TM>
 __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
                                              const Cand& c, float2 b0, float2 b1, float sum0, bool fast,
-                                             bool fastp) {
+                                             bool fastp, float thr2) {
     constexpr int TW = TileSmem<R, TM>::TW;
     const size_t lsz = (size_t)P.ex.w * P.ex.h;
     const size_t lo = (size_t)ex_layer(P.ex, c.layer) * lsz;
@@ -113,73 +148,82 @@ __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, 
     const float4* LO = P.ex.out + lo;
     const size_t lp = TM ? (size_t)ex_layer(P.ex, px.prev.layer) * lsz : 0;
     const float hw = (float)P.histW, hh = (float)P.histH;
-    float sum = sum0, sumW = 0.0f;
+    const unsigned mask = __activemask();
+    float sum = sum0;
+    bool act = !(sum >= thr2);
+    int cols = 0;
 #pragma unroll 1
     for (int i = -R; i <= R; i++) {
+        if (!__any_sync(mask, act)) break;
+        cols += act ? 1 : 0;
+        if (act) {
 #pragma unroll
-        for (int j = -R; j <= R; j++) {
-            const bool valid = (i >= px.imin) && (i <= px.imax) && (j >= px.jmin) && (j <= px.jmax);
-            const int s = px.sidx + j * TW + i;
-            float4 base = T.base[s];
-            float4 canvas = T.canvas[s];
-            float tx = c.x + fmaf((float)i, b0.x, (float)j * b1.x);
-            float ty = c.y + fmaf((float)i, b0.y, (float)j * b1.y);
-            if (!fast) {
-                if (tx >= hw) tx -= hw; else if (tx < 0) tx += hw;
-                if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
+            for (int j = -R; j <= R; j++) {
+                const bool valid = (i >= px.imin) && (i <= px.imax) && (j >= px.jmin) && (j <= px.jmax);
+                const int s = px.sidx + j * TW + i;
+                float4 base = T.base[s];
+                float4 canvas = T.canvas[s];
+                float tx = c.x + fmaf((float)i, b0.x, (float)j * b1.x);
+                float ty = c.y + fmaf((float)i, b0.y, (float)j * b1.y);
+                if (!fast) {
+                    if (tx >= hw) tx -= hw; else if (tx < 0) tx += hw;
+                    if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
+                }
+                float4 tb, to;
+                sample2<true>(LB, LO, P.ex.w, P.ex.h, tx, ty, &tb, &to, fast);
+                float res = ssd_ap(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
+                if (TM) {
+                    if (px.temporal) {
+                        float4 pbase = T.pbase[s], pout = T.pout[s];
+                        float ptx = px.prev.x + fmaf((float)i, px.pb0.x, (float)j * px.pb1.x);
+                        float pty = px.prev.y + fmaf((float)i, px.pb0.y, (float)j * px.pb1.y);
+                        float4 peb, peo;
+                        sample2<true>(P.ex.base + lp, P.ex.out + lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo, fastp);
+                        float r = ssdp(sub4p(base, pbase), sub4p(tb, peb)) * P.tdIn;
+                        r = fmaf(ssdp(sub4p(canvas, pout), sub4p(to, peo)), P.tdOut, r);
+                        r = fmaf(ssdp(pout, to), P.tc, r);
+                        res = (T.phys[s] > 0) ? res + r : res;
+                    }
+                }
+                if (i == 0 && j == 0) {
+                    if (P.distTransWeight > 0.f) {
+                        float de = ex_sample_dt(P.ex, tx, ty, c.layer) / c.sv;
+                        float di = lay_texel(P.img.dt[P.img.cur], P, px.x, px.y);
+                        float diff = fminf(fmaxf(fabsf(de - di), 0.0f), 10.0f);
+                        res = res + diff * P.distTransWeight;
+                    }
+                    {
+                        int Lh = clampi(c.layer, 0, PT_MAX_STYLES - 1);
+                        float sh = (float)(P.histH / P.numStyles);
+                        int hx = clampi((int)tx, 0, P.histPitch - 1);
+                        int hy = clampi((int)(ty + sh * (float)c.layer), 0, P.histRows - 1);
+                        float h = __ldg(P.hist + (size_t)hy * P.histPitch + hx);
+                        float thr = P.histThreshold[Lh];
+                        res = res + ((h > thr) ? (h - thr) * P.histSlope[Lh] : 0.0f);
+                    }
+                    if (P.styleObjIdWeight > 0.f) {
+                        int imgID = lvl_texel(P.img.ids, px.x, px.y);
+                        int styleID = ex_point_id(P.ex, tx, ty, c.layer);
+                        res = res + ((imgID != styleID) ? P.styleObjIdWeight : 0.0f);
+                    }
+                } else {
+                    res = fmaf(ssd_ap(canvas, to, P.alphaWeight), P.canvasOutputWeight, res);
+                }
+                const float w = P.gauss[i + R] * P.gauss[j + R];
+                sum = valid ? fmaf(res, w, sum) : sum;
             }
-            float4 tb, to;
-            sample2(LB, LO, P.ex.w, P.ex.h, tx, ty, &tb, &to, fast);
-            float res = ssd_a(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
-            if (TM) {
-                if (px.temporal) {
-                    float4 pbase = T.pbase[s], pout = T.pout[s];
-                    float ptx = px.prev.x + fmaf((float)i, px.pb0.x, (float)j * px.pb1.x);
-                    float pty = px.prev.y + fmaf((float)i, px.pb0.y, (float)j * px.pb1.y);
-                    float4 peb, peo;
-                    sample2(P.ex.base + lp, P.ex.out + lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo, fastp);
-                    float r = ssd(sub4(base, pbase), sub4(tb, peb)) * P.tdIn;
-                    r = fmaf(ssd(sub4(canvas, pout), sub4(to, peo)), P.tdOut, r);
-                    r = fmaf(ssd(pout, to), P.tc, r);
-                    res = (T.phys[s] > 0) ? res + r : res;
-                }
-            }
-            if (i == 0 && j == 0) {
-                if (P.distTransWeight > 0.f) {
-                    float de = ex_sample_dt(P.ex, tx, ty, c.layer) / c.sv;
-                    float di = lay_texel(P.img.dt[P.img.cur], P, px.x, px.y);
-                    float diff = fminf(fmaxf(fabsf(de - di), 0.0f), 10.0f);
-                    res = res + diff * P.distTransWeight;
-                }
-                {
-                    int Lh = clampi(c.layer, 0, PT_MAX_STYLES - 1);
-                    float sh = (float)(P.histH / P.numStyles);
-                    int hx = clampi((int)tx, 0, P.histPitch - 1);
-                    int hy = clampi((int)(ty + sh * (float)c.layer), 0, P.histRows - 1);
-                    float h = __ldg(P.hist + (size_t)hy * P.histPitch + hx);
-                    float thr = P.histThreshold[Lh];
-                    res = res + ((h > thr) ? (h - thr) * P.histSlope[Lh] : 0.0f);
-                }
-                if (P.styleObjIdWeight > 0.f) {
-                    int imgID = lvl_texel(P.img.ids, px.x, px.y);
-                    int styleID = ex_point_id(P.ex, tx, ty, c.layer);
-                    res = res + ((imgID != styleID) ? P.styleObjIdWeight : 0.0f);
-                }
-            } else {
-                res = fmaf(ssd_a(canvas, to, P.alphaWeight), P.canvasOutputWeight, res);
-            }
-            const float w = P.gauss[i + R] * P.gauss[j + R];
-            sum = valid ? fmaf(res, w, sum) : sum;
-            sumW = valid ? sumW + w : sumW;
+            act = !(sum >= thr2);
         }
     }
-    if (sumW < kEpsilon) return kBigResidual;
-    return sum / sumW;
+    if (P.counters) count_taps(P, taps_done<R>(px, cols), px.temporal);
+    if (px.sumW < kEpsilon) return kBigResidual;
+    if (sum >= thr2) return INFINITY;
+    return sum / px.sumW;
 }
 
 template <int R, int TM>
 __device__ __forceinline__ float energy_tiled(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
-                                           const Cand& c) {
+                                           const Cand& c, float best) {
     float sum0 = 0.0f;
     if (px.hyst_on) sum0 = sum0 - px.hyst;
     float2 b0, b1;
@@ -187,21 +231,22 @@ __device__ __forceinline__ float energy_tiled(const Params& P, const TileSmem<R,
     const unsigned mask = __activemask();
     bool fast = __all_sync(mask, footprint_inside<R>(c.x, c.y, b0, b1, P.ex.w, P.ex.h));
     bool fastp = TM ? __all_sync(mask, !px.temporal || px.prev_fast) : true;
-    return energy_taps<R, TM>(P, T, px, c, b0, b1, sum0, fast, fastp);
+    return energy_taps<R, TM>(P, T, px, c, b0, b1, sum0, fast, fastp, exit_threshold(P, px, best));
 }
 
 // test_offset + isExemplarPixelCulled, texSynth_kernel.cu:200-205,695-721
+// (best: the energy the candidate has to beat; kNoBest computes it in full)
 template <int R, int TM>
 __device__ __forceinline__ float test_offset_tiled(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
-                                                   const Cand& c, float image_alpha) {
+                                                   const Cand& c, float image_alpha, float best) {
     float dte = ex_texel_dt(P.ex, (int)c.x, (int)c.y, c.layer);
     if (!((double)dte > (double)P.distTransCull * 1.25)) {
         if (!P.transparencyOk) {
             float ea = ex_sample_out_alpha(P.ex, c.x, c.y, c.layer);
             if (ea < kAlphaThreshold && image_alpha > kAlphaThreshold) return kBigResidual;
         }
-        if (P.counters) count_eval(P, px.x, px.y, px.temporal);
-        return energy_tiled<R, TM>(P, T, px, c);
+        if (P.counters) count_eval(P, px.x, px.y, px.temporal, false);
+        return energy_tiled<R, TM>(P, T, px, c, best);
     }
     return kBigResidual;
 }
@@ -236,6 +281,18 @@ __device__ __forceinline__ bool stage_tile(const Params& P, TileSmem<R, TM>& T, 
     px->sidx = (threadIdx.y + R) * TW + threadIdx.x + R;
     px->imin = max(-R, -x); px->imax = min(R, P.lw - 1 - x);
     px->jmin = max(-R, -y); px->jmax = min(R, P.lh - 1 - y);
+    {
+        float sw = 0.0f;
+#pragma unroll 1
+        for (int i = -R; i <= R; i++)
+#pragma unroll
+            for (int j = -R; j <= R; j++) {
+                const bool valid = (i >= px->imin) && (i <= px->imax) && (j >= px->jmin) && (j <= px->jmax);
+                const float w = P.gauss[i + R] * P.gauss[j + R];
+                sw = valid ? sw + w : sw;
+            }
+        px->sumW = sw;
+    }
     const size_t k = (size_t)y * P.W + x;
     px->hyst_on = false;
     px->hyst = 0.0f;
@@ -261,25 +318,40 @@ __device__ __forceinline__ bool stage_tile(const Params& P, TileSmem<R, TM>& T, 
 // Up to four candidates of one pixel evaluated in one tap loop: the
 // pixel-side reads and, for temporal passes, the previous-frame exemplar
 // sample of each tap (both independent of the candidate) are done once per
-// tap; every candidate keeps its own sums in the reference's tap order, so
-// each energy is bit-identical to a separate evaluation.
+// tap; every candidate keeps its own sum in the reference's tap order, so
+// each energy is bit-identical to a separate evaluation.  Each candidate
+// stops early against thr2 (see exit_threshold); the loop ends when no
+// candidate of the warp is still active.
 // AF: every footprint of the warp is inside the exemplar; fast and fastp
 // are then true at compile time and no wrap/clamp code is emitted.  The
 // multi-candidate loop runs long enough per call that this second copy pays.
 template <int R, int TM, int NC, bool AF>
 __device__ __forceinline__ void energyN_taps(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
                                              const Cand* c, const float2* b0, const float2* b1, int n,
-                                             bool fast_, bool fastp_, float* sum, float* sumW) {
+                                             bool fast_, bool fastp_, float thr2, float* sum, int* cols) {
     const bool fast = AF || fast_, fastp = AF || fastp_;
     constexpr int TW = TileSmem<R, TM>::TW;
     const size_t lsz = (size_t)P.ex.w * P.ex.h;
     size_t lo[NC];
+    bool act[NC];
 #pragma unroll
-    for (int k = 0; k < NC; k++) lo[k] = (size_t)ex_layer(P.ex, c[k].layer) * lsz;
+    for (int k = 0; k < NC; k++) {
+        lo[k] = (size_t)ex_layer(P.ex, c[k].layer) * lsz;
+        act[k] = (k < n) && !(sum[k] >= thr2);
+        cols[k] = 0;
+    }
     const size_t lp = TM ? (size_t)ex_layer(P.ex, px.prev.layer) * lsz : 0;
     const float hw = (float)P.histW, hh = (float)P.histH;
+    const unsigned mask = __activemask();
 #pragma unroll 1
     for (int i = -R; i <= R; i++) {
+        bool any = false;
+#pragma unroll
+        for (int k = 0; k < NC; k++) {
+            any = any || act[k];
+            cols[k] += act[k] ? 1 : 0;
+        }
+        if (!__any_sync(mask, any)) break;
 #pragma unroll 1
         for (int j = -R; j <= R; j++) {
             const bool valid = (i >= px.imin) && (i <= px.imax) && (j >= px.jmin) && (j <= px.jmax);
@@ -289,19 +361,19 @@ __device__ __forceinline__ void energyN_taps(const Params& P, const TileSmem<R, 
             float4 pbase, pout, peb, peo;
             bool tvalid = false;
             if (TM) {
-                if (px.temporal) {
+                if (px.temporal && any) {
                     pbase = T.pbase[s];
                     pout = T.pout[s];
                     float ptx = px.prev.x + fmaf((float)i, px.pb0.x, (float)j * px.pb1.x);
                     float pty = px.prev.y + fmaf((float)i, px.pb0.y, (float)j * px.pb1.y);
-                    sample2(P.ex.base + lp, P.ex.out + lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo, fastp);
+                    sample2<false>(P.ex.base + lp, P.ex.out + lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo, fastp);
                     tvalid = T.phys[s] > 0;
                 }
             }
             const float w = P.gauss[i + R] * P.gauss[j + R];
 #pragma unroll
             for (int k = 0; k < NC; k++) {
-                if (k < n) {
+                if (act[k]) {
                     float tx = c[k].x + fmaf((float)i, b0[k].x, (float)j * b1[k].x);
                     float ty = c[k].y + fmaf((float)i, b0[k].y, (float)j * b1[k].y);
                     if (!fast) {
@@ -309,7 +381,7 @@ __device__ __forceinline__ void energyN_taps(const Params& P, const TileSmem<R, 
                         if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
                     }
                     float4 tb, to;
-                    sample2(P.ex.base + lo[k], P.ex.out + lo[k], P.ex.w, P.ex.h, tx, ty, &tb, &to, fast);
+                    sample2<false>(P.ex.base + lo[k], P.ex.out + lo[k], P.ex.w, P.ex.h, tx, ty, &tb, &to, fast);
                     float res = ssd_a(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
                     if (TM) {
                         if (px.temporal) {
@@ -344,25 +416,28 @@ __device__ __forceinline__ void energyN_taps(const Params& P, const TileSmem<R, 
                         res = fmaf(ssd_a(canvas, to, P.alphaWeight), P.canvasOutputWeight, res);
                     }
                     sum[k] = valid ? fmaf(res, w, sum[k]) : sum[k];
-                    sumW[k] = valid ? sumW[k] + w : sumW[k];
                 }
             }
         }
+#pragma unroll
+        for (int k = 0; k < NC; k++) act[k] = act[k] && !(sum[k] >= thr2);
     }
 }
 
-// energies of n <= NC candidates (kBigResidual where sumW < eps)
+// energies of n <= NC candidates that have to beat `best` (kBigResidual
+// where the tap weights sum below kEpsilon, +inf where a candidate stopped
+// early)
 template <int R, int TM, int NC>
 __device__ __forceinline__ void energyN(const Params& P, const TileSmem<R, TM>& T, const PixT& px, const Cand* c,
-                                        int n, float* out) {
+                                        int n, float best, float* out) {
     float2 b0[NC], b1[NC];
-    float sum[NC], sumW[NC];
+    float sum[NC];
+    int cols[NC];
     bool f = true;
 #pragma unroll
     for (int k = 0; k < NC; k++) {
         sum[k] = 0.0f;
         if (px.hyst_on) sum[k] = sum[k] - px.hyst;
-        sumW[k] = 0.0f;
         b0[k] = make_float2(0.f, 0.f);
         b1[k] = make_float2(0.f, 0.f);
         if (k < n) {
@@ -373,10 +448,18 @@ __device__ __forceinline__ void energyN(const Params& P, const TileSmem<R, TM>& 
     const unsigned mask = __activemask();
     const bool fast = __all_sync(mask, f);
     const bool fastp = TM ? __all_sync(mask, !px.temporal || px.prev_fast) : true;
-    if (fast && fastp) energyN_taps<R, TM, NC, true>(P, T, px, c, b0, b1, n, true, true, sum, sumW);
-    else energyN_taps<R, TM, NC, false>(P, T, px, c, b0, b1, n, fast, fastp, sum, sumW);
+    const float thr2 = exit_threshold(P, px, best);
+    if (fast && fastp) energyN_taps<R, TM, NC, true>(P, T, px, c, b0, b1, n, true, true, thr2, sum, cols);
+    else energyN_taps<R, TM, NC, false>(P, T, px, c, b0, b1, n, fast, fastp, thr2, sum, cols);
+    if (P.counters) {
+        unsigned taps = 0;
 #pragma unroll
-    for (int k = 0; k < NC; k++) out[k] = (sumW[k] < kEpsilon) ? kBigResidual : sum[k] / sumW[k];
+        for (int k = 0; k < NC; k++) taps += (k < n) ? taps_done<R>(px, cols[k]) : 0u;
+        count_taps(P, taps, px.temporal);
+    }
+#pragma unroll
+    for (int k = 0; k < NC; k++)
+        out[k] = (px.sumW < kEpsilon) ? kBigResidual : (sum[k] >= thr2) ? INFINITY : sum[k] / px.sumW;
 }
 
 // propagate_kernel with the four jump candidates evaluated together
@@ -428,13 +511,13 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate4(const Params P,
             float ea = ex_sample_out_alpha(P.ex, t.x, t.y, t.layer);
             if (ea < kAlphaThreshold && ia > kAlphaThreshold) continue;
         }
-        if (P.counters) count_eval(P, x, y, px.temporal);
+        if (P.counters) count_eval(P, x, y, px.temporal, false);
         ev[n] = Cand{t.x, t.y, t.theta, t.su, t.sv, t.layer};
         slot[cdx] = n;
         n++;
     }
     float e[4];
-    energyN<R, TM, 4>(P, T, px, ev, n, e);
+    energyN<R, TM, 4>(P, T, px, ev, n, best, e);
     int win = -1;
 #pragma unroll
     for (int cdx = 0; cdx < 4; cdx++) {
@@ -542,7 +625,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter(const Params P, Pa
         } else {
             break;
         }
-        float r = test_offset_tiled<R, TM>(P, T, px, c, ia);
+        float r = test_offset_tiled<R, TM>(P, T, px, c, ia, best);
         if (r < best) {
             ow = have ? make_patch(c.x, c.y, c.theta, 0.0f, 0, sc.x, sc.y) : avg;
             best = r;
@@ -562,8 +645,8 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_residual(const Params P, f
     if (image_culled(P, px.x, px.y)) { out[k] = 0.0f; return; }
     Patch t = load_patch(P.off, k);
     Cand c{t.x, t.y, t.theta, t.su, t.sv, t.layer};
-    if (P.counters) count_eval(P, px.x, px.y, px.temporal);
-    out[k] = energy_tiled<R, TM>(P, T, px, c);
+    if (P.counters) count_eval(P, px.x, px.y, px.temporal, false);
+    out[k] = energy_tiled<R, TM>(P, T, px, c, kNoBest);
 }
 
 template <int R>

@@ -99,6 +99,7 @@ struct Params {
     const float4* canvas;
     AdvView adv[2];            // [0] = forward, [1] = backward
     unsigned long long* counters;  // profiling: energy evaluations, taps, temporal taps (null = off)
+    int earlyExit;             // every per-tap term is >= 0 (all weights >= 0): candidates may stop early
 };
 
 struct ConvKernel {
