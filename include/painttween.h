@@ -346,6 +346,13 @@ pt_status pt_set_profiling(pt_ctx* ctx, int on);
  * coherence term, one temporal direction), 0 = the generic kernels
  * everywhere.  Both compute identical results. */
 pt_status pt_set_tiled_kernels(pt_ctx* ctx, int on);
+/* Selects whether the propagate/scatter loops of pt_synthesize_frame and
+ * pt_synthesize_animation track which offsets each pass changed and skip the
+ * evaluations whose inputs are unchanged since an earlier pass with the same
+ * candidates (1, default; tiled kernels only), or evaluate everything (0).
+ * Both compute identical results.  No counterpart in the reference: its
+ * loop (synthesisFrame.cpp:483-508) always evaluates everything. */
+pt_status pt_set_incremental(pt_ctx* ctx, int on);
 /* Statistics of one kernel (waits for the stream). */
 pt_status pt_get_kernel_stats(pt_ctx* ctx, int kernel, pt_kernel_stats* out);
 /* Blocks until the context's stream is idle. */

@@ -64,6 +64,7 @@ SIGNATURES = {
     "pt_timer_elapsed": (_I, [_VP, _I, _I, ctypes.POINTER(ctypes.c_float)]),
     "pt_set_profiling": (_I, [_VP, _I]),
     "pt_set_tiled_kernels": (_I, [_VP, _I]),
+    "pt_set_incremental": (_I, [_VP, _I]),
     "pt_get_kernel_stats": (_I, [_VP, _I, ctypes.POINTER(_abi.KernelStats)]),
 }
 

@@ -251,6 +251,15 @@ static __device__ __forceinline__ unsigned lane_id() {
     asm volatile("mov.u32 %0, %%laneid;" : "=r"(l));
     return l;
 }
+// every byte of the two records equal
+static __device__ __forceinline__ bool same_record(const Patch& a, const Patch& b) {
+    return __float_as_uint(a.x) == __float_as_uint(b.x) && __float_as_uint(a.y) == __float_as_uint(b.y) &&
+           __float_as_uint(a.theta) == __float_as_uint(b.theta) && __float_as_uint(a.hyst) == __float_as_uint(b.hyst) &&
+           a.layer == b.layer && __float_as_uint(a.su) == __float_as_uint(b.su) &&
+           __float_as_uint(a.sv) == __float_as_uint(b.sv) && __float_as_uint(a.lumy) == __float_as_uint(b.lumy) &&
+           __float_as_uint(a.luma) == __float_as_uint(b.luma);
+}
+
 // profiling counters: one evaluation and (with_taps) its taps; the tiled
 // kernels count the taps they actually process after the tap loop
 static __device__ __forceinline__ void count_eval(const Params& P, int x, int y, bool temporal,
@@ -286,10 +295,13 @@ static __device__ float test_offset(const Params& P, int x, int y, const Patch& 
 
 // calculatePropagateOffset, :956-982 (pixelWrap with the level-0 size,
 // cudaImageBuffer.h:81-87)
-static __device__ Patch propagate_offset(const Params& P, int tx, int ty, int x, int y) {
+static __device__ __forceinline__ size_t pixel_wrap_index(const Params& P, int tx, int ty) {
     int wx = (int)((float)tx - (float)P.W * floorf((float)tx / (float)P.W));
     int wy = (int)((float)ty - (float)P.H * floorf((float)ty / (float)P.H));
-    size_t kk = (size_t)wy * P.W + wx;
+    return (size_t)wy * P.W + wx;
+}
+static __device__ Patch propagate_offset(const Params& P, int tx, int ty, int x, int y) {
+    size_t kk = pixel_wrap_index(P, tx, ty);
     float4 a = __ldg(P.off.A + kk);
     float2 sc = lvl_texel(P.img.scale, tx, ty);
     float2 b0, b1;

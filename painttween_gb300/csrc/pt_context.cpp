@@ -16,6 +16,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <climits>
 #include <map>
 #include <memory>
 #include <string>
@@ -127,6 +128,14 @@ struct pt_ctx {
     uint32_t pass_counter = 0;
     bool adv_written[2] = {false, false};  // advected F/B written since the last reset
     bool use_tiled = true;                 // tiled kernels where an instantiation exists
+
+    // change tracking of the driver's propagate/scatter loops
+    bool use_incremental = true;
+    uint8_t* chg = nullptr;
+    int* stamp_last = nullptr;
+    int* stamp_win = nullptr;
+    int inc_seq = 0;        // index of the last tracked pass
+    int inc_on = 0, inc_pi = 0, inc_prev = INT_MIN;
 
     // measurement
     cudaEvent_t timers[PT_TIMER_SLOTS] = {};
@@ -295,6 +304,7 @@ static Params make_params(pt_ctx* c, int level) {
     P.canvas = c->canvas;
     P.adv[0] = c->adv[0];
     P.adv[1] = c->adv[1];
+    P.inc = ptk::IncView{c->chg, c->stamp_last, c->stamp_win, c->inc_on, c->inc_pi, c->inc_prev};
     return P;
 }
 
@@ -684,6 +694,7 @@ pt_status pt_initialize(pt_ctx* c, int iw, int ih, int sw, int sh, int ns) {
     }
     dfree_t(c, c->canvas); dfree_t(c, c->up_orient); dfree_t(c, c->up_scale); dfree_t(c, c->up_ids);
     dfree_t(c, c->rnd);
+    dfree_t(c, c->chg); dfree_t(c, c->stamp_last); dfree_t(c, c->stamp_win);
     free_store(c);
     c->initialized = false;
     c->W = iw; c->H = ih; c->SW = sw; c->SH = sh; c->NS = ns;
@@ -699,6 +710,12 @@ pt_status pt_initialize(pt_ctx* c, int iw, int ih, int sw, int sh, int ns) {
         TRY(dalloc_t(c, &c->adv[i].ts, n));
     }
     TRY(dalloc_t(c, &c->canvas, n));
+    TRY(dalloc_t(c, &c->chg, n));
+    TRY(dalloc_t(c, &c->stamp_last, n));
+    TRY(dalloc_t(c, &c->stamp_win, n));
+    CU(cudaMemsetAsync(c->stamp_last, 0, n * sizeof(int), c->stream));
+    CU(cudaMemsetAsync(c->stamp_win, 0, n * sizeof(int), c->stream));
+    c->inc_seq = 0;
     c->base_i = c->work_i = 0;
     c->res_i = 0;
     memset(&c->img, 0, sizeof(c->img));
@@ -1359,6 +1376,12 @@ pt_status pt_set_tiled_kernels(pt_ctx* c, int on) {
     return PT_OK;
 }
 
+pt_status pt_set_incremental(pt_ctx* c, int on) {
+    if (!c) return PT_ERR_INVALID;
+    c->use_incremental = on != 0;
+    return PT_OK;
+}
+
 pt_status pt_get_kernel_stats(pt_ctx* c, int kernel, pt_kernel_stats* out) {
     if (!c || !out || kernel < 0 || kernel >= PT_KERNEL_COUNT) return PT_ERR_INVALID;
     CU(cudaStreamSynchronize(c->stream));
@@ -1446,12 +1469,41 @@ static pt_status store_load_residual(pt_ctx* c, int level, int frame, int pass) 
 }
 
 // SynthesisFrame::propagateAndScatter, synthesisFrame.cpp:483-508
+//
+// With change tracking (tiled kernels), every pass of the loop is numbered.
+// Within the loop nothing but the offsets changes (the levels' images, the
+// advected buffers and the parameters are fixed, and the offsets histogram
+// is all zero), so a pixel's residual depends only on the offset records in
+// its patch window, and a candidate's outcome only on its source record, the
+// target pixel's window and the target's residual.  A pass with the same
+// candidates as an earlier pass of the loop (the same propagate jump, or the
+// next scatter when its candidates are drawn with the reference's
+// generator) therefore skips every candidate whose inputs are unchanged
+// since then: it was rejected there against the same residual and would be
+// rejected again.  The sync after a pass recomputes only the canvas and
+// residuals whose inputs changed.  Results are bit-identical either way.
 static pt_status propagate_and_scatter(pt_ctx* c, int level, int iterations) {
+    const bool track = c->use_incremental && tiled_usable(c);
+    std::map<int, int> last_pass;  // jump (0 = scatter) -> index of its last pass
+    auto run = [&](int jump) -> pt_status {
+        if (track) {
+            c->inc_on = 1;
+            c->inc_pi = ++c->inc_seq;
+            auto it = last_pass.find(jump);
+            bool same = it != last_pass.end() && (jump != 0 || c->params.rngMode != PT_RNG_COUNTER);
+            c->inc_prev = same ? it->second : INT_MIN;
+            last_pass[jump] = c->inc_pi;
+        }
+        pt_status st = jump ? pt_propagate(c, level, jump, -1) : pt_scatter(c, level, -1);
+        c->inc_on = 0;
+        c->inc_prev = INT_MIN;
+        return st;
+    };
     for (int itr = 0; itr < iterations; itr++) {
-        for (int j = 128; j > 1; j /= 2) TRY(pt_propagate(c, level, j, -1));
-        TRY(pt_propagate(c, level, 1, -1));
-        TRY(pt_propagate(c, level, 1, -1));
-        if (itr < iterations - 1) TRY(pt_scatter(c, level, -1));
+        for (int j = 128; j > 1; j /= 2) TRY(run(j));
+        TRY(run(1));
+        TRY(run(1));
+        if (itr < iterations - 1) TRY(run(0));
     }
     return PT_OK;
 }

@@ -17,6 +17,8 @@
 //    are then no-ops -- are left out.
 #pragma once
 
+#include <climits>
+
 #include "pt_common.cuh"
 #include "pt_internal.h"
 
@@ -136,8 +138,9 @@ __device__ __forceinline__ void count_taps(const Params& P, unsigned taps, bool 
 
 // One body for both cases: the single-candidate kernels (scatter in
 // particular) are instruction-cache bound, and a second, compile-time fast
-// copy of this loop measured slower there.
-template <int R, int TM>
+// copy of this loop measured slower there.  EE: the early-exit test is
+// compiled in (false for the residual, which always needs the full sum).
+template <int R, int TM, bool EE>
 __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
                                              const Cand& c, float2 b0, float2 b1, float sum0, bool fast,
                                              bool fastp, float thr2) {
@@ -150,11 +153,11 @@ __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, 
     const float hw = (float)P.histW, hh = (float)P.histH;
     const unsigned mask = __activemask();
     float sum = sum0;
-    bool act = !(sum >= thr2);
+    bool act = EE ? !(sum >= thr2) : true;
     int cols = 0;
 #pragma unroll 1
     for (int i = -R; i <= R; i++) {
-        if (!__any_sync(mask, act)) break;
+        if (EE && !__any_sync(mask, act)) break;
         cols += act ? 1 : 0;
         if (act) {
 #pragma unroll
@@ -212,16 +215,16 @@ __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, 
                 const float w = P.gauss[i + R] * P.gauss[j + R];
                 sum = valid ? fmaf(res, w, sum) : sum;
             }
-            act = !(sum >= thr2);
+            if (EE) act = !(sum >= thr2);
         }
     }
     if (P.counters) count_taps(P, taps_done<R>(px, cols), px.temporal);
     if (px.sumW < kEpsilon) return kBigResidual;
-    if (sum >= thr2) return INFINITY;
+    if (EE && sum >= thr2) return INFINITY;
     return sum / px.sumW;
 }
 
-template <int R, int TM>
+template <int R, int TM, bool EE>
 __device__ __forceinline__ float energy_tiled(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
                                            const Cand& c, float best) {
     float sum0 = 0.0f;
@@ -231,7 +234,8 @@ __device__ __forceinline__ float energy_tiled(const Params& P, const TileSmem<R,
     const unsigned mask = __activemask();
     bool fast = __all_sync(mask, footprint_inside<R>(c.x, c.y, b0, b1, P.ex.w, P.ex.h));
     bool fastp = TM ? __all_sync(mask, !px.temporal || px.prev_fast) : true;
-    return energy_taps<R, TM>(P, T, px, c, b0, b1, sum0, fast, fastp, exit_threshold(P, px, best));
+    return energy_taps<R, TM, EE>(P, T, px, c, b0, b1, sum0, fast, fastp,
+                                  EE ? exit_threshold(P, px, best) : kNoBest);
 }
 
 // test_offset + isExemplarPixelCulled, texSynth_kernel.cu:200-205,695-721
@@ -246,7 +250,7 @@ __device__ __forceinline__ float test_offset_tiled(const Params& P, const TileSm
             if (ea < kAlphaThreshold && image_alpha > kAlphaThreshold) return kBigResidual;
         }
         if (P.counters) count_eval(P, px.x, px.y, px.temporal, false);
-        return energy_tiled<R, TM>(P, T, px, c, best);
+        return energy_tiled<R, TM, true>(P, T, px, c, best);
     }
     return kBigResidual;
 }
@@ -462,21 +466,66 @@ __device__ __forceinline__ void energyN(const Params& P, const TileSmem<R, TM>& 
         out[k] = (px.sumW < kEpsilon) ? kBigResidual : (sum[k] >= thr2) ? INFINITY : sum[k] / px.sumW;
 }
 
+// the four propagate sources of pixel (x, y), in the reference's order
+__device__ __forceinline__ void propagate_source(int cdx, int x, int y, int jump, int* tx, int* ty) {
+    *tx = x;
+    *ty = y;
+    if (cdx == 0) *tx = x + jump;
+    else if (cdx == 1) *tx = x - jump;
+    else if (cdx == 2) *ty = y + jump;
+    else *ty = y - jump;
+}
+
+// A block whose pixels need no energy (change tracking skipped all their
+// candidates) copies its records and stops before staging its tile.
+// (write: the working buffer needs every record written)
+__device__ __forceinline__ bool block_idle(const Params& P, PatchPlanes work, bool need, bool in, size_t k,
+                                           bool write = true) {
+    if (__syncthreads_or(need)) return false;
+    if (in) {
+        if (write) store_patch(work, k, load_patch(P.off, k));
+        P.inc.chg[k] = 0;
+    }
+    return true;
+}
+
 // propagate_kernel with the four jump candidates evaluated together
 template <int R, int TM>
 __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate4(const Params P, PatchPlanes work, int jump) {
     __shared__ TileSmem<R, TM> T;
+    // Change tracking: a candidate whose source record and whose target's
+    // patch window are unchanged since the previous pass with this jump was
+    // rejected there against the same residual and is skipped (bit cdx of
+    // `skip`); a pass without a previous one skips nothing.
+    unsigned skip = 0;
+    if (P.inc.on) {
+        const int x = blockIdx.x * kTileW + threadIdx.x, y = blockIdx.y * kTileH + threadIdx.y;
+        const bool in = x < P.lw && y < P.lh;
+        const size_t k = (size_t)y * P.W + x;
+        bool need = in;
+        if (in && P.inc.prev != INT_MIN && __ldg(P.inc.win + k) < P.inc.prev) {
+#pragma unroll
+            for (int cdx = 0; cdx < 4; cdx++) {
+                int tx, ty;
+                propagate_source(cdx, x, y, jump, &tx, &ty);
+                if (__ldg(P.inc.last + pixel_wrap_index(P, tx, ty)) < P.inc.prev) skip |= 1u << cdx;
+            }
+            need = skip != 0xFu && !image_culled(P, x, y);
+        }
+        if (block_idle(P, work, need, in, k)) return;
+    }
     PixT px;
     if (!stage_tile<R, TM>(P, T, &px)) return;
     const int x = px.x, y = px.y;
     const size_t k = (size_t)y * P.W + x;
     if (image_culled(P, x, y)) {
-        store_patch(work, k, make_patch(0, 0, 0, 0, 0, 1.f, 1.f));
+        const Patch z = make_patch(0, 0, 0, 0, 0, 1.f, 1.f);
+        if (P.inc.on) P.inc.chg[k] = same_record(z, load_patch(P.off, k)) ? 0 : 1;
+        store_patch(work, k, z);
         return;
     }
     float best = __ldg(P.res + k);
     float ia = T.base[px.sidx].w;
-    Patch ow = load_patch(P.off, k);
     // the four candidates in the reference's order; a candidate that repeats
     // an earlier one, or that test_offset rejects before the energy, keeps
     // its fixed outcome.  Only the keys and the evaluated candidates stay
@@ -489,21 +538,22 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate4(const Params P,
     int n = 0;
 #pragma unroll
     for (int cdx = 0; cdx < 4; cdx++) {
-        int tx = x, ty = y;
-        if (cdx == 0) tx = x + jump;
-        else if (cdx == 1) tx = x - jump;
-        else if (cdx == 2) ty = y + jump;
-        else ty = y - jump;
+        slot[cdx] = -1;
+        kx[cdx] = ky[cdx] = kt[cdx] = 0u;
+        kl[cdx] = 0;
+        if (skip & (1u << cdx)) continue;  // rejected in the previous pass with this jump
+        int tx, ty;
+        propagate_source(cdx, x, y, jump, &tx, &ty);
         Patch t = propagate_offset(P, tx, ty, x, y);
         kx[cdx] = __float_as_uint(t.x);
         ky[cdx] = __float_as_uint(t.y);
         kt[cdx] = __float_as_uint(t.theta);
         kl[cdx] = t.layer;
-        slot[cdx] = -1;
         bool dup = false;
 #pragma unroll
         for (int q = 0; q < cdx; q++)
-            dup |= kx[q] == kx[cdx] && ky[q] == ky[cdx] && kt[q] == kt[cdx] && kl[q] == kl[cdx];
+            dup |= !(skip & (1u << q)) && kx[q] == kx[cdx] && ky[q] == ky[cdx] && kt[q] == kt[cdx] &&
+                   kl[q] == kl[cdx];
         if (dup) { slot[cdx] = -2; continue; }
         float dte = ex_texel_dt(P.ex, (int)t.x, (int)t.y, t.layer);
         if ((double)dte > (double)P.distTransCull * 1.25) continue;
@@ -521,7 +571,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate4(const Params P,
     int win = -1;
 #pragma unroll
     for (int cdx = 0; cdx < 4; cdx++) {
-        if (slot[cdx] < 0) continue;  // repeat (same energy, rejected by "<") or rejected early (1e31)
+        if (slot[cdx] < 0) continue;  // skipped, repeat (same energy, rejected by "<") or rejected early (1e31)
         float r = kBigResidual;
 #pragma unroll
         for (int q = 0; q < 4; q++)
@@ -529,14 +579,15 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate4(const Params P,
         if (r < best) { best = r; win = cdx; }
     }
     if (win >= 0) {
-        int tx = x, ty = y;
-        if (win == 0) tx = x + jump;
-        else if (win == 1) tx = x - jump;
-        else if (win == 2) ty = y + jump;
-        else ty = y - jump;
-        ow = propagate_offset(P, tx, ty, x, y);
+        int tx, ty;
+        propagate_source(win, x, y, jump, &tx, &ty);
+        const Patch ow = propagate_offset(P, tx, ty, x, y);
+        if (P.inc.on) P.inc.chg[k] = same_record(ow, load_patch(P.off, k)) ? 0 : 1;
+        store_patch(work, k, ow);
+    } else {
+        if (P.inc.on) P.inc.chg[k] = 0;
+        store_patch(work, k, load_patch(P.off, k));
     }
-    store_patch(work, k, ow);
 }
 
 // scatter_kernel + averageOffset, texSynth_kernel.cu:841-952
@@ -544,13 +595,26 @@ template <int R, int TM>
 __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter(const Params P, PatchPlanes work, int write_all,
                                                              uint32_t pass_id) {
     __shared__ TileSmem<R, TM> T;
+    // Change tracking: with the reference's generator a pixel's candidates
+    // follow from its own record and its 3x3 neighbours, so a pixel whose
+    // patch window is unchanged since the previous scatter of the loop had
+    // every candidate rejected there against the same residual, and again now.
+    bool stable = false;
+    if (P.inc.on) {
+        const int x = blockIdx.x * kTileW + threadIdx.x, y = blockIdx.y * kTileH + threadIdx.y;
+        const bool in = x < P.lw && y < P.lh;
+        const size_t k = (size_t)y * P.W + x;
+        stable = in && P.inc.prev != INT_MIN && __ldg(P.inc.win + k) < P.inc.prev;
+        if (block_idle(P, work, in && !stable, in, k, write_all != 0)) return;
+    }
     PixT px;
     if (!stage_tile<R, TM>(P, T, &px)) return;
     const int x = px.x, y = px.y;
     const size_t k = (size_t)y * P.W + x;
     Patch off = load_patch(P.off, k);
-    if (image_culled(P, x, y)) {
+    if (stable || image_culled(P, x, y)) {
         if (write_all) store_patch(work, k, off);
+        if (P.inc.on) P.inc.chg[k] = 0;
         return;
     }
     float cached = __ldg(P.res + k);
@@ -631,7 +695,9 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter(const Params P, Pa
             best = r;
         }
     }
-    if (best < cached) store_patch(work, k, ow);
+    const bool take = best < cached;
+    if (P.inc.on) P.inc.chg[k] = (take && !same_record(ow, off)) ? 1 : 0;
+    if (take) store_patch(work, k, ow);
     else if (write_all) store_patch(work, k, off);
 }
 
@@ -639,14 +705,47 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter(const Params P, Pa
 template <int R, int TM>
 __global__ void __launch_bounds__(kTileThreads, 2) kt_residual(const Params P, float* out) {
     __shared__ TileSmem<R, TM> T;
+    // Change tracking: only pixels with a changed record in their patch
+    // window get a new residual; the others keep theirs (the same inputs give
+    // the same value).  The pass stamps are updated here.
+    bool need = true;
+    if (P.inc.on) {
+        constexpr int TW = TileSmem<R, TM>::TW, N = TileSmem<R, TM>::N;
+        __shared__ uint8_t C[N];
+        const int tid = threadIdx.x + threadIdx.y * kTileW;
+        const int x0 = blockIdx.x * kTileW - R, y0 = blockIdx.y * kTileH - R;
+        for (int q = tid; q < N; q += kTileThreads) {
+            int gx = clampi(x0 + q % TW, 0, P.lw - 1);
+            int gy = clampi(y0 + q / TW, 0, P.lh - 1);
+            C[q] = P.inc.chg[(size_t)gy * P.W + gx];
+        }
+        __syncthreads();
+        const int x = blockIdx.x * kTileW + threadIdx.x, y = blockIdx.y * kTileH + threadIdx.y;
+        const bool in = x < P.lw && y < P.lh;
+        need = false;
+        if (in) {
+            const int c0 = threadIdx.y * TW + threadIdx.x;  // window corner
+            unsigned any = 0;
+#pragma unroll
+            for (int j = 0; j <= 2 * R; j++)
+#pragma unroll
+                for (int i = 0; i <= 2 * R; i++) any |= C[c0 + j * TW + i];
+            need = any != 0;
+            const size_t k = (size_t)y * P.W + x;
+            if (C[c0 + R * TW + R]) P.inc.last[k] = P.inc.pi;
+            if (need) P.inc.win[k] = P.inc.pi;
+        }
+        if (!__syncthreads_or(need)) return;
+    }
     PixT px;
     if (!stage_tile<R, TM>(P, T, &px)) return;
+    if (!need) return;
     const size_t k = (size_t)px.y * P.W + px.x;
     if (image_culled(P, px.x, px.y)) { out[k] = 0.0f; return; }
     Patch t = load_patch(P.off, k);
     Cand c{t.x, t.y, t.theta, t.su, t.sv, t.layer};
     if (P.counters) count_eval(P, px.x, px.y, px.temporal, false);
-    out[k] = energy_tiled<R, TM>(P, T, px, c, kNoBest);
+    out[k] = energy_tiled<R, TM, false>(P, T, px, c, kNoBest);
 }
 
 template <int R>

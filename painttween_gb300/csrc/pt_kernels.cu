@@ -147,6 +147,7 @@ __global__ void __launch_bounds__(128) k_residual(const Params P, float* out) {
 // offsetsToOutput, :263-274
 __global__ void k_canvas(const Params P, float4* canvas) {
     PIXEL_XY
+    if (P.inc.on && !P.inc.chg[k]) return;  // tracked pass left this record unchanged
     float4 a = __ldg(P.off.A + k);
     float lumy = __ldg(&P.off.B[k].w), luma = __ldg(P.off.C + k);
     float4 c = ex_sample_out(P.ex, a.x, a.y, __float_as_int(a.w));

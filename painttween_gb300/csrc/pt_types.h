@@ -69,6 +69,21 @@ struct AdvView {
     int* ts;
 };
 
+// Change tracking across the passes of one propagate/scatter loop.  A pass
+// sets chg[k] = 1 where it changed pixel k's offset record (any of its 36
+// bytes); the sync after it stamps last[k] (the last pass that changed k's
+// record) and win[k] (the last pass that changed a record inside k's patch
+// window).  Pass indices grow monotonically over the context's life, so a
+// stamp from an earlier loop reads as "unchanged since before this loop".
+struct IncView {
+    uint8_t* chg;
+    int* last;
+    int* win;
+    int on;    // this pass is tracked (chg written, stamps updated)
+    int pi;    // its index
+    int prev;  // index of the previous pass of this loop with the same candidates, INT_MIN if none
+};
+
 struct Params {
     int W, H;            // level-0 image size == buffer pitch / height
     int level, lw, lh;   // level and its size
@@ -100,6 +115,7 @@ struct Params {
     AdvView adv[2];            // [0] = forward, [1] = backward
     unsigned long long* counters;  // profiling: energy evaluations, taps, temporal taps (null = off)
     int earlyExit;             // every per-tap term is >= 0 (all weights >= 0): candidates may stop early
+    IncView inc;
 };
 
 struct ConvKernel {

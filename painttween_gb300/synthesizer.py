@@ -89,6 +89,9 @@ class TexSynth:
     def set_tiled_kernels(self, on):
         self._check(lib().pt_set_tiled_kernels(self.h, int(on)), "pt_set_tiled_kernels")
 
+    def set_incremental(self, on):
+        self._check(lib().pt_set_incremental(self.h, int(on)), "pt_set_incremental")
+
     def set_profiling(self, on):
         self._check(lib().pt_set_profiling(self.h, int(on)), "pt_set_profiling")
 

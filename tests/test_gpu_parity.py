@@ -390,3 +390,64 @@ def test_convolve_separable_matches_oracle(radius):
     t.synchronize()
     t.close()
     assert_array_equal(dst.cpu().numpy(), ref, "separable Gaussian r=%d" % radius)
+
+
+def _animate(p, ex, clip, W, H, incremental=True, tiled=True):
+    s = Synthesizer(device=0)
+    try:
+        s.setup(p, W, H, ex["w"], ex["h"], 1)
+        s.set_tiled_kernels(tiled)
+        s.set_incremental(incremental)
+        s.set_style(0, ex["base"], ex["output"], ex["orient_tensor"], ex["dist_trans"], ex["object_ids"])
+        for i, fr in enumerate(clip):
+            s.set_frame_dict(i, fr)
+        return s.synthesize_animation(0, len(clip) - 1)
+    finally:
+        s.close()
+
+
+@pytest.mark.parametrize("r", [2, 3, 4])
+def test_change_tracking_identical_and_matches_oracle(r):
+    """The propagate/scatter loop with change tracking (skipped candidates,
+    incremental canvas and residual) gives the same bytes as the loop that
+    evaluates everything, and as the oracle, over an animation with temporal,
+    hysteresis and distance-transform terms in both pass directions."""
+    p = config_params(r=r, levels=3, iterations=3)
+    p.temporalCoherenceWeight = 0.5
+    p.hysteresisWeight = 0.25
+    p.distTransWeight = 0.5
+    ex = synthetic.make_exemplar(64, 64, seed=70 + r)
+    clip = synthetic.make_clip(96, 72, 3, 3, seed=80 + r)
+    on = _animate(p, ex, clip, 96, 72, incremental=True)
+    off = _animate(p, ex, clip, 96, 72, incremental=False)
+    ref = O.OracleDriver(p, [ex], clip, threads=8).render(0, 2)
+    for f in range(3):
+        assert_offsets_equal(on[f][1], off[f][1], 1.0, "tracked vs full frame %d" % f)
+        assert_array_equal(on[f][0], off[f][0], "tracked vs full output frame %d" % f)
+        assert_offsets_equal(on[f][1], ref[f][0], 1.0, "tracked vs oracle frame %d" % f)
+        assert_array_equal(on[f][0], ref[f][2], "tracked vs oracle output frame %d" % f)
+
+
+def test_change_tracking_identical_large_still():
+    """A 640x360 still at patch radius 3: the tracked loop and the full loop
+    agree on every byte of the offsets and the output."""
+    p = config_params(r=3, levels=4, iterations=4)
+    ex = synthetic.make_exemplar(256, 256, seed=5)
+    fr = synthetic.make_still(640, 360, 6, seed=6)
+    on = _animate(p, ex, [fr], 640, 360, incremental=True)
+    off = _animate(p, ex, [fr], 640, 360, incremental=False)
+    assert_offsets_equal(on[0][1], off[0][1], 1.0, "tracked vs full offsets")
+    assert_array_equal(on[0][0], off[0][0], "tracked vs full output")
+
+
+def test_negative_weight_disables_early_exit():
+    """A negative term weight makes partial patch sums non-monotone, so the
+    early exit must stay off; the result still matches the oracle."""
+    p = config_params(r=3, levels=2, iterations=2)
+    p.canvasOutputWeight = -0.25
+    ex = synthetic.make_exemplar(64, 64, seed=90)
+    clip = synthetic.make_clip(80, 64, 3, 2, seed=91)
+    got = _animate(p, ex, clip, 80, 64)
+    ref = O.OracleDriver(p, [ex], clip, threads=8).render(0, 1)
+    for f in range(2):
+        assert_offsets_equal(got[f][1], ref[f][0], 1.0, "negative weight frame %d" % f)
