@@ -213,7 +213,7 @@ def test_still_synthesis_driver_bit_exact():
     try:
         rgba, offs = s.synthesize_frame(0)
         ref = d.render(0, 0)[0]
-        assert_offsets_equal(offs, ref[0], 0.999, "still offsets")
+        assert_offsets_equal(offs, ref[0], 1.0, "still offsets")
         assert np.abs(rgba - ref[2]).max() <= 1e-6
         psnr = 10 * np.log10(1.0 / max(np.mean((rgba - ref[2]) ** 2), 1e-20))
         assert psnr >= 40
@@ -229,7 +229,7 @@ def test_animation_driver_bit_exact():
         got = s.synthesize_animation(0, 3)
         ref = d.render(0, 3)
         for f in range(4):
-            assert_offsets_equal(got[f][1], ref[f][0], 0.999, "frame %d offsets" % f)
+            assert_offsets_equal(got[f][1], ref[f][0], 1.0, "frame %d offsets" % f)
             assert np.abs(got[f][0] - ref[f][2]).max() <= 1e-6
     finally:
         s.close()
@@ -243,7 +243,7 @@ def test_animation_scheme_fmbm_residual_merge():
         got = s.synthesize_animation(0, 2)
         ref = d.render(0, 2)
         for f in range(3):
-            assert_offsets_equal(got[f][1], ref[f][0], 0.999, "FMBM frame %d" % f)
+            assert_offsets_equal(got[f][1], ref[f][0], 1.0, "FMBM frame %d" % f)
     finally:
         s.close()
 
@@ -257,7 +257,7 @@ def test_still_config_256_full_size():
     try:
         rgba, offs = s.synthesize_frame(0)
         ref = d.render(0, 0)[0]
-        assert_offsets_equal(offs, ref[0], 0.999, "still256 offsets")
+        assert_offsets_equal(offs, ref[0], 1.0, "still256 offsets")
         psnr = 10 * np.log10(1.0 / max(np.mean((rgba - ref[2]) ** 2), 1e-20))
         assert psnr >= 40
     finally:
@@ -303,7 +303,7 @@ def test_counter_rng_mode_matches_oracle():
         got = s.synthesize_animation(0, 1)
         ref = d.render(0, 1)
         for f in range(2):
-            assert_offsets_equal(got[f][1], ref[f][0], 0.999, "counter mode frame %d" % f)
+            assert_offsets_equal(got[f][1], ref[f][0], 1.0, "counter mode frame %d" % f)
     finally:
         s.close()
 
@@ -371,7 +371,7 @@ def test_tiled_and_generic_kernels_identical(r):
         assert_array_equal(outs[0][f][0], outs[1][f][0], "tiled vs generic output frame %d" % f)
     ref = O.OracleDriver(p, [ex], clip, threads=8).render(0, 2)
     for f in range(3):
-        assert_offsets_equal(outs[0][f][1], ref[f][0], 0.999, "tiled vs oracle frame %d" % f)
+        assert_offsets_equal(outs[0][f][1], ref[f][0], 1.0, "tiled vs oracle frame %d" % f)
 
 
 @pytest.mark.parametrize("radius", [1, 3, 7])
