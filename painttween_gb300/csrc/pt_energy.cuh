@@ -238,23 +238,6 @@ __device__ __forceinline__ float energy_tiled(const Params& P, const TileSmem<R,
                                   EE ? exit_threshold(P, px, best) : kNoBest);
 }
 
-// test_offset + isExemplarPixelCulled, texSynth_kernel.cu:200-205,695-721
-// (best: the energy the candidate has to beat; kNoBest computes it in full)
-template <int R, int TM>
-__device__ __forceinline__ float test_offset_tiled(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
-                                                   const Cand& c, float image_alpha, float best) {
-    float dte = ex_texel_dt(P.ex, (int)c.x, (int)c.y, c.layer);
-    if (!((double)dte > (double)P.distTransCull * 1.25)) {
-        if (!P.transparencyOk) {
-            float ea = ex_sample_out_alpha(P.ex, c.x, c.y, c.layer);
-            if (ea < kAlphaThreshold && image_alpha > kAlphaThreshold) return kBigResidual;
-        }
-        if (P.counters) count_eval(P, px.x, px.y, px.temporal, false);
-        return energy_tiled<R, TM, true>(P, T, px, c, best);
-    }
-    return kBigResidual;
-}
-
 // Stages the tile (and halo) of the pixel-side inputs and fills the
 // per-pixel state.  Returns false for threads whose pixel is outside the
 // level rectangle.
@@ -319,153 +302,6 @@ __device__ __forceinline__ bool stage_tile(const Params& P, TileSmem<R, TM>& T, 
     return true;
 }
 
-// Up to four candidates of one pixel evaluated in one tap loop: the
-// pixel-side reads and, for temporal passes, the previous-frame exemplar
-// sample of each tap (both independent of the candidate) are done once per
-// tap; every candidate keeps its own sum in the reference's tap order, so
-// each energy is bit-identical to a separate evaluation.  Each candidate
-// stops early against thr2 (see exit_threshold); the loop ends when no
-// candidate of the warp is still active.
-// AF: every footprint of the warp is inside the exemplar; fast and fastp
-// are then true at compile time and no wrap/clamp code is emitted.  The
-// multi-candidate loop runs long enough per call that this second copy pays.
-template <int R, int TM, int NC, bool AF>
-__device__ __forceinline__ void energyN_taps(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
-                                             const Cand* c, const float2* b0, const float2* b1, int n,
-                                             bool fast_, bool fastp_, float thr2, float* sum, int* cols) {
-    const bool fast = AF || fast_, fastp = AF || fastp_;
-    constexpr int TW = TileSmem<R, TM>::TW;
-    const size_t lsz = (size_t)P.ex.w * P.ex.h;
-    size_t lo[NC];
-    bool act[NC];
-#pragma unroll
-    for (int k = 0; k < NC; k++) {
-        lo[k] = (size_t)ex_layer(P.ex, c[k].layer) * lsz;
-        act[k] = (k < n) && !(sum[k] >= thr2);
-        cols[k] = 0;
-    }
-    const size_t lp = TM ? (size_t)ex_layer(P.ex, px.prev.layer) * lsz : 0;
-    const float hw = (float)P.histW, hh = (float)P.histH;
-    const unsigned mask = __activemask();
-#pragma unroll 1
-    for (int i = -R; i <= R; i++) {
-        bool any = false;
-#pragma unroll
-        for (int k = 0; k < NC; k++) {
-            any = any || act[k];
-            cols[k] += act[k] ? 1 : 0;
-        }
-        if (!__any_sync(mask, any)) break;
-#pragma unroll 1
-        for (int j = -R; j <= R; j++) {
-            const bool valid = (i >= px.imin) && (i <= px.imax) && (j >= px.jmin) && (j <= px.jmax);
-            const int s = px.sidx + j * TW + i;
-            const float4 base = T.base[s];
-            const float4 canvas = T.canvas[s];
-            float4 pbase, pout, peb, peo;
-            bool tvalid = false;
-            if (TM) {
-                if (px.temporal && any) {
-                    pbase = T.pbase[s];
-                    pout = T.pout[s];
-                    float ptx = px.prev.x + fmaf((float)i, px.pb0.x, (float)j * px.pb1.x);
-                    float pty = px.prev.y + fmaf((float)i, px.pb0.y, (float)j * px.pb1.y);
-                    sample2<false>(P.ex.base + lp, P.ex.out + lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo, fastp);
-                    tvalid = T.phys[s] > 0;
-                }
-            }
-            const float w = P.gauss[i + R] * P.gauss[j + R];
-#pragma unroll
-            for (int k = 0; k < NC; k++) {
-                if (act[k]) {
-                    float tx = c[k].x + fmaf((float)i, b0[k].x, (float)j * b1[k].x);
-                    float ty = c[k].y + fmaf((float)i, b0[k].y, (float)j * b1[k].y);
-                    if (!fast) {
-                        if (tx >= hw) tx -= hw; else if (tx < 0) tx += hw;
-                        if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
-                    }
-                    float4 tb, to;
-                    sample2<false>(P.ex.base + lo[k], P.ex.out + lo[k], P.ex.w, P.ex.h, tx, ty, &tb, &to, fast);
-                    float res = ssd_a(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
-                    if (TM) {
-                        if (px.temporal) {
-                            float r = ssd(sub4(base, pbase), sub4(tb, peb)) * P.tdIn;
-                            r = fmaf(ssd(sub4(canvas, pout), sub4(to, peo)), P.tdOut, r);
-                            r = fmaf(ssd(pout, to), P.tc, r);
-                            res = tvalid ? res + r : res;
-                        }
-                    }
-                    if (i == 0 && j == 0) {
-                        if (P.distTransWeight > 0.f) {
-                            float de = ex_sample_dt(P.ex, tx, ty, c[k].layer) / c[k].sv;
-                            float di = lay_texel(P.img.dt[P.img.cur], P, px.x, px.y);
-                            float diff = fminf(fmaxf(fabsf(de - di), 0.0f), 10.0f);
-                            res = res + diff * P.distTransWeight;
-                        }
-                        {
-                            int Lh = clampi(c[k].layer, 0, PT_MAX_STYLES - 1);
-                            float sh = (float)(P.histH / P.numStyles);
-                            int hx = clampi((int)tx, 0, P.histPitch - 1);
-                            int hy = clampi((int)(ty + sh * (float)c[k].layer), 0, P.histRows - 1);
-                            float h = __ldg(P.hist + (size_t)hy * P.histPitch + hx);
-                            float thr = P.histThreshold[Lh];
-                            res = res + ((h > thr) ? (h - thr) * P.histSlope[Lh] : 0.0f);
-                        }
-                        if (P.styleObjIdWeight > 0.f) {
-                            int imgID = lvl_texel(P.img.ids, px.x, px.y);
-                            int styleID = ex_point_id(P.ex, tx, ty, c[k].layer);
-                            res = res + ((imgID != styleID) ? P.styleObjIdWeight : 0.0f);
-                        }
-                    } else {
-                        res = fmaf(ssd_a(canvas, to, P.alphaWeight), P.canvasOutputWeight, res);
-                    }
-                    sum[k] = valid ? fmaf(res, w, sum[k]) : sum[k];
-                }
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < NC; k++) act[k] = act[k] && !(sum[k] >= thr2);
-    }
-}
-
-// energies of n <= NC candidates that have to beat `best` (kBigResidual
-// where the tap weights sum below kEpsilon, +inf where a candidate stopped
-// early)
-template <int R, int TM, int NC>
-__device__ __forceinline__ void energyN(const Params& P, const TileSmem<R, TM>& T, const PixT& px, const Cand* c,
-                                        int n, float best, float* out) {
-    float2 b0[NC], b1[NC];
-    float sum[NC];
-    int cols[NC];
-    bool f = true;
-#pragma unroll
-    for (int k = 0; k < NC; k++) {
-        sum[k] = 0.0f;
-        if (px.hyst_on) sum[k] = sum[k] - px.hyst;
-        b0[k] = make_float2(0.f, 0.f);
-        b1[k] = make_float2(0.f, 0.f);
-        if (k < n) {
-            basis(c[k].theta, P.scaleWU * c[k].su, P.scaleWV * c[k].sv, &b0[k], &b1[k]);
-            f = f && footprint_inside<R>(c[k].x, c[k].y, b0[k], b1[k], P.ex.w, P.ex.h);
-        }
-    }
-    const unsigned mask = __activemask();
-    const bool fast = __all_sync(mask, f);
-    const bool fastp = TM ? __all_sync(mask, !px.temporal || px.prev_fast) : true;
-    const float thr2 = exit_threshold(P, px, best);
-    if (fast && fastp) energyN_taps<R, TM, NC, true>(P, T, px, c, b0, b1, n, true, true, thr2, sum, cols);
-    else energyN_taps<R, TM, NC, false>(P, T, px, c, b0, b1, n, fast, fastp, thr2, sum, cols);
-    if (P.counters) {
-        unsigned taps = 0;
-#pragma unroll
-        for (int k = 0; k < NC; k++) taps += (k < n) ? taps_done<R>(px, cols[k]) : 0u;
-        count_taps(P, taps, px.temporal);
-    }
-#pragma unroll
-    for (int k = 0; k < NC; k++)
-        out[k] = (px.sumW < kEpsilon) ? kBigResidual : (sum[k] >= thr2) ? INFINITY : sum[k] / px.sumW;
-}
-
 // the four propagate sources of pixel (x, y), in the reference's order
 __device__ __forceinline__ void propagate_source(int cdx, int x, int y, int jump, int* tx, int* ty) {
     *tx = x;
@@ -487,218 +323,6 @@ __device__ __forceinline__ bool block_idle(const Params& P, PatchPlanes work, bo
         P.inc.chg[k] = 0;
     }
     return true;
-}
-
-// propagate_kernel with the four jump candidates evaluated together
-template <int R, int TM>
-__global__ void __launch_bounds__(kTileThreads, 2) kt_propagate4(const Params P, PatchPlanes work, int jump) {
-    __shared__ TileSmem<R, TM> T;
-    // Change tracking: a candidate whose source record and whose target's
-    // patch window are unchanged since the previous pass with this jump was
-    // rejected there against the same residual and is skipped (bit cdx of
-    // `skip`); a pass without a previous one skips nothing.
-    unsigned skip = 0;
-    if (P.inc.on) {
-        const int x = blockIdx.x * kTileW + threadIdx.x, y = blockIdx.y * kTileH + threadIdx.y;
-        const bool in = x < P.lw && y < P.lh;
-        const size_t k = (size_t)y * P.W + x;
-        bool need = in;
-        if (in && P.inc.prev != INT_MIN && __ldg(P.inc.win + k) < P.inc.prev) {
-#pragma unroll
-            for (int cdx = 0; cdx < 4; cdx++) {
-                int tx, ty;
-                propagate_source(cdx, x, y, jump, &tx, &ty);
-                if (__ldg(P.inc.last + pixel_wrap_index(P, tx, ty)) < P.inc.prev) skip |= 1u << cdx;
-            }
-            need = skip != 0xFu && !image_culled(P, x, y);
-        }
-        if (block_idle(P, work, need, in, k)) return;
-    }
-    PixT px;
-    if (!stage_tile<R, TM>(P, T, &px)) return;
-    const int x = px.x, y = px.y;
-    const size_t k = (size_t)y * P.W + x;
-    if (image_culled(P, x, y)) {
-        const Patch z = make_patch(0, 0, 0, 0, 0, 1.f, 1.f);
-        if (P.inc.on) P.inc.chg[k] = same_record(z, load_patch(P.off, k)) ? 0 : 1;
-        store_patch(work, k, z);
-        return;
-    }
-    float best = __ldg(P.res + k);
-    float ia = T.base[px.sidx].w;
-    // the four candidates in the reference's order; a candidate that repeats
-    // an earlier one, or that test_offset rejects before the energy, keeps
-    // its fixed outcome.  Only the keys and the evaluated candidates stay
-    // live across the tap loop; the winner is rebuilt afterwards (the
-    // construction is deterministic).
-    uint32_t kx[4], ky[4], kt[4];
-    int kl[4];
-    int slot[4];
-    Cand ev[4];
-    int n = 0;
-#pragma unroll
-    for (int cdx = 0; cdx < 4; cdx++) {
-        slot[cdx] = -1;
-        kx[cdx] = ky[cdx] = kt[cdx] = 0u;
-        kl[cdx] = 0;
-        if (skip & (1u << cdx)) continue;  // rejected in the previous pass with this jump
-        int tx, ty;
-        propagate_source(cdx, x, y, jump, &tx, &ty);
-        Patch t = propagate_offset(P, tx, ty, x, y);
-        kx[cdx] = __float_as_uint(t.x);
-        ky[cdx] = __float_as_uint(t.y);
-        kt[cdx] = __float_as_uint(t.theta);
-        kl[cdx] = t.layer;
-        bool dup = false;
-#pragma unroll
-        for (int q = 0; q < cdx; q++)
-            dup |= !(skip & (1u << q)) && kx[q] == kx[cdx] && ky[q] == ky[cdx] && kt[q] == kt[cdx] &&
-                   kl[q] == kl[cdx];
-        if (dup) { slot[cdx] = -2; continue; }
-        float dte = ex_texel_dt(P.ex, (int)t.x, (int)t.y, t.layer);
-        if ((double)dte > (double)P.distTransCull * 1.25) continue;
-        if (!P.transparencyOk) {
-            float ea = ex_sample_out_alpha(P.ex, t.x, t.y, t.layer);
-            if (ea < kAlphaThreshold && ia > kAlphaThreshold) continue;
-        }
-        if (P.counters) count_eval(P, x, y, px.temporal, false);
-        ev[n] = Cand{t.x, t.y, t.theta, t.su, t.sv, t.layer};
-        slot[cdx] = n;
-        n++;
-    }
-    float e[4];
-    energyN<R, TM, 4>(P, T, px, ev, n, best, e);
-    int win = -1;
-#pragma unroll
-    for (int cdx = 0; cdx < 4; cdx++) {
-        if (slot[cdx] < 0) continue;  // skipped, repeat (same energy, rejected by "<") or rejected early (1e31)
-        float r = kBigResidual;
-#pragma unroll
-        for (int q = 0; q < 4; q++)
-            if (slot[cdx] == q) r = e[q];
-        if (r < best) { best = r; win = cdx; }
-    }
-    if (win >= 0) {
-        int tx, ty;
-        propagate_source(win, x, y, jump, &tx, &ty);
-        const Patch ow = propagate_offset(P, tx, ty, x, y);
-        if (P.inc.on) P.inc.chg[k] = same_record(ow, load_patch(P.off, k)) ? 0 : 1;
-        store_patch(work, k, ow);
-    } else {
-        if (P.inc.on) P.inc.chg[k] = 0;
-        store_patch(work, k, load_patch(P.off, k));
-    }
-}
-
-// scatter_kernel + averageOffset, texSynth_kernel.cu:841-952
-template <int R, int TM>
-__global__ void __launch_bounds__(kTileThreads, 2) kt_scatter(const Params P, PatchPlanes work, int write_all,
-                                                             uint32_t pass_id) {
-    __shared__ TileSmem<R, TM> T;
-    // Change tracking: with the reference's generator a pixel's candidates
-    // follow from its own record and its 3x3 neighbours, so a pixel whose
-    // patch window is unchanged since the previous scatter of the loop had
-    // every candidate rejected there against the same residual, and again now.
-    bool stable = false;
-    if (P.inc.on) {
-        const int x = blockIdx.x * kTileW + threadIdx.x, y = blockIdx.y * kTileH + threadIdx.y;
-        const bool in = x < P.lw && y < P.lh;
-        const size_t k = (size_t)y * P.W + x;
-        stable = in && P.inc.prev != INT_MIN && __ldg(P.inc.win + k) < P.inc.prev;
-        if (block_idle(P, work, in && !stable, in, k, write_all != 0)) return;
-    }
-    PixT px;
-    if (!stage_tile<R, TM>(P, T, &px)) return;
-    const int x = px.x, y = px.y;
-    const size_t k = (size_t)y * P.W + x;
-    Patch off = load_patch(P.off, k);
-    if (stable || image_culled(P, x, y)) {
-        if (write_all) store_patch(work, k, off);
-        if (P.inc.on) P.inc.chg[k] = 0;
-        return;
-    }
-    float cached = __ldg(P.res + k);
-    float best = (float)((double)cached + 10e-7);
-    Patch ow = off;
-    float ia = T.base[px.sidx].w;
-    float dist = (float)(P.ex.w > P.ex.h ? P.ex.w : P.ex.h);
-    const float closest = 10.f, factor = 0.9f;
-    float2 sc = lvl_texel(P.img.scale, x, y);
-    // averageOffset of the base field (texSynth_kernel.cu:841-861): it does
-    // not depend on the chain, so it is formed first and tested last
-    Patch avg = make_patch(0, 0, 0, 1.f, 0, 1.f, 1.f);
-    {
-        int n = 0;
-        for (int i = -1; i <= 1; i++)
-            for (int j = -1; j <= 1; j++) {
-                if (!in_rect(P, x + i, y + j) || (i == 0 && j == 0)) continue;
-                float4 nb = __ldg(P.off.A + (size_t)(y + j) * P.W + (x + i));
-                if (__float_as_int(nb.w) != 0) continue;
-                avg.x = avg.x + nb.x;
-                avg.y = avg.y + nb.y;
-                n++;
-            }
-        avg.x = avg.x / (float)n;
-        avg.y = avg.y / (float)n;
-        avg.theta = screen_to_exemplar_angle(P, x, y, avg.x, avg.y, 0);
-    }
-    // Each lane advances along its chain to the next candidate that needs
-    // an energy (an exact repeat of the previous evaluated candidate has the
-    // same energy and is rejected by the strict "<" test, so it is skipped);
-    // after the chain it takes the average offset.  The warp evaluates the
-    // lanes' candidates together through one call site of the energy, so
-    // lanes at different points of their chains still run converged and the
-    // tap loop is emitted once.
-    uint32_t lastx = 0xffffffffu, lasty = 0xffffffffu;
-    int i = 0;
-    bool avg_pending = true;
-#pragma unroll 1
-    while (true) {
-        bool have = false;
-        float ex = 0.f, ey = 0.f;
-#pragma unroll 1
-        while (i < P.scatterSamples && dist * factor >= closest) {
-            float dmin = dist * factor;
-            if (P.rngMode == PT_RNG_COUNTER) {
-                float rr = counter_u01(P.rngSeed, pass_id, x, y, 2 * i);
-                float th = counter_u01(P.rngSeed, pass_id, x, y, 2 * i + 1) * 6.28318530717958647692f;
-                float s, c;
-                sincos_poly(th, &s, &c);
-                float len = fmaf(rr, dist - dmin, dmin);
-                ex = fmaf(c, len, ow.x);
-                ey = fmaf(s, len, ow.y);
-            } else {
-                ex = ow.x + dmin;
-                ey = ow.y + 0.0f;
-            }
-            clamp_to_exemplar(&ex, &ey, P.ex.w, P.ex.h);
-            i++;
-            dist *= factor;
-            if (__float_as_uint(ex) == lastx && __float_as_uint(ey) == lasty) continue;
-            lastx = __float_as_uint(ex);
-            lasty = __float_as_uint(ey);
-            have = true;
-            break;
-        }
-        Cand c;
-        if (have) {
-            c = Cand{ex, ey, screen_to_exemplar_angle(P, x, y, ex, ey, 0), sc.x, sc.y, 0};
-        } else if (avg_pending) {
-            c = Cand{avg.x, avg.y, avg.theta, avg.su, avg.sv, 0};
-            avg_pending = false;
-        } else {
-            break;
-        }
-        float r = test_offset_tiled<R, TM>(P, T, px, c, ia, best);
-        if (r < best) {
-            ow = have ? make_patch(c.x, c.y, c.theta, 0.0f, 0, sc.x, sc.y) : avg;
-            best = r;
-        }
-    }
-    const bool take = best < cached;
-    if (P.inc.on) P.inc.chg[k] = (take && !same_record(ow, off)) ? 1 : 0;
-    if (take) store_patch(work, k, ow);
-    else if (write_all) store_patch(work, k, off);
 }
 
 // updateResidualCache_kernel, texSynth_kernel.cu:661-693
@@ -748,13 +372,568 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_residual(const Params P, f
     out[k] = energy_tiled<R, TM, false>(P, T, px, c, kNoBest);
 }
 
+// ---------------------------------------------------------------------------
+// Lane cursors.  In the kernels below every lane evaluates one candidate at
+// a time, one column of 2R+1 taps per step, and takes its next candidate as
+// soon as the current one is finished or stopped early, instead of waiting
+// for the slowest lane of its warp.  Propagate and residual take their
+// candidates from a queue in shared memory, so any lane may evaluate any
+// pixel of the tile (the pixel-side context is in shared memory too);
+// scatter's lanes each follow their own pixel's chain.  A candidate's sum
+// still runs over its taps in the reference's order, so every energy is
+// bit-identical to a separate evaluation.
+// ---------------------------------------------------------------------------
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// pixel side of an evaluation
+struct LanePix {
+    int x, y, sidx;
+    int imin, imax, jmin, jmax;
+    float sum0, sumW;
+    bool temporal, prev_fast;
+    float prevx, prevy;
+    int prevlayer;  // clamped to the exemplar's layers
+    float2 pb0, pb1;
+};
+
+// candidate side of an evaluation and its cursor
+struct LaneEval {
+    float cx, cy, sv;
+    int layer;
+    float2 b0, b1;
+    bool fast;  // footprint inside the exemplar
+    int col;    // next column, -R..R
+    float sum, thr2;
+};
+
+template <int R>
+__device__ __forceinline__ LanePix lane_pix(const Params& P, const PixT& px) {
+    LanePix q;
+    q.x = px.x; q.y = px.y; q.sidx = px.sidx;
+    q.imin = px.imin; q.imax = px.imax; q.jmin = px.jmin; q.jmax = px.jmax;
+    q.sum0 = px.hyst_on ? 0.0f - px.hyst : 0.0f;
+    q.sumW = px.sumW;
+    q.temporal = px.temporal;
+    q.prev_fast = px.prev_fast;
+    q.prevx = px.prev.x; q.prevy = px.prev.y;
+    q.prevlayer = ex_layer(P.ex, px.prev.layer);
+    q.pb0 = px.pb0; q.pb1 = px.pb1;
+    return q;
+}
+
+// the pixel contexts of a tile in shared memory
+struct PixShared {
+    float4 a[kTileThreads];  // sum0, sumW, prev x, prev y
+    float4 b[kTileThreads];  // prev basis
+    int bits[kTileThreads];  // window bounds + R (4 bits each), temporal, prev_fast, prev layer
+};
+
+template <int R>
+__device__ __forceinline__ void put_pix(PixShared& S, int pid, const LanePix& q) {
+    S.a[pid] = make_float4(q.sum0, q.sumW, q.prevx, q.prevy);
+    S.b[pid] = make_float4(q.pb0.x, q.pb0.y, q.pb1.x, q.pb1.y);
+    S.bits[pid] = (q.imin + R) | ((q.imax + R) << 4) | ((q.jmin + R) << 8) | ((q.jmax + R) << 12) |
+                  (q.temporal ? 1 << 16 : 0) | (q.prev_fast ? 1 << 17 : 0) | (q.prevlayer << 18);
+}
+
+template <int R, int TM>
+__device__ __forceinline__ LanePix get_pix(const Params& P, const PixShared& S, int pid) {
+    constexpr int TW = TileSmem<R, TM>::TW;
+    LanePix q;
+    const int lx = pid % kTileW, ly = pid / kTileW;
+    q.x = blockIdx.x * kTileW + lx;
+    q.y = blockIdx.y * kTileH + ly;
+    q.sidx = (ly + R) * TW + lx + R;
+    const float4 a = S.a[pid], b = S.b[pid];
+    const int bits = S.bits[pid];
+    q.imin = (bits & 15) - R; q.imax = ((bits >> 4) & 15) - R;
+    q.jmin = ((bits >> 8) & 15) - R; q.jmax = ((bits >> 12) & 15) - R;
+    q.temporal = (bits >> 16) & 1;
+    q.prev_fast = (bits >> 17) & 1;
+    q.prevlayer = bits >> 18;
+    q.sum0 = a.x; q.sumW = a.y; q.prevx = a.z; q.prevy = a.w;
+    q.pb0 = make_float2(b.x, b.y); q.pb1 = make_float2(b.z, b.w);
+    return q;
+}
+
+// best = the energy to beat (kNoBest: none, the energy is computed in full)
+template <int R>
+__device__ __forceinline__ void lane_start(const Params& P, const LanePix& q, float cx, float cy, float theta,
+                                           float su, float sv, int layer, float best, LaneEval* e) {
+    e->cx = cx; e->cy = cy; e->sv = sv; e->layer = layer;
+    basis(theta, P.scaleWU * su, P.scaleWV * sv, &e->b0, &e->b1);
+    e->fast = footprint_inside<R>(cx, cy, e->b0, e->b1, P.ex.w, P.ex.h);
+    e->col = -R;
+    e->sum = q.sum0;
+    e->thr2 = (P.earlyExit && q.sumW >= kEpsilon) ? __fmul_ru(best, q.sumW) : kNoBest;
+}
+
+// the taps of column e.col added to e.sum (calculateResidual's tap body,
+// texSynth_kernel.cu:537-659); fast / fastp are warp-uniform.  ROLL keeps
+// the column's taps in a loop (a smaller body: faster for scatter, whose
+// chain code competes for the instruction cache; propagate unrolls).
+template <int R, int TM, bool ROLL>
+__device__ __forceinline__ float lane_column(const Params& P, const TileSmem<R, TM>& T, const LanePix& q,
+                                             const LaneEval& e, bool fast, bool fastp) {
+    constexpr int TW = TileSmem<R, TM>::TW;
+    const int i = e.col;
+    const size_t lsz = (size_t)P.ex.w * P.ex.h;
+    const size_t lo = (size_t)ex_layer(P.ex, e.layer) * lsz;
+    const float4* LB = P.ex.base + lo;
+    const float4* LO = P.ex.out + lo;
+    const size_t lp = TM ? (size_t)q.prevlayer * lsz : 0;
+    const float hw = (float)P.histW, hh = (float)P.histH;
+    const bool cvalid = (i >= q.imin) && (i <= q.imax);
+    const float gi = P.gauss[i + R];
+    float sum = e.sum;
+#pragma unroll(ROLL ? 1 : 2 * R + 1)
+    for (int j = -R; j <= R; j++) {
+        const bool valid = cvalid && (j >= q.jmin) && (j <= q.jmax);
+        const int s = q.sidx + j * TW + i;
+        const float4 base = T.base[s];
+        const float4 canvas = T.canvas[s];
+        float tx = e.cx + fmaf((float)i, e.b0.x, (float)j * e.b1.x);
+        float ty = e.cy + fmaf((float)i, e.b0.y, (float)j * e.b1.y);
+        if (!fast) {
+            if (tx >= hw) tx -= hw; else if (tx < 0) tx += hw;
+            if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
+        }
+        float4 tb, to;
+        sample2<true>(LB, LO, P.ex.w, P.ex.h, tx, ty, &tb, &to, fast);
+        float res = ssd_ap(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
+        if (TM) {
+            if (q.temporal) {
+                const float4 pbase = T.pbase[s], pout = T.pout[s];
+                float ptx = q.prevx + fmaf((float)i, q.pb0.x, (float)j * q.pb1.x);
+                float pty = q.prevy + fmaf((float)i, q.pb0.y, (float)j * q.pb1.y);
+                float4 peb, peo;
+                sample2<true>(P.ex.base + lp, P.ex.out + lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo, fastp);
+                float r = ssdp(sub4p(base, pbase), sub4p(tb, peb)) * P.tdIn;
+                r = fmaf(ssdp(sub4p(canvas, pout), sub4p(to, peo)), P.tdOut, r);
+                r = fmaf(ssdp(pout, to), P.tc, r);
+                res = (T.phys[s] > 0) ? res + r : res;
+            }
+        }
+        if (j == 0 && i == 0) {
+            if (P.distTransWeight > 0.f) {
+                float de = ex_sample_dt(P.ex, tx, ty, e.layer) / e.sv;
+                float di = lay_texel(P.img.dt[P.img.cur], P, q.x, q.y);
+                float diff = fminf(fmaxf(fabsf(de - di), 0.0f), 10.0f);
+                res = res + diff * P.distTransWeight;
+            }
+            {
+                int Lh = clampi(e.layer, 0, PT_MAX_STYLES - 1);
+                float sh = (float)(P.histH / P.numStyles);
+                int hx = clampi((int)tx, 0, P.histPitch - 1);
+                int hy = clampi((int)(ty + sh * (float)e.layer), 0, P.histRows - 1);
+                float h = __ldg(P.hist + (size_t)hy * P.histPitch + hx);
+                float thr = P.histThreshold[Lh];
+                res = res + ((h > thr) ? (h - thr) * P.histSlope[Lh] : 0.0f);
+            }
+            if (P.styleObjIdWeight > 0.f) {
+                int imgID = lvl_texel(P.img.ids, q.x, q.y);
+                int styleID = ex_point_id(P.ex, tx, ty, e.layer);
+                res = res + ((imgID != styleID) ? P.styleObjIdWeight : 0.0f);
+            }
+        } else {
+            res = fmaf(ssd_ap(canvas, to, P.alphaWeight), P.canvasOutputWeight, res);
+        }
+        const float w = gi * P.gauss[j + R];
+        sum = valid ? fmaf(res, w, sum) : sum;
+    }
+    return sum;
+}
+
+// taps of the first `cols` columns inside the level rectangle
+template <int R>
+__device__ __forceinline__ unsigned lane_taps(const LanePix& q, int cols) {
+    const int last = min(-R + cols - 1, q.imax);
+    return last < q.imin ? 0u : (unsigned)((last - q.imin + 1) * (q.jmax - q.jmin + 1));
+}
+
+// One step of a lane: a column of its candidate; returns true when the
+// candidate is finished, with its energy in *r (kBigResidual where the tap
+// weights sum below kEpsilon, +inf where it stopped early).
+template <int R, int TM, bool EE, bool ROLL>
+__device__ __forceinline__ bool lane_step(const Params& P, const TileSmem<R, TM>& T, const LanePix& q, LaneEval& e,
+                                          bool fast, bool fastp, float* r) {
+    e.sum = lane_column<R, TM, ROLL>(P, T, q, e, fast, fastp);
+    e.col++;
+    const bool stop = EE && e.sum >= e.thr2;
+    if (!stop && e.col <= R) return false;
+    if (P.counters) count_taps(P, lane_taps<R>(q, e.col + R), q.temporal);
+    *r = (q.sumW < kEpsilon) ? kBigResidual : stop ? INFINITY : e.sum / q.sumW;
+    return true;
+}
+
+// a lane's index in a shared queue: warp-aggregated atomic on *next
+__device__ __forceinline__ int queue_take(bool want, int* next) {
+    const unsigned m = __ballot_sync(kFull, want);
+    const int lane = (int)lane_id();
+    const int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(next, __popc(m));
+    base = __shfl_sync(kFull, base, leader);
+    return base + __popc(m & ((1u << lane) - 1u));
+}
+
+// candidates of a propagate tile
+struct PropQueue {
+    float4 ca[kTileThreads * 4];     // x, y, theta, su; x holds the energy once evaluated
+    float2 cb[kTileThreads * 4];     // sv, layer bits
+    uint16_t list[kTileThreads * 4];  // pid * 4 + slot
+    float thr[kTileThreads];          // the pixel's residual
+    int slots[kTileThreads];          // per candidate (3 bits each): slot + 3, or 0 skipped, 1 repeat, 2 rejected
+    int count, next;
+};
+
+// propagate_kernel with lane cursors over the tile's candidates
+template <int R, int TM>
+__global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P, PatchPlanes work, int jump) {
+    __shared__ TileSmem<R, TM> T;
+    __shared__ PixShared S;
+    __shared__ PropQueue Q;
+    // Change tracking: a candidate whose source record and whose target's
+    // patch window are unchanged since the previous pass with this jump was
+    // rejected there against the same residual and is skipped (bit cdx of
+    // `skip`); a pass without a previous one skips nothing.
+    unsigned skip = 0;
+    if (P.inc.on) {
+        const int x = blockIdx.x * kTileW + threadIdx.x, y = blockIdx.y * kTileH + threadIdx.y;
+        const bool in = x < P.lw && y < P.lh;
+        const size_t k = (size_t)y * P.W + x;
+        bool need = in;
+        if (in && P.inc.prev != INT_MIN && __ldg(P.inc.win + k) < P.inc.prev) {
+#pragma unroll
+            for (int cdx = 0; cdx < 4; cdx++) {
+                int tx, ty;
+                propagate_source(cdx, x, y, jump, &tx, &ty);
+                if (__ldg(P.inc.last + pixel_wrap_index(P, tx, ty)) < P.inc.prev) skip |= 1u << cdx;
+            }
+            need = skip != 0xFu && !image_culled(P, x, y);
+        }
+        if (block_idle(P, work, need, in, k)) return;
+    }
+    const int pid = threadIdx.x + threadIdx.y * kTileW;
+    if (pid == 0) { Q.count = 0; Q.next = 0; }
+    PixT px;
+    const bool in = stage_tile<R, TM>(P, T, &px);  // (synchronises the block)
+    // phase 1: each pixel builds its candidates (the reference's order,
+    // repeats and test_offset rejections resolved here) and queues them
+    int n = 0;
+    bool culled = false;
+    if (in) {
+        const int x = px.x, y = px.y;
+        const size_t k = (size_t)y * P.W + x;
+        culled = image_culled(P, x, y);
+        if (culled) {
+            const Patch z = make_patch(0, 0, 0, 0, 0, 1.f, 1.f);
+            if (P.inc.on) P.inc.chg[k] = same_record(z, load_patch(P.off, k)) ? 0 : 1;
+            store_patch(work, k, z);
+        } else {
+            const float ia = T.base[px.sidx].w;
+            uint32_t kx[4], ky[4], kt[4];
+            int kl[4];
+            int codes = 0;
+#pragma unroll
+            for (int cdx = 0; cdx < 4; cdx++) {
+                kx[cdx] = ky[cdx] = kt[cdx] = 0u;
+                kl[cdx] = 0;
+                int code = 2;  // rejected before the energy
+                if (skip & (1u << cdx)) {
+                    code = 0;
+                } else {
+                    int tx, ty;
+                    propagate_source(cdx, x, y, jump, &tx, &ty);
+                    Patch t = propagate_offset(P, tx, ty, x, y);
+                    kx[cdx] = __float_as_uint(t.x);
+                    ky[cdx] = __float_as_uint(t.y);
+                    kt[cdx] = __float_as_uint(t.theta);
+                    kl[cdx] = t.layer;
+                    bool dup = false;
+#pragma unroll
+                    for (int q = 0; q < cdx; q++)
+                        dup |= !(skip & (1u << q)) && kx[q] == kx[cdx] && ky[q] == ky[cdx] && kt[q] == kt[cdx] &&
+                               kl[q] == kl[cdx];
+                    if (dup) {
+                        code = 1;
+                    } else {
+                        float dte = ex_texel_dt(P.ex, (int)t.x, (int)t.y, t.layer);
+                        bool ok = !((double)dte > (double)P.distTransCull * 1.25);
+                        if (ok && !P.transparencyOk) {
+                            float ea = ex_sample_out_alpha(P.ex, t.x, t.y, t.layer);
+                            ok = !(ea < kAlphaThreshold && ia > kAlphaThreshold);
+                        }
+                        if (ok) {
+                            if (P.counters) count_eval(P, x, y, px.temporal, false);
+                            Q.ca[pid * 4 + n] = make_float4(t.x, t.y, t.theta, t.su);
+                            Q.cb[pid * 4 + n] = make_float2(t.sv, __int_as_float(t.layer));
+                            code = n + 3;
+                            n++;
+                        }
+                    }
+                }
+                codes |= code << (3 * cdx);
+            }
+            Q.slots[pid] = codes;
+            Q.thr[pid] = __ldg(P.res + k);
+            put_pix<R>(S, pid, lane_pix<R>(P, px));
+        }
+    }
+    {
+        // queue this pixel's n candidates
+        const unsigned lane = lane_id();
+        int incl = n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(kFull, incl, o);
+            if ((int)lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(kFull, incl, 31);
+        int base = 0;
+        if (lane == 31 && total > 0) base = atomicAdd(&Q.count, total);
+        base = __shfl_sync(kFull, base, 31);
+        for (int j = 0; j < n; j++) Q.list[base + incl - n + j] = (uint16_t)(pid * 4 + j);
+    }
+    __syncthreads();
+    // phase 2: lane cursors over the queue
+    {
+        LanePix q;
+        LaneEval e;
+        bool act = false, more = true;
+        int cur = 0;
+        const int count = Q.count;
+#pragma unroll 1
+        while (true) {
+            const bool want = !act && more;
+            if (__any_sync(kFull, want)) {
+                const int t = queue_take(want, &Q.next);
+                if (want) {
+                    if (t < count) {
+                        cur = Q.list[t];
+                        const int op = cur >> 2;
+                        q = get_pix<R, TM>(P, S, op);
+                        const float4 a = Q.ca[cur];
+                        const float2 b = Q.cb[cur];
+                        lane_start<R>(P, q, a.x, a.y, a.z, a.w, b.x, __float_as_int(b.y), Q.thr[op], &e);
+                        act = true;
+                    } else {
+                        more = false;
+                    }
+                }
+            }
+            if (!__any_sync(kFull, act)) break;
+            const bool fast = __all_sync(kFull, !act || e.fast);
+            const bool fastp = TM ? __all_sync(kFull, !act || !q.temporal || q.prev_fast) : true;
+            if (act) {
+                float r;
+                if (lane_step<R, TM, true, false>(P, T, q, e, fast, fastp, &r)) {
+                    Q.ca[cur].x = r;
+                    act = false;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    // phase 3: each pixel takes the first candidate, in the reference's
+    // order, that beats its running best
+    if (in && !culled) {
+        const int x = px.x, y = px.y;
+        const size_t k = (size_t)y * P.W + x;
+        const int codes = Q.slots[pid];
+        float best = Q.thr[pid];
+        int win = -1;
+#pragma unroll
+        for (int cdx = 0; cdx < 4; cdx++) {
+            const int code = (codes >> (3 * cdx)) & 7;
+            // a skipped candidate or a repeat is rejected by "<"; one that
+            // test_offset rejected before the energy competes with 1e31
+            if (code < 2) continue;
+            const float r = code == 2 ? kBigResidual : Q.ca[pid * 4 + code - 3].x;
+            if (r < best) { best = r; win = cdx; }
+        }
+        if (win >= 0) {
+            int tx, ty;
+            propagate_source(win, x, y, jump, &tx, &ty);
+            const Patch ow = propagate_offset(P, tx, ty, x, y);
+            if (P.inc.on) P.inc.chg[k] = same_record(ow, load_patch(P.off, k)) ? 0 : 1;
+            store_patch(work, k, ow);
+        } else {
+            if (P.inc.on) P.inc.chg[k] = 0;
+            store_patch(work, k, load_patch(P.off, k));
+        }
+    }
+}
+
+// scatter_kernel + averageOffset, texSynth_kernel.cu:841-952, each lane
+// running its own pixel's chain with a lane cursor
+template <int R, int TM>
+__global__ void __launch_bounds__(kTileThreads, 2) kt_scatter_q(const Params P, PatchPlanes work, int write_all,
+                                                               uint32_t pass_id) {
+    __shared__ TileSmem<R, TM> T;
+    // Change tracking: with the reference's generator a pixel's candidates
+    // follow from its own record and its 3x3 neighbours, so a pixel whose
+    // patch window is unchanged since the previous scatter of the loop had
+    // every candidate rejected there against the same residual, and again now.
+    bool stable = false;
+    if (P.inc.on) {
+        const int x = blockIdx.x * kTileW + threadIdx.x, y = blockIdx.y * kTileH + threadIdx.y;
+        const bool in = x < P.lw && y < P.lh;
+        const size_t k = (size_t)y * P.W + x;
+        stable = in && P.inc.prev != INT_MIN && __ldg(P.inc.win + k) < P.inc.prev;
+        if (block_idle(P, work, in && !stable, in, k, write_all != 0)) return;
+    }
+    PixT px;
+    const bool in = stage_tile<R, TM>(P, T, &px);  // (synchronises the block)
+    const int x = px.x, y = px.y;
+    const size_t k = (size_t)y * P.W + x;
+    bool own = false;
+    if (in) {
+        if (stable || image_culled(P, x, y)) {
+            if (write_all) store_patch(work, k, load_patch(P.off, k));
+            if (P.inc.on) P.inc.chg[k] = 0;
+        } else {
+            own = true;
+        }
+    }
+    // chain state (the reference's loop, :896-937)
+    const float cached = own ? __ldg(P.res + k) : 0.0f;
+    float best = (float)((double)cached + 10e-7);
+    float owx = 0.f, owy = 0.f, owt = 0.f;  // running best offset
+    int wkind = 0;                           // 0: the pixel's own, 1: a chain candidate, 2: the average
+    float ia = 0.f, dist = 0.f;
+    float2 sc = make_float2(0.f, 0.f);
+    float avgx = 0.f, avgy = 0.f, avgt = 0.f;
+    LanePix q;
+    if (own) {
+        const float4 a = __ldg(P.off.A + k);
+        owx = a.x; owy = a.y;
+        ia = T.base[px.sidx].w;
+        dist = (float)(P.ex.w > P.ex.h ? P.ex.w : P.ex.h);
+        sc = lvl_texel(P.img.scale, x, y);
+        // averageOffset of the base field (:841-861)
+        int na = 0;
+        for (int i = -1; i <= 1; i++)
+            for (int j = -1; j <= 1; j++) {
+                if (!in_rect(P, x + i, y + j) || (i == 0 && j == 0)) continue;
+                float4 nb = __ldg(P.off.A + (size_t)(y + j) * P.W + (x + i));
+                if (__float_as_int(nb.w) != 0) continue;
+                avgx = avgx + nb.x;
+                avgy = avgy + nb.y;
+                na++;
+            }
+        avgx = avgx / (float)na;
+        avgy = avgy / (float)na;
+        avgt = screen_to_exemplar_angle(P, x, y, avgx, avgy, 0);
+        q = lane_pix<R>(P, px);
+    }
+    const float closest = 10.f, factor = 0.9f;
+    uint32_t lastx = 0xffffffffu, lasty = 0xffffffffu;
+    int i = 0;
+    bool avg_pending = true;
+    LaneEval e;
+    bool act = false, more = own;
+    bool cur_avg = false;
+    float cur_t = 0.f;
+#pragma unroll 1
+    while (true) {
+        if (!act && more) {
+            // the next candidate that needs an energy; one that test_offset
+            // rejects first competes with 1e31 right here
+#pragma unroll 1
+            while (true) {
+                bool have = false;
+                float ex = 0.f, ey = 0.f;
+#pragma unroll 1
+                while (i < P.scatterSamples && dist * factor >= closest) {
+                    float dmin = dist * factor;
+                    if (P.rngMode == PT_RNG_COUNTER) {
+                        float rr = counter_u01(P.rngSeed, pass_id, x, y, 2 * i);
+                        float th = counter_u01(P.rngSeed, pass_id, x, y, 2 * i + 1) * 6.28318530717958647692f;
+                        float sn, cs;
+                        sincos_poly(th, &sn, &cs);
+                        float len = fmaf(rr, dist - dmin, dmin);
+                        ex = fmaf(cs, len, owx);
+                        ey = fmaf(sn, len, owy);
+                    } else {
+                        ex = owx + dmin;
+                        ey = owy + 0.0f;
+                    }
+                    clamp_to_exemplar(&ex, &ey, P.ex.w, P.ex.h);
+                    i++;
+                    dist *= factor;
+                    // an exact repeat of the previous candidate has its energy
+                    // and is rejected by the strict "<"
+                    if (__float_as_uint(ex) == lastx && __float_as_uint(ey) == lasty) continue;
+                    lastx = __float_as_uint(ex);
+                    lasty = __float_as_uint(ey);
+                    have = true;
+                    break;
+                }
+                float cx, cy, ct, csu, csv;
+                if (have) {
+                    cx = ex; cy = ey; ct = screen_to_exemplar_angle(P, x, y, ex, ey, 0);
+                    csu = sc.x; csv = sc.y;
+                } else if (avg_pending) {
+                    cx = avgx; cy = avgy; ct = avgt; csu = 1.f; csv = 1.f;
+                    avg_pending = false;
+                } else {
+                    more = false;
+                    break;
+                }
+                bool ok = !((double)ex_texel_dt(P.ex, (int)cx, (int)cy, 0) > (double)P.distTransCull * 1.25);
+                if (ok && !P.transparencyOk) {
+                    float ea = ex_sample_out_alpha(P.ex, cx, cy, 0);
+                    ok = !(ea < kAlphaThreshold && ia > kAlphaThreshold);
+                }
+                if (!ok) {
+                    if (kBigResidual < best) {
+                        best = kBigResidual;
+                        owx = cx; owy = cy; owt = ct; wkind = have ? 1 : 2;
+                    }
+                    continue;
+                }
+                if (P.counters) count_eval(P, x, y, px.temporal, false);
+                lane_start<R>(P, q, cx, cy, ct, csu, csv, 0, best, &e);
+                cur_avg = !have;
+                cur_t = ct;
+                act = true;
+                break;
+            }
+        }
+        if (!__any_sync(kFull, act)) break;
+        const bool fast = __all_sync(kFull, !act || e.fast);
+        const bool fastp = TM ? __all_sync(kFull, !act || !q.temporal || q.prev_fast) : true;
+        if (act) {
+            float r;
+            if (lane_step<R, TM, true, true>(P, T, q, e, fast, fastp, &r)) {
+                if (r < best) {
+                    best = r;
+                    owx = e.cx; owy = e.cy; owt = cur_t; wkind = cur_avg ? 2 : 1;
+                }
+                act = false;
+            }
+        }
+    }
+    if (!own) return;
+    const Patch off = load_patch(P.off, k);
+    Patch ow = off;
+    if (wkind == 1) ow = make_patch(owx, owy, owt, 0.0f, 0, sc.x, sc.y);
+    else if (wkind == 2) ow = make_patch(owx, owy, owt, 1.f, 0, 1.f, 1.f);
+    const bool take = best < cached;
+    if (P.inc.on) P.inc.chg[k] = (take && !same_record(ow, off)) ? 1 : 0;
+    if (take) store_patch(work, k, ow);
+    else if (write_all) store_patch(work, k, off);
+}
+
 template <int R>
 cudaError_t launch_tiled_r(int kind, int tm, const Params& P, PatchPlanes work, int arg, uint32_t pass_id, float* out,
                            cudaStream_t s) {
     dim3 b(kTileW, kTileH), g((P.lw + kTileW - 1) / kTileW, (P.lh + kTileH - 1) / kTileH);
 #define PT_TILED_DISPATCH(TMV)                                                                   \
-    if (kind == 0) kt_propagate4<R, TMV><<<g, b, 0, s>>>(P, work, arg);                         \
-    else if (kind == 1) kt_scatter<R, TMV><<<g, b, 0, s>>>(P, work, arg, pass_id);              \
+    if (kind == 0) kt_propagate_q<R, TMV><<<g, b, 0, s>>>(P, work, arg);                        \
+    else if (kind == 1) kt_scatter_q<R, TMV><<<g, b, 0, s>>>(P, work, arg, pass_id);            \
     else kt_residual<R, TMV><<<g, b, 0, s>>>(P, out);
     if (tm == TM_NONE) { PT_TILED_DISPATCH(TM_NONE) }
     else if (tm == TM_FWD) { PT_TILED_DISPATCH(TM_FWD) }
