@@ -272,7 +272,7 @@ def run_reference(args, dist):
 # ---------------------------------------------------------------------------
 
 def run_ours(args, dist):
-    from painttween_gb300 import Synthesizer
+    from painttween_gb300 import Synthesizer, host_array
     from painttween_gb300 import build as B
     B.build()
     cfg = synthetic.config(WORKLOAD)
@@ -293,11 +293,20 @@ def run_ours(args, dist):
     for _ in range(args.warmup):
         render()
     s.synchronize()
+    # Evaluation and tap counts: one untimed step with the device-side
+    # counters (atomics inside the kernels).  The synthesis is deterministic,
+    # so every step repeats these counts exactly.
+    s.set_profiling(_abi.PROFILE_COUNTERS)
+    render()
+    counts = {k: s.kernel_stats(k) for k in range(4)}
+    s.set_profiling(0)
     dist.barrier()
 
+    # timed steps: an event pair around every launch gives the kernels'
+    # durations; no counters run here
     clocks = Clocks(device)
     clocks.start()
-    s.set_profiling(True)
+    s.set_profiling(_abi.PROFILE_TIMING)
     l0 = s.kernel_launches
     times = []
     for _ in range(args.steps):
@@ -307,27 +316,42 @@ def run_ours(args, dist):
         times.append(s.timer_elapsed(0, 1))
     launches = s.kernel_launches - l0
     stats = {k: s.kernel_stats(k) for k in range(4)}
-    s.set_profiling(False)
+    for k in stats:
+        for f in ("energy_evals", "taps", "temporal_taps"):
+            stats[k][f] = counts[k][f] * args.steps
+    s.set_profiling(0)
     ck = clocks.stop()
     total_ms = dist.max(sum(times))
     dist.barrier()
 
-    # end to end through the C ABI with host buffers
+    # end to end through the C ABI with host buffers: every step uploads the
+    # clip's inputs from page-locked host memory (pt_set_frame builds the
+    # pyramids on the device), synthesises, and reads every frame's output
+    # and offsets back into page-locked host memory (pt_get_frame_result)
     e2e_times = []
-    h2d = sum(fr[k].nbytes for fr in clip for k in ("rgba", "orient_tensor", "dist_trans", "object_ids",
-                                                       "vel_fwd", "vel_bwd", "scale"))
+    keys = ("rgba", "orient_tensor", "dist_trans", "object_ids", "vel_fwd", "vel_bwd", "scale")
+    pinned = []
+    for fr in clip:
+        d = {}
+        for key in keys:
+            d[key] = host_array(fr[key].shape, fr[key].dtype)
+            d[key][...] = fr[key]
+        pinned.append(d)
+    h2d = sum(d[key].nbytes for d in pinned for key in keys)
     h, w = cfg["h"] >> p.finalLevel, cfg["w"] >> p.finalLevel
-    d2h = frames * h * w * (16 + 36)
+    outs = [(host_array((h, w, 4), np.float32), host_array((h, w), _abi.PATCH_DTYPE)) for _ in range(frames)]
+    d2h = sum(a.nbytes + o.nbytes for a, o in outs)
     for _ in range(args.e2e_steps):
         s.synchronize()
         t0 = time.perf_counter()
         s.timer_record(2)
-        for i, fr in enumerate(clip):
-            s.set_frame_dict(i, fr)
-        out = s.synthesize_animation(0, frames - 1)
+        for i, d in enumerate(pinned):
+            s.set_frame_dict(i, d)
+        render()
+        for f, (a, o) in enumerate(outs):
+            s.get_frame_result(f, a, o)
         s.timer_record(3)
         e2e_times.append(max(s.timer_elapsed(2, 3), 1000.0 * (time.perf_counter() - t0)))
-        assert len(out) == frames
     e2e_ms = dist.max(float(np.mean(e2e_times)) * args.steps) if e2e_times else None
 
     # roofline of the dominant kernel (propagate)

@@ -317,6 +317,20 @@ typedef void (*pt_frame_callback)(int frame, const float* rgba,
 pt_status pt_synthesize_animation(pt_ctx* ctx, int first, int last,
                                   pt_frame_callback cb, void* user);
 
+/* The final output (level finalLevel) of one frame of the last
+ * pt_synthesize_frame / pt_synthesize_animation, copied into the caller's
+ * buffers; either pointer may be NULL.  No counterpart in the reference
+ * (its frames end up in EXR files): a caller that passes NULL as the
+ * animation callback fetches frames with this call, straight into its own
+ * (ideally page-locked) memory. */
+pt_status pt_get_frame_result(pt_ctx* ctx, int frame, float* out_rgba, pt_patchxf* out_offsets);
+
+/* Page-locked host memory (cudaMallocHost / cudaFreeHost) for frame inputs
+ * and results: copies from and to it run at the full host link speed.  No
+ * counterpart in the reference. */
+pt_status pt_host_alloc(size_t bytes, void** out);
+pt_status pt_host_free(void* p);
+
 /* Number of this library's kernel launches issued so far by the context. */
 uint64_t pt_kernel_launches(const pt_ctx* ctx);
 
@@ -338,9 +352,14 @@ typedef struct {
     uint64_t taps;            /* taps summed over those evaluations */
     uint64_t temporal_taps;   /* taps of evaluations with temporal terms */
 } pt_kernel_stats;
-/* Switches per-launch event timing and patch-distance counting on or off
- * (and clears the statistics). */
-pt_status pt_set_profiling(pt_ctx* ctx, int on);
+/* Profiling of the patch-distance and canvas launches (clears the
+ * statistics): flags = 0 (off) or a combination of PT_PROFILE_TIMING (a
+ * CUDA event pair around every launch, read back as total_ms / launches)
+ * and PT_PROFILE_COUNTERS (device-side counts of evaluations and taps, which
+ * cost atomics inside the kernels). */
+#define PT_PROFILE_TIMING 1
+#define PT_PROFILE_COUNTERS 2
+pt_status pt_set_profiling(pt_ctx* ctx, int flags);
 /* Selects the kernels of the patch-distance passes: 1 (default) = the tiled
  * shared-memory kernels where an instantiation exists (patch radius 2-4, no
  * coherence term, one temporal direction), 0 = the generic kernels

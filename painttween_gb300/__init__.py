@@ -5,6 +5,6 @@ the C ABI of include/painttween.h.
 """
 from . import _abi
 from ._abi import PATCH_DTYPE, Params, default_params
-from .synthesizer import PaintTweenError, Synthesizer, TexSynth
+from .synthesizer import PaintTweenError, Synthesizer, TexSynth, host_array
 
-__all__ = ["PATCH_DTYPE", "Params", "default_params", "PaintTweenError", "Synthesizer", "TexSynth", "_abi"]
+__all__ = ["PATCH_DTYPE", "Params", "default_params", "PaintTweenError", "Synthesizer", "TexSynth", "_abi", "host_array"]

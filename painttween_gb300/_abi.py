@@ -157,6 +157,7 @@ assert PATCH_DTYPE.itemsize == 36
 
 
 KERNEL_PROPAGATE, KERNEL_SCATTER, KERNEL_RESIDUAL, KERNEL_CANVAS = 0, 1, 2, 3
+PROFILE_TIMING, PROFILE_COUNTERS = 1, 2  # pt_set_profiling flags
 
 
 class KernelStats(ctypes.Structure):

@@ -92,6 +92,7 @@ struct pt_ctx {
     int res_i = 0;
     float4* canvas = nullptr;
     float* hist[2] = {nullptr, nullptr};  // [0] base, [1] working
+    bool hist_zero = false;                // both histogram buffers hold zeros
     AdvView adv[2]{};
 
     // storage behind the step-wise uploads
@@ -126,6 +127,8 @@ struct pt_ctx {
 
     uint64_t launches = 0;
     uint32_t pass_counter = 0;
+    void* cb_stage = nullptr;  // page-locked staging of the animation callback
+    size_t cb_stage_bytes = 0;
     bool adv_written[2] = {false, false};  // advected F/B written since the last reset
     bool use_tiled = true;                 // tiled kernels where an instantiation exists
 
@@ -139,7 +142,7 @@ struct pt_ctx {
 
     // measurement
     cudaEvent_t timers[PT_TIMER_SLOTS] = {};
-    bool profiling = false;
+    int profiling = 0;  // PT_PROFILE_* flags
     unsigned long long* counters = nullptr;  // [kernel][evals, taps, temporal taps]
     std::vector<cudaEvent_t> ev_pool;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pairs[PT_KERNEL_COUNT];
@@ -384,11 +387,11 @@ static cudaEvent_t pool_event(pt_ctx* c) {
 
 template <class F>
 static pt_status profiled(pt_ctx* c, int kernel, Params& P, F&& launch) {
-    if (!c->profiling) {
+    if (c->profiling & PT_PROFILE_COUNTERS) P.counters = c->counters + 3 * kernel;
+    if (!(c->profiling & PT_PROFILE_TIMING)) {
         LN(launch(P));
         return PT_OK;
     }
-    P.counters = c->counters + 3 * kernel;
     cudaEvent_t a = pool_event(c), b = pool_event(c);
     if (!a || !b) return fail(c, PT_ERR_CUDA, "cudaEventCreate failed");
     CU(cudaEventRecord(a, c->stream));
@@ -447,15 +450,18 @@ static pt_status do_residual(pt_ctx* c, int level) {
 // TexSynth::syncBuffers, texSynth_kernel.cu:1240-1303
 static pt_status do_sync(pt_ctx* c, int level, int flags) {
     if (!(flags & PT_DONT_COPY_OFFSETS)) c->base_i = c->work_i;
-    if (histogram_on(c)) {
+    // calculateOffsetsHistogram adds nothing (its atomicAdd is commented out
+    // at :258), so the histogram is zeroed and its blur (rows base ->
+    // working, columns working -> base) of zeros is zeros again: once both
+    // buffers hold zeros there is nothing left to recompute.
+    if (histogram_on(c) && !c->hist_zero) {
         size_t hn = (size_t)c->SW * c->SH * c->NS * sizeof(float);
         CU(cudaMemsetAsync(c->hist[0], 0, hn, c->stream));
         CU(cudaMemsetAsync(c->hist[1], 0, hn, c->stream));
-        // calculateOffsetsHistogram adds nothing (its atomicAdd is commented
-        // out at :258); rows base -> working, columns working -> base.
         int hw = c->SW >> level, hh = (c->SH * c->NS) >> level;
         LN(pt::launch_conv(c->hist[0], c->hist[1], hw, hh, c->SW, 1, c->hist_kernel, c->stream));
         LN(pt::launch_conv(c->hist[1], c->hist[0], hw, hh, c->SW, 0, c->hist_kernel, c->stream));
+        c->hist_zero = true;
     }
     Params P = make_params(c, level);
     TRY(profiled(c, PT_KERNEL_CANVAS, P, [&](const Params& Q) { return pt::launch_canvas(Q, c->canvas, c->stream); }));
@@ -620,6 +626,7 @@ pt_status pt_destroy(pt_ctx* c) {
         for (auto& pr : v) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
     for (auto& kv : c->allocs) cudaFree(kv.first);
     c->allocs.clear();
+    if (c->cb_stage) cudaFreeHost(c->cb_stage);
     cudaStreamDestroy(c->stream);
     delete c;
     return PT_OK;
@@ -703,6 +710,7 @@ pt_status pt_initialize(pt_ctx* c, int iw, int ih, int sw, int sh, int ns) {
         TRY(alloc_planes(c, &c->off[i], n));
         TRY(dalloc_t(c, &c->res[i], n));
         TRY(dalloc_t(c, &c->hist[i], (size_t)sw * sh * ns));
+        c->hist_zero = false;
         TRY(alloc_planes(c, &c->adv[i].off, n));
         TRY(dalloc_t(c, &c->adv[i].base, n));
         TRY(dalloc_t(c, &c->adv[i].out, n));
@@ -734,6 +742,7 @@ static pt_status reset_working(pt_ctx* c) {
         CU(cudaMemsetAsync(c->res[i], 0, n * sizeof(float), c->stream));
         CU(cudaMemsetAsync(c->hist[i], 0, (size_t)c->SW * c->SH * c->NS * sizeof(float), c->stream));
     }
+    c->hist_zero = true;
     CU(cudaMemsetAsync(c->canvas, 0, n * sizeof(float4), c->stream));
     c->base_i = c->work_i = 0;
     c->res_i = 0;
@@ -1360,13 +1369,13 @@ static void clear_profile(pt_ctx* c) {
     }
 }
 
-pt_status pt_set_profiling(pt_ctx* c, int on) {
-    if (!c) return PT_ERR_INVALID;
+pt_status pt_set_profiling(pt_ctx* c, int flags) {
+    if (!c || (flags & ~(PT_PROFILE_TIMING | PT_PROFILE_COUNTERS))) return PT_ERR_INVALID;
     CU(cudaStreamSynchronize(c->stream));
     clear_profile(c);
     if (!c->counters) TRY(dalloc_t(c, &c->counters, 3 * PT_KERNEL_COUNT));
     CU(cudaMemsetAsync(c->counters, 0, 3 * PT_KERNEL_COUNT * sizeof(unsigned long long), c->stream));
-    c->profiling = on != 0;
+    c->profiling = flags;
     return PT_OK;
 }
 
@@ -1635,13 +1644,46 @@ pt_status pt_synthesize_animation(pt_ctx* c, int first, int last, pt_frame_callb
     CU(cudaSetDevice(c->device));
     TRY(render_fmbm(c, first, last));
     if (cb) {
+        // each frame is handed to the callback from page-locked staging
         int lw = c->W >> c->params.finalLevel, lh = c->H >> c->params.finalLevel;
-        std::vector<float> rgba((size_t)lw * lh * 4);
-        std::vector<pt_patchxf> offs((size_t)lw * lh);
+        size_t n = (size_t)lw * lh;
+        size_t need = n * (sizeof(float4) + sizeof(pt_patchxf));
+        if (c->cb_stage_bytes < need) {
+            if (c->cb_stage) cudaFreeHost(c->cb_stage);
+            c->cb_stage = nullptr;
+            c->cb_stage_bytes = 0;
+            CU(cudaMallocHost(&c->cb_stage, need));
+            c->cb_stage_bytes = need;
+        }
+        float* rgba = (float*)c->cb_stage;
+        pt_patchxf* offs = (pt_patchxf*)((char*)c->cb_stage + n * sizeof(float4));
         for (int f = first; f <= last; f++) {
-            TRY(fetch_final(c, f, rgba.data(), offs.data()));
-            cb(f, rgba.data(), offs.data(), lw, lh, user);
+            TRY(fetch_final(c, f, rgba, offs));
+            cb(f, rgba, offs, lw, lh, user);
         }
     }
+    return PT_OK;
+}
+
+pt_status pt_get_frame_result(pt_ctx* c, int frame, float* out_rgba, pt_patchxf* out_offsets) {
+    if (!c) return PT_ERR_INVALID;
+    if (!c->initialized || !c->have_params) return fail(c, PT_ERR_STATE, "context not initialized");
+    CU(cudaSetDevice(c->device));
+    return fetch_final(c, frame, out_rgba, out_offsets);
+}
+
+pt_status pt_host_alloc(size_t bytes, void** out) {
+    if (!out) return PT_ERR_INVALID;
+    *out = nullptr;
+    if (bytes == 0) return PT_OK;
+    if (cudaMallocHost(out, bytes) != cudaSuccess) {
+        *out = nullptr;
+        return PT_ERR_CUDA;
+    }
+    return PT_OK;
+}
+
+pt_status pt_host_free(void* p) {
+    if (p && cudaFreeHost(p) != cudaSuccess) return PT_ERR_CUDA;
     return PT_OK;
 }

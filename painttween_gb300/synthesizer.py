@@ -31,6 +31,33 @@ def _c(a, dtype):
     return None if a is None else np.ascontiguousarray(a, dtype=dtype)
 
 
+class _HostBlock:
+    """A block of page-locked host memory (pt_host_alloc), freed with its last user."""
+
+    def __init__(self, nbytes):
+        p = ctypes.c_void_p()
+        st = lib().pt_host_alloc(nbytes, ctypes.byref(p))
+        if st != _abi.PT_OK:
+            raise PaintTweenError(st, "pt_host_alloc(%d) failed" % nbytes)
+        self.p = p
+
+    def __del__(self):
+        if getattr(self, "p", None):
+            lib().pt_host_free(self.p)
+            self.p = None
+
+
+def host_array(shape, dtype=np.float32):
+    """A numpy array in page-locked host memory: frame inputs and results in
+    such memory move between host and GPU at the full link speed."""
+    dtype = np.dtype(dtype)
+    n = max(int(np.prod(shape)) * dtype.itemsize, 1)
+    blk = _HostBlock(n)
+    raw = (ctypes.c_uint8 * n).from_address(blk.p.value)
+    raw._block = blk  # the array's base keeps the block alive
+    return np.frombuffer(raw, dtype=np.uint8, count=int(np.prod(shape)) * dtype.itemsize).view(dtype).reshape(shape)
+
+
 class TexSynth:
     """One synthesis context on one GPU (pt_create)."""
 
@@ -92,8 +119,11 @@ class TexSynth:
     def set_incremental(self, on):
         self._check(lib().pt_set_incremental(self.h, int(on)), "pt_set_incremental")
 
-    def set_profiling(self, on):
-        self._check(lib().pt_set_profiling(self.h, int(on)), "pt_set_profiling")
+    def set_profiling(self, flags):
+        """flags: 0, or _abi.PROFILE_TIMING | _abi.PROFILE_COUNTERS (True = both)."""
+        if flags is True:
+            flags = _abi.PROFILE_TIMING | _abi.PROFILE_COUNTERS
+        self._check(lib().pt_set_profiling(self.h, int(flags)), "pt_set_profiling")
 
     def kernel_stats(self, kernel):
         st = _abi.KernelStats()
@@ -251,11 +281,24 @@ class Synthesizer(TexSynth):
 
         def cb(frame, rgba, offs, w, h, user):
             a = np.ctypeslib.as_array(rgba, shape=(h, w, 4)).copy()
-            o = np.frombuffer(ctypes.string_at(offs, w * h * _abi.PATCH_DTYPE.itemsize),
-                              dtype=_abi.PATCH_DTYPE).reshape(h, w).copy()
-            results[frame] = (a, o)
+            nb = w * h * _abi.PATCH_DTYPE.itemsize
+            o = np.ctypeslib.as_array(ctypes.cast(offs, ctypes.POINTER(ctypes.c_uint8)), shape=(nb,))
+            results[frame] = (a, o.view(_abi.PATCH_DTYPE).reshape(h, w).copy())
 
         cfn = FRAME_CB(cb)
         self._check(lib().pt_synthesize_animation(self.h, first, last, ctypes.cast(cfn, ctypes.c_void_p), None),
                     "pt_synthesize_animation")
         return results
+
+    def get_frame_result(self, frame, rgba=None, offsets=None):
+        """Final output and offsets of one synthesised frame, written into the
+        given arrays (e.g. host_array ones) or new ones."""
+        h, w = self._final_shape()
+        if rgba is None:
+            rgba = np.empty((h, w, 4), np.float32)
+        if offsets is None:
+            offsets = np.empty((h, w), _abi.PATCH_DTYPE)
+        assert rgba.shape == (h, w, 4) and rgba.dtype == np.float32 and rgba.flags.c_contiguous
+        assert offsets.shape == (h, w) and offsets.dtype == _abi.PATCH_DTYPE and offsets.flags.c_contiguous
+        self._check(lib().pt_get_frame_result(self.h, frame, _p(rgba), _p(offsets)), "pt_get_frame_result")
+        return rgba, offsets

@@ -451,3 +451,34 @@ def test_negative_weight_disables_early_exit():
     ref = O.OracleDriver(p, [ex], clip, threads=8).render(0, 1)
     for f in range(2):
         assert_offsets_equal(got[f][1], ref[f][0], 1.0, "negative weight frame %d" % f)
+
+
+def test_frame_results_into_page_locked_memory():
+    """pt_get_frame_result into page-locked arrays (pt_host_alloc) returns
+    the same bytes as the animation callback; inputs may live in page-locked
+    memory too."""
+    from painttween_gb300 import host_array
+    p = config_params(r=3, levels=2, iterations=2)
+    ex = synthetic.make_exemplar(64, 64, seed=95)
+    clip = synthetic.make_clip(80, 64, 3, 2, seed=96)
+    ref = _animate(p, ex, clip, 80, 64)
+    s = Synthesizer(device=0)
+    try:
+        s.setup(p, 80, 64, 64, 64, 1)
+        s.set_style(0, ex["base"], ex["output"], ex["orient_tensor"], ex["dist_trans"], ex["object_ids"])
+        for i, fr in enumerate(clip):
+            pinned = {}
+            for key in ("rgba", "orient_tensor", "dist_trans", "object_ids", "vel_fwd", "vel_bwd", "scale"):
+                pinned[key] = host_array(fr[key].shape, fr[key].dtype)
+                pinned[key][...] = fr[key]
+            s.set_frame_dict(i, pinned)
+        lib = __import__("painttween_gb300._lib", fromlist=["lib"]).lib()
+        s._check(lib.pt_synthesize_animation(s.h, 0, 1, None, None), "pt_synthesize_animation")
+        for f in range(2):
+            a = host_array((64, 80, 4), np.float32)
+            o = host_array((64, 80), _abi.PATCH_DTYPE)
+            s.get_frame_result(f, a, o)
+            assert_offsets_equal(o, ref[f][1], 1.0, "pinned offsets frame %d" % f)
+            assert_array_equal(a, ref[f][0], "pinned output frame %d" % f)
+    finally:
+        s.close()
