@@ -139,6 +139,9 @@ struct pt_ctx {
     int* stamp_win = nullptr;
     int inc_seq = 0;        // index of the last tracked pass
     int inc_on = 0, inc_pi = 0, inc_prev = INT_MIN;
+    int inc_fill = 0;       // the next residual computes and stores every tap value
+    float* tap_cache = nullptr;  // per-tap residual values, (2r+1)^2 planes
+    int tap_cache_k = 0;         // planes allocated
 
     // measurement
     cudaEvent_t timers[PT_TIMER_SLOTS] = {};
@@ -307,7 +310,8 @@ static Params make_params(pt_ctx* c, int level) {
     P.canvas = c->canvas;
     P.adv[0] = c->adv[0];
     P.adv[1] = c->adv[1];
-    P.inc = ptk::IncView{c->chg, c->stamp_last, c->stamp_win, c->inc_on, c->inc_pi, c->inc_prev};
+    P.inc = ptk::IncView{c->chg, c->stamp_last, c->stamp_win, c->inc_on, c->inc_pi, c->inc_prev,
+                         c->tap_cache, c->inc_fill};
     return P;
 }
 
@@ -702,6 +706,8 @@ pt_status pt_initialize(pt_ctx* c, int iw, int ih, int sw, int sh, int ns) {
     dfree_t(c, c->canvas); dfree_t(c, c->up_orient); dfree_t(c, c->up_scale); dfree_t(c, c->up_ids);
     dfree_t(c, c->rnd);
     dfree_t(c, c->chg); dfree_t(c, c->stamp_last); dfree_t(c, c->stamp_win);
+    dfree_t(c, c->tap_cache);
+    c->tap_cache_k = 0;
     free_store(c);
     c->initialized = false;
     c->W = iw; c->H = ih; c->SW = sw; c->SH = sh; c->NS = ns;
@@ -1493,6 +1499,20 @@ static pt_status store_load_residual(pt_ctx* c, int level, int frame, int pass) 
 // residuals whose inputs changed.  Results are bit-identical either way.
 static pt_status propagate_and_scatter(pt_ctx* c, int level, int iterations) {
     const bool track = c->use_incremental && tiled_usable(c);
+    if (track) {
+        // the per-tap values of every residual, recomputed in full once
+        const int r = c->params.residualWindowSize, K = (2 * r + 1) * (2 * r + 1);
+        if (c->tap_cache_k < K) {
+            dfree_t(c, c->tap_cache);
+            c->tap_cache_k = 0;
+            TRY(dalloc_t(c, &c->tap_cache, (size_t)K * c->W * c->H));
+            c->tap_cache_k = K;
+        }
+        c->inc_fill = 1;
+        pt_status st = do_residual(c, level);
+        c->inc_fill = 0;
+        TRY(st);
+    }
     std::map<int, int> last_pass;  // jump (0 = scatter) -> index of its last pass
     auto run = [&](int jump) -> pt_status {
         if (track) {

@@ -469,76 +469,85 @@ __device__ __forceinline__ void lane_start(const Params& P, const LanePix& q, fl
     e->thr2 = (P.earlyExit && q.sumW >= kEpsilon) ? __fmul_ru(best, q.sumW) : kNoBest;
 }
 
-// the taps of column e.col added to e.sum (calculateResidual's tap body,
-// texSynth_kernel.cu:537-659); fast / fastp are warp-uniform.  ROLL keeps
-// the column's taps in a loop (a smaller body: faster for scatter, whose
-// chain code competes for the instruction cache; propagate unrolls).
-template <int R, int TM, bool ROLL>
-__device__ __forceinline__ float lane_column(const Params& P, const TileSmem<R, TM>& T, const LanePix& q,
-                                             const LaneEval& e, bool fast, bool fastp) {
+// calculateResidual's value at tap (i, j) of candidate e at pixel q, before
+// its Gaussian weight (texSynth_kernel.cu:537-659); fast / fastp are
+// warp-uniform
+template <int R, int TM>
+__device__ __forceinline__ float tap_value(const Params& P, const TileSmem<R, TM>& T, const LanePix& q,
+                                           const LaneEval& e, int i, int j, bool fast, bool fastp) {
     constexpr int TW = TileSmem<R, TM>::TW;
-    const int i = e.col;
     const size_t lsz = (size_t)P.ex.w * P.ex.h;
     const size_t lo = (size_t)ex_layer(P.ex, e.layer) * lsz;
     const float4* LB = P.ex.base + lo;
     const float4* LO = P.ex.out + lo;
     const size_t lp = TM ? (size_t)q.prevlayer * lsz : 0;
     const float hw = (float)P.histW, hh = (float)P.histH;
+    const int s = q.sidx + j * TW + i;
+    const float4 base = T.base[s];
+    const float4 canvas = T.canvas[s];
+    float tx = e.cx + fmaf((float)i, e.b0.x, (float)j * e.b1.x);
+    float ty = e.cy + fmaf((float)i, e.b0.y, (float)j * e.b1.y);
+    if (!fast) {
+        if (tx >= hw) tx -= hw; else if (tx < 0) tx += hw;
+        if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
+    }
+    float4 tb, to;
+    sample2<true>(LB, LO, P.ex.w, P.ex.h, tx, ty, &tb, &to, fast);
+    float res = ssd_ap(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
+    if (TM) {
+        if (q.temporal) {
+            const float4 pbase = T.pbase[s], pout = T.pout[s];
+            float ptx = q.prevx + fmaf((float)i, q.pb0.x, (float)j * q.pb1.x);
+            float pty = q.prevy + fmaf((float)i, q.pb0.y, (float)j * q.pb1.y);
+            float4 peb, peo;
+            sample2<true>(P.ex.base + lp, P.ex.out + lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo, fastp);
+            float r = ssdp(sub4p(base, pbase), sub4p(tb, peb)) * P.tdIn;
+            r = fmaf(ssdp(sub4p(canvas, pout), sub4p(to, peo)), P.tdOut, r);
+            r = fmaf(ssdp(pout, to), P.tc, r);
+            res = (T.phys[s] > 0) ? res + r : res;
+        }
+    }
+    if (j == 0 && i == 0) {
+        if (P.distTransWeight > 0.f) {
+            float de = ex_sample_dt(P.ex, tx, ty, e.layer) / e.sv;
+            float di = lay_texel(P.img.dt[P.img.cur], P, q.x, q.y);
+            float diff = fminf(fmaxf(fabsf(de - di), 0.0f), 10.0f);
+            res = res + diff * P.distTransWeight;
+        }
+        {
+            int Lh = clampi(e.layer, 0, PT_MAX_STYLES - 1);
+            float sh = (float)(P.histH / P.numStyles);
+            int hx = clampi((int)tx, 0, P.histPitch - 1);
+            int hy = clampi((int)(ty + sh * (float)e.layer), 0, P.histRows - 1);
+            float h = __ldg(P.hist + (size_t)hy * P.histPitch + hx);
+            float thr = P.histThreshold[Lh];
+            res = res + ((h > thr) ? (h - thr) * P.histSlope[Lh] : 0.0f);
+        }
+        if (P.styleObjIdWeight > 0.f) {
+            int imgID = lvl_texel(P.img.ids, q.x, q.y);
+            int styleID = ex_point_id(P.ex, tx, ty, e.layer);
+            res = res + ((imgID != styleID) ? P.styleObjIdWeight : 0.0f);
+        }
+    } else {
+        res = fmaf(ssd_ap(canvas, to, P.alphaWeight), P.canvasOutputWeight, res);
+    }
+    return res;
+}
+
+// the taps of column e.col added to e.sum in the reference's order.  ROLL
+// keeps the column's taps in a loop (a smaller body: faster for scatter,
+// whose chain code competes for the instruction cache; propagate unrolls).
+template <int R, int TM, bool ROLL>
+__device__ __forceinline__ float lane_column(const Params& P, const TileSmem<R, TM>& T, const LanePix& q,
+                                             const LaneEval& e, bool fast, bool fastp) {
+    const int i = e.col;
     const bool cvalid = (i >= q.imin) && (i <= q.imax);
     const float gi = P.gauss[i + R];
     float sum = e.sum;
 #pragma unroll(ROLL ? 1 : 2 * R + 1)
     for (int j = -R; j <= R; j++) {
         const bool valid = cvalid && (j >= q.jmin) && (j <= q.jmax);
-        const int s = q.sidx + j * TW + i;
-        const float4 base = T.base[s];
-        const float4 canvas = T.canvas[s];
-        float tx = e.cx + fmaf((float)i, e.b0.x, (float)j * e.b1.x);
-        float ty = e.cy + fmaf((float)i, e.b0.y, (float)j * e.b1.y);
-        if (!fast) {
-            if (tx >= hw) tx -= hw; else if (tx < 0) tx += hw;
-            if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
-        }
-        float4 tb, to;
-        sample2<true>(LB, LO, P.ex.w, P.ex.h, tx, ty, &tb, &to, fast);
-        float res = ssd_ap(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
-        if (TM) {
-            if (q.temporal) {
-                const float4 pbase = T.pbase[s], pout = T.pout[s];
-                float ptx = q.prevx + fmaf((float)i, q.pb0.x, (float)j * q.pb1.x);
-                float pty = q.prevy + fmaf((float)i, q.pb0.y, (float)j * q.pb1.y);
-                float4 peb, peo;
-                sample2<true>(P.ex.base + lp, P.ex.out + lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo, fastp);
-                float r = ssdp(sub4p(base, pbase), sub4p(tb, peb)) * P.tdIn;
-                r = fmaf(ssdp(sub4p(canvas, pout), sub4p(to, peo)), P.tdOut, r);
-                r = fmaf(ssdp(pout, to), P.tc, r);
-                res = (T.phys[s] > 0) ? res + r : res;
-            }
-        }
-        if (j == 0 && i == 0) {
-            if (P.distTransWeight > 0.f) {
-                float de = ex_sample_dt(P.ex, tx, ty, e.layer) / e.sv;
-                float di = lay_texel(P.img.dt[P.img.cur], P, q.x, q.y);
-                float diff = fminf(fmaxf(fabsf(de - di), 0.0f), 10.0f);
-                res = res + diff * P.distTransWeight;
-            }
-            {
-                int Lh = clampi(e.layer, 0, PT_MAX_STYLES - 1);
-                float sh = (float)(P.histH / P.numStyles);
-                int hx = clampi((int)tx, 0, P.histPitch - 1);
-                int hy = clampi((int)(ty + sh * (float)e.layer), 0, P.histRows - 1);
-                float h = __ldg(P.hist + (size_t)hy * P.histPitch + hx);
-                float thr = P.histThreshold[Lh];
-                res = res + ((h > thr) ? (h - thr) * P.histSlope[Lh] : 0.0f);
-            }
-            if (P.styleObjIdWeight > 0.f) {
-                int imgID = lvl_texel(P.img.ids, q.x, q.y);
-                int styleID = ex_point_id(P.ex, tx, ty, e.layer);
-                res = res + ((imgID != styleID) ? P.styleObjIdWeight : 0.0f);
-            }
-        } else {
-            res = fmaf(ssd_ap(canvas, to, P.alphaWeight), P.canvasOutputWeight, res);
-        }
+        const float res = tap_value<R, TM>(P, T, q, e, i, j, fast, fastp);
         const float w = gi * P.gauss[j + R];
         sum = valid ? fmaf(res, w, sum) : sum;
     }
@@ -927,6 +936,166 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter_q(const Params P, 
     else if (write_all) store_patch(work, k, off);
 }
 
+// updateResidualCache_kernel, texSynth_kernel.cu:661-693, inside a tracked
+// propagate/scatter loop.  The residual is the reference-order weighted sum
+// of per-tap values; each pixel keeps those values (P.inc.taps).  A tap's
+// value changes only when the pixel's own record changed (all taps) or the
+// record of the pixel under the tap changed (its canvas), so only those taps
+// are recomputed and the sum is then taken again over the stored values:
+// the same operations on the same values, so the same bits.  With `fill`
+// every tap of every pixel is computed (the loop's first residual).
+template <int R, int TM>
+__global__ void __launch_bounds__(kTileThreads, 2) kt_residual_inc(const Params P, float* out) {
+    constexpr int TW = TileSmem<R, TM>::TW, N = TileSmem<R, TM>::N, K = (2 * R + 1) * (2 * R + 1);
+    __shared__ TileSmem<R, TM> T;
+    __shared__ PixShared S;
+    __shared__ float4 CA[kTileThreads];  // own record: x, y, sv, layer bits | fast << 30
+    __shared__ float4 CB[kTileThreads];  // its basis
+    __shared__ uint16_t list[kTileThreads * K];  // pid << 7 | tap
+    __shared__ uint8_t C[N];
+    __shared__ int count;
+    const int pid = threadIdx.x + threadIdx.y * kTileW;
+    const size_t plane = (size_t)P.W * P.H;
+    const int x0 = blockIdx.x * kTileW - R, y0 = blockIdx.y * kTileH - R;
+    if (!P.inc.fill) {
+        for (int q = pid; q < N; q += kTileThreads) {
+            int gx = clampi(x0 + q % TW, 0, P.lw - 1);
+            int gy = clampi(y0 + q / TW, 0, P.lh - 1);
+            C[q] = P.inc.chg[(size_t)gy * P.W + gx];
+        }
+    }
+    if (pid == 0) count = 0;
+    __syncthreads();
+    // tap mask of this pixel (bit t: recompute tap t) and the pass stamps
+    const int x = blockIdx.x * kTileW + threadIdx.x, y = blockIdx.y * kTileH + threadIdx.y;
+    const bool in = x < P.lw && y < P.lh;
+    const size_t k = (size_t)y * P.W + x;
+    const int c0 = threadIdx.y * TW + threadIdx.x;  // window corner in C
+    uint64_t m0 = 0, m1 = 0;                        // taps 0..63, 64..80
+    bool own = P.inc.fill != 0;
+    if (in && !P.inc.fill) {
+        own = C[c0 + R * TW + R] != 0;
+#pragma unroll
+        for (int t = 0; t < K; t++) {
+            const int i = t / (2 * R + 1), j = t % (2 * R + 1);  // column-major (reference order)
+            if (C[c0 + j * TW + i]) {
+                if (t < 64) m0 |= 1ull << t; else m1 |= 1ull << (t - 64);
+            }
+        }
+        if (own) P.inc.last[k] = P.inc.pi;
+        if (m0 | m1) P.inc.win[k] = P.inc.pi;
+    }
+    const bool need = in && (own || (m0 | m1));
+    if (!__syncthreads_or(need)) return;
+    PixT px;
+    stage_tile<R, TM>(P, T, &px);  // (synchronises the block)
+    bool mine = false;
+    int nt = 0;
+    if (need) {
+        if (image_culled(P, x, y)) {
+            out[k] = 0.0f;
+        } else {
+            mine = true;
+            const LanePix q = lane_pix<R>(P, px);
+            put_pix<R>(S, pid, q);
+            const Patch o = load_patch(P.off, k);
+            LaneEval e;
+            lane_start<R>(P, q, o.x, o.y, o.theta, o.su, o.sv, o.layer, kNoBest, &e);
+            CA[pid] = make_float4(e.cx, e.cy, e.sv, __int_as_float(e.layer | (e.fast ? 1 << 30 : 0)));
+            CB[pid] = make_float4(e.b0.x, e.b0.y, e.b1.x, e.b1.y);
+            if (own) {  // every tap t < K
+                m0 = K >= 64 ? ~0ull : (1ull << K) - 1ull;
+                m1 = K > 64 ? (1ull << (K - 64)) - 1ull : 0ull;
+            }
+            // only taps inside the level rectangle enter the sum
+#pragma unroll
+            for (int t = 0; t < K; t++) {
+                const int i = t / (2 * R + 1) - R, j = t % (2 * R + 1) - R;
+                const bool valid = (i >= q.imin) && (i <= q.imax) && (j >= q.jmin) && (j <= q.jmax);
+                if (!valid) {
+                    if (t < 64) m0 &= ~(1ull << t); else m1 &= ~(1ull << (t - 64));
+                }
+            }
+            nt = __popcll(m0) + __popcll(m1);
+            if (P.counters && own) count_eval(P, x, y, px.temporal, false);
+        }
+    }
+    {
+        // queue this pixel's nt taps
+        const unsigned lane = lane_id();
+        int incl = nt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(kFull, incl, o);
+            if ((int)lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(kFull, incl, 31);
+        int base = 0;
+        if (lane == 31 && total > 0) base = atomicAdd(&count, total);
+        base = __shfl_sync(kFull, base, 31);
+        int w = base + incl - nt;
+        for (int t = 0; t < K; t++) {
+            const bool b = t < 64 ? (m0 >> t) & 1 : (m1 >> (t - 64)) & 1;
+            if (mine && b && w < kTileThreads * K) list[w++] = (uint16_t)((pid << 7) | t);
+        }
+    }
+    __syncthreads();
+    // every lane takes every 256th queued tap
+    const int n = count;
+#pragma unroll 1
+    for (int b = 0; b < n; b += kTileThreads) {
+        const int it = b + pid;
+        bool act = it < n;
+        LanePix q;
+        LaneEval e;
+        int t = 0, op = 0;
+        if (act) {
+            const int v = list[it];
+            op = v >> 7;
+            t = v & 127;
+        }
+        act = act && t < K && op < kTileThreads;  // (every queued entry satisfies this)
+        if (act) {
+            q = get_pix<R, TM>(P, S, op);
+            const float4 a = CA[op], bb = CB[op];
+            const int lb = __float_as_int(a.w);
+            e.cx = a.x; e.cy = a.y; e.sv = a.z;
+            e.layer = lb & ~(1 << 30);
+            e.fast = (lb >> 30) & 1;
+            e.b0 = make_float2(bb.x, bb.y);
+            e.b1 = make_float2(bb.z, bb.w);
+        }
+        const bool fast = __all_sync(kFull, !act || e.fast);
+        const bool fastp = TM ? __all_sync(kFull, !act || !q.temporal || q.prev_fast) : true;
+        if (act) {
+            const int i = t / (2 * R + 1) - R, j = t % (2 * R + 1) - R;
+            const float v = tap_value<R, TM>(P, T, q, e, i, j, fast, fastp);
+            P.inc.taps[(size_t)t * plane + (size_t)q.y * P.W + q.x] = v;
+        }
+    }
+    if (P.counters) count_taps(P, (unsigned)nt, px.temporal);
+    __syncthreads();
+    // the residual: the stored values summed in the reference's order
+    if (mine) {
+        const LanePix q = get_pix<R, TM>(P, S, pid);
+        float sum = q.sum0;
+#pragma unroll 1
+        for (int i = -R; i <= R; i++) {
+            const float gi = P.gauss[i + R];
+            const bool cvalid = (i >= q.imin) && (i <= q.imax);
+#pragma unroll
+            for (int j = -R; j <= R; j++) {
+                const bool valid = cvalid && (j >= q.jmin) && (j <= q.jmax);
+                const int t = (i + R) * (2 * R + 1) + (j + R);
+                const float v = valid ? P.inc.taps[(size_t)t * plane + k] : 0.0f;
+                const float w = gi * P.gauss[j + R];
+                sum = valid ? fmaf(v, w, sum) : sum;
+            }
+        }
+        out[k] = (q.sumW < kEpsilon) ? kBigResidual : sum / q.sumW;
+    }
+}
+
 template <int R>
 cudaError_t launch_tiled_r(int kind, int tm, const Params& P, PatchPlanes work, int arg, uint32_t pass_id, float* out,
                            cudaStream_t s) {
@@ -934,6 +1103,7 @@ cudaError_t launch_tiled_r(int kind, int tm, const Params& P, PatchPlanes work, 
 #define PT_TILED_DISPATCH(TMV)                                                                   \
     if (kind == 0) kt_propagate_q<R, TMV><<<g, b, 0, s>>>(P, work, arg);                        \
     else if (kind == 1) kt_scatter_q<R, TMV><<<g, b, 0, s>>>(P, work, arg, pass_id);            \
+    else if (P.inc.on || P.inc.fill) kt_residual_inc<R, TMV><<<g, b, 0, s>>>(P, out);   \
     else kt_residual<R, TMV><<<g, b, 0, s>>>(P, out);
     if (tm == TM_NONE) { PT_TILED_DISPATCH(TM_NONE) }
     else if (tm == TM_FWD) { PT_TILED_DISPATCH(TM_FWD) }

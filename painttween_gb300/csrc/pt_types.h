@@ -82,6 +82,10 @@ struct IncView {
     int on;    // this pass is tracked (chg written, stamps updated)
     int pi;    // its index
     int prev;  // index of the previous pass of this loop with the same candidates, INT_MIN if none
+    // per-tap values of every pixel's residual, (2r+1)^2 planes at level-0
+    // pitch, tap t = (i + r) * (2r + 1) + (j + r); `fill` recomputes all
+    float* taps;
+    int fill;
 };
 
 struct Params {
