@@ -44,6 +44,8 @@ int level_count(int w, int h) {
 struct ExLevel {  // one exemplar pyramid level, all styles (base and output planes)
     float4* base = nullptr;
     float4* out = nullptr;
+    float4* bo = nullptr;   // base and output interleaved per texel, rebuilt when stale
+    bool bo_stale = true;
     float* orient = nullptr;
     float* dt = nullptr;
     int* ids = nullptr;
@@ -297,6 +299,7 @@ static Params make_params(pt_ctx* c, int level) {
     if (c->ex) {
         P.ex.base = c->ex->base;
         P.ex.out = c->ex->out;
+        P.ex.bo = c->ex->bo;
         P.ex.orient = c->ex->orient;
         P.ex.dt = c->ex->dt;
         P.ex.ids = c->ex->ids;
@@ -315,12 +318,22 @@ static Params make_params(pt_ctx* c, int level) {
     return P;
 }
 
+// the interleaved copy of an exemplar level that the tiled kernels gather
+// from, rebuilt after its planes were written
+static pt_status refresh_interleaved(pt_ctx* c, ExLevel* L) {
+    if (!L->bo_stale || !L->bo || !L->base) return PT_OK;
+    LN(pt::launch_interleave_texels(L->base, L->out, L->bo, (size_t)L->w * L->h * c->NS, c->stream));
+    L->bo_stale = false;
+    return PT_OK;
+}
+
 static pt_status check_ready(pt_ctx* c, int level, bool need_ex = true, bool need_img = true) {
     if (!c->initialized) return fail(c, PT_ERR_STATE, "pt_initialize has not been called");
     if (!c->have_params) return fail(c, PT_ERR_STATE, "pt_set_params has not been called");
     if (level < 0 || (c->W >> level) < 1 || (c->H >> level) < 1)
         return fail(c, PT_ERR_INVALID, "level %d out of range", level);
     if (need_ex && (!c->ex || !c->ex->base)) return fail(c, PT_ERR_STATE, "no exemplar level loaded");
+    if (need_ex) TRY(refresh_interleaved(c, c->ex));
     if (need_img) {
         const ImgView& I = c->img;
         int lw = c->W >> level, lh = c->H >> level;
@@ -778,10 +791,11 @@ pt_status pt_initialize_exemplars(pt_ctx* c, int w, int h, int ns) {
     if (w < 2 || h < 2 || ns != c->NS) return fail(c, PT_ERR_INVALID, "bad exemplar size %dx%dx%d", w, h, ns);
     size_t n = (size_t)w * h * ns;
     if (n > c->ex_cap) {
-        dfree_t(c, c->up_ex.base); dfree_t(c, c->up_ex.out);
+        dfree_t(c, c->up_ex.base); dfree_t(c, c->up_ex.out); dfree_t(c, c->up_ex.bo);
         dfree_t(c, c->up_ex.orient); dfree_t(c, c->up_ex.dt); dfree_t(c, c->up_ex.ids);
         TRY(dalloc_t(c, &c->up_ex.base, n));
         TRY(dalloc_t(c, &c->up_ex.out, n));
+        TRY(dalloc_t(c, &c->up_ex.bo, 2 * n));
         TRY(dalloc_t(c, &c->up_ex.orient, n));
         TRY(dalloc_t(c, &c->up_ex.dt, n));
         TRY(dalloc_t(c, &c->up_ex.ids, n));
@@ -790,6 +804,7 @@ pt_status pt_initialize_exemplars(pt_ctx* c, int w, int h, int ns) {
     c->up_ex.w = w;
     c->up_ex.h = h;
     c->up_ex.transparent = -1;
+    c->up_ex.bo_stale = true;
     c->ex = &c->up_ex;
     return PT_OK;
 }
@@ -814,6 +829,7 @@ pt_status pt_upload_image_color4(pt_ctx* c, int level, int layer, const float* r
         float4* plane = (layer == PT_LAYER_EXEMPLAR_OUTPUT) ? c->up_ex.out : c->up_ex.base;
         TRY(h2d(c, plane + n * style, rgba, n * sizeof(float4)));
         if (layer == PT_LAYER_EXEMPLAR_OUTPUT) c->up_ex.transparent = -1;
+        c->up_ex.bo_stale = true;
         return PT_OK;
     }
     if (level < 0 || w != (c->W >> level) || h != (c->H >> level))
@@ -931,7 +947,7 @@ pt_status pt_create_random_level(pt_ctx* c, int level, int frame) {
     int mx = (c->SW >> level) - 1, my = (c->SH >> level) - 1;
     if (mx < 1 || my < 1) return fail(c, PT_ERR_INVALID, "style too small for level %d", level);
     if (!c->rnd) TRY(dalloc_t(c, &c->rnd, (size_t)c->W * c->H));
-    ExView ex{c->ex->base, c->ex->out, c->ex->orient, c->ex->dt, c->ex->ids, c->ex->w, c->ex->h, c->NS};
+    ExView ex{c->ex->base, c->ex->out, c->ex->bo, c->ex->orient, c->ex->dt, c->ex->ids, c->ex->w, c->ex->h, c->NS};
     const ImgView& I = c->img;
     int mode;
     uint32_t seed = (uint32_t)(frame * level);
@@ -1243,7 +1259,8 @@ pt_status pt_set_style(pt_ctx* c, int style, int w, int h, const float* base, co
     int nlev = level_count(w, h);
     if ((int)c->style_levels.size() != nlev) {
         for (auto& L : c->style_levels) {
-            dfree_t(c, L.base); dfree_t(c, L.out); dfree_t(c, L.orient); dfree_t(c, L.dt); dfree_t(c, L.ids);
+            dfree_t(c, L.base); dfree_t(c, L.out); dfree_t(c, L.bo); dfree_t(c, L.orient); dfree_t(c, L.dt);
+            dfree_t(c, L.ids);
         }
         c->style_levels.assign(nlev, ExLevel());
         for (int l = 0; l < nlev; l++) {
@@ -1253,6 +1270,7 @@ pt_status pt_set_style(pt_ctx* c, int style, int w, int h, const float* base, co
             size_t n = (size_t)L.w * L.h * c->NS;
             TRY(dalloc_t(c, &L.base, n));
             TRY(dalloc_t(c, &L.out, n));
+            TRY(dalloc_t(c, &L.bo, 2 * n));
             TRY(dalloc_t(c, &L.orient, n));
             TRY(dalloc_t(c, &L.dt, n));
             TRY(dalloc_t(c, &L.ids, n));
@@ -1282,6 +1300,7 @@ pt_status pt_set_style(pt_ctx* c, int style, int w, int h, const float* base, co
         CU(cudaMemcpyAsync(L.dt + n * style, pd[l], n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
         CU(cudaMemcpyAsync(L.ids + n * style, pi[l], n * sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
         L.transparent = -1;
+        L.bo_stale = true;
     }
     CU(cudaStreamSynchronize(c->stream));
     for (int l = 0; l < nlev; l++) {
@@ -1425,7 +1444,7 @@ static pt_status bind_style_level(pt_ctx* c, int level) {
     for (int s = 0; s < c->NS; s++)
         if (!c->style_set[s]) return fail(c, PT_ERR_STATE, "style %d not set", s);
     c->ex = &c->style_levels[level];
-    return PT_OK;
+    return refresh_interleaved(c, c->ex);
 }
 
 // SynthesisFrame::loadImages + loadAnimImages, synthesisFrame.cpp:562-656

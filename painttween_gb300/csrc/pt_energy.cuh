@@ -42,12 +42,23 @@ struct TileSmem {
     float phys[TM ? N : 1];
 };
 
-// bilinear base+output at (u, v) of one exemplar layer (LB: base plane,
-// LO: output plane); fast (warp-uniform): the footprint is known to be
-// inside [0, w-1] x [0, h-1], so the clamps are no-ops and are skipped
+// both colours of one exemplar texel: a 32-byte record of the interleaved
+// copy, one 256-bit read-only load (records start on 32-byte boundaries)
+__device__ __forceinline__ void ld_texel(const float4* p, float4* b, float4* o) {
+    float r0, r1, r2, r3, r4, r5, r6, r7;
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(r0), "=f"(r1), "=f"(r2), "=f"(r3), "=f"(r4), "=f"(r5), "=f"(r6), "=f"(r7)
+        : "l"(p));
+    *b = make_float4(r0, r1, r2, r3);
+    *o = make_float4(r4, r5, r6, r7);
+}
+
+// bilinear base+output at (u, v) of one exemplar layer (LBO: its interleaved
+// records); fast (warp-uniform): the footprint is known to be inside
+// [0, w-1] x [0, h-1], so the clamps are no-ops and are skipped
 template <bool PK>
-__device__ __forceinline__ void sample2(const float4* LB, const float4* LO, int w, int h, float u, float v,
-                                        float4* base, float4* out, bool fast) {
+__device__ __forceinline__ void sample2(const float4* LBO, int w, int h, float u, float v, float4* base, float4* out,
+                                        bool fast) {
     float xs = u + 0.5f, ys = v + 0.5f;
     float xb = xs - 0.5f, yb = ys - 0.5f;
     float fx = floorf(xb), fy = floorf(yb);
@@ -66,10 +77,11 @@ __device__ __forceinline__ void sample2(const float4* LB, const float4* LO, int 
     Bl bw;
     bw.w00 = oa * oc; bw.w10 = a * oc; bw.w01 = oa * c; bw.w11 = a * c;
     const size_t r0 = (size_t)y0 * w, r1 = (size_t)y1 * w;
-    float4 b00 = __ldg(LB + r0 + x0), b10 = __ldg(LB + r0 + x1);
-    float4 b01 = __ldg(LB + r1 + x0), b11 = __ldg(LB + r1 + x1);
-    float4 o00 = __ldg(LO + r0 + x0), o10 = __ldg(LO + r0 + x1);
-    float4 o01 = __ldg(LO + r1 + x0), o11 = __ldg(LO + r1 + x1);
+    float4 b00, b10, b01, b11, o00, o10, o01, o11;
+    ld_texel(LBO + 2 * (r0 + x0), &b00, &o00);
+    ld_texel(LBO + 2 * (r0 + x1), &b10, &o10);
+    ld_texel(LBO + 2 * (r1 + x0), &b01, &o01);
+    ld_texel(LBO + 2 * (r1 + x1), &b11, &o11);
     *base = PK ? bl4p(bw, b00, b10, b01, b11) : bl4(bw, b00, b10, b01, b11);
     *out = PK ? bl4p(bw, o00, o10, o01, o11) : bl4(bw, o00, o10, o01, o11);
 }
@@ -147,8 +159,7 @@ __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, 
     constexpr int TW = TileSmem<R, TM>::TW;
     const size_t lsz = (size_t)P.ex.w * P.ex.h;
     const size_t lo = (size_t)ex_layer(P.ex, c.layer) * lsz;
-    const float4* LB = P.ex.base + lo;
-    const float4* LO = P.ex.out + lo;
+    const float4* LBO = P.ex.bo + 2 * lo;
     const size_t lp = TM ? (size_t)ex_layer(P.ex, px.prev.layer) * lsz : 0;
     const float hw = (float)P.histW, hh = (float)P.histH;
     const unsigned mask = __activemask();
@@ -173,7 +184,7 @@ __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, 
                     if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
                 }
                 float4 tb, to;
-                sample2<true>(LB, LO, P.ex.w, P.ex.h, tx, ty, &tb, &to, fast);
+                sample2<true>(LBO, P.ex.w, P.ex.h, tx, ty, &tb, &to, fast);
                 float res = ssd_ap(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
                 if (TM) {
                     if (px.temporal) {
@@ -181,7 +192,7 @@ __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, 
                         float ptx = px.prev.x + fmaf((float)i, px.pb0.x, (float)j * px.pb1.x);
                         float pty = px.prev.y + fmaf((float)i, px.pb0.y, (float)j * px.pb1.y);
                         float4 peb, peo;
-                        sample2<true>(P.ex.base + lp, P.ex.out + lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo, fastp);
+                        sample2<true>(P.ex.bo + 2 * lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo, fastp);
                         float r = ssdp(sub4p(base, pbase), sub4p(tb, peb)) * P.tdIn;
                         r = fmaf(ssdp(sub4p(canvas, pout), sub4p(to, peo)), P.tdOut, r);
                         r = fmaf(ssdp(pout, to), P.tc, r);
@@ -478,8 +489,7 @@ __device__ __forceinline__ float tap_value(const Params& P, const TileSmem<R, TM
     constexpr int TW = TileSmem<R, TM>::TW;
     const size_t lsz = (size_t)P.ex.w * P.ex.h;
     const size_t lo = (size_t)ex_layer(P.ex, e.layer) * lsz;
-    const float4* LB = P.ex.base + lo;
-    const float4* LO = P.ex.out + lo;
+    const float4* LBO = P.ex.bo + 2 * lo;
     const size_t lp = TM ? (size_t)q.prevlayer * lsz : 0;
     const float hw = (float)P.histW, hh = (float)P.histH;
     const int s = q.sidx + j * TW + i;
@@ -492,7 +502,7 @@ __device__ __forceinline__ float tap_value(const Params& P, const TileSmem<R, TM
         if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
     }
     float4 tb, to;
-    sample2<true>(LB, LO, P.ex.w, P.ex.h, tx, ty, &tb, &to, fast);
+    sample2<true>(LBO, P.ex.w, P.ex.h, tx, ty, &tb, &to, fast);
     float res = ssd_ap(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
     if (TM) {
         if (q.temporal) {
@@ -500,7 +510,7 @@ __device__ __forceinline__ float tap_value(const Params& P, const TileSmem<R, TM
             float ptx = q.prevx + fmaf((float)i, q.pb0.x, (float)j * q.pb1.x);
             float pty = q.prevy + fmaf((float)i, q.pb0.y, (float)j * q.pb1.y);
             float4 peb, peo;
-            sample2<true>(P.ex.base + lp, P.ex.out + lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo, fastp);
+            sample2<true>(P.ex.bo + 2 * lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo, fastp);
             float r = ssdp(sub4p(base, pbase), sub4p(tb, peb)) * P.tdIn;
             r = fmaf(ssdp(sub4p(canvas, pout), sub4p(to, peo)), P.tdOut, r);
             r = fmaf(ssdp(pout, to), P.tc, r);

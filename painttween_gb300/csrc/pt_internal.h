@@ -39,6 +39,7 @@ cudaError_t launch_random_level(int mode, int w, int h, int mx, int my, int tran
                                 Arr<float4> img, Arr<float> iorient, ExView ex, float4* out,
                                 const uint32_t* states, uint32_t seed, cudaStream_t s);
 cudaError_t launch_any_transparent(const float4* out, size_t n, int* flag, cudaStream_t s);
+cudaError_t launch_interleave_texels(const float4* base, const float4* out, float4* bo, size_t n, cudaStream_t s);
 
 // tiled patch-distance kernels for patch radius 2, 3, 4 (pt_tiled_r*.cu):
 // kind 0 = propagate (arg = jump), 1 = scatter (arg = write_all),

@@ -144,6 +144,15 @@ __global__ void __launch_bounds__(128) k_residual(const Params P, float* out) {
     out[k] = energy(P, x, y, t, pc);
 }
 
+// base and output exemplar texels interleaved into 32-byte records (the
+// tiled kernels fetch a texel's two colours with one 256-bit load)
+__global__ void k_interleave_texels(const float4* base, const float4* out, float4* bo, size_t n) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    bo[2 * t] = base[t];
+    bo[2 * t + 1] = out[t];
+}
+
 // offsetsToOutput, :263-274
 __global__ void k_canvas(const Params P, float4* canvas) {
     PIXEL_XY
@@ -645,6 +654,13 @@ cudaError_t launch_random_level(int mode, int w, int h, int mx, int my, int tran
         dim3 b(32, 4);
         k_counter_random<<<grid2(w, h, b), b, 0, s>>>(R, seed);
     }
+    LAUNCH_CHECK();
+}
+cudaError_t launch_interleave_texels(const float4* base, const float4* out, float4* bo, size_t n, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const int threads = 256;
+    const unsigned blocks = (unsigned)((n + threads - 1) / threads);
+    k_interleave_texels<<<blocks, threads, 0, s>>>(base, out, bo, n);
     LAUNCH_CHECK();
 }
 cudaError_t launch_any_transparent(const float4* out, size_t n, int* flag, cudaStream_t s) {

@@ -32,6 +32,7 @@ struct PatchPlanes {
 struct ExView {
     const float4* base;
     const float4* out;
+    const float4* bo;  // the same texels interleaved: bo[2t] = base[t], bo[2t + 1] = out[t] (32-byte records)
     const float* orient;
     const float* dt;
     const int* ids;
