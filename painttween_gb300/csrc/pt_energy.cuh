@@ -604,7 +604,7 @@ struct PropQueue {
     uint16_t list[kTileThreads * 4];  // pid * 4 + slot
     float thr[kTileThreads];          // the pixel's residual
     int slots[kTileThreads];          // per candidate (3 bits each): slot + 3, or 0 skipped, 1 repeat, 2 rejected
-    int count, next;
+    int count[kTileH], next[kTileH];  // per warp: its row's candidates (list[128 * warp ...])
 };
 
 // propagate_kernel with lane cursors over the tile's candidates
@@ -635,7 +635,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P
         if (block_idle(P, work, need, in, k)) return;
     }
     const int pid = threadIdx.x + threadIdx.y * kTileW;
-    if (pid == 0) { Q.count = 0; Q.next = 0; }
+    if (pid < kTileH) { Q.count[pid] = 0; Q.next[pid] = 0; }
     PixT px;
     const bool in = stage_tile<R, TM>(P, T, &px);  // (synchronises the block)
     // phase 1: each pixel builds its candidates (the reference's order,
@@ -709,11 +709,12 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P
             int v = __shfl_up_sync(kFull, incl, o);
             if ((int)lane >= o) incl += v;
         }
-        const int total = __shfl_sync(kFull, incl, 31);
-        int base = 0;
-        if (lane == 31 && total > 0) base = atomicAdd(&Q.count, total);
-        base = __shfl_sync(kFull, base, 31);
-        for (int j = 0; j < n; j++) Q.list[base + incl - n + j] = (uint16_t)(pid * 4 + j);
+        // each warp queues its own row's candidates, so that its lanes
+        // gather from neighbouring exemplar regions (a coherent field maps
+        // neighbouring pixels to neighbouring texels)
+        const int warp = pid / kTileW;
+        if (lane == 31) Q.count[warp] = incl;
+        for (int j = 0; j < n; j++) Q.list[warp * 4 * kTileW + incl - n + j] = (uint16_t)(pid * 4 + j);
     }
     __syncthreads();
     // phase 2: lane cursors over the queue
@@ -722,15 +723,16 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P
         LaneEval e;
         bool act = false, more = true;
         int cur = 0;
-        const int count = Q.count;
+        const int warp = pid / kTileW;
+        const int count = Q.count[warp];
 #pragma unroll 1
         while (true) {
             const bool want = !act && more;
             if (__any_sync(kFull, want)) {
-                const int t = queue_take(want, &Q.next);
+                const int t = queue_take(want, &Q.next[warp]);
                 if (want) {
                     if (t < count) {
-                        cur = Q.list[t];
+                        cur = Q.list[warp * 4 * kTileW + t];
                         const int op = cur >> 2;
                         q = get_pix<R, TM>(P, S, op);
                         const float4 a = Q.ca[cur];
