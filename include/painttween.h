@@ -331,6 +331,48 @@ pt_status pt_get_frame_result(pt_ctx* ctx, int frame, float* out_rgba, pt_patchx
 pt_status pt_host_alloc(size_t bytes, void** out);
 pt_status pt_host_free(void* p);
 
+/* ---- Serving: many requests on one GPU --------------------------------------
+ * No counterpart in the reference, which runs one synthesis per process.
+ * A request is a style plus one frame (a still) or several (a clip).
+ * pt_serve runs up to max_in_flight requests at once, each on its own
+ * context and CUDA stream, so the kernels of requests in flight overlap on
+ * the GPU (a small request alone leaves most of it idle).  Requests are
+ * admitted in arrival order once their arrival time has passed and their
+ * estimated device memory fits hbm_budget beside the requests in flight
+ * (0: no budget); a request larger than the budget still runs, alone.  Each
+ * result equals pt_synthesize_frame / pt_synthesize_animation of that request
+ * on a context of its own.  Returns the first failing request's status, after
+ * all requests have run. */
+typedef struct {
+    const float* rgba;           /* image_w x image_h RGBA (required) */
+    const float* orient_tensor;  /* x3 structure tensor, or NULL */
+    const float* dist_trans;     /* or NULL */
+    const int32_t* ids;          /* or NULL */
+    const float* vel_fwd;        /* x2, or NULL */
+    const float* vel_bwd;        /* x2, or NULL */
+    const float* scale;          /* x2, or NULL (1, 1) */
+} pt_frame_inputs;
+
+typedef struct {
+    pt_params params;
+    int style_w, style_h;
+    const float* style_base;           /* RGBA */
+    const float* style_output;         /* RGBA */
+    const float* style_orient_tensor;  /* or NULL */
+    const float* style_dist_trans;     /* or NULL */
+    const int32_t* style_ids;          /* or NULL */
+    int image_w, image_h, frames;
+    const pt_frame_inputs* inputs;     /* `frames` entries */
+    float* out_rgba;          /* frames x (image_h >> finalLevel) x (image_w >> finalLevel) x 4, or NULL */
+    pt_patchxf* out_offsets;  /* frames x (image_h >> finalLevel) x (image_w >> finalLevel), or NULL */
+    double arrival_ms;        /* arrival, in ms after pt_serve starts */
+    double start_ms;          /* out: when its synthesis started */
+    double done_ms;           /* out: when its results were written */
+    pt_status status;         /* out */
+} pt_request;
+
+pt_status pt_serve(int device, pt_request* requests, int count, int max_in_flight, size_t hbm_budget);
+
 /* Number of this library's kernel launches issued so far by the context. */
 uint64_t pt_kernel_launches(const pt_ctx* ctx);
 

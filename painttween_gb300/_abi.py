@@ -169,3 +169,21 @@ class KernelStats(ctypes.Structure):
 
 def status_name(s):
     return STATUS_NAMES.get(s, "PT_STATUS_%d" % s)
+
+
+class FrameInputs(ctypes.Structure):
+    """pt_frame_inputs (include/painttween.h)."""
+    _fields_ = [("rgba", ctypes.c_void_p), ("orient_tensor", ctypes.c_void_p), ("dist_trans", ctypes.c_void_p),
+                ("ids", ctypes.c_void_p), ("vel_fwd", ctypes.c_void_p), ("vel_bwd", ctypes.c_void_p),
+                ("scale", ctypes.c_void_p)]
+
+
+class Request(ctypes.Structure):
+    """pt_request (include/painttween.h)."""
+    _fields_ = [("params", Params), ("style_w", ctypes.c_int), ("style_h", ctypes.c_int),
+                ("style_base", ctypes.c_void_p), ("style_output", ctypes.c_void_p),
+                ("style_orient_tensor", ctypes.c_void_p), ("style_dist_trans", ctypes.c_void_p),
+                ("style_ids", ctypes.c_void_p), ("image_w", ctypes.c_int), ("image_h", ctypes.c_int),
+                ("frames", ctypes.c_int), ("inputs", ctypes.POINTER(FrameInputs)), ("out_rgba", ctypes.c_void_p),
+                ("out_offsets", ctypes.c_void_p), ("arrival_ms", ctypes.c_double), ("start_ms", ctypes.c_double),
+                ("done_ms", ctypes.c_double), ("status", ctypes.c_int)]

@@ -1,8 +1,8 @@
 """In-tree build of libpainttween_gb300.so for sm_103a.
 
-Two translation units compiled in parallel: the kernels with nvcc
+Translation units compiled in parallel: the kernels with nvcc
 (-fmad=false: multiply-adds are fused only where the source writes fmaf) and
-the host library with g++ against the CUDA runtime; linked with nvcc (static
+the host code with g++ against the CUDA runtime; linked with nvcc (static
 cudart).  No CPU fallback is built.
 """
 import os
@@ -44,12 +44,14 @@ def build(force=False, verbose=False):
     inc = ["-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
     cu_files = sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
     objs = [os.path.join(BUILD, f[:-3] + ".o") for f in cu_files]
-    h_obj = os.path.join(BUILD, "pt_context.o")
+    cpp_files = sorted(f for f in os.listdir(CSRC) if f.endswith(".cpp"))
+    h_objs = [os.path.join(BUILD, f[:-4] + ".o") for f in cpp_files]
     jobs = [[nvcc, ARCH, "-lineinfo", "-O3", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
              "--expt-relaxed-constexpr"] + inc + ["-c", os.path.join(CSRC, f), "-o", o]
             for f, o in zip(cu_files, objs)]
-    jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function",
-                 "-I" + os.path.join(cuda, "include")] + inc + ["-c", os.path.join(CSRC, "pt_context.cpp"), "-o", h_obj])
+    for f, o in zip(cpp_files, h_objs):
+        jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function",
+                     "-I" + os.path.join(cuda, "include")] + inc + ["-c", os.path.join(CSRC, f), "-o", o])
     procs = []
     for cmd in jobs:
         if verbose:
@@ -64,8 +66,8 @@ def build(force=False, verbose=False):
             print(out.decode(errors="replace"))
     if failed:
         raise RuntimeError("painttween_gb300 build failed:\n" + "\n".join(failed))
-    link = [nvcc, ARCH, "-shared", "-o", LIB + ".tmp"] + objs + [h_obj, "-lcudart_static", "-lrt", "-lpthread",
-                                                                "-ldl"]
+    link = [nvcc, ARCH, "-shared", "-o", LIB + ".tmp"] + objs + h_objs + ["-lcudart_static", "-lrt", "-lpthread",
+                                                                     "-ldl"]
     if verbose:
         print(" ".join(link))
     subprocess.check_call(link)

@@ -79,6 +79,8 @@ struct pt_ctx {
     size_t budget = 0, allocated = 0;
     std::string err;
     std::map<void*, size_t> allocs;
+    std::multimap<size_t, void*> cache;  // freed blocks by size
+    size_t cached = 0;
 
     pt_params params{};
     bool have_params = false;
@@ -187,20 +189,51 @@ static pt_status fail(pt_ctx* c, pt_status s, const char* fmt, ...) {
         if (s_ != PT_OK) return s_;    \
     } while (0)
 
+// Device memory of a context.  Freed blocks are kept in a per-context cache
+// and handed out again (all of a context's work is ordered on its stream, so
+// a block's next user runs after its previous one): in steady state no
+// cudaFree runs, which would wait for the whole device and stall the other
+// contexts working beside this one.  The cache is released when an
+// allocation would exceed the budget or cudaMalloc fails.
+static void release_cache(pt_ctx* c) {
+    if (c->cache.empty()) return;
+    cudaStreamSynchronize(c->stream);
+    for (auto& kv : c->cache) cudaFree(kv.second);
+    c->cache.clear();
+    c->cached = 0;
+}
 static pt_status dalloc(pt_ctx* c, void** p, size_t bytes) {
     *p = nullptr;
     if (bytes == 0) bytes = 16;
-    if (c->budget && c->allocated + bytes > c->budget)
-        return fail(c, PT_ERR_BUDGET, "allocation of %zu bytes exceeds the HBM budget (%zu of %zu used)", bytes,
-                    c->allocated, c->budget);
-    cudaError_t e = cudaMalloc(p, bytes);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return fail(c, PT_ERR_OOM, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    bytes = (bytes + 255) & ~(size_t)255;
+    auto it = c->cache.lower_bound(bytes);  // the smallest cached block that fits, if not much larger
+    if (it != c->cache.end() && it->first <= bytes + bytes / 8) {
+        const size_t sz = it->first;
+        *p = it->second;
+        c->cache.erase(it);
+        c->cached -= sz;
+        c->allocated += sz;
+        c->allocs[*p] = sz;
+    } else {
+        if (c->budget && c->allocated + c->cached + bytes > c->budget) release_cache(c);
+        if (c->budget && c->allocated + bytes > c->budget)
+            return fail(c, PT_ERR_BUDGET, "allocation of %zu bytes exceeds the HBM budget (%zu of %zu used)", bytes,
+                        c->allocated, c->budget);
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            release_cache(c);
+            e = cudaMalloc(p, bytes);
+        }
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            *p = nullptr;
+            return fail(c, PT_ERR_OOM, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+        }
+        c->allocated += bytes;
+        c->allocs[*p] = bytes;
     }
-    c->allocated += bytes;
-    c->allocs[*p] = bytes;
-    e = cudaMemsetAsync(*p, 0, bytes, c->stream);
+    cudaError_t e = cudaMemsetAsync(*p, 0, c->allocs[*p], c->stream);
     if (e != cudaSuccess) return fail(c, PT_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));
     return PT_OK;
 }
@@ -214,11 +247,14 @@ static pt_status dalloc_t(pt_ctx* c, T** p, size_t count) {
 static void dfree(pt_ctx* c, void* p) {
     if (!p) return;
     auto it = c->allocs.find(p);
-    if (it != c->allocs.end()) {
-        c->allocated -= it->second;
-        c->allocs.erase(it);
+    if (it == c->allocs.end()) {
+        cudaFree(p);
+        return;
     }
-    cudaFree(p);
+    c->allocated -= it->second;
+    c->cached += it->second;
+    c->cache.insert(std::make_pair(it->second, p));
+    c->allocs.erase(it);
 }
 template <class T>
 static void dfree_t(pt_ctx* c, T*& p) {
@@ -557,7 +593,7 @@ const char* pt_status_string(pt_status s) {
 }
 
 const char* pt_last_error(const pt_ctx* c) { return c ? c->err.c_str() : "null context"; }
-size_t pt_device_bytes(const pt_ctx* c) { return c ? c->allocated : 0; }
+size_t pt_device_bytes(const pt_ctx* c) { return c ? c->allocated + c->cached : 0; }
 uint64_t pt_kernel_launches(const pt_ctx* c) { return c ? c->launches : 0; }
 
 void pt_default_params(pt_params* p) {
@@ -643,6 +679,8 @@ pt_status pt_destroy(pt_ctx* c) {
         for (auto& pr : v) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
     for (auto& kv : c->allocs) cudaFree(kv.first);
     c->allocs.clear();
+    for (auto& kv : c->cache) cudaFree(kv.second);
+    c->cache.clear();
     if (c->cb_stage) cudaFreeHost(c->cb_stage);
     cudaStreamDestroy(c->stream);
     delete c;
@@ -1257,7 +1295,7 @@ pt_status pt_set_style(pt_ctx* c, int style, int w, int h, const float* base, co
         return fail(c, PT_ERR_UNSUPPORTED, "style %dx%d differs from the initialized style size %dx%d", w, h, c->SW,
                     c->SH);
     int nlev = level_count(w, h);
-    if ((int)c->style_levels.size() != nlev) {
+    if ((int)c->style_levels.size() != nlev || c->style_levels[0].w != w || c->style_levels[0].h != h) {
         for (auto& L : c->style_levels) {
             dfree_t(c, L.base); dfree_t(c, L.out); dfree_t(c, L.bo); dfree_t(c, L.orient); dfree_t(c, L.dt);
             dfree_t(c, L.ids);

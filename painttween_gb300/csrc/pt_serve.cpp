@@ -1,0 +1,147 @@
+// pt_serve.cpp -- many synthesis requests on one GPU (pt_serve).
+//
+// Worker threads each own a context (its own device buffers and CUDA
+// stream) and take requests in arrival order.  A request is admitted once
+// its arrival time has passed and its estimated device memory fits the
+// budget beside the requests in flight, so several requests' kernels run on
+// the GPU at once: a small still alone fills only a few of the GPU's 152
+// SMs.  Everything here goes through the public C ABI; the contexts share
+// nothing, so each result is the one a request gets on a context of its own.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "painttween.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+double ms_since(Clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+}
+
+// Device memory a request needs, estimated from its sizes: per image pixel
+// the offset, residual, canvas and advected planes, the change-tracking
+// planes and the per-tap residual values, per frame pixel its pyramid, per
+// style texel its pyramid with the interleaved copy and the histogram.
+size_t estimate_bytes(const pt_request& r) {
+    const size_t px = (size_t)r.image_w * r.image_h;
+    const size_t taps = (size_t)(2 * r.params.residualWindowSize + 1) * (2 * r.params.residualWindowSize + 1);
+    const size_t per_px = 720 + 4 * taps;
+    const size_t per_frame_px = 96;
+    const size_t per_texel = 150;
+    return px * per_px + px * per_frame_px * (size_t)std::max(r.frames, 1) +
+           (size_t)r.style_w * r.style_h * per_texel;
+}
+
+pt_status run_request(pt_ctx* c, pt_request& r) {
+#define PT_TRY(expr)                   \
+    do {                               \
+        pt_status s_ = (expr);         \
+        if (s_ != PT_OK) return s_;    \
+    } while (0)
+    if (r.frames < 1 || !r.inputs || r.image_w < 2 || r.image_h < 2) return PT_ERR_INVALID;
+    PT_TRY(pt_initialize(c, r.image_w, r.image_h, r.style_w, r.style_h, 1));
+    PT_TRY(pt_set_params(c, &r.params));
+    PT_TRY(pt_set_style(c, 0, r.style_w, r.style_h, r.style_base, r.style_output, r.style_orient_tensor,
+                        r.style_dist_trans, r.style_ids));
+    PT_TRY(pt_clear_frames(c));
+    for (int f = 0; f < r.frames; f++) {
+        const pt_frame_inputs& in = r.inputs[f];
+        PT_TRY(pt_set_frame(c, f, r.image_w, r.image_h, in.rgba, in.orient_tensor, in.dist_trans, in.ids, in.vel_fwd,
+                            in.vel_bwd, in.scale));
+    }
+    const int fl = r.params.finalLevel;
+    const size_t n = (size_t)(r.image_w >> fl) * (size_t)(r.image_h >> fl);
+    if (r.frames == 1) {
+        PT_TRY(pt_synthesize_frame(c, 0, r.out_rgba, r.out_offsets));
+    } else {
+        PT_TRY(pt_synthesize_animation(c, 0, r.frames - 1, nullptr, nullptr));
+        for (int f = 0; f < r.frames; f++)
+            PT_TRY(pt_get_frame_result(c, f, r.out_rgba ? r.out_rgba + (size_t)f * n * 4 : nullptr,
+                                       r.out_offsets ? r.out_offsets + (size_t)f * n : nullptr));
+    }
+    PT_TRY(pt_clear_frames(c));
+    return PT_OK;
+#undef PT_TRY
+}
+
+struct Queue {
+    std::mutex m;
+    std::condition_variable cv;
+    std::vector<int> order;  // request indices by arrival time
+    size_t next = 0;         // next request of `order` to admit
+    size_t in_flight = 0;    // estimated bytes of the admitted, unfinished requests
+    int running = 0;
+};
+
+}  // namespace
+
+pt_status pt_serve(int device, pt_request* reqs, int count, int max_in_flight, size_t hbm_budget) {
+    if (count < 0 || (count > 0 && !reqs) || max_in_flight < 1) return PT_ERR_INVALID;
+    for (int i = 0; i < count; i++) {
+        reqs[i].status = PT_ERR_STATE;  // not run
+        reqs[i].start_ms = reqs[i].done_ms = 0.0;
+    }
+    Queue q;
+    q.order.resize(count);
+    for (int i = 0; i < count; i++) q.order[i] = i;
+    std::stable_sort(q.order.begin(), q.order.end(),
+                     [&](int a, int b) { return reqs[a].arrival_ms < reqs[b].arrival_ms; });
+    const Clock::time_point t0 = Clock::now();
+    const int workers = std::min(max_in_flight, std::max(count, 1));
+    std::vector<std::thread> pool;
+    for (int w = 0; w < workers; w++) {
+        pool.emplace_back([&]() {
+            pt_ctx* c = nullptr;
+            const pt_status created = pt_create(device, 0, &c);
+            for (;;) {
+                int idx = -1;
+                size_t est = 0;
+                {
+                    std::unique_lock<std::mutex> lk(q.m);
+                    for (;;) {
+                        if (q.next >= q.order.size()) break;
+                        idx = q.order[q.next];
+                        est = estimate_bytes(reqs[idx]);
+                        const double now = ms_since(t0);
+                        if (now < reqs[idx].arrival_ms) {  // not arrived yet
+                            q.cv.wait_for(lk, std::chrono::duration<double, std::milli>(reqs[idx].arrival_ms - now));
+                            idx = -1;
+                            continue;
+                        }
+                        if (hbm_budget && q.running > 0 && q.in_flight + est > hbm_budget) {  // no room yet
+                            q.cv.wait(lk);
+                            idx = -1;
+                            continue;
+                        }
+                        q.next++;
+                        q.in_flight += est;
+                        q.running++;
+                        break;
+                    }
+                }
+                if (idx < 0) break;
+                pt_request& r = reqs[idx];
+                r.start_ms = ms_since(t0);
+                r.status = (created == PT_OK) ? run_request(c, r) : created;
+                r.done_ms = ms_since(t0);
+                {
+                    std::lock_guard<std::mutex> lk(q.m);
+                    q.in_flight -= est;
+                    q.running--;
+                }
+                q.cv.notify_all();
+            }
+            if (c) pt_destroy(c);
+        });
+    }
+    for (auto& t : pool) t.join();
+    for (int i = 0; i < count; i++)
+        if (reqs[i].status != PT_OK) return reqs[i].status;
+    return PT_OK;
+}

@@ -65,3 +65,33 @@ def test_create_without_device_reports_error(gpu_lib):
     h = ctypes.c_void_p()
     st = gpu_lib.pt_create(0, 0, ctypes.byref(h))
     assert st == 2 and not h.value  # PT_ERR_CUDA, no context, no exit()
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """The ctypes mirrors of pt_params, pt_frame_inputs and pt_request have
+    the header's sizes and field offsets (checked by a C program compiled
+    against include/painttween.h)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"pt_params": _abi.Params, "pt_frame_inputs": _abi.FrameInputs, "pt_request": _abi.Request}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "painttween.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append('printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for fname, _ in py._fields_:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, fname, cname, fname))
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.check_call([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = {}
+    for line in subprocess.check_output([str(exe)]).decode().splitlines():
+        a, b, v = line.split()
+        got[(a, b)] = int(v)
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
