@@ -417,9 +417,63 @@ def run_ours(args, dist):
                                 "evals_per_s": rate}
         line["evals_per_frame"] = {"schedule": per_frame, "counted": counted}
     s.close()
+    if dist.rank == 0 and dist.ws == 1 and args.batch_stills > 0:
+        line["batched"] = run_batched(args.batch_stills, args.batch_in_flight)
     if dist.rank == 0:
         print(json.dumps(line))
     return 0
+
+
+def batch_requests(n, seed=7):
+    """n independent stills with sizes drawn uniformly from 128x128 to
+    1024x1024, each with an exemplar of 256..1024 px (8 exemplars of the
+    configuration-0 generator, handed to the requests in turn), synthesised
+    with the configuration-0 settings: patch radius 2, 3 levels, 4
+    iterations.  Inputs and results are in page-locked host memory."""
+    from painttween_gb300 import host_array
+
+    def pinned(d):  # the client keeps its request data in page-locked memory
+        out = {}
+        for key, v in d.items():
+            if isinstance(v, np.ndarray):
+                out[key] = host_array(v.shape, v.dtype)
+                out[key][...] = v
+            else:
+                out[key] = v
+        return out
+    rng = np.random.default_rng(seed)
+    sizes = [256, 368, 480, 592, 704, 816, 912, 1024]
+    exs = [pinned(synthetic.make_exemplar(sz, sz, seed=100 + i)) for i, sz in enumerate(sizes)]
+    reqs = []
+    for i in range(n):
+        w, h = (int(v) for v in rng.integers(128, 1025, size=2))
+        p = synthetic.config("still256")["params"]
+        reqs.append(dict(params=p, style=exs[i % len(exs)],
+                         frames=[pinned(synthetic.make_still(w, h, 3, seed=1000 + i))]))
+    return reqs
+
+
+def run_batched(n, in_flight):
+    """Batched vs plain on the same GPU: the same requests through a server
+    (pt_server) one at a time and `in_flight` at a time (all arriving at
+    once), each after a warm-up run of the same requests.  Latency is each
+    request's service time, from admission to its results written."""
+    from painttween_gb300.serving import Server
+    reqs = batch_requests(n)
+    out = {"workload": "%d stills 128-1024 px, exemplars 256-1024 px, r2 / 3 levels / 4 iterations" % n,
+           "latency": "per-request service time (admission to results), ms"}
+    for name, k in (("plain", 1), ("batched", in_flight)):
+        srv = Server(max_in_flight=k)
+        srv.run(reqs, offsets=False, pinned=True)  # warm-up: the workers' contexts and memory caches
+        t0 = time.perf_counter()
+        res = srv.run(reqs, offsets=False, pinned=True)
+        wall = time.perf_counter() - t0
+        srv.close()
+        lat = np.array([r["done_ms"] - r["start_ms"] for r in res])
+        out[name] = {"in_flight": k, "requests_per_s": len(reqs) / wall, "p50_ms": float(np.percentile(lat, 50)),
+                     "p99_ms": float(np.percentile(lat, 99)), "wall_s": wall}
+    out["speedup"] = out["batched"]["requests_per_s"] / out["plain"]["requests_per_s"]
+    return out
 
 
 def main():
@@ -431,6 +485,8 @@ def main():
     ap.add_argument("--frames", type=int, default=0, help="override the clip length (testing only)")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-stills", type=int, default=64, help="requests of the batched-vs-plain run (0: skip)")
+    ap.add_argument("--batch-in-flight", type=int, default=8)
     args = ap.parse_args()
     dist = Dist()
     try:

@@ -373,6 +373,14 @@ typedef struct {
 
 pt_status pt_serve(int device, pt_request* requests, int count, int max_in_flight, size_t hbm_budget);
 
+/* The same as a server that keeps its worker contexts (device buffers,
+ * memory cache, CUDA streams) between runs, so that later runs skip their
+ * set-up: create once, run any number of request lists, destroy. */
+typedef struct pt_server pt_server;
+pt_status pt_server_create(int device, int max_in_flight, size_t hbm_budget, pt_server** out);
+pt_status pt_server_run(pt_server* server, pt_request* requests, int count);
+pt_status pt_server_destroy(pt_server* server);
+
 /* Number of this library's kernel launches issued so far by the context. */
 uint64_t pt_kernel_launches(const pt_ctx* ctx);
 

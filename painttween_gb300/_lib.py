@@ -67,6 +67,9 @@ SIGNATURES = {
     "pt_set_incremental": (_I, [_VP, _I]),
     "pt_get_frame_result": (_I, [_VP, _I, _VP, _VP]),
     "pt_serve": (_I, [_I, _VP, _I, _I, ctypes.c_size_t]),
+    "pt_server_create": (_I, [_I, _I, ctypes.c_size_t, ctypes.POINTER(_VP)]),
+    "pt_server_run": (_I, [_VP, _VP, _I]),
+    "pt_server_destroy": (_I, [_VP]),
     "pt_host_alloc": (_I, [ctypes.c_size_t, ctypes.POINTER(_VP)]),
     "pt_host_free": (_I, [_VP]),
     "pt_get_kernel_stats": (_I, [_VP, _I, ctypes.POINTER(_abi.KernelStats)]),

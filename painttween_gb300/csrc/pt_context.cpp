@@ -202,12 +202,21 @@ static void release_cache(pt_ctx* c) {
     c->cache.clear();
     c->cached = 0;
 }
+// Block sizes are rounded up to classes of 1/8 of a power of two (at most
+// 12.5 % larger than asked), so blocks are reused across nearby sizes.
+static size_t size_class(size_t bytes) {
+    if (bytes <= 4096) return (bytes + 255) & ~(size_t)255;
+    size_t top = 1;
+    while ((top << 1) <= bytes) top <<= 1;  // highest power of two <= bytes
+    const size_t step = top / 8;
+    return (bytes + step - 1) / step * step;
+}
 static pt_status dalloc(pt_ctx* c, void** p, size_t bytes) {
     *p = nullptr;
     if (bytes == 0) bytes = 16;
-    bytes = (bytes + 255) & ~(size_t)255;
-    auto it = c->cache.lower_bound(bytes);  // the smallest cached block that fits, if not much larger
-    if (it != c->cache.end() && it->first <= bytes + bytes / 8) {
+    bytes = size_class(bytes);
+    auto it = c->cache.find(bytes);  // a cached block of this class
+    if (it != c->cache.end()) {
         const size_t sz = it->first;
         *p = it->second;
         c->cache.erase(it);

@@ -1,7 +1,8 @@
-// pt_serve.cpp -- many synthesis requests on one GPU (pt_serve).
+// pt_serve.cpp -- many synthesis requests on one GPU (pt_server_*, pt_serve).
 //
-// Worker threads each own a context (its own device buffers and CUDA
-// stream) and take requests in arrival order.  A request is admitted once
+// Worker threads each use a context of the server (its own device buffers,
+// memory cache and CUDA stream, kept between runs) and take requests in
+// arrival order.  A request is admitted once
 // its arrival time has passed and its estimated device memory fits the
 // budget beside the requests in flight, so several requests' kernels run on
 // the GPU at once: a small still alone fills only a few of the GPU's 152
@@ -81,8 +82,36 @@ struct Queue {
 
 }  // namespace
 
-pt_status pt_serve(int device, pt_request* reqs, int count, int max_in_flight, size_t hbm_budget) {
-    if (count < 0 || (count > 0 && !reqs) || max_in_flight < 1) return PT_ERR_INVALID;
+struct pt_server {
+    int device = 0;
+    int max_in_flight = 1;
+    size_t budget = 0;
+    std::vector<pt_ctx*> ctxs;  // one per worker, created on first use and kept
+};
+
+pt_status pt_server_create(int device, int max_in_flight, size_t hbm_budget, pt_server** out) {
+    if (!out || max_in_flight < 1) return PT_ERR_INVALID;
+    pt_server* s = new pt_server;
+    s->device = device;
+    s->max_in_flight = max_in_flight;
+    s->budget = hbm_budget;
+    s->ctxs.assign(max_in_flight, nullptr);
+    *out = s;
+    return PT_OK;
+}
+
+pt_status pt_server_destroy(pt_server* s) {
+    if (!s) return PT_ERR_INVALID;
+    for (pt_ctx* c : s->ctxs)
+        if (c) pt_destroy(c);
+    delete s;
+    return PT_OK;
+}
+
+pt_status pt_server_run(pt_server* srv, pt_request* reqs, int count) {
+    if (!srv || count < 0 || (count > 0 && !reqs)) return PT_ERR_INVALID;
+    const int device = srv->device, max_in_flight = srv->max_in_flight;
+    const size_t hbm_budget = srv->budget;
     for (int i = 0; i < count; i++) {
         reqs[i].status = PT_ERR_STATE;  // not run
         reqs[i].start_ms = reqs[i].done_ms = 0.0;
@@ -96,9 +125,9 @@ pt_status pt_serve(int device, pt_request* reqs, int count, int max_in_flight, s
     const int workers = std::min(max_in_flight, std::max(count, 1));
     std::vector<std::thread> pool;
     for (int w = 0; w < workers; w++) {
-        pool.emplace_back([&]() {
-            pt_ctx* c = nullptr;
-            const pt_status created = pt_create(device, 0, &c);
+        pool.emplace_back([&, w]() {
+            pt_ctx*& c = srv->ctxs[w];
+            const pt_status created = c ? PT_OK : pt_create(device, 0, &c);
             for (;;) {
                 int idx = -1;
                 size_t est = 0;
@@ -137,11 +166,19 @@ pt_status pt_serve(int device, pt_request* reqs, int count, int max_in_flight, s
                 }
                 q.cv.notify_all();
             }
-            if (c) pt_destroy(c);
         });
     }
     for (auto& t : pool) t.join();
     for (int i = 0; i < count; i++)
         if (reqs[i].status != PT_OK) return reqs[i].status;
     return PT_OK;
+}
+
+pt_status pt_serve(int device, pt_request* reqs, int count, int max_in_flight, size_t hbm_budget) {
+    pt_server* s = nullptr;
+    pt_status st = pt_server_create(device, max_in_flight, hbm_budget, &s);
+    if (st != PT_OK) return st;
+    st = pt_server_run(s, reqs, count);
+    pt_server_destroy(s);
+    return st;
 }

@@ -79,3 +79,16 @@ def test_arrivals_and_budget_admission():
     spans = sorted((r["start_ms"], r["done_ms"]) for r in res)
     for (s0, d0), (s1, d1) in zip(spans, spans[1:]):
         assert s1 >= d0
+
+
+def test_server_keeps_contexts_between_runs():
+    from painttween_gb300.serving import Server
+    reqs = _mix()
+    ref = serve(reqs, max_in_flight=3)
+    with Server(max_in_flight=3) as srv:
+        for run in range(2):
+            got = srv.run(reqs)
+            for i, (a, m) in enumerate(zip(ref, got)):
+                for f in range(a["rgba"].shape[0]):
+                    assert_offsets_equal(m["offsets"][f], a["offsets"][f], 1.0, "run %d request %d" % (run, i))
+                    assert_array_equal(m["rgba"][f], a["rgba"][f], "run %d request %d output" % (run, i))
