@@ -547,7 +547,10 @@ __device__ __forceinline__ float tap_value(const Params& P, const TileSmem<R, TM
 // the taps of column e.col added to e.sum in the reference's order.  ROLL
 // keeps the column's taps in a loop (a smaller body: faster for scatter,
 // whose chain code competes for the instruction cache; propagate unrolls).
-template <int R, int TM, bool ROLL>
+// EE: a lane leaves the column as soon as its sum reaches e.thr2 (the sum
+// only grows, so stopping at any tap gives the decision of stopping at the
+// column's end), and the loads of its remaining taps are not issued.
+template <int R, int TM, bool ROLL, bool EE>
 __device__ __forceinline__ float lane_column(const Params& P, const TileSmem<R, TM>& T, const LanePix& q,
                                              const LaneEval& e, bool fast, bool fastp) {
     const int i = e.col;
@@ -560,6 +563,7 @@ __device__ __forceinline__ float lane_column(const Params& P, const TileSmem<R, 
         const float res = tap_value<R, TM>(P, T, q, e, i, j, fast, fastp);
         const float w = gi * P.gauss[j + R];
         sum = valid ? fmaf(res, w, sum) : sum;
+        if (EE && sum >= e.thr2) break;
     }
     return sum;
 }
@@ -577,7 +581,7 @@ __device__ __forceinline__ unsigned lane_taps(const LanePix& q, int cols) {
 template <int R, int TM, bool EE, bool ROLL>
 __device__ __forceinline__ bool lane_step(const Params& P, const TileSmem<R, TM>& T, const LanePix& q, LaneEval& e,
                                           bool fast, bool fastp, float* r) {
-    e.sum = lane_column<R, TM, ROLL>(P, T, q, e, fast, fastp);
+    e.sum = lane_column<R, TM, ROLL, EE>(P, T, q, e, fast, fastp);
     e.col++;
     const bool stop = EE && e.sum >= e.thr2;
     if (!stop && e.col <= R) return false;
