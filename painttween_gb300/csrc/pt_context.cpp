@@ -326,6 +326,15 @@ static Params make_params(pt_ctx* c, int level) {
         for (int i = 0; i < 2 * P.r + 1; i++) nonneg = nonneg && P.gauss[i] >= 0.f;
         P.earlyExit = nonneg ? 1 : 0;
     }
+    if (P.r <= 4) {
+        // taps by descending weight (the weights as the kernels form them)
+        const int n = 2 * P.r + 1, K = n * n;
+        std::vector<std::pair<float, int>> order;
+        for (int t = 0; t < K; t++) order.push_back(std::make_pair(P.gauss[t / n] * P.gauss[t % n], t));
+        std::stable_sort(order.begin(), order.end(),
+                         [](const std::pair<float, int>& a, const std::pair<float, int>& b) { return a.first > b.first; });
+        for (int k = 0; k < K; k++) P.tapOrder[k] = (uint8_t)order[k].second;
+    }
     P.jitter = p.advectionJitter;
     P.numStyles = p.numStyles > 0 ? p.numStyles : 1;
     P.transparencyOk = p.transparencyOk;

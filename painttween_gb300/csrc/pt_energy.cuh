@@ -396,6 +396,16 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_residual(const Params P, f
 // ---------------------------------------------------------------------------
 
 constexpr unsigned kFull = 0xffffffffu;
+// (1 -/+ 2^-17): bounds of the rounding of a reference-order sum of <= 81 terms
+constexpr float kBoundLo = 1.0f - 1.0f / 131072.0f;
+constexpr float kBoundHi = 1.0f + 1.0f / 131072.0f;
+// Groups of 2R+1 taps of propagate's bound pass: none.  Propagate's
+// candidates come from coherent neighbours, so their energies are mostly
+// close to the best and a bound pass rarely rejects them before its end
+// (measured: 1 or 2 groups +45-53 %, the full pass +20 % propagate time);
+// scatter's random-search candidates are rejected after a few heavy taps
+// (full bound pass: -45 % scatter time).
+constexpr int kPropagateBoundGroups = 0;
 
 // pixel side of an evaluation
 struct LanePix {
@@ -413,10 +423,32 @@ struct LaneEval {
     float cx, cy, sv;
     int layer;
     float2 b0, b1;
-    bool fast;  // footprint inside the exemplar
-    int col;    // next column, -R..R
-    float sum, thr2;
+    bool fast;   // footprint inside the exemplar
+    bool exact;  // the reference-order pass (else the bound pass)
+    int col;     // exact pass: next column, -R..R; bound pass: next position in the weight order
+    float sum;   // exact pass: the running sum; bound pass: the lower bound of the weighted taps so far
+    float thr2;  // exit threshold (see exit_threshold)
+    float s0lo;  // lower bound of the start sum's share of the reference-order sum
 };
+
+// The taps of the window by descending weight, with their weights, for the
+// bound pass; filled once per block from Params::tapOrder.
+template <int R>
+struct TapTable {
+    uint8_t ij[(2 * R + 1) * (2 * R + 1)];  // (i + R) | (j + R) << 4
+    float w[(2 * R + 1) * (2 * R + 1)];
+};
+template <int R>
+__device__ __forceinline__ void load_tap_table(const Params& P, TapTable<R>& TT) {
+    constexpr int n = 2 * R + 1, K = n * n;
+    const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+    if (tid < K) {
+        const int t = P.tapOrder[tid];
+        const int i = t / n, j = t % n;
+        TT.ij[tid] = (uint8_t)(i | (j << 4));
+        TT.w[tid] = P.gauss[i] * P.gauss[j];
+    }
+}
 
 template <int R>
 __device__ __forceinline__ LanePix lane_pix(const Params& P, const PixT& px) {
@@ -475,9 +507,15 @@ __device__ __forceinline__ void lane_start(const Params& P, const LanePix& q, fl
     e->cx = cx; e->cy = cy; e->sv = sv; e->layer = layer;
     basis(theta, P.scaleWU * su, P.scaleWV * sv, &e->b0, &e->b1);
     e->fast = footprint_inside<R>(cx, cy, e->b0, e->b1, P.ex.w, P.ex.h);
-    e->col = -R;
-    e->sum = q.sum0;
     e->thr2 = (P.earlyExit && q.sumW >= kEpsilon) ? __fmul_ru(best, q.sumW) : kNoBest;
+    // With an exit threshold, a bound pass over the taps by descending
+    // weight comes first (see lane_step); without one, or with one so small
+    // (|thr2| < 2^-100) that subnormal rounding could matter, only the exact
+    // pass.
+    e->exact = !(fabsf(e->thr2) >= 0x1p-100f);
+    e->col = e->exact ? -R : 0;
+    e->sum = e->exact ? q.sum0 : 0.0f;
+    e->s0lo = q.sum0 >= 0.0f ? __fmul_rd(q.sum0, kBoundLo) : __fmul_rd(q.sum0, kBoundHi);
 }
 
 // calculateResidual's value at tap (i, j) of candidate e at pixel q, before
@@ -575,12 +613,67 @@ __device__ __forceinline__ unsigned lane_taps(const LanePix& q, int cols) {
     return last < q.imin ? 0u : (unsigned)((last - q.imin + 1) * (q.jmax - q.jmin + 1));
 }
 
-// One step of a lane: a column of its candidate; returns true when the
+// One step of a lane: 2R+1 taps of its candidate; returns true when the
 // candidate is finished, with its energy in *r (kBigResidual where the tap
-// weights sum below kEpsilon, +inf where it stopped early).
-template <int R, int TM, bool EE, bool ROLL>
-__device__ __forceinline__ bool lane_step(const Params& P, const TileSmem<R, TM>& T, const LanePix& q, LaneEval& e,
-                                          bool fast, bool fastp, float* r) {
+// weights sum below kEpsilon, +inf where it was rejected early).
+//
+// With an exit threshold a candidate first takes a bound pass: its taps by
+// descending weight (TT), accumulating a lower bound of the weighted sum with
+// round-down products and sums.  The reference forms its sum in tap order
+// with round-to-nearest fmaf over at most 81 non-negative terms, which is at
+// least (1 - 2^-17) times the exact sum of those terms, plus its start sum
+// (the hysteresis term, <= 0) scaled by at most (1 + 2^-17).  So once
+// (1 - 2^-17) * bound + that start-sum share, rounded down, reaches
+// thr2 = best * sumW rounded up, the reference-order energy is >= best and
+// the strict "<" rejects the candidate.  The heavy central taps come first,
+// so a rejection needs a few taps instead of several columns.  A candidate
+// the bound pass does not reject (a winner or a near tie) then takes the
+// exact pass: its sum in the reference's tap order, as calculateResidual
+// forms it (texSynth_kernel.cu:537-659), exiting early on the exact sum.
+// BC bounds the bound pass to its first BC groups of 2R+1 taps (the exact
+// pass follows a candidate it has not rejected by then): candidates whose
+// energy is often close to the best (propagate's) pay the bound pass without
+// being rejected by it.
+template <int R, int TM, bool EE, bool ROLL, int BC>
+__device__ __forceinline__ bool lane_step(const Params& P, const TileSmem<R, TM>& T, const TapTable<R>& TT,
+                                          const LanePix& q, LaneEval& e, bool fast, bool fastp, float* r) {
+    constexpr int K = (2 * R + 1) * (2 * R + 1);
+    constexpr int KB = BC * (2 * R + 1) < K ? BC * (2 * R + 1) : K;  // taps of the bound pass at most
+    if (!e.exact && KB == 0) {
+        e.exact = true;
+        e.col = -R;
+        e.sum = q.sum0;
+    }
+    if (EE && KB > 0 && !e.exact) {
+        bool rejected = false;
+#pragma unroll(ROLL ? 1 : 2 * R + 1)
+        for (int k = 0; k < 2 * R + 1; k++) {
+            const int pos = e.col + k;
+            if (pos >= KB) break;
+            const int ij = TT.ij[pos];
+            const int i = (ij & 15) - R, j = (ij >> 4) - R;
+            const bool valid = (i >= q.imin) && (i <= q.imax) && (j >= q.jmin) && (j <= q.jmax);
+            const float res = tap_value<R, TM>(P, T, q, e, i, j, fast, fastp);
+            e.sum = valid ? __fadd_rd(e.sum, __fmul_rd(res, TT.w[pos])) : e.sum;
+            if (__fadd_rd(__fmul_rd(e.sum, kBoundLo), e.s0lo) >= e.thr2) {
+                rejected = true;
+                break;
+            }
+        }
+        e.col += 2 * R + 1;
+        if (rejected) {
+            if (P.counters) count_taps(P, (unsigned)min(e.col, K), q.temporal);
+            *r = INFINITY;
+            return true;
+        }
+        if (e.col >= KB) {  // not rejected: the exact pass
+            if (P.counters) count_taps(P, (unsigned)KB, q.temporal);
+            e.exact = true;
+            e.col = -R;
+            e.sum = q.sum0;
+        }
+        return false;
+    }
     e.sum = lane_column<R, TM, ROLL, EE>(P, T, q, e, fast, fastp);
     e.col++;
     const bool stop = EE && e.sum >= e.thr2;
@@ -617,6 +710,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P
     __shared__ TileSmem<R, TM> T;
     __shared__ PixShared S;
     __shared__ PropQueue Q;
+    __shared__ TapTable<R> TT;
     // Change tracking: a candidate whose source record and whose target's
     // patch window are unchanged since the previous pass with this jump was
     // rejected there against the same residual and is skipped (bit cdx of
@@ -640,6 +734,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P
     }
     const int pid = threadIdx.x + threadIdx.y * kTileW;
     if (pid < kTileH) { Q.count[pid] = 0; Q.next[pid] = 0; }
+    load_tap_table<R>(P, TT);
     PixT px;
     const bool in = stage_tile<R, TM>(P, T, &px);  // (synchronises the block)
     // phase 1: each pixel builds its candidates (the reference's order,
@@ -753,7 +848,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P
             const bool fastp = TM ? __all_sync(kFull, !act || !q.temporal || q.prev_fast) : true;
             if (act) {
                 float r;
-                if (lane_step<R, TM, true, false>(P, T, q, e, fast, fastp, &r)) {
+                if (lane_step<R, TM, true, false, kPropagateBoundGroups>(P, T, TT, q, e, fast, fastp, &r)) {
                     Q.ca[cur].x = r;
                     act = false;
                 }
@@ -809,6 +904,8 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter_q(const Params P, 
         stable = in && P.inc.prev != INT_MIN && __ldg(P.inc.win + k) < P.inc.prev;
         if (block_idle(P, work, in && !stable, in, k, write_all != 0)) return;
     }
+    __shared__ TapTable<R> TT;
+    load_tap_table<R>(P, TT);
     PixT px;
     const bool in = stage_tile<R, TM>(P, T, &px);  // (synchronises the block)
     const int x = px.x, y = px.y;
@@ -932,7 +1029,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter_q(const Params P, 
         const bool fastp = TM ? __all_sync(kFull, !act || !q.temporal || q.prev_fast) : true;
         if (act) {
             float r;
-            if (lane_step<R, TM, true, true>(P, T, q, e, fast, fastp, &r)) {
+            if (lane_step<R, TM, true, true, 2 * R + 1>(P, T, TT, q, e, fast, fastp, &r)) {
                 if (r < best) {
                     best = r;
                     owx = e.cx; owy = e.cy; owt = cur_t; wkind = cur_avg ? 2 : 1;

@@ -120,6 +120,9 @@ struct Params {
     AdvView adv[2];            // [0] = forward, [1] = backward
     unsigned long long* counters;  // profiling: energy evaluations, taps, temporal taps (null = off)
     int earlyExit;             // every per-tap term is >= 0 (all weights >= 0): candidates may stop early
+    // the taps of a patch window of radius <= 4 by descending weight (ties in
+    // the reference's order), tap t = (i + r) * (2r + 1) + (j + r)
+    uint8_t tapOrder[81];
     IncView inc;
 };
 
