@@ -482,3 +482,24 @@ def test_frame_results_into_page_locked_memory():
             assert_array_equal(a, ref[f][0], "pinned output frame %d" % f)
     finally:
         s.close()
+
+
+def test_near_ties_match_oracle():
+    """An exemplar whose colours differ by ~1e-5 makes many candidates tie or
+    nearly tie with the best: scatter's bound pass must leave every such
+    candidate to the exact reference-order sum (checked against the oracle
+    on every byte)."""
+    p = config_params(r=3, levels=2, iterations=3)
+    p.temporalCoherenceWeight = 0.5
+    ex = synthetic.make_exemplar(64, 64, seed=97)
+    rng = np.random.default_rng(98)
+    for key in ("base", "output"):
+        a = ex[key].copy()
+        a[..., :3] = 0.5 + 1e-5 * np.round(rng.standard_normal(a[..., :3].shape), 1)
+        ex[key] = a.astype(np.float32)
+    clip = synthetic.make_clip(80, 64, 3, 2, seed=99)
+    got = _animate(p, ex, clip, 80, 64)
+    ref = O.OracleDriver(p, [ex], clip, threads=8).render(0, 1)
+    for f in range(2):
+        assert_offsets_equal(got[f][1], ref[f][0], 1.0, "near ties frame %d" % f)
+        assert_array_equal(got[f][0], ref[f][2], "near ties output frame %d" % f)
