@@ -41,10 +41,10 @@ UNIT = "frames/s"
 
 # DRAM bytes (read + write) per level pixel of one kt_propagate_q launch: the
 # ncu capture of a level-0 temporal launch of this workload (1920x1080 level,
-# 333.6 MB read + 64.9 MB written) summarised in
+# 340.1 MB read + 64.9 MB written) summarised in
 # profiles/kt_energy_kernels_clip1080p.md.  The exemplar planes stay in L2,
 # so DRAM traffic follows the staged pixel-side planes, i.e. the level area.
-PROPAGATE_DRAM_BYTES_PER_PIXEL = (333.572608e6 + 64.884736e6) / (1920 * 1080)
+PROPAGATE_DRAM_BYTES_PER_PIXEL = (340.1e6 + 64.9e6) / (1920 * 1080)
 
 
 def peaks():
