@@ -450,6 +450,27 @@ class OracleDriver:
         lib().pto_copy_base_to_working(self.o.h)
 
     def render(self, first, last):
+        """SynthesisProcessor::renderAnimation, synthesisProcessor.cpp:769-805:
+        the FMBM schemes (renderAnimationFMBM) or IND (renderAnimationIND)."""
+        if self.user.scheme == _abi.S_IND:
+            return self._render_ind(first, last)
+        return self._render_fmbm(first, last)
+
+    def _render_ind(self, first, last):
+        """renderAnimationIND, synthesisProcessor.cpp:807-844: every frame on
+        its own, coarse to fine, each pass a first frame going forwards."""
+        total = self.user.fixupPasses + 1
+        for f in range(first, last + 1):
+            for level in range(self.levels - 1, self.user.finalLevel - 1, -1):
+                self.o.load_style_level(self.styles, level)
+                self.o.reset_advected()
+                for pass_ in range(total):
+                    self.o.load_frame_level(self.frames[f], level)
+                    self.synthesize_consecutive(f, level, pass_, True, True, pass_, pass_ == 0)
+        final_pass = total - 1 if self.user.finalLevel == 0 else 0
+        return {f: self.store[(self.user.finalLevel, f, final_pass)] for f in range(first, last + 1)}
+
+    def _render_fmbm(self, first, last):
         """renderAnimationFMBM, synthesisProcessor.cpp:846-878."""
         total = self.user.fixupPasses + 1
         for level in range(self.levels - 1, self.user.finalLevel - 1, -1):

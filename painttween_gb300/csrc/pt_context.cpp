@@ -73,6 +73,8 @@ struct StoreEntry {
 
 }  // namespace
 
+constexpr int kSpanNone = 1 << 20;  // a level coarser than any image has
+
 struct pt_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -92,6 +94,13 @@ struct pt_ctx {
 
     PatchPlanes off[2]{};
     int base_i = 0, work_i = 0;
+    // The two offset buffers hold the same records outside the rectangle of
+    // level `off_span` (kSpanNone: everywhere).  Kernels write only inside
+    // their level's rectangle, so when a coarser level follows a finer one
+    // (the IND scheme's next frame) the buffer that becomes the working one
+    // must first be made whole: propagate reads records outside a coarse
+    // rectangle, and upsample keeps the working buffer's border.
+    int off_span = 0;
     float* res[2] = {nullptr, nullptr};
     int res_i = 0;
     float4* canvas = nullptr;
@@ -402,11 +411,6 @@ static pt_status check_ready(pt_ctx* c, int level, bool need_ex = true, bool nee
 }
 
 // copy-on-write helpers for the offsets pair
-static PatchPlanes writable_work(pt_ctx* c, bool* was_aliased) {
-    if (was_aliased) *was_aliased = (c->work_i == c->base_i);
-    if (c->work_i == c->base_i) c->work_i = 1 - c->base_i;
-    return c->off[c->work_i];
-}
 static pt_status copy_planes_full(pt_ctx* c, PatchPlanes dst, PatchPlanes src) {
     size_t n = (size_t)c->W * c->H;
     CU(cudaMemcpyAsync(dst.A, src.A, n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
@@ -414,20 +418,50 @@ static pt_status copy_planes_full(pt_ctx* c, PatchPlanes dst, PatchPlanes src) {
     CU(cudaMemcpyAsync(dst.C, src.C, n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
     return PT_OK;
 }
+// The shared buffer of an aliased pair is about to be split for a write
+// inside the rectangle of `level`: the other buffer is taken as it is when
+// it already holds the same records outside that rectangle, else after a
+// full copy.
+static pt_status split_aliased(pt_ctx* c, int level) {
+    const int other = 1 - c->base_i;
+    if (c->off_span < level) {
+        TRY(copy_planes_full(c, c->off[other], c->off[c->base_i]));
+        c->off_span = kSpanNone;
+    }
+    c->off_span = std::min(c->off_span, level);
+    return PT_OK;
+}
+static pt_status writable_work(pt_ctx* c, int level, PatchPlanes* out, bool* was_aliased = nullptr) {
+    if (was_aliased) *was_aliased = (c->work_i == c->base_i);
+    if (c->work_i == c->base_i) {
+        TRY(split_aliased(c, level));
+        c->work_i = 1 - c->base_i;
+    }
+    c->off_span = std::min(c->off_span, level);
+    *out = c->off[c->work_i];
+    return PT_OK;
+}
 // base about to be partly overwritten: give it its own buffer first
-static pt_status base_for_partial_write(pt_ctx* c, PatchPlanes* out) {
+static pt_status base_for_partial_write(pt_ctx* c, int level, PatchPlanes* out) {
     if (c->base_i == c->work_i) {
         int nb = 1 - c->work_i;
         TRY(copy_planes_full(c, c->off[nb], c->off[c->work_i]));
         c->base_i = nb;
+        c->off_span = kSpanNone;
     }
+    c->off_span = std::min(c->off_span, level);
     *out = c->off[c->base_i];
     return PT_OK;
 }
 // base about to be overwritten on the whole level rectangle
-static PatchPlanes base_for_full_write(pt_ctx* c) {
-    if (c->base_i == c->work_i) c->base_i = 1 - c->work_i;
-    return c->off[c->base_i];
+static pt_status base_for_full_write(pt_ctx* c, int level, PatchPlanes* out) {
+    if (c->base_i == c->work_i) {
+        TRY(split_aliased(c, level));
+        c->base_i = 1 - c->work_i;
+    }
+    c->off_span = std::min(c->off_span, level);
+    *out = c->off[c->base_i];
+    return PT_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -800,6 +834,7 @@ pt_status pt_initialize(pt_ctx* c, int iw, int ih, int sw, int sh, int ns) {
     CU(cudaMemsetAsync(c->stamp_win, 0, n * sizeof(int), c->stream));
     c->inc_seq = 0;
     c->base_i = c->work_i = 0;
+    c->off_span = 0;  // fresh buffers: nothing known to agree
     c->res_i = 0;
     memset(&c->img, 0, sizeof(c->img));
     c->initialized = true;
@@ -820,6 +855,7 @@ static pt_status reset_working(pt_ctx* c) {
     c->hist_zero = true;
     CU(cudaMemsetAsync(c->canvas, 0, n * sizeof(float4), c->stream));
     c->base_i = c->work_i = 0;
+    c->off_span = kSpanNone;  // both buffers all zero
     c->res_i = 0;
     c->pass_counter = 0;
     return pt_reset_advected_buffers(c);
@@ -1052,7 +1088,8 @@ pt_status pt_randomize_offsets(pt_ctx* c, int level) {
     if (!c) return PT_ERR_INVALID;
     TRY(check_ready(c, level));
     if (!c->img.rnd.p) return fail(c, PT_ERR_STATE, "no random level");
-    PatchPlanes work = writable_work(c, nullptr);
+    PatchPlanes work;
+    TRY(writable_work(c, level, &work));
     Params P = make_params(c, level);
     LN(pt::launch_random_offsets(P, work, c->stream));
     return do_sync(c, level, 0);
@@ -1060,7 +1097,8 @@ pt_status pt_randomize_offsets(pt_ctx* c, int level) {
 
 // one propagate pass into the working buffer
 static pt_status propagate_pass(pt_ctx* c, int level, int jump) {
-    PatchPlanes work = writable_work(c, nullptr);
+    PatchPlanes work;
+    TRY(writable_work(c, level, &work));
     Params P = make_params(c, level);
     return profiled(c, PT_KERNEL_PROPAGATE, P, [&](const Params& Q) {
         bool done = false;
@@ -1071,7 +1109,8 @@ static pt_status propagate_pass(pt_ctx* c, int level, int jump) {
 
 static pt_status scatter_pass(pt_ctx* c, int level) {
     bool aliased = false;
-    PatchPlanes work = writable_work(c, &aliased);
+    PatchPlanes work;
+    TRY(writable_work(c, level, &work, &aliased));
     Params P = make_params(c, level);
     uint32_t pass_id = c->pass_counter++;
     return profiled(c, PT_KERNEL_SCATTER, P, [&](const Params& Q) {
@@ -1102,7 +1141,8 @@ pt_status pt_upsample(pt_ctx* c, int fine_level) {
     TRY(check_ready(c, fine_level));
     bool aliased = false;
     PatchPlanes old_base = base_planes(c);
-    PatchPlanes work = writable_work(c, &aliased);
+    PatchPlanes work;
+    TRY(writable_work(c, fine_level, &work, &aliased));
     Params P = make_params(c, fine_level);
     float* res_out = c->res[1 - c->res_i];
     LN(pt::launch_upsample(P, work, old_base, aliased ? 1 : 0, res_out, c->stream));
@@ -1121,7 +1161,8 @@ pt_status pt_advect_offsets(pt_ctx* c, int level, int time_step, int forwards, i
     Params P = make_params(c, level);
     LN(pt::launch_advect(P, d, forwards ? 1 : 0, time_step, flags, c->stream));
     c->adv_written[d] = true;
-    PatchPlanes dst = base_for_full_write(c);
+    PatchPlanes dst;
+    TRY(base_for_full_write(c, level, &dst));
     P = make_params(c, level);
     LN(pt::launch_copy_patch(P, dst, c->adv[d].off, c->stream));
     TRY(do_sync(c, level, PT_DONT_COPY_OFFSETS | PT_DONT_UPDATE_RESIDUAL));
@@ -1135,7 +1176,8 @@ pt_status pt_merge_randomly(pt_ctx* c, int level, int forwards, float weight, in
     if (!c) return PT_ERR_INVALID;
     TRY(check_ready(c, level));
     if (!c->img.rnd.p) return fail(c, PT_ERR_STATE, "no random level");
-    PatchPlanes work = writable_work(c, nullptr);
+    PatchPlanes work;
+    TRY(writable_work(c, level, &work));
     Params P = make_params(c, level);
     LN(pt::launch_merge_random(P, forwards ? 0 : 1, forwards ? 1 : 0, weight, force_valid ? 1 : 0, work, c->stream));
     return do_sync(c, level, 0);
@@ -1144,7 +1186,8 @@ pt_status pt_merge_randomly(pt_ctx* c, int level, int forwards, float weight, in
 pt_status pt_merge_using_residual(pt_ctx* c, int level, int forwards) {
     if (!c) return PT_ERR_INVALID;
     TRY(check_ready(c, level));
-    PatchPlanes work = writable_work(c, nullptr);
+    PatchPlanes work;
+    TRY(writable_work(c, level, &work));
     Params P = make_params(c, level);
     LN(pt::launch_merge_residual(P, forwards ? 0 : 1, work, c->stream));
     return do_sync(c, level, 0);
@@ -1171,7 +1214,7 @@ pt_status pt_load_offsets(pt_ctx* c, int level, const pt_patchxf* offs) {
     TRY(ensure_stage(c, n * sizeof(pt_patchxf)));
     TRY(h2d(c, c->stage, offs, n * sizeof(pt_patchxf)));
     PatchPlanes dst;
-    TRY(base_for_partial_write(c, &dst));
+    TRY(base_for_partial_write(c, level, &dst));
     Params P = make_params(c, level);
     LN(pt::launch_unpack_patch(P, (const pt_patchxf*)c->stage, dst, c->stream));
     return PT_OK;
@@ -1545,7 +1588,7 @@ static pt_status store_load_offsets(pt_ctx* c, int level, int frame, int pass) {
     auto it = c->store.find(std::make_tuple(level, frame, pass));
     if (it == c->store.end()) return fail(c, PT_ERR_STATE, "no saved offsets for level %d frame %d pass %d", level, frame, pass);
     PatchPlanes dst;
-    TRY(base_for_partial_write(c, &dst));
+    TRY(base_for_partial_write(c, level, &dst));
     Params P = make_params(c, level);
     LN(pt::launch_unpack_patch(P, it->second.offs, dst, c->stream));
     return PT_OK;
@@ -1661,14 +1704,54 @@ static pt_status synthesize_consecutive(pt_ctx* c, const pt_params& user, int fr
 
 // SynthesisProcessor::renderAnimationFMBM + renderConsecutivePass,
 // synthesisProcessor.cpp:703-753,846-878
+// frees the saved states of `level`
+static void drop_store_level(pt_ctx* c, int level) {
+    for (auto it = c->store.begin(); it != c->store.end();) {
+        if (std::get<0>(it->first) == level) {
+            dfree_t(c, it->second.offs); dfree_t(c, it->second.res); dfree_t(c, it->second.canvas);
+            it = c->store.erase(it);
+        } else {
+            ++it;
+        }
+    }
+}
+
+// SynthesisProcessor::renderAnimationIND, synthesisProcessor.cpp:807-844:
+// every frame synthesised on its own, coarse to fine, each pass through
+// synthesizeConsecutive as a first frame going forwards
+static pt_status render_ind(pt_ctx* c, int first, int last) {
+    const pt_params user = c->params;
+    TRY(reset_working(c));
+    c->img.cur = 0;
+    free_store(c);
+    const int total = user.fixupPasses + 1;
+    const int final_pass = (user.finalLevel == 0) ? total - 1 : 0;
+    for (int f = first; f <= last; f++) {
+        for (int level = user.levels - 1; level >= user.finalLevel; level--) {
+            TRY(bind_style_level(c, level));
+            TRY(pt_reset_advected_buffers(c));
+            for (int pass = 0; pass < total; pass++) {
+                const bool save_canvas = (level == user.finalLevel && pass == final_pass);
+                TRY(bind_frame_level(c, f, level));
+                TRY(synthesize_consecutive(c, user, f, level, pass, true, true, pass, pass == 0, save_canvas));
+            }
+            // the coarser level is no longer needed (earlier frames are done)
+            if (level + 1 < user.levels) drop_store_level(c, level + 1);
+        }
+    }
+    c->params = user;
+    return PT_OK;
+}
+
 static pt_status render_fmbm(pt_ctx* c, int first, int last) {
     const pt_params user = c->params;
-    if (user.scheme != PT_S_FMBM && user.scheme != PT_S_FMBM_RM)
-        return fail(c, PT_ERR_UNSUPPORTED, "only the FMBM schemes are implemented");
     if (user.levels < 1 || user.finalLevel < 0 || user.finalLevel >= user.levels)
         return fail(c, PT_ERR_INVALID, "bad levels/finalLevel");
     for (int f = first; f <= last; f++)
         if (!c->frames.count(f)) return fail(c, PT_ERR_STATE, "frame %d not set", f);
+    if (user.scheme == PT_S_IND) return render_ind(c, first, last);
+    if (user.scheme != PT_S_FMBM && user.scheme != PT_S_FMBM_RM)
+        return fail(c, PT_ERR_UNSUPPORTED, "the FBMO and TCTF schemes are not implemented");
     TRY(reset_working(c));
     c->img.cur = 0;
     free_store(c);
@@ -1696,16 +1779,7 @@ static pt_status render_fmbm(pt_ctx* c, int first, int last) {
             }
         }
         // the coarser level's saved state is no longer needed
-        if (level + 1 < user.levels) {
-            for (auto it = c->store.begin(); it != c->store.end();) {
-                if (std::get<0>(it->first) == level + 1) {
-                    dfree_t(c, it->second.offs); dfree_t(c, it->second.res); dfree_t(c, it->second.canvas);
-                    it = c->store.erase(it);
-                } else {
-                    ++it;
-                }
-            }
-        }
+        if (level + 1 < user.levels) drop_store_level(c, level + 1);
     }
     c->params = user;
     return PT_OK;

@@ -503,3 +503,17 @@ def test_near_ties_match_oracle():
     for f in range(2):
         assert_offsets_equal(got[f][1], ref[f][0], 1.0, "near ties frame %d" % f)
         assert_array_equal(got[f][0], ref[f][2], "near ties output frame %d" % f)
+
+
+def test_ind_scheme_matches_oracle():
+    """The IND scheme (every frame on its own) against the oracle."""
+    p = config_params(r=3, levels=2, iterations=2)
+    p.scheme = _abi.S_IND
+    p.temporalCoherenceWeight = 0.5
+    ex = synthetic.make_exemplar(64, 64, seed=63)
+    clip = synthetic.make_clip(80, 64, 3, 3, seed=64)
+    got = _animate(p, ex, clip, 80, 64)
+    ref = O.OracleDriver(p, [ex], clip, threads=8).render(0, 2)
+    for f in range(3):
+        assert_offsets_equal(got[f][1], ref[f][0], 1.0, "IND frame %d" % f)
+        assert_array_equal(got[f][0], ref[f][2], "IND output frame %d" % f)

@@ -141,3 +141,21 @@ def test_animation_oracle_runs():
     assert sorted(res) == [0, 1, 2]
     for f in res:
         assert np.isfinite(res[f][2]).all()
+
+
+def test_ind_scheme_equals_fmbm_on_a_still():
+    """For one frame and no fix-up passes renderAnimationIND and
+    renderAnimationFMBM run the same steps (one forward pass of a first frame
+    per level), so they agree on every byte.  (Across frames IND's frames are not independent: as in the
+    reference, propagate's level-0 wrap reads offsets that earlier frames left
+    outside a coarse level's rectangle.)"""
+    ex = synthetic.make_exemplar(48, 48, seed=61)
+    fr = synthetic.make_still(56, 40, 3, seed=62)
+    out = []
+    for scheme in (_abi.S_IND, _abi.S_FMBM_RM):
+        p = _abi.default_params()
+        p.residualWindowSize, p.levels, p.iterations = 2, 2, 2
+        p.scheme, p.fixupPasses = scheme, 0
+        out.append(O.OracleDriver(p, [ex], [fr], threads=4).render(0, 0)[0])
+    assert (out[0][0].view(np.uint8) == out[1][0].view(np.uint8)).all()
+    assert np.array_equal(out[0][2], out[1][2])
