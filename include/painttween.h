@@ -230,6 +230,10 @@ pt_status pt_merge_using_residual(pt_ctx* ctx, int level, int forwards); /* :197
 pt_status pt_update_residual_cache(pt_ctx* ctx, int level);       /* :1221 */
 pt_status pt_sync_buffers(pt_ctx* ctx, int level, int op_flags);  /* :1240 */
 pt_status pt_reset_advected_buffers(pt_ctx* ctx); /* workingBuffers.cpp:112-116 */
+/* offsets.base().copyTo(advectedF/B.offsets()) and
+ * residualCache.base().copyTo(advectedF/B.residual()), the merge set-up of
+ * renderAnimationFBMO (synthesisProcessor.cpp:979-980). */
+pt_status pt_copy_offsets_to_advected(pt_ctx* ctx, int forwards);
 
 /* ---- state transfer (WorkingBuffers load/getOutput,
  *      workingBuffers.cpp:118-207) ---------------------------------------- */

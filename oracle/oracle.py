@@ -7,6 +7,9 @@ and drives it in the reference's call sequence:
   (src/PaintTweenCUDA/synthesisProcessor.cpp:703-753,846-878)
 * SynthesisFrame::synthesizeConsecutive / propagateAndScatter
   (src/PaintTweenCUDA/synthesisFrame.cpp:214-323,483-508)
+* renderAnimationIND and renderAnimationFBMO with synthesizeInterpolated /
+  advectNeighbors (synthesisProcessor.cpp:807-844,880-1022,
+  synthesisFrame.cpp:325-418)
 * the EXR temp-file round trip between levels and passes becomes an
   in-memory store (offsets exact, residual rounded through half precision as
   WorkingBuffers::loadResidual reads the half .b channel).
@@ -48,6 +51,7 @@ def lib():
             "pto_flip": (None, [vp]),
             "pto_copy_base_to_working": (None, [vp]),
             "pto_reset_advected": (None, [vp]),
+            "pto_copy_base_to_advected": (None, [vp, i]),
             "pto_randomize": (None, [vp, i]),
             "pto_propagate": (None, [vp, i, i]),
             "pto_scatter": (None, [vp, i]),
@@ -260,11 +264,21 @@ class Oracle:
 
     def load_frame_level(self, fp, level):
         """SynthesisFrame::loadImages + loadAnimImages, synthesisFrame.cpp:562-656."""
+        self.load_images(fp, level)
+        self.load_anim_images(fp, level)
+
+    def load_images(self, fp, level):
+        """SynthesisFrame::loadImages, synthesisFrame.cpp:562-580."""
         L = lib()
         w, h = self.lw(level), self.lh(level)
         L.pto_upload_layered(self.h, _abi.LAYER_INPUT_COLOR, _p(_c(fp["rgba"][level], np.float32)), w, h)
         L.pto_upload_plain(self.h, _abi.LAYER_INPUT_ORIENTATION, _p(_c(fp["orient"][level], np.float32)), w, h)
         L.pto_upload_plain(self.h, _abi.LAYER_INPUT_ID, _p(_c(fp["ids"][level], np.int32)), w, h)
+
+    def load_anim_images(self, fp, level):
+        """SynthesisFrame::loadAnimImages, synthesisFrame.cpp:583-656."""
+        L = lib()
+        w, h = self.lw(level), self.lh(level)
         L.pto_upload_layered(self.h, _abi.LAYER_INPUT_VEL_B, _p(_c(fp["velb"][level], np.float32)), w, h)
         L.pto_upload_layered(self.h, _abi.LAYER_INPUT_VEL_F, _p(_c(fp["velf"][level], np.float32)), w, h)
         L.pto_upload_layered(self.h, _abi.LAYER_INPUT_DIST_TRANS, _p(_c(fp["dt"][level], np.float32)), w, h)
@@ -279,6 +293,9 @@ class Oracle:
 
     def reset_advected(self):
         lib().pto_reset_advected(self.h)
+
+    def copy_base_to_advected(self, forwards):
+        lib().pto_copy_base_to_advected(self.h, int(forwards))
 
     # --- TexSynth compute calls (each ends with syncBuffers as the reference's
     #     host wrappers do) --------------------------------------------------
@@ -360,6 +377,7 @@ class OracleDriver:
         sh = max(s["h"] for s in styles)
         self.o = Oracle(self.W, self.H, sw, sh, len(styles), threads=threads)
         self.store = {}
+        self.last_saved = {}  # SynthesisFrame::_last_saved_pass: (frame, level) -> pass
         self.levels = params.levels
 
     def _update_parameters(self, frame, direction):
@@ -443,7 +461,12 @@ class OracleDriver:
                 o.merge_using_residual(level, forwards)
         o.sync(level)
         self.propagate_and_scatter(level, self.user.iterations)
+        self._save_images(level, frame, pass_)
+
+    def _save_images(self, level, frame, pass_):
+        """SynthesisFrame::saveImages, synthesisFrame.cpp:758-767."""
         self._save(level, frame, pass_)
+        self.last_saved[(frame, level)] = pass_
 
     def _copy_base_to_working(self, level):
         """CudaBufferPair::copyBaseToWorking for the offsets pair."""
@@ -454,7 +477,75 @@ class OracleDriver:
         the FMBM schemes (renderAnimationFMBM) or IND (renderAnimationIND)."""
         if self.user.scheme == _abi.S_IND:
             return self._render_ind(first, last)
+        if self.user.scheme == _abi.S_FBMO:
+            return self._render_fbmo(first, last)
         return self._render_fmbm(first, last)
+
+    def _advect_neighbors(self, frame, level, source_pass, first, last):
+        """SynthesisFrame::advectNeighbors, synthesisFrame.cpp:325-382, with
+        the frames of the synthesised range as neighbours."""
+        o, u = self.o, self.user
+        o.reset_advected()
+        prior = frame - 1 if frame - 1 >= first else None
+        nxt = frame + 1 if frame + 1 <= last else None
+        temporal = (u.timeDerivativeInputWeight > 0 or u.timeDerivativeOutputWeight > 0
+                    or u.temporalCoherenceWeight > 0)
+        if last == first or not temporal or (prior is None and nxt is None):
+            o.load_anim_images(self.frames[frame], level)
+            return
+        for nb, fwd in ((prior, True), (nxt, False)):
+            if nb is None or source_pass < 0:
+                continue
+            o.load_frame_level(self.frames[nb], level)
+            o.flip()
+            o.load_anim_images(self.frames[frame], level)
+            self._load_offsets(level, nb, self.last_saved[(nb, level)])
+            o.advect(level, 1, fwd, 0)
+
+    def synthesize_interpolated(self, frame, level, this_pass, source_pass, first, last):
+        """SynthesisFrame::synthesizeInterpolated, synthesisFrame.cpp:384-418."""
+        o = self.o
+        self._update_parameters(frame, _abi.BIDIRECTIONAL)
+        self._advect_neighbors(frame, level, source_pass, first, last)
+        o.load_images(self.frames[frame], level)
+        self._load_offsets(level, frame, source_pass)
+        o.sync(level, _abi.DONT_COPY_OFFSETS | _abi.DONT_UPDATE_RESIDUAL)
+        self.propagate_and_scatter(level, self.user.iterations)
+        self._save_images(level, frame, this_pass)
+
+    def _render_fbmo(self, first, last):
+        """renderAnimationFBMO, synthesisProcessor.cpp:926-1022, with
+        renderInterpolatedFixupPass (:880-924) for every frame."""
+        o, u = self.o, self.user
+        final_pass = u.fixupPasses + 2
+        for level in range(self.levels - 1, u.finalLevel - 1, -1):
+            o.load_style_level(self.styles, level)
+            for pass_ in (0, 1):
+                o.reset_advected()
+                forwards = pass_ == 0
+                frames = list(range(first, last + 1)) if forwards else list(range(last, first - 1, -1))
+                for i, f in enumerate(frames):
+                    is_first = i == 0
+                    if not is_first or pass_ > 0:
+                        o.flip()
+                    o.load_frame_level(self.frames[f], level)
+                    self.synthesize_consecutive(f, level, pass_, is_first, forwards, final_pass, True)
+            for f in range(first, last + 1):  # pass 2: forward and backward merged
+                self._load_offsets(level, f, 0)
+                self._load_residual(level, f, 0)
+                o.copy_base_to_advected(True)
+                o.sync(level, _abi.DONT_COPY_OFFSETS | _abi.DONT_UPDATE_RESIDUAL)
+                self._load_offsets(level, f, 1)
+                self._load_residual(level, f, 1)
+                o.sync(level, _abi.DONT_COPY_OFFSETS | _abi.DONT_UPDATE_RESIDUAL)
+                o.merge_randomly(level, True, 0.5, True)  # TexSynth::mergeRandomly ends with a sync
+                o.sync(level)
+                self._save(level, f, 2)
+            for pass_ in range(3, u.fixupPasses + 3):
+                for f in range(first, last + 1):
+                    self._random_level(f, level)
+                    self.synthesize_interpolated(f, level, pass_, pass_ - 1, first, last)
+        return {f: self.store[(u.finalLevel, f, final_pass)] for f in range(first, last + 1)}
 
     def _render_ind(self, first, last):
         """renderAnimationIND, synthesisProcessor.cpp:807-844: every frame on

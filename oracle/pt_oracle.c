@@ -1238,6 +1238,14 @@ void pto_flip(pto* o) { o->cur = (o->cur + 1) % 2; }
 void pto_copy_base_to_working(pto* o) {
     memcpy(o->off_work, o->off_base, sizeof(pt_patchxf) * (size_t)o->W * o->H);
 }
+/* renderAnimationFBMO's merge set-up, synthesisProcessor.cpp:979-980:
+ * offsets.base().copyTo(advected.offsets()),
+ * residualCache.base().copyTo(advected.residual()) */
+void pto_copy_base_to_advected(pto* o, int forwards) {
+    int d = forwards ? 0 : 1;
+    memcpy(o->adv_off[d], o->off_base, sizeof(pt_patchxf) * (size_t)o->W * o->H);
+    memcpy(o->adv_res[d], o->res_base, sizeof(float) * (size_t)o->W * o->H);
+}
 void pto_reset_advected(pto* o) {
     size_t n = (size_t)o->W * o->H;
     for (int l = 0; l < 2; l++) {

@@ -46,6 +46,7 @@ SIGNATURES = {
     "pt_update_residual_cache": (_I, [_VP, _I]),
     "pt_sync_buffers": (_I, [_VP, _I, _I]),
     "pt_reset_advected_buffers": (_I, [_VP]),
+    "pt_copy_offsets_to_advected": (_I, [_VP, _I]),
     "pt_load_offsets": (_I, [_VP, _I, _VP]),
     "pt_load_residual": (_I, [_VP, _I, _VP]),
     "pt_get_offsets": (_I, [_VP, _I, _VP]),

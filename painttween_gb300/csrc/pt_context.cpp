@@ -137,6 +137,9 @@ struct pt_ctx {
     std::vector<int> style_set;
     std::map<int, std::vector<FrameLevel>> frames;
     std::map<std::tuple<int, int, int>, StoreEntry> store;
+    // SynthesisFrame::_last_saved_pass: (frame, level) -> last pass saved
+    // through saveImages
+    std::map<std::pair<int, int>, int> last_saved;
 
     uint64_t launches = 0;
     uint32_t pass_counter = 0;
@@ -718,6 +721,7 @@ static void free_store(pt_ctx* c) {
         dfree_t(c, kv.second.canvas);
     }
     c->store.clear();
+    c->last_saved.clear();
 }
 
 pt_status pt_destroy(pt_ctx* c) {
@@ -1032,15 +1036,22 @@ static pt_status ensure_transparency_known(pt_ctx* c) {
     return PT_OK;
 }
 
+// SynthesisFrame::createRandomPyramid, synthesisFrame.cpp:66-150, over the
+// frame's colour (transparency) and orientation of `level`
+static pt_status random_level(pt_ctx* c, int level, int frame, Arr<float4> rgba, Arr<float> orient);
+
 pt_status pt_create_random_level(pt_ctx* c, int level, int frame) {
     if (!c) return PT_ERR_INVALID;
     TRY(check_ready(c, level));
+    return random_level(c, level, frame, c->img.base[c->img.cur], c->img.orient);
+}
+
+static pt_status random_level(pt_ctx* c, int level, int frame, Arr<float4> rgba, Arr<float> orient) {
     int lw = c->W >> level, lh = c->H >> level;
     int mx = (c->SW >> level) - 1, my = (c->SH >> level) - 1;
     if (mx < 1 || my < 1) return fail(c, PT_ERR_INVALID, "style too small for level %d", level);
     if (!c->rnd) TRY(dalloc_t(c, &c->rnd, (size_t)c->W * c->H));
     ExView ex{c->ex->base, c->ex->out, c->ex->bo, c->ex->orient, c->ex->dt, c->ex->ids, c->ex->w, c->ex->h, c->NS};
-    const ImgView& I = c->img;
     int mode;
     uint32_t seed = (uint32_t)(frame * level);
     if (c->params.rngMode == PT_RNG_COUNTER) {
@@ -1079,7 +1090,7 @@ pt_status pt_create_random_level(pt_ctx* c, int level, int frame) {
         CU(cudaStreamSynchronize(c->stream));  // host vector goes out of scope
     }
     LN(pt::launch_random_level(mode, lw, lh, mx, my, c->params.transparencyOk, c->params.orientationEnabled,
-                               I.base[I.cur], I.orient, ex, c->rnd, c->states, seed, c->stream));
+                               rgba, orient, ex, c->rnd, c->states, seed, c->stream));
     c->img.rnd = Arr<float4>{c->rnd, lw, lh};
     return PT_OK;
 }
@@ -1547,20 +1558,38 @@ static pt_status bind_style_level(pt_ctx* c, int level) {
 }
 
 // SynthesisFrame::loadImages + loadAnimImages, synthesisFrame.cpp:562-656
-static pt_status bind_frame_level(pt_ctx* c, int frame, int level) {
+static pt_status frame_level(pt_ctx* c, int frame, int level, const FrameLevel** out) {
     auto it = c->frames.find(frame);
     if (it == c->frames.end()) return fail(c, PT_ERR_STATE, "frame %d not set", frame);
     if (level >= (int)it->second.size()) return fail(c, PT_ERR_INVALID, "frame pyramid too shallow");
-    const FrameLevel& L = it->second[level];
-    int cur = c->img.cur;
-    c->img.base[cur] = Arr<float4>{L.rgba, L.w, L.h};
-    c->img.dt[cur] = Arr<float>{L.dt, L.w, L.h};
-    c->img.velf[cur] = Arr<float2>{L.velf, L.w, L.h};
-    c->img.velb[cur] = Arr<float2>{L.velb, L.w, L.h};
-    c->img.orient = Arr<float>{L.orient, L.w, L.h};
-    c->img.scale = Arr<float2>{L.scale, L.w, L.h};
-    c->img.ids = Arr<int>{L.ids, L.w, L.h};
+    *out = &it->second[level];
     return PT_OK;
+}
+// SynthesisFrame::loadImages, synthesisFrame.cpp:562-580: the colour into
+// the current layer, orientation and ids
+static pt_status bind_frame_images(pt_ctx* c, int frame, int level) {
+    const FrameLevel* L;
+    TRY(frame_level(c, frame, level, &L));
+    c->img.base[c->img.cur] = Arr<float4>{L->rgba, L->w, L->h};
+    c->img.orient = Arr<float>{L->orient, L->w, L->h};
+    c->img.ids = Arr<int>{L->ids, L->w, L->h};
+    return PT_OK;
+}
+// SynthesisFrame::loadAnimImages, synthesisFrame.cpp:583-656: velocities and
+// distance transform into the current layer, scale
+static pt_status bind_frame_anim(pt_ctx* c, int frame, int level) {
+    const FrameLevel* L;
+    TRY(frame_level(c, frame, level, &L));
+    int cur = c->img.cur;
+    c->img.dt[cur] = Arr<float>{L->dt, L->w, L->h};
+    c->img.velf[cur] = Arr<float2>{L->velf, L->w, L->h};
+    c->img.velb[cur] = Arr<float2>{L->velb, L->w, L->h};
+    c->img.scale = Arr<float2>{L->scale, L->w, L->h};
+    return PT_OK;
+}
+static pt_status bind_frame_level(pt_ctx* c, int frame, int level) {
+    TRY(bind_frame_images(c, frame, level));
+    return bind_frame_anim(c, frame, level);
 }
 
 static pt_status store_save(pt_ctx* c, int level, int frame, int pass, bool with_canvas) {
@@ -1600,6 +1629,13 @@ static pt_status store_load_residual(pt_ctx* c, int level, int frame, int pass) 
     LN(pt::launch_load_residual(P, it->second.res, c->res[c->res_i], c->stream));
     return PT_OK;
 }
+// SynthesisFrame::saveImages, synthesisFrame.cpp:758-767: saved and
+// remembered as the frame's last saved pass of the level
+static pt_status save_images(pt_ctx* c, int level, int frame, int pass, bool with_canvas) {
+    TRY(store_save(c, level, frame, pass, with_canvas));
+    c->last_saved[std::make_pair(frame, level)] = pass;
+    return PT_OK;
+}
 
 // SynthesisFrame::propagateAndScatter, synthesisFrame.cpp:483-508
 //
@@ -1615,8 +1651,15 @@ static pt_status store_load_residual(pt_ctx* c, int level, int frame, int pass) 
 // since then: it was rejected there against the same residual and would be
 // rejected again.  The sync after a pass recomputes only the canvas and
 // residuals whose inputs changed.  Results are bit-identical either way.
-static pt_status propagate_and_scatter(pt_ctx* c, int level, int iterations) {
+//
+// `residual_fresh`: the residual cache holds the residuals of the base
+// offsets.  synthesizeInterpolated syncs without updating it, so its first
+// propagate pass compares against the residuals left by earlier steps, as
+// the reference's does; that pass then runs untracked and its sync computes
+// every residual and tap value.
+static pt_status propagate_and_scatter(pt_ctx* c, int level, int iterations, bool residual_fresh = true) {
     const bool track = c->use_incremental && tiled_usable(c);
+    bool fill_after_first = false;
     if (track) {
         // the per-tap values of every residual, recomputed in full once
         const int r = c->params.residualWindowSize, K = (2 * r + 1) * (2 * r + 1);
@@ -1626,13 +1669,24 @@ static pt_status propagate_and_scatter(pt_ctx* c, int level, int iterations) {
             TRY(dalloc_t(c, &c->tap_cache, (size_t)K * c->W * c->H));
             c->tap_cache_k = K;
         }
-        c->inc_fill = 1;
-        pt_status st = do_residual(c, level);
-        c->inc_fill = 0;
-        TRY(st);
+        if (residual_fresh) {
+            c->inc_fill = 1;
+            pt_status st = do_residual(c, level);
+            c->inc_fill = 0;
+            TRY(st);
+        } else {
+            fill_after_first = true;
+        }
     }
     std::map<int, int> last_pass;  // jump (0 = scatter) -> index of its last pass
     auto run = [&](int jump) -> pt_status {
+        if (fill_after_first) {
+            fill_after_first = false;
+            c->inc_fill = 1;
+            pt_status st = pt_propagate(c, level, jump, -1);
+            c->inc_fill = 0;
+            return st;
+        }
         if (track) {
             c->inc_on = 1;
             c->inc_pi = ++c->inc_seq;
@@ -1699,7 +1753,7 @@ static pt_status synthesize_consecutive(pt_ctx* c, const pt_params& user, int fr
     }
     TRY(do_sync(c, level, 0));
     TRY(propagate_and_scatter(c, level, user.iterations));
-    return store_save(c, level, frame, pass, save_canvas);
+    return save_images(c, level, frame, pass, save_canvas);
 }
 
 // SynthesisProcessor::renderAnimationFMBM + renderConsecutivePass,
@@ -1743,6 +1797,112 @@ static pt_status render_ind(pt_ctx* c, int first, int last) {
     return PT_OK;
 }
 
+// WorkingBuffers, as renderAnimationFBMO uses them
+// (synthesisProcessor.cpp:979-980): the base offsets and residual copied
+// whole into the advected buffers of `forwards`
+pt_status pt_copy_offsets_to_advected(pt_ctx* c, int forwards) {
+    if (!c) return PT_ERR_INVALID;
+    if (!c->initialized) return fail(c, PT_ERR_STATE, "context not initialized");
+    const int d = forwards ? 0 : 1;
+    TRY(copy_planes_full(c, c->adv[d].off, base_planes(c)));
+    CU(cudaMemcpyAsync(c->adv[d].res, c->res[c->res_i], (size_t)c->W * c->H * sizeof(float),
+                       cudaMemcpyDeviceToDevice, c->stream));
+    c->adv_written[d] = true;
+    return PT_OK;
+}
+
+// SynthesisFrame::advectNeighbors, synthesisFrame.cpp:325-382: the
+// neighbours' last saved offsets advected into this frame (the neighbour's
+// images in the current layer, then this frame's velocities in the other).
+// Neighbours are the frames of the synthesised range.
+static pt_status advect_neighbors(pt_ctx* c, int frame, int level, int source_pass, int first, int last) {
+    TRY(pt_reset_advected_buffers(c));
+    const pt_params& p = c->params;
+    const bool has_prior = frame - 1 >= first, has_next = frame + 1 <= last;
+    const bool temporal = p.timeDerivativeInputWeight > 0.f || p.timeDerivativeOutputWeight > 0.f ||
+                          p.temporalCoherenceWeight > 0.f;
+    if (last == first || !temporal || !(has_prior || has_next)) return bind_frame_anim(c, frame, level);
+    for (int side = 0; side < 2; side++) {
+        const bool fwd = side == 0;
+        const int nb = fwd ? frame - 1 : frame + 1;
+        if (!(fwd ? has_prior : has_next) || source_pass < 0) continue;
+        TRY(bind_frame_level(c, nb, level));
+        TRY(pt_flip_anim_buffers(c));
+        TRY(bind_frame_anim(c, frame, level));
+        auto it = c->last_saved.find(std::make_pair(nb, level));
+        if (it == c->last_saved.end()) return fail(c, PT_ERR_STATE, "frame %d has no saved level %d", nb, level);
+        TRY(store_load_offsets(c, level, nb, it->second));
+        TRY(pt_advect_offsets(c, level, 1, fwd ? 1 : 0, 0));
+    }
+    return PT_OK;
+}
+
+// SynthesisFrame::synthesizeInterpolated, synthesisFrame.cpp:384-418: one
+// frame between its advected neighbours, both temporal terms on
+static pt_status synthesize_interpolated(pt_ctx* c, const pt_params& user, int frame, int level, int this_pass,
+                                         int source_pass, int first, int last, bool save_canvas) {
+    pt_params p = user;  // updateParameters(BIDIRECTIONAL), :522-542
+    p.advectionJitter = (frame % 3 == 0) ? user.advectionJitter * 0.01f : 0.0f;
+    p.direction = PT_BIDIRECTIONAL;
+    TRY(pt_set_params(c, &p));
+    TRY(advect_neighbors(c, frame, level, source_pass, first, last));
+    TRY(bind_frame_images(c, frame, level));
+    TRY(store_load_offsets(c, level, frame, source_pass));
+    TRY(do_sync(c, level, PT_DONT_COPY_OFFSETS | PT_DONT_UPDATE_RESIDUAL));
+    TRY(propagate_and_scatter(c, level, user.iterations, false));
+    return save_images(c, level, frame, this_pass, save_canvas);
+}
+
+// SynthesisProcessor::renderAnimationFBMO, synthesisProcessor.cpp:926-1022:
+// per level a forward and a backward consecutive pass, their results merged
+// at random (pass 2), then fix-up passes that synthesise every frame between
+// its neighbours
+static pt_status render_fbmo(pt_ctx* c, int first, int last) {
+    const pt_params user = c->params;
+    TRY(reset_working(c));
+    c->img.cur = 0;
+    free_store(c);
+    const int final_pass = user.fixupPasses + 2;
+    for (int level = user.levels - 1; level >= user.finalLevel; level--) {
+        TRY(bind_style_level(c, level));
+        const bool final_level = level == user.finalLevel;
+        for (int pass = 0; pass < 2; pass++) {  // passes 0 and 1
+            TRY(pt_reset_advected_buffers(c));
+            const bool forwards = pass == 0;
+            for (int i = 0; i <= last - first; i++) {
+                const int f = forwards ? first + i : last - i;
+                const bool is_first = i == 0;
+                if (!is_first || pass > 0) TRY(pt_flip_anim_buffers(c));
+                TRY(bind_frame_level(c, f, level));
+                TRY(synthesize_consecutive(c, user, f, level, pass, is_first, forwards, final_pass, true, false));
+            }
+        }
+        for (int f = first; f <= last; f++) {  // pass 2
+            TRY(store_load_offsets(c, level, f, 0));
+            TRY(store_load_residual(c, level, f, 0));
+            TRY(pt_copy_offsets_to_advected(c, 1));
+            TRY(do_sync(c, level, PT_DONT_COPY_OFFSETS | PT_DONT_UPDATE_RESIDUAL));
+            TRY(store_load_offsets(c, level, f, 1));
+            TRY(store_load_residual(c, level, f, 1));
+            TRY(do_sync(c, level, PT_DONT_COPY_OFFSETS | PT_DONT_UPDATE_RESIDUAL));
+            TRY(pt_merge_randomly(c, level, 1, 0.5f, 1));  // SynthesisFrame::mergeRandomly, :510-520
+            TRY(store_save(c, level, f, 2, final_level && final_pass == 2));
+        }
+        for (int pass = 3; pass < user.fixupPasses + 3; pass++) {  // renderInterpolatedFixupPass, :880-924
+            for (int f = first; f <= last; f++) {
+                const FrameLevel* L;
+                TRY(frame_level(c, f, level, &L));
+                TRY(random_level(c, level, f, Arr<float4>{L->rgba, L->w, L->h}, Arr<float>{L->orient, L->w, L->h}));
+                TRY(synthesize_interpolated(c, user, f, level, pass, pass - 1, first, last,
+                                            final_level && pass == final_pass));
+            }
+        }
+        if (level + 1 < user.levels) drop_store_level(c, level + 1);
+    }
+    c->params = user;
+    return PT_OK;
+}
+
 static pt_status render_fmbm(pt_ctx* c, int first, int last) {
     const pt_params user = c->params;
     if (user.levels < 1 || user.finalLevel < 0 || user.finalLevel >= user.levels)
@@ -1750,8 +1910,9 @@ static pt_status render_fmbm(pt_ctx* c, int first, int last) {
     for (int f = first; f <= last; f++)
         if (!c->frames.count(f)) return fail(c, PT_ERR_STATE, "frame %d not set", f);
     if (user.scheme == PT_S_IND) return render_ind(c, first, last);
+    if (user.scheme == PT_S_FBMO) return render_fbmo(c, first, last);
     if (user.scheme != PT_S_FMBM && user.scheme != PT_S_FMBM_RM)
-        return fail(c, PT_ERR_UNSUPPORTED, "the FBMO and TCTF schemes are not implemented");
+        return fail(c, PT_ERR_UNSUPPORTED, "the TCTF scheme is not implemented");
     TRY(reset_working(c));
     c->img.cur = 0;
     free_store(c);
@@ -1785,9 +1946,14 @@ static pt_status render_fmbm(pt_ctx* c, int first, int last) {
     return PT_OK;
 }
 
+// the pass whose output copyOutputToFinal hands out
+static int final_pass_of(const pt_params& p) {
+    if (p.scheme == PT_S_FBMO) return p.fixupPasses + 2;
+    return (p.finalLevel == 0) ? p.fixupPasses : 0;
+}
+
 static pt_status fetch_final(pt_ctx* c, int frame, float* out_rgba, pt_patchxf* out_offsets) {
-    const int total = c->params.fixupPasses + 1;
-    const int final_pass = (c->params.finalLevel == 0) ? total - 1 : 0;
+    const int final_pass = final_pass_of(c->params);
     auto it = c->store.find(std::make_tuple(c->params.finalLevel, frame, final_pass));
     if (it == c->store.end()) return fail(c, PT_ERR_STATE, "no final output for frame %d", frame);
     size_t n = (size_t)it->second.w * it->second.h;

@@ -201,6 +201,9 @@ class TexSynth:
     def reset_advected_buffers(self):
         self._check(lib().pt_reset_advected_buffers(self.h), "pt_reset_advected_buffers")
 
+    def copy_offsets_to_advected(self, forwards):
+        self._check(lib().pt_copy_offsets_to_advected(self.h, int(forwards)), "pt_copy_offsets_to_advected")
+
     def convolve_separable(self, src_dev, dst_dev, w, h, pitch, radius):
         """Gaussian blur of a device float image (device pointers as ints)."""
         self._check(lib().pt_convolve_separable(self.h, ctypes.c_void_p(src_dev), ctypes.c_void_p(dst_dev), w, h,

@@ -517,3 +517,21 @@ def test_ind_scheme_matches_oracle():
     for f in range(3):
         assert_offsets_equal(got[f][1], ref[f][0], 1.0, "IND frame %d" % f)
         assert_array_equal(got[f][0], ref[f][2], "IND output frame %d" % f)
+
+
+@pytest.mark.parametrize("r,fixups", [(2, 1), (3, 2)])
+def test_fbmo_scheme_matches_oracle(r, fixups):
+    """The FBMO scheme (forward and backward passes, random merge, fix-up
+    passes between advected neighbours with both temporal terms) against the
+    oracle."""
+    p = config_params(r=r, levels=2, iterations=2)
+    p.scheme, p.fixupPasses = _abi.S_FBMO, fixups
+    p.temporalCoherenceWeight = 0.5
+    p.timeDerivativeInputWeight = 0.25
+    ex = synthetic.make_exemplar(64, 64, seed=67 + r)
+    clip = synthetic.make_clip(80, 64, 3, 4, seed=68 + r)
+    got = _animate(p, ex, clip, 80, 64)
+    ref = O.OracleDriver(p, [ex], clip, threads=8).render(0, 3)
+    for f in range(4):
+        assert_offsets_equal(got[f][1], ref[f][0], 1.0, "FBMO frame %d" % f)
+        assert_array_equal(got[f][0], ref[f][2], "FBMO output frame %d" % f)

@@ -159,3 +159,25 @@ def test_ind_scheme_equals_fmbm_on_a_still():
         out.append(O.OracleDriver(p, [ex], [fr], threads=4).render(0, 0)[0])
     assert (out[0][0].view(np.uint8) == out[1][0].view(np.uint8)).all()
     assert np.array_equal(out[0][2], out[1][2])
+
+
+def test_fbmo_merge_pass_takes_each_record_from_a_directional_pass():
+    """renderAnimationFBMO's pass 2 merges the forward (pass 0) and backward
+    (pass 1) offsets at random: every record of pass 2 is one of the two."""
+    p = _abi.default_params()
+    p.residualWindowSize, p.levels, p.iterations = 2, 2, 2
+    p.scheme, p.fixupPasses = _abi.S_FBMO, 1
+    p.temporalCoherenceWeight = 0.5
+    ex = synthetic.make_exemplar(48, 48, seed=65)
+    clip = synthetic.make_clip(56, 40, 3, 3, seed=66)
+    drv = O.OracleDriver(p, [ex], clip, threads=4)
+    out = drv.render(0, 2)
+    assert sorted(out) == [0, 1, 2]
+    for f in range(3):
+        rec = lambda pass_: drv.store[(0, f, pass_)][0].view(np.uint8).reshape(40, 56, -1)
+        fw, bw, mg = rec(0), rec(1), rec(2)
+        from_fw = (mg == fw).all(-1)
+        from_bw = (mg == bw).all(-1)
+        assert (from_fw | from_bw).all()
+        assert from_fw.any() and from_bw.any() and not (from_fw & from_bw).all()
+        assert drv.last_saved[(f, 0)] == 3  # the fix-up pass, not the merge
