@@ -113,6 +113,7 @@ struct pt_ctx {
     float* up_dt[2] = {nullptr, nullptr};
     float2* up_velf[2] = {nullptr, nullptr};
     float2* up_velb[2] = {nullptr, nullptr};
+    bool slot_copy = false;  // driver binds copy into the layered arrays (IND)
     float* up_orient = nullptr;
     float2* up_scale = nullptr;
     int* up_ids = nullptr;
@@ -403,9 +404,12 @@ static pt_status check_ready(pt_ctx* c, int level, bool need_ex = true, bool nee
     if (need_img) {
         const ImgView& I = c->img;
         int lw = c->W >> level, lh = c->H >> level;
-        if (!I.base[I.cur].p || I.base[I.cur].w != lw || I.base[I.cur].h != lh)
+        // a layer holds one level (bound at its size) or the full-size
+        // layered array that level uploads write into
+        auto fits = [&](int w, int h) { return (w == lw && h == lh) || (w == c->W && h == c->H); };
+        if (!I.base[I.cur].p || !fits(I.base[I.cur].w, I.base[I.cur].h))
             return fail(c, PT_ERR_STATE, "input colour of level %d not uploaded", level);
-        if (!I.dt[I.cur].p || I.dt[I.cur].w != lw || I.dt[I.cur].h != lh)
+        if (!I.dt[I.cur].p || !fits(I.dt[I.cur].w, I.dt[I.cur].h))
             return fail(c, PT_ERR_STATE, "input distance transform of level %d not uploaded", level);
         if (!I.orient.p || !I.scale.p || !I.ids.p)
             return fail(c, PT_ERR_STATE, "input orientation/scale/ids not uploaded");
@@ -914,6 +918,42 @@ static pt_status h2d(pt_ctx* c, void* dst, const void* src, size_t bytes) {
     return PT_OK;
 }
 
+// A layered input image (colour, distance transform, velocities) as the
+// reference keeps it (cudaImageBuffer.h layered copyFromHost): one
+// full-size array per layer, which an upload of a level overwrites on that
+// level's rectangle only, so texels outside the rectangle keep what a finer
+// level left there.  Allocated zeroed; bound with the full width as pitch.
+template <class T>
+static pt_status slot_write(pt_ctx* c, T** slot, Arr<T>* bind, const void* src, int w, int h, cudaMemcpyKind kind) {
+    const size_t n = (size_t)c->W * c->H;
+    if (!*slot) {
+        TRY(dalloc_t(c, slot, n));
+        CU(cudaMemsetAsync(*slot, 0, n * sizeof(T), c->stream));
+    }
+    CU(cudaMemcpy2DAsync(*slot, (size_t)c->W * sizeof(T), src, (size_t)w * sizeof(T), (size_t)w * sizeof(T), h, kind,
+                         c->stream));
+    if (kind == cudaMemcpyHostToDevice) CU(cudaStreamSynchronize(c->stream));
+    *bind = Arr<T>{*slot, c->W, c->H};
+    return PT_OK;
+}
+
+// A fresh run: no input image bound, the layered arrays all zero.
+static pt_status reset_image_slots(pt_ctx* c) {
+    const size_t n = (size_t)c->W * c->H;
+    for (int i = 0; i < 2; i++) {
+        c->img.base[i] = Arr<float4>{};
+        c->img.dt[i] = Arr<float>{};
+        c->img.velf[i] = Arr<float2>{};
+        c->img.velb[i] = Arr<float2>{};
+        if (c->up_base[i]) CU(cudaMemsetAsync(c->up_base[i], 0, n * sizeof(float4), c->stream));
+        if (c->up_dt[i]) CU(cudaMemsetAsync(c->up_dt[i], 0, n * sizeof(float), c->stream));
+        if (c->up_velf[i]) CU(cudaMemsetAsync(c->up_velf[i], 0, n * sizeof(float2), c->stream));
+        if (c->up_velb[i]) CU(cudaMemsetAsync(c->up_velb[i], 0, n * sizeof(float2), c->stream));
+    }
+    c->img.cur = 0;
+    return PT_OK;
+}
+
 pt_status pt_upload_image_color4(pt_ctx* c, int level, int layer, const float* rgba, int w, int h, int style) {
     if (!c || !rgba) return PT_ERR_INVALID;
     if (!c->initialized) return fail(c, PT_ERR_STATE, "pt_initialize has not been called");
@@ -931,12 +971,8 @@ pt_status pt_upload_image_color4(pt_ctx* c, int level, int layer, const float* r
     if (level < 0 || w != (c->W >> level) || h != (c->H >> level))
         return fail(c, PT_ERR_INVALID, "image upload %dx%d does not match level %d", w, h, level);
     int cur = c->img.cur;
-    if (layer == PT_LAYER_INPUT_COLOR) {
-        if (!c->up_base[cur]) TRY(dalloc_t(c, &c->up_base[cur], (size_t)c->W * c->H));
-        TRY(h2d(c, c->up_base[cur], rgba, n * sizeof(float4)));
-        c->img.base[cur] = Arr<float4>{c->up_base[cur], w, h};
-        return PT_OK;
-    }
+    if (layer == PT_LAYER_INPUT_COLOR)
+        return slot_write(c, &c->up_base[cur], &c->img.base[cur], rgba, w, h, cudaMemcpyHostToDevice);
     if (layer == PT_LAYER_RANDOM) {
         if (!c->rnd) TRY(dalloc_t(c, &c->rnd, (size_t)c->W * c->H));
         TRY(h2d(c, c->rnd, rgba, n * sizeof(float4)));
@@ -965,12 +1001,8 @@ pt_status pt_upload_image_float(pt_ctx* c, int level, int layer, const float* da
         c->img.orient = Arr<float>{c->up_orient, w, h};
         return PT_OK;
     }
-    if (layer == PT_LAYER_INPUT_DIST_TRANS) {
-        if (!c->up_dt[cur]) TRY(dalloc_t(c, &c->up_dt[cur], (size_t)c->W * c->H));
-        TRY(h2d(c, c->up_dt[cur], data, n * sizeof(float)));
-        c->img.dt[cur] = Arr<float>{c->up_dt[cur], w, h};
-        return PT_OK;
-    }
+    if (layer == PT_LAYER_INPUT_DIST_TRANS)
+        return slot_write(c, &c->up_dt[cur], &c->img.dt[cur], data, w, h, cudaMemcpyHostToDevice);
     return fail(c, PT_ERR_UNSUPPORTED, "float layer %d not supported", layer);
 }
 
@@ -991,6 +1023,7 @@ pt_status pt_upload_image_float2(pt_ctx* c, int level, int layer, const float* x
         case PT_LAYER_INPUT_SCALE: store = &c->up_scale; slot = &c->img.scale; break;
         default: return fail(c, PT_ERR_UNSUPPORTED, "float2 layer %d not supported", layer);
     }
+    if (layer != PT_LAYER_INPUT_SCALE) return slot_write(c, store, slot, xy, w, h, cudaMemcpyHostToDevice);
     if (!*store) TRY(dalloc_t(c, store, (size_t)c->W * c->H));
     TRY(h2d(c, *store, xy, n * sizeof(float2)));
     *slot = Arr<float2>{*store, w, h};
@@ -1567,10 +1600,21 @@ static pt_status frame_level(pt_ctx* c, int frame, int level, const FrameLevel**
 }
 // SynthesisFrame::loadImages, synthesisFrame.cpp:562-580: the colour into
 // the current layer, orientation and ids
+//
+// While levels run coarse to fine (FMBM, FBMO) a layer's texels outside the
+// current rectangle were never written, so the level's own array is bound
+// (reads there give zero, as from the zeroed layered array).  The IND scheme
+// visits a coarse level after a finer one: it copies into the full-size
+// layered arrays as the reference's uploads do (`slot_copy`).
 static pt_status bind_frame_images(pt_ctx* c, int frame, int level) {
     const FrameLevel* L;
     TRY(frame_level(c, frame, level, &L));
-    c->img.base[c->img.cur] = Arr<float4>{L->rgba, L->w, L->h};
+    if (c->slot_copy) {
+        TRY(slot_write(c, &c->up_base[c->img.cur], &c->img.base[c->img.cur], L->rgba, L->w, L->h,
+                       cudaMemcpyDeviceToDevice));
+    } else {
+        c->img.base[c->img.cur] = Arr<float4>{L->rgba, L->w, L->h};
+    }
     c->img.orient = Arr<float>{L->orient, L->w, L->h};
     c->img.ids = Arr<int>{L->ids, L->w, L->h};
     return PT_OK;
@@ -1581,9 +1625,16 @@ static pt_status bind_frame_anim(pt_ctx* c, int frame, int level) {
     const FrameLevel* L;
     TRY(frame_level(c, frame, level, &L));
     int cur = c->img.cur;
-    c->img.dt[cur] = Arr<float>{L->dt, L->w, L->h};
-    c->img.velf[cur] = Arr<float2>{L->velf, L->w, L->h};
-    c->img.velb[cur] = Arr<float2>{L->velb, L->w, L->h};
+    if (c->slot_copy) {
+        const cudaMemcpyKind d2d = cudaMemcpyDeviceToDevice;
+        TRY(slot_write(c, &c->up_dt[cur], &c->img.dt[cur], L->dt, L->w, L->h, d2d));
+        TRY(slot_write(c, &c->up_velf[cur], &c->img.velf[cur], L->velf, L->w, L->h, d2d));
+        TRY(slot_write(c, &c->up_velb[cur], &c->img.velb[cur], L->velb, L->w, L->h, d2d));
+    } else {
+        c->img.dt[cur] = Arr<float>{L->dt, L->w, L->h};
+        c->img.velf[cur] = Arr<float2>{L->velf, L->w, L->h};
+        c->img.velb[cur] = Arr<float2>{L->velb, L->w, L->h};
+    }
     c->img.scale = Arr<float2>{L->scale, L->w, L->h};
     return PT_OK;
 }
@@ -1776,7 +1827,12 @@ static void drop_store_level(pt_ctx* c, int level) {
 static pt_status render_ind(pt_ctx* c, int first, int last) {
     const pt_params user = c->params;
     TRY(reset_working(c));
-    c->img.cur = 0;
+    TRY(reset_image_slots(c));
+    struct SlotCopy {  // frame binds copy into the layered arrays for this run
+        pt_ctx* c;
+        explicit SlotCopy(pt_ctx* x) : c(x) { c->slot_copy = true; }
+        ~SlotCopy() { c->slot_copy = false; }
+    } slot_copy(c);
     free_store(c);
     const int total = user.fixupPasses + 1;
     const int final_pass = (user.finalLevel == 0) ? total - 1 : 0;
@@ -1860,7 +1916,7 @@ static pt_status synthesize_interpolated(pt_ctx* c, const pt_params& user, int f
 static pt_status render_fbmo(pt_ctx* c, int first, int last) {
     const pt_params user = c->params;
     TRY(reset_working(c));
-    c->img.cur = 0;
+    TRY(reset_image_slots(c));
     free_store(c);
     const int final_pass = user.fixupPasses + 2;
     for (int level = user.levels - 1; level >= user.finalLevel; level--) {
@@ -1914,7 +1970,7 @@ static pt_status render_fmbm(pt_ctx* c, int first, int last) {
     if (user.scheme != PT_S_FMBM && user.scheme != PT_S_FMBM_RM)
         return fail(c, PT_ERR_UNSUPPORTED, "the TCTF scheme is not implemented");
     TRY(reset_working(c));
-    c->img.cur = 0;
+    TRY(reset_image_slots(c));
     free_store(c);
     const int total = user.fixupPasses + 1;
     const int final_pass = (user.finalLevel == 0) ? total - 1 : 0;

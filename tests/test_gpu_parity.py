@@ -506,10 +506,14 @@ def test_near_ties_match_oracle():
 
 
 def test_ind_scheme_matches_oracle():
-    """The IND scheme (every frame on its own) against the oracle."""
+    """The IND scheme (every frame on its own) against the oracle.  Coarse
+    levels of later frames read texels that earlier frames' finer levels left
+    outside the level rectangle (hysteresis velocities at the right and
+    bottom edges, propagate's wrap)."""
     p = config_params(r=3, levels=2, iterations=2)
     p.scheme = _abi.S_IND
     p.temporalCoherenceWeight = 0.5
+    p.hysteresisWeight = 0.25
     ex = synthetic.make_exemplar(64, 64, seed=63)
     clip = synthetic.make_clip(80, 64, 3, 3, seed=64)
     got = _animate(p, ex, clip, 80, 64)
