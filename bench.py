@@ -338,7 +338,7 @@ def run_ours(args, dist):
             d[key][...] = fr[key]
         pinned.append(d)
     h2d = sum(d[key].nbytes for d in pinned for key in keys)
-    h, w = cfg["h"] >> p.finalLevel, cfg["w"] >> p.finalLevel
+    h, w = cfg["h"] >> _abi.output_level(p), cfg["w"] >> _abi.output_level(p)
     outs = [(host_array((h, w, 4), np.float32), host_array((h, w), _abi.PATCH_DTYPE)) for _ in range(frames)]
     d2h = sum(a.nbytes + o.nbytes for a, o in outs)
     for _ in range(args.e2e_steps):

@@ -61,7 +61,8 @@ typedef struct {
 /* Pass direction (types.h:122-126). */
 enum { PT_FORWARD = 0, PT_BACKWARD = 1, PT_BIDIRECTIONAL = 2 };
 
-/* Synthesis schemes (types.h:128-134); FMBM and FMBM_RM are implemented. */
+/* Synthesis schemes (types.h:128-134); all five are implemented (TCTF
+ * without ribbon inputs: time step 1). */
 enum { PT_S_FMBM = 0, PT_S_FMBM_RM = 1, PT_S_FBMO = 2, PT_S_TCTF = 3, PT_S_IND = 4 };
 
 /* Random-number mode.
@@ -304,10 +305,16 @@ pt_status pt_set_frame(pt_ctx* ctx, int frame, int w, int h,
                        const float* scale);
 pt_status pt_clear_frames(pt_ctx* ctx);
 
-/* Synthesises one still (renderAnimationFMBM with one frame,
- * synthesisProcessor.cpp:846-878 -> synthesizeConsecutive,
- * synthesisFrame.cpp:214-323).  Outputs at level finalLevel; either output
- * pointer may be NULL. */
+/* Level of the final output (copyOutputToFinal, synthesisProcessor.cpp:
+ * 122-139, hands out level 0): FMBM, FMBM_RM and TCTF upsample their final
+ * level down to level 0; IND and FBMO write no level-0 output in the
+ * reference when finalLevel > 0, and here hand out their final level. */
+#define PT_OUTPUT_LEVEL(params) \
+    (((params)->scheme == PT_S_IND || (params)->scheme == PT_S_FBMO) ? (params)->finalLevel : 0)
+
+/* Synthesises one still (renderAnimation with one frame,
+ * synthesisProcessor.cpp:769-1312 for the scheme of pt_params.scheme).
+ * Outputs at PT_OUTPUT_LEVEL; either output pointer may be NULL. */
 pt_status pt_synthesize_frame(pt_ctx* ctx, int frame, float* out_rgba,
                               pt_patchxf* out_offsets);
 
@@ -316,12 +323,13 @@ typedef void (*pt_frame_callback)(int frame, const float* rgba,
                                   const pt_patchxf* offsets, int w, int h,
                                   void* user);
 /* Synthesises frames first..last (all uploaded with pt_set_frame) with the
- * forward/backward consecutive-pass scheme FMBM(_RM)
- * (synthesisProcessor.cpp:703-753,846-878). */
+ * scheme of pt_params.scheme: FMBM(_RM) forward/backward consecutive passes
+ * (synthesisProcessor.cpp:703-753,846-878), FBMO (:880-1022), TCTF without
+ * ribbon inputs (time step 1, :1047-1312) or IND (:807-844). */
 pt_status pt_synthesize_animation(pt_ctx* ctx, int first, int last,
                                   pt_frame_callback cb, void* user);
 
-/* The final output (level finalLevel) of one frame of the last
+/* The final output (level PT_OUTPUT_LEVEL) of one frame of the last
  * pt_synthesize_frame / pt_synthesize_animation, copied into the caller's
  * buffers; either pointer may be NULL.  No counterpart in the reference
  * (its frames end up in EXR files): a caller that passes NULL as the
@@ -367,8 +375,8 @@ typedef struct {
     const int32_t* style_ids;          /* or NULL */
     int image_w, image_h, frames;
     const pt_frame_inputs* inputs;     /* `frames` entries */
-    float* out_rgba;          /* frames x (image_h >> finalLevel) x (image_w >> finalLevel) x 4, or NULL */
-    pt_patchxf* out_offsets;  /* frames x (image_h >> finalLevel) x (image_w >> finalLevel), or NULL */
+    float* out_rgba;          /* frames x (image_h >> L) x (image_w >> L) x 4, or NULL; L = PT_OUTPUT_LEVEL */
+    pt_patchxf* out_offsets;  /* frames x (image_h >> L) x (image_w >> L), or NULL */
     double arrival_ms;        /* arrival, in ms after pt_serve starts */
     double start_ms;          /* out: when its synthesis started */
     double done_ms;           /* out: when its results were written */

@@ -7,9 +7,9 @@ and drives it in the reference's call sequence:
   (src/PaintTweenCUDA/synthesisProcessor.cpp:703-753,846-878)
 * SynthesisFrame::synthesizeConsecutive / propagateAndScatter
   (src/PaintTweenCUDA/synthesisFrame.cpp:214-323,483-508)
-* renderAnimationIND and renderAnimationFBMO with synthesizeInterpolated /
-  advectNeighbors (synthesisProcessor.cpp:807-844,880-1022,
-  synthesisFrame.cpp:325-418)
+* renderAnimationIND, renderAnimationFBMO and renderAnimationTCTF with
+  synthesizeInterpolated / advectNeighbors / refine / spatialUpsample
+  (synthesisProcessor.cpp:807-1312, synthesisFrame.cpp:325-481)
 * the EXR temp-file round trip between levels and passes becomes an
   in-memory store (offsets exact, residual rounded through half precision as
   WorkingBuffers::loadResidual reads the half .b channel).
@@ -473,12 +473,15 @@ class OracleDriver:
         lib().pto_copy_base_to_working(self.o.h)
 
     def render(self, first, last):
-        """SynthesisProcessor::renderAnimation, synthesisProcessor.cpp:769-805:
-        the FMBM schemes (renderAnimationFMBM) or IND (renderAnimationIND)."""
+        """SynthesisProcessor::renderAnimation, synthesisProcessor.cpp:769-805,
+        for the scheme of the parameters; returns {frame: (offsets, residual,
+        output)} at the level PT_OUTPUT_LEVEL names."""
         if self.user.scheme == _abi.S_IND:
             return self._render_ind(first, last)
         if self.user.scheme == _abi.S_FBMO:
             return self._render_fbmo(first, last)
+        if self.user.scheme == _abi.S_TCTF:
+            return self._render_tctf(first, last)
         return self._render_fmbm(first, last)
 
     def _advect_neighbors(self, frame, level, source_pass, first, last):
@@ -499,7 +502,7 @@ class OracleDriver:
             o.load_frame_level(self.frames[nb], level)
             o.flip()
             o.load_anim_images(self.frames[frame], level)
-            self._load_offsets(level, nb, self.last_saved[(nb, level)])
+            self._load_last_saved(nb, level)
             o.advect(level, 1, fwd, 0)
 
     def synthesize_interpolated(self, frame, level, this_pass, source_pass, first, last):
@@ -562,15 +565,83 @@ class OracleDriver:
         return {f: self.store[(self.user.finalLevel, f, final_pass)] for f in range(first, last + 1)}
 
     def _render_fmbm(self, first, last):
-        """renderAnimationFMBM, synthesisProcessor.cpp:846-878."""
+        """renderAnimationFMBM, synthesisProcessor.cpp:846-878, with
+        renderSpatialUpsample (:1025-1045) from a final level down to 0."""
         total = self.user.fixupPasses + 1
         for level in range(self.levels - 1, self.user.finalLevel - 1, -1):
             self.o.load_style_level(self.styles, level)
             self.o.reset_advected()
             for pass_ in range(total):
                 self._render_pass(level, pass_, total - 1, first, last)
+        for level in range(self.user.finalLevel, 0, -1):
+            self.o.load_style_level(self.styles, level - 1)
+            for f in range(first, last + 1):
+                self._spatial_upsample(f, level, level - 1, True)
         final_pass = total - 1 if self.user.finalLevel == 0 else 0
-        return {f: self.store[(self.user.finalLevel, f, final_pass)] for f in range(first, last + 1)}
+        return {f: self.store[(0, f, final_pass)] for f in range(first, last + 1)}
+
+    def _load_last_saved(self, frame, level):
+        """SynthesisFrame::loadLastSavedOffsets, synthesisFrame.cpp:769-772:
+        pass 0 before any save (a zero-filled vector); a pass never saved
+        leaves the base offsets as they are (the file load fails)."""
+        key = (level, frame, self.last_saved.get((frame, level), 0))
+        if key in self.store:
+            self.o.load_offsets(level, self.store[key][0])
+
+    def _spatial_upsample(self, frame, coarse, fine, save):
+        """SynthesisFrame::spatialUpsample, synthesisFrame.cpp:465-481."""
+        self._load_last_saved(frame, coarse)
+        self.o.upsample(fine)
+        self.o.sync(fine, _abi.DONT_COPY_OFFSETS | _abi.DONT_UPDATE_RESIDUAL)
+        if save:
+            self._save_images(fine, frame, 0)
+
+    def _refine_pass(self, level, last_coarse_pass, this_pass, first, last):
+        """renderRefinePass (REFINE_EVEN_AND_ODD), synthesisProcessor.cpp:
+        1078-1150, and SynthesisFrame::refine, synthesisFrame.cpp:420-463."""
+        o = self.o
+        spatial = last_coarse_pass == this_pass - 1
+        for f in range(first, last + 1):
+            self._update_parameters(f, _abi.BIDIRECTIONAL)
+            self._advect_neighbors(f, level, this_pass - 1, first, last)
+            if spatial:
+                self._spatial_upsample(f, level + 1, level, False)
+            else:
+                self._load_last_saved(f, level)
+                o.sync(level, _abi.DONT_COPY_OFFSETS | _abi.DONT_UPDATE_RESIDUAL)
+            o.load_images(self.frames[f], level)
+            self.propagate_and_scatter(level, self.user.iterations)
+            self._save_images(level, f, this_pass)
+
+    def _render_tctf(self, first, last):
+        """renderAnimationTCTF, synthesisProcessor.cpp:1152-1312, run locally
+        without ribbon inputs (time step 1)."""
+        u = self.user
+        ops = [("consecutive", self.levels - 1)]
+        for level in range(self.levels - 1, u.finalLevel - 1, -1):
+            ops.append(("refine", level))
+            if 1 < last - first:
+                ops += [("refine", level)] * (u.fixupPasses + 1)
+        ops += [("upsample", level) for level in range(u.finalLevel - 1, -1, -1)]
+        self.o.reset_advected()
+        passes_this = passes_last = 0
+        last_level = -1
+        for op, level in ops:
+            if last_level != level:
+                self.o.load_style_level(self.styles, level)
+                passes_last = passes_this
+                last_level = level
+            if op == "consecutive":
+                self._render_pass(level, passes_this, passes_this - 1, first, last)
+                passes_this += 1
+            elif op == "refine":
+                self._refine_pass(level, passes_last - 1, passes_this, first, last)
+                passes_this += 1
+            else:
+                for f in range(first, last + 1):
+                    self._spatial_upsample(f, level + 1, level, True)
+                passes_this = 1
+        return {f: self.store[(0, f, passes_this - 1)] for f in range(first, last + 1)}
 
     def _render_pass(self, level, pass_, source_pass, first, last):
         """renderConsecutivePass, synthesisProcessor.cpp:703-753."""

@@ -148,6 +148,11 @@ def default_params():
     return p
 
 
+def output_level(p):
+    """PT_OUTPUT_LEVEL: the level of the final output of a run."""
+    return p.finalLevel if p.scheme in (S_IND, S_FBMO) else 0
+
+
 PATCH_DTYPE = np.dtype([
     ("x", "<f4"), ("y", "<f4"), ("theta", "<f4"), ("hysteresis", "<f4"),
     ("layer", "<i4"), ("scaleU", "<f4"), ("scaleV", "<f4"),

@@ -141,6 +141,7 @@ struct pt_ctx {
     // SynthesisFrame::_last_saved_pass: (frame, level) -> last pass saved
     // through saveImages
     std::map<std::pair<int, int>, int> last_saved;
+    int out_level = 0, out_pass = 0;  // where the last run's final output was saved
 
     uint64_t launches = 0;
     uint32_t pass_counter = 0;
@@ -402,15 +403,13 @@ static pt_status check_ready(pt_ctx* c, int level, bool need_ex = true, bool nee
     if (need_ex && (!c->ex || !c->ex->base)) return fail(c, PT_ERR_STATE, "no exemplar level loaded");
     if (need_ex) TRY(refresh_interleaved(c, c->ex));
     if (need_img) {
+        // A layered input holds whatever level was last written into it, as
+        // the reference's layered textures do (a kernel at another level
+        // reads that level's texels, and zero outside them), so only its
+        // presence is checked.
         const ImgView& I = c->img;
-        int lw = c->W >> level, lh = c->H >> level;
-        // a layer holds one level (bound at its size) or the full-size
-        // layered array that level uploads write into
-        auto fits = [&](int w, int h) { return (w == lw && h == lh) || (w == c->W && h == c->H); };
-        if (!I.base[I.cur].p || !fits(I.base[I.cur].w, I.base[I.cur].h))
-            return fail(c, PT_ERR_STATE, "input colour of level %d not uploaded", level);
-        if (!I.dt[I.cur].p || !fits(I.dt[I.cur].w, I.dt[I.cur].h))
-            return fail(c, PT_ERR_STATE, "input distance transform of level %d not uploaded", level);
+        if (!I.base[I.cur].p) return fail(c, PT_ERR_STATE, "input colour not uploaded (level %d)", level);
+        if (!I.dt[I.cur].p) return fail(c, PT_ERR_STATE, "input distance transform not uploaded (level %d)", level);
         if (!I.orient.p || !I.scale.p || !I.ids.p)
             return fail(c, PT_ERR_STATE, "input orientation/scale/ids not uploaded");
     }
@@ -1688,6 +1687,17 @@ static pt_status save_images(pt_ctx* c, int level, int frame, int pass, bool wit
     return PT_OK;
 }
 
+// SynthesisFrame::loadLastSavedOffsets, synthesisFrame.cpp:769-772: the
+// frame's last pass saved through saveImages (0 before any, the reference's
+// zero-filled vector); a pass that was never saved leaves the base offsets
+// as they are (WorkingBuffers::loadOffsets fails on the missing file)
+static pt_status load_last_saved_offsets(pt_ctx* c, int frame, int level) {
+    auto it = c->last_saved.find(std::make_pair(frame, level));
+    const int pass = it == c->last_saved.end() ? 0 : it->second;
+    if (!c->store.count(std::make_tuple(level, frame, pass))) return PT_OK;
+    return store_load_offsets(c, level, frame, pass);
+}
+
 // SynthesisFrame::propagateAndScatter, synthesisFrame.cpp:483-508
 //
 // With change tracking (tiled kernels), every pass of the loop is numbered.
@@ -1836,6 +1846,8 @@ static pt_status render_ind(pt_ctx* c, int first, int last) {
     free_store(c);
     const int total = user.fixupPasses + 1;
     const int final_pass = (user.finalLevel == 0) ? total - 1 : 0;
+    c->out_level = user.finalLevel;
+    c->out_pass = final_pass;
     for (int f = first; f <= last; f++) {
         for (int level = user.levels - 1; level >= user.finalLevel; level--) {
             TRY(bind_style_level(c, level));
@@ -1885,9 +1897,7 @@ static pt_status advect_neighbors(pt_ctx* c, int frame, int level, int source_pa
         TRY(bind_frame_level(c, nb, level));
         TRY(pt_flip_anim_buffers(c));
         TRY(bind_frame_anim(c, frame, level));
-        auto it = c->last_saved.find(std::make_pair(nb, level));
-        if (it == c->last_saved.end()) return fail(c, PT_ERR_STATE, "frame %d has no saved level %d", nb, level);
-        TRY(store_load_offsets(c, level, nb, it->second));
+        TRY(load_last_saved_offsets(c, nb, level));
         TRY(pt_advect_offsets(c, level, 1, fwd ? 1 : 0, 0));
     }
     return PT_OK;
@@ -1919,6 +1929,8 @@ static pt_status render_fbmo(pt_ctx* c, int first, int last) {
     TRY(reset_image_slots(c));
     free_store(c);
     const int final_pass = user.fixupPasses + 2;
+    c->out_level = user.finalLevel;
+    c->out_pass = final_pass;
     for (int level = user.levels - 1; level >= user.finalLevel; level--) {
         TRY(bind_style_level(c, level));
         const bool final_level = level == user.finalLevel;
@@ -1959,58 +1971,166 @@ static pt_status render_fbmo(pt_ctx* c, int first, int last) {
     return PT_OK;
 }
 
+// SynthesisProcessor::renderConsecutivePass, synthesisProcessor.cpp:703-753
+static pt_status consecutive_pass(pt_ctx* c, const pt_params& user, int level, int pass, int source_pass, int first,
+                                  int last, bool save_canvas) {
+    const bool forwards = (pass % 2) == 0;
+    std::vector<int> fr;
+    if (forwards) for (int f = first; f <= last; f++) fr.push_back(f);
+    else for (int f = last; f >= first; f--) fr.push_back(f);
+    if (pass > 0) {  // the frame still in memory starts the fix-up pass
+        TRY(store_save(c, level, fr[0], pass, save_canvas));
+        fr.erase(fr.begin());
+    }
+    for (size_t i = 0; i < fr.size(); i++) {
+        const bool is_first = (i == 0) && (pass == 0);
+        if (!is_first) TRY(pt_flip_anim_buffers(c));
+        TRY(bind_frame_level(c, fr[i], level));
+        TRY(synthesize_consecutive(c, user, fr[i], level, pass, is_first, forwards, source_pass, pass == 0,
+                                   save_canvas));
+    }
+    return PT_OK;
+}
+
+// SynthesisFrame::spatialUpsample, synthesisFrame.cpp:465-481: the frame's
+// last saved offsets of the coarse level upsampled (no images are loaded)
+static pt_status spatial_upsample(pt_ctx* c, int frame, int coarse, int fine, bool save, bool save_canvas) {
+    TRY(load_last_saved_offsets(c, frame, coarse));
+    TRY(pt_upsample(c, fine));
+    TRY(do_sync(c, fine, PT_DONT_COPY_OFFSETS | PT_DONT_UPDATE_RESIDUAL));
+    if (save) TRY(save_images(c, fine, frame, 0, save_canvas));
+    return PT_OK;
+}
+
+// SynthesisProcessor::renderAnimationFMBM, synthesisProcessor.cpp:846-878
 static pt_status render_fmbm(pt_ctx* c, int first, int last) {
     const pt_params user = c->params;
-    if (user.levels < 1 || user.finalLevel < 0 || user.finalLevel >= user.levels)
-        return fail(c, PT_ERR_INVALID, "bad levels/finalLevel");
-    for (int f = first; f <= last; f++)
-        if (!c->frames.count(f)) return fail(c, PT_ERR_STATE, "frame %d not set", f);
-    if (user.scheme == PT_S_IND) return render_ind(c, first, last);
-    if (user.scheme == PT_S_FBMO) return render_fbmo(c, first, last);
-    if (user.scheme != PT_S_FMBM && user.scheme != PT_S_FMBM_RM)
-        return fail(c, PT_ERR_UNSUPPORTED, "the TCTF scheme is not implemented");
     TRY(reset_working(c));
     TRY(reset_image_slots(c));
     free_store(c);
     const int total = user.fixupPasses + 1;
     const int final_pass = (user.finalLevel == 0) ? total - 1 : 0;
+    c->out_level = 0;
+    c->out_pass = final_pass;
     for (int level = user.levels - 1; level >= user.finalLevel; level--) {
         TRY(bind_style_level(c, level));
         TRY(pt_reset_advected_buffers(c));
-        for (int pass = 0; pass < total; pass++) {
-            bool forwards = (pass % 2) == 0;
-            std::vector<int> fr;
-            if (forwards) for (int f = first; f <= last; f++) fr.push_back(f);
-            else for (int f = last; f >= first; f--) fr.push_back(f);
-            bool save_canvas = (level == user.finalLevel && pass == final_pass);
-            if (pass > 0) {
-                TRY(store_save(c, level, fr[0], pass, save_canvas));
-                fr.erase(fr.begin());
-            }
-            for (size_t i = 0; i < fr.size(); i++) {
-                bool is_first = (i == 0) && (pass == 0);
-                if (!is_first) TRY(pt_flip_anim_buffers(c));
-                TRY(bind_frame_level(c, fr[i], level));
-                TRY(synthesize_consecutive(c, user, fr[i], level, pass, is_first, forwards, total - 1, pass == 0,
-                                           save_canvas));
-            }
-        }
+        for (int pass = 0; pass < total; pass++)
+            TRY(consecutive_pass(c, user, level, pass, total - 1, first, last,
+                                 level == 0 && pass == final_pass));
         // the coarser level's saved state is no longer needed
+        if (level + 1 < user.levels) drop_store_level(c, level + 1);
+    }
+    // renderSpatialUpsample (:1025-1045) down to level 0 from a final level
+    for (int level = user.finalLevel; level > 0; level--) {
+        TRY(bind_style_level(c, level - 1));
+        for (int f = first; f <= last; f++) TRY(spatial_upsample(c, f, level, level - 1, true, level == 1));
         if (level + 1 < user.levels) drop_store_level(c, level + 1);
     }
     c->params = user;
     return PT_OK;
 }
 
-// the pass whose output copyOutputToFinal hands out
-static int final_pass_of(const pt_params& p) {
-    if (p.scheme == PT_S_FBMO) return p.fixupPasses + 2;
-    return (p.finalLevel == 0) ? p.fixupPasses : 0;
+// SynthesisProcessor::renderRefinePass with REFINE_EVEN_AND_ODD,
+// synthesisProcessor.cpp:1078-1150, and SynthesisFrame::refine,
+// synthesisFrame.cpp:420-463: every frame between its advected neighbours,
+// started from the upsampled coarse level (the level's first refine pass)
+// or from its own last saved pass
+static pt_status refine_pass(pt_ctx* c, const pt_params& user, int level, int last_coarse_pass, int this_pass,
+                             int first, int last, bool save_canvas) {
+    const bool spatial = last_coarse_pass == this_pass - 1;
+    for (int f = first; f <= last; f++) {
+        pt_params p = user;  // updateParameters(BIDIRECTIONAL), :522-542
+        p.advectionJitter = (f % 3 == 0) ? user.advectionJitter * 0.01f : 0.0f;
+        p.direction = PT_BIDIRECTIONAL;
+        TRY(pt_set_params(c, &p));
+        TRY(advect_neighbors(c, f, level, this_pass - 1, first, last));
+        if (spatial) {
+            TRY(spatial_upsample(c, f, level + 1, level, false, false));
+        } else {
+            TRY(load_last_saved_offsets(c, f, level));
+            TRY(do_sync(c, level, PT_DONT_COPY_OFFSETS | PT_DONT_UPDATE_RESIDUAL));
+        }
+        TRY(bind_frame_images(c, f, level));
+        TRY(propagate_and_scatter(c, level, user.iterations, false));
+        TRY(save_images(c, level, f, this_pass, save_canvas));
+    }
+    return PT_OK;
+}
+
+// SynthesisProcessor::renderAnimationTCTF, synthesisProcessor.cpp:1152-1312,
+// run locally with time step 1 (no ribbon inputs, so getMaxRibbonStep gives
+// 1): a consecutive pass at the coarsest level, refine passes at every level
+// from the coarsest to the final one (fixupPasses + 1 more when the range
+// spans more than two frames), then spatial upsampling down to level 0
+static pt_status render_tctf(pt_ctx* c, int first, int last) {
+    const pt_params user = c->params;
+    TRY(reset_working(c));
+    TRY(reset_image_slots(c));
+    free_store(c);
+    enum { CONSECUTIVE, REFINE, UPSAMPLE };
+    std::vector<std::pair<int, int>> ops;  // (operation, level)
+    ops.emplace_back(CONSECUTIVE, user.levels - 1);
+    for (int level = user.levels - 1; level >= user.finalLevel; level--) {
+        ops.emplace_back(REFINE, level);
+        if (1 < last - first)
+            for (int i = 0; i < user.fixupPasses + 1; i++) ops.emplace_back(REFINE, level);
+    }
+    for (int level = user.finalLevel - 1; level >= 0; level--) ops.emplace_back(UPSAMPLE, level);
+    // the pass counters of the schedule (:1257-1285), first to find the pass
+    // whose output is handed out, then to run it
+    auto walk = [&](bool run) -> pt_status {
+        int passes_this = 0, passes_last = 0, last_level = -1;
+        for (const auto& op : ops) {
+            const int level = op.second;
+            if (last_level != level) {
+                if (run) TRY(bind_style_level(c, level));
+                if (run && last_level >= 0 && last_level + 1 < user.levels) drop_store_level(c, last_level + 1);
+                passes_last = passes_this;
+                last_level = level;
+            }
+            const bool final_save = level == 0 && run && passes_this == c->out_pass;
+            if (op.first == CONSECUTIVE) {
+                if (run) TRY(consecutive_pass(c, user, level, passes_this, passes_this - 1, first, last, final_save));
+                passes_this++;
+            } else if (op.first == REFINE) {
+                if (run) TRY(refine_pass(c, user, level, passes_last - 1, passes_this, first, last, final_save));
+                passes_this++;
+            } else {
+                if (run)
+                    for (int f = first; f <= last; f++) TRY(spatial_upsample(c, f, level + 1, level, true, level == 0));
+                passes_this = 1;
+            }
+        }
+        if (!run) c->out_pass = passes_this - 1;
+        return PT_OK;
+    };
+    c->out_level = 0;
+    TRY(walk(false));
+    TRY(pt_reset_advected_buffers(c));
+    TRY(walk(true));
+    c->params = user;
+    return PT_OK;
+}
+
+static pt_status render(pt_ctx* c, int first, int last) {
+    const pt_params& user = c->params;
+    if (user.levels < 1 || user.finalLevel < 0 || user.finalLevel >= user.levels)
+        return fail(c, PT_ERR_INVALID, "bad levels/finalLevel");
+    for (int f = first; f <= last; f++)
+        if (!c->frames.count(f)) return fail(c, PT_ERR_STATE, "frame %d not set", f);
+    switch (user.scheme) {
+        case PT_S_FMBM:
+        case PT_S_FMBM_RM: return render_fmbm(c, first, last);
+        case PT_S_FBMO: return render_fbmo(c, first, last);
+        case PT_S_TCTF: return render_tctf(c, first, last);
+        case PT_S_IND: return render_ind(c, first, last);
+        default: return fail(c, PT_ERR_INVALID, "unknown scheme %d", user.scheme);
+    }
 }
 
 static pt_status fetch_final(pt_ctx* c, int frame, float* out_rgba, pt_patchxf* out_offsets) {
-    const int final_pass = final_pass_of(c->params);
-    auto it = c->store.find(std::make_tuple(c->params.finalLevel, frame, final_pass));
+    auto it = c->store.find(std::make_tuple(c->out_level, frame, c->out_pass));
     if (it == c->store.end()) return fail(c, PT_ERR_STATE, "no final output for frame %d", frame);
     size_t n = (size_t)it->second.w * it->second.h;
     if (out_rgba)
@@ -2025,7 +2145,7 @@ pt_status pt_synthesize_frame(pt_ctx* c, int frame, float* out_rgba, pt_patchxf*
     if (!c) return PT_ERR_INVALID;
     if (!c->initialized || !c->have_params) return fail(c, PT_ERR_STATE, "context not initialized");
     CU(cudaSetDevice(c->device));
-    TRY(render_fmbm(c, frame, frame));
+    TRY(render(c, frame, frame));
     return fetch_final(c, frame, out_rgba, out_offsets);
 }
 
@@ -2033,10 +2153,10 @@ pt_status pt_synthesize_animation(pt_ctx* c, int first, int last, pt_frame_callb
     if (!c || last < first) return PT_ERR_INVALID;
     if (!c->initialized || !c->have_params) return fail(c, PT_ERR_STATE, "context not initialized");
     CU(cudaSetDevice(c->device));
-    TRY(render_fmbm(c, first, last));
+    TRY(render(c, first, last));
     if (cb) {
         // each frame is handed to the callback from page-locked staging
-        int lw = c->W >> c->params.finalLevel, lh = c->H >> c->params.finalLevel;
+        int lw = c->W >> c->out_level, lh = c->H >> c->out_level;
         size_t n = (size_t)lw * lh;
         size_t need = n * (sizeof(float4) + sizeof(pt_patchxf));
         if (c->cb_stage_bytes < need) {

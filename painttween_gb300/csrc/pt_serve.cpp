@@ -56,7 +56,7 @@ pt_status run_request(pt_ctx* c, pt_request& r) {
         PT_TRY(pt_set_frame(c, f, r.image_w, r.image_h, in.rgba, in.orient_tensor, in.dist_trans, in.ids, in.vel_fwd,
                             in.vel_bwd, in.scale));
     }
-    const int fl = r.params.finalLevel;
+    const int fl = PT_OUTPUT_LEVEL(&r.params);
     const size_t n = (size_t)(r.image_w >> fl) * (size_t)(r.image_h >> fl);
     if (r.frames == 1) {
         PT_TRY(pt_synthesize_frame(c, 0, r.out_rgba, r.out_offsets));

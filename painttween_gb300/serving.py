@@ -36,7 +36,7 @@ def _build(requests, offsets, pinned=False):
         p, st, frames = rq["params"], rq["style"], rq["frames"]
         h, w = frames[0]["rgba"].shape[:2]
         sh, sw = st["base"].shape[:2]
-        fl = p.finalLevel
+        fl = _abi.output_level(p)
         oh, ow = h >> fl, w >> fl
         alloc = host_array if pinned else np.empty
         out_rgba = alloc((len(frames), oh, ow, 4), np.float32)

@@ -269,7 +269,7 @@ class Synthesizer(TexSynth):
         self._check(lib().pt_clear_frames(self.h), "pt_clear_frames")
 
     def _final_shape(self):
-        fl = self.params.finalLevel
+        fl = _abi.output_level(self.params)
         return self.H >> fl, self.W >> fl
 
     def synthesize_frame(self, frame):

@@ -539,3 +539,37 @@ def test_fbmo_scheme_matches_oracle(r, fixups):
     for f in range(4):
         assert_offsets_equal(got[f][1], ref[f][0], 1.0, "FBMO frame %d" % f)
         assert_array_equal(got[f][0], ref[f][2], "FBMO output frame %d" % f)
+
+
+@pytest.mark.parametrize("frames,levels,final_level", [(3, 2, 0), (4, 3, 1), (2, 2, 0)])
+def test_tctf_scheme_matches_oracle(frames, levels, final_level):
+    """The TCTF scheme without ribbon inputs (a consecutive pass at the
+    coarsest level, refine passes between advected neighbours at every level,
+    spatial upsampling below the final level) against the oracle."""
+    p = config_params(r=2, levels=levels, iterations=2)
+    p.scheme, p.finalLevel = _abi.S_TCTF, final_level
+    p.temporalCoherenceWeight = 0.5
+    ex = synthetic.make_exemplar(64, 64, seed=73 + frames)
+    clip = synthetic.make_clip(80, 64, 3, frames, seed=74 + frames)
+    got = _animate(p, ex, clip, 80, 64)
+    ref = O.OracleDriver(p, [ex], clip, threads=8).render(0, frames - 1)
+    for f in range(frames):
+        assert got[f][0].shape == (64, 80, 4)
+        assert_offsets_equal(got[f][1], ref[f][0], 1.0, "TCTF frame %d" % f)
+        assert_array_equal(got[f][0], ref[f][2], "TCTF output frame %d" % f)
+
+
+def test_final_level_upsampled_to_full_size_matches_oracle():
+    """FMBM with a final level above 0: the final level's offsets upsampled
+    level by level to the full image (renderSpatialUpsample)."""
+    p = config_params(r=2, levels=3, iterations=2)
+    p.finalLevel = 1
+    p.temporalCoherenceWeight = 0.5
+    ex = synthetic.make_exemplar(64, 64, seed=79)
+    clip = synthetic.make_clip(80, 64, 3, 3, seed=80)
+    got = _animate(p, ex, clip, 80, 64)
+    ref = O.OracleDriver(p, [ex], clip, threads=8).render(0, 2)
+    for f in range(3):
+        assert got[f][0].shape == (64, 80, 4)
+        assert_offsets_equal(got[f][1], ref[f][0], 1.0, "frame %d" % f)
+        assert_array_equal(got[f][0], ref[f][2], "output frame %d" % f)

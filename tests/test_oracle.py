@@ -181,3 +181,22 @@ def test_fbmo_merge_pass_takes_each_record_from_a_directional_pass():
         assert (from_fw | from_bw).all()
         assert from_fw.any() and from_bw.any() and not (from_fw & from_bw).all()
         assert drv.last_saved[(f, 0)] == 3  # the fix-up pass, not the merge
+
+
+@pytest.mark.parametrize("scheme,final_level,full", [(_abi.S_FMBM_RM, 1, True), (_abi.S_TCTF, 1, True),
+                                                     (_abi.S_TCTF, 0, True), (_abi.S_IND, 1, False)])
+def test_output_level_of_each_scheme(scheme, final_level, full):
+    """FMBM and TCTF upsample a final level > 0 down to level 0 (the level
+    copyOutputToFinal hands out); IND hands out its final level."""
+    p = _abi.default_params()
+    p.residualWindowSize, p.levels, p.iterations = 2, 3, 1
+    p.scheme, p.finalLevel, p.fixupPasses = scheme, final_level, 1
+    ex = synthetic.make_exemplar(48, 48, seed=71)
+    clip = synthetic.make_clip(64, 48, 3, 3, seed=72)
+    out = O.OracleDriver(p, [ex], clip, threads=4).render(0, 2)
+    lv = _abi.output_level(p)
+    assert lv == (0 if full else final_level)
+    for f in range(3):
+        offs, res, rgba = out[f]
+        assert offs.shape == (48 >> lv, 64 >> lv) and rgba.shape == (48 >> lv, 64 >> lv, 4)
+        assert np.isfinite(rgba).all()
