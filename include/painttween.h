@@ -58,6 +58,15 @@ typedef struct {
     float lumShiftY, lumShiftA; /* Luminance luminanceShift {y, a} */
 } pt_patchxf;
 
+/* RibbonP (types.h:111-126): accumulated motion from a pixel to a keyframe
+ * (x, y), the frames it spans and the keyframe's index; layer < 0 marks an
+ * invalid ribbon.  As an RGBA image (toColor4) it is (time_step, y, x,
+ * layer). */
+typedef struct {
+    float x, y;
+    int32_t time_step, layer;
+} pt_ribbon;
+
 /* Pass direction (types.h:122-126). */
 enum { PT_FORWARD = 0, PT_BACKWARD = 1, PT_BIDIRECTIONAL = 2 };
 
@@ -103,7 +112,7 @@ typedef struct {
     float timeDerivativeOutputWeight;
     float temporalCoherenceWeight;
     float hysteresisWeight;
-    int32_t interpolateKeyFrame; /* must be 0: keyframe mode not implemented */
+    int32_t interpolateKeyFrame; /* keyframe kernels (step-wise calls only) */
     int32_t useGuide;
     int32_t currentInterpolationIndex;
     int32_t numFrames;
@@ -141,6 +150,10 @@ enum {
     PT_LAYER_INPUT_VEL_F = 12,
     PT_LAYER_INPUT_VEL_B_PREVIOUS = 13,
     PT_LAYER_INPUT_VEL_F_PREVIOUS = 14,
+    PT_LAYER_CUMUL_FIELD_B = 17,          /* key-to-key ribbons, layer = key index */
+    PT_LAYER_CUMUL_FIELD_F = 18,
+    PT_LAYER_FRAME_TO_KEY_RIBBON_B = 19,  /* frame-to-key ribbons of the level */
+    PT_LAYER_FRAME_TO_KEY_RIBBON_F = 20,
     PT_LAYER_RANDOM = 21
 };
 
@@ -235,6 +248,34 @@ pt_status pt_reset_advected_buffers(pt_ctx* ctx); /* workingBuffers.cpp:112-116 
  * residualCache.base().copyTo(advectedF/B.residual()), the merge set-up of
  * renderAnimationFBMO (synthesisProcessor.cpp:979-980). */
 pt_status pt_copy_offsets_to_advected(pt_ctx* ctx, int forwards);
+
+/* ---- keyframe interpolation (texSynth_kernel.cu:290-304,723-1110,
+ *      1728-1853,2061-2118,2138-2142).  With params.interpolateKeyFrame set,
+ *      pt_propagate / pt_scatter run propagate_kernel_keys /
+ *      scatter_kernel_keys, which also test the candidates that the
+ *      key-to-key cumulative fields carry to the keys firstKeyIndex ..
+ *      lastKeyIndex; with key_index >= 0 a pixel under that key's mask (the
+ *      alpha of exemplar output layer key_index at the pixel) takes the key
+ *      (propagate) or keeps its offset (scatter).  The cumulative fields and
+ *      frame-to-key ribbons are uploaded as RGBA images
+ *      (pt_upload_image_color4 with PT_LAYER_CUMUL_FIELD_B/F, style = key
+ *      layer, and PT_LAYER_FRAME_TO_KEY_RIBBON_B/F).  The keyframe driver
+ *      (keyFramesPreprocess, accumulateRibbon) is not implemented:
+ *      pt_synthesize_* return PT_ERR_UNSUPPORTED with interpolateKeyFrame. */
+pt_status pt_initialize_cumulative_fields(pt_ctx* ctx, int w, int h, int layers); /* :2138 */
+/* The ribbon field (working <- base carried along the velocities from the
+ * previous frame, then copied to base) and advectedF.output <- the canvas at
+ * each ribbon's end (accumulateRibbonField, :1830-1853). */
+pt_status pt_accumulate_ribbon_field(pt_ctx* ctx, int level, int forwards, int time_step, int overwrite);
+/* Offsets from the frame-to-key ribbons, random where a ribbon is invalid
+ * (offsetsFromFrameToKeyRibbon, :2111-2118; ends with a sync). */
+pt_status pt_offsets_from_frame_to_key_ribbon(pt_ctx* ctx, int level, int look_forwards);
+/* ribbonField.base() and canvasOutputCache to and from the host (level
+ * rectangle, row-major), advectedF/B.output() to the host. */
+pt_status pt_load_ribbon_field(pt_ctx* ctx, int level, const pt_ribbon* ribbons);
+pt_status pt_get_ribbon_field(pt_ctx* ctx, int level, pt_ribbon* out);
+pt_status pt_load_canvas(pt_ctx* ctx, int level, const float* rgba);
+pt_status pt_get_advected_output(pt_ctx* ctx, int forwards, int level, float* out_rgba);
 
 /* ---- state transfer (WorkingBuffers load/getOutput,
  *      workingBuffers.cpp:118-207) ---------------------------------------- */

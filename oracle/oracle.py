@@ -78,6 +78,19 @@ def lib():
             "pto_downsample_vote": (None, [vp, i, i, vp]),
             "pto_tensor_to_angle": (None, [vp, i, vp]),
             "pto_convolve_separable": (None, [vp, vp, i, i, i]),
+            "pto_propagate_k": (None, [vp, i, i, i]),
+            "pto_scatter_k": (None, [vp, i, u32, i]),
+            "pto_propagate_keys": (None, [vp, i, i, i]),
+            "pto_scatter_keys": (None, [vp, i, i]),
+            "pto_init_cumulative_fields": (None, [vp, i, i, i]),
+            "pto_upload_cumul": (None, [vp, i, i, vp, i, i]),
+            "pto_upload_f2k": (None, [vp, i, vp, i, i]),
+            "pto_accumulate_ribbon": (None, [vp, i, i, i, i]),
+            "pto_frame_to_key_ribbon": (None, [vp, i, i]),
+            "pto_load_ribbon": (None, [vp, i, vp]),
+            "pto_get_ribbon": (None, [vp, i, vp]),
+            "pto_load_canvas": (None, [vp, i, vp]),
+            "pto_get_advected_output": (None, [vp, i, i, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -302,14 +315,57 @@ class Oracle:
     def randomize_offsets(self, level):
         lib().pto_randomize(self.h, level)
 
-    def propagate(self, level, jump):
-        lib().pto_propagate(self.h, level, jump)
+    def propagate(self, level, jump, key=-1):
+        """TexSynth::propagate, texSynth_kernel.cu:1306-1357: the keyframe
+        kernel when interpolateKeyFrame is set."""
+        if self.params.interpolateKeyFrame:
+            lib().pto_propagate_keys(self.h, level, jump, key)
+        else:
+            lib().pto_propagate_k(self.h, level, jump, key)
         lib().pto_sync(self.h, level, 0)
 
-    def scatter(self, level):
-        lib().pto_scatter_pass(self.h, level, self.pass_counter)
+    def scatter(self, level, key=-1):
+        """TexSynth::scatter, texSynth_kernel.cu:1360-1401."""
+        if self.params.interpolateKeyFrame:
+            lib().pto_scatter_keys(self.h, level, key)
+        else:
+            lib().pto_scatter_k(self.h, level, self.pass_counter, key)
         self.pass_counter += 1
         lib().pto_sync(self.h, level, 0)
+
+    # --- keyframe interpolation ----------------------------------------------
+    def init_cumulative_fields(self, w, h, n):
+        lib().pto_init_cumulative_fields(self.h, w, h, n)
+
+    def upload_cumulative_field(self, forwards, layer, rgba):
+        a = _c(rgba, np.float32)
+        lib().pto_upload_cumul(self.h, int(forwards), layer, _p(a), a.shape[1], a.shape[0])
+
+    def upload_frame_to_key_ribbon(self, forwards, rgba):
+        a = _c(rgba, np.float32)
+        lib().pto_upload_f2k(self.h, int(forwards), _p(a), a.shape[1], a.shape[0])
+
+    def accumulate_ribbon_field(self, level, forwards, time_step, overwrite):
+        lib().pto_accumulate_ribbon(self.h, level, int(forwards), time_step, int(overwrite))
+
+    def offsets_from_frame_to_key_ribbon(self, level, look_forwards):
+        lib().pto_frame_to_key_ribbon(self.h, level, int(look_forwards))
+
+    def load_ribbon_field(self, level, rib):
+        lib().pto_load_ribbon(self.h, level, _p(np.ascontiguousarray(rib)))
+
+    def get_ribbon_field(self, level):
+        out = np.empty((self.lh(level), self.lw(level)), _abi.RIBBON_DTYPE)
+        lib().pto_get_ribbon(self.h, level, _p(out))
+        return out
+
+    def load_canvas(self, level, rgba):
+        lib().pto_load_canvas(self.h, level, _p(_c(rgba, np.float32)))
+
+    def get_advected_output(self, forwards, level):
+        out = np.empty((self.lh(level), self.lw(level), 4), np.float32)
+        lib().pto_get_advected_output(self.h, int(forwards), level, _p(out))
+        return out
 
     def upsample(self, level):
         lib().pto_upsample(self.h, level)

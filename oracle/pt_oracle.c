@@ -83,6 +83,12 @@ typedef struct {
     float* hist_base; float* hist_work; /* SW x (SH*NS) */
     pt_patchxf* adv_off[2]; f4* adv_base[2]; f4* adv_out[2];
     float* adv_res[2]; int32_t* adv_ts[2]; /* [0] = F, [1] = B */
+    /* keyframe interpolation: key-to-key cumulative fields [0] = B, [1] = F
+     * (layered by key index, cf_w x cf_h, linear filter), frame-to-key
+     * ribbons [0] = B, [1] = F (level arrays), the ribbon field pair */
+    f4* cumul[2]; int cf_w, cf_h, cf_n;
+    f4* f2k[2]; int fk_w[2], fk_h[2];
+    pt_ribbon* rib_base; pt_ribbon* rib_work;
     int threads;
 } pto;
 
@@ -658,12 +664,15 @@ static pt_patchxf propagate_offset(const pto* o, const pt_patchxf* src, int tx, 
 
 /* propagate_kernel, texSynth_kernel.cu:1112-1219 (advected candidates at
  * :1184-1216 are rebuilt with hysteresis 0 at :981 and never tested) */
-void pto_propagate(pto* o, int level, int jump) {
+static float keymask_alpha(const pto* o, int x, int y, int key);
+/* with key >= 0, pixels under the key's mask take the key itself (:1137-1142) */
+void pto_propagate_k(pto* o, int level, int jump, int key) {
     const pt_patchxf* base = o->off_base;
     pt_patchxf* work = o->off_work;
     FOR_RECT(o, level) {
         size_t k = (size_t)y * o->W + x;
         if (image_culled(o, x, y)) { work[k] = patch(0, 0, 0, 0, 0, 1.f, 1.f); continue; }
+        if (keymask_alpha(o, x, y, key) > 0) { work[k] = patch((float)x, (float)y, 0.f, 1.f, key, 1.f, 1.f); continue; }
         float best = o->res_base[k];
         float ia = o->img_base[o->cur][k].w;
         pt_patchxf ow = base[k];
@@ -682,19 +691,23 @@ void pto_propagate(pto* o, int level, int jump) {
         work[k] = ow;
     }
 }
+void pto_propagate(pto* o, int level, int jump) { pto_propagate_k(o, level, jump, -1); }
 
 /* scatter_kernel + averageOffset, texSynth_kernel.cu:841-952; the reference's
  * randFloat() returns unsigned int 0 (texSynth_util.h:155-163), so every
  * candidate is (best.x + 0.9*dist, best.y). */
-void pto_scatter_pass(pto* o, int level, uint32_t pass_id);
-void pto_scatter(pto* o, int level) { pto_scatter_pass(o, level, 0); }
-void pto_scatter_pass(pto* o, int level, uint32_t pass_id) {
+void pto_scatter_k(pto* o, int level, uint32_t pass_id, int key);
+void pto_scatter(pto* o, int level) { pto_scatter_k(o, level, 0, -1); }
+void pto_scatter_pass(pto* o, int level, uint32_t pass_id) { pto_scatter_k(o, level, pass_id, -1); }
+/* with key >= 0, pixels under the key's mask keep their offset (:887-892) */
+void pto_scatter_k(pto* o, int level, uint32_t pass_id, int key) {
     const pt_patchxf* base = o->off_base;
     pt_patchxf* work = o->off_work;
     FOR_RECT(o, level) {
         size_t k = (size_t)y * o->W + x;
         if (image_culled(o, x, y)) continue;
         pt_patchxf off = base[k];
+        if (keymask_alpha(o, x, y, key) > 0) { work[k] = off; continue; }
         float cached = o->res_base[k];
         float best = (float)((double)cached + 10e-7);
         pt_patchxf ow = off;
@@ -1143,6 +1156,9 @@ pto* pto_create(int W, int H, int SW, int SH, int NS) {
     o->res_base = (float*)zalloc(n * sizeof(float));
     o->res_work = (float*)zalloc(n * sizeof(float));
     o->canvas = (f4*)zalloc(n * sizeof(f4));
+    o->rib_base = (pt_ribbon*)zalloc(n * sizeof(pt_ribbon));
+    o->rib_work = (pt_ribbon*)zalloc(n * sizeof(pt_ribbon));
+    for (size_t i = 0; i < n; i++) o->rib_base[i].layer = o->rib_work[i].layer = -1; /* RibbonP() */
     size_t hn = (size_t)SW * SH * NS;
     o->hist_base = (float*)zalloc(hn * sizeof(float));
     o->hist_work = (float*)zalloc(hn * sizeof(float));
@@ -1159,6 +1175,8 @@ void pto_destroy(pto* o) {
     free(o->hist_base); free(o->hist_work);
     free(o->img_orient); free(o->img_scale); free(o->img_ids); free(o->rnd);
     free(o->ex_base); free(o->ex_out); free(o->ex_orient); free(o->ex_dt); free(o->ex_ids);
+    free(o->cumul[0]); free(o->cumul[1]); free(o->f2k[0]); free(o->f2k[1]);
+    free(o->rib_base); free(o->rib_work);
     free(o);
 }
 
@@ -1253,6 +1271,296 @@ void pto_reset_advected(pto* o) {
         memset(o->adv_out[l], 0, n * sizeof(f4)); memset(o->adv_res[l], 0, n * sizeof(float));
         memset(o->adv_ts[l], 0, n * sizeof(int32_t));
     }
+}
+
+/* ------------------------------------------------------------------------ */
+/* keyframe interpolation                                                   */
+/* ------------------------------------------------------------------------ */
+
+/* TexSynth::initialize_cumulativeFields, texSynth_kernel.cu:2138-2142 */
+void pto_init_cumulative_fields(pto* o, int w, int h, int n) {
+    for (int d = 0; d < 2; d++) {
+        free(o->cumul[d]);
+        o->cumul[d] = (f4*)zalloc((size_t)w * h * n * sizeof(f4));
+    }
+    o->cf_w = w; o->cf_h = h; o->cf_n = n;
+}
+/* uploadImage_Color4 of TS_LAYER_CUMUL_FIELD_B/F (layer = key index) and
+ * TS_LAYER_FRAME_TO_KEY_RIBBON_B/F, texSynth_kernel.cu:2196-2206 */
+void pto_upload_cumul(pto* o, int forwards, int layer, const float* rgba, int w, int h) {
+    f4* dst = o->cumul[forwards ? 1 : 0] + (size_t)layer * o->cf_w * o->cf_h;
+    for (int y = 0; y < h; y++) memcpy(dst + (size_t)y * o->cf_w, rgba + (size_t)y * w * 4, (size_t)w * sizeof(f4));
+}
+void pto_upload_f2k(pto* o, int forwards, const float* rgba, int w, int h) {
+    int d = forwards ? 1 : 0;
+    free(o->f2k[d]);
+    o->f2k[d] = (f4*)zalloc((size_t)w * h * sizeof(f4));
+    memcpy(o->f2k[d], rgba, (size_t)w * h * sizeof(f4));
+    o->fk_w[d] = w; o->fk_h[d] = h;
+}
+/* a cumulative-field fetch at exemplar (u, v) of key layer j: linear filter,
+ * clamp; a layer that was never uploaded reads zero */
+static f4 cumul_sample(const pto* o, int forwards, float u, float v, int j) {
+    f4 z = {0, 0, 0, 0};
+    const f4* F = o->cumul[forwards ? 1 : 0];
+    if (!F || j < 0 || j >= o->cf_n) return z;
+    bl_t b = bl_setup(u, v, o->cf_w, o->cf_h);
+    const f4* L = F + (size_t)j * o->cf_w * o->cf_h;
+    return bl4(&b, L[(size_t)b.y0 * o->cf_w + b.x0], L[(size_t)b.y0 * o->cf_w + b.x1],
+               L[(size_t)b.y1 * o->cf_w + b.x0], L[(size_t)b.y1 * o->cf_w + b.x1]);
+}
+/* a frame-to-key ribbon texel at integer (x, y): point read, clamp */
+static f4 f2k_texel(const pto* o, int forwards, int x, int y) {
+    int d = forwards ? 1 : 0;
+    f4 z = {0, 0, 0, 0};
+    if (!o->f2k[d]) return z;
+    x = clampi(x, 0, o->fk_w[d] - 1); y = clampi(y, 0, o->fk_h[d] - 1);
+    return o->f2k[d][(size_t)y * o->fk_w[d] + x];
+}
+/* RibbonP(Color4): (x, y, time_step, layer) = (b, g, r, a) */
+static pt_ribbon ribbon_of(f4 c) {
+    pt_ribbon r;
+    r.x = c.z; r.y = c.y; r.time_step = f2i(c.x); r.layer = f2i(c.w);
+    return r;
+}
+/* the keyframe mask of key layer `key` at pixel (x, y): the key's output
+ * alpha (PYRAMID_FETCH_LAYER(gExemplarOutput, x, y, keyIndex)) */
+static float keymask_alpha(const pto* o, int x, int y, int key) {
+    if (key < 0) return -1.0f;
+    return ex_sample_out(o, (float)x, (float)y, key).w;
+}
+
+/* propagate_kernel_keys, texSynth_kernel.cu:984-1110 */
+void pto_propagate_keys(pto* o, int level, int jump, int key) {
+    const pt_patchxf* base = o->off_base;
+    pt_patchxf* work = o->off_work;
+    FOR_RECT(o, level) {
+        size_t k = (size_t)y * o->W + x;
+        if (image_culled(o, x, y)) { work[k] = patch(0, 0, 0, 0, 0, 1.f, 1.f); continue; }
+        if (keymask_alpha(o, x, y, key) > 0) { work[k] = patch((float)x, (float)y, 0.f, 1.f, key, 1.f, 1.f); continue; }
+        float best = o->res_base[k];
+        float ia = o->img_base[o->cur][k].w;
+        pt_patchxf ow = base[k];
+        pixctx pc;
+        make_pixctx(o, x, y, level, &pc);
+        for (int c = 0; c < 4; c++) {
+            int tx = x, ty = y;
+            if (c == 0) tx = x + jump;
+            else if (c == 1) tx = x - jump;
+            else if (c == 2) ty = y + jump;
+            else ty = y - jump;
+            pt_patchxf t = propagate_offset(o, base, tx, ty, x, y);
+            float r = test_offset(o, x, y, &t, level, ia, &pc);
+            if (r < best) { ow = t; best = r; }
+            const float ex0 = t.x, ey0 = t.y;
+            const int elayer = t.layer;
+            float ex = ex0, ey = ey0;
+            for (int j = elayer - 1; j >= o->p.firstKeyIndex; j--) {
+                f4 m = cumul_sample(o, 0, ex, ey, j + 1);
+                if (m.x < -EPSILON_F) break;
+                ex = ex + m.z; ey = ey + m.y;
+                pt_patchxf q = patch(ex, ey, screen_to_exemplar_angle(o, x, y, ex, ey, j), 0.f, j, 1.f, 1.f);
+                r = test_offset(o, x, y, &q, level, ia, &pc);
+                if (r < best) { ow = q; best = r; }
+            }
+            ex = ex0; ey = ey0;
+            for (int j = elayer + 1; j <= o->p.lastKeyIndex; j++) {
+                f4 m = cumul_sample(o, 1, ex, ey, j - 1);
+                if (m.x < -EPSILON_F) break;
+                ex = ex + m.z; ey = ey + m.y;
+                pt_patchxf q = patch(ex, ey, screen_to_exemplar_angle(o, x, y, ex, ey, j), 0.f, j, 1.f, 1.f);
+                r = test_offset(o, x, y, &q, level, ia, &pc);
+                if (r < best) { ow = q; best = r; }
+            }
+        }
+        work[k] = ow;
+    }
+}
+
+/* scatter_kernel_keys, texSynth_kernel.cu:723-839 (randFloat() is 0: the
+ * candidate is (best.x + 0.9*dist, best.y)) */
+void pto_scatter_keys(pto* o, int level, int key) {
+    const pt_patchxf* base = o->off_base;
+    pt_patchxf* work = o->off_work;
+    const int span = o->p.lastKeyIndex - o->p.firstKeyIndex + 1;
+    const int samples = span != 0 ? o->p.scatterSamplesCount / span : 0;
+    FOR_RECT(o, level) {
+        size_t k = (size_t)y * o->W + x;
+        if (image_culled(o, x, y)) continue;
+        pt_patchxf off = base[k];
+        if (keymask_alpha(o, x, y, key) > 0) { work[k] = off; continue; }
+        float cached = o->res_base[k];
+        float best = (float)((double)cached + 10e-7);
+        pt_patchxf ow = off;
+        float ia = o->img_base[o->cur][k].w;
+        float dist = (float)(o->ew > o->eh ? o->ew : o->eh);
+        const float closest = 10.f, factor = 0.9f;
+        pixctx pc;
+        make_pixctx(o, x, y, level, &pc);
+        for (int i = 0; i < samples && dist * factor >= closest; i++) {
+            float dmin = dist * factor;
+            float ex = ow.x + dmin, ey = ow.y + 0.0f;
+            clamp_to_exemplar(&ex, &ey, o->ew, o->eh);
+            const int elayer = ow.layer;
+            pt_patchxf t = patch(ex, ey, screen_to_exemplar_angle(o, x, y, ex, ey, elayer), 0.f, elayer, 1.f, 1.f);
+            float r = test_offset(o, x, y, &t, level, ia, &pc);
+            if (r < best) { ow = t; best = r; }
+            const float ex0 = ex, ey0 = ey;
+            for (int j = elayer - 1; j >= o->p.firstKeyIndex; j--) {
+                pt_ribbon m = ribbon_of(cumul_sample(o, 0, ex, ey, j + 1));
+                if (m.layer < 0) break;
+                ex = ex + m.x; ey = ey + m.y;
+                pt_patchxf q = patch(ex, ey, screen_to_exemplar_angle(o, x, y, ex, ey, j), 0.f, j, 1.f, 1.f);
+                r = test_offset(o, x, y, &q, level, ia, &pc);
+                if (r < best) { ow = q; best = r; }
+            }
+            ex = ex0; ey = ey0;
+            for (int j = elayer + 1; j <= o->p.lastKeyIndex; j++) {
+                pt_ribbon m = ribbon_of(cumul_sample(o, 1, ex, ey, j - 1));
+                if (m.layer < 0) break;
+                ex = ex + m.x; ey = ey + m.y;
+                pt_patchxf q = patch(ex, ey, screen_to_exemplar_angle(o, x, y, ex, ey, j), 0.f, j, 1.f, 1.f);
+                r = test_offset(o, x, y, &q, level, ia, &pc);
+                if (r < best) { ow = q; best = r; }
+            }
+            dist *= factor;
+        }
+        if (best < cached) work[k] = ow;
+    }
+}
+
+/* calculateTranslatedPosition, texSynth_kernel.cu:1540-1574, for a buffer
+ * of the level's size */
+static int translated_position(const pto* o, int forwards, int x, int y, int level, float* ptx, float* pty) {
+    int prev = (o->cur + 1) % 2;
+    f2 fw, bk;
+    float tx, ty;
+    if (forwards) {
+        bk = vel_texel(o->vel_b[o->cur], o, x, y);
+        tx = (float)x + bk.x; ty = (float)y + bk.y;
+        fw = vel_bilinear(o->vel_f[prev], o, tx, ty);
+    } else {
+        fw = vel_texel(o->vel_f[o->cur], o, x, y);
+        tx = (float)x + fw.x; ty = (float)y + fw.y;
+        bk = vel_bilinear(o->vel_b[prev], o, tx, ty);
+    }
+    fw.x = -fw.x; fw.y = -fw.y;
+    float ddx = fw.x - bk.x, ddy = fw.y - bk.y;
+    float dist = sqrtf(fmaf(ddy, ddy, ddx * ddx));
+    float cxf = fminf(fmaxf(ceilf(tx), -2.f), 1e9f), cyf = fminf(fmaxf(ceilf(ty), -2.f), 1e9f);
+    float fxf = fminf(fmaxf(floorf(tx), -2.f), 1e9f), fyf = fminf(fmaxf(floorf(ty), -2.f), 1e9f);
+    *ptx = tx; *pty = ty;
+    return in_rect(o, f2i(cxf), f2i(cyf), level, 0) && in_rect(o, f2i(fxf), f2i(fyf), level, 0) &&
+           (dist < (float)(1.414 * 2));
+}
+
+/* accumulateAdvectionKernel + cumulativeAdvectionFieldToOutput +
+ * TexSynth::accumulateRibbonField, texSynth_kernel.cu:290-304,1728-1853
+ * (cacheVelocities is display-only).  The chained comparison of :1776 is
+ * kept as written: ((l00 == l10) == l01) == l11 compares booleans with
+ * layers. */
+void pto_accumulate_ribbon(pto* o, int level, int forwards, int time_step, int overwrite) {
+    const pt_ribbon* src = o->rib_base;
+    pt_ribbon* dest = o->rib_work;
+    FOR_RECT(o, level) {
+        size_t k = (size_t)y * o->W + x;
+        pt_ribbon out = {0.f, 0.f, 0, -1};
+        float tx, ty;
+        int masked = img_texel(o, o->cur, x, y).w == 0.0f;
+        if (masked || !translated_position(o, forwards, x, y, level, &tx, &ty)) {
+            if (overwrite) dest[k] = out;
+            continue;
+        }
+        int ftx = (int)floorf(tx), fty = (int)floorf(ty), ctx = (int)ceilf(tx), cty = (int)ceilf(ty);
+        pt_ribbon s00 = src[(size_t)fty * o->W + ftx], s10 = src[(size_t)fty * o->W + ctx];
+        pt_ribbon s01 = src[(size_t)cty * o->W + ftx], s11 = src[(size_t)cty * o->W + ctx];
+        int v00 = s00.layer >= 0, v10 = s10.layer >= 0, v01 = s01.layer >= 0, v11 = s11.layer >= 0;
+        if (!(v00 || v10 || v01 || v11)) {
+            if (overwrite) dest[k] = out;
+            continue;
+        }
+        int all_valid = v00 && v10 && v01 && v11;
+        int same = (((s00.layer == s10.layer) == s01.layer) == s11.layer);
+        const float th = 5.f;
+        int diverges = fabsf(s00.x - s10.x) > th || fabsf(s00.x - s01.x) > th || fabsf(s00.x - s11.x) > th ||
+                       fabsf(s00.y - s10.y) > th || fabsf(s00.y - s01.y) > th || fabsf(s00.y - s11.y) > th;
+        if (!all_valid || !same || diverges) {
+            int rtx = (int)roundf(tx), rty = (int)roundf(ty);
+            if (ftx == rtx && fty == rty) out = s00;
+            else if (ftx + 1 == rtx && fty == rty) out = s10;
+            else if (ftx == rtx && fty + 1 == rty) out = s01;
+            else out = s11;
+        } else {
+            float wx = tx - (float)ftx, wy = ty - (float)fty;
+            float rx0 = s00.x * (1.f - wx) + s10.x * wx;
+            float ry0 = s00.y * (1.f - wx) + s10.y * wx;
+            float rx1 = s01.x * (1.f - wx) + s11.x * wx;
+            float ry1 = s01.y * (1.f - wx) + s11.y * wx;
+            out.x = rx0 * (1.f - wy) + rx1 * wy;
+            out.y = ry0 * (1.f - wy) + ry1 * wy;
+            out.time_step = s00.time_step;
+            out.layer = s00.layer;
+        }
+        out.x = out.x + (tx - (float)x);
+        out.y = out.y + (ty - (float)y);
+        out.time_step = out.time_step + time_step;
+        pt_ribbon cur = dest[k];
+        if (overwrite || cur.layer < 0 || fabsf((float)cur.time_step) >= fabsf((float)out.time_step)) dest[k] = out;
+    }
+    memcpy(o->rib_base, o->rib_work, sizeof(pt_ribbon) * (size_t)o->W * o->H); /* copyWorkingToBase */
+    /* cumulativeAdvectionFieldToOutput into advectedF.output from the
+     * canvas (keyFrame.pixel(x + field.x, y + field.y), truncated to int;
+     * a position outside the image reads zero) */
+    FOR_RECT(o, level) {
+        size_t k = (size_t)y * o->W + x;
+        pt_ribbon f = o->rib_base[k];
+        f4 c = {0, 0, 0, 0};
+        if (f.layer >= 0) {
+            int px = f2i((float)x + f.x), py = f2i((float)y + f.y);
+            if (px >= 0 && py >= 0 && px < o->W && py < o->H) c = o->canvas[(size_t)py * o->W + px];
+        }
+        o->adv_out[0][k] = c;
+    }
+}
+
+/* copyFrameToKeyRibbonKernel + TexSynth::offsetsFromFrameToKeyRibbon,
+ * texSynth_kernel.cu:2061-2097,2111-2118 */
+void pto_frame_to_key_ribbon(pto* o, int level, int look_forwards) {
+    pt_patchxf* work = o->off_work;
+    FOR_RECT(o, level) {
+        size_t k = (size_t)y * o->W + x;
+        pt_ribbon rb = ribbon_of(f2k_texel(o, look_forwards, x, y));
+        pt_patchxf out;
+        if (rb.layer >= 0) {
+            float ox = rb.x + (float)x, oy = rb.y + (float)y;
+            out = patch(ox, oy, screen_to_exemplar_angle(o, x, y, ox, oy, rb.layer), 1.0f, rb.layer, 1.f, 1.f);
+        } else {
+            f4 r = rnd_texel(o, x, y); /* copyRandomKernel's toPatchXF */
+            out = patch(r.x, r.y, r.z, 0.f, f2i(r.w), 1.f, 1.f);
+        }
+        work[k] = out;
+    }
+    pto_sync(o, level, 0);
+}
+
+/* ribbonField.base() copyFromHost / copyToHost of the level rectangle;
+ * canvasOutputCache.copyFromHost; advectedF/B.output().copyToHost */
+void pto_load_ribbon(pto* o, int level, const pt_ribbon* src) {
+    int w = lvl_w(o, level), h = lvl_h(o, level);
+    for (int y = 0; y < h; y++) memcpy(o->rib_base + (size_t)y * o->W, src + (size_t)y * w, w * sizeof(pt_ribbon));
+}
+void pto_get_ribbon(const pto* o, int level, pt_ribbon* out) {
+    int w = lvl_w(o, level), h = lvl_h(o, level);
+    for (int y = 0; y < h; y++) memcpy(out + (size_t)y * w, o->rib_base + (size_t)y * o->W, w * sizeof(pt_ribbon));
+}
+void pto_load_canvas(pto* o, int level, const float* rgba) {
+    int w = lvl_w(o, level), h = lvl_h(o, level);
+    for (int y = 0; y < h; y++) memcpy(o->canvas + (size_t)y * o->W, rgba + (size_t)y * w * 4, w * sizeof(f4));
+}
+void pto_get_advected_output(const pto* o, int forwards, int level, float* out) {
+    int w = lvl_w(o, level), h = lvl_h(o, level);
+    const f4* src = o->adv_out[forwards ? 0 : 1];
+    for (int y = 0; y < h; y++) memcpy(out + (size_t)y * w * 4, src + (size_t)y * o->W, w * sizeof(f4));
 }
 
 /* WorkingBuffers::loadOffsets / loadResidual, workingBuffers.cpp:166-207 */

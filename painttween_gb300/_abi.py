@@ -148,6 +148,12 @@ def default_params():
     return p
 
 
+RIBBON_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("time_step", "<i4"), ("layer", "<i4")])
+assert RIBBON_DTYPE.itemsize == 16
+LAYER_CUMUL_FIELD_B, LAYER_CUMUL_FIELD_F = 17, 18
+LAYER_FRAME_TO_KEY_RIBBON_B, LAYER_FRAME_TO_KEY_RIBBON_F = 19, 20
+
+
 def output_level(p):
     """PT_OUTPUT_LEVEL: the level of the final output of a run."""
     return p.finalLevel if p.scheme in (S_IND, S_FBMO) else 0

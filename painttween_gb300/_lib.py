@@ -47,6 +47,13 @@ SIGNATURES = {
     "pt_sync_buffers": (_I, [_VP, _I, _I]),
     "pt_reset_advected_buffers": (_I, [_VP]),
     "pt_copy_offsets_to_advected": (_I, [_VP, _I]),
+    "pt_initialize_cumulative_fields": (_I, [_VP, _I, _I, _I]),
+    "pt_accumulate_ribbon_field": (_I, [_VP, _I, _I, _I, _I]),
+    "pt_offsets_from_frame_to_key_ribbon": (_I, [_VP, _I, _I]),
+    "pt_load_ribbon_field": (_I, [_VP, _I, _VP]),
+    "pt_get_ribbon_field": (_I, [_VP, _I, _VP]),
+    "pt_load_canvas": (_I, [_VP, _I, _VP]),
+    "pt_get_advected_output": (_I, [_VP, _I, _I, _VP]),
     "pt_load_offsets": (_I, [_VP, _I, _VP]),
     "pt_load_residual": (_I, [_VP, _I, _VP]),
     "pt_get_offsets": (_I, [_VP, _I, _VP]),

@@ -114,6 +114,13 @@ struct pt_ctx {
     float2* up_velf[2] = {nullptr, nullptr};
     float2* up_velb[2] = {nullptr, nullptr};
     bool slot_copy = false;  // driver binds copy into the layered arrays (IND)
+    // keyframe interpolation: cumulative fields (B, F), frame-to-key ribbons
+    // (B, F) and the ribbon field pair ([0] base, [1] working)
+    float4* cumul[2] = {nullptr, nullptr};
+    int cf_w = 0, cf_h = 0, cf_n = 0;
+    float4* f2k_buf[2] = {nullptr, nullptr};
+    Arr<float4> f2k[2]{};
+    ptk::Ribbon* rib[2] = {nullptr, nullptr};
     float* up_orient = nullptr;
     float2* up_scale = nullptr;
     int* up_ids = nullptr;
@@ -357,6 +364,8 @@ static Params make_params(pt_ctx* c, int level) {
     P.distTransCull = p.distTransCull;
     P.direction = p.direction;
     P.scatterSamples = p.scatterSamplesCount;
+    P.firstKey = p.firstKeyIndex;
+    P.lastKey = p.lastKeyIndex;
     P.rngMode = p.rngMode;
     P.rngSeed = p.rngSeed;
     P.histPitch = c->SW;
@@ -757,7 +766,6 @@ pt_status pt_set_params(pt_ctx* c, const pt_params* p) {
     if (p->residualWindowSize < 0 || p->residualWindowSize > ptk::kMaxRadius)
         return fail(c, PT_ERR_INVALID, "residualWindowSize %d outside [0, %d]", p->residualWindowSize,
                     ptk::kMaxRadius);
-    if (p->interpolateKeyFrame) return fail(c, PT_ERR_UNSUPPORTED, "keyframe interpolation is not implemented");
     if (p->colorspace != 0) return fail(c, PT_ERR_UNSUPPORTED, "only the RGB colour space is implemented");
     if (p->numStyles < 1 || p->numStyles > PT_MAX_STYLES) return fail(c, PT_ERR_INVALID, "numStyles out of range");
     if (p->rngMode != PT_RNG_REFERENCE && p->rngMode != PT_RNG_COUNTER)
@@ -815,6 +823,11 @@ pt_status pt_initialize(pt_ctx* c, int iw, int ih, int sw, int sh, int ns) {
     }
     dfree_t(c, c->canvas); dfree_t(c, c->up_orient); dfree_t(c, c->up_scale); dfree_t(c, c->up_ids);
     dfree_t(c, c->rnd);
+    for (int i = 0; i < 2; i++) {
+        dfree_t(c, c->cumul[i]); dfree_t(c, c->f2k_buf[i]); dfree_t(c, c->rib[i]);
+        c->f2k[i] = Arr<float4>{};
+    }
+    c->cf_w = c->cf_h = c->cf_n = 0;
     dfree_t(c, c->chg); dfree_t(c, c->stamp_last); dfree_t(c, c->stamp_win);
     dfree_t(c, c->tap_cache);
     c->tap_cache_k = 0;
@@ -911,6 +924,14 @@ pt_status pt_initialize_exemplars(pt_ctx* c, int w, int h, int ns) {
 // Host-to-device copy that has finished reading `src` on return, so callers
 // may reuse or free their host buffer at once (the reference's uploads are
 // synchronous as well).
+// a level rectangle between a host array and a full-pitch device buffer
+static pt_status rect_copy(pt_ctx* c, void* dst, size_t dpitch, const void* src, size_t spitch, size_t row_bytes,
+                           int rows, cudaMemcpyKind kind) {
+    CU(cudaMemcpy2DAsync(dst, dpitch, src, spitch, row_bytes, rows, kind, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return PT_OK;
+}
+
 static pt_status h2d(pt_ctx* c, void* dst, const void* src, size_t bytes) {
     CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream));
     CU(cudaStreamSynchronize(c->stream));
@@ -967,11 +988,27 @@ pt_status pt_upload_image_color4(pt_ctx* c, int level, int layer, const float* r
         c->up_ex.bo_stale = true;
         return PT_OK;
     }
+    if (layer == PT_LAYER_CUMUL_FIELD_B || layer == PT_LAYER_CUMUL_FIELD_F) {
+        const int d = layer == PT_LAYER_CUMUL_FIELD_F ? 1 : 0;
+        if (!c->cumul[d] || style < 0 || style >= c->cf_n || w > c->cf_w || h > c->cf_h)
+            return fail(c, PT_ERR_INVALID, "cumulative field %dx%d layer %d does not fit pt_initialize_cumulative_fields",
+                        w, h, style);
+        float4* dst = c->cumul[d] + (size_t)style * c->cf_w * c->cf_h;
+        return rect_copy(c, dst, (size_t)c->cf_w * sizeof(float4), rgba, (size_t)w * sizeof(float4),
+                         (size_t)w * sizeof(float4), h, cudaMemcpyHostToDevice);
+    }
     if (level < 0 || w != (c->W >> level) || h != (c->H >> level))
         return fail(c, PT_ERR_INVALID, "image upload %dx%d does not match level %d", w, h, level);
     int cur = c->img.cur;
     if (layer == PT_LAYER_INPUT_COLOR)
         return slot_write(c, &c->up_base[cur], &c->img.base[cur], rgba, w, h, cudaMemcpyHostToDevice);
+    if (layer == PT_LAYER_FRAME_TO_KEY_RIBBON_B || layer == PT_LAYER_FRAME_TO_KEY_RIBBON_F) {
+        const int d = layer == PT_LAYER_FRAME_TO_KEY_RIBBON_F ? 1 : 0;
+        if (!c->f2k_buf[d]) TRY(dalloc_t(c, &c->f2k_buf[d], (size_t)c->W * c->H));
+        TRY(h2d(c, c->f2k_buf[d], rgba, n * sizeof(float4)));
+        c->f2k[d] = Arr<float4>{c->f2k_buf[d], w, h};
+        return PT_OK;
+    }
     if (layer == PT_LAYER_RANDOM) {
         if (!c->rnd) TRY(dalloc_t(c, &c->rnd, (size_t)c->W * c->H));
         TRY(h2d(c, c->rnd, rgba, n * sizeof(float4)));
@@ -1138,45 +1175,151 @@ pt_status pt_randomize_offsets(pt_ctx* c, int level) {
     return do_sync(c, level, 0);
 }
 
-// one propagate pass into the working buffer
-static pt_status propagate_pass(pt_ctx* c, int level, int jump) {
+static ptk::KeyView key_view(const pt_ctx* c) {
+    ptk::KeyView K{};
+    K.cumul[0] = c->cumul[0];
+    K.cumul[1] = c->cumul[1];
+    K.w = c->cf_w;
+    K.h = c->cf_h;
+    K.n = c->cf_n;
+    K.f2k[0] = c->f2k[0];
+    K.f2k[1] = c->f2k[1];
+    return K;
+}
+
+// one propagate pass into the working buffer; a keyframe layer (key >= 0)
+// or keyframe interpolation takes the generic kernels
+static pt_status propagate_pass(pt_ctx* c, int level, int jump, int key = -1) {
     PatchPlanes work;
     TRY(writable_work(c, level, &work));
     Params P = make_params(c, level);
+    const bool keys = c->params.interpolateKeyFrame != 0;
     return profiled(c, PT_KERNEL_PROPAGATE, P, [&](const Params& Q) {
+        if (keys) return pt::launch_propagate_keys(Q, work, jump, key, key_view(c), c->stream);
         bool done = false;
-        cudaError_t e = launch_tiled(c, 0, Q, work, jump, 0, nullptr, &done);
-        return done ? e : pt::launch_propagate(Q, work, jump, c->stream);
+        cudaError_t e = key >= 0 ? cudaSuccess : launch_tiled(c, 0, Q, work, jump, 0, nullptr, &done);
+        return done ? e : pt::launch_propagate(Q, work, jump, key, c->stream);
     });
 }
 
-static pt_status scatter_pass(pt_ctx* c, int level) {
+static pt_status scatter_pass(pt_ctx* c, int level, int key = -1) {
     bool aliased = false;
     PatchPlanes work;
     TRY(writable_work(c, level, &work, &aliased));
     Params P = make_params(c, level);
     uint32_t pass_id = c->pass_counter++;
+    const bool keys = c->params.interpolateKeyFrame != 0;
     return profiled(c, PT_KERNEL_SCATTER, P, [&](const Params& Q) {
+        if (keys) return pt::launch_scatter_keys(Q, work, aliased ? 1 : 0, key, key_view(c), c->stream);
         bool done = false;
-        cudaError_t e = launch_tiled(c, 1, Q, work, aliased ? 1 : 0, pass_id, nullptr, &done);
-        return done ? e : pt::launch_scatter(Q, work, aliased ? 1 : 0, pass_id, c->stream);
+        cudaError_t e = key >= 0 ? cudaSuccess : launch_tiled(c, 1, Q, work, aliased ? 1 : 0, pass_id, nullptr, &done);
+        return done ? e : pt::launch_scatter(Q, work, aliased ? 1 : 0, pass_id, key, c->stream);
     });
 }
 
 pt_status pt_propagate(pt_ctx* c, int level, int jump, int key_index) {
     if (!c) return PT_ERR_INVALID;
     TRY(check_ready(c, level));
-    if (key_index >= 0) return fail(c, PT_ERR_UNSUPPORTED, "keyframe propagation is not implemented");
-    TRY(propagate_pass(c, level, jump));
+    if (key_index >= c->NS) return fail(c, PT_ERR_INVALID, "key index %d outside the %d style layers", key_index, c->NS);
+    TRY(propagate_pass(c, level, jump, key_index));
     return do_sync(c, level, 0);
 }
 
 pt_status pt_scatter(pt_ctx* c, int level, int key_index) {
     if (!c) return PT_ERR_INVALID;
     TRY(check_ready(c, level));
-    if (key_index >= 0) return fail(c, PT_ERR_UNSUPPORTED, "keyframe scatter is not implemented");
-    TRY(scatter_pass(c, level));
+    if (key_index >= c->NS) return fail(c, PT_ERR_INVALID, "key index %d outside the %d style layers", key_index, c->NS);
+    TRY(scatter_pass(c, level, key_index));
     return do_sync(c, level, 0);
+}
+
+// --- keyframe interpolation -----------------------------------------------------
+
+// TexSynth::initialize_cumulativeFields, texSynth_kernel.cu:2138-2142: the
+// key-to-key fields, `layers` layers of w x h, zeroed
+pt_status pt_initialize_cumulative_fields(pt_ctx* c, int w, int h, int layers) {
+    if (!c || w < 1 || h < 1 || layers < 1) return PT_ERR_INVALID;
+    if (!c->initialized) return fail(c, PT_ERR_STATE, "pt_initialize has not been called");
+    const size_t n = (size_t)w * h * layers;
+    for (int d = 0; d < 2; d++) {
+        dfree_t(c, c->cumul[d]);
+        TRY(dalloc_t(c, &c->cumul[d], n));
+        CU(cudaMemsetAsync(c->cumul[d], 0, n * sizeof(float4), c->stream));
+    }
+    c->cf_w = w;
+    c->cf_h = h;
+    c->cf_n = layers;
+    return PT_OK;
+}
+
+static pt_status ensure_ribbons(pt_ctx* c) {
+    const size_t n = (size_t)c->W * c->H;
+    for (int i = 0; i < 2; i++) {
+        if (c->rib[i]) continue;
+        TRY(dalloc_t(c, &c->rib[i], n));
+        LN(pt::launch_fill_ribbons(c->rib[i], n, c->stream));
+    }
+    return PT_OK;
+}
+
+// TexSynth::accumulateRibbonField, texSynth_kernel.cu:1830-1853
+pt_status pt_accumulate_ribbon_field(pt_ctx* c, int level, int forwards, int time_step, int overwrite) {
+    if (!c) return PT_ERR_INVALID;
+    TRY(check_ready(c, level, false, true));
+    if (!c->img.velf[1 - c->img.cur].p && !c->img.velb[1 - c->img.cur].p)
+        return fail(c, PT_ERR_STATE, "no previous-frame velocities");
+    TRY(ensure_ribbons(c));
+    Params P = make_params(c, level);
+    LN(pt::launch_accumulate_ribbon(P, forwards ? 1 : 0, c->rib[1], c->rib[0], time_step, overwrite ? 1 : 0,
+                                    c->stream));
+    // ribbonField.copyWorkingToBase
+    CU(cudaMemcpyAsync(c->rib[0], c->rib[1], (size_t)c->W * c->H * sizeof(ptk::Ribbon), cudaMemcpyDeviceToDevice,
+                       c->stream));
+    LN(pt::launch_ribbon_output(P, c->rib[0], c->canvas, c->adv[0].out, c->stream));
+    return PT_OK;
+}
+
+// TexSynth::offsetsFromFrameToKeyRibbon, texSynth_kernel.cu:2111-2118
+pt_status pt_offsets_from_frame_to_key_ribbon(pt_ctx* c, int level, int look_forwards) {
+    if (!c) return PT_ERR_INVALID;
+    TRY(check_ready(c, level));
+    if (!c->img.rnd.p) return fail(c, PT_ERR_STATE, "no random level");
+    PatchPlanes work;
+    TRY(writable_work(c, level, &work));
+    Params P = make_params(c, level);
+    LN(pt::launch_frame_to_key(P, work, look_forwards ? 1 : 0, key_view(c), c->stream));
+    return do_sync(c, level, 0);
+}
+
+// ribbonField.base().copyFromHost / copyToHost, workingBuffers.cpp
+pt_status pt_load_ribbon_field(pt_ctx* c, int level, const pt_ribbon* rib) {
+    if (!c || !rib) return PT_ERR_INVALID;
+    TRY(check_ready(c, level, false, false));
+    TRY(ensure_ribbons(c));
+    const size_t lw = (size_t)(c->W >> level), rb = sizeof(pt_ribbon);
+    return rect_copy(c, c->rib[0], c->W * rb, rib, lw * rb, lw * rb, c->H >> level, cudaMemcpyHostToDevice);
+}
+pt_status pt_get_ribbon_field(pt_ctx* c, int level, pt_ribbon* out) {
+    if (!c || !out) return PT_ERR_INVALID;
+    TRY(check_ready(c, level, false, false));
+    TRY(ensure_ribbons(c));
+    const size_t lw = (size_t)(c->W >> level), rb = sizeof(pt_ribbon);
+    return rect_copy(c, out, lw * rb, c->rib[0], c->W * rb, lw * rb, c->H >> level, cudaMemcpyDeviceToHost);
+}
+// canvasOutputCache.copyFromHost (accumulateRibbon puts a keyframe there)
+pt_status pt_load_canvas(pt_ctx* c, int level, const float* rgba) {
+    if (!c || !rgba) return PT_ERR_INVALID;
+    TRY(check_ready(c, level, false, false));
+    const size_t lw = (size_t)(c->W >> level), px = sizeof(float4);
+    return rect_copy(c, c->canvas, c->W * px, rgba, lw * px, lw * px, c->H >> level, cudaMemcpyHostToDevice);
+}
+// advectedF/B.output().copyToHost (the guide colours of accumulateRibbon)
+pt_status pt_get_advected_output(pt_ctx* c, int forwards, int level, float* out) {
+    if (!c || !out) return PT_ERR_INVALID;
+    TRY(check_ready(c, level, false, false));
+    const size_t lw = (size_t)(c->W >> level), px = sizeof(float4);
+    return rect_copy(c, out, lw * px, c->adv[forwards ? 0 : 1].out, c->W * px, lw * px, c->H >> level,
+                     cudaMemcpyDeviceToHost);
 }
 
 pt_status pt_upsample(pt_ctx* c, int fine_level) {
@@ -2115,6 +2258,10 @@ static pt_status render_tctf(pt_ctx* c, int first, int last) {
 
 static pt_status render(pt_ctx* c, int first, int last) {
     const pt_params& user = c->params;
+    if (user.interpolateKeyFrame)
+        return fail(c, PT_ERR_UNSUPPORTED,
+                    "the keyframe driver (keyFramesPreprocess, accumulateRibbon) is not implemented; the keyframe "
+                    "kernels are reached through the step-wise calls");
     if (user.levels < 1 || user.finalLevel < 0 || user.finalLevel >= user.levels)
         return fail(c, PT_ERR_INVALID, "bad levels/finalLevel");
     for (int f = first; f <= last; f++)

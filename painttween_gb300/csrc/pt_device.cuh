@@ -272,6 +272,11 @@ __device__ __forceinline__ float ex_sample_out_alpha(const ExView& e, float u, f
     return bl1(b, __ldg(r0 + 4 * b.x0 + 3), __ldg(r0 + 4 * b.x1 + 3),
                __ldg(r1 + 4 * b.x0 + 3), __ldg(r1 + 4 * b.x1 + 3));
 }
+// the mask of keyframe layer `key` at pixel (x, y): the key's output alpha
+// (PYRAMID_FETCH_LAYER(gExemplarOutput, x, y, keyIndex)); -1 without a key
+__device__ __forceinline__ float keymask_alpha(const ExView& e, int x, int y, int key) {
+    return key < 0 ? -1.0f : ex_sample_out_alpha(e, (float)x, (float)y, key);
+}
 __device__ __forceinline__ float ex_sample_dt(const ExView& e, float u, float v, int layer) {
     Bl b = bl_setup(u, v, e.w, e.h);
     const float* D = e.dt + (size_t)ex_layer(e, layer) * e.w * e.h;

@@ -13,8 +13,24 @@ using ptk::ExView;
 using ptk::Params;
 using ptk::PatchPlanes;
 
-cudaError_t launch_propagate(const Params& P, PatchPlanes work, int jump, cudaStream_t s);
-cudaError_t launch_scatter(const Params& P, PatchPlanes work, int write_all, uint32_t pass_id, cudaStream_t s);
+using ptk::KeyView;
+using ptk::Ribbon;
+
+cudaError_t launch_propagate(const Params& P, PatchPlanes work, int jump, int key, cudaStream_t s);
+cudaError_t launch_scatter(const Params& P, PatchPlanes work, int write_all, uint32_t pass_id, int key,
+                           cudaStream_t s);
+// keyframe interpolation (pt_keys.cu)
+cudaError_t launch_propagate_keys(const Params& P, PatchPlanes work, int jump, int key, const KeyView& K,
+                                  cudaStream_t s);
+cudaError_t launch_scatter_keys(const Params& P, PatchPlanes work, int write_all, int key, const KeyView& K,
+                                cudaStream_t s);
+cudaError_t launch_accumulate_ribbon(const Params& P, int forwards, Ribbon* dest, const Ribbon* src, int time_step,
+                                     int overwrite, cudaStream_t s);
+cudaError_t launch_ribbon_output(const Params& P, const Ribbon* rib, const float4* canvas, float4* out,
+                                 cudaStream_t s);
+cudaError_t launch_frame_to_key(const Params& P, PatchPlanes work, int look_forwards, const KeyView& K,
+                                cudaStream_t s);
+cudaError_t launch_fill_ribbons(Ribbon* r, size_t n, cudaStream_t s);
 cudaError_t launch_residual(const Params& P, float* out, cudaStream_t s);
 cudaError_t launch_canvas(const Params& P, float4* canvas, cudaStream_t s);
 cudaError_t launch_random_offsets(const Params& P, PatchPlanes work, cudaStream_t s);

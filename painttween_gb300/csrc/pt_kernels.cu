@@ -25,10 +25,15 @@ namespace ptk {
     const size_t k = (size_t)y * P.W + x;
 
 // propagate_kernel, :1112-1219 (advected candidates are dead code, :981)
-__global__ void __launch_bounds__(128) k_propagate(const Params P, PatchPlanes work, int jump) {
+// With key >= 0, a pixel under the key's mask takes the key (:1137-1142).
+__global__ void __launch_bounds__(128) k_propagate(const Params P, PatchPlanes work, int jump, int key) {
     PIXEL_XY
     if (image_culled(P, x, y)) {
         store_patch(work, k, make_patch(0, 0, 0, 0, 0, 1.f, 1.f));
+        return;
+    }
+    if (keymask_alpha(P.ex, x, y, key) > 0.0f) {
+        store_patch(work, k, make_patch((float)x, (float)y, 0.f, 1.f, key, 1.f, 1.f));
         return;
     }
     float best = __ldg(P.res + k);
@@ -67,11 +72,13 @@ __global__ void __launch_bounds__(128) k_propagate(const Params P, PatchPlanes w
 // (best.x + 0.9*dist_i, best.y).  COUNTER mode draws r and theta in [0, 1)
 // and [0, 2pi) from a counter-based hash.  write_all: the working buffer
 // aliases base, so unchanged pixels are written too.
-__global__ void __launch_bounds__(128) k_scatter(const Params P, PatchPlanes work, int write_all, uint32_t pass_id) {
+// With key >= 0, a pixel under the key's mask keeps its offset (:887-892).
+__global__ void __launch_bounds__(128) k_scatter(const Params P, PatchPlanes work, int write_all, uint32_t pass_id,
+                                                 int key) {
     PIXEL_XY
     Patch off = load_patch(P.off, k);
-    if (image_culled(P, x, y)) {
-        if (write_all) store_patch(work, k, off);
+    if (image_culled(P, x, y) || keymask_alpha(P.ex, x, y, key) > 0.0f) {
+        if (write_all || !image_culled(P, x, y)) store_patch(work, k, off);
         return;
     }
     float cached = __ldg(P.res + k);
@@ -556,12 +563,13 @@ static const dim3 kPix(32, 4);
 
 #define LAUNCH_CHECK() return cudaGetLastError()
 
-cudaError_t launch_propagate(const Params& P, PatchPlanes work, int jump, cudaStream_t s) {
-    k_propagate<<<grid2(P.lw, P.lh, kPix), kPix, 0, s>>>(P, work, jump);
+cudaError_t launch_propagate(const Params& P, PatchPlanes work, int jump, int key, cudaStream_t s) {
+    k_propagate<<<grid2(P.lw, P.lh, kPix), kPix, 0, s>>>(P, work, jump, key);
     LAUNCH_CHECK();
 }
-cudaError_t launch_scatter(const Params& P, PatchPlanes work, int write_all, uint32_t pass_id, cudaStream_t s) {
-    k_scatter<<<grid2(P.lw, P.lh, kPix), kPix, 0, s>>>(P, work, write_all, pass_id);
+cudaError_t launch_scatter(const Params& P, PatchPlanes work, int write_all, uint32_t pass_id, int key,
+                           cudaStream_t s) {
+    k_scatter<<<grid2(P.lw, P.lh, kPix), kPix, 0, s>>>(P, work, write_all, pass_id, key);
     LAUNCH_CHECK();
 }
 cudaError_t launch_residual(const Params& P, float* out, cudaStream_t s) {

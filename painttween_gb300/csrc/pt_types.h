@@ -70,6 +70,21 @@ struct AdvView {
     int* ts;
 };
 
+// Keyframe interpolation inputs: the key-to-key cumulative fields
+// [0] = backward, [1] = forward (n key layers of w x h RGBA texels, RibbonP
+// packed as (time_step, y, x, layer), linear filter) and the level's
+// frame-to-key ribbons [0] = backward, [1] = forward (point reads).
+struct KeyView {
+    const float4* cumul[2];
+    int w, h, n;
+    Arr<float4> f2k[2];
+};
+// RibbonP (types.h:111-126) in the ribbon field buffers; layer < 0 = invalid
+struct Ribbon {
+    float x, y;
+    int time_step, layer;
+};
+
 // Change tracking across the passes of one propagate/scatter loop.  A pass
 // sets chg[k] = 1 where it changed pixel k's offset record (any of its 36
 // bytes); the sync after it stamps last[k] (the last pass that changed k's
@@ -107,6 +122,7 @@ struct Params {
     int distTransCull;
     int direction;
     int scatterSamples;
+    int firstKey, lastKey;     // first and last keyframe layer (keyframe interpolation)
     int rngMode;
     uint32_t rngSeed;
     int histW, histH;          // histogram level size (style w, style h * ns) >> level

@@ -204,6 +204,37 @@ class TexSynth:
     def copy_offsets_to_advected(self, forwards):
         self._check(lib().pt_copy_offsets_to_advected(self.h, int(forwards)), "pt_copy_offsets_to_advected")
 
+    # -- keyframe interpolation (TexSynth::accumulateRibbonField,
+    #    offsetsFromFrameToKeyRibbon, initialize_cumulativeFields) -----------------
+    def initialize_cumulative_fields(self, w, h, layers):
+        self._check(lib().pt_initialize_cumulative_fields(self.h, w, h, layers), "pt_initialize_cumulative_fields")
+
+    def accumulate_ribbon_field(self, level, forwards, time_step, overwrite):
+        self._check(lib().pt_accumulate_ribbon_field(self.h, level, int(forwards), time_step, int(overwrite)),
+                    "pt_accumulate_ribbon_field")
+
+    def offsets_from_frame_to_key_ribbon(self, level, look_forwards):
+        self._check(lib().pt_offsets_from_frame_to_key_ribbon(self.h, level, int(look_forwards)),
+                    "pt_offsets_from_frame_to_key_ribbon")
+
+    def load_ribbon_field(self, level, ribbons):
+        a = np.ascontiguousarray(ribbons, dtype=_abi.RIBBON_DTYPE)
+        self._check(lib().pt_load_ribbon_field(self.h, level, _p(a)), "pt_load_ribbon_field")
+
+    def get_ribbon_field(self, level):
+        out = np.empty((self.H >> level, self.W >> level), _abi.RIBBON_DTYPE)
+        self._check(lib().pt_get_ribbon_field(self.h, level, _p(out)), "pt_get_ribbon_field")
+        return out
+
+    def load_canvas(self, level, rgba):
+        a = _c(rgba, np.float32)
+        self._check(lib().pt_load_canvas(self.h, level, _p(a)), "pt_load_canvas")
+
+    def get_advected_output(self, forwards, level):
+        out = np.empty((self.H >> level, self.W >> level, 4), np.float32)
+        self._check(lib().pt_get_advected_output(self.h, int(forwards), level, _p(out)), "pt_get_advected_output")
+        return out
+
     def convolve_separable(self, src_dev, dst_dev, w, h, pitch, radius):
         """Gaussian blur of a device float image (device pointers as ints)."""
         self._check(lib().pt_convolve_separable(self.h, ctypes.c_void_p(src_dev), ctypes.c_void_p(dst_dev), w, h,

@@ -1,0 +1,230 @@
+"""Keyframe interpolation kernels against the oracle, bit for bit.
+
+Keys are exemplar layers of the frame's size (the reference loads keyframes
+as style layers).  Covered: the key mask of propagate_kernel / scatter_kernel
+(key_index >= 0), propagate_kernel_keys / scatter_kernel_keys walking the
+key-to-key cumulative fields, accumulateAdvectionKernel with its output
+(accumulateRibbonField) and copyFrameToKeyRibbonKernel
+(offsetsFromFrameToKeyRibbon), src/PaintTweenCUDA/texSynth_kernel.cu:
+290-304,723-1110,1728-1853,2061-2118.
+"""
+import numpy as np
+import pytest
+
+from painttween_gb300 import TexSynth, _abi, synthetic
+from oracle import oracle as O
+
+from _harness import assert_array_equal, assert_offsets_equal, config_params
+
+pytestmark = pytest.mark.gpu
+
+W, H = 64, 48
+NK = 3  # key layers
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(gpu_lib):
+    return gpu_lib
+
+
+def _keys():
+    keys = [synthetic.make_exemplar(W, H, seed=90 + i) for i in range(NK)]
+    yy, xx = np.mgrid[0:H, 0:W]
+    mask = ((xx - 40) ** 2 + (yy - 20) ** 2) < 12 ** 2
+    out = keys[1]["output"].copy()
+    out[..., 3] = np.where(mask, 1.0, 0.0)
+    keys[1]["output"] = out
+    return keys
+
+
+def _ribbon_image(rng, valid=0.7):
+    """A ribbon field as an RGBA image (time_step, y, x, layer)."""
+    img = np.zeros((H, W, 4), np.float32)
+    img[..., 0] = rng.integers(1, 4, (H, W))
+    img[..., 1] = rng.normal(0.0, 2.0, (H, W))
+    img[..., 2] = rng.normal(0.0, 2.0, (H, W))
+    layer = rng.integers(0, NK, (H, W)).astype(np.float32)
+    bad = rng.random((H, W)) > valid
+    layer[bad] = -1.0
+    img[..., 0][bad] = -1.0
+    img[..., 3] = layer
+    return img
+
+
+def _ribbons(rng, valid=0.7):
+    r = np.zeros((H, W), _abi.RIBBON_DTYPE)
+    r["x"] = rng.normal(0.0, 3.0, (H, W))
+    r["y"] = rng.normal(0.0, 3.0, (H, W))
+    r["time_step"] = rng.integers(-3, 4, (H, W))
+    r["layer"] = np.where(rng.random((H, W)) < valid, rng.integers(0, NK, (H, W)), -1)
+    return r
+
+
+class KeyPair:
+    """The oracle and the GPU library with NK key layers at level 0."""
+
+    def __init__(self, p, frames=2, seed=5):
+        self.keys = _keys()
+        self.sps = [O.style_pyramids(k) for k in self.keys]
+        clip = synthetic.make_clip(W, H, 3, frames, seed=seed)
+        rgba = clip[-1]["rgba"].copy()
+        rgba[30:40, 5:25, 3] = 0.0  # masked-out pixels for the ribbon accumulation
+        clip[-1]["rgba"] = rgba
+        self.fps = [O.frame_pyramids(f) for f in clip]
+        self.o = O.Oracle(W, H, W, H, NK, threads=8)
+        self.g = TexSynth(device=0)
+        self.g.initialize(W, H, W, H, NK)
+        self.set_params(p)
+        self.o.load_style_level(self.sps, 0)
+        g = self.g
+        g.initialize_exemplars(W, H, NK)
+        for k, s in enumerate(self.sps):
+            g.upload_image_color4(0, _abi.LAYER_EXEMPLAR_BASE, s["base"][0], k)
+            g.upload_image_color4(0, _abi.LAYER_EXEMPLAR_OUTPUT, s["output"][0], k)
+            g.upload_image_float(0, _abi.LAYER_EXEMPLAR_ORIENTATION, s["orient"][0], k)
+            g.upload_image_float(0, _abi.LAYER_EXEMPLAR_DIST_TRANS, s["dt"][0], k)
+            g.upload_image_int(0, _abi.LAYER_EXEMPLAR_OBJECT_IDS, s["ids"][0], k)
+
+    def close(self):
+        self.g.close()
+        self.o.close()
+
+    def set_params(self, p):
+        self.o.set_params(p)
+        self.g.set_params(p)
+
+    def load_frame(self, f):
+        fp = self.fps[f]
+        self.o.load_frame_level(fp, 0)
+        g = self.g
+        g.upload_image_color4(0, _abi.LAYER_INPUT_COLOR, fp["rgba"][0])
+        g.upload_image_float(0, _abi.LAYER_INPUT_ORIENTATION, fp["orient"][0])
+        g.upload_image_int(0, _abi.LAYER_INPUT_ID, fp["ids"][0])
+        g.upload_image_float2(0, _abi.LAYER_INPUT_VEL_B, fp["velb"][0])
+        g.upload_image_float2(0, _abi.LAYER_INPUT_VEL_F, fp["velf"][0])
+        g.upload_image_float(0, _abi.LAYER_INPUT_DIST_TRANS, fp["dt"][0])
+        g.upload_image_float2(0, _abi.LAYER_INPUT_SCALE, fp["scale"][0])
+
+    def random(self, f, seed=7):
+        fp = self.fps[f]
+        rnd = O.random_level(seed, 0, W, H, fp["rgba"][0], fp["orient"][0], self.sps[0]["output"][0],
+                             self.sps[0]["orient"][0], False, True)
+        self.o.upload_random(rnd)
+        self.g.upload_image_color4(0, _abi.LAYER_RANDOM, rnd)
+
+    def flip(self):
+        self.o.flip()
+        self.g.flip_anim_buffers()
+
+    def both(self, name, *args):
+        getattr(self.o, name)(*args)
+        getattr(self.g, name)(*args)
+
+    def compare(self, what):
+        assert_offsets_equal(self.g.get_offsets(0), self.o.get_offsets(0), 1.0, "offsets " + what)
+        assert_array_equal(self.g.get_residual(0), self.o.get_residual(0), "residual " + what)
+        assert_array_equal(self.g.get_output(0), self.o.get_output(0), "output " + what)
+
+
+def _params(keys=False):
+    p = config_params(r=2)
+    p.numStyles = NK
+    if keys:
+        p.interpolateKeyFrame = 1
+        p.firstKeyIndex, p.lastKeyIndex = 0, NK - 1
+    return p
+
+
+def test_key_mask_in_propagate_and_scatter():
+    kp = KeyPair(_params())
+    try:
+        kp.load_frame(0)
+        kp.random(0)
+        kp.both("randomize_offsets", 0)
+        for jump in (8, 1):
+            kp.both("propagate", 0, jump, 1)
+            kp.compare("propagate, key 1, jump %d" % jump)
+        kp.both("scatter", 0, 1)
+        kp.compare("scatter, key 1")
+        # under the mask the key's own positions on layer 1
+        offs = kp.g.get_offsets(0)
+        yy, xx = np.mgrid[0:H, 0:W]
+        inside = ((xx - 40) ** 2 + (yy - 20) ** 2) < 10 ** 2
+        assert (offs["layer"][inside] == 1).all()
+        assert (offs["x"][inside] == xx[inside]).all() and (offs["y"][inside] == yy[inside]).all()
+        kp.both("scatter", 0, -1)
+        kp.compare("scatter, no key")
+    finally:
+        kp.close()
+
+
+def _upload_cumulative(kp, rng):
+    kp.o.init_cumulative_fields(W, H, NK)
+    kp.g.initialize_cumulative_fields(W, H, NK)
+    for fwd, layer_id in ((False, _abi.LAYER_CUMUL_FIELD_B), (True, _abi.LAYER_CUMUL_FIELD_F)):
+        for j in range(NK):
+            img = _ribbon_image(rng)
+            kp.o.upload_cumulative_field(fwd, j, img)
+            kp.g.upload_image_color4(0, layer_id, img, j)
+
+
+def test_keyframe_propagate_and_scatter_through_cumulative_fields():
+    kp = KeyPair(_params(keys=True))
+    try:
+        _upload_cumulative(kp, np.random.default_rng(11))
+        kp.load_frame(0)
+        kp.random(0)
+        kp.both("randomize_offsets", 0)
+        for jump in (16, 4, 1):
+            kp.both("propagate", 0, jump, -1)
+            kp.compare("propagate_kernel_keys jump %d" % jump)
+        kp.both("scatter", 0, -1)
+        kp.compare("scatter_kernel_keys")
+        kp.both("propagate", 0, 0, 1)
+        kp.compare("propagate_kernel_keys jump 0, key 1")
+        kp.both("scatter", 0, 2)
+        kp.compare("scatter_kernel_keys, key 2")
+    finally:
+        kp.close()
+
+
+def test_accumulate_ribbon_field():
+    kp = KeyPair(_params())
+    rng = np.random.default_rng(12)
+    try:
+        kp.load_frame(0)
+        kp.flip()
+        kp.load_frame(1)
+        canvas = rng.random((H, W, 4)).astype(np.float32)
+        kp.o.load_canvas(0, canvas)
+        kp.g.load_canvas(0, canvas)
+        for fwd, ts, overwrite in ((True, 1, True), (True, 2, False), (False, -1, True), (False, -4, False)):
+            rib = _ribbons(rng)
+            kp.o.load_ribbon_field(0, rib)
+            kp.g.load_ribbon_field(0, rib)
+            kp.both("accumulate_ribbon_field", 0, fwd, ts, overwrite)
+            what = "forwards %s, step %d, overwrite %s" % (fwd, ts, overwrite)
+            got, ref = kp.g.get_ribbon_field(0), kp.o.get_ribbon_field(0)
+            assert got.tobytes() == ref.tobytes(), "ribbon field " + what
+            assert_array_equal(kp.g.get_advected_output(True, 0), kp.o.get_advected_output(True, 0),
+                               "key colours " + what)
+            assert (ref["layer"] >= 0).any() and (ref["layer"] < 0).any()
+    finally:
+        kp.close()
+
+
+@pytest.mark.parametrize("look_forwards", [True, False])
+def test_offsets_from_frame_to_key_ribbon(look_forwards):
+    kp = KeyPair(_params())
+    rng = np.random.default_rng(13)
+    try:
+        kp.load_frame(0)
+        kp.random(0)
+        for fwd, layer_id in ((False, _abi.LAYER_FRAME_TO_KEY_RIBBON_B), (True, _abi.LAYER_FRAME_TO_KEY_RIBBON_F)):
+            img = _ribbon_image(rng, valid=0.6)
+            kp.o.upload_frame_to_key_ribbon(fwd, img)
+            kp.g.upload_image_color4(0, layer_id, img)
+        kp.both("offsets_from_frame_to_key_ribbon", 0, look_forwards)
+        kp.compare("frame-to-key ribbon offsets")
+    finally:
+        kp.close()

@@ -334,7 +334,7 @@ def test_errors_are_status_codes():
     with pytest.raises(PaintTweenError):
         t.upload_image_color4(0, _abi.LAYER_INPUT_COLOR, np.zeros((10, 10, 4), np.float32))
     p = config_params()
-    p.interpolateKeyFrame = 1
+    p.colorspace = 1  # Lab
     with pytest.raises(PaintTweenError):
         t.set_params(p)
     t.close()
