@@ -270,6 +270,11 @@ pt_status pt_accumulate_ribbon_field(pt_ctx* ctx, int level, int forwards, int t
 /* Offsets from the frame-to-key ribbons, random where a ribbon is invalid
  * (offsetsFromFrameToKeyRibbon, :2111-2118; ends with a sync). */
 pt_status pt_offsets_from_frame_to_key_ribbon(pt_ctx* ctx, int level, int look_forwards);
+/* mergeAdvectedKernel (:1938-1976, host :2025-2042): the forward and
+ * backward advected offsets merged, at random where both are valid, else
+ * PT_MERGE_FALLBACK_RANDOM (the random level's fractional parts) or
+ * PT_MERGE_FALLBACK_LAST_PASS (the base offsets); ends with a sync. */
+pt_status pt_merge_advected_buffers(pt_ctx* ctx, int level, int merge_fallback);
 /* ribbonField.base() and canvasOutputCache to and from the host (level
  * rectangle, row-major), advectedF/B.output() to the host. */
 pt_status pt_load_ribbon_field(pt_ctx* ctx, int level, const pt_ribbon* ribbons);

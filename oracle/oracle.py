@@ -91,6 +91,7 @@ def lib():
             "pto_get_ribbon": (None, [vp, i, vp]),
             "pto_load_canvas": (None, [vp, i, vp]),
             "pto_get_advected_output": (None, [vp, i, i, vp]),
+            "pto_merge_advected": (None, [vp, i, i]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -347,6 +348,9 @@ class Oracle:
 
     def accumulate_ribbon_field(self, level, forwards, time_step, overwrite):
         lib().pto_accumulate_ribbon(self.h, level, int(forwards), time_step, int(overwrite))
+
+    def merge_advected_buffers(self, level, fallback):
+        lib().pto_merge_advected(self.h, level, fallback)
 
     def offsets_from_frame_to_key_ribbon(self, level, look_forwards):
         lib().pto_frame_to_key_ribbon(self.h, level, int(look_forwards))

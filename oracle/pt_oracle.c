@@ -922,8 +922,11 @@ void pto_upsample(pto* o, int level) {
     memcpy(o->res_base, o->res_work, sizeof(float) * (size_t)o->W * o->H);
 }
 
+static f4 f2k_texel(const pto* o, int forwards, int x, int y);
+static pt_ribbon ribbon_of(f4 c);
+
 /* calculateTranslatedPosition + advectKernel + TexSynth::advectOffsets,
- * texSynth_kernel.cu:1540-1726 (keyframe ribbons not in scope) */
+ * texSynth_kernel.cu:1540-1726 */
 void pto_advect(pto* o, int level, int time_step, int forwards, int flags) {
     int d = forwards ? 0 : 1;
     int prev = (o->cur + 1) % 2;
@@ -989,6 +992,21 @@ void pto_advect(pto* o, int level, int time_step, int forwards, int flags) {
             o->adv_base[d][k] = pcol;
             o->adv_out[d][k] = ex_sample_out(o, out.x, out.y, out.layer);
             o->adv_ts[d][k] = time_step;
+        }
+        /* keyframe interpolation, :1652-1675 */
+        if ((flags & PT_ADVECT_CHECK_FRAME_TO_KEY) && (time_step > 1 || out.hysteresis == 0)) {
+            pt_ribbon rb = ribbon_of(f2k_texel(o, !forwards, x, y));
+            if (rb.layer >= 0 && (abs(rb.time_step) < time_step || out.hysteresis == 0)) {
+                out.x = rb.x + (float)x;
+                out.y = rb.y + (float)y;
+                out.layer = rb.layer;
+                out.hysteresis = 1.0f;
+                out.lumShiftY = 0.f; out.lumShiftA = 0.f;
+            }
+            f4 eb, eo;
+            ex_sample2(o, out.x, out.y, out.layer, &eb, &eo);
+            o->adv_base[d][k] = eb; o->adv_out[d][k] = eo;
+            o->adv_ts[d][k] = abs(rb.time_step);
         }
         if (out.hysteresis == 0) {
             out = patch(rnd.x, rnd.y, rnd.z, 0.0f, f2i(rnd.w), 1.f, 1.f);
@@ -1521,6 +1539,27 @@ void pto_accumulate_ribbon(pto* o, int level, int forwards, int time_step, int o
         }
         o->adv_out[0][k] = c;
     }
+}
+
+/* mergeAdvectedKernel + TexSynth::mergeAdvectedBuffers,
+ * texSynth_kernel.cu:1938-1976,2025-2042: r is the fractional part that
+ * randomFloat4 returns through its argument, and the random fallback is
+ * made of those fractional parts */
+void pto_merge_advected(pto* o, int level, int fallback) {
+    pt_patchxf* work = o->off_work;
+    FOR_RECT(o, level) {
+        size_t k = (size_t)y * o->W + x;
+        pt_patchxf f = o->adv_off[0][k], b = o->adv_off[1][k], res;
+        f4 rnd = rnd_texel(o, x, y);
+        f4 fr = {rnd.x - floorf(rnd.x), rnd.y - floorf(rnd.y), rnd.z - floorf(rnd.z), rnd.w - floorf(rnd.w)};
+        if (f.hysteresis > 0 && b.hysteresis > 0) res = (fr.x < 0.5f) ? f : b;
+        else if (f.hysteresis > 0) res = f;
+        else if (b.hysteresis > 0) res = b;
+        else if (fallback == PT_MERGE_FALLBACK_RANDOM) res = patch(fr.x, fr.y, fr.z, 0.f, f2i(fr.w), 1.f, 1.f);
+        else res = o->off_base[k];
+        work[k] = res;
+    }
+    pto_sync(o, level, 0);
 }
 
 /* copyFrameToKeyRibbonKernel + TexSynth::offsetsFromFrameToKeyRibbon,

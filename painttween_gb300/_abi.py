@@ -39,6 +39,7 @@ LAYER_RANDOM = 21
 
 DONT_COPY_OFFSETS = 0x01
 DONT_UPDATE_RESIDUAL = 0x10
+MERGE_FALLBACK_RANDOM, MERGE_FALLBACK_LAST_PASS = 0x20, 0x40
 ADVECT_IGNORE_RANDOM = 0x1
 ADVECT_DO_NOT_CHECK_PREVIOUS = 0x10
 ADVECT_CHECK_FRAME_TO_KEY = 0x20

@@ -119,7 +119,6 @@ struct pt_ctx {
     float4* cumul[2] = {nullptr, nullptr};
     int cf_w = 0, cf_h = 0, cf_n = 0;
     float4* f2k_buf[2] = {nullptr, nullptr};
-    Arr<float4> f2k[2]{};
     ptk::Ribbon* rib[2] = {nullptr, nullptr};
     float* up_orient = nullptr;
     float2* up_scale = nullptr;
@@ -825,7 +824,6 @@ pt_status pt_initialize(pt_ctx* c, int iw, int ih, int sw, int sh, int ns) {
     dfree_t(c, c->rnd);
     for (int i = 0; i < 2; i++) {
         dfree_t(c, c->cumul[i]); dfree_t(c, c->f2k_buf[i]); dfree_t(c, c->rib[i]);
-        c->f2k[i] = Arr<float4>{};
     }
     c->cf_w = c->cf_h = c->cf_n = 0;
     dfree_t(c, c->chg); dfree_t(c, c->stamp_last); dfree_t(c, c->stamp_win);
@@ -1006,7 +1004,7 @@ pt_status pt_upload_image_color4(pt_ctx* c, int level, int layer, const float* r
         const int d = layer == PT_LAYER_FRAME_TO_KEY_RIBBON_F ? 1 : 0;
         if (!c->f2k_buf[d]) TRY(dalloc_t(c, &c->f2k_buf[d], (size_t)c->W * c->H));
         TRY(h2d(c, c->f2k_buf[d], rgba, n * sizeof(float4)));
-        c->f2k[d] = Arr<float4>{c->f2k_buf[d], w, h};
+        c->img.f2k[d] = Arr<float4>{c->f2k_buf[d], w, h};
         return PT_OK;
     }
     if (layer == PT_LAYER_RANDOM) {
@@ -1182,8 +1180,6 @@ static ptk::KeyView key_view(const pt_ctx* c) {
     K.w = c->cf_w;
     K.h = c->cf_h;
     K.n = c->cf_n;
-    K.f2k[0] = c->f2k[0];
-    K.f2k[1] = c->f2k[1];
     return K;
 }
 
@@ -1279,6 +1275,18 @@ pt_status pt_accumulate_ribbon_field(pt_ctx* c, int level, int forwards, int tim
     return PT_OK;
 }
 
+// TexSynth::mergeAdvectedBuffers, texSynth_kernel.cu:2025-2042
+pt_status pt_merge_advected_buffers(pt_ctx* c, int level, int merge_fallback) {
+    if (!c) return PT_ERR_INVALID;
+    TRY(check_ready(c, level));
+    if (!c->img.rnd.p) return fail(c, PT_ERR_STATE, "no random level");
+    PatchPlanes work;
+    TRY(writable_work(c, level, &work));
+    Params P = make_params(c, level);
+    LN(pt::launch_merge_advected(P, merge_fallback, work, c->stream));
+    return do_sync(c, level, 0);
+}
+
 // TexSynth::offsetsFromFrameToKeyRibbon, texSynth_kernel.cu:2111-2118
 pt_status pt_offsets_from_frame_to_key_ribbon(pt_ctx* c, int level, int look_forwards) {
     if (!c) return PT_ERR_INVALID;
@@ -1340,8 +1348,6 @@ pt_status pt_upsample(pt_ctx* c, int fine_level) {
 pt_status pt_advect_offsets(pt_ctx* c, int level, int time_step, int forwards, int flags) {
     if (!c) return PT_ERR_INVALID;
     TRY(check_ready(c, level));
-    if (flags & PT_ADVECT_CHECK_FRAME_TO_KEY)
-        return fail(c, PT_ERR_UNSUPPORTED, "frame-to-key ribbons are not implemented");
     if (!c->img.rnd.p) return fail(c, PT_ERR_STATE, "no random level");
     int d = forwards ? 0 : 1;
     Params P = make_params(c, level);

@@ -30,6 +30,7 @@ cudaError_t launch_ribbon_output(const Params& P, const Ribbon* rib, const float
                                  cudaStream_t s);
 cudaError_t launch_frame_to_key(const Params& P, PatchPlanes work, int look_forwards, const KeyView& K,
                                 cudaStream_t s);
+cudaError_t launch_merge_advected(const Params& P, int fallback, PatchPlanes work, cudaStream_t s);
 cudaError_t launch_fill_ribbons(Ribbon* r, size_t n, cudaStream_t s);
 cudaError_t launch_residual(const Params& P, float* out, cudaStream_t s);
 cudaError_t launch_canvas(const Params& P, float4* canvas, cudaStream_t s);

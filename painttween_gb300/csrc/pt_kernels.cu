@@ -294,6 +294,26 @@ __global__ void k_advect(const Params P, int d, int forwards, int time_step, int
         A.out[k] = ex_sample_out(P.ex, out.x, out.y, out.layer);
         A.ts[k] = time_step;
     }
+    // keyframe interpolation, :1652-1675: long-range advection, or a pixel
+    // left without one, takes the frame-to-key ribbon where it is shorter
+    if ((flags & PT_ADVECT_CHECK_FRAME_TO_KEY) && (time_step > 1 || out.hyst == 0)) {
+        const Arr<float4>& R = P.img.f2k[forwards ? 0 : 1];
+        const float4 c = R.p ? lvl_texel(R, x, y) : f4(0.f, 0.f, 0.f, 0.f);
+        const int rts = f2i(c.x), rlayer = f2i(c.w);
+        if (rlayer >= 0 && (abs(rts) < time_step || out.hyst == 0)) {
+            out.x = c.z + (float)x;
+            out.y = c.y + (float)y;
+            out.layer = rlayer;
+            out.hyst = 1.0f;
+            out.lumy = 0.f;
+            out.luma = 0.f;
+        }
+        float4 eb, eo;
+        ex_sample2(P.ex, out.x, out.y, out.layer, &eb, &eo);
+        A.base[k] = eb;
+        A.out[k] = eo;
+        A.ts[k] = abs(rts);
+    }
     if (out.hyst == 0) {
         out = make_patch(rnd.x, rnd.y, rnd.z, 0.0f, f2i(rnd.w), 1.f, 1.f);
         A.base[k] = f4(0, 0, 0, 0);

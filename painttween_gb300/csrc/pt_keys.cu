@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(kKeyPix) k_ribbon_output(const Params P, const
 __global__ void __launch_bounds__(kKeyPix) k_frame_to_key(const Params P, PatchPlanes work, int look_forwards,
                                                           const KeyView K) {
     KEY_PIXEL_XY
-    const Arr<float4>& R = K.f2k[look_forwards ? 1 : 0];
+    const Arr<float4>& R = P.img.f2k[look_forwards ? 1 : 0];
     const Ribbon rb = ribbon_of(R.p ? lvl_texel(R, x, y) : f4(0.f, 0.f, 0.f, 0.f));
     Patch out;
     if (rb.layer >= 0) {
@@ -265,6 +265,24 @@ __global__ void __launch_bounds__(kKeyPix) k_frame_to_key(const Params P, PatchP
         out = make_patch(r.x, r.y, r.z, 0.f, f2i(r.w), 1.f, 1.f);
     }
     store_patch(work, k, out);
+}
+
+// mergeAdvectedKernel, :1938-1976: the advected offsets of both directions
+// merged (at random where both are valid), else the fallback: the random
+// level's fractional parts (randomFloat4's output argument, :207-213) or
+// the last pass's offsets
+__global__ void __launch_bounds__(kKeyPix) k_merge_advected(const Params P, int fallback, PatchPlanes work) {
+    KEY_PIXEL_XY
+    const Patch f = load_patch(P.adv[0].off, k), b = load_patch(P.adv[1].off, k);
+    const float4 rnd = lvl_texel(P.img.rnd, x, y);
+    const float4 fr = f4(rnd.x - floorf(rnd.x), rnd.y - floorf(rnd.y), rnd.z - floorf(rnd.z), rnd.w - floorf(rnd.w));
+    Patch res;
+    if (f.hyst > 0 && b.hyst > 0) res = (fr.x < 0.5f) ? f : b;
+    else if (f.hyst > 0) res = f;
+    else if (b.hyst > 0) res = b;
+    else if (fallback == PT_MERGE_FALLBACK_RANDOM) res = make_patch(fr.x, fr.y, fr.z, 0.f, f2i(fr.w), 1.f, 1.f);
+    else res = load_patch(P.off, k);
+    store_patch(work, k, res);
 }
 
 // RibbonP() in every texel
@@ -311,6 +329,10 @@ cudaError_t launch_ribbon_output(const Params& P, const Ribbon* rib, const float
 cudaError_t launch_frame_to_key(const Params& P, PatchPlanes work, int look_forwards, const KeyView& K,
                                 cudaStream_t s) {
     ptk::k_frame_to_key<<<ptk::grid_of(P.lw, P.lh), dim3(32, 4), 0, s>>>(P, work, look_forwards, K);
+    KEY_LAUNCH_CHECK();
+}
+cudaError_t launch_merge_advected(const Params& P, int fallback, PatchPlanes work, cudaStream_t s) {
+    ptk::k_merge_advected<<<ptk::grid_of(P.lw, P.lh), dim3(32, 4), 0, s>>>(P, fallback, work);
     KEY_LAUNCH_CHECK();
 }
 cudaError_t launch_fill_ribbons(Ribbon* r, size_t n, cudaStream_t s) {

@@ -59,6 +59,7 @@ struct ImgView {
     Arr<float2> scale;
     Arr<int> ids;
     Arr<float4> rnd;
+    Arr<float4> f2k[2];  // frame-to-key ribbons of the level, [0] = backward, [1] = forward
     int cur;
 };
 
@@ -72,12 +73,10 @@ struct AdvView {
 
 // Keyframe interpolation inputs: the key-to-key cumulative fields
 // [0] = backward, [1] = forward (n key layers of w x h RGBA texels, RibbonP
-// packed as (time_step, y, x, layer), linear filter) and the level's
-// frame-to-key ribbons [0] = backward, [1] = forward (point reads).
+// packed as (time_step, y, x, layer), linear filter).
 struct KeyView {
     const float4* cumul[2];
     int w, h, n;
-    Arr<float4> f2k[2];
 };
 // RibbonP (types.h:111-126) in the ribbon field buffers; layer < 0 = invalid
 struct Ribbon {

@@ -217,6 +217,9 @@ class TexSynth:
         self._check(lib().pt_offsets_from_frame_to_key_ribbon(self.h, level, int(look_forwards)),
                     "pt_offsets_from_frame_to_key_ribbon")
 
+    def merge_advected_buffers(self, level, merge_fallback):
+        self._check(lib().pt_merge_advected_buffers(self.h, level, merge_fallback), "pt_merge_advected_buffers")
+
     def load_ribbon_field(self, level, ribbons):
         a = np.ascontiguousarray(ribbons, dtype=_abi.RIBBON_DTYPE)
         self._check(lib().pt_load_ribbon_field(self.h, level, _p(a)), "pt_load_ribbon_field")

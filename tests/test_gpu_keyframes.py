@@ -228,3 +228,37 @@ def test_offsets_from_frame_to_key_ribbon(look_forwards):
         kp.compare("frame-to-key ribbon offsets")
     finally:
         kp.close()
+
+
+@pytest.mark.parametrize("fallback", [_abi.MERGE_FALLBACK_RANDOM, _abi.MERGE_FALLBACK_LAST_PASS])
+def test_advect_with_frame_to_key_ribbons_and_merge_advected(fallback):
+    """advectKernel with ADVECT_CHECK_FRAME_TO_KEY (long steps and pixels
+    without an advection take the frame-to-key ribbon) in both directions,
+    then mergeAdvectedKernel with either fallback."""
+    kp = KeyPair(_params(), frames=3)
+    rng = np.random.default_rng(14)
+    try:
+        for fwd, layer_id in ((False, _abi.LAYER_FRAME_TO_KEY_RIBBON_B), (True, _abi.LAYER_FRAME_TO_KEY_RIBBON_F)):
+            img = _ribbon_image(rng, valid=0.6)
+            kp.o.upload_frame_to_key_ribbon(fwd, img)
+            kp.g.upload_image_color4(0, layer_id, img)
+        kp.o.reset_advected()
+        kp.g.reset_advected_buffers()
+        kp.load_frame(0)
+        kp.random(0)
+        kp.both("randomize_offsets", 0)
+        kp.both("propagate", 0, 2, -1)
+        kp.flip()
+        kp.load_frame(1)
+        kp.random(1, seed=8)
+        flags = _abi.ADVECT_CHECK_FRAME_TO_KEY
+        kp.o.advect(0, 2, True, flags)
+        kp.g.advect_offsets(0, 2, True, flags)
+        kp.compare("advect forwards, step 2, frame-to-key")
+        kp.o.advect(0, 1, False, flags | _abi.ADVECT_DO_NOT_CHECK_PREVIOUS)
+        kp.g.advect_offsets(0, 1, False, flags | _abi.ADVECT_DO_NOT_CHECK_PREVIOUS)
+        kp.compare("advect backwards, step 1, frame-to-key")
+        kp.both("merge_advected_buffers", 0, fallback)
+        kp.compare("merge advected")
+    finally:
+        kp.close()
