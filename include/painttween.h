@@ -112,7 +112,7 @@ typedef struct {
     float timeDerivativeOutputWeight;
     float temporalCoherenceWeight;
     float hysteresisWeight;
-    int32_t interpolateKeyFrame; /* keyframe kernels (step-wise calls only) */
+    int32_t interpolateKeyFrame; /* keyframe interpolation (pt_set_keyframes) */
     int32_t useGuide;
     int32_t currentInterpolationIndex;
     int32_t numFrames;
@@ -249,6 +249,16 @@ pt_status pt_reset_advected_buffers(pt_ctx* ctx); /* workingBuffers.cpp:112-116 
  * renderAnimationFBMO (synthesisProcessor.cpp:979-980). */
 pt_status pt_copy_offsets_to_advected(pt_ctx* ctx, int forwards);
 
+/* Keyframes for pt_synthesize_* with params.interpolateKeyFrame: style
+ * layer i (pt_set_style, the image's size) is the painted key of frame
+ * frames[i], increasing (DataAccess::keyFrameIndices).  The run then does
+ * keyFramesPreprocess (synthesisProcessor.cpp:528-674: ribbons from every
+ * frame to its nearest keys, accumulated frame by frame) and
+ * renderAnimationFMBM with SynthesisFrame's keyframe paths (FMBM and
+ * FMBM_RM schemes); frames from the nearest keys outside first..last must
+ * be set too. */
+pt_status pt_set_keyframes(pt_ctx* ctx, const int32_t* frames, int count);
+
 /* ---- keyframe interpolation (texSynth_kernel.cu:290-304,723-1110,
  *      1728-1853,2061-2118,2138-2142).  With params.interpolateKeyFrame set,
  *      pt_propagate / pt_scatter run propagate_kernel_keys /
@@ -259,9 +269,7 @@ pt_status pt_copy_offsets_to_advected(pt_ctx* ctx, int forwards);
  *      (propagate) or keeps its offset (scatter).  The cumulative fields and
  *      frame-to-key ribbons are uploaded as RGBA images
  *      (pt_upload_image_color4 with PT_LAYER_CUMUL_FIELD_B/F, style = key
- *      layer, and PT_LAYER_FRAME_TO_KEY_RIBBON_B/F).  The keyframe driver
- *      (keyFramesPreprocess, accumulateRibbon) is not implemented:
- *      pt_synthesize_* return PT_ERR_UNSUPPORTED with interpolateKeyFrame. */
+ *      layer, and PT_LAYER_FRAME_TO_KEY_RIBBON_B/F). */
 pt_status pt_initialize_cumulative_fields(pt_ctx* ctx, int w, int h, int layers); /* :2138 */
 /* The ribbon field (working <- base carried along the velocities from the
  * previous frame, then copied to base) and advectedF.output <- the canvas at

@@ -92,6 +92,7 @@ def lib():
             "pto_load_canvas": (None, [vp, i, vp]),
             "pto_get_advected_output": (None, [vp, i, i, vp]),
             "pto_merge_advected": (None, [vp, i, i]),
+            "pto_random_level_keys": (i, [u32, i, i, i, i, i, vp, vp, vp, vp, i, i, i, i, i, i, i, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -439,6 +440,11 @@ class OracleDriver:
         self.store = {}
         self.last_saved = {}  # SynthesisFrame::_last_saved_pass: (frame, level) -> pass
         self.levels = params.levels
+        self.keys = []        # DataAccess::keyFrameIndices: style i is the key of frame keys[i]
+        self.key_sub = []
+        self.keyed = False
+        self.f2k = ({}, {})   # frame -> frame-to-key ribbon pyramid, [0] backward, [1] forward
+        self.k2k = ({}, {})   # key full index -> key-to-key ribbon pyramid
 
     def _update_parameters(self, frame, direction):
         """SynthesisFrame::updateParameters, synthesisFrame.cpp:522-542."""
@@ -453,7 +459,9 @@ class OracleDriver:
         s = self.styles[0]
         args = (level, s["w"], s["h"], fp["rgba"][level], fp["orient"][level], s["output"][level],
                 s["orient"][level], bool(self.user.transparencyOk), bool(self.user.orientationEnabled))
-        if self.user.rngMode == _abi.RNG_COUNTER:
+        if self.keyed:
+            rnd = self._random_level_keyed(frame, level)
+        elif self.user.rngMode == _abi.RNG_COUNTER:
             rnd = counter_random_level(counter_seed(self.user.rngSeed, frame, level), *args)
         else:
             rnd = random_level(frame * level, *args)
@@ -469,28 +477,34 @@ class OracleDriver:
     def _load_residual(self, level, frame, pass_):
         self.o.load_residual(level, self.store[(level, frame, pass_)][1])
 
-    def propagate_and_scatter(self, level, iterations):
-        """synthesisFrame.cpp:483-508."""
+    def propagate_and_scatter(self, level, iterations, key=-1):
+        """synthesisFrame.cpp:483-508 (with keys: a jump-0 pass first, and
+        every pass with the frame's key index)."""
         for itr in range(iterations):
+            if self.keyed:
+                self.o.propagate(level, 0, key)
             j = 128
             while j > 1:
-                self.o.propagate(level, j)
+                self.o.propagate(level, j, key)
                 j //= 2
-            self.o.propagate(level, 1)
-            self.o.propagate(level, 1)
+            self.o.propagate(level, 1, key)
+            self.o.propagate(level, 1, key)
             if itr < iterations - 1:
-                self.o.scatter(level)
+                self.o.scatter(level, key)
 
     def synthesize_consecutive(self, frame, level, pass_, is_first, forwards, source_pass, first_pass):
         o = self.o
         self._update_parameters(frame, _abi.FORWARD if forwards else _abi.BACKWARD)
         rm = self.user.scheme == _abi.S_FMBM_RM
-        ops = 0 if rm else _abi.ADVECT_UPDATE_RESIDUAL
+        ops = (_abi.ADVECT_CHECK_FRAME_TO_KEY if self.keyed else 0) | (0 if rm else _abi.ADVECT_UPDATE_RESIDUAL)
+        weight = self._key_advect_weight(frame, forwards) if self.keyed else 0.5
         coarsest = level == self.levels - 1
         if first_pass:
             self._random_level(frame, level)
             if is_first:
-                if coarsest:
+                if coarsest and self.keyed:
+                    o.offsets_from_frame_to_key_ribbon(level, forwards)
+                elif coarsest:
                     o.randomize_offsets(level)
                 else:
                     self._load_offsets(level + 1, frame, source_pass)
@@ -507,7 +521,7 @@ class OracleDriver:
                 o.upsample(level)
                 o.sync(level)
                 if rm:
-                    o.merge_randomly(level, forwards, 0.5, False)
+                    o.merge_randomly(level, forwards, weight, False)
                 else:
                     o.merge_using_residual(level, forwards)
         else:
@@ -516,11 +530,11 @@ class OracleDriver:
             self._load_residual(level, frame, pass_ - 1)
             o.sync(level, _abi.DONT_COPY_OFFSETS | _abi.DONT_UPDATE_RESIDUAL)
             if rm:
-                o.merge_randomly(level, forwards, 0.5, False)
+                o.merge_randomly(level, forwards, weight, False)
             else:
                 o.merge_using_residual(level, forwards)
         o.sync(level)
-        self.propagate_and_scatter(level, self.user.iterations)
+        self.propagate_and_scatter(level, self.user.iterations, self._key_full(frame) if self.keyed else -1)
         self._save_images(level, frame, pass_)
 
     def _save_images(self, level, frame, pass_):
@@ -536,6 +550,8 @@ class OracleDriver:
         """SynthesisProcessor::renderAnimation, synthesisProcessor.cpp:769-805,
         for the scheme of the parameters; returns {frame: (offsets, residual,
         output)} at the level PT_OUTPUT_LEVEL names."""
+        if self.user.interpolateKeyFrame:
+            return self._render_keyed(first, last)
         if self.user.scheme == _abi.S_IND:
             return self._render_ind(first, last)
         if self.user.scheme == _abi.S_FBMO:
@@ -543,6 +559,166 @@ class OracleDriver:
         if self.user.scheme == _abi.S_TCTF:
             return self._render_tctf(first, last)
         return self._render_fmbm(first, last)
+
+    # --- keyframe interpolation ------------------------------------------------
+    def set_keyframes(self, frames):
+        self.keys = list(frames)
+
+    def _key_full(self, frame):
+        return self.keys.index(frame) if frame in self.keys else -1
+
+    def _key_sub_index(self, frame):
+        return self.key_sub.index(frame) if frame in self.key_sub else -1
+
+    def _update_key_subrange(self, first, last):
+        """Style::updateKeyFrameSubrange, style.cpp:175-196."""
+        K = self.keys
+        self.key_sub = []
+        for i, idx in enumerate(K):
+            if first <= idx <= last:
+                self.key_sub.append(idx)
+            else:
+                if i + 1 < len(K) and first < K[i + 1] <= last:
+                    self.key_sub.append(idx)
+                if i > 0 and first <= K[i - 1] < last:
+                    self.key_sub.append(idx)
+
+    def _key_advect_weight(self, frame, forwards):
+        """Style::keyFrameAdvectWeight, style.cpp:207-223."""
+        K = self.key_sub
+        prev_key = -1
+        while prev_key < len(K) - 1 and frame > K[prev_key + 1]:
+            prev_key += 1
+        has_prev, has_next = prev_key >= 0, prev_key < len(K) - 1
+        prev_frame = K[prev_key] if has_prev else self.run_first
+        next_frame = K[prev_key + 1] if has_next else self.run_last
+        f32 = np.float32
+        if forwards:
+            return float(f32(next_frame - frame) / f32(next_frame - prev_frame)) if has_next else 1.0
+        return float(f32(frame - prev_frame) / f32(next_frame - prev_frame)) if has_prev else 1.0
+
+    def _random_level_keyed(self, frame, level):
+        """createRandomPyramid with setupWithKeys, synthesisFrame.cpp:94-139."""
+        fp = self.frames[frame]
+        h, w = fp["orient"][level].shape
+        ew, eh = self.styles[0]["w"] >> level, self.styles[0]["h"] >> level
+        ex_out = np.ascontiguousarray(np.stack([s["output"][level] for s in self.styles]), np.float32)
+        ex_or = np.ascontiguousarray(np.stack([s["orient"][level] for s in self.styles]), np.float32)
+        out = np.empty((h, w, 4), np.float32)
+        lib().pto_random_level_keys((frame * level) & 0xFFFFFFFF, w, h, level, self.styles[0]["w"],
+                                    self.styles[0]["h"], _p(_c(fp["rgba"][level], np.float32)),
+                                    _p(_c(fp["orient"][level], np.float32)), _p(ex_out), _p(ex_or), ew, eh,
+                                    len(self.styles), len(self.key_sub), self._key_full(self.key_sub[0]),
+                                    int(self.user.transparencyOk), int(self.user.orientationEnabled), _p(out))
+        return out
+
+    def _ribbon_pyramid(self, rib, levels):
+        """initializeRibbonPyramid, imagePyramid.cpp:211-235."""
+        lv0 = np.stack([rib["time_step"].astype(np.float32), rib["y"], rib["x"],
+                        rib["layer"].astype(np.float32)], axis=-1).astype(np.float32)
+        pyr = [lv0]
+        for l in range(1, levels):
+            h, w = self.H >> l, self.W >> l
+            p00 = pyr[-1][0:2 * h:2, 0:2 * w:2]
+            lv = np.empty((h, w, 4), np.float32)
+            lv[..., 0] = np.trunc(p00[..., 0])
+            lv[..., 1] = p00[..., 1] * np.float32(0.5)
+            lv[..., 2] = p00[..., 2] * np.float32(0.5)
+            lv[..., 3] = np.trunc(p00[..., 3])
+            pyr.append(lv)
+        return pyr
+
+    @staticmethod
+    def _ribbons(h, w, layer):
+        r = np.zeros((h, w), _abi.RIBBON_DTYPE)
+        r["layer"] = layer
+        return r
+
+    def _accumulate(self, forwards, sfirst, slast):
+        """SynthesisProcessor::accumulateRibbon, synthesisProcessor.cpp:528-627
+        (level 0; one-frame steps, no ribbon inputs)."""
+        o = self.o
+        d = 0 if forwards else 1
+        fk, lk = self.key_sub[0], self.key_sub[-1]
+        if forwards:
+            blank, frames = range(self.run_first, fk), list(range(fk, slast + 1))
+        else:
+            blank, frames = range(lk + 1, self.run_last + 1), list(range(lk, sfirst - 1, -1))
+        acc = {frames[0]: self._ribbons(self.H, self.W, -1)}
+        o.load_ribbon_field(0, acc[frames[0]])
+        for f in blank:
+            self.f2k[d][f] = self._ribbon_pyramid(acc[frames[0]], len(self.frames[f]["orient"]))
+        for f in frames:
+            fp = self.frames[f]
+            o.load_images(fp, 0)
+            ts = -1 if forwards else 1
+            pf = f + ts
+            if (forwards and pf >= fk) or (not forwards and pf <= lk):
+                pp = self.frames[pf]
+                L = lib()
+                w, h = self.W, self.H
+                if pf < f:
+                    L.pto_upload_layered(o.h, _abi.LAYER_INPUT_VEL_B, _p(_c(fp["velb"][0], np.float32)), w, h)
+                    L.pto_upload_layered(o.h, _abi.LAYER_INPUT_VEL_F_PREVIOUS, _p(_c(pp["velf"][0], np.float32)), w, h)
+                else:
+                    L.pto_upload_layered(o.h, _abi.LAYER_INPUT_VEL_F, _p(_c(fp["velf"][0], np.float32)), w, h)
+                    L.pto_upload_layered(o.h, _abi.LAYER_INPUT_VEL_B_PREVIOUS, _p(_c(pp["velb"][0], np.float32)), w, h)
+                o.load_ribbon_field(0, acc[pf])
+                o.accumulate_ribbon_field(0, forwards, ts, True)
+            acc[f] = o.get_ribbon_field(0)
+            k = self._key_sub_index(f)
+            if k >= 0:
+                full = self._key_full(f)
+                self.k2k[d][full] = self._ribbon_pyramid(acc[f], len(fp["orient"]))
+                o.load_canvas(0, self.styles[full]["output"][0])
+                acc[f] = self._ribbons(self.H, self.W, k)
+                o.load_ribbon_field(0, acc[f])
+            self.f2k[d][f] = self._ribbon_pyramid(acc[f], len(fp["orient"]))
+
+    def _bind_frame_keys(self, frame, level):
+        for d in (0, 1):
+            pyr = self.f2k[d].get(frame)
+            if pyr is not None and level < len(pyr):
+                self.o.upload_frame_to_key_ribbon(d == 1, pyr[level])
+
+    def _upload_key_fields(self, level):
+        """Style::load with keys, style.cpp:122-134."""
+        if 0 not in self.k2k[0] or not self.key_sub:
+            return
+        lw, lh = self.W >> level, self.H >> level
+        self.o.init_cumulative_fields(lw, lh, len(self.key_sub))
+        for i, kf in enumerate(self.key_sub):
+            full = self._key_full(kf)
+            for d in (0, 1):
+                pyr = self.k2k[d].get(full)
+                if pyr is not None and level < len(pyr):
+                    self.o.upload_cumulative_field(d == 1, i, pyr[level])
+
+    def _render_keyed(self, first, last):
+        """keyFramesPreprocess (synthesisProcessor.cpp:629-674), then
+        renderAnimationFMBM with the keyframe paths."""
+        user = self.user.copy()
+        self._update_key_subrange(first, last)
+        sfirst, slast = min(first, self.key_sub[0]), max(last, self.key_sub[-1])
+        self.run_first, self.run_last = first, last
+        self.keyed = True
+        try:
+            p = user.copy()
+            p.interpolateKeyFrame = 0
+            self.o.set_params(p)
+            self.o.load_style_level(self.styles, 0)
+            self._accumulate(True, sfirst, slast)
+            self._accumulate(False, sfirst, slast)
+            p = user.copy()
+            p.interpolateKeyFrame = 1
+            p.numFrames = slast - sfirst
+            p.firstKeyIndex = self._key_full(self.key_sub[0])
+            p.lastKeyIndex = self._key_full(self.key_sub[-1])
+            self.user = p
+            return self._render_fmbm(first, last)
+        finally:
+            self.user = user
+            self.keyed = False
 
     def _advect_neighbors(self, frame, level, source_pass, first, last):
         """SynthesisFrame::advectNeighbors, synthesisFrame.cpp:325-382, with
@@ -630,11 +806,15 @@ class OracleDriver:
         total = self.user.fixupPasses + 1
         for level in range(self.levels - 1, self.user.finalLevel - 1, -1):
             self.o.load_style_level(self.styles, level)
+            if self.keyed:
+                self._upload_key_fields(level)
             self.o.reset_advected()
             for pass_ in range(total):
                 self._render_pass(level, pass_, total - 1, first, last)
         for level in range(self.user.finalLevel, 0, -1):
             self.o.load_style_level(self.styles, level - 1)
+            if self.keyed:
+                self._upload_key_fields(level - 1)
             for f in range(first, last + 1):
                 self._spatial_upsample(f, level, level - 1, True)
         final_pass = total - 1 if self.user.finalLevel == 0 else 0
@@ -715,5 +895,7 @@ class OracleDriver:
             if not is_first:
                 self.o.flip()
             self.o.load_frame_level(self.frames[f], level)
+            if self.keyed:
+                self._bind_frame_keys(f, level)
             self.synthesize_consecutive(f, level, pass_, is_first, forwards, source_pass, pass_ == 0)
 

@@ -1727,6 +1727,43 @@ int pto_random_level(uint32_t seed, int w, int h, int level, int style_w0, int s
     return retried;
 }
 
+/* createRandomPyramid with setupWithKeys, synthesisFrame.cpp:94-139: the
+ * key layer is drawn first (rand() % nk + first_key), then the offset in
+ * that layer (retry rule on its output alpha), then the two fractions.
+ * ex_out_rgba / ex_orient hold ns layers of ew x eh. */
+int pto_random_level_keys(uint32_t seed, int w, int h, int level, int style_w0, int style_h0,
+                          const float* img_rgba, const float* img_orient, const float* ex_out_rgba,
+                          const float* ex_orient, int ew, int eh, int ns, int nk, int first_key,
+                          int transparency_ok, int orientation_enabled, float* out) {
+    pto_glibc g;
+    glibc_srand(&g, seed);
+    int retried = 0;
+    int mx = (style_w0 >> level) - 1, my = (style_h0 >> level) - 1;
+    size_t lsz = (size_t)ew * eh;
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            int style = (int)(glibc_rand(&g) % (uint32_t)nk) + first_key;
+            int sl = clampi(style, 0, ns - 1);
+            int ox, oy, trial = 0;
+            float ia = img_rgba[((size_t)y * w + x) * 4 + 3];
+            do {
+                ox = (int)(glibc_rand(&g) % (uint32_t)mx);
+                oy = (int)(glibc_rand(&g) % (uint32_t)my);
+                trial++;
+            } while (!transparency_ok && ia > ALPHA_THRESHOLD &&
+                     ex_out_rgba[(sl * lsz + (size_t)oy * ew + ox) * 4 + 3] < ALPHA_THRESHOLD && trial < 50);
+            if (trial > 1) retried++;
+            float orient = orientation_enabled
+                               ? img_orient[(size_t)y * w + x] - ex_orient[sl * lsz + (size_t)oy * ew + ox]
+                               : 0.f;
+            float rx = (float)glibc_rand(&g) / (float)2147483647;
+            float ry = (float)glibc_rand(&g) / (float)2147483647;
+            float* p = out + ((size_t)y * w + x) * 4;
+            p[0] = (float)ox + rx; p[1] = (float)oy + ry; p[2] = orient; p[3] = (float)style;
+        }
+    return retried;
+}
+
 /* PT_RNG_COUNTER random level: four hashed draws per pixel and trial, with
  * the reference's retry rule for opaque pixels on transparent texels */
 void pto_counter_random_level(uint32_t seed, int w, int h, int level, int style_w0, int style_h0,

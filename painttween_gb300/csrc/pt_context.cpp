@@ -120,6 +120,16 @@ struct pt_ctx {
     int cf_w = 0, cf_h = 0, cf_n = 0;
     float4* f2k_buf[2] = {nullptr, nullptr};
     ptk::Ribbon* rib[2] = {nullptr, nullptr};
+    // keyframe interpolation driver: style i is the key of frame
+    // key_frames[i] (DataAccess::keyFrameIndices); key_sub is the run's key
+    // subrange (Style::keyFrameSubrange); keyed is set while a run
+    // interpolates keys.  keyFramesPreprocess leaves per frame its
+    // frame-to-key ribbon pyramid and per key (full index) its key-to-key
+    // ribbon pyramid, [0] backward, [1] forward, as RGBA levels.
+    std::vector<int> key_frames, key_sub;
+    bool keyed = false;
+    int run_first = 0, run_last = 0;
+    std::map<int, std::vector<float4*>> f2k_pyr[2], k2k_pyr[2];
     float* up_orient = nullptr;
     float2* up_scale = nullptr;
     int* up_ids = nullptr;
@@ -537,7 +547,8 @@ static int temporal_mode(pt_ctx* c) {
 // whether the tiled kernels cover the current configuration
 static bool tiled_usable(pt_ctx* c) {
     int r = c->params.residualWindowSize;
-    return c->use_tiled && c->params.coherenceWeight <= 0.f && temporal_mode(c) >= 0 && r >= 2 && r <= 4;
+    return c->use_tiled && !c->params.interpolateKeyFrame && c->params.coherenceWeight <= 0.f &&
+           temporal_mode(c) >= 0 && r >= 2 && r <= 4;
 }
 
 // launches the tiled kernel of `kind` if one is instantiated for this
@@ -1253,7 +1264,7 @@ static pt_status ensure_ribbons(pt_ctx* c) {
     for (int i = 0; i < 2; i++) {
         if (c->rib[i]) continue;
         TRY(dalloc_t(c, &c->rib[i], n));
-        LN(pt::launch_fill_ribbons(c->rib[i], n, c->stream));
+        LN(pt::launch_fill_ribbons(c->rib[i], n, -1, c->stream));
     }
     return PT_OK;
 }
@@ -1261,9 +1272,7 @@ static pt_status ensure_ribbons(pt_ctx* c) {
 // TexSynth::accumulateRibbonField, texSynth_kernel.cu:1830-1853
 pt_status pt_accumulate_ribbon_field(pt_ctx* c, int level, int forwards, int time_step, int overwrite) {
     if (!c) return PT_ERR_INVALID;
-    TRY(check_ready(c, level, false, true));
-    if (!c->img.velf[1 - c->img.cur].p && !c->img.velb[1 - c->img.cur].p)
-        return fail(c, PT_ERR_STATE, "no previous-frame velocities");
+    TRY(check_ready(c, level, false, false));  // unbound layers read as zero
     TRY(ensure_ribbons(c));
     Params P = make_params(c, level);
     LN(pt::launch_accumulate_ribbon(P, forwards ? 1 : 0, c->rib[1], c->rib[0], time_step, overwrite ? 1 : 0,
@@ -1867,7 +1876,11 @@ static pt_status load_last_saved_offsets(pt_ctx* c, int frame, int level) {
 // propagate pass compares against the residuals left by earlier steps, as
 // the reference's does; that pass then runs untracked and its sync computes
 // every residual and tap value.
-static pt_status propagate_and_scatter(pt_ctx* c, int level, int iterations, bool residual_fresh = true) {
+//
+// With keyframe interpolation every iteration starts with a jump-0 pass and
+// all passes carry the frame's key index (-1 if it is not a key).
+static pt_status propagate_and_scatter(pt_ctx* c, int level, int iterations, bool residual_fresh = true,
+                                       int key = -1) {
     const bool track = c->use_incremental && tiled_usable(c);
     bool fill_after_first = false;
     if (track) {
@@ -1893,7 +1906,7 @@ static pt_status propagate_and_scatter(pt_ctx* c, int level, int iterations, boo
         if (fill_after_first) {
             fill_after_first = false;
             c->inc_fill = 1;
-            pt_status st = pt_propagate(c, level, jump, -1);
+            pt_status st = pt_propagate(c, level, jump, key);
             c->inc_fill = 0;
             return st;
         }
@@ -1905,12 +1918,13 @@ static pt_status propagate_and_scatter(pt_ctx* c, int level, int iterations, boo
             c->inc_prev = same ? it->second : INT_MIN;
             last_pass[jump] = c->inc_pi;
         }
-        pt_status st = jump ? pt_propagate(c, level, jump, -1) : pt_scatter(c, level, -1);
+        pt_status st = jump ? pt_propagate(c, level, jump, key) : pt_scatter(c, level, key);
         c->inc_on = 0;
         c->inc_prev = INT_MIN;
         return st;
     };
     for (int itr = 0; itr < iterations; itr++) {
+        if (c->keyed) TRY(pt_propagate(c, level, 0, key));
         for (int j = 128; j > 1; j /= 2) TRY(run(j));
         TRY(run(1));
         TRY(run(1));
@@ -1920,6 +1934,57 @@ static pt_status propagate_and_scatter(pt_ctx* c, int level, int iterations, boo
 }
 
 // SynthesisFrame::synthesizeConsecutive, synthesisFrame.cpp:214-323
+// DataAccess::keyFrameIndices().indexOf(frame): the key's full index
+static int key_full_index(const pt_ctx* c, int frame) {
+    for (size_t i = 0; i < c->key_frames.size(); i++)
+        if (c->key_frames[i] == frame) return (int)i;
+    return -1;
+}
+// Style::keyFrameSubrangeIndex, style.cpp:198-205
+static int key_sub_index(const pt_ctx* c, int frame) {
+    for (size_t i = 0; i < c->key_sub.size(); i++)
+        if (c->key_sub[i] == frame) return (int)i;
+    return -1;
+}
+// Style::keyFrameAdvectWeight, style.cpp:207-223
+static float key_advect_weight(const pt_ctx* c, int frame, bool forwards) {
+    const std::vector<int>& K = c->key_sub;
+    int prev_key = -1;
+    while (prev_key < (int)K.size() - 1 && frame > K[prev_key + 1]) prev_key++;
+    const bool has_prev = prev_key >= 0, has_next = prev_key < (int)K.size() - 1;
+    const int prev_frame = has_prev ? K[prev_key] : c->run_first;
+    const int next_frame = has_next ? K[prev_key + 1] : c->run_last;
+    if (forwards) return has_next ? float(next_frame - frame) / float(next_frame - prev_frame) : 1.0f;
+    return has_prev ? float(frame - prev_frame) / float(next_frame - prev_frame) : 1.0f;
+}
+
+// SynthesisFrame::createRandomPyramid with setupWithKeys
+// (synthesisFrame.cpp:66-150): the glibc stream of srand(frame*level), each
+// pixel drawing its key layer first; one GPU thread walks the stream.
+static pt_status random_level_keyed(pt_ctx* c, int level, int frame) {
+    TRY(check_ready(c, level));
+    const int lw = c->W >> level, lh = c->H >> level;
+    const int mx = (c->SW >> level) - 1, my = (c->SH >> level) - 1;
+    if (mx < 1 || my < 1) return fail(c, PT_ERR_INVALID, "style too small for level %d", level);
+    if (!c->rnd) TRY(dalloc_t(c, &c->rnd, (size_t)c->W * c->H));
+    if (c->states_cap < 31) {
+        dfree_t(c, c->states);
+        TRY(dalloc_t(c, &c->states, (size_t)31));
+        c->states_cap = 31;
+    }
+    uint32_t s0[31];
+    glibc_state((uint32_t)(frame * level), s0);
+    CU(cudaMemcpyAsync(c->states, s0, sizeof(s0), cudaMemcpyHostToDevice, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    ExView ex{c->ex->base, c->ex->out, c->ex->bo, c->ex->orient, c->ex->dt, c->ex->ids, c->ex->w, c->ex->h, c->NS};
+    const int nk = (int)c->key_sub.size(), first_key = key_full_index(c, c->key_sub.front());
+    LN(pt::launch_random_level_keys(lw, lh, mx, my, c->params.transparencyOk, c->params.orientationEnabled,
+                                    c->img.base[c->img.cur], c->img.orient, ex, c->rnd, c->states, nk, first_key,
+                                    c->stream));
+    c->img.rnd = Arr<float4>{c->rnd, lw, lh};
+    return PT_OK;
+}
+
 static pt_status synthesize_consecutive(pt_ctx* c, const pt_params& user, int frame, int level, int pass,
                                         bool is_first, bool forwards, int source_pass, bool first_pass,
                                         bool save_canvas) {
@@ -1928,13 +1993,17 @@ static pt_status synthesize_consecutive(pt_ctx* c, const pt_params& user, int fr
     p.direction = forwards ? PT_FORWARD : PT_BACKWARD;
     TRY(pt_set_params(c, &p));
     bool rm = user.scheme == PT_S_FMBM_RM;
-    int ops = rm ? 0 : PT_ADVECT_UPDATE_RESIDUAL;
+    int ops = (c->keyed ? PT_ADVECT_CHECK_FRAME_TO_KEY : 0) | (rm ? 0 : PT_ADVECT_UPDATE_RESIDUAL);
     bool coarsest = level == user.levels - 1;
+    // SynthesisFrame::mergeRandomly, :510-520
+    const float advect_weight = c->keyed ? key_advect_weight(c, frame, forwards) : 0.5f;
     if (first_pass) {
-        TRY(pt_create_random_level(c, level, frame));
+        if (c->keyed) TRY(random_level_keyed(c, level, frame));
+        else TRY(pt_create_random_level(c, level, frame));
         if (is_first) {
             if (coarsest) {
-                TRY(pt_randomize_offsets(c, level));
+                if (c->keyed) TRY(pt_offsets_from_frame_to_key_ribbon(c, level, forwards));
+                else TRY(pt_randomize_offsets(c, level));
             } else {
                 TRY(store_load_offsets(c, level + 1, frame, source_pass));
                 TRY(pt_upsample(c, level));
@@ -1950,7 +2019,7 @@ static pt_status synthesize_consecutive(pt_ctx* c, const pt_params& user, int fr
             TRY(store_load_residual(c, level + 1, frame, source_pass));
             TRY(pt_upsample(c, level));
             TRY(do_sync(c, level, 0));
-            if (rm) TRY(pt_merge_randomly(c, level, forwards, 0.5f, 0));
+            if (rm) TRY(pt_merge_randomly(c, level, forwards, advect_weight, 0));
             else TRY(pt_merge_using_residual(c, level, forwards));
         }
     } else {
@@ -1958,11 +2027,11 @@ static pt_status synthesize_consecutive(pt_ctx* c, const pt_params& user, int fr
         TRY(store_load_offsets(c, level, frame, pass - 1));
         TRY(store_load_residual(c, level, frame, pass - 1));
         TRY(do_sync(c, level, PT_DONT_COPY_OFFSETS | PT_DONT_UPDATE_RESIDUAL));
-        if (rm) TRY(pt_merge_randomly(c, level, forwards, 0.5f, 0));
+        if (rm) TRY(pt_merge_randomly(c, level, forwards, advect_weight, 0));
         else TRY(pt_merge_using_residual(c, level, forwards));
     }
     TRY(do_sync(c, level, 0));
-    TRY(propagate_and_scatter(c, level, user.iterations));
+    TRY(propagate_and_scatter(c, level, user.iterations, true, c->keyed ? key_full_index(c, frame) : -1));
     return save_images(c, level, frame, pass, save_canvas);
 }
 
@@ -2120,6 +2189,208 @@ static pt_status render_fbmo(pt_ctx* c, int first, int last) {
     return PT_OK;
 }
 
+// --- keyframe interpolation driver ----------------------------------------------
+
+static void free_key_ribbons(pt_ctx* c) {
+    for (int d = 0; d < 2; d++) {
+        for (auto& kv : c->f2k_pyr[d])
+            for (float4* p : kv.second) dfree_t(c, p);
+        for (auto& kv : c->k2k_pyr[d])
+            for (float4* p : kv.second) dfree_t(c, p);
+        c->f2k_pyr[d].clear();
+        c->k2k_pyr[d].clear();
+    }
+    c->img.f2k[0] = c->img.f2k[1] = Arr<float4>{};
+}
+
+// SynthesisFrame::loadAnimImages with keys (synthesisFrame.cpp:613-627):
+// the frame's frame-to-key ribbons of the level
+static void bind_frame_keys(pt_ctx* c, int frame, int level) {
+    for (int d = 0; d < 2; d++) {
+        auto it = c->f2k_pyr[d].find(frame);
+        if (it == c->f2k_pyr[d].end() || level >= (int)it->second.size()) continue;
+        c->img.f2k[d] = Arr<float4>{it->second[level], c->W >> level, c->H >> level};
+    }
+}
+
+// Style::load with keys (style.cpp:122-134): the key-to-key ribbons of the
+// subrange's keys as the cumulative fields of the level, layer = subrange
+// index (uploaded only once the first key's backward ribbon exists)
+static pt_status upload_key_fields(pt_ctx* c, int level) {
+    if (!c->k2k_pyr[0].count(0) || c->key_sub.empty()) return PT_OK;
+    const int lw = c->W >> level, lh = c->H >> level;
+    const size_t n = (size_t)lw * lh;
+    TRY(pt_initialize_cumulative_fields(c, lw, lh, (int)c->key_sub.size()));
+    for (size_t i = 0; i < c->key_sub.size(); i++) {
+        const int full = key_full_index(c, c->key_sub[i]);
+        for (int d = 0; d < 2; d++) {
+            auto it = c->k2k_pyr[d].find(full);
+            if (it == c->k2k_pyr[d].end() || level >= (int)it->second.size()) continue;
+            CU(cudaMemcpyAsync(c->cumul[d] + i * n, it->second[level], n * sizeof(float4), cudaMemcpyDeviceToDevice,
+                               c->stream));
+        }
+    }
+    return PT_OK;
+}
+
+// initializeRibbonPyramid (imagePyramid.cpp:211-235) of a level-0 ribbon field
+static pt_status ribbon_pyramid(pt_ctx* c, const ptk::Ribbon* src, int levels, std::vector<float4*>* out) {
+    for (float4* p : *out) dfree_t(c, p);
+    out->assign(levels, nullptr);
+    for (int l = 0; l < levels; l++) {
+        const int w = c->W >> l, h = c->H >> l;
+        TRY(dalloc_t(c, &(*out)[l], (size_t)std::max(w, 1) * std::max(h, 1)));
+        if (l == 0) LN(pt::launch_ribbon_pack(src, w, h, (*out)[0], c->stream));
+        else LN(pt::launch_ribbon_down((*out)[l - 1], c->W >> (l - 1), (*out)[l], w, h, c->stream));
+    }
+    return PT_OK;
+}
+
+// SynthesisProcessor::accumulateRibbon, synthesisProcessor.cpp:528-627, at
+// level 0: every frame's ribbon to the nearest key behind it in time,
+// carried frame to frame by accumulateRibbonField.  Steps of more than one
+// frame need ribbon inputs (getRibbonB/F), which this library does not take,
+// so each frame accumulates from its neighbour only, as the reference does
+// without ribbon files.  Guides are not built (no kernel reads them).
+static pt_status accumulate_ribbons(pt_ctx* c, bool forwards, int sfirst, int slast) {
+    const int d = forwards ? 0 : 1;
+    const int first_key = c->key_sub.front(), last_key = c->key_sub.back();
+    const size_t n = (size_t)c->W * c->H, rb = n * sizeof(ptk::Ribbon);
+    std::vector<int> blank, frames;
+    if (forwards) {
+        for (int f = c->run_first; f < first_key; f++) blank.push_back(f);
+        for (int f = first_key; f <= slast; f++) frames.push_back(f);
+    } else {
+        for (int f = last_key + 1; f <= c->run_last; f++) blank.push_back(f);
+        for (int f = last_key; f >= sfirst; f--) frames.push_back(f);
+    }
+    std::map<int, ptk::Ribbon*> acc;
+    struct Free {
+        pt_ctx* c;
+        std::map<int, ptk::Ribbon*>* m;
+        ~Free() {
+            for (auto& kv : *m) dfree_t(c, kv.second);
+        }
+    } free_acc{c, &acc};
+    auto levels_of = [&](int f) { return (int)c->frames[f].size(); };
+    TRY(ensure_ribbons(c));
+    const int k0 = frames.front();
+    TRY(dalloc_t(c, &acc[k0], n));
+    LN(pt::launch_fill_ribbons(acc[k0], n, -1, c->stream));
+    CU(cudaMemcpyAsync(c->rib[0], acc[k0], rb, cudaMemcpyDeviceToDevice, c->stream));
+    for (int f : blank) TRY(ribbon_pyramid(c, acc[k0], levels_of(f), &c->f2k_pyr[d][f]));
+    const int cur = c->img.cur, prev_slot = 1 - c->img.cur;
+    for (int f : frames) {
+        TRY(bind_frame_images(c, f, 0));  // loadImages(0)
+        const int ts = forwards ? -1 : 1;
+        const int pf = f + ts;
+        if ((forwards && pf >= first_key) || (!forwards && pf <= last_key)) {
+            // loadRibbonPair(0, f + ts), synthesisFrame.cpp:658-706
+            const FrameLevel *Lc, *Lp;
+            TRY(frame_level(c, f, 0, &Lc));
+            TRY(frame_level(c, pf, 0, &Lp));
+            const cudaMemcpyKind d2d = cudaMemcpyDeviceToDevice;
+            if (pf < f) {
+                TRY(slot_write(c, &c->up_velb[cur], &c->img.velb[cur], Lc->velb, Lc->w, Lc->h, d2d));
+                TRY(slot_write(c, &c->up_velf[prev_slot], &c->img.velf[prev_slot], Lp->velf, Lp->w, Lp->h, d2d));
+            } else {
+                TRY(slot_write(c, &c->up_velf[cur], &c->img.velf[cur], Lc->velf, Lc->w, Lc->h, d2d));
+                TRY(slot_write(c, &c->up_velb[prev_slot], &c->img.velb[prev_slot], Lp->velb, Lp->w, Lp->h, d2d));
+            }
+            CU(cudaMemcpyAsync(c->rib[0], acc[pf], rb, cudaMemcpyDeviceToDevice, c->stream));
+            TRY(pt_accumulate_ribbon_field(c, 0, forwards ? 1 : 0, ts, 1));
+        }
+        if (!acc.count(f)) TRY(dalloc_t(c, &acc[f], n));
+        CU(cudaMemcpyAsync(acc[f], c->rib[0], rb, cudaMemcpyDeviceToDevice, c->stream));
+        const int k = key_sub_index(c, f);
+        if (k >= 0) {
+            const int full = key_full_index(c, f);
+            TRY(ribbon_pyramid(c, acc[f], levels_of(f), &c->k2k_pyr[d][full]));
+            const ExLevel& S = c->style_levels[0];
+            const float4* key_out = S.out + (size_t)full * S.w * S.h;
+            const size_t px = sizeof(float4);
+            CU(cudaMemcpy2DAsync(c->canvas, c->W * px, key_out, S.w * px, S.w * px, S.h, cudaMemcpyDeviceToDevice,
+                                 c->stream));
+            CU(cudaMemcpy2DAsync(c->adv[0].out, c->W * px, key_out, S.w * px, S.w * px, S.h,
+                                 cudaMemcpyDeviceToDevice, c->stream));
+            LN(pt::launch_fill_ribbons(acc[f], n, k, c->stream));
+            CU(cudaMemcpyAsync(c->rib[0], acc[f], rb, cudaMemcpyDeviceToDevice, c->stream));
+        }
+        TRY(ribbon_pyramid(c, acc[f], levels_of(f), &c->f2k_pyr[d][f]));
+    }
+    CU(cudaStreamSynchronize(c->stream));
+    return PT_OK;
+}
+
+// Style::updateKeyFrameSubrange, style.cpp:175-196 (a key just outside the
+// range joins it through each neighbour inside, once per neighbour)
+static void update_key_subrange(pt_ctx* c, int first, int last) {
+    const std::vector<int>& K = c->key_frames;
+    c->key_sub.clear();
+    for (size_t i = 0; i < K.size(); i++) {
+        const int idx = K[i];
+        if (idx >= first && idx <= last) {
+            c->key_sub.push_back(idx);
+        } else {
+            if (i + 1 < K.size() && K[i + 1] > first && K[i + 1] <= last) c->key_sub.push_back(idx);
+            if (i > 0 && K[i - 1] >= first && K[i - 1] < last) c->key_sub.push_back(idx);
+        }
+    }
+}
+
+// renderAnimation with keyframe interpolation: keyFramesPreprocess
+// (synthesisProcessor.cpp:629-674) then renderAnimationFMBM with
+// SynthesisFrame's keyframe paths
+static pt_status render_fmbm(pt_ctx* c, int first, int last, bool fresh);
+static pt_status render_keyed(pt_ctx* c, int first, int last) {
+    const pt_params user = c->params;
+    if (user.scheme != PT_S_FMBM && user.scheme != PT_S_FMBM_RM)
+        return fail(c, PT_ERR_UNSUPPORTED, "keyframe interpolation runs with the FMBM schemes");
+    if (c->key_frames.empty()) return fail(c, PT_ERR_STATE, "no keyframes set (pt_set_keyframes)");
+    update_key_subrange(c, first, last);
+    if (c->key_sub.empty()) return fail(c, PT_ERR_INVALID, "no keyframe in or next to frames %d..%d", first, last);
+    const int sfirst = std::min(first, c->key_sub.front()), slast = std::max(last, c->key_sub.back());
+    for (int f = sfirst; f <= slast; f++)
+        if (!c->frames.count(f)) return fail(c, PT_ERR_STATE, "frame %d not set", f);
+    const ExLevel& S0 = c->style_levels.empty() ? ExLevel() : c->style_levels[0];
+    if (S0.w != c->W || S0.h != c->H) return fail(c, PT_ERR_INVALID, "keyframe styles must have the image's size");
+    TRY(reset_working(c));
+    TRY(reset_image_slots(c));
+    free_store(c);
+    free_key_ribbons(c);
+    struct Keyed {  // this run interpolates keys; layered uploads copy
+        pt_ctx* c;
+        explicit Keyed(pt_ctx* x) : c(x) { c->keyed = c->slot_copy = true; }
+        ~Keyed() { c->keyed = c->slot_copy = false; }
+    } keyed(c);
+    c->run_first = first;
+    c->run_last = last;
+    pt_params p = user;
+    p.interpolateKeyFrame = 0;  // the preprocess runs the plain kernels
+    TRY(pt_set_params(c, &p));
+    TRY(bind_style_level(c, 0));
+    TRY(accumulate_ribbons(c, true, sfirst, slast));
+    TRY(accumulate_ribbons(c, false, sfirst, slast));
+    p = user;  // keyFramesPreprocess, :664-671
+    p.interpolateKeyFrame = 1;
+    p.numFrames = slast - sfirst;
+    p.firstKeyIndex = key_full_index(c, c->key_sub.front());
+    p.lastKeyIndex = key_full_index(c, c->key_sub.back());
+    TRY(pt_set_params(c, &p));
+    pt_status st = render_fmbm(c, first, last, false);
+    c->params = user;
+    return st;
+}
+
+pt_status pt_set_keyframes(pt_ctx* c, const int32_t* frames, int count) {
+    if (!c || count < 0 || (count > 0 && !frames)) return PT_ERR_INVALID;
+    if (count > c->NS) return fail(c, PT_ERR_INVALID, "%d keyframes but %d style layers", count, c->NS);
+    for (int i = 1; i < count; i++)
+        if (frames[i] <= frames[i - 1]) return fail(c, PT_ERR_INVALID, "keyframes must increase");
+    c->key_frames.assign(frames, frames + count);
+    return PT_OK;
+}
+
 // SynthesisProcessor::renderConsecutivePass, synthesisProcessor.cpp:703-753
 static pt_status consecutive_pass(pt_ctx* c, const pt_params& user, int level, int pass, int source_pass, int first,
                                   int last, bool save_canvas) {
@@ -2135,6 +2406,7 @@ static pt_status consecutive_pass(pt_ctx* c, const pt_params& user, int level, i
         const bool is_first = (i == 0) && (pass == 0);
         if (!is_first) TRY(pt_flip_anim_buffers(c));
         TRY(bind_frame_level(c, fr[i], level));
+        if (c->keyed) bind_frame_keys(c, fr[i], level);
         TRY(synthesize_consecutive(c, user, fr[i], level, pass, is_first, forwards, source_pass, pass == 0,
                                    save_canvas));
     }
@@ -2152,17 +2424,22 @@ static pt_status spatial_upsample(pt_ctx* c, int frame, int coarse, int fine, bo
 }
 
 // SynthesisProcessor::renderAnimationFMBM, synthesisProcessor.cpp:846-878
-static pt_status render_fmbm(pt_ctx* c, int first, int last) {
+// (`fresh`: a new run; a keyed run starts from the state its
+// keyFramesPreprocess left)
+static pt_status render_fmbm(pt_ctx* c, int first, int last, bool fresh) {
     const pt_params user = c->params;
-    TRY(reset_working(c));
-    TRY(reset_image_slots(c));
-    free_store(c);
+    if (fresh) {
+        TRY(reset_working(c));
+        TRY(reset_image_slots(c));
+        free_store(c);
+    }
     const int total = user.fixupPasses + 1;
     const int final_pass = (user.finalLevel == 0) ? total - 1 : 0;
     c->out_level = 0;
     c->out_pass = final_pass;
     for (int level = user.levels - 1; level >= user.finalLevel; level--) {
         TRY(bind_style_level(c, level));
+        if (c->keyed) TRY(upload_key_fields(c, level));
         TRY(pt_reset_advected_buffers(c));
         for (int pass = 0; pass < total; pass++)
             TRY(consecutive_pass(c, user, level, pass, total - 1, first, last,
@@ -2173,6 +2450,7 @@ static pt_status render_fmbm(pt_ctx* c, int first, int last) {
     // renderSpatialUpsample (:1025-1045) down to level 0 from a final level
     for (int level = user.finalLevel; level > 0; level--) {
         TRY(bind_style_level(c, level - 1));
+        if (c->keyed) TRY(upload_key_fields(c, level - 1));
         for (int f = first; f <= last; f++) TRY(spatial_upsample(c, f, level, level - 1, true, level == 1));
         if (level + 1 < user.levels) drop_store_level(c, level + 1);
     }
@@ -2264,17 +2542,14 @@ static pt_status render_tctf(pt_ctx* c, int first, int last) {
 
 static pt_status render(pt_ctx* c, int first, int last) {
     const pt_params& user = c->params;
-    if (user.interpolateKeyFrame)
-        return fail(c, PT_ERR_UNSUPPORTED,
-                    "the keyframe driver (keyFramesPreprocess, accumulateRibbon) is not implemented; the keyframe "
-                    "kernels are reached through the step-wise calls");
+    if (user.interpolateKeyFrame) return render_keyed(c, first, last);
     if (user.levels < 1 || user.finalLevel < 0 || user.finalLevel >= user.levels)
         return fail(c, PT_ERR_INVALID, "bad levels/finalLevel");
     for (int f = first; f <= last; f++)
         if (!c->frames.count(f)) return fail(c, PT_ERR_STATE, "frame %d not set", f);
     switch (user.scheme) {
         case PT_S_FMBM:
-        case PT_S_FMBM_RM: return render_fmbm(c, first, last);
+        case PT_S_FMBM_RM: return render_fmbm(c, first, last, true);
         case PT_S_FBMO: return render_fbmo(c, first, last);
         case PT_S_TCTF: return render_tctf(c, first, last);
         case PT_S_IND: return render_ind(c, first, last);

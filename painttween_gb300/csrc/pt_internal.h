@@ -31,7 +31,9 @@ cudaError_t launch_ribbon_output(const Params& P, const Ribbon* rib, const float
 cudaError_t launch_frame_to_key(const Params& P, PatchPlanes work, int look_forwards, const KeyView& K,
                                 cudaStream_t s);
 cudaError_t launch_merge_advected(const Params& P, int fallback, PatchPlanes work, cudaStream_t s);
-cudaError_t launch_fill_ribbons(Ribbon* r, size_t n, cudaStream_t s);
+cudaError_t launch_fill_ribbons(Ribbon* r, size_t n, int layer, cudaStream_t s);
+cudaError_t launch_ribbon_pack(const Ribbon* src, int w, int h, float4* dst, cudaStream_t s);
+cudaError_t launch_ribbon_down(const float4* src, int sw, float4* dst, int w, int h, cudaStream_t s);
 cudaError_t launch_residual(const Params& P, float* out, cudaStream_t s);
 cudaError_t launch_canvas(const Params& P, float4* canvas, cudaStream_t s);
 cudaError_t launch_random_offsets(const Params& P, PatchPlanes work, cudaStream_t s);
@@ -52,6 +54,9 @@ cudaError_t launch_gather_level(const Params& P, const float* src, int ch, float
 cudaError_t launch_down_avg(const float* src, int w, int h, int ch, int vel, float* dst, cudaStream_t s);
 cudaError_t launch_down_vote(const int* src, int w, int h, int* dst, cudaStream_t s);
 cudaError_t launch_tensor_angle(const float* t3, int n, float* out, cudaStream_t s);
+cudaError_t launch_random_level_keys(int w, int h, int mx, int my, int transparencyOk, int orientationEnabled,
+                                     Arr<float4> img, Arr<float> iorient, ExView ex, float4* out,
+                                     const uint32_t* state31, int nk, int first_key, cudaStream_t s);
 cudaError_t launch_random_level(int mode, int w, int h, int mx, int my, int transparencyOk, int orientationEnabled,
                                 Arr<float4> img, Arr<float> iorient, ExView ex, float4* out,
                                 const uint32_t* states, uint32_t seed, cudaStream_t s);

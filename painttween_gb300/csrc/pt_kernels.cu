@@ -538,6 +538,47 @@ __global__ void k_glibc_serial(const RandParams R, const uint32_t* state31) {
         }
 }
 
+// Keyframe interpolation (createRandomPyramid with setupWithKeys,
+// synthesisFrame.cpp:94-139): each pixel first draws its key layer
+// (rand() % nk + first_key), then the offset in that layer with the retry
+// rule, then the two fractions; one thread, exact glibc order.
+__global__ void k_glibc_serial_keys(const RandParams R, const uint32_t* state31, int nk, int first_key) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    uint32_t ring[31];
+    for (int i = 0; i < 31; i++) ring[i] = state31[i];
+    int head = 0;
+    auto next = [&]() -> uint32_t {
+        int h28 = head + 28;
+        if (h28 >= 31) h28 -= 31;
+        uint32_t v = ring[head] + ring[h28];
+        ring[head] = v;
+        head = (head == 30) ? 0 : head + 1;
+        return v;
+    };
+    const size_t lsz = (size_t)R.ex.w * R.ex.h;
+    for (int y = 0; y < R.h; y++)
+        for (int x = 0; x < R.w; x++) {
+            const int style = (int)((next() >> 1) % (uint32_t)nk) + first_key;
+            const int sl = clampi(style, 0, R.ex.ns - 1);  // a layer of the uploaded exemplar
+            float ia = __ldg(R.img.p + (size_t)y * R.img.w + x).w;
+            int ox, oy, trial = 0;
+            bool again;
+            do {
+                ox = (int)((next() >> 1) % (uint32_t)R.mx);
+                oy = (int)((next() >> 1) % (uint32_t)R.my);
+                trial++;
+                float ea = __ldg(R.ex.out + sl * lsz + (size_t)oy * R.ex.w + ox).w;
+                again = !R.transparencyOk && ia > kAlphaThreshold && ea < kAlphaThreshold && trial < 50;
+            } while (again);
+            float orient = R.orientationEnabled ? __ldg(R.iorient.p + (size_t)y * R.iorient.w + x) -
+                                                      __ldg(R.ex.orient + sl * lsz + (size_t)oy * R.ex.w + ox)
+                                                : 0.f;
+            float rx = (float)(next() >> 1) / (float)2147483647;
+            float ry = (float)(next() >> 1) / (float)2147483647;
+            R.out[(size_t)y * R.w + x] = f4((float)ox + rx, (float)oy + ry, orient, (float)style);
+        }
+}
+
 // counter-based random level: four hashed draws per pixel and trial
 __global__ void k_counter_random(const RandParams R, uint32_t seed) {
     int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -664,6 +705,16 @@ cudaError_t launch_down_vote(const int* src, int w, int h, int* dst, cudaStream_
 }
 cudaError_t launch_tensor_angle(const float* t3, int n, float* out, cudaStream_t s) {
     k_tensor_angle<<<(n + 255) / 256, 256, 0, s>>>(t3, n, out);
+    LAUNCH_CHECK();
+}
+cudaError_t launch_random_level_keys(int w, int h, int mx, int my, int transparencyOk, int orientationEnabled,
+                                     Arr<float4> img, Arr<float> iorient, ExView ex, float4* out,
+                                     const uint32_t* state31, int nk, int first_key, cudaStream_t s) {
+    RandParams R;
+    R.w = w; R.h = h; R.mx = mx; R.my = my;
+    R.transparencyOk = transparencyOk; R.orientationEnabled = orientationEnabled;
+    R.img = img; R.iorient = iorient; R.ex = ex; R.out = out;
+    k_glibc_serial_keys<<<1, 1, 0, s>>>(R, state31, nk, first_key);
     LAUNCH_CHECK();
 }
 cudaError_t launch_random_level(int mode, int w, int h, int mx, int my, int transparencyOk, int orientationEnabled,

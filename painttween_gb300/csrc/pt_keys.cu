@@ -285,16 +285,34 @@ __global__ void __launch_bounds__(kKeyPix) k_merge_advected(const Params P, int 
     store_patch(work, k, res);
 }
 
-// RibbonP() in every texel
-__global__ void k_fill_ribbons(Ribbon* r, size_t n) {
+// RibbonP() with the given layer in every texel (resetRibbonField,
+// synthesisProcessor.cpp:509-517)
+__global__ void k_fill_ribbons(Ribbon* r, size_t n, int layer) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     Ribbon v;
     v.x = 0.f;
     v.y = 0.f;
     v.time_step = 0;
-    v.layer = -1;
+    v.layer = layer;
     r[i] = v;
+}
+
+// initializeRibbonPyramid, imagePyramid.cpp:211-235: level 0 packed as
+// RGBA (toColor4: time_step, y, x, layer) ...
+__global__ void k_ribbon_pack(const Ribbon* src, int w, int h, float4* dst) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    const Ribbon r = src[(size_t)y * w + x];
+    dst[(size_t)y * w + x] = f4((float)r.time_step, r.y, r.x, (float)r.layer);
+}
+// ... and each coarser level the top-left texel of its 2x2 block
+// (RibbonP(Color4) truncates time step and layer to int) with x, y halved
+__global__ void k_ribbon_down(const float4* src, int sw, float4* dst, int w, int h) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    const Ribbon r = ribbon_of(src[(size_t)(2 * y) * sw + 2 * x]);
+    dst[(size_t)y * w + x] = f4((float)r.time_step, r.y * 0.5f, r.x * 0.5f, (float)r.layer);
 }
 
 }  // namespace
@@ -335,9 +353,18 @@ cudaError_t launch_merge_advected(const Params& P, int fallback, PatchPlanes wor
     ptk::k_merge_advected<<<ptk::grid_of(P.lw, P.lh), dim3(32, 4), 0, s>>>(P, fallback, work);
     KEY_LAUNCH_CHECK();
 }
-cudaError_t launch_fill_ribbons(Ribbon* r, size_t n, cudaStream_t s) {
+cudaError_t launch_fill_ribbons(Ribbon* r, size_t n, int layer, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    ptk::k_fill_ribbons<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(r, n);
+    ptk::k_fill_ribbons<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(r, n, layer);
+    KEY_LAUNCH_CHECK();
+}
+cudaError_t launch_ribbon_pack(const Ribbon* src, int w, int h, float4* dst, cudaStream_t s) {
+    ptk::k_ribbon_pack<<<ptk::grid_of(w, h), dim3(32, 4), 0, s>>>(src, w, h, dst);
+    KEY_LAUNCH_CHECK();
+}
+cudaError_t launch_ribbon_down(const float4* src, int sw, float4* dst, int w, int h, cudaStream_t s) {
+    if (w < 1 || h < 1) return cudaSuccess;
+    ptk::k_ribbon_down<<<ptk::grid_of(w, h), dim3(32, 4), 0, s>>>(src, sw, dst, w, h);
     KEY_LAUNCH_CHECK();
 }
 

@@ -217,6 +217,11 @@ class TexSynth:
         self._check(lib().pt_offsets_from_frame_to_key_ribbon(self.h, level, int(look_forwards)),
                     "pt_offsets_from_frame_to_key_ribbon")
 
+    def set_keyframes(self, frames):
+        """Style layer i is the key of frames[i] (increasing)."""
+        a = np.ascontiguousarray(frames, dtype=np.int32)
+        self._check(lib().pt_set_keyframes(self.h, _p(a), int(a.size)), "pt_set_keyframes")
+
     def merge_advected_buffers(self, level, merge_fallback):
         self._check(lib().pt_merge_advected_buffers(self.h, level, merge_fallback), "pt_merge_advected_buffers")
 

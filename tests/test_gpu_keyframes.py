@@ -262,3 +262,40 @@ def test_advect_with_frame_to_key_ribbons_and_merge_advected(fallback):
         kp.compare("merge advected")
     finally:
         kp.close()
+
+
+@pytest.mark.parametrize("keys,first,last,scheme", [([2, 4], 0, 4, _abi.S_FMBM_RM), ([0, 2, 5], 1, 4, _abi.S_FMBM),
+                                                    ([1, 3], 0, 4, _abi.S_FMBM_RM)])
+def test_keyframe_interpolation_driver_matches_oracle(keys, first, last, scheme):
+    """keyFramesPreprocess (ribbons accumulated frame by frame in both
+    directions, key-to-key and frame-to-key pyramids) and the FMBM schedule
+    with SynthesisFrame's keyframe paths, frames before the first key and
+    keys outside the range included."""
+    from painttween_gb300 import Synthesizer
+    p = config_params(r=2, levels=2, iterations=2)
+    p.scheme = scheme
+    p.interpolateKeyFrame = 1
+    p.numStyles = len(keys)
+    styles = [synthetic.make_exemplar(W, H, seed=100 + i) for i in range(len(keys))]
+    out = styles[0]["output"].copy()
+    out[:, : W // 3, 3] = 0.0  # part of the first key left unpainted
+    styles[0]["output"] = out
+    nf = max(last, keys[-1]) + 1
+    clip = synthetic.make_clip(W, H, 3, nf, seed=101)
+    s = Synthesizer(device=0)
+    try:
+        s.setup(p, W, H, W, H, len(keys))
+        for i, ex in enumerate(styles):
+            s.set_style(i, ex["base"], ex["output"], ex["orient_tensor"], ex["dist_trans"], ex["object_ids"])
+        for i, fr in enumerate(clip):
+            s.set_frame_dict(i, fr)
+        s.set_keyframes(keys)
+        got = s.synthesize_animation(first, last)
+    finally:
+        s.close()
+    drv = O.OracleDriver(p, styles, clip, threads=8)
+    drv.set_keyframes(keys)
+    ref = drv.render(first, last)
+    for f in range(first, last + 1):
+        assert_offsets_equal(got[f][1], ref[f][0], 1.0, "keyed frame %d" % f)
+        assert_array_equal(got[f][0], ref[f][2], "keyed output frame %d" % f)
