@@ -593,9 +593,10 @@ class OracleDriver:
         prev_frame = K[prev_key] if has_prev else self.run_first
         next_frame = K[prev_key + 1] if has_next else self.run_last
         f32 = np.float32
-        if forwards:
-            return float(f32(next_frame - frame) / f32(next_frame - prev_frame)) if has_next else 1.0
-        return float(f32(frame - prev_frame) / f32(next_frame - prev_frame)) if has_prev else 1.0
+        with np.errstate(invalid="ignore", divide="ignore"):  # 0/0 at a key: NaN, as in C
+            if forwards:
+                return float(f32(next_frame - frame) / f32(next_frame - prev_frame)) if has_next else 1.0
+            return float(f32(frame - prev_frame) / f32(next_frame - prev_frame)) if has_prev else 1.0
 
     def _random_level_keyed(self, frame, level):
         """createRandomPyramid with setupWithKeys, synthesisFrame.cpp:94-139."""
@@ -675,6 +676,17 @@ class OracleDriver:
                 o.load_ribbon_field(0, acc[f])
             self.f2k[d][f] = self._ribbon_pyramid(acc[f], len(fp["orient"]))
 
+    def _frame(self, f, level):
+        """loadImages + loadAnimImages (with keys: the frame-to-key ribbons)."""
+        self.o.load_frame_level(self.frames[f], level)
+        if self.keyed:
+            self._bind_frame_keys(f, level)
+
+    def _anim(self, f, level):
+        self.o.load_anim_images(self.frames[f], level)
+        if self.keyed:
+            self._bind_frame_keys(f, level)
+
     def _bind_frame_keys(self, frame, level):
         for d in (0, 1):
             pyr = self.f2k[d].get(frame)
@@ -715,31 +727,36 @@ class OracleDriver:
             p.firstKeyIndex = self._key_full(self.key_sub[0])
             p.lastKeyIndex = self._key_full(self.key_sub[-1])
             self.user = p
-            return self._render_fmbm(first, last)
+            return {_abi.S_FBMO: self._render_fbmo, _abi.S_TCTF: self._render_tctf,
+                    _abi.S_IND: self._render_ind}.get(p.scheme, self._render_fmbm)(first, last)
         finally:
             self.user = user
             self.keyed = False
 
-    def _advect_neighbors(self, frame, level, source_pass, first, last):
+    def _advect_neighbors(self, frame, level, source_pass, first, last, neighbours=True):
         """SynthesisFrame::advectNeighbors, synthesisFrame.cpp:325-382, with
-        the frames of the synthesised range as neighbours."""
+        the frames of the synthesised range as neighbours (with keys, a side
+        without one advects the frame-to-key ribbons)."""
         o, u = self.o, self.user
         o.reset_advected()
-        prior = frame - 1 if frame - 1 >= first else None
-        nxt = frame + 1 if frame + 1 <= last else None
+        ops = _abi.ADVECT_CHECK_FRAME_TO_KEY if self.keyed else 0
+        prior = frame - 1 if neighbours and frame - 1 >= first else None
+        nxt = frame + 1 if neighbours and frame + 1 <= last else None
         temporal = (u.timeDerivativeInputWeight > 0 or u.timeDerivativeOutputWeight > 0
                     or u.temporalCoherenceWeight > 0)
-        if last == first or not temporal or (prior is None and nxt is None):
-            o.load_anim_images(self.frames[frame], level)
+        if last == first or not temporal or (prior is None and nxt is None and not self.keyed):
+            self._anim(frame, level)
             return
         for nb, fwd in ((prior, True), (nxt, False)):
-            if nb is None or source_pass < 0:
-                continue
-            o.load_frame_level(self.frames[nb], level)
-            o.flip()
-            o.load_anim_images(self.frames[frame], level)
-            self._load_last_saved(nb, level)
-            o.advect(level, 1, fwd, 0)
+            if nb is not None and source_pass >= 0:
+                self._frame(nb, level)
+                o.flip()
+                self._anim(frame, level)
+                self._load_last_saved(nb, level)
+                o.advect(level, 1, fwd, ops)
+            elif self.keyed:
+                self._anim(frame, level)
+                o.advect(level, 1, fwd, ops | _abi.ADVECT_DO_NOT_CHECK_PREVIOUS)
 
     def synthesize_interpolated(self, frame, level, this_pass, source_pass, first, last):
         """SynthesisFrame::synthesizeInterpolated, synthesisFrame.cpp:384-418."""
@@ -749,7 +766,7 @@ class OracleDriver:
         o.load_images(self.frames[frame], level)
         self._load_offsets(level, frame, source_pass)
         o.sync(level, _abi.DONT_COPY_OFFSETS | _abi.DONT_UPDATE_RESIDUAL)
-        self.propagate_and_scatter(level, self.user.iterations)
+        self.propagate_and_scatter(level, self.user.iterations, self._key_full(frame) if self.keyed else -1)
         self._save_images(level, frame, this_pass)
 
     def _render_fbmo(self, first, last):
@@ -759,6 +776,8 @@ class OracleDriver:
         final_pass = u.fixupPasses + 2
         for level in range(self.levels - 1, u.finalLevel - 1, -1):
             o.load_style_level(self.styles, level)
+            if self.keyed:
+                self._upload_key_fields(level)
             for pass_ in (0, 1):
                 o.reset_advected()
                 forwards = pass_ == 0
@@ -767,7 +786,7 @@ class OracleDriver:
                     is_first = i == 0
                     if not is_first or pass_ > 0:
                         o.flip()
-                    o.load_frame_level(self.frames[f], level)
+                    self._frame(f, level)
                     self.synthesize_consecutive(f, level, pass_, is_first, forwards, final_pass, True)
             for f in range(first, last + 1):  # pass 2: forward and backward merged
                 self._load_offsets(level, f, 0)
@@ -777,7 +796,8 @@ class OracleDriver:
                 self._load_offsets(level, f, 1)
                 self._load_residual(level, f, 1)
                 o.sync(level, _abi.DONT_COPY_OFFSETS | _abi.DONT_UPDATE_RESIDUAL)
-                o.merge_randomly(level, True, 0.5, True)  # TexSynth::mergeRandomly ends with a sync
+                w = self._key_advect_weight(f, True) if self.keyed else 0.5
+                o.merge_randomly(level, True, w, True)  # TexSynth::mergeRandomly ends with a sync
                 o.sync(level)
                 self._save(level, f, 2)
             for pass_ in range(3, u.fixupPasses + 3):
@@ -793,9 +813,11 @@ class OracleDriver:
         for f in range(first, last + 1):
             for level in range(self.levels - 1, self.user.finalLevel - 1, -1):
                 self.o.load_style_level(self.styles, level)
+                if self.keyed:
+                    self._upload_key_fields(level)
                 self.o.reset_advected()
                 for pass_ in range(total):
-                    self.o.load_frame_level(self.frames[f], level)
+                    self._frame(f, level)
                     self.synthesize_consecutive(f, level, pass_, True, True, pass_, pass_ == 0)
         final_pass = total - 1 if self.user.finalLevel == 0 else 0
         return {f: self.store[(self.user.finalLevel, f, final_pass)] for f in range(first, last + 1)}
@@ -836,28 +858,35 @@ class OracleDriver:
         if save:
             self._save_images(fine, frame, 0)
 
-    def _refine_pass(self, level, last_coarse_pass, this_pass, first, last):
+    def _refine_pass(self, level, last_coarse_pass, this_pass, first, last, initialize=False):
         """renderRefinePass (REFINE_EVEN_AND_ODD), synthesisProcessor.cpp:
-        1078-1150, and SynthesisFrame::refine, synthesisFrame.cpp:420-463."""
+        1078-1150, and SynthesisFrame::refine, synthesisFrame.cpp:420-463;
+        `initialize`: renderInitializationPass (:1047-1076), the frames
+        without neighbours, merged from the advected buffers at the coarsest
+        level."""
         o = self.o
-        spatial = last_coarse_pass == this_pass - 1
+        coarsest = level == self.levels - 1
+        temporal_up = initialize and coarsest
+        spatial = (not coarsest) if initialize else last_coarse_pass == this_pass - 1
         for f in range(first, last + 1):
             self._update_parameters(f, _abi.BIDIRECTIONAL)
-            self._advect_neighbors(f, level, this_pass - 1, first, last)
-            if spatial:
+            self._advect_neighbors(f, level, this_pass - 1, first, last, not initialize)
+            if temporal_up:
+                o.merge_advected_buffers(level, _abi.MERGE_FALLBACK_RANDOM)
+            elif spatial:
                 self._spatial_upsample(f, level + 1, level, False)
             else:
                 self._load_last_saved(f, level)
                 o.sync(level, _abi.DONT_COPY_OFFSETS | _abi.DONT_UPDATE_RESIDUAL)
             o.load_images(self.frames[f], level)
-            self.propagate_and_scatter(level, self.user.iterations)
+            self.propagate_and_scatter(level, self.user.iterations, self._key_full(f) if self.keyed else -1)
             self._save_images(level, f, this_pass)
 
     def _render_tctf(self, first, last):
         """renderAnimationTCTF, synthesisProcessor.cpp:1152-1312, run locally
         without ribbon inputs (time step 1)."""
         u = self.user
-        ops = [("consecutive", self.levels - 1)]
+        ops = [("initialize" if self.keyed else "consecutive", self.levels - 1)]
         for level in range(self.levels - 1, u.finalLevel - 1, -1):
             ops.append(("refine", level))
             if 1 < last - first:
@@ -869,9 +898,14 @@ class OracleDriver:
         for op, level in ops:
             if last_level != level:
                 self.o.load_style_level(self.styles, level)
+                if self.keyed:
+                    self._upload_key_fields(level)
                 passes_last = passes_this
                 last_level = level
-            if op == "consecutive":
+            if op == "initialize":
+                self._refine_pass(level, passes_this - 1, 0, first, last, initialize=True)
+                passes_this = 1
+            elif op == "consecutive":
                 self._render_pass(level, passes_this, passes_this - 1, first, last)
                 passes_this += 1
             elif op == "refine":
@@ -894,8 +928,6 @@ class OracleDriver:
             is_first = (i == 0) and (pass_ == 0)
             if not is_first:
                 self.o.flip()
-            self.o.load_frame_level(self.frames[f], level)
-            if self.keyed:
-                self._bind_frame_keys(f, level)
+            self._frame(f, level)
             self.synthesize_consecutive(f, level, pass_, is_first, forwards, source_pass, pass_ == 0)
 

@@ -393,6 +393,7 @@ static inline int id_texel(const pto* o, int x, int y) {
     return o->img_ids[(size_t)y * o->ii_w + x];
 }
 static inline f4 rnd_texel(const pto* o, int x, int y) {
+    if (!o->rnd) { f4 z = {0, 0, 0, 0}; return z; } /* never uploaded: zero */
     x = clampi(x, 0, o->rn_w - 1); y = clampi(y, 0, o->rn_h - 1);
     return o->rnd[(size_t)y * o->rn_w + x];
 }

@@ -413,6 +413,25 @@ static pt_status refresh_interleaved(pt_ctx* c, ExLevel* L) {
     return PT_OK;
 }
 
+template <class T>
+static pt_status zero_layer(pt_ctx* c, T** buf, Arr<T>* bind) {
+    if (bind->p) return PT_OK;
+    const size_t n = (size_t)c->W * c->H;
+    if (!*buf) TRY(dalloc_t(c, buf, n));
+    CU(cudaMemsetAsync(*buf, 0, n * sizeof(T), c->stream));
+    *bind = Arr<T>{*buf, c->W, c->H};
+    return PT_OK;
+}
+static pt_status bind_unwritten_layers(pt_ctx* c) {
+    for (int i = 0; i < 2; i++) {
+        TRY(zero_layer(c, &c->up_base[i], &c->img.base[i]));
+        TRY(zero_layer(c, &c->up_dt[i], &c->img.dt[i]));
+        TRY(zero_layer(c, &c->up_velf[i], &c->img.velf[i]));
+        TRY(zero_layer(c, &c->up_velb[i], &c->img.velb[i]));
+    }
+    return PT_OK;
+}
+
 static pt_status check_ready(pt_ctx* c, int level, bool need_ex = true, bool need_img = true) {
     if (!c->initialized) return fail(c, PT_ERR_STATE, "pt_initialize has not been called");
     if (!c->have_params) return fail(c, PT_ERR_STATE, "pt_set_params has not been called");
@@ -423,11 +442,10 @@ static pt_status check_ready(pt_ctx* c, int level, bool need_ex = true, bool nee
     if (need_img) {
         // A layered input holds whatever level was last written into it, as
         // the reference's layered textures do (a kernel at another level
-        // reads that level's texels, and zero outside them), so only its
-        // presence is checked.
+        // reads that level's texels, and zero outside them); a layer never
+        // written reads zero (a zeroed full-size array is bound to it).
+        TRY(bind_unwritten_layers(c));
         const ImgView& I = c->img;
-        if (!I.base[I.cur].p) return fail(c, PT_ERR_STATE, "input colour not uploaded (level %d)", level);
-        if (!I.dt[I.cur].p) return fail(c, PT_ERR_STATE, "input distance transform not uploaded (level %d)", level);
         if (!I.orient.p || !I.scale.p || !I.ids.p)
             return fail(c, PT_ERR_STATE, "input orientation/scale/ids not uploaded");
     }
@@ -966,9 +984,11 @@ static pt_status slot_write(pt_ctx* c, T** slot, Arr<T>* bind, const void* src, 
     return PT_OK;
 }
 
-// A fresh run: no input image bound, the layered arrays all zero.
+// A fresh run: no input image or random level bound, the layered arrays all
+// zero.
 static pt_status reset_image_slots(pt_ctx* c) {
     const size_t n = (size_t)c->W * c->H;
+    c->img.rnd = Arr<float4>{};
     for (int i = 0; i < 2; i++) {
         c->img.base[i] = Arr<float4>{};
         c->img.dt[i] = Arr<float>{};
@@ -1351,6 +1371,16 @@ pt_status pt_upsample(pt_ctx* c, int fine_level) {
     LN(pt::launch_upsample(P, work, old_base, aliased ? 1 : 0, res_out, c->stream));
     c->res_i = 1 - c->res_i;
     c->base_i = c->work_i;  // copyWorkingToBase for offsets and residual
+    return PT_OK;
+}
+
+// A run that advects before any random level was drawn (TCTF's keyframe
+// initialisation) reads the never-uploaded random texture: zero.
+static pt_status ensure_random(pt_ctx* c) {
+    if (c->img.rnd.p) return PT_OK;
+    if (!c->rnd) TRY(dalloc_t(c, &c->rnd, (size_t)c->W * c->H));
+    CU(cudaMemsetAsync(c->rnd, 0, sizeof(float4), c->stream));
+    c->img.rnd = Arr<float4>{c->rnd, 1, 1};
     return PT_OK;
 }
 
@@ -1747,6 +1777,8 @@ static pt_status bind_style_level(pt_ctx* c, int level) {
     return refresh_interleaved(c, c->ex);
 }
 
+static void bind_frame_keys(pt_ctx* c, int frame, int level);
+
 // SynthesisFrame::loadImages + loadAnimImages, synthesisFrame.cpp:562-656
 static pt_status frame_level(pt_ctx* c, int frame, int level, const FrameLevel** out) {
     auto it = c->frames.find(frame);
@@ -1793,6 +1825,7 @@ static pt_status bind_frame_anim(pt_ctx* c, int frame, int level) {
         c->img.velb[cur] = Arr<float2>{L->velb, L->w, L->h};
     }
     c->img.scale = Arr<float2>{L->scale, L->w, L->h};
+    if (c->keyed) bind_frame_keys(c, frame, level);
     return PT_OK;
 }
 static pt_status bind_frame_level(pt_ctx* c, int frame, int level) {
@@ -1961,7 +1994,7 @@ static float key_advect_weight(const pt_ctx* c, int frame, bool forwards) {
 // SynthesisFrame::createRandomPyramid with setupWithKeys
 // (synthesisFrame.cpp:66-150): the glibc stream of srand(frame*level), each
 // pixel drawing its key layer first; one GPU thread walks the stream.
-static pt_status random_level_keyed(pt_ctx* c, int level, int frame) {
+static pt_status random_level_keyed(pt_ctx* c, int level, int frame, Arr<float4> rgba, Arr<float> orient) {
     TRY(check_ready(c, level));
     const int lw = c->W >> level, lh = c->H >> level;
     const int mx = (c->SW >> level) - 1, my = (c->SH >> level) - 1;
@@ -1978,9 +2011,8 @@ static pt_status random_level_keyed(pt_ctx* c, int level, int frame) {
     CU(cudaStreamSynchronize(c->stream));
     ExView ex{c->ex->base, c->ex->out, c->ex->bo, c->ex->orient, c->ex->dt, c->ex->ids, c->ex->w, c->ex->h, c->NS};
     const int nk = (int)c->key_sub.size(), first_key = key_full_index(c, c->key_sub.front());
-    LN(pt::launch_random_level_keys(lw, lh, mx, my, c->params.transparencyOk, c->params.orientationEnabled,
-                                    c->img.base[c->img.cur], c->img.orient, ex, c->rnd, c->states, nk, first_key,
-                                    c->stream));
+    LN(pt::launch_random_level_keys(lw, lh, mx, my, c->params.transparencyOk, c->params.orientationEnabled, rgba,
+                                    orient, ex, c->rnd, c->states, nk, first_key, c->stream));
     c->img.rnd = Arr<float4>{c->rnd, lw, lh};
     return PT_OK;
 }
@@ -1998,7 +2030,7 @@ static pt_status synthesize_consecutive(pt_ctx* c, const pt_params& user, int fr
     // SynthesisFrame::mergeRandomly, :510-520
     const float advect_weight = c->keyed ? key_advect_weight(c, frame, forwards) : 0.5f;
     if (first_pass) {
-        if (c->keyed) TRY(random_level_keyed(c, level, frame));
+        if (c->keyed) TRY(random_level_keyed(c, level, frame, c->img.base[c->img.cur], c->img.orient));
         else TRY(pt_create_random_level(c, level, frame));
         if (is_first) {
             if (coarsest) {
@@ -2049,19 +2081,24 @@ static void drop_store_level(pt_ctx* c, int level) {
     }
 }
 
+static pt_status upload_key_fields(pt_ctx* c, int level);
+
 // SynthesisProcessor::renderAnimationIND, synthesisProcessor.cpp:807-844:
 // every frame synthesised on its own, coarse to fine, each pass through
 // synthesizeConsecutive as a first frame going forwards
-static pt_status render_ind(pt_ctx* c, int first, int last) {
+static pt_status render_ind(pt_ctx* c, int first, int last, bool fresh) {
     const pt_params user = c->params;
-    TRY(reset_working(c));
-    TRY(reset_image_slots(c));
+    if (fresh) {
+        TRY(reset_working(c));
+        TRY(reset_image_slots(c));
+        free_store(c);
+    }
     struct SlotCopy {  // frame binds copy into the layered arrays for this run
         pt_ctx* c;
-        explicit SlotCopy(pt_ctx* x) : c(x) { c->slot_copy = true; }
-        ~SlotCopy() { c->slot_copy = false; }
+        bool was;
+        explicit SlotCopy(pt_ctx* x) : c(x), was(x->slot_copy) { c->slot_copy = true; }
+        ~SlotCopy() { c->slot_copy = was; }
     } slot_copy(c);
-    free_store(c);
     const int total = user.fixupPasses + 1;
     const int final_pass = (user.finalLevel == 0) ? total - 1 : 0;
     c->out_level = user.finalLevel;
@@ -2069,6 +2106,7 @@ static pt_status render_ind(pt_ctx* c, int first, int last) {
     for (int f = first; f <= last; f++) {
         for (int level = user.levels - 1; level >= user.finalLevel; level--) {
             TRY(bind_style_level(c, level));
+            if (c->keyed) TRY(upload_key_fields(c, level));
             TRY(pt_reset_advected_buffers(c));
             for (int pass = 0; pass < total; pass++) {
                 const bool save_canvas = (level == user.finalLevel && pass == final_pass);
@@ -2101,22 +2139,32 @@ pt_status pt_copy_offsets_to_advected(pt_ctx* c, int forwards) {
 // neighbours' last saved offsets advected into this frame (the neighbour's
 // images in the current layer, then this frame's velocities in the other).
 // Neighbours are the frames of the synthesised range.
-static pt_status advect_neighbors(pt_ctx* c, int frame, int level, int source_pass, int first, int last) {
+// With keys, a side without a neighbour advects this frame's frame-to-key
+// ribbons instead (ADVECT_DO_NOT_CHECK_PREVIOUS).  `neighbours` false: the
+// refine of TCTF's initialisation pass, which is given none.
+static pt_status advect_neighbors(pt_ctx* c, int frame, int level, int source_pass, int first, int last,
+                                  bool neighbours = true) {
     TRY(pt_reset_advected_buffers(c));
     const pt_params& p = c->params;
-    const bool has_prior = frame - 1 >= first, has_next = frame + 1 <= last;
+    const int ops = c->keyed ? PT_ADVECT_CHECK_FRAME_TO_KEY : 0;
+    const bool has_prior = neighbours && frame - 1 >= first, has_next = neighbours && frame + 1 <= last;
     const bool temporal = p.timeDerivativeInputWeight > 0.f || p.timeDerivativeOutputWeight > 0.f ||
                           p.temporalCoherenceWeight > 0.f;
-    if (last == first || !temporal || !(has_prior || has_next)) return bind_frame_anim(c, frame, level);
+    if (last == first || !temporal || !(has_prior || has_next || c->keyed)) return bind_frame_anim(c, frame, level);
     for (int side = 0; side < 2; side++) {
         const bool fwd = side == 0;
         const int nb = fwd ? frame - 1 : frame + 1;
-        if (!(fwd ? has_prior : has_next) || source_pass < 0) continue;
-        TRY(bind_frame_level(c, nb, level));
-        TRY(pt_flip_anim_buffers(c));
-        TRY(bind_frame_anim(c, frame, level));
-        TRY(load_last_saved_offsets(c, nb, level));
-        TRY(pt_advect_offsets(c, level, 1, fwd ? 1 : 0, 0));
+        if ((fwd ? has_prior : has_next) && source_pass >= 0) {
+            TRY(bind_frame_level(c, nb, level));
+            TRY(pt_flip_anim_buffers(c));
+            TRY(bind_frame_anim(c, frame, level));
+            TRY(load_last_saved_offsets(c, nb, level));
+            TRY(pt_advect_offsets(c, level, 1, fwd ? 1 : 0, ops));
+        } else if (c->keyed) {
+            TRY(bind_frame_anim(c, frame, level));
+            TRY(ensure_random(c));
+            TRY(pt_advect_offsets(c, level, 1, fwd ? 1 : 0, ops | PT_ADVECT_DO_NOT_CHECK_PREVIOUS));
+        }
     }
     return PT_OK;
 }
@@ -2133,7 +2181,7 @@ static pt_status synthesize_interpolated(pt_ctx* c, const pt_params& user, int f
     TRY(bind_frame_images(c, frame, level));
     TRY(store_load_offsets(c, level, frame, source_pass));
     TRY(do_sync(c, level, PT_DONT_COPY_OFFSETS | PT_DONT_UPDATE_RESIDUAL));
-    TRY(propagate_and_scatter(c, level, user.iterations, false));
+    TRY(propagate_and_scatter(c, level, user.iterations, false, c->keyed ? key_full_index(c, frame) : -1));
     return save_images(c, level, frame, this_pass, save_canvas);
 }
 
@@ -2141,16 +2189,19 @@ static pt_status synthesize_interpolated(pt_ctx* c, const pt_params& user, int f
 // per level a forward and a backward consecutive pass, their results merged
 // at random (pass 2), then fix-up passes that synthesise every frame between
 // its neighbours
-static pt_status render_fbmo(pt_ctx* c, int first, int last) {
+static pt_status render_fbmo(pt_ctx* c, int first, int last, bool fresh) {
     const pt_params user = c->params;
-    TRY(reset_working(c));
-    TRY(reset_image_slots(c));
-    free_store(c);
+    if (fresh) {
+        TRY(reset_working(c));
+        TRY(reset_image_slots(c));
+        free_store(c);
+    }
     const int final_pass = user.fixupPasses + 2;
     c->out_level = user.finalLevel;
     c->out_pass = final_pass;
     for (int level = user.levels - 1; level >= user.finalLevel; level--) {
         TRY(bind_style_level(c, level));
+        if (c->keyed) TRY(upload_key_fields(c, level));
         const bool final_level = level == user.finalLevel;
         for (int pass = 0; pass < 2; pass++) {  // passes 0 and 1
             TRY(pt_reset_advected_buffers(c));
@@ -2171,14 +2222,18 @@ static pt_status render_fbmo(pt_ctx* c, int first, int last) {
             TRY(store_load_offsets(c, level, f, 1));
             TRY(store_load_residual(c, level, f, 1));
             TRY(do_sync(c, level, PT_DONT_COPY_OFFSETS | PT_DONT_UPDATE_RESIDUAL));
-            TRY(pt_merge_randomly(c, level, 1, 0.5f, 1));  // SynthesisFrame::mergeRandomly, :510-520
+            // SynthesisFrame::mergeRandomly, :510-520
+            TRY(pt_merge_randomly(c, level, 1, c->keyed ? key_advect_weight(c, f, true) : 0.5f, 1));
             TRY(store_save(c, level, f, 2, final_level && final_pass == 2));
         }
         for (int pass = 3; pass < user.fixupPasses + 3; pass++) {  // renderInterpolatedFixupPass, :880-924
             for (int f = first; f <= last; f++) {
                 const FrameLevel* L;
                 TRY(frame_level(c, f, level, &L));
-                TRY(random_level(c, level, f, Arr<float4>{L->rgba, L->w, L->h}, Arr<float>{L->orient, L->w, L->h}));
+                const Arr<float4> rgba{L->rgba, L->w, L->h};
+                const Arr<float> orient{L->orient, L->w, L->h};
+                if (c->keyed) TRY(random_level_keyed(c, level, f, rgba, orient));
+                else TRY(random_level(c, level, f, rgba, orient));
                 TRY(synthesize_interpolated(c, user, f, level, pass, pass - 1, first, last,
                                             final_level && pass == final_pass));
             }
@@ -2342,10 +2397,11 @@ static void update_key_subrange(pt_ctx* c, int first, int last) {
 // (synthesisProcessor.cpp:629-674) then renderAnimationFMBM with
 // SynthesisFrame's keyframe paths
 static pt_status render_fmbm(pt_ctx* c, int first, int last, bool fresh);
+static pt_status render_fbmo(pt_ctx* c, int first, int last, bool fresh);
+static pt_status render_tctf(pt_ctx* c, int first, int last, bool fresh);
+static pt_status render_ind(pt_ctx* c, int first, int last, bool fresh);
 static pt_status render_keyed(pt_ctx* c, int first, int last) {
     const pt_params user = c->params;
-    if (user.scheme != PT_S_FMBM && user.scheme != PT_S_FMBM_RM)
-        return fail(c, PT_ERR_UNSUPPORTED, "keyframe interpolation runs with the FMBM schemes");
     if (c->key_frames.empty()) return fail(c, PT_ERR_STATE, "no keyframes set (pt_set_keyframes)");
     update_key_subrange(c, first, last);
     if (c->key_sub.empty()) return fail(c, PT_ERR_INVALID, "no keyframe in or next to frames %d..%d", first, last);
@@ -2377,7 +2433,13 @@ static pt_status render_keyed(pt_ctx* c, int first, int last) {
     p.firstKeyIndex = key_full_index(c, c->key_sub.front());
     p.lastKeyIndex = key_full_index(c, c->key_sub.back());
     TRY(pt_set_params(c, &p));
-    pt_status st = render_fmbm(c, first, last, false);
+    pt_status st;
+    switch (user.scheme) {
+        case PT_S_FBMO: st = render_fbmo(c, first, last, false); break;
+        case PT_S_TCTF: st = render_tctf(c, first, last, false); break;
+        case PT_S_IND: st = render_ind(c, first, last, false); break;
+        default: st = render_fmbm(c, first, last, false); break;
+    }
     c->params = user;
     return st;
 }
@@ -2406,7 +2468,6 @@ static pt_status consecutive_pass(pt_ctx* c, const pt_params& user, int level, i
         const bool is_first = (i == 0) && (pass == 0);
         if (!is_first) TRY(pt_flip_anim_buffers(c));
         TRY(bind_frame_level(c, fr[i], level));
-        if (c->keyed) bind_frame_keys(c, fr[i], level);
         TRY(synthesize_consecutive(c, user, fr[i], level, pass, is_first, forwards, source_pass, pass == 0,
                                    save_canvas));
     }
@@ -2463,23 +2524,32 @@ static pt_status render_fmbm(pt_ctx* c, int first, int last, bool fresh) {
 // synthesisFrame.cpp:420-463: every frame between its advected neighbours,
 // started from the upsampled coarse level (the level's first refine pass)
 // or from its own last saved pass
+//
+// `initialize`: renderInitializationPass (:1047-1076) with keys, each frame
+// refined as pass 0 without neighbours, from the advected buffers merged
+// (mergeAdvectedBuffers, random fallback) at the coarsest level
 static pt_status refine_pass(pt_ctx* c, const pt_params& user, int level, int last_coarse_pass, int this_pass,
-                             int first, int last, bool save_canvas) {
-    const bool spatial = last_coarse_pass == this_pass - 1;
+                             int first, int last, bool save_canvas, bool initialize = false) {
+    const bool coarsest = level == user.levels - 1;
+    const bool temporal_up = initialize && coarsest;
+    const bool spatial = initialize ? !coarsest : last_coarse_pass == this_pass - 1;
     for (int f = first; f <= last; f++) {
         pt_params p = user;  // updateParameters(BIDIRECTIONAL), :522-542
         p.advectionJitter = (f % 3 == 0) ? user.advectionJitter * 0.01f : 0.0f;
         p.direction = PT_BIDIRECTIONAL;
         TRY(pt_set_params(c, &p));
-        TRY(advect_neighbors(c, f, level, this_pass - 1, first, last));
-        if (spatial) {
+        TRY(advect_neighbors(c, f, level, this_pass - 1, first, last, !initialize));
+        if (temporal_up) {
+            TRY(ensure_random(c));
+            TRY(pt_merge_advected_buffers(c, level, PT_MERGE_FALLBACK_RANDOM));
+        } else if (spatial) {
             TRY(spatial_upsample(c, f, level + 1, level, false, false));
         } else {
             TRY(load_last_saved_offsets(c, f, level));
             TRY(do_sync(c, level, PT_DONT_COPY_OFFSETS | PT_DONT_UPDATE_RESIDUAL));
         }
         TRY(bind_frame_images(c, f, level));
-        TRY(propagate_and_scatter(c, level, user.iterations, false));
+        TRY(propagate_and_scatter(c, level, user.iterations, false, c->keyed ? key_full_index(c, f) : -1));
         TRY(save_images(c, level, f, this_pass, save_canvas));
     }
     return PT_OK;
@@ -2490,14 +2560,16 @@ static pt_status refine_pass(pt_ctx* c, const pt_params& user, int level, int la
 // 1): a consecutive pass at the coarsest level, refine passes at every level
 // from the coarsest to the final one (fixupPasses + 1 more when the range
 // spans more than two frames), then spatial upsampling down to level 0
-static pt_status render_tctf(pt_ctx* c, int first, int last) {
+static pt_status render_tctf(pt_ctx* c, int first, int last, bool fresh) {
     const pt_params user = c->params;
-    TRY(reset_working(c));
-    TRY(reset_image_slots(c));
-    free_store(c);
-    enum { CONSECUTIVE, REFINE, UPSAMPLE };
+    if (fresh) {
+        TRY(reset_working(c));
+        TRY(reset_image_slots(c));
+        free_store(c);
+    }
+    enum { CONSECUTIVE, REFINE, UPSAMPLE, INITIALIZE };
     std::vector<std::pair<int, int>> ops;  // (operation, level)
-    ops.emplace_back(CONSECUTIVE, user.levels - 1);
+    ops.emplace_back(c->keyed ? INITIALIZE : CONSECUTIVE, user.levels - 1);
     for (int level = user.levels - 1; level >= user.finalLevel; level--) {
         ops.emplace_back(REFINE, level);
         if (1 < last - first)
@@ -2512,12 +2584,17 @@ static pt_status render_tctf(pt_ctx* c, int first, int last) {
             const int level = op.second;
             if (last_level != level) {
                 if (run) TRY(bind_style_level(c, level));
+                if (run && c->keyed) TRY(upload_key_fields(c, level));
                 if (run && last_level >= 0 && last_level + 1 < user.levels) drop_store_level(c, last_level + 1);
                 passes_last = passes_this;
                 last_level = level;
             }
             const bool final_save = level == 0 && run && passes_this == c->out_pass;
-            if (op.first == CONSECUTIVE) {
+            if (op.first == INITIALIZE) {
+                if (run) TRY(refine_pass(c, user, level, passes_this - 1, 0, first, last, final_save && 0 == c->out_pass,
+                                         true));
+                passes_this = 1;
+            } else if (op.first == CONSECUTIVE) {
                 if (run) TRY(consecutive_pass(c, user, level, passes_this, passes_this - 1, first, last, final_save));
                 passes_this++;
             } else if (op.first == REFINE) {
@@ -2550,9 +2627,9 @@ static pt_status render(pt_ctx* c, int first, int last) {
     switch (user.scheme) {
         case PT_S_FMBM:
         case PT_S_FMBM_RM: return render_fmbm(c, first, last, true);
-        case PT_S_FBMO: return render_fbmo(c, first, last);
-        case PT_S_TCTF: return render_tctf(c, first, last);
-        case PT_S_IND: return render_ind(c, first, last);
+        case PT_S_FBMO: return render_fbmo(c, first, last, true);
+        case PT_S_TCTF: return render_tctf(c, first, last, true);
+        case PT_S_IND: return render_ind(c, first, last, true);
         default: return fail(c, PT_ERR_INVALID, "unknown scheme %d", user.scheme);
     }
 }

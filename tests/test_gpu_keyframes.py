@@ -265,12 +265,14 @@ def test_advect_with_frame_to_key_ribbons_and_merge_advected(fallback):
 
 
 @pytest.mark.parametrize("keys,first,last,scheme", [([2, 4], 0, 4, _abi.S_FMBM_RM), ([0, 2, 5], 1, 4, _abi.S_FMBM),
-                                                    ([1, 3], 0, 4, _abi.S_FMBM_RM)])
+                                                    ([1, 3], 0, 4, _abi.S_FMBM_RM), ([1, 4], 0, 4, _abi.S_FBMO),
+                                                    ([1, 4], 0, 4, _abi.S_TCTF), ([0, 3], 0, 3, _abi.S_IND)])
 def test_keyframe_interpolation_driver_matches_oracle(keys, first, last, scheme):
     """keyFramesPreprocess (ribbons accumulated frame by frame in both
-    directions, key-to-key and frame-to-key pyramids) and the FMBM schedule
-    with SynthesisFrame's keyframe paths, frames before the first key and
-    keys outside the range included."""
+    directions, key-to-key and frame-to-key pyramids) and each scheme's
+    schedule with SynthesisFrame's keyframe paths (TCTF starting with its
+    initialisation pass), frames before the first key and keys outside the
+    range included."""
     from painttween_gb300 import Synthesizer
     p = config_params(r=2, levels=2, iterations=2)
     p.scheme = scheme
