@@ -102,7 +102,7 @@ typedef struct {
     int32_t transparencyOk;
     float styleObjIdWeight;
     int32_t orientationEnabled;
-    int32_t colorspace; /* 0 = RGB (1 = Lab is not implemented) */
+    int32_t colorspace; /* 0 = RGB, 1 = Lab (RGBtoLAB before every comparison) */
     float coherenceRatioRange;
     float coherenceAngleRange;
     int32_t levels;

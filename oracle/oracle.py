@@ -92,6 +92,8 @@ def lib():
             "pto_load_canvas": (None, [vp, i, vp]),
             "pto_get_advected_output": (None, [vp, i, i, vp]),
             "pto_merge_advected": (None, [vp, i, i]),
+            "pto_rgb_to_lab": (f, [vp, vp]),
+            "pto_powd": (ctypes.c_double, [ctypes.c_double, ctypes.c_double]),
             "pto_random_level_keys": (i, [u32, i, i, i, i, i, vp, vp, vp, vp, i, i, i, i, i, i, i, vp]),
         }
         for name, (res, args) in sig.items():
@@ -204,6 +206,14 @@ def counter_random_level(seed, level, style_w0, style_h0, img_rgba, img_orient, 
 def counter_seed(rng_seed, frame, level):
     """Seed of one random level in PT_RNG_COUNTER mode."""
     return (rng_seed ^ ((0x9E3779B9 * (frame + 1)) & 0xFFFFFFFF) ^ ((0x85EBCA6B * (level + 1)) & 0xFFFFFFFF)) & 0xFFFFFFFF
+
+
+def rgb_to_lab(rgba):
+    """RGBtoLAB of one colour (the oracle's double pow)."""
+    a = np.ascontiguousarray(rgba, np.float32)
+    out = np.empty(4, np.float32)
+    lib().pto_rgb_to_lab(_p(a), _p(out))
+    return out
 
 
 def glibc_stream(seed, n):

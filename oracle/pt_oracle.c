@@ -184,6 +184,72 @@ static float pt_logf(float x) {
     return fmaf(fe, 0x1.62e430p-1f, fmaf(fe, -0x1.05c610p-29f, lm));
 }
 
+/* double log, exp and pow for the Lab conversion (shared contract with the
+ * CUDA side): log by frexp to m in [sqrt(1/2), sqrt(2)) and the atanh series
+ * 2 (s + s^3/3 + ... + s^23/23), s = (m-1)/(m+1); exp by k = rint(y/ln2),
+ * r = y - k ln2 (two-part ln2) and the Taylor series to r^22; pow(x, y) =
+ * exp(y log x) for x > 0. */
+static double pt_logd(double x) {
+    int e;
+    double m = frexp(x, &e);
+    if (m < 0.70710678118654752440) { m = m * 2.0; e -= 1; }
+    double s = (m - 1.0) / (m + 1.0);
+    double s2 = s * s;
+    double p = 1.0 / 23.0;
+    for (int k = 21; k >= 3; k -= 2) p = fma(s2, p, 1.0 / (double)k);
+    p = p * s2;
+    double lm = 2.0 * fma(s, p, s);
+    double fe = (double)e;
+    return fma(fe, 6.93147180369123816490e-01, fma(fe, 1.90821492927058770002e-10, lm));
+}
+static double pt_expd(double y) {
+    double k = rint(y * 1.44269504088896338700);
+    double r = fma(-k, 6.93147180369123816490e-01, y);
+    r = fma(-k, 1.90821492927058770002e-10, r);
+    double p = 1.0; /* 1 + r/1 (1 + r/2 (1 + ... (1 + r/22))) */
+    for (int n = 22; n >= 1; n--) p = fma(r / (double)n, p, 1.0);
+    return ldexp(p, (int)k);
+}
+static double pt_powd(double x, double y) {
+    if (!(x > 0.0)) return (x == 0.0) ? 0.0 : NAN;
+    return pt_expd(y * pt_logd(x));
+}
+
+/* RGBtoLAB with Clinear and f_Lab, texSynth_util.h:175-192,220-246 (D65;
+ * the double-precision steps are the ones the C++ promotes to double) */
+static float lab_clinear(float c) {
+    const float a = 0.055f;
+    if ((double)c > 0.04045) return (float)pt_powd((double)(c + a) / (1.0 + (double)a), 2.4);
+    return (float)((double)c / 12.92);
+}
+static float lab_f(float t) {
+    const float lim = (float)pt_powd((double)(float)(6.0 / 29.0), 3.0);
+    if (t > lim) return (float)pt_powd((double)t, (double)(float)(1.0 / 3.0));
+    const float sq = (float)pt_powd((double)(float)(29.0 / 6.0), 2.0);
+    return (float)((1.0 / 3.0) * (double)sq * (double)t + (4.0 / 29.0));
+}
+static f4 rgb_to_lab(f4 c) {
+    const float refX = 95.047f, refY = 100.0f, refZ = 108.883f;
+    float rl = 100.0f * lab_clinear(c.x), gl = 100.0f * lab_clinear(c.y), bl = 100.0f * lab_clinear(c.z);
+    float X = (float)(0.4124 * (double)rl + 0.3576 * (double)gl + 0.1805 * (double)bl);
+    float Y = (float)(0.2126 * (double)rl + 0.7152 * (double)gl + 0.0722 * (double)bl);
+    float Z = (float)(0.0193 * (double)rl + 0.1192 * (double)gl + 0.9505 * (double)bl);
+    float fy = lab_f(Y / refY);
+    f4 o;
+    o.x = (116.f * fy - 16.0f) / 100.f;
+    o.y = (500.f * (lab_f(X / refX) - fy) + 100.0f) / 200.f;
+    o.z = (200.f * (fy - lab_f(Z / refZ)) + 100.0f) / 200.f;
+    o.w = c.w;
+    return o;
+}
+float pto_rgb_to_lab(const float* in, float* out) {
+    f4 c = {in[0], in[1], in[2], in[3]};
+    f4 o = rgb_to_lab(c);
+    out[0] = o.x; out[1] = o.y; out[2] = o.z; out[3] = o.w;
+    return o.x;
+}
+double pto_powd(double x, double y) { return pt_powd(x, y); }
+
 /* asin on [0, 1/2] by its Taylor series (12 terms). */
 static float pt_asin_small(float x) {
     static const double c[12] = {
@@ -518,6 +584,10 @@ static float time_derivative(const pto* o, int dir, const pt_patchxf* prev, f2 p
     new_coord((float)i, (float)j, prev->x, prev->y, pb0, pb1, &px, &py);
     f4 peb, peo;
     ex_sample2(o, px, py, prev->layer, &peb, &peo);
+    if (o->p.colorspace == 1) { /* :454-459 */
+        pbase = rgb_to_lab(pbase); pout = rgb_to_lab(pout);
+        peb = rgb_to_lab(peb); peo = rgb_to_lab(peo);
+    }
     float r = ssd(sub4(base, pbase), sub4(tb, peb)) * o->p.timeDerivativeInputWeight;
     r = fmaf(ssd(sub4(canvas, pout), sub4(to, peo)), o->p.timeDerivativeOutputWeight, r);
     r = fmaf(ssd(pout, to), o->p.temporalCoherenceWeight, r);
@@ -567,12 +637,14 @@ static float energy_f32(const pto* o, int x, int y, int level, const pt_patchxf*
             size_t k = (size_t)(y + j) * o->W + (x + i);
             f4 base = o->img_base[o->cur][k];
             f4 canvas = o->canvas[k];
+            if (P->colorspace == 1) { base = rgb_to_lab(base); canvas = rgb_to_lab(canvas); } /* :575-578 */
             float tx, ty;
             new_coord((float)i, (float)j, t->x, t->y, b0, b1, &tx, &ty);
             if (tx >= (float)hw) tx -= (float)hw; else if (tx < 0) tx += (float)hw;
             if (ty >= (float)hh) ty -= (float)hh; else if (ty < 0) ty += (float)hh;
             f4 tb, to;
             ex_sample2(o, tx, ty, t->layer, &tb, &to);
+            if (P->colorspace == 1) { tb = rgb_to_lab(tb); to = rgb_to_lab(to); } /* :603-606 */
             float res = ssd_a(base, tb, P->alphaWeight) * P->inputAnalogyWeight;
             if (pc->temporalF && o->adv_off[0][k].hysteresis > 0)
                 res = res + time_derivative(o, 0, &pc->prevF, pc->fb0, pc->fb1, base, tb, canvas, to, x, y, i, j);

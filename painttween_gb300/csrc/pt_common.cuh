@@ -145,6 +145,12 @@ static __device__ float time_derivative(const Params& P, int d, const Patch& pre
     new_coord((float)i, (float)j, prev.x, prev.y, pb0, pb1, &px, &py);
     float4 peb, peo;
     ex_sample2(P.ex, px, py, prev.layer, &peb, &peo);
+    if (P.colorspace == 1) {  // :454-459
+        pbase = rgb_to_lab(pbase);
+        pout = rgb_to_lab(pout);
+        peb = rgb_to_lab(peb);
+        peo = rgb_to_lab(peo);
+    }
     float r = ssd(sub4(base, pbase), sub4(tb, peb)) * P.tdIn;
     r = fmaf(ssd(sub4(canvas, pout), sub4(to, peo)), P.tdOut, r);
     r = fmaf(ssd(pout, to), P.tc, r);
@@ -196,12 +202,20 @@ static __device__ float energy(const Params& P, int x, int y, const Patch& t, co
             size_t k = (size_t)(y + j) * P.W + (x + i);
             float4 base = __ldg(imgb + (size_t)(y + j) * imgw + (x + i));
             float4 canvas = __ldg(P.canvas + k);
+            if (P.colorspace == 1) {  // :575-578
+                base = rgb_to_lab(base);
+                canvas = rgb_to_lab(canvas);
+            }
             float tx, ty;
             new_coord((float)i, (float)j, t.x, t.y, b0, b1, &tx, &ty);
             if (tx >= hw) tx -= hw; else if (tx < 0) tx += hw;
             if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
             float4 tb, to;
             ex_sample2(P.ex, tx, ty, t.layer, &tb, &to);
+            if (P.colorspace == 1) {  // :603-606
+                tb = rgb_to_lab(tb);
+                to = rgb_to_lab(to);
+            }
             float res = ssd_a(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
             if (pc.temporalF && __ldg(&P.adv[0].off.B[k].x) > 0)
                 res = res + time_derivative(P, 0, pc.prevF, pc.fb0, pc.fb1, base, tb, canvas, to, k, i, j);

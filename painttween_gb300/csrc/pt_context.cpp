@@ -373,6 +373,7 @@ static Params make_params(pt_ctx* c, int level) {
     P.distTransCull = p.distTransCull;
     P.direction = p.direction;
     P.scatterSamples = p.scatterSamplesCount;
+    P.colorspace = p.colorspace;
     P.firstKey = p.firstKeyIndex;
     P.lastKey = p.lastKeyIndex;
     P.rngMode = p.rngMode;
@@ -565,7 +566,8 @@ static int temporal_mode(pt_ctx* c) {
 // whether the tiled kernels cover the current configuration
 static bool tiled_usable(pt_ctx* c) {
     int r = c->params.residualWindowSize;
-    return c->use_tiled && !c->params.interpolateKeyFrame && c->params.coherenceWeight <= 0.f &&
+    return c->use_tiled && !c->params.interpolateKeyFrame && c->params.colorspace == 0 &&
+           c->params.coherenceWeight <= 0.f &&
            temporal_mode(c) >= 0 && r >= 2 && r <= 4;
 }
 
@@ -794,7 +796,7 @@ pt_status pt_set_params(pt_ctx* c, const pt_params* p) {
     if (p->residualWindowSize < 0 || p->residualWindowSize > ptk::kMaxRadius)
         return fail(c, PT_ERR_INVALID, "residualWindowSize %d outside [0, %d]", p->residualWindowSize,
                     ptk::kMaxRadius);
-    if (p->colorspace != 0) return fail(c, PT_ERR_UNSUPPORTED, "only the RGB colour space is implemented");
+    if (p->colorspace != 0 && p->colorspace != 1) return fail(c, PT_ERR_INVALID, "colorspace must be 0 (RGB) or 1 (Lab)");
     if (p->numStyles < 1 || p->numStyles > PT_MAX_STYLES) return fail(c, PT_ERR_INVALID, "numStyles out of range");
     if (p->rngMode != PT_RNG_REFERENCE && p->rngMode != PT_RNG_COUNTER)
         return fail(c, PT_ERR_INVALID, "unknown rngMode");

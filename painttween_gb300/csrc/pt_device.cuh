@@ -94,6 +94,61 @@ __device__ __forceinline__ float atan2_poly(float y, float x) {
 }
 
 // log(x) = e ln2 + 2 atanh((m-1)/(m+1)), m in [sqrt(1/2), sqrt(2)).
+// double log, exp and pow for the Lab conversion (the oracle restates the
+// same steps): log by frexp to m in [sqrt(1/2), sqrt(2)) and the atanh
+// series to s^23, exp by k = rint(y/ln2) with a two-part ln2 and the Taylor
+// series to r^22, pow(x, y) = exp(y log x) for x > 0
+static __device__ __noinline__ double log_d(double x) {
+    int e;
+    double m = frexp(x, &e);
+    if (m < 0.70710678118654752440) {
+        m = m * 2.0;
+        e -= 1;
+    }
+    const double s = (m - 1.0) / (m + 1.0);
+    const double s2 = s * s;
+    double p = 1.0 / 23.0;
+    for (int k = 21; k >= 3; k -= 2) p = fma(s2, p, 1.0 / (double)k);
+    p = p * s2;
+    const double lm = 2.0 * fma(s, p, s);
+    const double fe = (double)e;
+    return fma(fe, 6.93147180369123816490e-01, fma(fe, 1.90821492927058770002e-10, lm));
+}
+static __device__ __noinline__ double exp_d(double y) {
+    const double k = rint(y * 1.44269504088896338700);
+    double r = fma(-k, 6.93147180369123816490e-01, y);
+    r = fma(-k, 1.90821492927058770002e-10, r);
+    double p = 1.0;
+    for (int n = 22; n >= 1; n--) p = fma(r / (double)n, p, 1.0);
+    return ldexp(p, (int)k);
+}
+__device__ __forceinline__ double pow_d(double x, double y) {
+    if (!(x > 0.0)) return (x == 0.0) ? 0.0 : __longlong_as_double(0x7ff8000000000000LL);
+    return exp_d(y * log_d(x));
+}
+// RGBtoLAB with Clinear and f_Lab (texSynth_util.h:175-192,220-246)
+__device__ __forceinline__ float lab_clinear(float c) {
+    const float a = 0.055f;
+    if ((double)c > 0.04045) return (float)pow_d((double)(c + a) / (1.0 + (double)a), 2.4);
+    return (float)((double)c / 12.92);
+}
+__device__ __forceinline__ float lab_f(float t) {
+    const float lim = (float)pow_d((double)(float)(6.0 / 29.0), 3.0);
+    if (t > lim) return (float)pow_d((double)t, (double)(float)(1.0 / 3.0));
+    const float sq = (float)pow_d((double)(float)(29.0 / 6.0), 2.0);
+    return (float)((1.0 / 3.0) * (double)sq * (double)t + (4.0 / 29.0));
+}
+static __device__ __noinline__ float4 rgb_to_lab(float4 c) {
+    const float refX = 95.047f, refY = 100.0f, refZ = 108.883f;
+    const float rl = 100.0f * lab_clinear(c.x), gl = 100.0f * lab_clinear(c.y), bl = 100.0f * lab_clinear(c.z);
+    const float X = (float)(0.4124 * (double)rl + 0.3576 * (double)gl + 0.1805 * (double)bl);
+    const float Y = (float)(0.2126 * (double)rl + 0.7152 * (double)gl + 0.0722 * (double)bl);
+    const float Z = (float)(0.0193 * (double)rl + 0.1192 * (double)gl + 0.9505 * (double)bl);
+    const float fy = lab_f(Y / refY);
+    return make_float4((116.f * fy - 16.0f) / 100.f, (500.f * (lab_f(X / refX) - fy) + 100.0f) / 200.f,
+                       (200.f * (fy - lab_f(Z / refZ)) + 100.0f) / 200.f, c.w);
+}
+
 __device__ __forceinline__ float log_poly(float x) {
     if (!(x > 0.0f)) return (x == 0.0f) ? -INFINITY : NAN;
     if (isinf(x)) return x;

@@ -122,6 +122,7 @@ struct Params {
     int direction;
     int scatterSamples;
     int firstKey, lastKey;     // first and last keyframe layer (keyframe interpolation)
+    int colorspace;            // 1: the energy compares Lab colours
     int rngMode;
     uint32_t rngSeed;
     int histW, histH;          // histogram level size (style w, style h * ns) >> level

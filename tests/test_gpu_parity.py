@@ -334,7 +334,7 @@ def test_errors_are_status_codes():
     with pytest.raises(PaintTweenError):
         t.upload_image_color4(0, _abi.LAYER_INPUT_COLOR, np.zeros((10, 10, 4), np.float32))
     p = config_params()
-    p.colorspace = 1  # Lab
+    p.colorspace = 2  # neither RGB nor Lab
     with pytest.raises(PaintTweenError):
         t.set_params(p)
     t.close()
@@ -573,3 +573,21 @@ def test_final_level_upsampled_to_full_size_matches_oracle():
         assert got[f][0].shape == (64, 80, 4)
         assert_offsets_equal(got[f][1], ref[f][0], 1.0, "frame %d" % f)
         assert_array_equal(got[f][0], ref[f][2], "output frame %d" % f)
+
+
+@pytest.mark.parametrize("scheme", [_abi.S_FMBM_RM, _abi.S_FMBM])
+def test_lab_colour_space_matches_oracle(scheme):
+    """colorspace 1: every colour the energy compares converted by RGBtoLAB
+    (texSynth_kernel.cu:454-459,575-578,603-606) with the shared double pow,
+    over an animation with temporal terms."""
+    p = config_params(r=2, levels=2, iterations=2)
+    p.colorspace = 1
+    p.scheme = scheme
+    p.temporalCoherenceWeight = 0.5
+    ex = synthetic.make_exemplar(32, 32, seed=91)
+    clip = synthetic.make_clip(40, 32, 3, 2, seed=92)
+    got = _animate(p, ex, clip, 40, 32)
+    ref = O.OracleDriver(p, [ex], clip, threads=8).render(0, 1)
+    for f in range(2):
+        assert_offsets_equal(got[f][1], ref[f][0], 1.0, "Lab frame %d" % f)
+        assert_array_equal(got[f][0], ref[f][2], "Lab output frame %d" % f)

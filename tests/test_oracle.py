@@ -200,3 +200,22 @@ def test_output_level_of_each_scheme(scheme, final_level, full):
         offs, res, rgba = out[f]
         assert offs.shape == (48 >> lv, 64 >> lv) and rgba.shape == (48 >> lv, 64 >> lv, 4)
         assert np.isfinite(rgba).all()
+
+
+def test_lab_conversion_against_float64_formula():
+    """RGBtoLAB (texSynth_util.h:175-246) with the shared double pow, against
+    the same formula in numpy float64: within 2e-6 absolute."""
+    rng = np.random.default_rng(21)
+    for x, y in zip(rng.uniform(1e-3, 4.0, 200), rng.uniform(0.1, 3.0, 200)):
+        got = O.lib().pto_powd(float(x), float(y))
+        assert abs(got - x ** y) <= 1e-13 * x ** y
+    cols = np.concatenate([rng.random((300, 4)), [[0, 0, 0, 1], [1, 1, 1, 0.5], [0.04, 0.5, 0.9, 1]]])
+    for c in cols.astype(np.float32):
+        lin = np.where(c[:3] > 0.04045, ((c[:3].astype(np.float64) + 0.055) / 1.055) ** 2.4, c[:3] / 12.92) * 100
+        X = 0.4124 * lin[0] + 0.3576 * lin[1] + 0.1805 * lin[2]
+        Y = 0.2126 * lin[0] + 0.7152 * lin[1] + 0.0722 * lin[2]
+        Z = 0.0193 * lin[0] + 0.1192 * lin[1] + 0.9505 * lin[2]
+        f = lambda t: t ** (1 / 3) if t > (6 / 29) ** 3 else t / 3 * (29 / 6) ** 2 + 4 / 29
+        ref = [(116 * f(Y / 100) - 16) / 100, (500 * (f(X / 95.047) - f(Y / 100)) + 100) / 200,
+               (200 * (f(Y / 100) - f(Z / 108.883)) + 100) / 200, c[3]]
+        assert np.allclose(O.rgb_to_lab(c), ref, atol=2e-6, rtol=0), c
