@@ -70,8 +70,7 @@ typedef struct {
 /* Pass direction (types.h:122-126). */
 enum { PT_FORWARD = 0, PT_BACKWARD = 1, PT_BIDIRECTIONAL = 2 };
 
-/* Synthesis schemes (types.h:128-134); all five are implemented (TCTF
- * without ribbon inputs: time step 1). */
+/* Synthesis schemes (types.h:128-134); all five are implemented. */
 enum { PT_S_FMBM = 0, PT_S_FMBM_RM = 1, PT_S_FBMO = 2, PT_S_TCTF = 3, PT_S_IND = 4 };
 
 /* Random-number mode.
@@ -357,6 +356,13 @@ pt_status pt_set_frame(pt_ctx* ctx, int frame, int w, int h,
                        const float* dist_trans, const int32_t* object_ids,
                        const float* vel_fwd, const float* vel_bwd,
                        const float* scale);
+/* Ribbon inputs of one frame (the shot's IN_RIBBON_F/B elements,
+ * GUI/nlShot.cpp:160-190, nlDataAccess.cpp:160-210): velocities to the frame
+ * `step` frames later (vel_fwd) and earlier (vel_bwd), step = 2, 4, 8 ...
+ * TCTF runs over time steps up to the longest step every frame of the range
+ * has; keyframe preprocessing accumulates ribbons over them. */
+pt_status pt_set_frame_ribbons(pt_ctx* ctx, int frame, int step, int w, int h, const float* vel_fwd,
+                               const float* vel_bwd);
 pt_status pt_clear_frames(pt_ctx* ctx);
 
 /* Level of the final output (copyOutputToFinal, synthesisProcessor.cpp:
@@ -378,8 +384,8 @@ typedef void (*pt_frame_callback)(int frame, const float* rgba,
                                   void* user);
 /* Synthesises frames first..last (all uploaded with pt_set_frame) with the
  * scheme of pt_params.scheme: FMBM(_RM) forward/backward consecutive passes
- * (synthesisProcessor.cpp:703-753,846-878), FBMO (:880-1022), TCTF without
- * ribbon inputs (time step 1, :1047-1312) or IND (:807-844). */
+ * (synthesisProcessor.cpp:703-753,846-878), FBMO (:880-1022), TCTF
+ * (:1047-1312, time steps from pt_set_frame_ribbons) or IND (:807-844). */
 pt_status pt_synthesize_animation(pt_ctx* ctx, int first, int last,
                                   pt_frame_callback cb, void* user);
 

@@ -455,6 +455,7 @@ class OracleDriver:
         self.keyed = False
         self.f2k = ({}, {})   # frame -> frame-to-key ribbon pyramid, [0] backward, [1] forward
         self.k2k = ({}, {})   # key full index -> key-to-key ribbon pyramid
+        self.ribbons = {}     # (frame, step) -> velocities over `step` frames
 
     def _update_parameters(self, frame, direction):
         """SynthesisFrame::updateParameters, synthesisFrame.cpp:522-542."""
@@ -502,7 +503,7 @@ class OracleDriver:
             if itr < iterations - 1:
                 self.o.scatter(level, key)
 
-    def synthesize_consecutive(self, frame, level, pass_, is_first, forwards, source_pass, first_pass):
+    def synthesize_consecutive(self, frame, level, pass_, is_first, forwards, source_pass, first_pass, time_step=1):
         o = self.o
         self._update_parameters(frame, _abi.FORWARD if forwards else _abi.BACKWARD)
         rm = self.user.scheme == _abi.S_FMBM_RM
@@ -521,11 +522,11 @@ class OracleDriver:
                     o.upsample(level)
                     o.sync(level)
             if not is_first and coarsest:
-                o.advect(level, 1, forwards, ops)
+                o.advect(level, time_step, forwards, ops)
                 # copyBaseToWorking
                 self._copy_base_to_working(level)
             elif not is_first:
-                o.advect(level, 1, forwards, ops | _abi.ADVECT_IGNORE_RANDOM)
+                o.advect(level, time_step, forwards, ops | _abi.ADVECT_IGNORE_RANDOM)
                 self._load_offsets(level + 1, frame, source_pass)
                 self._load_residual(level + 1, frame, source_pass)
                 o.upsample(level)
@@ -535,7 +536,7 @@ class OracleDriver:
                 else:
                     o.merge_using_residual(level, forwards)
         else:
-            o.advect(level, 1, forwards, ops | _abi.ADVECT_IGNORE_RANDOM)
+            o.advect(level, time_step, forwards, ops | _abi.ADVECT_IGNORE_RANDOM)
             self._load_offsets(level, frame, pass_ - 1)
             self._load_residual(level, frame, pass_ - 1)
             o.sync(level, _abi.DONT_COPY_OFFSETS | _abi.DONT_UPDATE_RESIDUAL)
@@ -647,7 +648,7 @@ class OracleDriver:
 
     def _accumulate(self, forwards, sfirst, slast):
         """SynthesisProcessor::accumulateRibbon, synthesisProcessor.cpp:528-627
-        (level 0; one-frame steps, no ribbon inputs)."""
+        (level 0; steps above one frame through the ribbon inputs)."""
         o = self.o
         d = 0 if forwards else 1
         fk, lk = self.key_sub[0], self.key_sub[-1]
@@ -659,23 +660,34 @@ class OracleDriver:
         o.load_ribbon_field(0, acc[frames[0]])
         for f in blank:
             self.f2k[d][f] = self._ribbon_pyramid(acc[frames[0]], len(self.frames[f]["orient"]))
+        def vel(f, step, key):
+            if step == 1:
+                return self.frames[f][key][0]
+            r = self.ribbons.get((f, step))
+            return None if r is None else r[key][0]
+
         for f in frames:
             fp = self.frames[f]
             o.load_images(fp, 0)
             ts = -1 if forwards else 1
-            pf = f + ts
-            if (forwards and pf >= fk) or (not forwards and pf <= lk):
-                pp = self.frames[pf]
+            while (forwards and f + ts >= fk) or (not forwards and f + ts <= lk):
+                pf, step = f + ts, abs(ts)
+                ahead = pf < f
+                vc = vel(f, step, "velb" if ahead else "velf")
+                vp = vel(pf, step, "velf" if ahead else "velb")
+                if vc is None or vp is None:
+                    break  # loadRibbonPair finds no ribbon of this step
                 L = lib()
                 w, h = self.W, self.H
-                if pf < f:
-                    L.pto_upload_layered(o.h, _abi.LAYER_INPUT_VEL_B, _p(_c(fp["velb"][0], np.float32)), w, h)
-                    L.pto_upload_layered(o.h, _abi.LAYER_INPUT_VEL_F_PREVIOUS, _p(_c(pp["velf"][0], np.float32)), w, h)
+                if ahead:
+                    L.pto_upload_layered(o.h, _abi.LAYER_INPUT_VEL_B, _p(_c(vc, np.float32)), w, h)
+                    L.pto_upload_layered(o.h, _abi.LAYER_INPUT_VEL_F_PREVIOUS, _p(_c(vp, np.float32)), w, h)
                 else:
-                    L.pto_upload_layered(o.h, _abi.LAYER_INPUT_VEL_F, _p(_c(fp["velf"][0], np.float32)), w, h)
-                    L.pto_upload_layered(o.h, _abi.LAYER_INPUT_VEL_B_PREVIOUS, _p(_c(pp["velb"][0], np.float32)), w, h)
+                    L.pto_upload_layered(o.h, _abi.LAYER_INPUT_VEL_F, _p(_c(vc, np.float32)), w, h)
+                    L.pto_upload_layered(o.h, _abi.LAYER_INPUT_VEL_B_PREVIOUS, _p(_c(vp, np.float32)), w, h)
                 o.load_ribbon_field(0, acc[pf])
-                o.accumulate_ribbon_field(0, forwards, ts, True)
+                o.accumulate_ribbon_field(0, forwards, ts, step == 1)
+                ts *= 2
             acc[f] = o.get_ribbon_field(0)
             k = self._key_sub_index(f)
             if k >= 0:
@@ -686,16 +698,42 @@ class OracleDriver:
                 o.load_ribbon_field(0, acc[f])
             self.f2k[d][f] = self._ribbon_pyramid(acc[f], len(fp["orient"]))
 
-    def _frame(self, f, level):
+    def set_frame_ribbons(self, frame, step, vel_fwd, vel_bwd):
+        """Velocities over `step` frames (pt_set_frame_ribbons)."""
+        self.ribbons[(frame, step)] = dict(velf=pyramid_avg(vel_fwd, vel=True), velb=pyramid_avg(vel_bwd, vel=True))
+
+    def _stepped(self, f, ts):
+        """The frame's inputs with the velocities of time step ts
+        (loadAnimImages, synthesisFrame.cpp:583-611)."""
+        fp = self.frames[f]
+        if ts == 1:
+            return fp
+        r = self.ribbons[(f, ts)]
+        return dict(fp, velf=r["velf"], velb=r["velb"])
+
+    def _max_ribbon_step(self, first, last):
+        step = 1
+        while all((f, step * 2) in self.ribbons for f in range(first, last + 1)):
+            step *= 2
+        return step
+
+    def _frame(self, f, level, ts=1):
         """loadImages + loadAnimImages (with keys: the frame-to-key ribbons)."""
-        self.o.load_frame_level(self.frames[f], level)
+        self.o.load_frame_level(self._stepped(f, ts), level)
         if self.keyed:
             self._bind_frame_keys(f, level)
 
-    def _anim(self, f, level):
-        self.o.load_anim_images(self.frames[f], level)
+    def _anim(self, f, level, ts=1):
+        self.o.load_anim_images(self._stepped(f, ts), level)
         if self.keyed:
             self._bind_frame_keys(f, level)
+
+    def _link(self, frame, level, this_pass):
+        """linkTempImagesToNextPass through linkImagesToPass (workingBuffers.cpp:
+        329-365): this pass becomes the frame's last saved pass."""
+        src = (level, frame, self.last_saved.get((frame, level), 0))
+        if src in self.store and src[2] != this_pass:
+            self.store[(level, frame, this_pass)] = self.store[src]
 
     def _bind_frame_keys(self, frame, level):
         for d in (0, 1):
@@ -743,30 +781,30 @@ class OracleDriver:
             self.user = user
             self.keyed = False
 
-    def _advect_neighbors(self, frame, level, source_pass, first, last, neighbours=True):
+    def _advect_neighbors(self, frame, level, source_pass, first, last, neighbours=True, ts=1):
         """SynthesisFrame::advectNeighbors, synthesisFrame.cpp:325-382, with
         the frames of the synthesised range as neighbours (with keys, a side
         without one advects the frame-to-key ribbons)."""
         o, u = self.o, self.user
         o.reset_advected()
         ops = _abi.ADVECT_CHECK_FRAME_TO_KEY if self.keyed else 0
-        prior = frame - 1 if neighbours and frame - 1 >= first else None
-        nxt = frame + 1 if neighbours and frame + 1 <= last else None
+        prior = frame - ts if neighbours and frame - ts >= first else None
+        nxt = frame + ts if neighbours and frame + ts <= last else None
         temporal = (u.timeDerivativeInputWeight > 0 or u.timeDerivativeOutputWeight > 0
                     or u.temporalCoherenceWeight > 0)
         if last == first or not temporal or (prior is None and nxt is None and not self.keyed):
-            self._anim(frame, level)
+            self._anim(frame, level, ts)
             return
         for nb, fwd in ((prior, True), (nxt, False)):
             if nb is not None and source_pass >= 0:
-                self._frame(nb, level)
+                self._frame(nb, level, ts)
                 o.flip()
-                self._anim(frame, level)
+                self._anim(frame, level, ts)
                 self._load_last_saved(nb, level)
-                o.advect(level, 1, fwd, ops)
+                o.advect(level, ts, fwd, ops)
             elif self.keyed:
-                self._anim(frame, level)
-                o.advect(level, 1, fwd, ops | _abi.ADVECT_DO_NOT_CHECK_PREVIOUS)
+                self._anim(frame, level, ts)
+                o.advect(level, ts, fwd, ops | _abi.ADVECT_DO_NOT_CHECK_PREVIOUS)
 
     def synthesize_interpolated(self, frame, level, this_pass, source_pass, first, last):
         """SynthesisFrame::synthesizeInterpolated, synthesisFrame.cpp:384-418."""
@@ -868,22 +906,30 @@ class OracleDriver:
         if save:
             self._save_images(fine, frame, 0)
 
-    def _refine_pass(self, level, last_coarse_pass, this_pass, first, last, initialize=False):
-        """renderRefinePass (REFINE_EVEN_AND_ODD), synthesisProcessor.cpp:
-        1078-1150, and SynthesisFrame::refine, synthesisFrame.cpp:420-463;
-        `initialize`: renderInitializationPass (:1047-1076), the frames
-        without neighbours, merged from the advected buffers at the coarsest
-        level."""
+    def _refine_pass(self, level, last_coarse_pass, this_pass, first, last, op="even_and_odd", ts=1):
+        """renderRefinePass (synthesisProcessor.cpp:1078-1150) and
+        renderInitializationPass (:1047-1076, op "initialize") with
+        SynthesisFrame::refine (synthesisFrame.cpp:420-463)."""
         o = self.o
         coarsest = level == self.levels - 1
-        temporal_up = initialize and coarsest
-        spatial = (not coarsest) if initialize else last_coarse_pass == this_pass - 1
-        for f in range(first, last + 1):
+        coarse_step = 2 * ts
+        if op == "odd":
+            frames = range(first + ts, last + 1, coarse_step)
+        elif op == "even":
+            frames = range(first, last + 1, coarse_step)
+        else:
+            frames = range(first, last + 1, ts)
+        init = "previous"
+        if op in ("initialize", "odd"):
+            init = "temporal" if coarsest else "spatial"
+        elif op == "even_and_odd" and last_coarse_pass == this_pass - 1:
+            init = "spatial"
+        for f in frames:
             self._update_parameters(f, _abi.BIDIRECTIONAL)
-            self._advect_neighbors(f, level, this_pass - 1, first, last, not initialize)
-            if temporal_up:
+            self._advect_neighbors(f, level, this_pass - 1, first, last, op != "initialize", ts)
+            if init == "temporal":
                 o.merge_advected_buffers(level, _abi.MERGE_FALLBACK_RANDOM)
-            elif spatial:
+            elif init == "spatial":
                 self._spatial_upsample(f, level + 1, level, False)
             else:
                 self._load_last_saved(f, level)
@@ -891,21 +937,36 @@ class OracleDriver:
             o.load_images(self.frames[f], level)
             self.propagate_and_scatter(level, self.user.iterations, self._key_full(f) if self.keyed else -1)
             self._save_images(level, f, this_pass)
+        if op == "odd":
+            for f in range(first, last + 1, coarse_step):
+                self._link(f, level, this_pass)
+        elif op == "even":
+            for f in range(first + ts, last + 1, coarse_step):
+                self._link(f, level, this_pass)
 
     def _render_tctf(self, first, last):
-        """renderAnimationTCTF, synthesisProcessor.cpp:1152-1312, run locally
-        without ribbon inputs (time step 1)."""
+        """renderAnimationTCTF, synthesisProcessor.cpp:1152-1312, run locally,
+        over the longest ribbon step every frame has."""
         u = self.user
-        ops = [("initialize" if self.keyed else "consecutive", self.levels - 1)]
-        for level in range(self.levels - 1, u.finalLevel - 1, -1):
-            ops.append(("refine", level))
-            if 1 < last - first:
-                ops += [("refine", level)] * (u.fixupPasses + 1)
-        ops += [("upsample", level) for level in range(u.finalLevel - 1, -1, -1)]
+        L = self.levels - 1
+        T = self._max_ribbon_step(first, last)
+        ops = [("initialize" if self.keyed else "consecutive", L, T)]
+        for level in range(L, u.finalLevel - 1, -1):
+            ops.append(("even_and_odd", level, T))
+            if T < last - first:
+                ops += [("even_and_odd", level, T)] * (u.fixupPasses + 1)
+        ts = T // 2
+        while ts > 0:
+            for level in range(L, u.finalLevel - 1, -1):
+                ops.append(("odd", level, ts))
+                if ts < last - first:
+                    ops += [("even_and_odd", level, ts)] * u.fixupPasses
+            ts //= 2
+        ops += [("upsample", level, 1) for level in range(u.finalLevel - 1, -1, -1)]
         self.o.reset_advected()
         passes_this = passes_last = 0
         last_level = -1
-        for op, level in ops:
+        for op, level, ts in ops:
             if last_level != level:
                 self.o.load_style_level(self.styles, level)
                 if self.keyed:
@@ -913,24 +974,25 @@ class OracleDriver:
                 passes_last = passes_this
                 last_level = level
             if op == "initialize":
-                self._refine_pass(level, passes_this - 1, 0, first, last, initialize=True)
+                self._refine_pass(level, passes_this - 1, 0, first, last, "initialize", ts)
                 passes_this = 1
             elif op == "consecutive":
-                self._render_pass(level, passes_this, passes_this - 1, first, last)
+                self._render_pass(level, passes_this, passes_this - 1, first, last, ts)
                 passes_this += 1
-            elif op == "refine":
-                self._refine_pass(level, passes_last - 1, passes_this, first, last)
-                passes_this += 1
-            else:
+            elif op == "upsample":
                 for f in range(first, last + 1):
                     self._spatial_upsample(f, level + 1, level, True)
                 passes_this = 1
+            else:
+                self._refine_pass(level, passes_last - 1, passes_this, first, last, op, ts)
+                passes_this += 1
         return {f: self.store[(0, f, passes_this - 1)] for f in range(first, last + 1)}
 
-    def _render_pass(self, level, pass_, source_pass, first, last):
+    def _render_pass(self, level, pass_, source_pass, first, last, time_step=1):
         """renderConsecutivePass, synthesisProcessor.cpp:703-753."""
         forwards = (pass_ % 2) == 0
-        frames = list(range(first, last + 1)) if forwards else list(range(last, first - 1, -1))
+        frames = (list(range(first, last + 1, time_step)) if forwards
+                  else list(range(last, first - 1, -time_step)))
         if pass_ > 0:
             self._save(level, frames[0], pass_)
             frames = frames[1:]
@@ -938,6 +1000,6 @@ class OracleDriver:
             is_first = (i == 0) and (pass_ == 0)
             if not is_first:
                 self.o.flip()
-            self._frame(f, level)
-            self.synthesize_consecutive(f, level, pass_, is_first, forwards, source_pass, pass_ == 0)
+            self._frame(f, level, time_step)
+            self.synthesize_consecutive(f, level, pass_, is_first, forwards, source_pass, pass_ == 0, time_step)
 

@@ -52,6 +52,7 @@ SIGNATURES = {
     "pt_offsets_from_frame_to_key_ribbon": (_I, [_VP, _I, _I]),
     "pt_merge_advected_buffers": (_I, [_VP, _I, _I]),
     "pt_set_keyframes": (_I, [_VP, _VP, _I]),
+    "pt_set_frame_ribbons": (_I, [_VP, _I, _I, _I, _I, _VP, _VP]),
     "pt_load_ribbon_field": (_I, [_VP, _I, _VP]),
     "pt_get_ribbon_field": (_I, [_VP, _I, _VP]),
     "pt_load_canvas": (_I, [_VP, _I, _VP]),

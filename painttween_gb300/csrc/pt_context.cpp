@@ -153,6 +153,10 @@ struct pt_ctx {
     std::vector<ExLevel> style_levels;
     std::vector<int> style_set;
     std::map<int, std::vector<FrameLevel>> frames;
+    // ribbon inputs: (frame, time step) -> per level forward and backward
+    // velocities over that many frames (getRibbonF/B, nlDataAccess.cpp:
+    // 160-205); time step 1 is the frame's own velocities
+    std::map<std::pair<int, int>, std::vector<std::pair<float2*, float2*>>> ribbons;
     std::map<std::tuple<int, int, int>, StoreEntry> store;
     // SynthesisFrame::_last_saved_pass: (frame, level) -> last pass saved
     // through saveImages
@@ -496,16 +500,6 @@ static pt_status base_for_partial_write(pt_ctx* c, int level, PatchPlanes* out) 
     *out = c->off[c->base_i];
     return PT_OK;
 }
-// base about to be overwritten on the whole level rectangle
-static pt_status base_for_full_write(pt_ctx* c, int level, PatchPlanes* out) {
-    if (c->base_i == c->work_i) {
-        TRY(split_aliased(c, level));
-        c->base_i = 1 - c->work_i;
-    }
-    c->off_span = std::min(c->off_span, level);
-    *out = c->off[c->base_i];
-    return PT_OK;
-}
 
 // ---------------------------------------------------------------------------
 // syncBuffers and friends
@@ -755,6 +749,11 @@ static void free_frames(pt_ctx* c) {
             dfree_t(c, L.velf); dfree_t(c, L.velb); dfree_t(c, L.scale);
         }
     c->frames.clear();
+    for (auto& kv : c->ribbons)
+        for (auto& L : kv.second) {
+            dfree_t(c, L.first); dfree_t(c, L.second);
+        }
+    c->ribbons.clear();
 }
 static void free_store(pt_ctx* c) {
     for (auto& kv : c->store) {
@@ -1394,10 +1393,14 @@ pt_status pt_advect_offsets(pt_ctx* c, int level, int time_step, int forwards, i
     Params P = make_params(c, level);
     LN(pt::launch_advect(P, d, forwards ? 1 : 0, time_step, flags, c->stream));
     c->adv_written[d] = true;
-    PatchPlanes dst;
-    TRY(base_for_full_write(c, level, &dst));
+    // dest->offsets().copyTo(offsets.base()) copies the whole buffer: outside
+    // the level rectangle the base then holds the advected buffer's texels
+    // (zero after a reset), which propagate's wrap can read before the next
+    // full sync
+    if (c->base_i == c->work_i) c->base_i = 1 - c->work_i;
+    TRY(copy_planes_full(c, c->off[c->base_i], c->adv[d].off));
+    c->off_span = 0;  // the two buffers may now differ anywhere
     P = make_params(c, level);
-    LN(pt::launch_copy_patch(P, dst, c->adv[d].off, c->stream));
     TRY(do_sync(c, level, PT_DONT_COPY_OFFSETS | PT_DONT_UPDATE_RESIDUAL));
     if (flags & PT_ADVECT_UPDATE_RESIDUAL) TRY(do_residual(c, level));
     P = make_params(c, level);
@@ -1692,6 +1695,37 @@ pt_status pt_set_frame(pt_ctx* c, int frame, int w, int h, const float* rgba, co
     return PT_OK;
 }
 
+// Ribbon inputs of time step `step` (2, 4, 8 ...): the velocities from the
+// frame to the frame `step` later (vel_fwd) and earlier (vel_bwd), pyramids
+// built as the velocities' (DOWNSAMPLE_SCALE_WITH_LEVELS)
+pt_status pt_set_frame_ribbons(pt_ctx* c, int frame, int step, int w, int h, const float* vel_fwd,
+                               const float* vel_bwd) {
+    if (!c || !vel_fwd || !vel_bwd) return PT_ERR_INVALID;
+    if (!c->initialized) return fail(c, PT_ERR_STATE, "pt_initialize has not been called");
+    if (w != c->W || h != c->H) return fail(c, PT_ERR_INVALID, "ribbons %dx%d differ from image size", w, h);
+    if (step < 2 || (step & (step - 1))) return fail(c, PT_ERR_INVALID, "ribbon step %d is not a power of two > 1", step);
+    const auto key = std::make_pair(frame, step);
+    auto it = c->ribbons.find(key);
+    if (it != c->ribbons.end()) {
+        for (auto& L : it->second) {
+            dfree_t(c, L.first); dfree_t(c, L.second);
+        }
+        c->ribbons.erase(it);
+    }
+    const int nlev = level_count(w, h);
+    const size_t n0 = (size_t)w * h;
+    float *vf0, *vb0;
+    TRY(upload_or_fill(c, &vf0, vel_fwd, n0, 2, 0.f));
+    TRY(upload_or_fill(c, &vb0, vel_bwd, n0, 2, 0.f));
+    std::vector<float*> pvf, pvb;
+    TRY(build_avg(c, vf0, w, h, 2, 1, nlev, pvf));
+    TRY(build_avg(c, vb0, w, h, 2, 1, nlev, pvb));
+    std::vector<std::pair<float2*, float2*>> lv(nlev);
+    for (int l = 0; l < nlev; l++) lv[l] = std::make_pair((float2*)pvf[l], (float2*)pvb[l]);
+    c->ribbons[key] = std::move(lv);
+    return PT_OK;
+}
+
 pt_status pt_clear_frames(pt_ctx* c) {
     if (!c) return PT_ERR_INVALID;
     CU(cudaStreamSynchronize(c->stream));
@@ -1812,9 +1846,18 @@ static pt_status bind_frame_images(pt_ctx* c, int frame, int level) {
 }
 // SynthesisFrame::loadAnimImages, synthesisFrame.cpp:583-656: velocities and
 // distance transform into the current layer, scale
-static pt_status bind_frame_anim(pt_ctx* c, int frame, int level) {
-    const FrameLevel* L;
-    TRY(frame_level(c, frame, level, &L));
+static pt_status bind_frame_anim(pt_ctx* c, int frame, int level, int time_step = 1) {
+    const FrameLevel* L0;
+    TRY(frame_level(c, frame, level, &L0));
+    FrameLevel Ls = *L0;  // loadAnimImages with time_step > 1 takes the ribbons of that step
+    if (time_step > 1) {
+        auto it = c->ribbons.find(std::make_pair(frame, time_step));
+        if (it == c->ribbons.end() || level >= (int)it->second.size())
+            return fail(c, PT_ERR_STATE, "frame %d has no ribbons of step %d", frame, time_step);
+        Ls.velf = it->second[level].first;
+        Ls.velb = it->second[level].second;
+    }
+    const FrameLevel* L = &Ls;
     int cur = c->img.cur;
     if (c->slot_copy) {
         const cudaMemcpyKind d2d = cudaMemcpyDeviceToDevice;
@@ -1830,9 +1873,9 @@ static pt_status bind_frame_anim(pt_ctx* c, int frame, int level) {
     if (c->keyed) bind_frame_keys(c, frame, level);
     return PT_OK;
 }
-static pt_status bind_frame_level(pt_ctx* c, int frame, int level) {
+static pt_status bind_frame_level(pt_ctx* c, int frame, int level, int time_step = 1) {
     TRY(bind_frame_images(c, frame, level));
-    return bind_frame_anim(c, frame, level);
+    return bind_frame_anim(c, frame, level, time_step);
 }
 
 static pt_status store_save(pt_ctx* c, int level, int frame, int pass, bool with_canvas) {
@@ -2021,7 +2064,7 @@ static pt_status random_level_keyed(pt_ctx* c, int level, int frame, Arr<float4>
 
 static pt_status synthesize_consecutive(pt_ctx* c, const pt_params& user, int frame, int level, int pass,
                                         bool is_first, bool forwards, int source_pass, bool first_pass,
-                                        bool save_canvas) {
+                                        bool save_canvas, int time_step = 1) {
     pt_params p = user;  // SynthesisFrame::updateParameters, :522-542
     p.advectionJitter = (frame % 3 == 0) ? user.advectionJitter * 0.01f : 0.0f;
     p.direction = forwards ? PT_FORWARD : PT_BACKWARD;
@@ -2045,10 +2088,10 @@ static pt_status synthesize_consecutive(pt_ctx* c, const pt_params& user, int fr
             }
         }
         if (!is_first && coarsest) {
-            TRY(pt_advect_offsets(c, level, 1, forwards, ops));
+            TRY(pt_advect_offsets(c, level, time_step, forwards, ops));
             c->work_i = c->base_i;  // copyBaseToWorking
         } else if (!is_first) {
-            TRY(pt_advect_offsets(c, level, 1, forwards, ops | PT_ADVECT_IGNORE_RANDOM));
+            TRY(pt_advect_offsets(c, level, time_step, forwards, ops | PT_ADVECT_IGNORE_RANDOM));
             TRY(store_load_offsets(c, level + 1, frame, source_pass));
             TRY(store_load_residual(c, level + 1, frame, source_pass));
             TRY(pt_upsample(c, level));
@@ -2057,7 +2100,7 @@ static pt_status synthesize_consecutive(pt_ctx* c, const pt_params& user, int fr
             else TRY(pt_merge_using_residual(c, level, forwards));
         }
     } else {
-        TRY(pt_advect_offsets(c, level, 1, forwards, ops | PT_ADVECT_IGNORE_RANDOM));
+        TRY(pt_advect_offsets(c, level, time_step, forwards, ops | PT_ADVECT_IGNORE_RANDOM));
         TRY(store_load_offsets(c, level, frame, pass - 1));
         TRY(store_load_residual(c, level, frame, pass - 1));
         TRY(do_sync(c, level, PT_DONT_COPY_OFFSETS | PT_DONT_UPDATE_RESIDUAL));
@@ -2145,27 +2188,28 @@ pt_status pt_copy_offsets_to_advected(pt_ctx* c, int forwards) {
 // ribbons instead (ADVECT_DO_NOT_CHECK_PREVIOUS).  `neighbours` false: the
 // refine of TCTF's initialisation pass, which is given none.
 static pt_status advect_neighbors(pt_ctx* c, int frame, int level, int source_pass, int first, int last,
-                                  bool neighbours = true) {
+                                  bool neighbours = true, int ts = 1) {
     TRY(pt_reset_advected_buffers(c));
     const pt_params& p = c->params;
     const int ops = c->keyed ? PT_ADVECT_CHECK_FRAME_TO_KEY : 0;
-    const bool has_prior = neighbours && frame - 1 >= first, has_next = neighbours && frame + 1 <= last;
+    const bool has_prior = neighbours && frame - ts >= first, has_next = neighbours && frame + ts <= last;
     const bool temporal = p.timeDerivativeInputWeight > 0.f || p.timeDerivativeOutputWeight > 0.f ||
                           p.temporalCoherenceWeight > 0.f;
-    if (last == first || !temporal || !(has_prior || has_next || c->keyed)) return bind_frame_anim(c, frame, level);
+    if (last == first || !temporal || !(has_prior || has_next || c->keyed))
+        return bind_frame_anim(c, frame, level, ts);
     for (int side = 0; side < 2; side++) {
         const bool fwd = side == 0;
-        const int nb = fwd ? frame - 1 : frame + 1;
+        const int nb = fwd ? frame - ts : frame + ts;
         if ((fwd ? has_prior : has_next) && source_pass >= 0) {
-            TRY(bind_frame_level(c, nb, level));
+            TRY(bind_frame_level(c, nb, level, ts));
             TRY(pt_flip_anim_buffers(c));
-            TRY(bind_frame_anim(c, frame, level));
+            TRY(bind_frame_anim(c, frame, level, ts));
             TRY(load_last_saved_offsets(c, nb, level));
-            TRY(pt_advect_offsets(c, level, 1, fwd ? 1 : 0, ops));
+            TRY(pt_advect_offsets(c, level, ts, fwd ? 1 : 0, ops));
         } else if (c->keyed) {
-            TRY(bind_frame_anim(c, frame, level));
+            TRY(bind_frame_anim(c, frame, level, ts));
             TRY(ensure_random(c));
-            TRY(pt_advect_offsets(c, level, 1, fwd ? 1 : 0, ops | PT_ADVECT_DO_NOT_CHECK_PREVIOUS));
+            TRY(pt_advect_offsets(c, level, ts, fwd ? 1 : 0, ops | PT_ADVECT_DO_NOT_CHECK_PREVIOUS));
         }
     }
     return PT_OK;
@@ -2305,10 +2349,9 @@ static pt_status ribbon_pyramid(pt_ctx* c, const ptk::Ribbon* src, int levels, s
 
 // SynthesisProcessor::accumulateRibbon, synthesisProcessor.cpp:528-627, at
 // level 0: every frame's ribbon to the nearest key behind it in time,
-// carried frame to frame by accumulateRibbonField.  Steps of more than one
-// frame need ribbon inputs (getRibbonB/F), which this library does not take,
-// so each frame accumulates from its neighbour only, as the reference does
-// without ribbon files.  Guides are not built (no kernel reads them).
+// carried by accumulateRibbonField from the frames 1, 2, 4 ... behind it
+// (steps above 1 through the ribbon inputs, as far as they exist).  Guides
+// are not built (no kernel reads them).
 static pt_status accumulate_ribbons(pt_ctx* c, bool forwards, int sfirst, int slast) {
     const int d = forwards ? 0 : 1;
     const int first_key = c->key_sub.front(), last_key = c->key_sub.back();
@@ -2337,25 +2380,34 @@ static pt_status accumulate_ribbons(pt_ctx* c, bool forwards, int sfirst, int sl
     CU(cudaMemcpyAsync(c->rib[0], acc[k0], rb, cudaMemcpyDeviceToDevice, c->stream));
     for (int f : blank) TRY(ribbon_pyramid(c, acc[k0], levels_of(f), &c->f2k_pyr[d][f]));
     const int cur = c->img.cur, prev_slot = 1 - c->img.cur;
+    // level-0 velocities of `f` over `step` frames: its own, or its ribbons
+    auto vel = [&](int f, int step, bool fwd) -> const float2* {
+        if (step == 1) return fwd ? c->frames[f][0].velf : c->frames[f][0].velb;
+        auto it = c->ribbons.find(std::make_pair(f, step));
+        if (it == c->ribbons.end()) return nullptr;
+        return fwd ? it->second[0].first : it->second[0].second;
+    };
     for (int f : frames) {
         TRY(bind_frame_images(c, f, 0));  // loadImages(0)
-        const int ts = forwards ? -1 : 1;
-        const int pf = f + ts;
-        if ((forwards && pf >= first_key) || (!forwards && pf <= last_key)) {
-            // loadRibbonPair(0, f + ts), synthesisFrame.cpp:658-706
-            const FrameLevel *Lc, *Lp;
-            TRY(frame_level(c, f, 0, &Lc));
-            TRY(frame_level(c, pf, 0, &Lp));
+        for (int ts = forwards ? -1 : 1; (forwards && f + ts >= first_key) || (!forwards && f + ts <= last_key);
+             ts *= 2) {
+            // loadRibbonPair(0, f + ts), synthesisFrame.cpp:658-706: steps
+            // above 1 read the ribbon inputs and stop where there are none
+            const int pf = f + ts, step = ts < 0 ? -ts : ts;
             const cudaMemcpyKind d2d = cudaMemcpyDeviceToDevice;
-            if (pf < f) {
-                TRY(slot_write(c, &c->up_velb[cur], &c->img.velb[cur], Lc->velb, Lc->w, Lc->h, d2d));
-                TRY(slot_write(c, &c->up_velf[prev_slot], &c->img.velf[prev_slot], Lp->velf, Lp->w, Lp->h, d2d));
+            const bool ahead = pf < f;
+            const float2* vc = vel(f, step, !ahead);
+            const float2* vp = vel(pf, step, ahead);
+            if (!vc || !vp) break;
+            if (ahead) {
+                TRY(slot_write(c, &c->up_velb[cur], &c->img.velb[cur], vc, c->W, c->H, d2d));
+                TRY(slot_write(c, &c->up_velf[prev_slot], &c->img.velf[prev_slot], vp, c->W, c->H, d2d));
             } else {
-                TRY(slot_write(c, &c->up_velf[cur], &c->img.velf[cur], Lc->velf, Lc->w, Lc->h, d2d));
-                TRY(slot_write(c, &c->up_velb[prev_slot], &c->img.velb[prev_slot], Lp->velb, Lp->w, Lp->h, d2d));
+                TRY(slot_write(c, &c->up_velf[cur], &c->img.velf[cur], vc, c->W, c->H, d2d));
+                TRY(slot_write(c, &c->up_velb[prev_slot], &c->img.velb[prev_slot], vp, c->W, c->H, d2d));
             }
             CU(cudaMemcpyAsync(c->rib[0], acc[pf], rb, cudaMemcpyDeviceToDevice, c->stream));
-            TRY(pt_accumulate_ribbon_field(c, 0, forwards ? 1 : 0, ts, 1));
+            TRY(pt_accumulate_ribbon_field(c, 0, forwards ? 1 : 0, ts, step == 1 ? 1 : 0));
         }
         if (!acc.count(f)) TRY(dalloc_t(c, &acc[f], n));
         CU(cudaMemcpyAsync(acc[f], c->rib[0], rb, cudaMemcpyDeviceToDevice, c->stream));
@@ -2457,11 +2509,11 @@ pt_status pt_set_keyframes(pt_ctx* c, const int32_t* frames, int count) {
 
 // SynthesisProcessor::renderConsecutivePass, synthesisProcessor.cpp:703-753
 static pt_status consecutive_pass(pt_ctx* c, const pt_params& user, int level, int pass, int source_pass, int first,
-                                  int last, bool save_canvas) {
+                                  int last, bool save_canvas, int time_step = 1) {
     const bool forwards = (pass % 2) == 0;
     std::vector<int> fr;
-    if (forwards) for (int f = first; f <= last; f++) fr.push_back(f);
-    else for (int f = last; f >= first; f--) fr.push_back(f);
+    if (forwards) for (int f = first; f <= last; f += time_step) fr.push_back(f);
+    else for (int f = last; f >= first; f -= time_step) fr.push_back(f);
     if (pass > 0) {  // the frame still in memory starts the fix-up pass
         TRY(store_save(c, level, fr[0], pass, save_canvas));
         fr.erase(fr.begin());
@@ -2469,9 +2521,9 @@ static pt_status consecutive_pass(pt_ctx* c, const pt_params& user, int level, i
     for (size_t i = 0; i < fr.size(); i++) {
         const bool is_first = (i == 0) && (pass == 0);
         if (!is_first) TRY(pt_flip_anim_buffers(c));
-        TRY(bind_frame_level(c, fr[i], level));
+        TRY(bind_frame_level(c, fr[i], level, time_step));
         TRY(synthesize_consecutive(c, user, fr[i], level, pass, is_first, forwards, source_pass, pass == 0,
-                                   save_canvas));
+                                   save_canvas, time_step));
     }
     return PT_OK;
 }
@@ -2521,30 +2573,67 @@ static pt_status render_fmbm(pt_ctx* c, int first, int last, bool fresh) {
     return PT_OK;
 }
 
-// SynthesisProcessor::renderRefinePass with REFINE_EVEN_AND_ODD,
-// synthesisProcessor.cpp:1078-1150, and SynthesisFrame::refine,
-// synthesisFrame.cpp:420-463: every frame between its advected neighbours,
-// started from the upsampled coarse level (the level's first refine pass)
-// or from its own last saved pass
-//
-// `initialize`: renderInitializationPass (:1047-1076) with keys, each frame
-// refined as pass 0 without neighbours, from the advected buffers merged
-// (mergeAdvectedBuffers, random fallback) at the coarsest level
+// WorkingBuffers::linkTempImagesToNextPass (workingBuffers.cpp:329-365)
+// through SynthesisFrame::linkImagesToPass: pass `this_pass` of the frame
+// becomes a copy of its last saved pass (the frame's last saved pass stays)
+static pt_status link_to_pass(pt_ctx* c, int frame, int level, int this_pass) {
+    auto ls = c->last_saved.find(std::make_pair(frame, level));
+    const int src = ls == c->last_saved.end() ? 0 : ls->second;
+    auto it = c->store.find(std::make_tuple(level, frame, src));
+    if (it == c->store.end() || src == this_pass) return PT_OK;  // no file to link
+    const StoreEntry S = it->second;
+    StoreEntry& D = c->store[std::make_tuple(level, frame, this_pass)];
+    const size_t n = (size_t)S.w * S.h;
+    if (!D.offs || D.w != S.w || D.h != S.h) {
+        dfree_t(c, D.offs); dfree_t(c, D.res); dfree_t(c, D.canvas);
+        D.canvas = nullptr;
+        TRY(dalloc_t(c, &D.offs, n));
+        TRY(dalloc_t(c, &D.res, n));
+        D.w = S.w;
+        D.h = S.h;
+    }
+    CU(cudaMemcpyAsync(D.offs, S.offs, n * sizeof(pt_patchxf), cudaMemcpyDeviceToDevice, c->stream));
+    CU(cudaMemcpyAsync(D.res, S.res, n * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+    if (S.canvas) {
+        if (!D.canvas) TRY(dalloc_t(c, &D.canvas, n));
+        CU(cudaMemcpyAsync(D.canvas, S.canvas, n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
+    }
+    return PT_OK;
+}
+
+enum RefineOp { REFINE_ODD, REFINE_EVEN, REFINE_EVEN_AND_ODD, INITIALIZE_EVEN_AND_ODD };
+
+// SynthesisProcessor::renderRefinePass (synthesisProcessor.cpp:1078-1150)
+// and renderInitializationPass (:1047-1076) with SynthesisFrame::refine
+// (synthesisFrame.cpp:420-463): the frames of the op (odd multiples of the
+// time step, even ones, or all) each synthesised between its neighbours one
+// time step away, started by temporal upsampling (mergeAdvectedBuffers,
+// random fallback: the odd frames of the coarsest level, and every frame of
+// the keyframe initialisation there), spatial upsampling (the level's
+// first refine, odd frames below the coarsest level) or from its own last
+// saved pass; ODD and EVEN passes link the frames they skip to the new pass
 static pt_status refine_pass(pt_ctx* c, const pt_params& user, int level, int last_coarse_pass, int this_pass,
-                             int first, int last, bool save_canvas, bool initialize = false) {
+                             int first, int last, bool save_canvas, int op = REFINE_EVEN_AND_ODD, int ts = 1) {
     const bool coarsest = level == user.levels - 1;
-    const bool temporal_up = initialize && coarsest;
-    const bool spatial = initialize ? !coarsest : last_coarse_pass == this_pass - 1;
-    for (int f = first; f <= last; f++) {
+    const int coarse_step = ts * 2;
+    std::vector<int> frames;
+    const int start = op == REFINE_ODD ? first + ts : first;
+    const int step = (op == REFINE_ODD || op == REFINE_EVEN) ? coarse_step : ts;
+    for (int f = start; f <= last; f += step) frames.push_back(f);
+    enum { PREVIOUS, SPATIAL, TEMPORAL } init = PREVIOUS;
+    if (op == INITIALIZE_EVEN_AND_ODD || op == REFINE_ODD) init = coarsest ? TEMPORAL : SPATIAL;
+    else if (op == REFINE_EVEN_AND_ODD && last_coarse_pass == this_pass - 1) init = SPATIAL;
+    const bool neighbours = op != INITIALIZE_EVEN_AND_ODD;
+    for (int f : frames) {
         pt_params p = user;  // updateParameters(BIDIRECTIONAL), :522-542
         p.advectionJitter = (f % 3 == 0) ? user.advectionJitter * 0.01f : 0.0f;
         p.direction = PT_BIDIRECTIONAL;
         TRY(pt_set_params(c, &p));
-        TRY(advect_neighbors(c, f, level, this_pass - 1, first, last, !initialize));
-        if (temporal_up) {
+        TRY(advect_neighbors(c, f, level, this_pass - 1, first, last, neighbours, ts));
+        if (init == TEMPORAL) {
             TRY(ensure_random(c));
             TRY(pt_merge_advected_buffers(c, level, PT_MERGE_FALLBACK_RANDOM));
-        } else if (spatial) {
+        } else if (init == SPATIAL) {
             TRY(spatial_upsample(c, f, level + 1, level, false, false));
         } else {
             TRY(load_last_saved_offsets(c, f, level));
@@ -2554,14 +2643,33 @@ static pt_status refine_pass(pt_ctx* c, const pt_params& user, int level, int la
         TRY(propagate_and_scatter(c, level, user.iterations, false, c->keyed ? key_full_index(c, f) : -1));
         TRY(save_images(c, level, f, this_pass, save_canvas));
     }
+    if (op == REFINE_ODD)
+        for (int f = first; f <= last; f += coarse_step) TRY(link_to_pass(c, f, level, this_pass));
+    else if (op == REFINE_EVEN)
+        for (int f = first + ts; f <= last; f += coarse_step) TRY(link_to_pass(c, f, level, this_pass));
     return PT_OK;
 }
 
+// the longest ribbon step every frame of the range has, with all shorter
+// ones (NLShot::setup stops at the first step a frame lacks; 1 without
+// ribbons, the max(1, ...) of renderAnimationTCTF)
+static int max_ribbon_step(const pt_ctx* c, int first, int last) {
+    int step = 1;
+    for (;;) {
+        const int next = step * 2;
+        for (int f = first; f <= last; f++)
+            if (!c->ribbons.count(std::make_pair(f, next))) return step;
+        step = next;
+    }
+}
+
 // SynthesisProcessor::renderAnimationTCTF, synthesisProcessor.cpp:1152-1312,
-// run locally with time step 1 (no ribbon inputs, so getMaxRibbonStep gives
-// 1): a consecutive pass at the coarsest level, refine passes at every level
-// from the coarsest to the final one (fixupPasses + 1 more when the range
-// spans more than two frames), then spatial upsampling down to level 0
+// run locally: the longest ribbon step T every frame has (1 without ribbon
+// inputs); a consecutive pass at the coarsest level over every T-th frame
+// (with keys: the initialisation pass), refine passes at every level for
+// step T (fixupPasses + 1 more while T < last - first), then for each
+// halved step the odd frames refined at every level with fix-up passes, then
+// spatial upsampling down to level 0.  Level-0 passes keep their output.
 static pt_status render_tctf(pt_ctx* c, int first, int last, bool fresh) {
     const pt_params user = c->params;
     if (fresh) {
@@ -2569,52 +2677,62 @@ static pt_status render_tctf(pt_ctx* c, int first, int last, bool fresh) {
         TRY(reset_image_slots(c));
         free_store(c);
     }
-    enum { CONSECUTIVE, REFINE, UPSAMPLE, INITIALIZE };
-    std::vector<std::pair<int, int>> ops;  // (operation, level)
-    ops.emplace_back(c->keyed ? INITIALIZE : CONSECUTIVE, user.levels - 1);
-    for (int level = user.levels - 1; level >= user.finalLevel; level--) {
-        ops.emplace_back(REFINE, level);
-        if (1 < last - first)
-            for (int i = 0; i < user.fixupPasses + 1; i++) ops.emplace_back(REFINE, level);
-    }
-    for (int level = user.finalLevel - 1; level >= 0; level--) ops.emplace_back(UPSAMPLE, level);
-    // the pass counters of the schedule (:1257-1285), first to find the pass
-    // whose output is handed out, then to run it
-    auto walk = [&](bool run) -> pt_status {
-        int passes_this = 0, passes_last = 0, last_level = -1;
-        for (const auto& op : ops) {
-            const int level = op.second;
-            if (last_level != level) {
-                if (run) TRY(bind_style_level(c, level));
-                if (run && c->keyed) TRY(upload_key_fields(c, level));
-                if (run && last_level >= 0 && last_level + 1 < user.levels) drop_store_level(c, last_level + 1);
-                passes_last = passes_this;
-                last_level = level;
-            }
-            const bool final_save = level == 0 && run && passes_this == c->out_pass;
-            if (op.first == INITIALIZE) {
-                if (run) TRY(refine_pass(c, user, level, passes_this - 1, 0, first, last, final_save && 0 == c->out_pass,
-                                         true));
-                passes_this = 1;
-            } else if (op.first == CONSECUTIVE) {
-                if (run) TRY(consecutive_pass(c, user, level, passes_this, passes_this - 1, first, last, final_save));
-                passes_this++;
-            } else if (op.first == REFINE) {
-                if (run) TRY(refine_pass(c, user, level, passes_last - 1, passes_this, first, last, final_save));
-                passes_this++;
-            } else {
-                if (run)
-                    for (int f = first; f <= last; f++) TRY(spatial_upsample(c, f, level + 1, level, true, level == 0));
-                passes_this = 1;
-            }
-        }
-        if (!run) c->out_pass = passes_this - 1;
-        return PT_OK;
+    enum { CONSECUTIVE = 100, UPSAMPLE = 101 };
+    struct Op {
+        int kind, level, ts;
     };
-    c->out_level = 0;
-    TRY(walk(false));
+    const int max_ts = max_ribbon_step(c, first, last);
+    const int L = user.levels - 1;
+    // with several time steps the levels are revisited coarse after fine:
+    // frame binds copy into the full-size layered arrays (as for IND)
+    struct SlotCopy {
+        pt_ctx* c;
+        bool was;
+        SlotCopy(pt_ctx* x, bool on) : c(x), was(x->slot_copy) { c->slot_copy = was || on; }
+        ~SlotCopy() { c->slot_copy = was; }
+    } slot_copy(c, max_ts > 1);
+    std::vector<Op> ops;
+    ops.push_back({c->keyed ? (int)INITIALIZE_EVEN_AND_ODD : (int)CONSECUTIVE, L, max_ts});
+    for (int level = L; level >= user.finalLevel; level--) {
+        ops.push_back({REFINE_EVEN_AND_ODD, level, max_ts});
+        if (max_ts < last - first)
+            for (int i = 0; i < user.fixupPasses + 1; i++) ops.push_back({REFINE_EVEN_AND_ODD, level, max_ts});
+    }
+    for (int ts = max_ts / 2; ts > 0; ts /= 2)
+        for (int level = L; level >= user.finalLevel; level--) {
+            ops.push_back({REFINE_ODD, level, ts});
+            if (ts < last - first)
+                for (int i = 0; i < user.fixupPasses; i++) ops.push_back({REFINE_EVEN_AND_ODD, level, ts});
+        }
+    for (int level = user.finalLevel - 1; level >= 0; level--) ops.push_back({UPSAMPLE, level, 1});
+    // the pass counters of the schedule (:1257-1285)
+    int passes_this = 0, passes_last = 0, last_level = -1;
     TRY(pt_reset_advected_buffers(c));
-    TRY(walk(true));
+    for (const Op& op : ops) {
+        const int level = op.level;
+        if (last_level != level) {
+            TRY(bind_style_level(c, level));
+            if (c->keyed) TRY(upload_key_fields(c, level));
+            passes_last = passes_this;  // (levels are revisited per time step: every level's passes stay)
+            last_level = level;
+        }
+        const bool keep = level == 0;
+        if (op.kind == INITIALIZE_EVEN_AND_ODD) {
+            TRY(refine_pass(c, user, level, passes_this - 1, 0, first, last, keep, INITIALIZE_EVEN_AND_ODD, op.ts));
+            passes_this = 1;
+        } else if (op.kind == CONSECUTIVE) {
+            TRY(consecutive_pass(c, user, level, passes_this, passes_this - 1, first, last, keep, op.ts));
+            passes_this++;
+        } else if (op.kind == UPSAMPLE) {
+            for (int f = first; f <= last; f++) TRY(spatial_upsample(c, f, level + 1, level, true, keep));
+            passes_this = 1;
+        } else {
+            TRY(refine_pass(c, user, level, passes_last - 1, passes_this, first, last, keep, op.kind, op.ts));
+            passes_this++;
+        }
+    }
+    c->out_level = 0;
+    c->out_pass = passes_this - 1;
     c->params = user;
     return PT_OK;
 }

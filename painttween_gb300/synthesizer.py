@@ -300,6 +300,12 @@ class Synthesizer(TexSynth):
                                        _p(_c(vel_fwd, np.float32)), _p(_c(vel_bwd, np.float32)),
                                        _p(_c(scale, np.float32))), "pt_set_frame")
 
+    def set_frame_ribbons(self, frame, step, vel_fwd, vel_bwd):
+        """Velocities over `step` frames (2, 4, ...), forwards and backwards."""
+        f, b = _c(vel_fwd, np.float32), _c(vel_bwd, np.float32)
+        h, w = f.shape[:2]
+        self._check(lib().pt_set_frame_ribbons(self.h, frame, step, w, h, _p(f), _p(b)), "pt_set_frame_ribbons")
+
     def set_frame_dict(self, frame, fr):
         self.set_frame(frame, fr["rgba"], fr.get("orient_tensor"), fr.get("dist_trans"), fr.get("object_ids"),
                        fr.get("vel_fwd"), fr.get("vel_bwd"), fr.get("scale"))

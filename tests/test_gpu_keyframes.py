@@ -301,3 +301,50 @@ def test_keyframe_interpolation_driver_matches_oracle(keys, first, last, scheme)
     for f in range(first, last + 1):
         assert_offsets_equal(got[f][1], ref[f][0], 1.0, "keyed frame %d" % f)
         assert_array_equal(got[f][0], ref[f][2], "keyed output frame %d" % f)
+
+
+@pytest.mark.parametrize("keyed", [False, True])
+def test_tctf_with_ribbon_steps_matches_oracle(keyed):
+    """TCTF over ribbon inputs of steps 2 and 4: a consecutive pass (or the
+    keyframe initialisation) every 4th frame, refine passes at step 4, odd
+    frames refined at steps 2 and 1 with the skipped frames linked to each
+    new pass; with keys, the ribbons also carry the preprocessing's
+    accumulation over 2 and 4 frames."""
+    from painttween_gb300 import Synthesizer
+    w, h, n = 48, 40, 6
+    p = config_params(r=2, levels=2, iterations=2)
+    p.scheme = _abi.S_TCTF
+    if keyed:
+        p.interpolateKeyFrame = 1
+        p.numStyles = 2
+        styles = [synthetic.make_exemplar(w, h, seed=100 + i) for i in range(2)]
+    else:
+        styles = [synthetic.make_exemplar(32, 32, seed=100)]
+    clip = synthetic.make_clip(w, h, 3, n, seed=101)
+    rng = np.random.default_rng(5)
+    rib = {(f, st): (rng.normal(0, 1, (h, w, 2)).astype(np.float32), rng.normal(0, 1, (h, w, 2)).astype(np.float32))
+           for f in range(n) for st in (2, 4)}
+    s = Synthesizer(device=0)
+    try:
+        sh, sw = styles[0]["base"].shape[:2]
+        s.setup(p, w, h, sw, sh, len(styles))
+        for i, ex in enumerate(styles):
+            s.set_style(i, ex["base"], ex["output"], ex["orient_tensor"], ex["dist_trans"], ex["object_ids"])
+        for i, fr in enumerate(clip):
+            s.set_frame_dict(i, fr)
+        for (f, st), (vf, vb) in rib.items():
+            s.set_frame_ribbons(f, st, vf, vb)
+        if keyed:
+            s.set_keyframes([0, 5])
+        got = s.synthesize_animation(0, n - 1)
+    finally:
+        s.close()
+    drv = O.OracleDriver(p, styles, clip, threads=8)
+    for (f, st), (vf, vb) in rib.items():
+        drv.set_frame_ribbons(f, st, vf, vb)
+    if keyed:
+        drv.set_keyframes([0, 5])
+    ref = drv.render(0, n - 1)
+    for f in range(n):
+        assert_offsets_equal(got[f][1], ref[f][0], 1.0, "TCTF ribbons frame %d" % f)
+        assert_array_equal(got[f][0], ref[f][2], "TCTF ribbons output frame %d" % f)
