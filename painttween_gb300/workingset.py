@@ -15,7 +15,8 @@ without Qt (GUI/nlSynthesizer.cpp:99-160).
         <unit name="..."/> <shot name="..."/> <shotDir path="..."/>
         <workingDir path="..."/> <fileAccess checkFarm="0"/>
         <elements inputElem="rgba" orientationElem="..." distTransElem="..."
-                  scaleElem="..." idMergedElem="..." velBElem="..." velFElem="..."/>
+                  scaleElem="..." idMergedElem="..." velBElem="..." velFElem="..."
+                  ribbonBElem="vel_b_[NN]" ribbonFElem="vel_f_[NN]"/>
       </anim>
     </doc>
 
@@ -160,7 +161,7 @@ class WorkingSet:
         self.shot_dir = os.path.normpath(os.path.join(root_dir, attr("shotDir", "path")))
         self.working_dir = os.path.normpath(os.path.join(root_dir, attr("workingDir", "path")))
         fa = anim.find("fileAccess")
-        farm = fa is not None and fa.attrib.get("checkFarm", "0").strip() == "1"
+        farm = self.farm = fa is not None and fa.attrib.get("checkFarm", "0").strip() == "1"
         el = anim.find("elements")
         self.elements = {}
         for key, xml, layer, names in _INPUT_LAYERS:
@@ -170,6 +171,43 @@ class WorkingSet:
                 self.elements[key] = (base + "." + name + ".%d.exr", layer, names)
         if "rgba" not in self.elements:
             raise WorkingSetError("no input element (inputElem)")
+        # ribbon elements (GUI/nlShot.cpp:162-190): "[..]" in the name is the
+        # two-digit step; without checkFarm the files are named relative to
+        # the working directory of the process, as in the reference
+        self.ribbon_elements = {}
+        for key, xml in (("vel_bwd", "ribbonBElem"), ("vel_fwd", "ribbonFElem")):
+            name = el.attrib.get(xml, "").strip(".") if el is not None else ""
+            if name:
+                self.ribbon_elements[key] = name
+
+    def _ribbon_path(self, key, step, frame):
+        import re
+        elem = re.sub(r"\[.*\]", "%02d" % step, self.ribbon_elements[key])
+        if self.farm:
+            return os.path.join(self.shot_dir, elem, self.shot + "." + elem) + ".%d.exr" % frame
+        return elem + ".%d.exr" % frame
+
+    def ribbon_steps(self, first, last):
+        """Steps 1, 2, 4 ... whose ribbon files exist for every frame, up to
+        the first missing one (at most 512)."""
+        steps = []
+        if len(self.ribbon_elements) < 2:
+            return steps
+        for i in range(10):
+            st = 1 << i
+            if not all(os.path.exists(self._ribbon_path(k, st, f)) for k in ("vel_bwd", "vel_fwd")
+                       for f in range(first, last + 1)):
+                break
+            steps.append(st)
+        return steps
+
+    def ribbons(self, frame, step):
+        """(vel_fwd, vel_bwd) of one frame and step; the layer is vel_f_<step>
+        / vel_b_<step>."""
+        out = []
+        for key, layer in (("vel_fwd", "vel_f_%d" % step), ("vel_bwd", "vel_b_%d" % step)):
+            out.append(_image(self._ribbon_path(key, step, frame), key, layer, ("x", "y")))
+        return tuple(out)
 
     def frame_path(self, key, frame):
         return self.elements[key][0] % frame
@@ -210,6 +248,9 @@ class WorkingSet:
             hi = max([last] + [k for k in self.keyframes if k > last][:1])
         for f in range(lo, hi + 1):
             synth.set_frame_dict(f, fr0 if f == first else self.frame(f))
+        for st in self.ribbon_steps(lo, hi)[1:]:  # step 1 is the frames' own velocities
+            for f in range(lo, hi + 1):
+                synth.set_frame_ribbons(f, st, *self.ribbons(f, st))
         return first, last
 
 

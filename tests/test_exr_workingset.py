@@ -148,3 +148,27 @@ def test_keyed_working_set_feeds_keyframes(tmp_path):
     assert ws.setup(r) == (1, 2)
     names = [c[0] for c in r.calls]
     assert names[:3] == ["setup", "set_style", "set_keyframes"] and names.count("set_frame_dict") == 2
+
+
+def test_ribbon_elements(tmp_path, monkeypatch):
+    """Ribbon files per step (vel_b_01, vel_b_02 ...), relative to the
+    working directory as in the reference; steps stop at the first missing."""
+    p, _, _ = _write_set(str(tmp_path))
+    xml = open(p).read().replace('velBElem="velB"', 'velBElem="velB" ribbonBElem="rb_[NN]" ribbonFElem="rf_[NN]"')
+    open(p, "w").write(xml)
+    monkeypatch.chdir(str(tmp_path))
+    rng = np.random.default_rng(4)
+    vals = {}
+    for st in (1, 2, 4):
+        for f in (1, 2):
+            for key, elem, layer in (("vel_bwd", "rb", "vel_b"), ("vel_fwd", "rf", "vel_f")):
+                if st == 4 and f == 2 and key == "vel_fwd":
+                    continue  # step 4 incomplete
+                v = rng.normal(size=(10, 14, 2)).astype(np.float32)
+                vals[(key, st, f)] = v
+                exr.write("%s_%02d.%d.exr" % (elem, st, f), {"%s_%d.x" % (layer, st): v[..., 0],
+                                                            "%s_%d.y" % (layer, st): v[..., 1]})
+    ws = workingset.load(p)
+    assert ws.ribbon_steps(1, 2) == [1, 2]
+    vf, vb = ws.ribbons(2, 2)
+    assert np.array_equal(vf, vals[("vel_fwd", 2, 2)]) and np.array_equal(vb, vals[("vel_bwd", 2, 2)])
