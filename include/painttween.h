@@ -145,10 +145,13 @@ enum {
     PT_LAYER_INPUT_DIST_TRANS = 7,
     PT_LAYER_INPUT_SCALE = 8,
     PT_LAYER_INPUT_ID = 9,
+    PT_LAYER_INPUT_SURF_ID = 10,          /* accepted, read by no kernel */
     PT_LAYER_INPUT_VEL_B = 11,
     PT_LAYER_INPUT_VEL_F = 12,
     PT_LAYER_INPUT_VEL_B_PREVIOUS = 13,
     PT_LAYER_INPUT_VEL_F_PREVIOUS = 14,
+    PT_LAYER_GUIDE_B = 15,                /* accepted, read by no kernel */
+    PT_LAYER_GUIDE_F = 16,
     PT_LAYER_CUMUL_FIELD_B = 17,          /* key-to-key ribbons, layer = key index */
     PT_LAYER_CUMUL_FIELD_F = 18,
     PT_LAYER_FRAME_TO_KEY_RIBBON_B = 19,  /* frame-to-key ribbons of the level */

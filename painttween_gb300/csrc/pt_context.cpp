@@ -1045,6 +1045,9 @@ pt_status pt_upload_image_color4(pt_ctx* c, int level, int layer, const float* r
         c->img.rnd = Arr<float4>{c->rnd, w, h};
         return PT_OK;
     }
+    // the keyframe guides: uploaded by loadAnimImages with
+    // guidedInterpolation, read by no kernel (texSynth_kernel.cu:85-86)
+    if (layer == PT_LAYER_GUIDE_B || layer == PT_LAYER_GUIDE_F) return PT_OK;
     return fail(c, PT_ERR_UNSUPPORTED, "colour layer %d not supported", layer);
 }
 
@@ -1087,6 +1090,8 @@ pt_status pt_upload_image_float2(pt_ctx* c, int level, int layer, const float* x
         case PT_LAYER_INPUT_VEL_B_PREVIOUS: store = &c->up_velb[prev]; slot = &c->img.velb[prev]; break;
         case PT_LAYER_INPUT_VEL_F_PREVIOUS: store = &c->up_velf[prev]; slot = &c->img.velf[prev]; break;
         case PT_LAYER_INPUT_SCALE: store = &c->up_scale; slot = &c->img.scale; break;
+        // surface ids: uploaded by loadAnimImages, read by no kernel
+        case PT_LAYER_INPUT_SURF_ID: return PT_OK;
         default: return fail(c, PT_ERR_UNSUPPORTED, "float2 layer %d not supported", layer);
     }
     if (layer != PT_LAYER_INPUT_SCALE) return slot_write(c, store, slot, xy, w, h, cudaMemcpyHostToDevice);
