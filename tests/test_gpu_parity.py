@@ -591,3 +591,22 @@ def test_lab_colour_space_matches_oracle(scheme):
     for f in range(2):
         assert_offsets_equal(got[f][1], ref[f][0], 1.0, "Lab frame %d" % f)
         assert_array_equal(got[f][0], ref[f][2], "Lab output frame %d" % f)
+
+
+@pytest.mark.parametrize("w,h,scheme", [(17, 13, _abi.S_FMBM_RM), (31, 7, _abi.S_FBMO), (23, 19, _abi.S_TCTF),
+                                        (9, 9, _abi.S_IND)])
+def test_small_odd_sizes_match_oracle(w, h, scheme):
+    """Odd, tiny images (a coarse level a few pixels across, narrower than
+    the patch window) through each scheme, against the oracle."""
+    p = config_params(r=2, levels=2, iterations=2)
+    p.scheme = scheme
+    p.temporalCoherenceWeight = 0.5
+    ex = synthetic.make_exemplar(24, 20, seed=95)
+    clip = synthetic.make_clip(w, h, 2, 3, seed=96)
+    got = _animate(p, ex, clip, w, h)
+    ref = O.OracleDriver(p, [ex], clip, threads=4).render(0, 2)
+    lv = _abi.output_level(p)
+    for f in range(3):
+        assert got[f][0].shape == (h >> lv, w >> lv, 4)
+        assert_offsets_equal(got[f][1], ref[f][0], 1.0, "%dx%d frame %d" % (w, h, f))
+        assert_array_equal(got[f][0], ref[f][2], "%dx%d output frame %d" % (w, h, f))
