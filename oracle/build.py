@@ -1,10 +1,16 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
 Compiles pt_oracle.c into oracle/libpt_oracle.so with FP contraction off so
-that its FP32 arithmetic follows the written operation order exactly.  The
-reference's own sources cannot be compiled here (its CUDA uses texture
-references and cudaThreadSynchronize, both removed in CUDA 13, and its host
-code needs Qt5/OpenEXR/GLEW), so there is no oracle/_ref build.
+that its FP32 arithmetic follows the written operation order exactly.
+
+The reference's kernels and drivers cannot be compiled here (its CUDA uses
+texture references and cudaThreadSynchronize, both removed in CUDA 13, and
+its host code needs Qt5/OpenEXR/GLEW).  Its device helper header
+(texSynth_util.h: colour conversion, exemplar basis and coordinates,
+clamping, squared differences, ribbon unpacking) does compile for the host:
+where the reference tree is present, build_ref() compiles it through
+ref_helpers.cpp into oracle/_ref/libref_helpers.so, against which the tests
+check the oracle's restatement of those helpers.
 """
 import os
 import platform
@@ -34,5 +40,59 @@ def build(force=False, verbose=False):
     return OUT
 
 
+REF_SRC = os.environ.get("PT_REFERENCE_SRC", "/root/reference/src/PaintTweenCUDA")
+REF_SHIM = os.path.join(HERE, "ref_helpers.cpp")
+REF_OUT = os.path.join(HERE, "_ref", "libref_helpers.so")
+
+
+def build_ref(force=False, verbose=False):
+    """oracle/_ref/libref_helpers.so from the reference's texSynth_util.h, or
+    None when the reference tree is not present."""
+    header = os.path.join(REF_SRC, "texSynth_util.h")
+    if not os.path.exists(header):
+        return None
+    if not force and os.path.exists(REF_OUT) and os.path.getmtime(REF_OUT) >= os.path.getmtime(REF_SHIM):
+        return REF_OUT
+    cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    os.makedirs(os.path.dirname(REF_OUT), exist_ok=True)
+    # contraction on, as nvcc compiles the reference's device code (--fmad=true)
+    flags = ["-O2", "-std=c++14", "-fPIC", "-shared", "-w", "-ffp-contract=fast"]
+    if platform.machine() in ("x86_64", "AMD64"):
+        flags.append("-mfma")
+    cmd = ["g++"] + flags + ["-I", REF_SRC, "-I", cuda_inc, REF_SHIM, "-o", REF_OUT + ".tmp", "-lm"]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd)
+    os.replace(REF_OUT + ".tmp", REF_OUT)
+    build_ref_cubin(force=force, verbose=verbose)
+    return REF_OUT
+
+
+REF_DEV_SHIM = os.path.join(HERE, "ref_helpers_dev.cu")
+REF_CUBIN = os.path.join(HERE, "_ref", "ref_helpers.cubin")
+
+
+def build_ref_cubin(force=False, verbose=False):
+    """oracle/_ref/ref_helpers.cubin: texSynth_util.h compiled by nvcc for
+    sm_103a with nvcc's default arithmetic, or None without the reference
+    tree.  A cubin is loaded by the driver, so one built here runs on any
+    host with a GB300."""
+    if not os.path.exists(os.path.join(REF_SRC, "texSynth_util.h")):
+        return None
+    if (not force and os.path.exists(REF_CUBIN)
+            and os.path.getmtime(REF_CUBIN) >= os.path.getmtime(REF_DEV_SHIM)):
+        return REF_CUBIN
+    nvcc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+    os.makedirs(os.path.dirname(REF_CUBIN), exist_ok=True)
+    cmd = [nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-w", "-I", REF_SRC,
+           REF_DEV_SHIM, "-o", REF_CUBIN + ".tmp"]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd)
+    os.replace(REF_CUBIN + ".tmp", REF_CUBIN)
+    return REF_CUBIN
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose=True))
+    print(build_ref(force="--force" in sys.argv, verbose=True))

@@ -94,6 +94,12 @@ def lib():
             "pto_merge_advected": (None, [vp, i, i]),
             "pto_rgb_to_lab": (f, [vp, vp]),
             "pto_powd": (ctypes.c_double, [ctypes.c_double, ctypes.c_double]),
+            "pto_basis": (None, [f, f, f, vp]),
+            "pto_new_coord": (None, [f, f, f, f, vp, vp]),
+            "pto_clamp_to_exemplar": (None, [vp, vp, i, i]),
+            "pto_ssd": (f, [vp, vp, f]),
+            "pto_ssd_plain": (f, [vp, vp]),
+            "pto_ribbon_of": (None, [vp, vp, vp]),
             "pto_random_level_keys": (i, [u32, i, i, i, i, i, vp, vp, vp, vp, i, i, i, i, i, i, i, vp]),
         }
         for name, (res, args) in sig.items():

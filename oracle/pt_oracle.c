@@ -12,11 +12,15 @@
  * occupies the top-left (W>>L) x (H>>L) rectangle, persistent across levels
  * and frames.  Every function cites the reference lines it follows.
  *
- * Parity status: UNPINNED against the reference itself.  The reference ships
- * no tests, golden vectors or fixtures for this path, and its CUDA sources do
- * not compile with the installed CUDA 13 (legacy texture references and
- * cudaThreadSynchronize are removed), so no reference output can be produced.
- * The glibc rand() restatement is pinned against the C library's rand().
+ * Parity status: pinned at the helper level, unpinned end to end.  The
+ * reference ships no tests, golden vectors or fixtures for this path, and its
+ * CUDA kernels do not compile with the installed CUDA 13 (legacy texture
+ * references and cudaThreadSynchronize are removed), so no end-to-end
+ * reference output can be produced.  Its helper header texSynth_util.h does
+ * compile: the pto_basis / pto_new_coord / pto_clamp_to_exemplar / pto_ssd /
+ * pto_ribbon_of / pto_rgb_to_lab hooks are checked against it, built for the
+ * host (g++) and for the GPU (nvcc cubin).  The glibc rand() restatement is
+ * pinned against the C library's rand().
  *
  * Arithmetic contract (shared, by specification, with the CUDA kernels so the
  * two agree bit for bit): FP32 everywhere the reference uses float, with
@@ -494,7 +498,9 @@ static inline void basis(float angle, float su, float sv, f2* b0, f2* b1) {
     b0->y = s * su;
 }
 
-/* calculateNewExemplarCoord, texSynth_util.h:106-118: e + (i*b0 + j*b1) */
+/* calculateNewExemplarCoord, texSynth_util.h:106-118: e + (i*b0 + j*b1),
+ * the first product fused with the second as nvcc contracts the reference's
+ * expression (checked against the reference's helper run on the GPU) */
 static inline void new_coord(float i, float j, float ex, float ey, f2 b0, f2 b1, float* ox, float* oy) {
     *ox = ex + fmaf(i, b0.x, j * b1.x);
     *oy = ey + fmaf(i, b0.y, j * b1.y);
@@ -527,6 +533,27 @@ static inline float ssd(f4 a, f4 b) {
     return s;
 }
 static inline f4 sub4(f4 a, f4 b) { f4 r = {a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w}; return r; }
+
+/* Test hooks: the helpers above on plain arrays, for checking them one by
+ * one against the reference's own texSynth_util.h compiled for the host. */
+void pto_basis(float angle, float su, float sv, float* out) {
+    f2 b0, b1;
+    basis(angle, su, sv, &b0, &b1);
+    out[0] = b0.x; out[1] = b0.y; out[2] = b1.x; out[3] = b1.y;
+}
+void pto_new_coord(float i, float j, float ex, float ey, const float* b, float* out) {
+    f2 b0 = {b[0], b[1]}, b1 = {b[2], b[3]};
+    new_coord(i, j, ex, ey, b0, b1, &out[0], &out[1]);
+}
+void pto_clamp_to_exemplar(float* x, float* y, int w, int h) { clamp_to_exemplar(x, y, w, h); }
+float pto_ssd(const float* a, const float* b, float alpha) {
+    f4 x = {a[0], a[1], a[2], a[3]}, y = {b[0], b[1], b[2], b[3]};
+    return ssd_a(x, y, alpha);
+}
+float pto_ssd_plain(const float* a, const float* b) {
+    f4 x = {a[0], a[1], a[2], a[3]}, y = {b[0], b[1], b[2], b[3]};
+    return ssd(x, y);
+}
 
 /* per-pixel values that calculateResidual recomputes for every candidate
  * but that do not depend on the candidate (texSynth_kernel.cu:545-561) */
@@ -1413,6 +1440,11 @@ static pt_ribbon ribbon_of(f4 c) {
     pt_ribbon r;
     r.x = c.z; r.y = c.y; r.time_step = f2i(c.x); r.layer = f2i(c.w);
     return r;
+}
+void pto_ribbon_of(const float* c, float* xy, int* ts_layer) {
+    f4 v = {c[0], c[1], c[2], c[3]};
+    pt_ribbon r = ribbon_of(v);
+    xy[0] = r.x; xy[1] = r.y; ts_layer[0] = r.time_step; ts_layer[1] = r.layer;
 }
 /* the keyframe mask of key layer `key` at pixel (x, y): the key's output
  * alpha (PYRAMID_FETCH_LAYER(gExemplarOutput, x, y, keyIndex)) */
