@@ -7,10 +7,13 @@ The reference's kernels and drivers cannot be compiled here (its CUDA uses
 texture references and cudaThreadSynchronize, both removed in CUDA 13, and
 its host code needs Qt5/OpenEXR/GLEW).  Its device helper header
 (texSynth_util.h: colour conversion, exemplar basis and coordinates,
-clamping, squared differences, ribbon unpacking) does compile for the host:
-where the reference tree is present, build_ref() compiles it through
-ref_helpers.cpp into oracle/_ref/libref_helpers.so, against which the tests
-check the oracle's restatement of those helpers.
+clamping, squared differences, ribbon unpacking) and its host pyramid code
+(downsample.cpp, given the small QtCore container shim in qt_shim/) do
+compile for the host: where the reference tree is present, build_ref()
+compiles them through ref_helpers.cpp and ref_downsample.cpp into
+oracle/_ref/libref_helpers.so, and the helper header through
+ref_helpers_dev.cu into an sm_103a cubin, against which the tests check the
+oracle's restatements.
 """
 import os
 import platform
@@ -42,16 +45,22 @@ def build(force=False, verbose=False):
 
 REF_SRC = os.environ.get("PT_REFERENCE_SRC", "/root/reference/src/PaintTweenCUDA")
 REF_SHIM = os.path.join(HERE, "ref_helpers.cpp")
+REF_DOWNSAMPLE_SHIM = os.path.join(HERE, "ref_downsample.cpp")
+QT_SHIM = os.path.join(HERE, "qt_shim")
 REF_OUT = os.path.join(HERE, "_ref", "libref_helpers.so")
 
 
 def build_ref(force=False, verbose=False):
-    """oracle/_ref/libref_helpers.so from the reference's texSynth_util.h, or
+    """oracle/_ref/libref_helpers.so from the reference's texSynth_util.h and
+    downsample.cpp (over the QtCore container shim in oracle/qt_shim), or
     None when the reference tree is not present."""
     header = os.path.join(REF_SRC, "texSynth_util.h")
     if not os.path.exists(header):
         return None
-    if not force and os.path.exists(REF_OUT) and os.path.getmtime(REF_OUT) >= os.path.getmtime(REF_SHIM):
+    deps = [REF_SHIM, REF_DOWNSAMPLE_SHIM, os.path.join(QT_SHIM, "QtCore", "qt_shim_core.h")]
+    if (not force and os.path.exists(REF_OUT)
+            and all(os.path.getmtime(REF_OUT) >= os.path.getmtime(d) for d in deps)):
+        build_ref_cubin(verbose=verbose)
         return REF_OUT
     cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
     os.makedirs(os.path.dirname(REF_OUT), exist_ok=True)
@@ -59,7 +68,8 @@ def build_ref(force=False, verbose=False):
     flags = ["-O2", "-std=c++14", "-fPIC", "-shared", "-w", "-ffp-contract=fast"]
     if platform.machine() in ("x86_64", "AMD64"):
         flags.append("-mfma")
-    cmd = ["g++"] + flags + ["-I", REF_SRC, "-I", cuda_inc, REF_SHIM, "-o", REF_OUT + ".tmp", "-lm"]
+    cmd = ["g++"] + flags + ["-I", QT_SHIM, "-I", REF_SRC, "-I", cuda_inc, REF_SHIM, REF_DOWNSAMPLE_SHIM,
+                             os.path.join(REF_SRC, "downsample.cpp"), "-o", REF_OUT + ".tmp", "-lm"]
     if verbose:
         print(" ".join(cmd))
     subprocess.check_call(cmd)

@@ -1,8 +1,11 @@
 """The oracle's restated helpers against the reference's own code.
 
 src/PaintTweenCUDA/texSynth_util.h (colour conversion, exemplar basis and
-coordinates, clamping, squared differences, ribbon unpacking) compiles for the
-host; oracle/build.py builds it through oracle/ref_helpers.cpp into
+coordinates, clamping, squared differences, ribbon unpacking) and
+src/PaintTweenCUDA/downsample.cpp (host pyramids: 2x2 averages, velocity
+scaling, majority vote of object ids) compile for the host; oracle/build.py
+builds them through oracle/ref_helpers.cpp and oracle/ref_downsample.cpp
+(downsample.cpp over the QtCore container shim oracle/qt_shim) into
 oracle/_ref/libref_helpers.so where the reference tree is present.  These
 tests are skipped where it is not (the library is built from the reference's
 sources and never committed).
@@ -50,6 +53,10 @@ def ref():
             "ref_ssd": (f, [vp, vp, f]),
             "ref_ssd_plain": (f, [vp, vp]),
             "ref_ribbon_of": (None, [vp, vp, vp]),
+            "ref_pyramid_rgba": (i, [vp, i, i, i, vp]),
+            "ref_pyramid_float": (i, [vp, i, i, i, vp]),
+            "ref_pyramid_float2": (i, [vp, i, i, i, vp]),
+            "ref_pyramid_int": (i, [vp, i, i, vp]),
         }.items():
             fn = getattr(L, name)
             fn.restype, fn.argtypes = res, args
@@ -163,3 +170,46 @@ def test_rgb_to_lab_against_reference():
         R.ref_rgb_to_lab(_p(c), _p(ro))
         oo = O.rgb_to_lab(c)
         assert np.abs(ro - oo).max() <= 1e-6, (c, ro, oo)
+
+
+def _ref_levels(fn, img, w, h, ch, dtype, *mode):
+    n = sum((w >> l) * (h >> l) for l in range(O.num_levels(w, h))) * ch
+    out = np.empty(n, dtype)
+    nl = fn(_p(np.ascontiguousarray(img)), w, h, *mode, _p(out))
+    assert nl == O.num_levels(w, h)
+    levels, off = [], 0
+    for l in range(nl):
+        k = (w >> l) * (h >> l) * ch
+        levels.append(out[off:off + k])
+        off += k
+    return levels
+
+
+@pytest.mark.parametrize("w,h", [(64, 48), (37, 20), (128, 128), (9, 300)])
+def test_pyramids_bit_exact_with_reference_downsample(w, h):
+    """downsamplePyramid<Color4/float/float2> (2x2 averages, with and without
+    the per-level halving of velocities) against the oracle's pyramids."""
+    rng = np.random.default_rng(w * 1000 + h)
+    R = ref()
+    for ch, fn in ((4, R.ref_pyramid_rgba), (1, R.ref_pyramid_float), (2, R.ref_pyramid_float2)):
+        img = (rng.standard_normal((h, w, ch)) * 3).astype(np.float32)
+        for scale_with_levels in (0, 1):
+            ref_levels = _ref_levels(fn, img, w, h, ch, np.float32, scale_with_levels)
+            ours = O.pyramid_avg(img if ch > 1 else img[..., 0], vel=bool(scale_with_levels))
+            assert len(ours) == len(ref_levels)
+            for a, b in zip(ours, ref_levels):
+                assert a.reshape(-1).tobytes() == b.tobytes(), (ch, scale_with_levels)
+
+
+@pytest.mark.parametrize("w,h,k", [(64, 48, 3), (37, 20, 2), (128, 64, 6), (16, 16, 1)])
+def test_object_id_vote_bit_exact_with_reference_downsample(w, h, k):
+    """downsamplePyramid<int> (majority vote of the 2x2 ids through QHash and
+    QMap) against the oracle's vote.  Ties follow the container shim's hash
+    order (descending ids, one of the orders Qt may give): the smallest id."""
+    rng = np.random.default_rng(w + h + k)
+    ids = rng.integers(-1, k, (h, w)).astype(np.int32)
+    ref_levels = _ref_levels(ref().ref_pyramid_int, ids, w, h, 1, np.int32)
+    ours = O.pyramid_vote(ids)
+    assert len(ours) == len(ref_levels)
+    for a, b in zip(ours, ref_levels):
+        assert (a.reshape(-1) == b).all()
