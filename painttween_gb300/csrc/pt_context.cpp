@@ -839,6 +839,10 @@ pt_status pt_initialize(pt_ctx* c, int iw, int ih, int sw, int sh, int ns) {
     if (!c) return PT_ERR_INVALID;
     if (iw < 2 || ih < 2 || sw < 2 || sh < 2 || ns < 1 || ns > PT_MAX_STYLES)
         return fail(c, PT_ERR_INVALID, "bad sizes %dx%d style %dx%dx%d", iw, ih, sw, sh, ns);
+    // pixel and texel ids are 32-bit in the kernels
+    if ((long long)iw * ih > INT32_MAX || (long long)sw * sh * ns > INT32_MAX)
+        return fail(c, PT_ERR_INVALID, "sizes too large: %dx%d image, %dx%dx%d styles (at most 2^31-1 pixels each)",
+                    iw, ih, sw, sh, ns);
     CU(cudaSetDevice(c->device));
     if (c->initialized && iw == c->W && ih == c->H && sw == c->SW && sh == c->SH && ns == c->NS) return PT_OK;
     // release the image-size state
@@ -928,7 +932,8 @@ pt_status pt_reset_advected_buffers(pt_ctx* c) {
 pt_status pt_initialize_exemplars(pt_ctx* c, int w, int h, int ns) {
     if (!c) return PT_ERR_INVALID;
     if (!c->initialized) return fail(c, PT_ERR_STATE, "pt_initialize has not been called");
-    if (w < 2 || h < 2 || ns != c->NS) return fail(c, PT_ERR_INVALID, "bad exemplar size %dx%dx%d", w, h, ns);
+    if (w < 2 || h < 2 || ns != c->NS || (long long)w * h * ns > INT32_MAX)
+        return fail(c, PT_ERR_INVALID, "bad exemplar size %dx%dx%d", w, h, ns);
     size_t n = (size_t)w * h * ns;
     if (n > c->ex_cap) {
         dfree_t(c, c->up_ex.base); dfree_t(c, c->up_ex.out); dfree_t(c, c->up_ex.bo);
@@ -1271,7 +1276,9 @@ pt_status pt_scatter(pt_ctx* c, int level, int key_index) {
 // TexSynth::initialize_cumulativeFields, texSynth_kernel.cu:2138-2142: the
 // key-to-key fields, `layers` layers of w x h, zeroed
 pt_status pt_initialize_cumulative_fields(pt_ctx* c, int w, int h, int layers) {
-    if (!c || w < 1 || h < 1 || layers < 1) return PT_ERR_INVALID;
+    if (!c) return PT_ERR_INVALID;
+    if (w < 1 || h < 1 || layers < 1 || (long long)w * h * layers > INT32_MAX)
+        return fail(c, PT_ERR_INVALID, "bad cumulative field size %dx%dx%d", w, h, layers);
     if (!c->initialized) return fail(c, PT_ERR_STATE, "pt_initialize has not been called");
     const size_t n = (size_t)w * h * layers;
     for (int d = 0; d < 2; d++) {

@@ -330,6 +330,11 @@ def test_errors_are_status_codes():
     t = TexSynth(device=0)
     with pytest.raises(PaintTweenError):
         t.propagate(0, 1)  # before initialize
+    for sizes in ((0, 32, 32, 32, 1), (32, 1, 32, 32, 1), (32, 32, 32, 32, 0), (70000, 70000, 32, 32, 1),
+                  (32, 32, 40000, 40000, 2)):
+        with pytest.raises(PaintTweenError) as e:
+            t.initialize(*sizes)  # empty, degenerate and oversized images are refused before any allocation
+        assert e.value.status == 1, sizes  # PT_ERR_INVALID
     t.initialize(32, 32, 32, 32, 1)
     with pytest.raises(PaintTweenError):
         t.upload_image_color4(0, _abi.LAYER_INPUT_COLOR, np.zeros((10, 10, 4), np.float32))
