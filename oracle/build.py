@@ -68,7 +68,7 @@ def build_ref(force=False, verbose=False):
     flags = ["-O2", "-std=c++14", "-fPIC", "-shared", "-w", "-ffp-contract=fast"]
     if platform.machine() in ("x86_64", "AMD64"):
         flags.append("-mfma")
-    cmd = ["g++"] + flags + ["-I", QT_SHIM, "-I", REF_SRC, "-I", cuda_inc, REF_SHIM, REF_DOWNSAMPLE_SHIM,
+    cmd = ["g++"] + flags + ["-I", QT_SHIM, "-I", os.path.join(QT_SHIM, "QtCore"), "-I", REF_SRC, "-I", cuda_inc, REF_SHIM, REF_DOWNSAMPLE_SHIM,
                              os.path.join(REF_SRC, "downsample.cpp"), "-o", REF_OUT + ".tmp", "-lm"]
     if verbose:
         print(" ".join(cmd))

@@ -19,7 +19,9 @@
  * reference output can be produced.  Its helper header texSynth_util.h does
  * compile: the pto_basis / pto_new_coord / pto_clamp_to_exemplar / pto_ssd /
  * pto_ribbon_of / pto_rgb_to_lab hooks are checked against it, built for the
- * host (g++) and for the GPU (nvcc cubin).  The glibc rand() restatement is
+ * host (g++) and for the GPU (nvcc cubin); pto_pixel_wrap / pto_in_bounds
+ * against cudaImageBuffer.h and the pyramids against downsample.cpp, both
+ * built for the host.  The glibc rand() restatement is
  * pinned against the C library's rand().
  *
  * Arithmetic contract (shared, by specification, with the CUDA kernels so the
@@ -336,11 +338,23 @@ static inline int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ?
 
 static inline int lvl_w(const pto* o, int level) { return o->W >> level; }
 static inline int lvl_h(const pto* o, int level) { return o->H >> level; }
-static inline int in_rect(const pto* o, int x, int y, int level, int border) {
-    /* CudaImageBufferDevice::inBounds, cudaImageBuffer.h:117-120 */
-    return x >= border && y >= border && x < lvl_w(o, level) - border &&
-           y < lvl_h(o, level) - border;
+/* CudaImageBufferDevice::inBounds, cudaImageBuffer.h:117-120 */
+static inline int in_bounds(int W, int H, int x, int y, int level, int border) {
+    return x >= border && y >= border && x < (W >> level) - border && y < (H >> level) - border;
 }
+static inline int in_rect(const pto* o, int x, int y, int level, int border) {
+    return in_bounds(o->W, o->H, x, y, level, border);
+}
+/* CudaImageBufferDevice::pixelWrap, cudaImageBuffer.h:81-87: the pixel index
+ * of (x, y) wrapped by the buffer's (level-0) size */
+static inline size_t pixel_wrap_index(int W, int H, int x, int y) {
+    int wx = (int)((float)x - (float)W * floorf((float)x / (float)W));
+    int wy = (int)((float)y - (float)H * floorf((float)y / (float)H));
+    return (size_t)wy * W + wx;
+}
+/* test hooks for the two above */
+int pto_in_bounds(int W, int H, int x, int y, int level, int border) { return in_bounds(W, H, x, y, level, border); }
+long long pto_pixel_wrap(int W, int H, int x, int y) { return (long long)pixel_wrap_index(W, H, x, y); }
 
 /* integer coordinate of a point-filtered fetch at unnormalised u (+0.5 as
  * PYRAMID_FETCH adds, cudaImagePyramid.h:102,108), clamp addressing */
@@ -738,10 +752,7 @@ static inline pt_patchxf patch(float x, float y, float th, float h, int layer, f
 
 /* calculatePropagateOffset, texSynth_kernel.cu:956-982 */
 static pt_patchxf propagate_offset(const pto* o, const pt_patchxf* src, int tx, int ty, int x, int y) {
-    /* pixelWrap with the level-0 size, cudaImageBuffer.h:81-87 */
-    int wx = (int)((float)tx - (float)o->W * floorf((float)tx / (float)o->W));
-    int wy = (int)((float)ty - (float)o->H * floorf((float)ty / (float)o->H));
-    pt_patchxf t = src[(size_t)wy * o->W + wx];
+    pt_patchxf t = src[pixel_wrap_index(o->W, o->H, tx, ty)]; /* level-0 size */
     f2 sc = scale_texel(o, tx, ty);
     f2 b0, b1;
     basis(t.theta, o->p.residualWindowScaleU * sc.x, o->p.residualWindowScaleV * sc.y, &b0, &b1);

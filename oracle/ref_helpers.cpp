@@ -1,6 +1,7 @@
 // ref_helpers.cpp -- C entry points over the reference's own device helpers
-// (src/PaintTweenCUDA/texSynth_util.h), compiled for the host from the
-// reference tree by oracle/build.py into oracle/_ref/libref_helpers.so.
+// (src/PaintTweenCUDA/texSynth_util.h) and image-buffer addressing
+// (cudaImageBuffer.h), compiled for the host from the reference tree by
+// oracle/build.py into oracle/_ref/libref_helpers.so.
 //
 // Test infrastructure only: tests/test_ref_helpers.py checks the oracle's
 // restatement of these helpers against the reference's code itself.  The
@@ -9,6 +10,7 @@
 #include <cuda_runtime.h>
 static uint3 threadIdx = {0, 0, 0};
 #include "texSynth_util.h"
+#include "cudaImageBuffer.h"
 
 extern "C" {
 
@@ -41,6 +43,18 @@ float ref_ssd_plain(const float* a, const float* b) {
 void ref_ribbon_of(const float* c, float* xy, int* ts_layer) {
     RibbonP r = toRibbonP(make_float4(c[0], c[1], c[2], c[3]));
     xy[0] = r.x; xy[1] = r.y; ts_layer[0] = r.time_step; ts_layer[1] = r.layer;
+}
+
+// CudaImageBufferDevice::pixelWrap and inBounds (cudaImageBuffer.h) on a
+// w x h image whose pixel i holds i: the wrapped pixel's index comes back.
+int ref_pixel_wrap(const int* index_image, int w, int h, int x, int y) {
+    CudaImageBufferDevice<int> b(const_cast<int*>(index_image), w * (int)sizeof(int), w, h);
+    return b.pixelWrap(x, y);
+}
+
+int ref_in_bounds(int w, int h, int x, int y, int level, int border) {
+    CudaImageBufferDevice<int> b(nullptr, w * (int)sizeof(int), w, h);
+    return b.inBounds(x, y, level, border) ? 1 : 0;
 }
 
 }  // extern "C"

@@ -2,9 +2,11 @@
 
 src/PaintTweenCUDA/texSynth_util.h (colour conversion, exemplar basis and
 coordinates, clamping, squared differences, ribbon unpacking) and
-src/PaintTweenCUDA/downsample.cpp (host pyramids: 2x2 averages, velocity
-scaling, majority vote of object ids) compile for the host; oracle/build.py
-builds them through oracle/ref_helpers.cpp and oracle/ref_downsample.cpp
+src/PaintTweenCUDA/cudaImageBuffer.h (pixelWrap and inBounds: the level-0
+wrap that coarse levels read through) and src/PaintTweenCUDA/downsample.cpp
+(host pyramids: 2x2 averages, velocity scaling, majority vote of object
+ids) compile for the host; oracle/build.py builds them through
+oracle/ref_helpers.cpp and oracle/ref_downsample.cpp
 (downsample.cpp over the QtCore container shim oracle/qt_shim) into
 oracle/_ref/libref_helpers.so where the reference tree is present.  These
 tests are skipped where it is not (the library is built from the reference's
@@ -57,6 +59,8 @@ def ref():
             "ref_pyramid_float": (i, [vp, i, i, i, vp]),
             "ref_pyramid_float2": (i, [vp, i, i, i, vp]),
             "ref_pyramid_int": (i, [vp, i, i, vp]),
+            "ref_pixel_wrap": (i, [vp, i, i, i, i]),
+            "ref_in_bounds": (i, [i, i, i, i, i, i]),
         }.items():
             fn = getattr(L, name)
             fn.restype, fn.argtypes = res, args
@@ -213,3 +217,23 @@ def test_object_id_vote_bit_exact_with_reference_downsample(w, h, k):
     assert len(ours) == len(ref_levels)
     for a, b in zip(ours, ref_levels):
         assert (a.reshape(-1) == b).all()
+
+
+@pytest.mark.parametrize("w,h", [(64, 48), (37, 20), (1920, 1080), (5, 3)])
+def test_pixel_wrap_and_bounds_bit_exact(w, h):
+    """CudaImageBufferDevice::pixelWrap (floorf-based wrap by the buffer's
+    level-0 size, which coarse levels read through) and inBounds (the level
+    rectangle with a border) against the oracle's restatements, over
+    coordinates from several periods below zero to several above."""
+    R, OL = ref(), O.lib()
+    index_image = np.arange(w * h, dtype=np.int32)
+    xs = list(range(-3 * w - 2, -3 * w + 3)) + list(range(-w - 2, w + 3)) + list(range(3 * w - 2, 3 * w + 3))
+    ys = list(range(-2 * h - 2, -2 * h + 3)) + list(range(-h - 2, h + 3)) + list(range(2 * h - 2, 2 * h + 3))
+    for y in ys[:: max(1, len(ys) // 40)] + [ys[0], ys[-1], 0, -1, h - 1, h]:
+        for x in xs[:: max(1, len(xs) // 60)] + [xs[0], xs[-1], 0, -1, w - 1, w]:
+            assert R.ref_pixel_wrap(_p(index_image), w, h, x, y) == OL.pto_pixel_wrap(w, h, x, y), (x, y)
+    for level in range(4):
+        for border in (0, 1, 3):
+            for y in (-1, 0, 1, 2, (h >> level) - 4, (h >> level) - 1, h >> level, h):
+                for x in (-1, 0, 1, 2, (w >> level) - 4, (w >> level) - 1, w >> level, w):
+                    assert R.ref_in_bounds(w, h, x, y, level, border) == OL.pto_in_bounds(w, h, x, y, level, border)
