@@ -282,6 +282,8 @@ def run_ours(args, dist):
     ex, clip = make_inputs(cfg, frames, seed=2026 + dist.rank)
     s = Synthesizer(device=device)
     s.setup(p, cfg["w"], cfg["h"], cfg["ew"], cfg["eh"], 1)
+    if args.generic_kernels:
+        s.set_tiled_kernels(False)  # same results, one-thread-per-pixel kernels (profiling them)
     s.set_style(0, ex["base"], ex["output"], ex["orient_tensor"], ex["dist_trans"], ex["object_ids"])
     for i, fr in enumerate(clip):
         s.set_frame_dict(i, fr)
@@ -387,6 +389,7 @@ def run_ours(args, dist):
         "config": {"workload": WORKLOAD, "frames": frames, "image": "%dx%d" % (cfg["w"], cfg["h"]),
                    "exemplar": "%dx%d" % (cfg["ew"], cfg["eh"]), "patch_radius": r, "levels": p.levels,
                    "iterations": p.iterations, "scheme": "FMBM_RM", "histogram": True,
+                   "kernels": "generic" if args.generic_kernels else "tiled",
                    "parallelism": "replicas" if dist.ws > 1 else "single",
                    "l2": "inputs larger than L2 (%.1f GB of resident frame pyramids per step)"
                          % (s.device_bytes / 1e9)},
@@ -487,6 +490,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-stills", type=int, default=64, help="requests of the batched-vs-plain run (0: skip)")
     ap.add_argument("--batch-in-flight", type=int, default=8)
+    ap.add_argument("--generic-kernels", action="store_true",
+                    help="run the generic one-thread-per-pixel kernels instead of the tiled ones (profiling only)")
     args = ap.parse_args()
     dist = Dist()
     try:
