@@ -245,7 +245,7 @@ pt_status pt_merge_randomly(pt_ctx* ctx, int level, int forwards,
 pt_status pt_merge_using_residual(pt_ctx* ctx, int level, int forwards); /* :1978 */
 pt_status pt_update_residual_cache(pt_ctx* ctx, int level);       /* :1221 */
 pt_status pt_sync_buffers(pt_ctx* ctx, int level, int op_flags);  /* :1240 */
-pt_status pt_reset_advected_buffers(pt_ctx* ctx); /* workingBuffers.cpp:112-116 */
+pt_status pt_reset_advected_buffers(pt_ctx* ctx); /* workingBuffers.cpp:119-123 */
 /* offsets.base().copyTo(advectedF/B.offsets()) and
  * residualCache.base().copyTo(advectedF/B.residual()), the merge set-up of
  * renderAnimationFBMO (synthesisProcessor.cpp:979-980). */
