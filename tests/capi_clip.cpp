@@ -16,7 +16,9 @@
 // output.bin: per frame, in frame order, the final rgba [oh][ow][4] f32 and
 //   offsets [oh][ow] pt_patchxf from pt_synthesize_animation's callback, then
 //   the last frame's rgba and offsets again as read back by
-//   pt_get_frame_result into page-locked memory.
+//   pt_get_frame_result into page-locked memory, then the results of the same
+//   clip submitted twice at once to pt_serve (two requests in flight): for
+//   each request, all frames' rgba, then all frames' offsets.
 //
 // Exits 0 on success; on any failure prints the status and the context's last
 // error and exits 1.
@@ -99,14 +101,22 @@ int main(int argc, char** argv) {
     check(pt_set_style(g_ctx, 0, ew, eh, ex_base.data(), ex_out.data(), ex_tensor.data(), ex_dt.data(),
                        ex_ids.data()),
           "pt_set_style");
+    struct Frame {
+        std::vector<float> rgba, tensor, dt, vf, vb, scale;
+        std::vector<int32_t> ids;
+    };
+    std::vector<Frame> clip(frames);
     for (int f = 0; f < frames; f++) {
-        std::vector<float> rgba = read_array<float>(in, ni * 4), tensor = read_array<float>(in, ni * 3);
-        std::vector<float> dt = read_array<float>(in, ni);
-        std::vector<int32_t> ids = read_array<int32_t>(in, ni);
-        std::vector<float> vf = read_array<float>(in, ni * 2), vb = read_array<float>(in, ni * 2);
-        std::vector<float> scale = read_array<float>(in, ni * 2);
-        check(pt_set_frame(g_ctx, f, w, h, rgba.data(), tensor.data(), dt.data(), ids.data(), vf.data(), vb.data(),
-                           scale.data()),
+        Frame& fr = clip[f];
+        fr.rgba = read_array<float>(in, ni * 4);
+        fr.tensor = read_array<float>(in, ni * 3);
+        fr.dt = read_array<float>(in, ni);
+        fr.ids = read_array<int32_t>(in, ni);
+        fr.vf = read_array<float>(in, ni * 2);
+        fr.vb = read_array<float>(in, ni * 2);
+        fr.scale = read_array<float>(in, ni * 2);
+        check(pt_set_frame(g_ctx, f, w, h, fr.rgba.data(), fr.tensor.data(), fr.dt.data(), fr.ids.data(),
+                           fr.vf.data(), fr.vb.data(), fr.scale.data()),
               "pt_set_frame");
     }
     std::fclose(in);
@@ -132,11 +142,49 @@ int main(int argc, char** argv) {
     check(pt_get_frame_result(g_ctx, frames - 1, rgba, offs), "pt_get_frame_result");
     std::fwrite(rgba, sizeof(float), no * 4, out);
     std::fwrite(offs, sizeof(pt_patchxf), no, out);
-    std::fclose(out);
     check(pt_host_free(rgba), "pt_host_free");
     check(pt_host_free(offs), "pt_host_free");
     std::printf("capi_clip: %d frames %dx%d, %llu kernel launches\n", frames, w >> fl, h >> fl,
                 (unsigned long long)pt_kernel_launches(g_ctx));
     check(pt_destroy(g_ctx), "pt_destroy");
+    g_ctx = nullptr;
+
+    // the same clip as two requests served at once
+    std::vector<pt_frame_inputs> inputs(frames);
+    for (int f = 0; f < frames; f++) {
+        const Frame& fr = clip[f];
+        inputs[f] = {fr.rgba.data(), fr.tensor.data(), fr.dt.data(), fr.ids.data(),
+                     fr.vf.data(), fr.vb.data(), fr.scale.data()};
+    }
+    const int nreq = 2;
+    std::vector<std::vector<float> > req_rgba(nreq, std::vector<float>(no * 4 * frames));
+    std::vector<std::vector<pt_patchxf> > req_offs(nreq, std::vector<pt_patchxf>(no * frames));
+    std::vector<pt_request> reqs(nreq);
+    for (int r = 0; r < nreq; r++) {
+        pt_request& q = reqs[r];
+        std::memset(&q, 0, sizeof(q));
+        q.params = params;
+        q.style_w = ew;
+        q.style_h = eh;
+        q.style_base = ex_base.data();
+        q.style_output = ex_out.data();
+        q.style_orient_tensor = ex_tensor.data();
+        q.style_dist_trans = ex_dt.data();
+        q.style_ids = ex_ids.data();
+        q.image_w = w;
+        q.image_h = h;
+        q.frames = frames;
+        q.inputs = inputs.data();
+        q.out_rgba = req_rgba[r].data();
+        q.out_offsets = req_offs[r].data();
+        q.arrival_ms = 0.0;
+    }
+    check(pt_serve(0, reqs.data(), nreq, nreq, 0), "pt_serve");
+    for (int r = 0; r < nreq; r++) {
+        check(reqs[r].status, "request");
+        std::fwrite(req_rgba[r].data(), sizeof(float), req_rgba[r].size(), out);
+        std::fwrite(req_offs[r].data(), sizeof(pt_patchxf), req_offs[r].size(), out);
+    }
+    std::fclose(out);
     return 0;
 }

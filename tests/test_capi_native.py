@@ -1,6 +1,7 @@
 """A native C++ caller of the C ABI (tests/capi_clip.cpp): compiled and linked
-against the library on any host; on a GPU it synthesises a clip and its
-results must equal the Python binding's and the oracle's bit for bit."""
+against the library on any host; on a GPU it synthesises a clip, directly and
+as two requests served at once, and every result must equal the Python
+binding's and the oracle's bit for bit."""
 import ctypes
 import os
 import shutil
@@ -48,18 +49,27 @@ def write_input(path, p, ex, clip):
                 f.write(np.ascontiguousarray(fr[k]).tobytes())
 
 
-def read_output(path, frames, w, h):
+def read_output(path, frames, w, h, requests=2):
+    """(per-frame results of the callback, pt_get_frame_result's last frame,
+    per request the served clip's (rgba, offsets) stacks)."""
     raw = np.fromfile(path, np.uint8)
     n = w * h
     per = n * 16 + n * _abi.PATCH_DTYPE.itemsize
-    assert raw.size == (frames + 1) * per
+    assert raw.size == (frames + 1) * per + requests * frames * per
     out = []
     for f in range(frames + 1):
         chunk = raw[f * per:(f + 1) * per]
         rgba = chunk[:n * 16].view(np.float32).reshape(h, w, 4)
         offs = chunk[n * 16:].view(_abi.PATCH_DTYPE).reshape(h, w)
         out.append((rgba, offs))
-    return out[:frames], out[frames]
+    served, off = [], (frames + 1) * per
+    for _ in range(requests):
+        rgba = raw[off:off + frames * n * 16].view(np.float32).reshape(frames, h, w, 4)
+        off += frames * n * 16
+        offs = raw[off:off + frames * n * _abi.PATCH_DTYPE.itemsize].view(_abi.PATCH_DTYPE).reshape(frames, h, w)
+        off += frames * n * _abi.PATCH_DTYPE.itemsize
+        served.append((rgba, offs))
+    return out[:frames], out[frames], served
 
 
 @pytest.mark.gpu
@@ -76,7 +86,7 @@ def test_native_consumer_matches_python_binding_and_oracle(tmp_path):
     write_input(inp, p, ex, clip)
     run = subprocess.run([exe, inp, outp], capture_output=True, text=True, timeout=300)
     assert run.returncode == 0, run.stdout + run.stderr
-    native, last = read_output(outp, 3, 72, 56)
+    native, last, served = read_output(outp, 3, 72, 56)
 
     s = Synthesizer(device=0)
     try:
@@ -95,3 +105,7 @@ def test_native_consumer_matches_python_binding_and_oracle(tmp_path):
         assert np.abs(native[f][0] - ref[f][2]).max() <= 1e-6
     assert_offsets_equal(last[1], native[2][1], 1.0, "pt_get_frame_result offsets")
     assert_array_equal(last[0], native[2][0], "pt_get_frame_result output")
+    for r, (rgba, offs) in enumerate(served):
+        for f in range(3):
+            assert_offsets_equal(offs[f], native[f][1], 1.0, "served request %d, frame %d offsets" % (r, f))
+            assert_array_equal(rgba[f], native[f][0], "served request %d, frame %d output" % (r, f))
