@@ -5,6 +5,10 @@ seeds createRandomPyramid uses (frame * level) -- produced by libc itself,
 not by the restatement.
 still48.npz: the oracle's result for a 48x48 still (r2, 3 levels, 2
 iterations), a regression lock of the oracle.
+clip40.npz: the oracle's results for a 40x32 three-frame clip with moving
+discs (48x48 exemplar, r2, 2 levels, 2 iterations, temporal coherence 0.5)
+under the FMBM_RM, FBMO and TCTF schedules, a regression lock of the
+temporal paths.
 """
 import ctypes
 import os
@@ -33,6 +37,32 @@ def main():
     offs, res, out = O.OracleDriver(p, [ex], [fr], threads=4).render(0, 0)[0]
     np.savez_compressed(os.path.join(HERE, "still48.npz"), offsets=offs, residual=res, output=out,
                         ex_seed=101, fr_seed=102)
+
+    arrays = {}
+    for name, scheme in CLIP_SCHEMES:
+        results = render_clip(scheme)
+        for f in range(3):
+            offs, res, out = results[f]
+            arrays["%s_offsets_%d" % (name, f)] = offs
+            arrays["%s_output_%d" % (name, f)] = out
+    np.savez_compressed(os.path.join(HERE, "clip40.npz"), **arrays)
+
+
+CLIP_SCHEMES = (("fmbm_rm", 1), ("fbmo", 2), ("tctf", 3))
+
+
+def render_clip(scheme):
+    """The clip40 case: 40x32, 3 frames, 48x48 exemplar, r2, 2 levels,
+    2 iterations, temporal coherence 0.5, the given scheme."""
+    from oracle import oracle as O
+    from painttween_gb300 import _abi, synthetic
+    p = _abi.default_params()
+    p.residualWindowSize, p.levels, p.iterations = 2, 2, 2
+    p.temporalCoherenceWeight = 0.5
+    p.scheme = scheme
+    ex = synthetic.make_exemplar(48, 48, seed=111)
+    clip = synthetic.make_clip(40, 32, 3, 3, seed=112)
+    return O.OracleDriver(p, [ex], clip, threads=4).render(0, 2)
 
 
 if __name__ == "__main__":

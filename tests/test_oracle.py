@@ -109,6 +109,23 @@ def test_oracle_still_matches_golden_fixture():
     assert np.array_equal(out, g["output"])
 
 
+def test_oracle_clip_schemes_match_golden_fixture():
+    """Regression lock of the oracle's temporal paths: a 40x32 three-frame
+    clip under FMBM_RM, FBMO and TCTF (fixture written by
+    tests/golden/make_golden.py)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    g = np.load(os.path.join(GOLDEN, "clip40.npz"))
+    for name, scheme in mg.CLIP_SCHEMES:
+        results = mg.render_clip(scheme)
+        for f in range(3):
+            offs, _, out = results[f]
+            assert np.array_equal(offs.view(np.uint8), g["%s_offsets_%d" % (name, f)].view(np.uint8)), (name, f)
+            assert np.array_equal(out, g["%s_output_%d" % (name, f)]), (name, f)
+
+
 def test_energy_fp32_close_to_fp64():
     p = _abi.default_params()
     p.residualWindowSize, p.levels, p.iterations = 3, 2, 2
