@@ -9,6 +9,9 @@ clip40.npz: the oracle's results for a 40x32 three-frame clip with moving
 discs (48x48 exemplar, r2, 2 levels, 2 iterations, temporal coherence 0.5)
 under the FMBM_RM, FBMO and TCTF schedules, a regression lock of the
 temporal paths.
+keys32.npz: the oracle's results for a 32x24 four-frame clip interpolating
+keyframes 1 and 3 (FMBM_RM, r2, 2 levels, 2 iterations; part of the first
+key left unpainted), a regression lock of the keyframe path.
 """
 import ctypes
 import os
@@ -46,6 +49,30 @@ def main():
             arrays["%s_offsets_%d" % (name, f)] = offs
             arrays["%s_output_%d" % (name, f)] = out
     np.savez_compressed(os.path.join(HERE, "clip40.npz"), **arrays)
+
+    results = render_keyed()
+    np.savez_compressed(os.path.join(HERE, "keys32.npz"),
+                        **{"%s_%d" % (k, f): results[f][i] for f in range(4) for i, k in ((0, "offsets"), (2, "output"))})
+
+
+def render_keyed():
+    """The keys32 case: 32x24, 4 frames, keys 1 and 3, FMBM_RM, r2, 2 levels,
+    2 iterations; the left third of the first key's output is transparent."""
+    from oracle import oracle as O
+    from painttween_gb300 import _abi, synthetic
+    p = _abi.default_params()
+    p.residualWindowSize, p.levels, p.iterations = 2, 2, 2
+    p.scheme = _abi.S_FMBM_RM
+    p.interpolateKeyFrame = 1
+    p.numStyles = 2
+    styles = [synthetic.make_exemplar(32, 24, seed=120 + i) for i in range(2)]
+    out = styles[0]["output"].copy()
+    out[:, : 32 // 3, 3] = 0.0
+    styles[0]["output"] = out
+    clip = synthetic.make_clip(32, 24, 3, 4, seed=122)
+    d = O.OracleDriver(p, styles, clip, threads=4)
+    d.set_keyframes([1, 3])
+    return d.render(0, 3)
 
 
 CLIP_SCHEMES = (("fmbm_rm", 1), ("fbmo", 2), ("tctf", 3))

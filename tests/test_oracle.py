@@ -126,6 +126,21 @@ def test_oracle_clip_schemes_match_golden_fixture():
             assert np.array_equal(out, g["%s_output_%d" % (name, f)]), (name, f)
 
 
+def test_oracle_keyframe_path_matches_golden_fixture():
+    """Regression lock of the oracle's keyframe path: a 32x24 four-frame clip
+    interpolating keys 1 and 3 (fixture written by tests/golden/make_golden.py)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    g = np.load(os.path.join(GOLDEN, "keys32.npz"))
+    results = mg.render_keyed()
+    for f in range(4):
+        offs, _, out = results[f]
+        assert np.array_equal(offs.view(np.uint8), g["offsets_%d" % f].view(np.uint8)), f
+        assert np.array_equal(out, g["output_%d" % f]), f
+
+
 def test_energy_fp32_close_to_fp64():
     p = _abi.default_params()
     p.residualWindowSize, p.levels, p.iterations = 3, 2, 2
