@@ -102,6 +102,7 @@ def lib():
             "pto_ribbon_of": (None, [vp, vp, vp]),
             "pto_in_bounds": (i, [i, i, i, i, i, i]),
             "pto_pixel_wrap": (ctypes.c_longlong, [i, i, i, i]),
+            "pto_to_patchxf": (None, [vp, vp]),
             "pto_random_level_keys": (i, [u32, i, i, i, i, i, vp, vp, vp, vp, i, i, i, i, i, i, i, vp]),
         }
         for name, (res, args) in sig.items():

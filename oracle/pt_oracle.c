@@ -18,7 +18,7 @@
  * references and cudaThreadSynchronize are removed), so no end-to-end
  * reference output can be produced.  Its helper header texSynth_util.h does
  * compile: the pto_basis / pto_new_coord / pto_clamp_to_exemplar / pto_ssd /
- * pto_ribbon_of / pto_rgb_to_lab hooks are checked against it, built for the
+ * pto_ribbon_of / pto_to_patchxf / pto_rgb_to_lab hooks are checked against it, built for the
  * host (g++) and for the GPU (nvcc cubin); pto_pixel_wrap / pto_in_bounds
  * against cudaImageBuffer.h and the pyramids against downsample.cpp, both
  * built for the host.  The glibc rand() restatement is
@@ -969,11 +969,19 @@ void pto_sync(pto* o, int level, int flags) {
     if (!(flags & PT_DONT_UPDATE_RESIDUAL)) pto_update_residual(o, level);
 }
 
+/* toPatchXF, texSynth_util.h:212-214: a packed random texel (x, y, theta,
+ * layer) as a PatchXF with zero hysteresis and unit scale */
+static inline pt_patchxf to_patchxf(f4 r) { return patch(r.x, r.y, r.z, 0.f, f2i(r.w), 1.f, 1.f); }
+void pto_to_patchxf(const float* c, pt_patchxf* out) {
+    f4 r = {c[0], c[1], c[2], c[3]};
+    *out = to_patchxf(r);
+}
+
 /* copyRandomKernel + randomizeOffsets, texSynth_kernel.cu:2044-2059,2100-2109 */
 void pto_randomize(pto* o, int level) {
     FOR_RECT(o, level) {
         f4 r = rnd_texel(o, x, y);
-        o->off_work[(size_t)y * o->W + x] = patch(r.x, r.y, r.z, 0.f, f2i(r.w), 1.f, 1.f);
+        o->off_work[(size_t)y * o->W + x] = to_patchxf(r);
     }
     pto_sync(o, level, 0);
 }
@@ -1690,8 +1698,7 @@ void pto_frame_to_key_ribbon(pto* o, int level, int look_forwards) {
             float ox = rb.x + (float)x, oy = rb.y + (float)y;
             out = patch(ox, oy, screen_to_exemplar_angle(o, x, y, ox, oy, rb.layer), 1.0f, rb.layer, 1.f, 1.f);
         } else {
-            f4 r = rnd_texel(o, x, y); /* copyRandomKernel's toPatchXF */
-            out = patch(r.x, r.y, r.z, 0.f, f2i(r.w), 1.f, 1.f);
+            out = to_patchxf(rnd_texel(o, x, y)); /* copyRandomKernel */
         }
         work[k] = out;
     }

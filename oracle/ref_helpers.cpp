@@ -7,6 +7,8 @@
 // restatement of these helpers against the reference's code itself.  The
 // header's device-only random generator reads threadIdx, which a host build
 // does not declare: a zero index stands in (randFloat is not exported).
+#include <cstring>
+
 #include <cuda_runtime.h>
 static uint3 threadIdx = {0, 0, 0};
 #include "texSynth_util.h"
@@ -43,6 +45,14 @@ float ref_ssd_plain(const float* a, const float* b) {
 void ref_ribbon_of(const float* c, float* xy, int* ts_layer) {
     RibbonP r = toRibbonP(make_float4(c[0], c[1], c[2], c[3]));
     xy[0] = r.x; xy[1] = r.y; ts_layer[0] = r.time_step; ts_layer[1] = r.layer;
+}
+
+// toPatchXF (texSynth_util.h): the random layer's packed texel as a PatchXF,
+// copied out as its 36 bytes.
+int ref_to_patchxf(const float* c, unsigned char* out36) {
+    PatchXF p = toPatchXF(make_float4(c[0], c[1], c[2], c[3]));
+    std::memcpy(out36, &p, sizeof(PatchXF) < 36 ? sizeof(PatchXF) : 36);
+    return (int)sizeof(PatchXF);
 }
 
 // CudaImageBufferDevice::pixelWrap and inBounds (cudaImageBuffer.h) on a

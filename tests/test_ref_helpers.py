@@ -34,6 +34,7 @@ import pytest
 
 from oracle import build as ob
 from oracle import oracle as O
+from painttween_gb300 import _abi
 
 pytestmark = pytest.mark.skipif(
     not os.path.exists(os.path.join(ob.REF_SRC, "texSynth_util.h")),
@@ -61,6 +62,7 @@ def ref():
             "ref_pyramid_int": (i, [vp, i, i, vp]),
             "ref_pixel_wrap": (i, [vp, i, i, i, i]),
             "ref_in_bounds": (i, [i, i, i, i, i, i]),
+            "ref_to_patchxf": (i, [vp, vp]),
         }.items():
             fn = getattr(L, name)
             fn.restype, fn.argtypes = res, args
@@ -237,3 +239,21 @@ def test_pixel_wrap_and_bounds_bit_exact(w, h):
             for y in (-1, 0, 1, 2, (h >> level) - 4, (h >> level) - 1, h >> level, h):
                 for x in (-1, 0, 1, 2, (w >> level) - 4, (w >> level) - 1, w >> level, w):
                     assert R.ref_in_bounds(w, h, x, y, level, border) == OL.pto_in_bounds(w, h, x, y, level, border)
+
+
+def test_random_texel_to_patchxf_bit_exact():
+    """toPatchXF (the random layer's packed texel as a PatchXF: zero
+    hysteresis, unit scale, layer truncated) against the oracle, all 36
+    bytes of the record."""
+    R, OL = ref(), O.lib()
+    rng = np.random.default_rng(17)
+    cases = [np.float32([3.25, 7.5, 0.3, 0.0]), np.float32([0.0, 0.0, -1.2, 2.9]),
+             np.float32([5.5, 1.0, 3.0, -0.5]), np.float32([1.0, 2.0, 0.0, -1.5])]
+    cases += [np.float32([rng.random() * 500, rng.random() * 500, rng.random() * 6 - 3, rng.integers(0, 8)])
+              for _ in range(300)]
+    for c in cases:
+        r = np.zeros(36, np.uint8)
+        o = np.zeros(1, _abi.PATCH_DTYPE)
+        assert R.ref_to_patchxf(_p(c), _p(r)) == 36
+        OL.pto_to_patchxf(_p(c), _p(o))
+        assert r.tobytes() == o.tobytes(), (c, r, o)
