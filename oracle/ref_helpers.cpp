@@ -13,6 +13,9 @@
 static uint3 threadIdx = {0, 0, 0};
 #include "texSynth_util.h"
 #include "cudaImageBuffer.h"
+#include "texSynth_interface.h"
+
+#include <cstddef>
 
 extern "C" {
 
@@ -53,6 +56,74 @@ int ref_to_patchxf(const float* c, unsigned char* out36) {
     PatchXF p = toPatchXF(make_float4(c[0], c[1], c[2], c[3]));
     std::memcpy(out36, &p, sizeof(PatchXF) < 36 ? sizeof(PatchXF) : 36);
     return (int)sizeof(PatchXF);
+}
+
+// TsParameters (texSynth_interface.h): every field the C ABI's pt_params
+// mirrors, in pt_params' order, with its offset and size in the reference's
+// struct.  A name missing from TsParameters fails this file's compilation.
+#define PT_REF_FIELD(f) {#f, (long)offsetof(TsParameters, f), (long)sizeof(((TsParameters*)0)->f)}
+static const struct {
+    const char* name;
+    long offset, size;
+} kParamFields[] = {
+    PT_REF_FIELD(residualWindowSize), PT_REF_FIELD(coherenceWeight), PT_REF_FIELD(distTransWeight),
+    PT_REF_FIELD(lumShiftWeight), PT_REF_FIELD(lumShiftEnable), PT_REF_FIELD(inputAnalogyWeight),
+    PT_REF_FIELD(canvasOutputWeight), PT_REF_FIELD(numStyles), PT_REF_FIELD(offsetsHistogramSlope),
+    PT_REF_FIELD(offsetsHistogramThreshold), PT_REF_FIELD(maxDistortion), PT_REF_FIELD(alphaWeight),
+    PT_REF_FIELD(transparencyOk), PT_REF_FIELD(styleObjIdWeight), PT_REF_FIELD(orientationEnabled),
+    PT_REF_FIELD(colorspace), PT_REF_FIELD(coherenceRatioRange), PT_REF_FIELD(coherenceAngleRange),
+    PT_REF_FIELD(levels), PT_REF_FIELD(scatterSamplesCount), PT_REF_FIELD(advectionJitter),
+    PT_REF_FIELD(timeDerivativeInputWeight), PT_REF_FIELD(timeDerivativeOutputWeight),
+    PT_REF_FIELD(temporalCoherenceWeight), PT_REF_FIELD(hysteresisWeight), PT_REF_FIELD(interpolateKeyFrame),
+    PT_REF_FIELD(useGuide), PT_REF_FIELD(currentInterpolationIndex), PT_REF_FIELD(numFrames),
+    PT_REF_FIELD(numKeyFrames), PT_REF_FIELD(firstKeyIndex), PT_REF_FIELD(lastKeyIndex),
+    PT_REF_FIELD(distTransCull), PT_REF_FIELD(residualWindowScaleU), PT_REF_FIELD(residualWindowScaleV),
+    PT_REF_FIELD(direction),
+};
+#undef PT_REF_FIELD
+
+// TsImageLayer values under the names the C ABI gives them (PT_LAYER_<name>)
+#define PT_REF_LAYER(n) {#n, (long)TS_LAYER_##n}
+static const struct {
+    const char* name;
+    long value;
+} kLayers[] = {
+    PT_REF_LAYER(EXEMPLAR_BASE), PT_REF_LAYER(EXEMPLAR_OUTPUT), PT_REF_LAYER(EXEMPLAR_ORIENTATION),
+    PT_REF_LAYER(EXEMPLAR_DIST_TRANS), PT_REF_LAYER(EXEMPLAR_OBJECT_IDS), PT_REF_LAYER(INPUT_COLOR),
+    PT_REF_LAYER(INPUT_ORIENTATION), PT_REF_LAYER(INPUT_DIST_TRANS), PT_REF_LAYER(INPUT_SCALE),
+    PT_REF_LAYER(INPUT_ID), PT_REF_LAYER(INPUT_SURF_ID), PT_REF_LAYER(INPUT_VEL_B), PT_REF_LAYER(INPUT_VEL_F),
+    PT_REF_LAYER(INPUT_VEL_B_PREVIOUS), PT_REF_LAYER(INPUT_VEL_F_PREVIOUS), PT_REF_LAYER(GUIDE_B),
+    PT_REF_LAYER(GUIDE_F), PT_REF_LAYER(CUMUL_FIELD_B), PT_REF_LAYER(CUMUL_FIELD_F),
+    PT_REF_LAYER(FRAME_TO_KEY_RIBBON_B), PT_REF_LAYER(FRAME_TO_KEY_RIBBON_F), PT_REF_LAYER(RANDOM),
+};
+#undef PT_REF_LAYER
+
+// i-th entry of the tables above; each returns the table's length
+int ref_param_field(int i, const char** name, long* offset, long* size) {
+    const int n = (int)(sizeof(kParamFields) / sizeof(kParamFields[0]));
+    if (i >= 0 && i < n) {
+        *name = kParamFields[i].name;
+        *offset = kParamFields[i].offset;
+        *size = kParamFields[i].size;
+    }
+    return n;
+}
+int ref_layer(int i, const char** name, long* value) {
+    const int n = (int)(sizeof(kLayers) / sizeof(kLayers[0]));
+    if (i >= 0 && i < n) {
+        *name = kLayers[i].name;
+        *value = kLayers[i].value;
+    }
+    return n;
+}
+// NUM_MAX_STYLES, sizeof(TsParameters), and PassDirection's FORWARD,
+// BACKWARD, BIDIRECTIONAL
+void ref_param_constants(long* out5) {
+    out5[0] = NUM_MAX_STYLES;
+    out5[1] = (long)sizeof(TsParameters);
+    out5[2] = FORWARD;
+    out5[3] = BACKWARD;
+    out5[4] = BIDIRECTIONAL;
 }
 
 // CudaImageBufferDevice::pixelWrap and inBounds (cudaImageBuffer.h) on a

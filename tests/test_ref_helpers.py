@@ -63,6 +63,10 @@ def ref():
             "ref_pixel_wrap": (i, [vp, i, i, i, i]),
             "ref_in_bounds": (i, [i, i, i, i, i, i]),
             "ref_to_patchxf": (i, [vp, vp]),
+            "ref_param_field": (i, [i, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_long),
+                                    ctypes.POINTER(ctypes.c_long)]),
+            "ref_layer": (i, [i, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_long)]),
+            "ref_param_constants": (None, [vp]),
         }.items():
             fn = getattr(L, name)
             fn.restype, fn.argtypes = res, args
@@ -257,3 +261,46 @@ def test_random_texel_to_patchxf_bit_exact():
         assert R.ref_to_patchxf(_p(c), _p(r)) == 36
         OL.pto_to_patchxf(_p(c), _p(o))
         assert r.tobytes() == o.tobytes(), (c, r, o)
+
+
+def test_params_mirror_tsparameters_field_for_field():
+    """pt_params lists TsParameters' fields (texSynth_interface.h) by name and
+    in order, each the same size except the reference's bools, which are
+    int32 here; the fields after them are this library's own.  The style
+    limit and PassDirection's values are the reference's."""
+    R = ref()
+    name, off, size = ctypes.c_char_p(), ctypes.c_long(), ctypes.c_long()
+    n = R.ref_param_field(0, ctypes.byref(name), ctypes.byref(off), ctypes.byref(size))
+    ref_fields = []
+    for k in range(n):
+        R.ref_param_field(k, ctypes.byref(name), ctypes.byref(off), ctypes.byref(size))
+        ref_fields.append((name.value.decode(), off.value, size.value))
+    ours = [(f[0], ctypes.sizeof(f[1])) for f in _abi.Params._fields_]
+    assert [f[0] for f in ref_fields] == [f[0] for f in ours[:n]]
+    offsets = [f[1] for f in ref_fields]
+    assert offsets == sorted(offsets) and len(set(offsets)) == n  # declaration order in the reference
+    bools = {"lumShiftEnable", "transparencyOk", "orientationEnabled", "interpolateKeyFrame", "useGuide"}
+    for (nm, _, rsize), (_, osize) in zip(ref_fields, ours):
+        assert rsize == (1 if nm in bools else osize), (nm, rsize, osize)
+    consts = (ctypes.c_long * 5)()
+    R.ref_param_constants(consts)
+    assert consts[0] == _abi.PT_MAX_STYLES
+    assert (consts[2], consts[3], consts[4]) == (0, 1, 2)  # PT_FORWARD, PT_BACKWARD, PT_BIDIRECTIONAL
+
+
+def test_layer_numbers_are_tsimagelayer_values():
+    """Every PT_LAYER_<name> of include/painttween.h has the value of the
+    reference's TS_LAYER_<name> (texSynth_interface.h)."""
+    import re
+    header = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                               "painttween.h")).read()
+    ours = {m.group(1): int(m.group(2)) for m in re.finditer(r"PT_LAYER_([A-Z0-9_]+)\s*=\s*(\d+)", header)}
+    R = ref()
+    name, value = ctypes.c_char_p(), ctypes.c_long()
+    n = R.ref_layer(0, ctypes.byref(name), ctypes.byref(value))
+    theirs = {}
+    for k in range(n):
+        R.ref_layer(k, ctypes.byref(name), ctypes.byref(value))
+        theirs[name.value.decode()] = value.value
+    assert set(ours) == set(theirs)
+    assert ours == theirs
