@@ -1,6 +1,7 @@
 // qt_shim_core.h -- the few QtCore containers that the reference's
 // downsample.cpp uses (QVector, QList, QHash, QMap and their Java-style
-// iterators), over the standard library, so that file compiles for the
+// iterators), over the standard library, plus empty QString / QStringList /
+// QFile types that its headers name, so that those files compile for the
 // oracle's reference checks without Qt.  Test infrastructure only.
 //
 // Semantics kept: QVector(n) value-initialises; insert() on QHash/QMap
@@ -51,6 +52,16 @@ public:
 private:
     std::vector<T> v_;
 };
+
+// Declaration-level stand-ins: the reference's headers name these types in
+// signatures and members; nothing here calls into them.
+class QString {
+public:
+    QString() {}
+    QString(const char*) {}
+};
+class QStringList : public QList<QString> {};
+class QFile {};
 
 template <class K, class V>
 class QHash {

@@ -14,6 +14,7 @@ static uint3 threadIdx = {0, 0, 0};
 #include "texSynth_util.h"
 #include "cudaImageBuffer.h"
 #include "texSynth_interface.h"
+#include "texSynth_kernel.h"
 
 #include <cstddef>
 
@@ -116,6 +117,21 @@ int ref_layer(int i, const char** name, long* value) {
     }
     return n;
 }
+// TexSynth's syncBuffers / merge and advect flags (texSynth_kernel.h):
+// DONT_COPY_OFFSETS, DONT_UPDATE_RESIDUAL, MERGE_FALLBACK_RANDOM,
+// MERGE_FALLBACK_LAST_PASS, ADVECT_IGNORE_RANDOM, ADVECT_DO_NOT_CHECK_PREVIOUS,
+// ADVECT_CHECK_FRAME_TO_KEY, ADVECT_UPDATE_RESIDUAL
+void ref_flags(long* out8) {
+    out8[0] = TexSynth::DONT_COPY_OFFSETS;
+    out8[1] = TexSynth::DONT_UPDATE_RESIDUAL;
+    out8[2] = TexSynth::MERGE_FALLBACK_RANDOM;
+    out8[3] = TexSynth::MERGE_FALLBACK_LAST_PASS;
+    out8[4] = TexSynth::ADVECT_IGNORE_RANDOM;
+    out8[5] = TexSynth::ADVECT_DO_NOT_CHECK_PREVIOUS;
+    out8[6] = TexSynth::ADVECT_CHECK_FRAME_TO_KEY;
+    out8[7] = TexSynth::ADVECT_UPDATE_RESIDUAL;
+}
+
 // NUM_MAX_STYLES, sizeof(TsParameters), and PassDirection's FORWARD,
 // BACKWARD, BIDIRECTIONAL
 void ref_param_constants(long* out5) {

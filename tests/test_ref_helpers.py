@@ -67,6 +67,7 @@ def ref():
                                     ctypes.POINTER(ctypes.c_long)]),
             "ref_layer": (i, [i, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_long)]),
             "ref_param_constants": (None, [vp]),
+            "ref_flags": (None, [vp]),
         }.items():
             fn = getattr(L, name)
             fn.restype, fn.argtypes = res, args
@@ -304,3 +305,18 @@ def test_layer_numbers_are_tsimagelayer_values():
         theirs[name.value.decode()] = value.value
     assert set(ours) == set(theirs)
     assert ours == theirs
+
+
+def test_sync_advect_merge_flags_are_the_references():
+    """PT_DONT_COPY_OFFSETS ... PT_ADVECT_UPDATE_RESIDUAL have the values of
+    TexSynth's flags (texSynth_kernel.h), so callers pass the same constants."""
+    import re
+    header = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                               "painttween.h")).read()
+    ours = {m.group(1): int(m.group(2), 16) for m in re.finditer(r"PT_([A-Z_]+)\s*=\s*(0x[0-9a-fA-F]+)", header)}
+    names = ["DONT_COPY_OFFSETS", "DONT_UPDATE_RESIDUAL", "MERGE_FALLBACK_RANDOM", "MERGE_FALLBACK_LAST_PASS",
+             "ADVECT_IGNORE_RANDOM", "ADVECT_DO_NOT_CHECK_PREVIOUS", "ADVECT_CHECK_FRAME_TO_KEY",
+             "ADVECT_UPDATE_RESIDUAL"]
+    vals = (ctypes.c_long * 8)()
+    ref().ref_flags(vals)
+    assert {n: ours[n] for n in names} == dict(zip(names, vals))
