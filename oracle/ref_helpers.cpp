@@ -132,6 +132,28 @@ void ref_flags(long* out8) {
     out8[7] = TexSynth::ADVECT_UPDATE_RESIDUAL;
 }
 
+// PatchXF's and RibbonP's layouts (types.h): sizeof, then the offsets of
+// x, y, theta, hysteresis, layer, scaleU, scaleV, luminanceShift.y,
+// luminanceShift.a; then sizeof(RibbonP) and the offsets of x, y,
+// time_step, layer
+void ref_record_layouts(long* out15) {
+    out15[0] = (long)sizeof(PatchXF);
+    out15[1] = (long)offsetof(PatchXF, x);
+    out15[2] = (long)offsetof(PatchXF, y);
+    out15[3] = (long)offsetof(PatchXF, theta);
+    out15[4] = (long)offsetof(PatchXF, hysteresis);
+    out15[5] = (long)offsetof(PatchXF, layer);
+    out15[6] = (long)offsetof(PatchXF, scaleU);
+    out15[7] = (long)offsetof(PatchXF, scaleV);
+    out15[8] = (long)(offsetof(PatchXF, luminanceShift) + offsetof(Luminance, y));
+    out15[9] = (long)(offsetof(PatchXF, luminanceShift) + offsetof(Luminance, a));
+    out15[10] = (long)sizeof(RibbonP);
+    out15[11] = (long)offsetof(RibbonP, x);
+    out15[12] = (long)offsetof(RibbonP, y);
+    out15[13] = (long)offsetof(RibbonP, time_step);
+    out15[14] = (long)offsetof(RibbonP, layer);
+}
+
 // NUM_MAX_STYLES, sizeof(TsParameters), and PassDirection's FORWARD,
 // BACKWARD, BIDIRECTIONAL
 void ref_param_constants(long* out5) {

@@ -68,6 +68,7 @@ def ref():
             "ref_layer": (i, [i, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_long)]),
             "ref_param_constants": (None, [vp]),
             "ref_flags": (None, [vp]),
+            "ref_record_layouts": (None, [vp]),
         }.items():
             fn = getattr(L, name)
             fn.restype, fn.argtypes = res, args
@@ -320,3 +321,18 @@ def test_sync_advect_merge_flags_are_the_references():
     vals = (ctypes.c_long * 8)()
     ref().ref_flags(vals)
     assert {n: ours[n] for n in names} == dict(zip(names, vals))
+
+
+def test_patchxf_and_ribbon_records_have_the_references_layout():
+    """pt_patchxf is PatchXF byte for byte (36 bytes, same field offsets) and
+    pt_ribbon is RibbonP (types.h), so the reference's QVector<PatchXF> and
+    QVector<RibbonP> buffers pass through the C ABI as they are."""
+    v = (ctypes.c_long * 15)()
+    ref().ref_record_layouts(v)
+    pf = _abi.PATCH_DTYPE.fields
+    assert v[0] == _abi.PATCH_DTYPE.itemsize == 36
+    names = ["x", "y", "theta", "hysteresis", "layer", "scaleU", "scaleV", "lumShiftY", "lumShiftA"]
+    assert [v[1 + k] for k in range(9)] == [pf[n][1] for n in names]
+    rf = _abi.RIBBON_DTYPE.fields
+    assert v[10] == _abi.RIBBON_DTYPE.itemsize == 16
+    assert [v[11 + k] for k in range(4)] == [rf[n][1] for n in ("x", "y", "time_step", "layer")]
