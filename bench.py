@@ -257,7 +257,8 @@ def run_reference(args, dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * frames / fps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "frames": frames, "image": "1920x1080", "exemplar": "1024x1024",
-                   "patch_radius": p.residualWindowSize, "levels": p.levels, "iterations": p.iterations},
+                   "patch_radius": p.residualWindowSize, "levels": p.levels, "iterations": p.iterations,
+                   "scheme": "FMBM_RM", "histogram": True, "parallelism": "host threads"},
         "cpu_baseline": {"value": fps, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": desc + "; frames/s = evaluations/s / evaluations per frame of the schedule"},
         "e2e": {"value": fps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
