@@ -314,6 +314,13 @@ pt_status pt_get_output(pt_ctx* ctx, int level, float* out_rgba);
 pt_status pt_convolve_separable(pt_ctx* ctx, const float* src_dev, float* dst_dev, int w, int h, int pitch,
                                 int radius);
 
+/* The Gaussian weights allocateGaussianKernel (convolution.cu:37-60)
+ * uploads: 2*radius+1 floats into `out` (host memory), sigma = radius / 3,
+ * unnormalised (the patch-distance window) or, with `normalize`, divided by
+ * sqrt(2*pi)*sigma (the histogram smoothing of pt_convolve_separable).
+ * Host-only: no device is used. */
+pt_status pt_gaussian_kernel(int radius, int normalize, float* out);
+
 /* Allocation-free variant of pt_convolve_separable, for callers that cannot
  * allocate device memory when they call it (a plugin host that owns all
  * device memory through its own pool and forbids cudaMalloc in its frame
@@ -327,8 +334,13 @@ pt_status pt_convolve_separable(pt_ctx* ctx, const float* src_dev, float* dst_de
  *    which every GPU that loads the library holds until the process exits.
  *    pitch * h above that limit returns PT_ERR_INVALID.  Nothing is
  *    allocated or freed by the call.
- *  - The first call on a device looks up the array's device address (once
- *    per device); make that first call outside any stream capture.
+ *  - Every call looks up the array's device address in the current
+ *    device's context (cudaGetSymbolAddress), so the address stays right
+ *    after a cudaDeviceReset.  The first call on a device also loads the
+ *    library's device code there; make that first call outside any stream
+ *    capture.
+ *  - A CUDA error already pending on the calling thread is left in place
+ *    and the call returns PT_ERR_CUDA without launching anything.
  *  - All calls share the one array and it keeps the last call's contents:
  *    calls that overlap on the GPU (different streams, or different host
  *    threads on one device) race on it and must be serialised by the caller.

@@ -43,7 +43,16 @@ def build(force=False, verbose=False):
     return OUT
 
 
-REF_SRC = os.environ.get("PT_REFERENCE_SRC", "/root/reference/src/PaintTweenCUDA")
+def _reference_src():
+    """The reference's src/PaintTweenCUDA: $PT_REFERENCE_SRC, else a
+    `reference` tree beside this repository."""
+    env = os.environ.get("PT_REFERENCE_SRC")
+    if env:
+        return env
+    return os.path.normpath(os.path.join(HERE, "..", "..", "reference", "src", "PaintTweenCUDA"))
+
+
+REF_SRC = _reference_src()
 REF_SHIM = os.path.join(HERE, "ref_helpers.cpp")
 REF_DOWNSAMPLE_SHIM = os.path.join(HERE, "ref_downsample.cpp")
 QT_SHIM = os.path.join(HERE, "qt_shim")
@@ -61,6 +70,7 @@ def build_ref(force=False, verbose=False):
     if (not force and os.path.exists(REF_OUT)
             and all(os.path.getmtime(REF_OUT) >= os.path.getmtime(d) for d in deps)):
         build_ref_cubin(verbose=verbose)
+        build_ref_gauss(verbose=verbose)
         return REF_OUT
     cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
     os.makedirs(os.path.dirname(REF_OUT), exist_ok=True)
@@ -75,7 +85,33 @@ def build_ref(force=False, verbose=False):
     subprocess.check_call(cmd)
     os.replace(REF_OUT + ".tmp", REF_OUT)
     build_ref_cubin(force=force, verbose=verbose)
+    build_ref_gauss(force=force, verbose=verbose)
     return REF_OUT
+
+
+REF_GAUSS_SHIM = os.path.join(HERE, "ref_gauss.cu")
+REF_GAUSS_OUT = os.path.join(HERE, "_ref", "libref_gauss.so")
+
+
+def build_ref_gauss(force=False, verbose=False):
+    """oracle/_ref/libref_gauss.so: the reference's allocateGaussianKernel
+    (convolution.cu) compiled for the host by nvcc over the QtCore container
+    shim, or None without the reference tree."""
+    if not os.path.exists(os.path.join(REF_SRC, "convolution.cu")):
+        return None
+    if (not force and os.path.exists(REF_GAUSS_OUT)
+            and os.path.getmtime(REF_GAUSS_OUT) >= os.path.getmtime(REF_GAUSS_SHIM)):
+        return REF_GAUSS_OUT
+    nvcc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+    os.makedirs(os.path.dirname(REF_GAUSS_OUT), exist_ok=True)
+    cmd = [nvcc, "-shared", "-Xcompiler", "-fPIC", "-gencode", "arch=compute_103a,code=sm_103a", "-w",
+           "-I", QT_SHIM, "-I", os.path.join(QT_SHIM, "QtCore"), "-I", REF_SRC, REF_GAUSS_SHIM,
+           "-o", REF_GAUSS_OUT + ".tmp"]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd)
+    os.replace(REF_GAUSS_OUT + ".tmp", REF_GAUSS_OUT)
+    return REF_GAUSS_OUT
 
 
 REF_DEV_SHIM = os.path.join(HERE, "ref_helpers_dev.cu")

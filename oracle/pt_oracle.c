@@ -898,6 +898,20 @@ static void offsets_to_output(pto* o, int level) {
 
 /* separable Gaussian, convolution.cu:76-210 (normalised weights, zero
  * apron); the smoothed histogram is input to histogramTerm. */
+/* allocateGaussianKernel, convolution.cu:37-60: sigma = r/3 in float, the
+ * exponential in float, and with `normalize` the division by
+ * sqrt(2*pi)*sigma in double (M_PI promotes the expression), rounded back
+ * to float.  kern has 2r+1 entries. */
+static void gauss_weights(int r, int normalize, float* kern) {
+    float sigma = (float)r / 3.0f, s2 = sigma * sigma;
+    for (int i = 0; i <= r; i++) {
+        float wgt = expf(-(float)(i * i) / (2.f * s2));
+        if (normalize) wgt = (float)((double)wgt / (sqrt(2.0 * M_PI) * (double)sigma));
+        kern[r + i] = wgt; kern[r - i] = wgt;
+    }
+}
+void pto_gauss_weights(int r, int normalize, float* kern) { gauss_weights(r, normalize, kern); }
+
 static void conv_pass(pto* o, const float* src, float* dst, int w, int h, int rows, const float* kern, int r) {
     for (int y = 0; y < h; y++)
         for (int x = 0; x < w; x++) {
@@ -914,12 +928,7 @@ static void conv_pass(pto* o, const float* src, float* dst, int w, int h, int ro
 /* convolutionRowsGPU + convolutionColumnsGPU on one w x h image (pitch w) */
 void pto_convolve_separable(const float* src, float* dst, int w, int h, int r) {
     float kern[64];
-    float sigma = (float)r / 3.0f, s2 = sigma * sigma;
-    for (int i = 0; i <= r; i++) {
-        float wgt = expf(-(float)(i * i) / (2.f * s2));
-        wgt = wgt / (sqrtf(2.f * (float)M_PI) * sigma);
-        kern[r + i] = wgt; kern[r - i] = wgt;
-    }
+    gauss_weights(r, 1, kern);
     float* tmp = (float*)malloc(sizeof(float) * (size_t)w * h);
     for (int pass = 0; pass < 2; pass++) {
         const float* s = pass ? tmp : src;
@@ -953,12 +962,7 @@ void pto_sync(pto* o, int level, int flags) {
         /* calculateOffsetsHistogram adds nothing (:258 is commented out) */
         int r = o->p.residualWindowSize;
         float kern[64];
-        float sigma = (float)r / 3.0f, s2 = sigma * sigma;
-        for (int i = 0; i <= r; i++) {
-            float wgt = expf(-(float)(i * i) / (2.f * s2));
-            wgt = wgt / (sqrtf(2.f * (float)M_PI) * sigma);
-            kern[r + i] = wgt; kern[r - i] = wgt;
-        }
+        gauss_weights(r, 1, kern);
         int w = o->SW >> level, h = (o->SH * o->NS) >> level;
         /* convolutionRowsGPU(dst = working, src = base), then
          * convolutionColumnsGPU(dst = base, src = working) */
@@ -1323,11 +1327,7 @@ void pto_set_threads(pto* o, int n) { o->threads = n < 1 ? 1 : n; }
 void pto_set_params(pto* o, const pt_params* p) {
     o->p = *p;
     int r = p->residualWindowSize;
-    float sigma = (float)r / 3.0f, s2 = sigma * sigma;
-    for (int i = 0; i <= r && i < 32; i++) {
-        float w = expf(-(float)(i * i) / (2.f * s2));
-        o->gauss[r + i] = w; o->gauss[r - i] = w;
-    }
+    if (r >= 0 && r < 32) gauss_weights(r, 0, o->gauss);
 }
 
 void pto_init_exemplars(pto* o, int ew, int eh, int ns) {

@@ -63,6 +63,7 @@ SIGNATURES = {
     "pt_get_residual": (_I, [_VP, _I, _VP]),
     "pt_get_output": (_I, [_VP, _I, _VP]),
     "pt_convolve_separable": (_I, [_VP, _VP, _VP, _I, _I, _I, _I]),
+    "pt_gaussian_kernel": (_I, [_I, _I, _VP]),
     "pt_convolve_separable_noalloc": (_I, [_VP, _VP, _I, _I, _I, _I, _VP]),
     "pt_set_style": (_I, [_VP, _I, _I, _I, _VP, _VP, _VP, _VP, _VP]),
     "pt_set_frame": (_I, [_VP, _I, _I, _I, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),

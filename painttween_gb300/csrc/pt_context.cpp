@@ -804,16 +804,9 @@ pt_status pt_set_params(pt_ctx* c, const pt_params* p) {
     // TexSynth::setup: unnormalised Gaussian with sigma = r/3
     // (allocateGaussianKernel(..., normalize=false), convolution.cu:37-60)
     int r = p->residualWindowSize;
-    float sigma = (float)r / 3.0f, s2 = sigma * sigma;
-    c->hist_kernel.r = r;
-    for (int i = 0; i <= r; i++) {
-        float w = expf(-(float)(i * i) / (2.f * s2));
-        c->gauss[r + i] = w;
-        c->gauss[r - i] = w;
-        float wn = w / (sqrtf(2.f * (float)M_PI) * sigma);  // normalised copy for the histogram
-        c->hist_kernel.w[r + i] = wn;
-        c->hist_kernel.w[r - i] = wn;
-    }
+    pt::gaussian_weights(r, false, c->gauss);
+    c->hist_kernel.r = r;  // normalised copy for the histogram smoothing
+    pt::gaussian_weights(r, true, c->hist_kernel.w);
     return PT_OK;
 }
 
@@ -1512,17 +1505,11 @@ pt_status pt_get_output(pt_ctx* c, int level, float* out) {
     return get_plane(c, level, (const float*)c->canvas, 4, out);
 }
 
-// normalised Gaussian of radius r (allocateGaussianKernel(..., normalize=true),
-// convolution.cu:37-60)
-static void normalized_gaussian(int r, ConvKernel* k) {
-    float sigma = (float)r / 3.0f, s2 = sigma * sigma;
-    k->r = r;
-    for (int i = 0; i <= r; i++) {
-        float w = expf(-(float)(i * i) / (2.f * s2));
-        w = w / (sqrtf(2.f * (float)M_PI) * sigma);
-        k->w[r + i] = w;
-        k->w[r - i] = w;
-    }
+
+pt_status pt_gaussian_kernel(int radius, int normalize, float* out) {
+    if (!out || radius < 0 || radius > ptk::kMaxRadius) return PT_ERR_INVALID;
+    pt::gaussian_weights(radius, normalize != 0, out);
+    return PT_OK;
 }
 
 pt_status pt_convolve_separable(pt_ctx* c, const float* src, float* dst, int w, int h, int pitch, int radius) {
@@ -1538,7 +1525,8 @@ pt_status pt_convolve_separable(pt_ctx* c, const float* src, float* dst, int w, 
         c->conv_scratch_elems = n;
     }
     ConvKernel k;
-    normalized_gaussian(radius, &k);
+    k.r = radius;
+    pt::gaussian_weights(radius, true, k.w);
     LN(pt::launch_conv(src, c->conv_scratch, w, h, pitch, 1, k, c->stream));
     LN(pt::launch_conv(c->conv_scratch, dst, w, h, pitch, 0, k, c->stream));
     return PT_OK;

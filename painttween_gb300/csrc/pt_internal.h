@@ -1,12 +1,28 @@
 // pt_internal.h -- launchers shared by the kernel and host translation units.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 
 #include "pt_types.h"
 
 namespace pt {
+
+// Gaussian weights of radius r, sigma = r / 3, as allocateGaussianKernel
+// (src/PaintTweenCUDA/convolution.cu:37-60) forms them: the exponential in
+// float, and with `normalize` the division by sqrt(2*pi)*sigma in double
+// (M_PI promotes the expression) rounded back to float.  w has 2r+1 entries.
+inline void gaussian_weights(int r, bool normalize, float* w) {
+    float sigma = (float)r / 3.0f, s2 = sigma * sigma;
+    for (int i = 0; i <= r; i++) {
+        float v = expf(-(float)(i * i) / (2.f * s2));
+        if (normalize) v = (float)((double)v / (std::sqrt(2.0 * M_PI) * (double)sigma));
+        w[r + i] = v;
+        w[r - i] = v;
+    }
+}
+
 using ptk::Arr;
 using ptk::ConvKernel;
 using ptk::ExView;

@@ -10,9 +10,6 @@
 // that intermediate image in a fixed array in the library's own device
 // memory, so a call allocates nothing: the caller passes its own input and
 // output buffers and a stream.
-#include <cmath>
-#include <mutex>
-
 #include <cuda_runtime.h>
 
 #include "painttween.h"
@@ -23,49 +20,24 @@
 // PT_NOALLOC_MAX_PIXELS floats (4 MiB) until the process exits.
 static __device__ __align__(256) float g_noalloc_scratch[PT_NOALLOC_MAX_PIXELS];
 
-namespace {
-
-// Device address of g_noalloc_scratch per device ordinal, looked up once per
-// device.  In host code the array's name is only a host-side stand-in, so a
-// kernel must be given this address, never the name.
-constexpr int kMaxDevices = 64;
-float* g_scratch_addr[kMaxDevices] = {};
-std::mutex g_scratch_mu;
-
-cudaError_t scratch_address(int device, float** out) {
-    if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_addr[device]) {
-        float* ptr = nullptr;
-        cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch);  // with `device` current
-        if (e != cudaSuccess) return e;
-        g_scratch_addr[device] = ptr;
-    }
-    *out = g_scratch_addr[device];
-    return cudaSuccess;
-}
-
-}  // namespace
-
 pt_status pt_convolve_separable_noalloc(const float* src_dev, float* dst_dev, int w, int h, int pitch, int radius,
                                         void* stream) {
     if (!src_dev || !dst_dev || w < 1 || h < 1 || pitch < w || radius < 1 || radius > ptk::kMaxRadius)
         return PT_ERR_INVALID;
     if ((size_t)pitch * (size_t)h > (size_t)PT_NOALLOC_MAX_PIXELS) return PT_ERR_INVALID;  // beyond the fixed array
-    int device = 0;
-    if (cudaGetDevice(&device) != cudaSuccess) return PT_ERR_CUDA;
+    // An error left pending on this thread by earlier work is not ours to
+    // report or to clear: refuse the call and leave it for the caller.
+    if (cudaPeekAtLastError() != cudaSuccess) return PT_ERR_CUDA;
+    // Device address of the array in the current device's context.  In host
+    // code the array's name is only a host-side stand-in, so the kernels are
+    // given this address.  It is looked up on every call (cheap once the
+    // module is loaded), so it stays valid after the caller resets the device
+    // and the module is loaded again.
     float* scratch = nullptr;
-    if (scratch_address(device, &scratch) != cudaSuccess) return PT_ERR_CUDA;
-    // normalised Gaussian, sigma = radius / 3 (convolution.cu:37-60)
+    if (cudaGetSymbolAddress((void**)&scratch, g_noalloc_scratch) != cudaSuccess || !scratch) return PT_ERR_CUDA;
     ptk::ConvKernel k;
     k.r = radius;
-    float sigma = (float)radius / 3.0f, s2 = sigma * sigma;
-    for (int i = 0; i <= radius; i++) {
-        float wgt = expf(-(float)(i * i) / (2.f * s2));
-        wgt = wgt / (sqrtf(2.f * (float)M_PI) * sigma);
-        k.w[radius + i] = wgt;
-        k.w[radius - i] = wgt;
-    }
+    pt::gaussian_weights(radius, true, k.w);  // normalised, sigma = radius / 3
     // every scratch element the column pass reads is written by the row pass
     // first, so nothing has to be cleared between calls
     cudaStream_t s = static_cast<cudaStream_t>(stream);

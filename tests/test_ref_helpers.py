@@ -336,3 +336,30 @@ def test_patchxf_and_ribbon_records_have_the_references_layout():
     rf = _abi.RIBBON_DTYPE.fields
     assert v[10] == _abi.RIBBON_DTYPE.itemsize == 16
     assert [v[11 + k] for k in range(4)] == [rf[n][1] for n in ("x", "y", "time_step", "layer")]
+
+
+def test_gaussian_weights_bit_exact_with_reference_allocate_gaussian_kernel(gpu_lib):
+    """allocateGaussianKernel (convolution.cu:37-60), compiled from the
+    reference's own source for the host, against the oracle's weights and the
+    library's (pt_gaussian_kernel), unnormalised (the patch window) and
+    normalised (the histogram smoothing), for every radius the library
+    takes."""
+    path = ob.build_ref_gauss()
+    assert path is not None
+    R = ctypes.CDLL(path)
+    R.ref_gaussian_kernel.restype = ctypes.c_int
+    R.ref_gaussian_kernel.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    L = O.lib()
+    L.pto_gauss_weights.restype = None
+    L.pto_gauss_weights.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    for r in range(1, 16):
+        for norm in (0, 1):
+            ref = np.zeros(64, np.float32)
+            n = R.ref_gaussian_kernel(r, norm, _p(ref))
+            assert n == 2 * r + 1
+            orc = np.zeros(2 * r + 1, np.float32)
+            L.pto_gauss_weights(r, norm, _p(orc))
+            lib = np.zeros(2 * r + 1, np.float32)
+            assert gpu_lib.pt_gaussian_kernel(r, norm, _p(lib)) == 0
+            assert np.array_equal(ref[:n].view(np.uint32), orc.view(np.uint32)), (r, norm)
+            assert np.array_equal(ref[:n].view(np.uint32), lib.view(np.uint32)), (r, norm)
