@@ -83,6 +83,19 @@ enum { PT_S_FMBM = 0, PT_S_FMBM_RM = 1, PT_S_FBMO = 2, PT_S_TCTF = 3, PT_S_IND =
  *    for both the random pyramid and a real random search. */
 enum { PT_RNG_REFERENCE = 0, PT_RNG_COUNTER = 1 };
 
+/* Filtering of the linearly filtered inputs (exemplar colours and distance
+ * transform, image colours, distance transform, velocities and scale,
+ * keyframe ribbon fields), which the reference fetches through the texture
+ * unit with bilinear filtering (texSynth_kernel.cu:2120-2253).
+ *  PT_FILTER_TEXTURE: the texture unit's own arithmetic, as measured on
+ *    GB300: weights quantised to 1/256 (round half up of the fractions,
+ *    w11 = round(a*b), the others by difference), texels aligned to the
+ *    largest exponent and truncated to 28 bits, the weighted sum rounded
+ *    half away from zero, subnormal texels read as zero.  The exemplar
+ *    colour samples of the tiled kernels go through the texture unit itself.
+ *  PT_FILTER_EXACT: bilinear weights and sums in exact FP32 arithmetic. */
+enum { PT_FILTER_EXACT = 0, PT_FILTER_TEXTURE = 1 };
+
 /* Field-for-field copy of TsParameters (texSynth_interface.h:79-152); C bools
  * are int32 here.  The trailing fields are this library's additions. */
 typedef struct {
@@ -129,7 +142,8 @@ typedef struct {
     int32_t finalLevel;
     int32_t rngMode;     /* PT_RNG_* */
     uint32_t rngSeed;    /* seed of PT_RNG_COUNTER */
-    int32_t reserved[6];
+    int32_t filterMode;  /* PT_FILTER_* */
+    int32_t reserved[5];
 } pt_params;
 
 /* Image layers (TsImageLayer, texSynth_interface.h:53-77, in-scope subset;

@@ -104,6 +104,8 @@ def lib():
             "pto_pixel_wrap": (ctypes.c_longlong, [i, i, i, i]),
             "pto_to_patchxf": (None, [vp, vp]),
             "pto_random_level_keys": (i, [u32, i, i, i, i, i, vp, vp, vp, vp, i, i, i, i, i, i, i, vp]),
+            "pto_tex_fetch": (None, [vp, i, i, i, i, vp, i, i, vp]),
+            "pto_gauss_weights": (None, [i, i, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -217,6 +219,18 @@ def counter_seed(rng_seed, frame, level):
     return (rng_seed ^ ((0x9E3779B9 * (frame + 1)) & 0xFFFFFFFF) ^ ((0x85EBCA6B * (level + 1)) & 0xFFFFFFFF)) & 0xFFFFFFFF
 
 
+def tex_fetch(tex, q, hw=True):
+    """Bilinear fetches of a (L, H, W, C) float texture at texture coordinates
+    q[:, 0:2] (texel centres at +0.5) of layers q[:, 2]: the texture unit's
+    arithmetic (hw) or exact FP32 bilinear."""
+    tex = _c(tex, np.float32)
+    q = _c(q, np.float32)
+    L, H, W, C = tex.shape
+    out = np.empty((q.shape[0], C), np.float32)
+    lib().pto_tex_fetch(_p(tex), W, H, L, C, _p(q), q.shape[0], int(hw), _p(out))
+    return out
+
+
 def rgb_to_lab(rgba):
     """RGBtoLAB of one colour (the oracle's double pow)."""
     a = np.ascontiguousarray(rgba, np.float32)
@@ -321,6 +335,14 @@ class Oracle:
     def upload_random(self, rnd):
         h, w = rnd.shape[:2]
         lib().pto_upload_plain(self.h, _abi.LAYER_RANDOM, _p(_c(rnd, np.float32)), w, h)
+
+    def upload_layered(self, layer, arr):
+        """A level-0-sized upload into one of the layered image inputs."""
+        h, w = arr.shape[:2]
+        lib().pto_upload_layered(self.h, layer, _p(_c(arr, np.float32)), w, h)
+
+    def copy_base_to_working(self):
+        lib().pto_copy_base_to_working(self.h)
 
     def flip(self):
         lib().pto_flip(self.h)
@@ -455,7 +477,7 @@ class OracleDriver:
         self.W, self.H = f0["w"], f0["h"]
         sw = max(s["w"] for s in styles)
         sh = max(s["h"] for s in styles)
-        self.o = Oracle(self.W, self.H, sw, sh, len(styles), threads=threads)
+        self.o = self._make_backend(self.W, self.H, sw, sh, len(styles), threads)
         self.store = {}
         self.last_saved = {}  # SynthesisFrame::_last_saved_pass: (frame, level) -> pass
         self.levels = params.levels
@@ -465,6 +487,10 @@ class OracleDriver:
         self.f2k = ({}, {})   # frame -> frame-to-key ribbon pyramid, [0] backward, [1] forward
         self.k2k = ({}, {})   # key full index -> key-to-key ribbon pyramid
         self.ribbons = {}     # (frame, step) -> velocities over `step` frames
+
+    def _make_backend(self, W, H, SW, SH, NS, threads):
+        """The object with TexSynth's step surface that the driver calls."""
+        return Oracle(W, H, SW, SH, NS, threads=threads)
 
     def _update_parameters(self, frame, direction):
         """SynthesisFrame::updateParameters, synthesisFrame.cpp:522-542."""
@@ -564,7 +590,7 @@ class OracleDriver:
 
     def _copy_base_to_working(self, level):
         """CudaBufferPair::copyBaseToWorking for the offsets pair."""
-        lib().pto_copy_base_to_working(self.o.h)
+        self.o.copy_base_to_working()
 
     def render(self, first, last):
         """SynthesisProcessor::renderAnimation, synthesisProcessor.cpp:769-805,
@@ -686,14 +712,12 @@ class OracleDriver:
                 vp = vel(pf, step, "velf" if ahead else "velb")
                 if vc is None or vp is None:
                     break  # loadRibbonPair finds no ribbon of this step
-                L = lib()
-                w, h = self.W, self.H
                 if ahead:
-                    L.pto_upload_layered(o.h, _abi.LAYER_INPUT_VEL_B, _p(_c(vc, np.float32)), w, h)
-                    L.pto_upload_layered(o.h, _abi.LAYER_INPUT_VEL_F_PREVIOUS, _p(_c(vp, np.float32)), w, h)
+                    o.upload_layered(_abi.LAYER_INPUT_VEL_B, vc)
+                    o.upload_layered(_abi.LAYER_INPUT_VEL_F_PREVIOUS, vp)
                 else:
-                    L.pto_upload_layered(o.h, _abi.LAYER_INPUT_VEL_F, _p(_c(vc, np.float32)), w, h)
-                    L.pto_upload_layered(o.h, _abi.LAYER_INPUT_VEL_B_PREVIOUS, _p(_c(vp, np.float32)), w, h)
+                    o.upload_layered(_abi.LAYER_INPUT_VEL_F, vc)
+                    o.upload_layered(_abi.LAYER_INPUT_VEL_B_PREVIOUS, vp)
                 o.load_ribbon_field(0, acc[pf])
                 o.accumulate_ribbon_field(0, forwards, ts, step == 1)
                 ts *= 2

@@ -1,6 +1,6 @@
 // qt_shim_core.h -- the few QtCore containers that the reference's
-// downsample.cpp uses (QVector, QList, QHash, QMap and their Java-style
-// iterators), over the standard library, plus empty QString / QStringList /
+// downsample.cpp and the headers of its CUDA code use (QVector, QList,
+// QHash, QMap and their Java-style iterators), over the standard library, plus empty QString / QStringList /
 // QFile types that its headers name, so that those files compile for the
 // oracle's reference checks without Qt.  Test infrastructure only.
 //
@@ -32,6 +32,9 @@ public:
     const T& operator[](int i) const { return v_[(size_t)i]; }
     void resize(int n) { v_.resize((size_t)n); }
     void append(const T& t) { v_.push_back(t); }
+    bool isEmpty() const { return v_.empty(); }
+    const T& at(int i) const { return v_[(size_t)i]; }
+    void clear() { v_.clear(); }
 
 private:
     std::vector<T> v_;
@@ -48,6 +51,11 @@ public:
     const T& operator[](int i) const { return v_[(size_t)i]; }
     const T& at(int i) const { return v_[(size_t)i]; }
     void clear() { v_.clear(); }
+    bool isEmpty() const { return v_.empty(); }
+    T& first() { return v_.front(); }
+    const T& first() const { return v_.front(); }
+    void push_front(const T& t) { v_.insert(v_.begin(), t); }
+    T takeLast() { T t = v_.back(); v_.pop_back(); return t; }
 
 private:
     std::vector<T> v_;

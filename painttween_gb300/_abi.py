@@ -20,6 +20,7 @@ STATUS_NAMES = {
 FORWARD, BACKWARD, BIDIRECTIONAL = 0, 1, 2
 S_FMBM, S_FMBM_RM, S_FBMO, S_TCTF, S_IND = 0, 1, 2, 3, 4
 RNG_REFERENCE, RNG_COUNTER = 0, 1
+FILTER_EXACT, FILTER_TEXTURE = 0, 1
 
 LAYER_EXEMPLAR_BASE = 0
 LAYER_EXEMPLAR_OUTPUT = 1
@@ -91,7 +92,8 @@ class Params(ctypes.Structure):
         ("finalLevel", ctypes.c_int32),
         ("rngMode", ctypes.c_int32),
         ("rngSeed", ctypes.c_uint32),
-        ("reserved", ctypes.c_int32 * 6),
+        ("filterMode", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 5),
     ]
 
     def copy(self):
