@@ -278,6 +278,7 @@ def run_ours(args, dist):
     B.build()
     cfg = synthetic.config(WORKLOAD)
     p = cfg["params"]
+    p.filterMode = _abi.FILTER_EXACT if args.filter == "exact" else _abi.FILTER_TEXTURE
     frames = args.frames or cfg["frames"]
     device = dist.local
     ex, clip = make_inputs(cfg, frames, seed=2026 + dist.rank)
@@ -391,6 +392,7 @@ def run_ours(args, dist):
                    "exemplar": "%dx%d" % (cfg["ew"], cfg["eh"]), "patch_radius": r, "levels": p.levels,
                    "iterations": p.iterations, "scheme": "FMBM_RM", "histogram": True,
                    "kernels": "generic" if args.generic_kernels else "tiled",
+                   "filter": args.filter,
                    "parallelism": "replicas" if dist.ws > 1 else "single",
                    "l2": "inputs larger than L2 (%.1f GB of resident frame pyramids per step)"
                          % (s.device_bytes / 1e9)},
@@ -491,6 +493,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-stills", type=int, default=64, help="requests of the batched-vs-plain run (0: skip)")
     ap.add_argument("--batch-in-flight", type=int, default=8)
+    ap.add_argument("--filter", default="texture", choices=["texture", "exact"],
+                    help="bilinear arithmetic: the texture unit's (the reference's) or exact FP32")
     ap.add_argument("--generic-kernels", action="store_true",
                     help="run the generic one-thread-per-pixel kernels instead of the tiled ones (profiling only)")
     args = ap.parse_args()

@@ -397,6 +397,10 @@ static inline bl_t bl_setup_at(float xs, float ys, int n, int m, int hw) {
     float oa = 1.0f - a, oc = 1.0f - c;
     b.w00 = oa * oc; b.w10 = a * oc; b.w01 = oa * c; b.w11 = a * c;
     b.hw = hw;
+    /* a coordinate of NaN or +-inf reads the edge texel (NaN the low edge,
+     * as measured): the clamps above give its index, the fraction is 0 */
+    if (a != a) a = 0.0f;
+    if (c != c) c = 0.0f;
     int A = (int)floor((double)a * 256.0 + 0.5), B = (int)floor((double)c * 256.0 + 0.5);
     b.q11 = (A * B + 128) >> 8;
     b.q10 = A - b.q11; b.q01 = B - b.q11; b.q00 = 256 - A - B + b.q11;
@@ -406,47 +410,75 @@ static inline bl_t bl_setup_at(float xs, float ys, int n, int m, int hw) {
 }
 static inline bl_t bl_setup(float u, float v, int n, int m, int hw) { return bl_setup_at(u + 0.5f, v + 0.5f, n, m, hw); }
 
-/* x rounded to float, ties away from zero (x exact in double) */
-static inline float round_half_away_f(double x) {
-    float f = (float)x;
-    if ((double)f == x) return f;
-    float lo, hi;
-    if (fabs((double)f) > fabs(x)) { hi = f; lo = nextafterf(f, 0.0f); }
-    else { lo = f; hi = nextafterf(f, x > 0 ? INFINITY : -INFINITY); }
-    double mid = ((double)lo + (double)hi) * 0.5;
-    return fabs(x) >= fabs(mid) ? hi : lo;
+/* A NaN produced by device arithmetic (0/0 here) is the GPU's canonical
+ * quiet NaN, bits 0x7fffffff, where the host's x86 arithmetic produces
+ * 0xffc00000; NaN inputs pass through arithmetic unchanged on both.  The
+ * reference stores such a NaN offset when a pixel's average-offset candidate
+ * has no same-layer neighbour and its energy is still the best (with
+ * texture filtering a NaN coordinate reads the edge texel). */
+static inline float gpu_nan(float v) {
+    if (v == v) return v;
+    uint32_t u = 0x7fffffffu;
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
 }
 
 /* a texel as the texture unit reads it: subnormals as (signed) zero */
 static inline float tex_ftz(float t) { return fpclassify(t) == FP_SUBNORMAL ? copysignf(0.0f, t) : t; }
 
+static inline uint32_t f_bits(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
+static inline float f_of_bits(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
+
 /* the texture unit's weighted sum of one channel: the texels with a nonzero
  * weight are aligned to the largest exponent among them and truncated
  * toward zero to 28 bits below it, summed exactly with the 1/256 weights,
  * and the sum is rounded to float ties away from zero; a sum of zeros is -0
- * only if every texel with a nonzero unrounded weight is negative-signed */
+ * only if every texel with a nonzero unrounded weight is negative-signed.
+ * Integer arithmetic throughout: a normal texel t = M * 2^(e - 24) with the
+ * 24-bit significand M and frexp exponent e, so t * 2^(28 - E) = M * 2^(4 +
+ * e - E). */
 static inline float hw_sum(const bl_t* b, float t00, float t10, float t01, float t11) {
-    float t[4] = {tex_ftz(t00), tex_ftz(t10), tex_ftz(t01), tex_ftz(t11)};
+    const float t[4] = {tex_ftz(t00), tex_ftz(t10), tex_ftz(t01), tex_ftz(t11)};
     const int q[4] = {b->q00, b->q10, b->q01, b->q11};
     const int r[4] = {b->r00, b->r10, b->r01, b->r11};
-    int E = 0, any = 0;
-    for (int k = 0; k < 4; k++)
-        if (q[k] > 0 && t[k] != 0.0f) {
-            int e;
-            frexpf(t[k], &e);
-            if (!any || e > E) E = e;
-            any = 1;
-        }
-    if (!any) {
+    int E = -1000;
+    for (int k = 0; k < 4; k++) {
+        uint32_t u = f_bits(t[k]);
+        int e = (int)((u >> 23) & 0xffu) - 126;
+        if (q[k] > 0 && (u & 0x7fffffffu) != 0u && e > E) E = e;
+    }
+    if (E == -1000) {
         int neg = 1;
         for (int k = 0; k < 4; k++)
-            if (r[k] && !signbit(t[k])) neg = 0;
+            if (r[k] && !(f_bits(t[k]) >> 31)) neg = 0;
         return neg ? -0.0f : 0.0f;
     }
     long long S = 0;
-    for (int k = 0; k < 4; k++)
-        if (q[k] > 0) S += (long long)q[k] * (long long)ldexp((double)t[k], 28 - E);
-    return round_half_away_f(ldexp((double)S, E - 36));
+    for (int k = 0; k < 4; k++) {
+        uint32_t u = f_bits(t[k]);
+        if (q[k] <= 0 || (u & 0x7fffffffu) == 0u) continue;
+        int e = (int)((u >> 23) & 0xffu) - 126;
+        long long M = (long long)((u & 0x7fffffu) | 0x800000u);
+        int sh = 4 + e - E;
+        long long m = sh >= 0 ? (M << sh) : (sh > -25 ? (M >> -sh) : 0);
+        S += (long long)q[k] * ((u >> 31) ? -m : m);
+    }
+    /* S * 2^(E - 36) to float, ties away from zero */
+    if (S == 0) return 0.0f;
+    int neg = S < 0;
+    unsigned long long mag = (unsigned long long)(neg ? -S : S);
+    int msb = 63 - __builtin_clzll(mag);
+    int e2 = E - 36;
+    if (msb > 23) {
+        int drop = msb - 23;
+        unsigned long long rem = mag & ((1ull << drop) - 1ull);
+        mag >>= drop;
+        if (rem >= (1ull << (drop - 1))) mag += 1ull;
+        e2 += drop;
+    }
+    float f = ldexpf((float)mag, e2);
+    return neg ? -f : f;
 }
 
 static inline float bl1(const bl_t* b, float t00, float t10, float t01, float t11) {
@@ -958,8 +990,8 @@ void pto_scatter_k(pto* o, int level, uint32_t pass_id, int key) {
                 avg.y = avg.y + nb->y;
                 n++;
             }
-        avg.x = avg.x / (float)n;
-        avg.y = avg.y / (float)n;
+        avg.x = gpu_nan(avg.x / (float)n);  /* 0/0 without a same-layer neighbour */
+        avg.y = gpu_nan(avg.y / (float)n);
         avg.theta = screen_to_exemplar_angle(o, x, y, avg.x, avg.y, 0);
         float r = test_offset(o, x, y, &avg, level, ia, &pc);
         if (r < best) { ow = avg; best = r; }

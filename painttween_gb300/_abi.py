@@ -148,6 +148,7 @@ def default_params():
     p.finalLevel = 0
     p.rngMode = RNG_REFERENCE
     p.rngSeed = 0
+    p.filterMode = FILTER_TEXTURE  # the reference's texture-unit sampling
     return p
 
 

@@ -200,7 +200,7 @@ static __device__ float energy(const Params& P, int x, int y, const Patch& t, co
         for (int j = -r; j <= r; j++) {
             if (!in_rect(P, x + i, y + j)) continue;
             size_t k = (size_t)(y + j) * P.W + (x + i);
-            float4 base = __ldg(imgb + (size_t)(y + j) * imgw + (x + i));
+            float4 base = lin_texel_of(__ldg(imgb + (size_t)(y + j) * imgw + (x + i)), P.hwFilter);
             float4 canvas = __ldg(P.canvas + k);
             if (P.colorspace == 1) {  // :575-578
                 base = rgb_to_lab(base);
@@ -317,7 +317,7 @@ static __device__ __forceinline__ size_t pixel_wrap_index(const Params& P, int t
 static __device__ Patch propagate_offset(const Params& P, int tx, int ty, int x, int y) {
     size_t kk = pixel_wrap_index(P, tx, ty);
     float4 a = __ldg(P.off.A + kk);
-    float2 sc = lvl_texel(P.img.scale, tx, ty);
+    float2 sc = lvl_texel_lin(P.img.scale, tx, ty, P.hwFilter);
     float2 b0, b1;
     basis(a.z, P.scaleWU * sc.x, P.scaleWV * sc.y, &b0, &b1);
     float ex, ey;
@@ -325,7 +325,7 @@ static __device__ Patch propagate_offset(const Params& P, int tx, int ty, int x,
     clamp_to_exemplar(&ex, &ey, P.ex.w, P.ex.h);
     int layer = __float_as_int(a.w);
     float ang = screen_to_exemplar_angle(P, x, y, ex, ey, layer);
-    float2 s2 = lvl_texel(P.img.scale, x, y);
+    float2 s2 = lvl_texel_lin(P.img.scale, x, y, P.hwFilter);
     return make_patch(ex, ey, ang, 0.0f, layer, s2.x, s2.y);
 }
 

@@ -46,6 +46,13 @@ struct ExLevel {  // one exemplar pyramid level, all styles (base and output pla
     float4* out = nullptr;
     float4* bo = nullptr;   // base and output interleaved per texel, rebuilt when stale
     bool bo_stale = true;
+    // PT_FILTER_TEXTURE: base and output as layered arrays (one layer per
+    // style) bound to texture objects with the reference's sampling state
+    // (linear filter, clamp, unnormalised coordinates), refreshed when stale
+    cudaArray_t tarr[2] = {nullptr, nullptr};
+    cudaTextureObject_t tex[2] = {0, 0};
+    int tw = 0, th = 0;
+    bool tex_stale = true;
     float* orient = nullptr;
     float* dt = nullptr;
     int* ids = nullptr;
@@ -397,7 +404,13 @@ static Params make_params(pt_ctx* c, int level) {
         P.ex.w = c->ex->w;
         P.ex.h = c->ex->h;
         P.ex.ns = c->NS;
+        P.ex.hw = p.filterMode == PT_FILTER_TEXTURE;
+        if (P.ex.hw && !c->ex->tex_stale) {
+            P.ex.tbase = c->ex->tex[0];
+            P.ex.tout = c->ex->tex[1];
+        }
     }
+    P.hwFilter = p.filterMode == PT_FILTER_TEXTURE;
     P.img = c->img;
     P.off = base_planes(c);
     P.res = c->res[c->res_i];
@@ -409,12 +422,62 @@ static Params make_params(pt_ctx* c, int level) {
     return P;
 }
 
-// the interleaved copy of an exemplar level that the tiled kernels gather
-// from, rebuilt after its planes were written
+static void free_textures(ExLevel* L) {
+    for (int k = 0; k < 2; k++) {
+        if (L->tex[k]) cudaDestroyTextureObject(L->tex[k]);
+        if (L->tarr[k]) cudaFreeArray(L->tarr[k]);
+        L->tex[k] = 0;
+        L->tarr[k] = nullptr;
+    }
+    L->tw = L->th = 0;
+    L->tex_stale = true;
+}
+
+// the layered textures of an exemplar level (PT_FILTER_TEXTURE), copied from
+// its planes after they were written
+static pt_status refresh_textures(pt_ctx* c, ExLevel* L) {
+    if (!L->base) return PT_OK;
+    if (L->tarr[0] && (L->tw != L->w || L->th != L->h)) free_textures(L);
+    if (!L->tex_stale && L->tarr[0]) return PT_OK;
+    cudaChannelFormatDesc d = cudaCreateChannelDesc<float4>();
+    for (int k = 0; k < 2; k++) {
+        if (!L->tarr[k]) {
+            CU(cudaMalloc3DArray(&L->tarr[k], &d, make_cudaExtent(L->w, L->h, c->NS), cudaArrayLayered));
+            cudaResourceDesc rd;
+            memset(&rd, 0, sizeof rd);
+            rd.resType = cudaResourceTypeArray;
+            rd.res.array.array = L->tarr[k];
+            cudaTextureDesc td;
+            memset(&td, 0, sizeof td);
+            td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;
+            td.filterMode = cudaFilterModeLinear;
+            td.readMode = cudaReadModeElementType;
+            td.normalizedCoords = 0;
+            CU(cudaCreateTextureObject(&L->tex[k], &rd, &td, nullptr));
+        }
+        cudaMemcpy3DParms cp;
+        memset(&cp, 0, sizeof cp);
+        cp.srcPtr = make_cudaPitchedPtr((void*)(k ? L->out : L->base), (size_t)L->w * sizeof(float4), L->w, L->h);
+        cp.dstArray = L->tarr[k];
+        cp.extent = make_cudaExtent(L->w, L->h, c->NS);
+        cp.kind = cudaMemcpyDeviceToDevice;
+        CU(cudaMemcpy3DAsync(&cp, c->stream));
+    }
+    L->tw = L->w;
+    L->th = L->h;
+    L->tex_stale = false;
+    return PT_OK;
+}
+
+// the copies of an exemplar level that the tiled kernels gather from (the
+// interleaved records, and with PT_FILTER_TEXTURE the textures), rebuilt
+// after its planes were written
 static pt_status refresh_interleaved(pt_ctx* c, ExLevel* L) {
-    if (!L->bo_stale || !L->bo || !L->base) return PT_OK;
-    LN(pt::launch_interleave_texels(L->base, L->out, L->bo, (size_t)L->w * L->h * c->NS, c->stream));
-    L->bo_stale = false;
+    if (L->bo_stale && L->bo && L->base) {
+        LN(pt::launch_interleave_texels(L->base, L->out, L->bo, (size_t)L->w * L->h * c->NS, c->stream));
+        L->bo_stale = false;
+    }
+    if (c->params.filterMode == PT_FILTER_TEXTURE) TRY(refresh_textures(c, L));
     return PT_OK;
 }
 
@@ -714,6 +777,7 @@ void pt_default_params(pt_params* p) {
     p->scheme = PT_S_FMBM_RM;
     p->finalLevel = 0;
     p->rngMode = PT_RNG_REFERENCE;
+    p->filterMode = PT_FILTER_TEXTURE;  // the reference's texture-unit sampling
 }
 
 pt_status pt_create(int device, size_t budget, pt_ctx** out) {
@@ -774,6 +838,8 @@ pt_status pt_destroy(pt_ctx* c) {
     for (auto& e : c->ev_pool) cudaEventDestroy(e);
     for (auto& v : c->ev_pairs)
         for (auto& pr : v) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+    free_textures(&c->up_ex);
+    for (auto& L : c->style_levels) free_textures(&L);
     for (auto& kv : c->allocs) cudaFree(kv.first);
     c->allocs.clear();
     for (auto& kv : c->cache) cudaFree(kv.second);
@@ -799,8 +865,11 @@ pt_status pt_set_params(pt_ctx* c, const pt_params* p) {
     if (p->numStyles < 1 || p->numStyles > PT_MAX_STYLES) return fail(c, PT_ERR_INVALID, "numStyles out of range");
     if (p->rngMode != PT_RNG_REFERENCE && p->rngMode != PT_RNG_COUNTER)
         return fail(c, PT_ERR_INVALID, "unknown rngMode");
+    if (p->filterMode != PT_FILTER_EXACT && p->filterMode != PT_FILTER_TEXTURE)
+        return fail(c, PT_ERR_INVALID, "unknown filterMode");
     c->params = *p;
     c->have_params = true;
+    if (c->ex) TRY(refresh_interleaved(c, c->ex));
     // TexSynth::setup: unnormalised Gaussian with sigma = r/3
     // (allocateGaussianKernel(..., normalize=false), convolution.cu:37-60)
     int r = p->residualWindowSize;
@@ -943,6 +1012,7 @@ pt_status pt_initialize_exemplars(pt_ctx* c, int w, int h, int ns) {
     c->up_ex.h = h;
     c->up_ex.transparent = -1;
     c->up_ex.bo_stale = true;
+    c->up_ex.tex_stale = true;
     c->ex = &c->up_ex;
     return PT_OK;
 }
@@ -1014,6 +1084,7 @@ pt_status pt_upload_image_color4(pt_ctx* c, int level, int layer, const float* r
         TRY(h2d(c, plane + n * style, rgba, n * sizeof(float4)));
         if (layer == PT_LAYER_EXEMPLAR_OUTPUT) c->up_ex.transparent = -1;
         c->up_ex.bo_stale = true;
+        c->up_ex.tex_stale = true;
         return PT_OK;
     }
     if (layer == PT_LAYER_CUMUL_FIELD_B || layer == PT_LAYER_CUMUL_FIELD_F) {
@@ -1215,6 +1286,7 @@ static ptk::KeyView key_view(const pt_ctx* c) {
     K.w = c->cf_w;
     K.h = c->cf_h;
     K.n = c->cf_n;
+    K.hw = c->params.filterMode == PT_FILTER_TEXTURE;
     return K;
 }
 
@@ -1596,6 +1668,7 @@ pt_status pt_set_style(pt_ctx* c, int style, int w, int h, const float* base, co
         for (auto& L : c->style_levels) {
             dfree_t(c, L.base); dfree_t(c, L.out); dfree_t(c, L.bo); dfree_t(c, L.orient); dfree_t(c, L.dt);
             dfree_t(c, L.ids);
+            free_textures(&L);
         }
         c->style_levels.assign(nlev, ExLevel());
         for (int l = 0; l < nlev; l++) {
@@ -1636,6 +1709,7 @@ pt_status pt_set_style(pt_ctx* c, int style, int w, int h, const float* base, co
         CU(cudaMemcpyAsync(L.ids + n * style, pi[l], n * sizeof(int), cudaMemcpyDeviceToDevice, c->stream));
         L.transparent = -1;
         L.bo_stale = true;
+        L.tex_stale = true;
     }
     CU(cudaStreamSynchronize(c->stream));
     for (int l = 0; l < nlev; l++) {

@@ -56,10 +56,20 @@ __device__ __forceinline__ void ld_texel(const float4* p, float4* b, float4* o) 
 // bilinear base+output at (u, v) of one exemplar layer (LBO: its interleaved
 // records); fast (warp-uniform): the footprint is known to be inside
 // [0, w-1] x [0, h-1], so the clamps are no-ops and are skipped
-template <bool PK>
-__device__ __forceinline__ void sample2(const float4* LBO, int w, int h, float u, float v, float4* base, float4* out,
-                                        bool fast) {
+// With HW (PT_FILTER_TEXTURE, textures bound) both colours come from the
+// texture unit: layered fetches of layer `li` (the clamped style layer) at the
+// texture coordinate u + 0.5, which is the reference's own sampling
+// (PYRAMID_FETCH_LAYER, texSynth_kernel.cu:600-601).
+template <bool PK, int HW>
+__device__ __forceinline__ void sample2(const ExView& E, int li, const float4* LBO, float u, float v, float4* base,
+                                        float4* out, bool fast) {
+    const int w = E.w, h = E.h;
     float xs = u + 0.5f, ys = v + 0.5f;
+    if (HW) {
+        *base = tex2DLayered<float4>(E.tbase, xs, ys, li);
+        *out = tex2DLayered<float4>(E.tout, xs, ys, li);
+        return;
+    }
     float xb = xs - 0.5f, yb = ys - 0.5f;
     float fx = floorf(xb), fy = floorf(yb);
     float a = xb - fx, c = yb - fy;
@@ -84,6 +94,15 @@ __device__ __forceinline__ void sample2(const float4* LBO, int w, int h, float u
     ld_texel(LBO + 2 * (r1 + x1), &b11, &o11);
     *base = PK ? bl4p(bw, b00, b10, b01, b11) : bl4(bw, b00, b10, b01, b11);
     *out = PK ? bl4p(bw, o00, o10, o01, o11) : bl4(bw, o00, o10, o01, o11);
+}
+
+// the exemplar view with its filter mode fixed at compile time (the tiled
+// kernels are instantiated per mode, so the other mode's code is dropped)
+template <int HW>
+__device__ __forceinline__ ExView ex_mode(const ExView& e) {
+    ExView v = e;
+    v.hw = HW;
+    return v;
 }
 
 struct Cand {
@@ -152,15 +171,17 @@ __device__ __forceinline__ void count_taps(const Params& P, unsigned taps, bool 
 // particular) are instruction-cache bound, and a second, compile-time fast
 // copy of this loop measured slower there.  EE: the early-exit test is
 // compiled in (false for the residual, which always needs the full sum).
-template <int R, int TM, bool EE>
+template <int R, int TM, int HW, bool EE>
 __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
                                              const Cand& c, float2 b0, float2 b1, float sum0, bool fast,
                                              bool fastp, float thr2) {
     constexpr int TW = TileSmem<R, TM>::TW;
     const size_t lsz = (size_t)P.ex.w * P.ex.h;
-    const size_t lo = (size_t)ex_layer(P.ex, c.layer) * lsz;
+    const int li = ex_layer(P.ex, c.layer);
+    const size_t lo = (size_t)li * lsz;
     const float4* LBO = P.ex.bo + 2 * lo;
-    const size_t lp = TM ? (size_t)ex_layer(P.ex, px.prev.layer) * lsz : 0;
+    const int lpi = TM ? ex_layer(P.ex, px.prev.layer) : 0;
+    const size_t lp = (size_t)lpi * lsz;
     const float hw = (float)P.histW, hh = (float)P.histH;
     const unsigned mask = __activemask();
     float sum = sum0;
@@ -184,7 +205,7 @@ __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, 
                     if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
                 }
                 float4 tb, to;
-                sample2<true>(LBO, P.ex.w, P.ex.h, tx, ty, &tb, &to, fast);
+                sample2<true, HW>(P.ex, li, LBO, tx, ty, &tb, &to, fast);
                 float res = ssd_ap(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
                 if (TM) {
                     if (px.temporal) {
@@ -192,7 +213,7 @@ __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, 
                         float ptx = px.prev.x + fmaf((float)i, px.pb0.x, (float)j * px.pb1.x);
                         float pty = px.prev.y + fmaf((float)i, px.pb0.y, (float)j * px.pb1.y);
                         float4 peb, peo;
-                        sample2<true>(P.ex.bo + 2 * lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo, fastp);
+                        sample2<true, HW>(P.ex, lpi, P.ex.bo + 2 * lp, ptx, pty, &peb, &peo, fastp);
                         float r = ssdp(sub4p(base, pbase), sub4p(tb, peb)) * P.tdIn;
                         r = fmaf(ssdp(sub4p(canvas, pout), sub4p(to, peo)), P.tdOut, r);
                         r = fmaf(ssdp(pout, to), P.tc, r);
@@ -201,7 +222,7 @@ __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, 
                 }
                 if (i == 0 && j == 0) {
                     if (P.distTransWeight > 0.f) {
-                        float de = ex_sample_dt(P.ex, tx, ty, c.layer) / c.sv;
+                        float de = ex_sample_dt(ex_mode<HW>(P.ex), tx, ty, c.layer) / c.sv;
                         float di = lay_texel(P.img.dt[P.img.cur], P, px.x, px.y);
                         float diff = fminf(fmaxf(fabsf(de - di), 0.0f), 10.0f);
                         res = res + diff * P.distTransWeight;
@@ -235,7 +256,7 @@ __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, 
     return sum / px.sumW;
 }
 
-template <int R, int TM, bool EE>
+template <int R, int TM, int HW, bool EE>
 __device__ __forceinline__ float energy_tiled(const Params& P, const TileSmem<R, TM>& T, const PixT& px,
                                            const Cand& c, float best) {
     float sum0 = 0.0f;
@@ -245,7 +266,7 @@ __device__ __forceinline__ float energy_tiled(const Params& P, const TileSmem<R,
     const unsigned mask = __activemask();
     bool fast = __all_sync(mask, footprint_inside<R>(c.x, c.y, b0, b1, P.ex.w, P.ex.h));
     bool fastp = TM ? __all_sync(mask, !px.temporal || px.prev_fast) : true;
-    return energy_taps<R, TM, EE>(P, T, px, c, b0, b1, sum0, fast, fastp,
+    return energy_taps<R, TM, HW, EE>(P, T, px, c, b0, b1, sum0, fast, fastp,
                                   EE ? exit_threshold(P, px, best) : kNoBest);
 }
 
@@ -262,7 +283,7 @@ __device__ __forceinline__ bool stage_tile(const Params& P, TileSmem<R, TM>& T, 
         int gx = clampi(x0 + q % TW, 0, P.lw - 1);
         int gy = clampi(y0 + q / TW, 0, P.lh - 1);
         size_t k = (size_t)gy * P.W + gx;
-        T.base[q] = __ldg(ib.p + (size_t)gy * ib.w + gx);
+        T.base[q] = lin_texel_of(__ldg(ib.p + (size_t)gy * ib.w + gx), P.hwFilter);
         T.canvas[q] = __ldg(P.canvas + k);
         if (TM) {
             const AdvView& A = P.adv[TM == TM_FWD ? 0 : 1];
@@ -337,7 +358,7 @@ __device__ __forceinline__ bool block_idle(const Params& P, PatchPlanes work, bo
 }
 
 // updateResidualCache_kernel, texSynth_kernel.cu:661-693
-template <int R, int TM>
+template <int R, int TM, int HW>
 __global__ void __launch_bounds__(kTileThreads, 2) kt_residual(const Params P, float* out) {
     __shared__ TileSmem<R, TM> T;
     // Change tracking: only pixels with a changed record in their patch
@@ -380,7 +401,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_residual(const Params P, f
     Patch t = load_patch(P.off, k);
     Cand c{t.x, t.y, t.theta, t.su, t.sv, t.layer};
     if (P.counters) count_eval(P, px.x, px.y, px.temporal, false);
-    out[k] = energy_tiled<R, TM, false>(P, T, px, c, kNoBest);
+    out[k] = energy_tiled<R, TM, HW, false>(P, T, px, c, kNoBest);
 }
 
 // ---------------------------------------------------------------------------
@@ -521,12 +542,13 @@ __device__ __forceinline__ void lane_start(const Params& P, const LanePix& q, fl
 // calculateResidual's value at tap (i, j) of candidate e at pixel q, before
 // its Gaussian weight (texSynth_kernel.cu:537-659); fast / fastp are
 // warp-uniform
-template <int R, int TM>
+template <int R, int TM, int HW>
 __device__ __forceinline__ float tap_value(const Params& P, const TileSmem<R, TM>& T, const LanePix& q,
                                            const LaneEval& e, int i, int j, bool fast, bool fastp) {
     constexpr int TW = TileSmem<R, TM>::TW;
     const size_t lsz = (size_t)P.ex.w * P.ex.h;
-    const size_t lo = (size_t)ex_layer(P.ex, e.layer) * lsz;
+    const int li = ex_layer(P.ex, e.layer);
+    const size_t lo = (size_t)li * lsz;
     const float4* LBO = P.ex.bo + 2 * lo;
     const size_t lp = TM ? (size_t)q.prevlayer * lsz : 0;
     const float hw = (float)P.histW, hh = (float)P.histH;
@@ -540,7 +562,7 @@ __device__ __forceinline__ float tap_value(const Params& P, const TileSmem<R, TM
         if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
     }
     float4 tb, to;
-    sample2<true>(LBO, P.ex.w, P.ex.h, tx, ty, &tb, &to, fast);
+    sample2<true, HW>(P.ex, li, LBO, tx, ty, &tb, &to, fast);
     float res = ssd_ap(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
     if (TM) {
         if (q.temporal) {
@@ -548,7 +570,7 @@ __device__ __forceinline__ float tap_value(const Params& P, const TileSmem<R, TM
             float ptx = q.prevx + fmaf((float)i, q.pb0.x, (float)j * q.pb1.x);
             float pty = q.prevy + fmaf((float)i, q.pb0.y, (float)j * q.pb1.y);
             float4 peb, peo;
-            sample2<true>(P.ex.bo + 2 * lp, P.ex.w, P.ex.h, ptx, pty, &peb, &peo, fastp);
+            sample2<true, HW>(P.ex, TM ? q.prevlayer : 0, P.ex.bo + 2 * lp, ptx, pty, &peb, &peo, fastp);
             float r = ssdp(sub4p(base, pbase), sub4p(tb, peb)) * P.tdIn;
             r = fmaf(ssdp(sub4p(canvas, pout), sub4p(to, peo)), P.tdOut, r);
             r = fmaf(ssdp(pout, to), P.tc, r);
@@ -557,7 +579,7 @@ __device__ __forceinline__ float tap_value(const Params& P, const TileSmem<R, TM
     }
     if (j == 0 && i == 0) {
         if (P.distTransWeight > 0.f) {
-            float de = ex_sample_dt(P.ex, tx, ty, e.layer) / e.sv;
+            float de = ex_sample_dt(ex_mode<HW>(P.ex), tx, ty, e.layer) / e.sv;
             float di = lay_texel(P.img.dt[P.img.cur], P, q.x, q.y);
             float diff = fminf(fmaxf(fabsf(de - di), 0.0f), 10.0f);
             res = res + diff * P.distTransWeight;
@@ -588,7 +610,7 @@ __device__ __forceinline__ float tap_value(const Params& P, const TileSmem<R, TM
 // EE: a lane leaves the column as soon as its sum reaches e.thr2 (the sum
 // only grows, so stopping at any tap gives the decision of stopping at the
 // column's end), and the loads of its remaining taps are not issued.
-template <int R, int TM, bool ROLL, bool EE>
+template <int R, int TM, int HW, bool ROLL, bool EE>
 __device__ __forceinline__ float lane_column(const Params& P, const TileSmem<R, TM>& T, const LanePix& q,
                                              const LaneEval& e, bool fast, bool fastp) {
     const int i = e.col;
@@ -598,7 +620,7 @@ __device__ __forceinline__ float lane_column(const Params& P, const TileSmem<R, 
 #pragma unroll(ROLL ? 1 : 2 * R + 1)
     for (int j = -R; j <= R; j++) {
         const bool valid = cvalid && (j >= q.jmin) && (j <= q.jmax);
-        const float res = tap_value<R, TM>(P, T, q, e, i, j, fast, fastp);
+        const float res = tap_value<R, TM, HW>(P, T, q, e, i, j, fast, fastp);
         const float w = gi * P.gauss[j + R];
         sum = valid ? fmaf(res, w, sum) : sum;
         if (EE && sum >= e.thr2) break;
@@ -634,7 +656,7 @@ __device__ __forceinline__ unsigned lane_taps(const LanePix& q, int cols) {
 // pass follows a candidate it has not rejected by then): candidates whose
 // energy is often close to the best (propagate's) pay the bound pass without
 // being rejected by it.
-template <int R, int TM, bool EE, bool ROLL, int BC>
+template <int R, int TM, int HW, bool EE, bool ROLL, int BC>
 __device__ __forceinline__ bool lane_step(const Params& P, const TileSmem<R, TM>& T, const TapTable<R>& TT,
                                           const LanePix& q, LaneEval& e, bool fast, bool fastp, float* r) {
     constexpr int K = (2 * R + 1) * (2 * R + 1);
@@ -653,7 +675,7 @@ __device__ __forceinline__ bool lane_step(const Params& P, const TileSmem<R, TM>
             const int ij = TT.ij[pos];
             const int i = (ij & 15) - R, j = (ij >> 4) - R;
             const bool valid = (i >= q.imin) && (i <= q.imax) && (j >= q.jmin) && (j <= q.jmax);
-            const float res = tap_value<R, TM>(P, T, q, e, i, j, fast, fastp);
+            const float res = tap_value<R, TM, HW>(P, T, q, e, i, j, fast, fastp);
             e.sum = valid ? __fadd_rd(e.sum, __fmul_rd(res, TT.w[pos])) : e.sum;
             if (__fadd_rd(__fmul_rd(e.sum, kBoundLo), e.s0lo) >= e.thr2) {
                 rejected = true;
@@ -674,7 +696,7 @@ __device__ __forceinline__ bool lane_step(const Params& P, const TileSmem<R, TM>
         }
         return false;
     }
-    e.sum = lane_column<R, TM, ROLL, EE>(P, T, q, e, fast, fastp);
+    e.sum = lane_column<R, TM, HW, ROLL, EE>(P, T, q, e, fast, fastp);
     e.col++;
     const bool stop = EE && e.sum >= e.thr2;
     if (!stop && e.col <= R) return false;
@@ -705,7 +727,7 @@ struct PropQueue {
 };
 
 // propagate_kernel with lane cursors over the tile's candidates
-template <int R, int TM>
+template <int R, int TM, int HW>
 __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P, PatchPlanes work, int jump) {
     __shared__ TileSmem<R, TM> T;
     __shared__ PixShared S;
@@ -777,10 +799,10 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P
                     if (dup) {
                         code = 1;
                     } else {
-                        float dte = ex_texel_dt(P.ex, (int)t.x, (int)t.y, t.layer);
+                        float dte = ex_texel_dt(ex_mode<HW>(P.ex), (int)t.x, (int)t.y, t.layer);
                         bool ok = !((double)dte > (double)P.distTransCull * 1.25);
                         if (ok && !P.transparencyOk) {
-                            float ea = ex_sample_out_alpha(P.ex, t.x, t.y, t.layer);
+                            float ea = ex_sample_out_alpha(ex_mode<HW>(P.ex), t.x, t.y, t.layer);
                             ok = !(ea < kAlphaThreshold && ia > kAlphaThreshold);
                         }
                         if (ok) {
@@ -848,7 +870,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P
             const bool fastp = TM ? __all_sync(kFull, !act || !q.temporal || q.prev_fast) : true;
             if (act) {
                 float r;
-                if (lane_step<R, TM, true, false, kPropagateBoundGroups>(P, T, TT, q, e, fast, fastp, &r)) {
+                if (lane_step<R, TM, HW, true, false, kPropagateBoundGroups>(P, T, TT, q, e, fast, fastp, &r)) {
                     Q.ca[cur].x = r;
                     act = false;
                 }
@@ -888,7 +910,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P
 
 // scatter_kernel + averageOffset, texSynth_kernel.cu:841-952, each lane
 // running its own pixel's chain with a lane cursor
-template <int R, int TM>
+template <int R, int TM, int HW>
 __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter_q(const Params P, PatchPlanes work, int write_all,
                                                                uint32_t pass_id) {
     __shared__ TileSmem<R, TM> T;
@@ -933,7 +955,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter_q(const Params P, 
         owx = a.x; owy = a.y;
         ia = T.base[px.sidx].w;
         dist = (float)(P.ex.w > P.ex.h ? P.ex.w : P.ex.h);
-        sc = lvl_texel(P.img.scale, x, y);
+        sc = lvl_texel_lin(P.img.scale, x, y, P.hwFilter);
         // averageOffset of the base field (:841-861)
         int na = 0;
         for (int i = -1; i <= 1; i++)
@@ -1004,9 +1026,9 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter_q(const Params P, 
                     more = false;
                     break;
                 }
-                bool ok = !((double)ex_texel_dt(P.ex, (int)cx, (int)cy, 0) > (double)P.distTransCull * 1.25);
+                bool ok = !((double)ex_texel_dt(ex_mode<HW>(P.ex), (int)cx, (int)cy, 0) > (double)P.distTransCull * 1.25);
                 if (ok && !P.transparencyOk) {
-                    float ea = ex_sample_out_alpha(P.ex, cx, cy, 0);
+                    float ea = ex_sample_out_alpha(ex_mode<HW>(P.ex), cx, cy, 0);
                     ok = !(ea < kAlphaThreshold && ia > kAlphaThreshold);
                 }
                 if (!ok) {
@@ -1029,7 +1051,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter_q(const Params P, 
         const bool fastp = TM ? __all_sync(kFull, !act || !q.temporal || q.prev_fast) : true;
         if (act) {
             float r;
-            if (lane_step<R, TM, true, true, 2 * R + 1>(P, T, TT, q, e, fast, fastp, &r)) {
+            if (lane_step<R, TM, HW, true, true, 2 * R + 1>(P, T, TT, q, e, fast, fastp, &r)) {
                 if (r < best) {
                     best = r;
                     owx = e.cx; owy = e.cy; owt = cur_t; wkind = cur_avg ? 2 : 1;
@@ -1057,7 +1079,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter_q(const Params P, 
 // are recomputed and the sum is then taken again over the stored values:
 // the same operations on the same values, so the same bits.  With `fill`
 // every tap of every pixel is computed (the loop's first residual).
-template <int R, int TM>
+template <int R, int TM, int HW>
 __global__ void __launch_bounds__(kTileThreads, 2) kt_residual_inc(const Params P, float* out) {
     constexpr int TW = TileSmem<R, TM>::TW, N = TileSmem<R, TM>::N, K = (2 * R + 1) * (2 * R + 1);
     __shared__ TileSmem<R, TM> T;
@@ -1182,7 +1204,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_residual_inc(const Params 
         const bool fastp = TM ? __all_sync(kFull, !act || !q.temporal || q.prev_fast) : true;
         if (act) {
             const int i = t / (2 * R + 1) - R, j = t % (2 * R + 1) - R;
-            const float v = tap_value<R, TM>(P, T, q, e, i, j, fast, fastp);
+            const float v = tap_value<R, TM, HW>(P, T, q, e, i, j, fast, fastp);
             P.inc.taps[(size_t)t * plane + (size_t)q.y * P.W + q.x] = v;
         }
     }
@@ -1213,14 +1235,23 @@ template <int R>
 cudaError_t launch_tiled_r(int kind, int tm, const Params& P, PatchPlanes work, int arg, uint32_t pass_id, float* out,
                            cudaStream_t s) {
     dim3 b(kTileW, kTileH), g((P.lw + kTileW - 1) / kTileW, (P.lh + kTileH - 1) / kTileH);
-#define PT_TILED_DISPATCH(TMV)                                                                   \
-    if (kind == 0) kt_propagate_q<R, TMV><<<g, b, 0, s>>>(P, work, arg);                        \
-    else if (kind == 1) kt_scatter_q<R, TMV><<<g, b, 0, s>>>(P, work, arg, pass_id);            \
-    else if (P.inc.on || P.inc.fill) kt_residual_inc<R, TMV><<<g, b, 0, s>>>(P, out);   \
-    else kt_residual<R, TMV><<<g, b, 0, s>>>(P, out);
-    if (tm == TM_NONE) { PT_TILED_DISPATCH(TM_NONE) }
-    else if (tm == TM_FWD) { PT_TILED_DISPATCH(TM_FWD) }
-    else { PT_TILED_DISPATCH(TM_BWD) }
+    // the texture-unit kernels fetch through the exemplar's textures, which
+    // must be bound
+    if (P.ex.hw && (!P.ex.tbase || !P.ex.tout)) return cudaErrorInvalidValue;
+#define PT_TILED_DISPATCH(TMV, HWV)                                                                   \
+    if (kind == 0) kt_propagate_q<R, TMV, HWV><<<g, b, 0, s>>>(P, work, arg);                        \
+    else if (kind == 1) kt_scatter_q<R, TMV, HWV><<<g, b, 0, s>>>(P, work, arg, pass_id);            \
+    else if (P.inc.on || P.inc.fill) kt_residual_inc<R, TMV, HWV><<<g, b, 0, s>>>(P, out);   \
+    else kt_residual<R, TMV, HWV><<<g, b, 0, s>>>(P, out);
+    if (P.ex.hw) {
+        if (tm == TM_NONE) { PT_TILED_DISPATCH(TM_NONE, 1) }
+        else if (tm == TM_FWD) { PT_TILED_DISPATCH(TM_FWD, 1) }
+        else { PT_TILED_DISPATCH(TM_BWD, 1) }
+    } else {
+        if (tm == TM_NONE) { PT_TILED_DISPATCH(TM_NONE, 0) }
+        else if (tm == TM_FWD) { PT_TILED_DISPATCH(TM_FWD, 0) }
+        else { PT_TILED_DISPATCH(TM_BWD, 0) }
+    }
 #undef PT_TILED_DISPATCH
     return cudaGetLastError();
 }

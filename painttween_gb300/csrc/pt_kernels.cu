@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(128) k_scatter(const Params P, PatchPlanes wor
     float ia = lay_texel(P.img.base[P.img.cur], P, x, y).w;
     float dist = (float)(P.ex.w > P.ex.h ? P.ex.w : P.ex.h);
     const float closest = 10.f, factor = 0.9f;
-    float2 sc = lvl_texel(P.img.scale, x, y);
+    float2 sc = lvl_texel_lin(P.img.scale, x, y, P.hwFilter);
     PixCtx pc;
     make_pixctx(P, x, y, &pc);
     uint32_t lastx = 0xffffffffu, lasty = 0xffffffffu;  // exact repeats are not re-evaluated
@@ -226,7 +226,7 @@ __global__ void k_upsample(const Params P, PatchPlanes work, PatchPlanes border_
     int layer = __float_as_int(o00.w);
     float rw = __ldg(P.res + (size_t)lcy * P.W + lcx);
     float ang = screen_to_exemplar_angle(P, x, y, up.x, up.y, layer);
-    float2 sc = lvl_texel(P.img.scale, x, y);
+    float2 sc = lvl_texel_lin(P.img.scale, x, y, P.hwFilter);
     store_patch(work, k, make_patch(up.x, up.y, ang, 0.0f, layer, sc.x, sc.y));
     res_out[k] = rw;
 }
@@ -298,7 +298,7 @@ __global__ void k_advect(const Params P, int d, int forwards, int time_step, int
     // left without one, takes the frame-to-key ribbon where it is shorter
     if ((flags & PT_ADVECT_CHECK_FRAME_TO_KEY) && (time_step > 1 || out.hyst == 0)) {
         const Arr<float4>& R = P.img.f2k[forwards ? 0 : 1];
-        const float4 c = R.p ? lvl_texel(R, x, y) : f4(0.f, 0.f, 0.f, 0.f);
+        const float4 c = R.p ? lvl_texel_lin(R, x, y, P.hwFilter) : f4(0.f, 0.f, 0.f, 0.f);
         const int rts = f2i(c.x), rlayer = f2i(c.w);
         if (rlayer >= 0 && (abs(rts) < time_step || out.hyst == 0)) {
             out.x = c.z + (float)x;

@@ -26,7 +26,7 @@ dim3 grid_of(int w, int h) { return dim3((w + 31) / 32, (h + 3) / 4); }
 __device__ float4 cumul_sample(const KeyView& K, int d, float u, float v, int j) {
     const float4* F = K.cumul[d];
     if (!F || j < 0 || j >= K.n) return f4(0.f, 0.f, 0.f, 0.f);
-    Bl b = bl_setup(u, v, K.w, K.h);
+    Bl b = bl_setup(u, v, K.w, K.h, K.hw);
     const float4* L = F + (size_t)j * K.w * K.h;
     const size_t r0 = (size_t)b.y0 * K.w, r1 = (size_t)b.y1 * K.w;
     return bl4(b, __ldg(L + r0 + b.x0), __ldg(L + r0 + b.x1), __ldg(L + r1 + b.x0), __ldg(L + r1 + b.x1));
@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(kKeyPix) k_frame_to_key(const Params P, PatchP
                                                           const KeyView K) {
     KEY_PIXEL_XY
     const Arr<float4>& R = P.img.f2k[look_forwards ? 1 : 0];
-    const Ribbon rb = ribbon_of(R.p ? lvl_texel(R, x, y) : f4(0.f, 0.f, 0.f, 0.f));
+    const Ribbon rb = ribbon_of(R.p ? lvl_texel_lin(R, x, y, P.hwFilter) : f4(0.f, 0.f, 0.f, 0.f));
     Patch out;
     if (rb.layer >= 0) {
         const float ox = rb.x + (float)x, oy = rb.y + (float)y;

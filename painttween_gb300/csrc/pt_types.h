@@ -37,6 +37,12 @@ struct ExView {
     const float* dt;
     const int* ids;
     int w, h, ns;
+    // PT_FILTER_TEXTURE: the linearly filtered inputs are read with the
+    // texture unit's arithmetic (hw); base and output are also bound as
+    // layered textures (linear filter, clamp, unnormalised coordinates) that
+    // the tiled kernels fetch through
+    int hw;
+    cudaTextureObject_t tbase, tout;
 };
 
 // A 2-D array of one pyramid level.  Image-side "layered" inputs (colour,
@@ -77,6 +83,7 @@ struct AdvView {
 struct KeyView {
     const float4* cumul[2];
     int w, h, n;
+    int hw;  // PT_FILTER_TEXTURE
 };
 // RibbonP (types.h:111-126) in the ribbon field buffers; layer < 0 = invalid
 struct Ribbon {
@@ -125,6 +132,7 @@ struct Params {
     int colorspace;            // 1: the energy compares Lab colours
     int rngMode;
     uint32_t rngSeed;
+    int hwFilter;              // PT_FILTER_TEXTURE: texture-unit arithmetic for the linearly filtered inputs
     int histW, histH;          // histogram level size (style w, style h * ns) >> level
     int histPitch, histRows;   // histogram buffer size at level 0
     const float* hist;

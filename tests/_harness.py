@@ -114,7 +114,13 @@ class Pair:
         return frac
 
 
-def config_params(r=2, levels=3, iterations=2):
+def config_params(r=2, levels=3, iterations=2, filter_mode=None):
     p = _abi.default_params()
     p.residualWindowSize, p.levels, p.iterations = r, levels, iterations
+    if filter_mode is not None:
+        p.filterMode = filter_mode
     return p
+
+
+# both sampling arithmetics: the texture unit's (the default) and exact FP32
+FILTER_MODES = [_abi.FILTER_TEXTURE, _abi.FILTER_EXACT]

@@ -4,7 +4,9 @@ glibc_rand.npz: the C library's own rand() output after srand(seed) for the
 seeds createRandomPyramid uses (frame * level) -- produced by libc itself,
 not by the restatement.
 still48.npz: the oracle's result for a 48x48 still (r2, 3 levels, 2
-iterations), a regression lock of the oracle.
+iterations), a regression lock of the oracle.  These three locks use exact
+FP32 bilinear filtering (PT_FILTER_EXACT); the texture-unit filtering is
+pinned by texfilter_gb300.npz (make_texfilter.py).
 clip40.npz: the oracle's results for a 40x32 three-frame clip with moving
 discs (48x48 exemplar, r2, 2 levels, 2 iterations, temporal coherence 0.5)
 under the FMBM_RM, FBMO and TCTF schedules, a regression lock of the
@@ -35,6 +37,7 @@ def main():
     from painttween_gb300 import _abi, synthetic
     p = _abi.default_params()
     p.residualWindowSize, p.levels, p.iterations = 2, 3, 2
+    p.filterMode = _abi.FILTER_EXACT
     ex = synthetic.make_exemplar(48, 48, seed=101)
     fr = synthetic.make_still(48, 48, 3, seed=102)
     offs, res, out = O.OracleDriver(p, [ex], [fr], threads=4).render(0, 0)[0]
@@ -62,6 +65,7 @@ def render_keyed():
     from painttween_gb300 import _abi, synthetic
     p = _abi.default_params()
     p.residualWindowSize, p.levels, p.iterations = 2, 2, 2
+    p.filterMode = _abi.FILTER_EXACT
     p.scheme = _abi.S_FMBM_RM
     p.interpolateKeyFrame = 1
     p.numStyles = 2
@@ -85,6 +89,7 @@ def render_clip(scheme):
     from painttween_gb300 import _abi, synthetic
     p = _abi.default_params()
     p.residualWindowSize, p.levels, p.iterations = 2, 2, 2
+    p.filterMode = _abi.FILTER_EXACT
     p.temporalCoherenceWeight = 0.5
     p.scheme = scheme
     ex = synthetic.make_exemplar(48, 48, seed=111)

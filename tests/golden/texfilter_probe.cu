@@ -174,6 +174,16 @@ int main(int argc, char** argv) {
         std::vector<float> tl0(t.begin(), t.begin() + (size_t)W * H * 4);
         run<float4>(dir, "special4_pitch", tl0, W, H, 1, q0, true);
     }
+    {   // coordinates that are not finite or far outside: NaN, +-inf, +-1e30
+        int W = 8, H = 6, L = 2;
+        std::vector<float> t((size_t)W * H * L * 4);
+        for (auto& v : t) v = U(rng);
+        const float odd[] = {NAN, -NAN, INFINITY, -INFINITY, 1e30f, -1e30f, 3.25f, 0.5f, 7.75f, -100.f};
+        std::vector<float> q;
+        for (float x : odd)
+            for (float y : odd) coord(q, x, y, 1);
+        run<float4>(dir, "nonfinite4", t, W, H, L, q, false);
+    }
     {   // large coordinates: fraction resolution at x near 3000
         int W = 4096, H = 4;
         std::vector<float> t((size_t)W * H, 0.f);

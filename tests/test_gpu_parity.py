@@ -3,7 +3,10 @@
 Integer and index work (random levels, offsets' layers, the pyramid
 indexing) and, by the shared FP32 arithmetic contract, the floating-point
 offsets, residuals and outputs are compared bit for bit.  The energy is also
-checked against the FP64 oracle within 1e-5 relative.
+checked against the FP64 oracle within 1e-5 relative.  Tests run with the
+default sampling (the texture unit's bilinear filtering, which the tiled
+kernels take from the texture unit itself and the oracle emulates); those
+parametrised by `fm` also run with exact FP32 bilinear filtering.
 """
 import numpy as np
 import pytest
@@ -11,7 +14,7 @@ import pytest
 from painttween_gb300 import Synthesizer, _abi, synthetic
 from oracle import oracle as O
 
-from _harness import Pair, assert_array_equal, assert_offsets_equal, config_params
+from _harness import FILTER_MODES, Pair, assert_array_equal, assert_offsets_equal, config_params
 
 pytestmark = pytest.mark.gpu
 
@@ -38,9 +41,10 @@ def test_random_level_and_randomize_bit_exact():
         pair.close()
 
 
+@pytest.mark.parametrize("fm", FILTER_MODES)
 @pytest.mark.parametrize("jump", [1, 2, 8, 128])
-def test_propagate_bit_exact(jump):
-    pair = Pair(64, 64, 64, 64, config_params())
+def test_propagate_bit_exact(jump, fm):
+    pair = Pair(64, 64, 64, 64, config_params(filter_mode=fm))
     try:
         _still_steps(pair, 1)
         pair.both("randomize_offsets", 1)
@@ -51,8 +55,9 @@ def test_propagate_bit_exact(jump):
         pair.close()
 
 
-def test_scatter_bit_exact():
-    pair = Pair(64, 64, 64, 64, config_params())
+@pytest.mark.parametrize("fm", FILTER_MODES)
+def test_scatter_bit_exact(fm):
+    pair = Pair(64, 64, 64, 64, config_params(filter_mode=fm))
     try:
         _still_steps(pair, 0)
         pair.both("randomize_offsets", 0)
@@ -82,9 +87,10 @@ def test_upsample_bit_exact_odd_sizes():
         pair.close()
 
 
+@pytest.mark.parametrize("fm", FILTER_MODES)
 @pytest.mark.parametrize("forwards", [True, False])
-def test_advect_and_merge_bit_exact(forwards):
-    p = config_params()
+def test_advect_and_merge_bit_exact(forwards, fm):
+    p = config_params(filter_mode=fm)
     pair = Pair(64, 64, 64, 64, p, frames=3)
     try:
         level = 0
@@ -207,8 +213,9 @@ def _driver_pair(W, H, EW, EH, p, frames, seed):
     return s, d
 
 
-def test_still_synthesis_driver_bit_exact():
-    p = config_params(r=2, levels=3, iterations=3)
+@pytest.mark.parametrize("fm", FILTER_MODES)
+def test_still_synthesis_driver_bit_exact(fm):
+    p = config_params(r=2, levels=3, iterations=3, filter_mode=fm)
     s, d = _driver_pair(96, 80, 64, 64, p, 1, seed=21)
     try:
         rgba, offs = s.synthesize_frame(0)
@@ -221,8 +228,9 @@ def test_still_synthesis_driver_bit_exact():
         s.close()
 
 
-def test_animation_driver_bit_exact():
-    p = config_params(r=2, levels=3, iterations=2)
+@pytest.mark.parametrize("fm", FILTER_MODES)
+def test_animation_driver_bit_exact(fm):
+    p = config_params(r=2, levels=3, iterations=2, filter_mode=fm)
     p.temporalCoherenceWeight = 0.5
     s, d = _driver_pair(64, 64, 64, 64, p, 4, seed=31)
     try:
@@ -350,12 +358,15 @@ def test_errors_are_status_codes():
     tb.close()
 
 
+@pytest.mark.parametrize("fm", FILTER_MODES)
 @pytest.mark.parametrize("r", [1, 2, 3, 4])
-def test_tiled_and_generic_kernels_identical(r):
+def test_tiled_and_generic_kernels_identical(r, fm):
     """The tiled shared-memory kernels (patch radius 2-4) and the generic
     kernels give bit-identical animations, including the temporal terms of
-    both pass directions; radius 1 runs the generic kernels in both cases."""
-    p = config_params(r=r, levels=2, iterations=2)
+    both pass directions; radius 1 runs the generic kernels in both cases.
+    With the texture unit's filtering the tiled kernels fetch through the
+    texture unit and the generic kernels emulate it."""
+    p = config_params(r=r, levels=2, iterations=2, filter_mode=fm)
     p.temporalCoherenceWeight = 0.5
     p.hysteresisWeight = 0.25
     p.distTransWeight = 0.5

@@ -100,6 +100,7 @@ def test_oracle_still_matches_golden_fixture():
     g = np.load(os.path.join(GOLDEN, "still48.npz"))
     p = _abi.default_params()
     p.residualWindowSize, p.levels, p.iterations = 2, 3, 2
+    p.filterMode = _abi.FILTER_EXACT
     ex = synthetic.make_exemplar(48, 48, seed=int(g["ex_seed"]))
     fr = synthetic.make_still(48, 48, 3, seed=int(g["fr_seed"]))
     d = O.OracleDriver(p, [ex], [fr], threads=4)
@@ -251,3 +252,26 @@ def test_lab_conversion_against_float64_formula():
         ref = [(116 * f(Y / 100) - 16) / 100, (500 * (f(X / 95.047) - f(Y / 100)) + 100) / 200,
                (200 * (f(Y / 100) - f(Z / 108.883)) + 100) / 200, c[3]]
         assert np.allclose(O.rgb_to_lab(c), ref, atol=2e-6, rtol=0), c
+
+
+def test_texture_filter_emulation_matches_recorded_gb300_fetches(oracle_mod):
+    """PT_FILTER_TEXTURE: the oracle's restatement of the texture unit's
+    bilinear filtering against fetches recorded on a GB300
+    (tests/golden/texfilter_gb300.npz, written by make_texfilter.py from
+    texfilter_probe.cu): 1-, 2- and 4-channel float textures, layered arrays
+    and pitched memory, unit weights, coordinates beyond the edges, fraction
+    ties, large coordinates, zeros, signed zeros, subnormals and values over
+    twelve decades -- every fetched bit."""
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "texfilter_gb300.npz"))
+    cases = sorted({k.split("/")[0] for k in d.files if not k.startswith("meta")})
+    assert len(cases) >= 7
+    total = 0
+    for name in cases:
+        tex, q, out = d[name + "/tex"], d[name + "/q"], d[name + "/out"]
+        got = oracle_mod.tex_fetch(tex, q, hw=True)
+        same = got.view(np.uint32) == out.view(np.uint32)
+        assert same.all(), "%s: %d of %d channels differ" % (name, (~same).sum(), same.size)
+        total += same.size
+        if name != "weights":  # exact FP32 bilinear is a different arithmetic
+            assert (oracle_mod.tex_fetch(tex, q, hw=False).view(np.uint32) != out.view(np.uint32)).any()
+    assert total > 100000
