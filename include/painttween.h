@@ -425,6 +425,11 @@ pt_status pt_synthesize_animation(pt_ctx* ctx, int first, int last,
  * animation callback fetches frames with this call, straight into its own
  * (ideally page-locked) memory. */
 pt_status pt_get_frame_result(pt_ctx* ctx, int frame, float* out_rgba, pt_patchxf* out_offsets);
+/* The residual (patch energy per pixel) stored with a synthesised frame's
+ * final offsets -- the reference saves it as the `residual` temporary image
+ * of that pass (WorkingBuffers::saveTempImages, workingBuffers.cpp:242-296);
+ * level-size float32, into caller memory. */
+pt_status pt_get_frame_residual(pt_ctx* ctx, int frame, float* out_residual);
 
 /* Page-locked host memory (cudaMallocHost / cudaFreeHost) for frame inputs
  * and results: copies from and to it run at the full host link speed.  No

@@ -821,7 +821,7 @@ static float energy_f32(const pto* o, int x, int y, int level, const pt_patchxf*
                 if (P->distTransWeight > 0.f) {
                     float de = ex_sample_dt(o, tx, ty, t->layer) / t->scaleV;
                     float di = dt_texel(o, o->cur, x, y);
-                    float diff = fminf(fmaxf(fabsf(de - di), 0.0f), 10.0f);
+                    float diff = fmaxf(0.0f, fminf(fabsf(de - di), 10.0f)); /* clamp = fmaxf(a, fminf(f, b)), cutil_math.h:1027: NaN gives 10 */
                     res = res + diff * P->distTransWeight;
                 }
                 { /* histogramTerm, :486-495 */
@@ -1389,7 +1389,7 @@ static double energy_f64(const pto* o, int x, int y, int level, const pt_patchxf
                                      D[(size_t)b.y1 * o->ew + b.x0], D[(size_t)b.y1 * o->ew + b.x1]);
                     de /= t->scaleV;
                     double di = dt_texel(o, o->cur, x, y);
-                    double diff = fmin(fmax(fabs(de - di), 0.0), 10.0);
+                    double diff = fmax(0.0, fmin(fabs(de - di), 10.0));
                     res += diff * P->distTransWeight;
                 }
                 {

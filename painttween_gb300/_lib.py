@@ -78,6 +78,7 @@ SIGNATURES = {
     "pt_set_tiled_kernels": (_I, [_VP, _I]),
     "pt_set_incremental": (_I, [_VP, _I]),
     "pt_get_frame_result": (_I, [_VP, _I, _VP, _VP]),
+    "pt_get_frame_residual": (_I, [_VP, _I, _VP]),
     "pt_serve": (_I, [_I, _VP, _I, _I, ctypes.c_size_t]),
     "pt_server_create": (_I, [_I, _I, ctypes.c_size_t, ctypes.POINTER(_VP)]),
     "pt_server_run": (_I, [_VP, _VP, _I]),

@@ -225,7 +225,7 @@ static __device__ float energy(const Params& P, int x, int y, const Patch& t, co
                 if (P.distTransWeight > 0.f) {
                     float de = ex_sample_dt(P.ex, tx, ty, t.layer) / t.sv;
                     float di = lay_texel(P.img.dt[P.img.cur], P, x, y);
-                    float diff = fminf(fmaxf(fabsf(de - di), 0.0f), 10.0f);
+                    float diff = fmaxf(0.0f, fminf(fabsf(de - di), 10.0f));  // clamp(diff, 0, 10): a NaN difference gives 10
                     res = res + diff * P.distTransWeight;
                 }
                 {  // histogramTerm, :486-495

@@ -2882,6 +2882,18 @@ pt_status pt_get_frame_result(pt_ctx* c, int frame, float* out_rgba, pt_patchxf*
     return fetch_final(c, frame, out_rgba, out_offsets);
 }
 
+pt_status pt_get_frame_residual(pt_ctx* c, int frame, float* out_residual) {
+    if (!c || !out_residual) return PT_ERR_INVALID;
+    if (!c->initialized || !c->have_params) return fail(c, PT_ERR_STATE, "context not initialized");
+    CU(cudaSetDevice(c->device));
+    auto it = c->store.find(std::make_tuple(c->out_level, frame, c->out_pass));
+    if (it == c->store.end()) return fail(c, PT_ERR_STATE, "no final output for frame %d", frame);
+    size_t n = (size_t)it->second.w * it->second.h;
+    CU(cudaMemcpyAsync(out_residual, it->second.res, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return PT_OK;
+}
+
 pt_status pt_host_alloc(size_t bytes, void** out) {
     if (!out) return PT_ERR_INVALID;
     *out = nullptr;

@@ -224,7 +224,7 @@ __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, 
                     if (P.distTransWeight > 0.f) {
                         float de = ex_sample_dt(ex_mode<HW>(P.ex), tx, ty, c.layer) / c.sv;
                         float di = lay_texel(P.img.dt[P.img.cur], P, px.x, px.y);
-                        float diff = fminf(fmaxf(fabsf(de - di), 0.0f), 10.0f);
+                        float diff = fmaxf(0.0f, fminf(fabsf(de - di), 10.0f));  // clamp(diff, 0, 10): a NaN difference gives 10
                         res = res + diff * P.distTransWeight;
                     }
                     {
@@ -581,7 +581,7 @@ __device__ __forceinline__ float tap_value(const Params& P, const TileSmem<R, TM
         if (P.distTransWeight > 0.f) {
             float de = ex_sample_dt(ex_mode<HW>(P.ex), tx, ty, e.layer) / e.sv;
             float di = lay_texel(P.img.dt[P.img.cur], P, q.x, q.y);
-            float diff = fminf(fmaxf(fabsf(de - di), 0.0f), 10.0f);
+            float diff = fmaxf(0.0f, fminf(fabsf(de - di), 10.0f));  // clamp(diff, 0, 10): a NaN difference gives 10
             res = res + diff * P.distTransWeight;
         }
         {

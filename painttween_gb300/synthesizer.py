@@ -338,6 +338,13 @@ class Synthesizer(TexSynth):
                     "pt_synthesize_animation")
         return results
 
+    def get_frame_residual(self, frame):
+        """The residual stored with a synthesised frame's final offsets."""
+        h, w = self._final_shape()
+        out = np.empty((h, w), np.float32)
+        self._check(lib().pt_get_frame_residual(self.h, frame, _p(out)), "pt_get_frame_residual")
+        return out
+
     def get_frame_result(self, frame, rgba=None, offsets=None):
         """Final output and offsets of one synthesised frame, written into the
         given arrays (e.g. host_array ones) or new ones."""

@@ -124,3 +124,21 @@ def config_params(r=2, levels=3, iterations=2, filter_mode=None):
 
 # both sampling arithmetics: the texture unit's (the default) and exact FP32
 FILTER_MODES = [_abi.FILTER_TEXTURE, _abi.FILTER_EXACT]
+
+
+def agreement(offs, res, out, ref_offs, ref_res, ref_out, energy_tol=1e-4):
+    """Agreement of a synthesis with the reference's by the stated tolerance:
+    the fraction of pixels whose offset record is identical, the fraction
+    whose record differs but whose energy (stored residual) is equal within
+    `energy_tol` relative, their sum, and the PSNR of the stylised output
+    (peak 1)."""
+    same = (patch_bytes(offs) == patch_bytes(ref_offs)).all(-1)
+    a = np.asarray(res, np.float64)
+    b = np.asarray(ref_res, np.float64)
+    close = np.abs(a - b) <= energy_tol * np.maximum(np.abs(a), np.abs(b)) + 1e-12
+    close |= (np.isnan(a) & np.isnan(b))
+    equal_energy = (~same) & close
+    mse = float(np.mean((np.asarray(out, np.float64) - np.asarray(ref_out, np.float64)) ** 2))
+    return {"identical": float(same.mean()), "equal_energy": float(equal_energy.mean()),
+            "agree": float((same | equal_energy).mean()),
+            "psnr_db": float(10 * np.log10(1.0 / max(mse, 1e-20)))}
