@@ -102,32 +102,55 @@ typedef struct {
 /* polynomial elementary functions (shared contract with the CUDA side)     */
 /* ------------------------------------------------------------------------ */
 
-/* sin/cos: k = rint(t*2/pi), r = t - k*pi/2 (two-term Cody-Waite with fma),
- * Taylor series to r^9 (sin) and r^10 (cos) on |r| <= pi/4. */
+/* sin t and cos t rounded to float.  The values are formed in double
+ * precision -- Cody-Waite reduction by pi/2 in three parts (the first two of
+ * 33 bits, so k*P1 and k*P2 are exact for |k| < 2^20), then the Taylor
+ * series of sin to r^17 and of cos to r^18 on |r| <= pi/4 by Horner's rule
+ * with fused multiply-adds, relative error below 2^-58 -- so the float
+ * results are the correctly rounded sin t and cos t unless the exact value
+ * lies within that error of a midpoint between two floats.  The reference
+ * calls CUDA's sinf/cosf, which agree with the correctly rounded values on
+ * all but a small fraction of arguments; the CUDA kernels use this same
+ * routine (pt_device.cuh).  NaN and +-inf give the canonical NaN. */
 static void pt_sincosf(float t, float* s, float* c) {
-    const float two_over_pi = 0x1.45f306p-1f;
-    const float pio2_hi = 0x1.921fb6p+0f;
-    const float pio2_lo = -0x1.777a5cp-25f;
-    float k = rintf(t * two_over_pi);
-    float r = fmaf(-k, pio2_hi, t);
-    r = fmaf(-k, pio2_lo, r);
-    float r2 = r * r;
-    float ps = fmaf(r2, (float)(1.0 / 362880.0), (float)(-1.0 / 5040.0));
-    ps = fmaf(r2, ps, (float)(1.0 / 120.0));
-    ps = fmaf(r2, ps, (float)(-1.0 / 6.0));
-    ps = ps * r2;
-    float sr = fmaf(r, ps, r);
-    float pc = fmaf(r2, (float)(-1.0 / 3628800.0), (float)(1.0 / 40320.0));
-    pc = fmaf(r2, pc, (float)(-1.0 / 720.0));
-    pc = fmaf(r2, pc, (float)(1.0 / 24.0));
-    pc = fmaf(r2, pc, -0.5f);
-    float cr = fmaf(r2, pc, 1.0f);
-    int q = f2i(k) & 3;
+    if (!(t == t) || isinf(t)) {
+        uint32_t u = 0x7fffffffu;
+        float q;
+        memcpy(&q, &u, 4);
+        *s = q; *c = q;
+        return;
+    }
+    const double x = (double)t;
+    const double k = rint(x * 0x1.45f306dc9c883p-1);
+    double r = fma(-k, 0x1.921fb544p+0, x);
+    r = fma(-k, 0x1.0b4611a6p-34, r);
+    r = fma(-k, 0x1.3198a2e037073p-69, r);
+    const double r2 = r * r;
+    double ps = 1.0 / 355687428096000.0;          /* 1/17! */
+    ps = fma(ps, r2, -1.0 / 1307674368000.0);      /* 1/15! */
+    ps = fma(ps, r2, 1.0 / 6227020800.0);          /* 1/13! */
+    ps = fma(ps, r2, -1.0 / 39916800.0);           /* 1/11! */
+    ps = fma(ps, r2, 1.0 / 362880.0);              /* 1/9! */
+    ps = fma(ps, r2, -1.0 / 5040.0);               /* 1/7! */
+    ps = fma(ps, r2, 1.0 / 120.0);                 /* 1/5! */
+    ps = fma(ps, r2, -1.0 / 6.0);                  /* 1/3! */
+    const double sr = fma(ps * r2, r, r);
+    double pc = 1.0 / 6402373705728000.0;         /* 1/18! */
+    pc = fma(pc, r2, -1.0 / 20922789888000.0);     /* 1/16! */
+    pc = fma(pc, r2, 1.0 / 87178291200.0);         /* 1/14! */
+    pc = fma(pc, r2, -1.0 / 479001600.0);          /* 1/12! */
+    pc = fma(pc, r2, 1.0 / 3628800.0);             /* 1/10! */
+    pc = fma(pc, r2, -1.0 / 40320.0);              /* 1/8! */
+    pc = fma(pc, r2, 1.0 / 720.0);                 /* 1/6! */
+    pc = fma(pc, r2, -1.0 / 24.0);                 /* 1/4! */
+    pc = fma(pc, r2, 0.5);                         /* 1/2! (subtracted) */
+    const double cr = fma(-pc, r2, 1.0);
+    const int q = (int)((long long)k & 3);
     switch (q) {
-        case 0: *s = sr; *c = cr; break;
-        case 1: *s = cr; *c = -sr; break;
-        case 2: *s = -sr; *c = -cr; break;
-        default: *s = -cr; *c = sr; break;
+        case 0: *s = (float)sr; *c = (float)cr; break;
+        case 1: *s = (float)cr; *c = (float)-sr; break;
+        case 2: *s = (float)-sr; *c = (float)-cr; break;
+        default: *s = (float)-cr; *c = (float)sr; break;
     }
 }
 
@@ -1146,14 +1169,17 @@ void pto_upsample(pto* o, int level) {
             const pt_patchxf* o11 = &base[(size_t)(lcy + 1) * o->W + lcx + 1];
             float a = cx - (float)lcx, b = cy - (float)lcy;
             float w00 = (1 - a) * (1 - b), w10 = a * (1 - b), w01 = (1 - a) * b, w11 = a * b;
-            float ix = w00 * o00->x; ix = fmaf(w10, o10->x, ix); ix = fmaf(w01, o01->x, ix); ix = fmaf(w11, o11->x, ix);
-            float iy = w00 * o00->y; iy = fmaf(w10, o10->y, iy); iy = fmaf(w01, o01->y, iy); iy = fmaf(w11, o11->y, iy);
+            /* the reference's sum as nvcc contracts it: the first product fused
+             * with the second, rounded; then fused multiply-adds (measured on
+             * the reference's upsample kernel) */
+            float ix = fmaf(w00, o00->x, w10 * o10->x); ix = fmaf(w01, o01->x, ix); ix = fmaf(w11, o11->x, ix);
+            float iy = fmaf(w00, o00->y, w10 * o10->y); iy = fmaf(w01, o01->y, iy); iy = fmaf(w11, o11->y, iy);
             f2 up = {fmaf(ix, 2.0f, 0.5f), fmaf(iy, 2.0f, 0.5f)};
             const pt_patchxf* cs[4] = {o00, o10, o01, o11};
             int far = 0;
             for (int q = 0; q < 4; q++) {
                 float dx = ix - cs[q]->x, dy = iy - cs[q]->y;
-                if (fmaf(dy, dy, dx * dx) > 16.0f) far = 1;
+                if (fmaf(dx, dx, dy * dy) > 16.0f) far = 1; /* length2: x*x + y*y, first product fused */
             }
             if (far) {
                 int rcx = (int)roundf(cx), rcy = (int)roundf(cy);

@@ -207,16 +207,19 @@ __global__ void k_upsample(const Params P, PatchPlanes work, PatchPlanes border_
     float4 o11 = __ldg(P.off.A + (size_t)(lcy + 1) * P.W + lcx + 1);
     float a = cx - (float)lcx, b = cy - (float)lcy;
     float w00 = (1 - a) * (1 - b), w10 = a * (1 - b), w01 = (1 - a) * b, w11 = a * b;
-    float ix = w00 * o00.x; ix = fmaf(w10, o10.x, ix); ix = fmaf(w01, o01.x, ix); ix = fmaf(w11, o11.x, ix);
-    float iy = w00 * o00.y; iy = fmaf(w10, o10.y, iy); iy = fmaf(w01, o01.y, iy); iy = fmaf(w11, o11.y, iy);
+    // the reference's sum as nvcc contracts it (the first product fused with
+    // the second, rounded, then the others added by fused multiply-adds;
+    // measured on its upsample kernel)
+    float ix = fmaf(w00, o00.x, w10 * o10.x); ix = fmaf(w01, o01.x, ix); ix = fmaf(w11, o11.x, ix);
+    float iy = fmaf(w00, o00.y, w10 * o10.y); iy = fmaf(w01, o01.y, iy); iy = fmaf(w11, o11.y, iy);
     float2 up = make_float2(fmaf(ix, 2.0f, 0.5f), fmaf(iy, 2.0f, 0.5f));
     bool far = false;
     {
         float dx, dy;
-        dx = ix - o00.x; dy = iy - o00.y; far |= fmaf(dy, dy, dx * dx) > 16.0f;
-        dx = ix - o10.x; dy = iy - o10.y; far |= fmaf(dy, dy, dx * dx) > 16.0f;
-        dx = ix - o01.x; dy = iy - o01.y; far |= fmaf(dy, dy, dx * dx) > 16.0f;
-        dx = ix - o11.x; dy = iy - o11.y; far |= fmaf(dy, dy, dx * dx) > 16.0f;
+        dx = ix - o00.x; dy = iy - o00.y; far |= fmaf(dx, dx, dy * dy) > 16.0f;
+        dx = ix - o10.x; dy = iy - o10.y; far |= fmaf(dx, dx, dy * dy) > 16.0f;
+        dx = ix - o01.x; dy = iy - o01.y; far |= fmaf(dx, dx, dy * dy) > 16.0f;
+        dx = ix - o11.x; dy = iy - o11.y; far |= fmaf(dx, dx, dy * dy) > 16.0f;
     }
     if (far) {
         int rcx = (int)roundf(cx), rcy = (int)roundf(cy);
