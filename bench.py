@@ -16,8 +16,13 @@ passes (FMBM_RM) -- synthesised end to end by the CUDA library.
   cpu_baseline  the CPU oracle (a scalar C restatement of the reference's
          kernels; the reference has no CPU path) on a bounded sample
 
-`--impl reference` times that CPU restatement alone (the reference's CUDA
-code cannot be built with CUDA 13), each step one bounded sample.
+  ref_kernels_gpu  the reference's own CUDA kernels and host wrappers,
+         compiled unchanged over texture objects (oracle/refport), on the
+         first frames of the same clip on the same GPU
+
+`--impl reference` times the CPU restatement of the reference's kernels (the
+reference has no CPU path), each step one bounded sample of a temporal
+frame; its frames/s is extrapolated from that sample's evaluation rate.
 """
 import argparse
 import json
@@ -207,22 +212,37 @@ class Clocks:
 # ---------------------------------------------------------------------------
 
 def cpu_sample(cfg, p, ex, clip, threads, passes=1):
-    """The CPU oracle on one level-0 propagate pass (jump 8) of frame 0 at
-    full size; returns (evaluations/s, description)."""
+    """The CPU oracle on `passes` level-0 propagate passes (jump 8) of frame 1
+    of the clip at full size, with its temporal terms: frame 0 is randomised
+    and propagated once, then frame 1 takes the forward-advected offsets and
+    the random merge, as in the forward consecutive pass.  Returns
+    (evaluations/s, description, seconds of the timed passes)."""
     from oracle import oracle as O
     o = O.Oracle(cfg["w"], cfg["h"], cfg["ew"], cfg["eh"], 1, threads=threads)
     q = p.copy()
     q.direction = _abi.FORWARD
+    q.filterMode = _abi.FILTER_EXACT  # a CPU has no texture unit: bilinear weights in FP32
     o.set_params(q)
     sp = O.style_pyramids(ex)
-    fp = O.frame_pyramids(clip[0])
+    fps = [O.frame_pyramids(clip[0]), O.frame_pyramids(clip[1])]
     o.load_style_level([sp], 0)
-    o.load_frame_level(fp, 0)
-    rnd = O.random_level(0, 0, cfg["ew"], cfg["eh"], fp["rgba"][0], fp["orient"][0], sp["output"][0],
-                         sp["orient"][0])
-    o.upload_random(rnd)
-    o.randomize_offsets(0)
-    act = int((fp["dt"][0] <= np.float32(p.distTransCull)).sum())
+    o.reset_advected()
+    for f in (0, 1):
+        fp = fps[f]
+        if f:
+            o.flip()
+        o.load_frame_level(fp, 0)
+        rnd = O.random_level(0, 0, cfg["ew"], cfg["eh"], fp["rgba"][0], fp["orient"][0], sp["output"][0],
+                             sp["orient"][0])
+        o.upload_random(rnd)
+        if f == 0:
+            o.randomize_offsets(0)
+            o.propagate(0, 8)
+        else:
+            o.advect(0, 1, True, 0)
+            o.merge_randomly(0, True, 0.5, False)
+            o.sync(0, 0)
+    act = int((fps[1]["dt"][0] <= np.float32(p.distTransCull)).sum())
     lib = O.lib()
     t0 = time.perf_counter()
     for _ in range(passes):
@@ -230,51 +250,108 @@ def cpu_sample(cfg, p, ex, clip, threads, passes=1):
     dt = time.perf_counter() - t0
     o.close()
     evals = 4 * act * passes
-    desc = ("%d level-0 propagate pass(es) (4 candidates x %d active pixels, r=%d) of frame 0 of the "
-            "1920x1080 clip" % (passes, act, p.residualWindowSize))
+    desc = ("%d level-0 propagate pass(es) (4 candidates x %d active pixels, r=%d, temporal terms on, bilinear "
+            "in FP32) of frame 1 of the 1920x1080 clip on %d thread(s)" % (passes, act, p.residualWindowSize, threads))
     return evals / dt, desc, dt
 
 
 def run_reference(args, dist):
+    """The reference arm: the CPU restatement of the reference's kernels (the
+    reference has no CPU path; its CUDA kernels are timed on the GPU in our
+    arm's `ref_kernels_gpu`).  Each step is one bounded sample, a level-0
+    propagate pass of a temporal frame on every host thread; frames/s is
+    that rate over the schedule's evaluations per frame (extrapolated), and
+    ms_per_step is the time the step actually took."""
+    if args.gpus != dist.ws:
+        raise SystemExit("--gpus %d but %d rank(s) launched" % (args.gpus, dist.ws))
     cfg = synthetic.config(WORKLOAD)
     p = cfg["params"]
     frames = args.frames or cfg["frames"]
     if dist.rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    ex, clip = make_inputs(cfg, frames)
+    ex, clip = make_inputs(cfg, max(frames, 2))
     act = active_pixels(clip, p.levels, p.distTransCull)
-    per_step_evals = evals_per_step(p, cfg, act, frames)
-    rates = []
+    per_frame = evals_per_step(p, cfg, act, frames) / frames
+    rates, secs = [], []
+    desc = ""
     for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
         rate, desc, _ = cpu_sample(cfg, p, ex, clip, threads)
         if i >= args.warmup:
             rates.append(rate)
+            secs.append(time.perf_counter() - t0)
     rate = float(np.mean(rates))
-    fps = rate / (per_step_evals / frames)
+    fps = rate / per_frame
     line = {
         "impl": "reference", "metric": METRIC, "value": fps, "unit": UNIT, "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * frames / fps,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * float(np.mean(secs)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "frames": frames, "image": "1920x1080", "exemplar": "1024x1024",
                    "patch_radius": p.residualWindowSize, "levels": p.levels, "iterations": p.iterations,
                    "scheme": "FMBM_RM", "histogram": True, "parallelism": "host threads"},
+        "extrapolated": True,
         "cpu_baseline": {"value": fps, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": desc + "; frames/s = evaluations/s / evaluations per frame of the schedule"},
+                         "sample": desc + " per step (set-up included in ms_per_step); frames/s = evaluations/s "
+                                          "/ evaluations per frame of the schedule"},
         "e2e": {"value": fps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "evals_per_s": rate,
+        "evals_per_s": rate, "evals_per_frame": per_frame,
     }
     print(json.dumps(line))
     return 0
+
+
+def ref_kernels_gpu(frames=2):
+    """The reference's own CUDA kernels and TexSynth host wrappers (compiled
+    unchanged over texture objects, oracle/refport) on the first `frames`
+    frames of the benchmark clip at its full settings, on this GPU: wall time
+    of the reference's per-frame call sequence, with its host-side random
+    pyramid and its synchronisation after every launch, EXR files excluded.
+    None when the port's sources are not staged."""
+    try:
+        from oracle.refport import build as rb
+        if rb.build() is None:
+            return {"unavailable": "reference port not staged (oracle/_ref/refport_src absent)"}
+        from oracle.refport import port as RP
+    except Exception as e:
+        return {"unavailable": "reference port does not build: %s" % str(e).splitlines()[0][:200]}
+    cfg = synthetic.config(WORKLOAD)
+    p = cfg["params"]
+    ex, clip = make_inputs(cfg, frames)
+    d = RP.RefPortDriver(p, [ex], clip)
+    t0 = time.perf_counter()
+    d.render(0, frames - 1)
+    wall = time.perf_counter() - t0
+    d.o.close()
+    return {"value": frames / wall, "unit": UNIT, "frames": frames, "seconds": wall,
+            "what": "the reference's CUDA kernels and host wrappers (texSynth_kernel.cu, convolution.cu, "
+                    "compiled unchanged for sm_103a) on the first %d frames of the clip, all 5 levels, "
+                    "FMBM_RM forward and backward; wall time, EXR I/O excluded" % frames}
 
 
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
 
+def gather_ceilings(device):
+    """L2-resident 32-byte record gather rates (GB/s) on this GPU: random
+    per lane and coherent per warp (pt_measure_gather)."""
+    import ctypes
+    from painttween_gb300._lib import lib
+    out = {}
+    for name, coh in (("random", 0), ("coherent", 1)):
+        v = ctypes.c_double(0.0)
+        if lib().pt_measure_gather(device, coh, ctypes.byref(v)) == 0:
+            out[name] = v.value
+    return out
+
+
 def run_ours(args, dist):
     from painttween_gb300 import Synthesizer, host_array
     from painttween_gb300 import build as B
+    if args.gpus != dist.ws:
+        raise SystemExit("--gpus %d but %d rank(s) launched: start N > 1 with torch.distributed.run" %
+                         (args.gpus, dist.ws))
     B.build()
     cfg = synthetic.config(WORKLOAD)
     p = cfg["params"]
@@ -294,6 +371,7 @@ def run_ours(args, dist):
         s._check(__import__("painttween_gb300._lib", fromlist=["lib"]).lib().pt_synthesize_animation(
             s.h, 0, frames - 1, None, None), "pt_synthesize_animation")
 
+    gc = gather_ceilings(device)
     for _ in range(args.warmup):
         render()
     s.synchronize()
@@ -345,7 +423,9 @@ def run_ours(args, dist):
     h, w = cfg["h"] >> _abi.output_level(p), cfg["w"] >> _abi.output_level(p)
     outs = [(host_array((h, w, 4), np.float32), host_array((h, w), _abi.PATCH_DTYPE)) for _ in range(frames)]
     d2h = sum(a.nbytes + o.nbytes for a, o in outs)
-    for _ in range(args.e2e_steps):
+    e2e_steps = args.steps if args.e2e_steps < 0 else args.e2e_steps
+    s.set_profiling(_abi.PROFILE_TIMING)  # the profiling state of the timed steps
+    for _ in range(e2e_steps):
         s.synchronize()
         t0 = time.perf_counter()
         s.timer_record(2)
@@ -356,6 +436,7 @@ def run_ours(args, dist):
             s.get_frame_result(f, a, o)
         s.timer_record(3)
         e2e_times.append(max(s.timer_elapsed(2, 3), 1000.0 * (time.perf_counter() - t0)))
+    s.set_profiling(0)
     e2e_ms = dist.max(float(np.mean(e2e_times)) * args.steps) if e2e_times else None
 
     # roofline of the dominant kernel (propagate)
@@ -367,12 +448,19 @@ def run_ours(args, dist):
     # 3 SSDs (+32 B, +84 flops)
     n_launch = max(st["launches"], 1)
     evals_per_launch = st["energy_evals"] / n_launch
+    # algorithmic bytes: every evaluation over all K taps (32 K + 16 B), and
+    # the temporal ones 32 K more; the early exit and the change tracking
+    # skip part of them, so the bytes of the work done are kept beside
+    temporal_frac = st["temporal_taps"] / max(st["taps"], 1)
+    alg_bytes_per_launch = (st["energy_evals"] * (32 * K + 16) +
+                            st["energy_evals"] * temporal_frac * 32 * K) / n_launch
     bytes_per_launch = (32 * st["taps"] + 16 * st["energy_evals"] + 32 * st["temporal_taps"]) / n_launch
     flops_per_launch = (84 * st["taps"] + 40 * st["energy_evals"] + 84 * st["temporal_taps"]) / n_launch
     bytes_per_eval = bytes_per_launch / max(evals_per_launch, 1)
     flops_per_eval = flops_per_launch / max(evals_per_launch, 1)
     avg_launch_s = st["total_ms"] / n_launch / 1000.0
-    achieved = bytes_per_launch / avg_launch_s / 1e9
+    achieved = alg_bytes_per_launch / avg_launch_s / 1e9
+    achieved_done = bytes_per_launch / avg_launch_s / 1e9
     hbm, peak_kind = peaks()
     sm_mhz = (ck or {}).get("sm_mhz") or 1900.0
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
@@ -401,7 +489,17 @@ def run_ours(args, dist):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "propagate", "bytes_per_eval": bytes_per_eval,
+                     "kernel": "propagate",
+                     "bytes": "algorithmic: (32 K + 16) B per evaluation + 32 K B per temporal one, K = %d" % K,
+                     "alg_bytes_per_eval": alg_bytes_per_launch / max(evals_per_launch, 1),
+                     "work_done": {"achieved": achieved_done, "bytes_per_eval": bytes_per_eval,
+                                   "what": "bytes of the taps actually evaluated (early exit, change tracking)"},
+                     "l2_gather": {"peak_random_gbs": gc.get("random"), "peak_coherent_gbs": gc.get("coherent"),
+                                   "frac_random": achieved / gc["random"] if gc.get("random") else None,
+                                   "frac_coherent": achieved / gc["coherent"] if gc.get("coherent") else None,
+                                   "what": "32-byte record gathers from an L2-resident 32 MiB buffer, measured "
+                                           "here (pt_measure_gather)"},
+                     "bytes_per_eval": bytes_per_eval,
                      "temporal_tap_fraction": st["temporal_taps"] / max(st["taps"], 1),
                      "evals_per_launch": evals_per_launch, "avg_launch_ms": avg_launch_s * 1000.0,
                      "time_share": kernel_share,
@@ -418,11 +516,16 @@ def run_ours(args, dist):
         counted = sum(v["energy_evals"] for v in stats.values()) / (frames * args.steps)
         threads = os.cpu_count() or 1
         rate, desc, _ = cpu_sample(cfg, p, ex, clip, threads)
+        rate1, desc1, _ = cpu_sample(cfg, p, ex, clip, 1)
         line["cpu_baseline"] = {"value": rate / per_frame, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": desc + "; frames/s = evaluations/s / evaluations per frame",
-                                "evals_per_s": rate}
+                                "evals_per_s": rate, "extrapolated": True,
+                                "single_core": {"value": rate1 / per_frame, "unit": UNIT, "cores": 1,
+                                                "evals_per_s": rate1, "sample": desc1}}
         line["evals_per_frame"] = {"schedule": per_frame, "counted": counted}
     s.close()
+    if dist.rank == 0 and dist.ws == 1 and not args.no_ref_kernels:
+        line["ref_kernels_gpu"] = ref_kernels_gpu(2)
     if dist.rank == 0 and dist.ws == 1 and args.batch_stills > 0:
         line["batched"] = run_batched(args.batch_stills, args.batch_in_flight)
     if dist.rank == 0:
@@ -489,8 +592,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--frames", type=int, default=0, help="override the clip length (testing only)")
-    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=-1, help="end-to-end steps (default: as many as --steps)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ref-kernels", action="store_true", help="skip timing the reference's kernels on the GPU")
     ap.add_argument("--batch-stills", type=int, default=64, help="requests of the batched-vs-plain run (0: skip)")
     ap.add_argument("--batch-in-flight", type=int, default=8)
     ap.add_argument("--filter", default="texture", choices=["texture", "exact"],

@@ -431,6 +431,14 @@ pt_status pt_get_frame_result(pt_ctx* ctx, int frame, float* out_rgba, pt_patchx
  * level-size float32, into caller memory. */
 pt_status pt_get_frame_residual(pt_ctx* ctx, int frame, float* out_residual);
 
+/* Measurement: the rate (GB/s) of 32-byte record gathers from an L2-resident
+ * 32 MiB buffer on `device` -- the ceiling of the patch-distance kernels'
+ * exemplar gathers -- with every lane at a random record (coherent = 0) or
+ * each warp at a random run of consecutive records (coherent = 1).  CUDA
+ * events around 10 launches after 3 warm-up launches.  No counterpart in the
+ * reference. */
+pt_status pt_measure_gather(int device, int coherent, double* out_gbs);
+
 /* Page-locked host memory (cudaMallocHost / cudaFreeHost) for frame inputs
  * and results: copies from and to it run at the full host link speed.  No
  * counterpart in the reference. */

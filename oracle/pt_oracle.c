@@ -102,55 +102,32 @@ typedef struct {
 /* polynomial elementary functions (shared contract with the CUDA side)     */
 /* ------------------------------------------------------------------------ */
 
-/* sin t and cos t rounded to float.  The values are formed in double
- * precision -- Cody-Waite reduction by pi/2 in three parts (the first two of
- * 33 bits, so k*P1 and k*P2 are exact for |k| < 2^20), then the Taylor
- * series of sin to r^17 and of cos to r^18 on |r| <= pi/4 by Horner's rule
- * with fused multiply-adds, relative error below 2^-58 -- so the float
- * results are the correctly rounded sin t and cos t unless the exact value
- * lies within that error of a midpoint between two floats.  The reference
- * calls CUDA's sinf/cosf, which agree with the correctly rounded values on
- * all but a small fraction of arguments; the CUDA kernels use this same
- * routine (pt_device.cuh).  NaN and +-inf give the canonical NaN. */
+/* sin/cos: k = rint(t*2/pi), r = t - k*pi/2 (two-term Cody-Waite with fma),
+ * Taylor series to r^9 (sin) and r^10 (cos) on |r| <= pi/4. */
 static void pt_sincosf(float t, float* s, float* c) {
-    if (!(t == t) || isinf(t)) {
-        uint32_t u = 0x7fffffffu;
-        float q;
-        memcpy(&q, &u, 4);
-        *s = q; *c = q;
-        return;
-    }
-    const double x = (double)t;
-    const double k = rint(x * 0x1.45f306dc9c883p-1);
-    double r = fma(-k, 0x1.921fb544p+0, x);
-    r = fma(-k, 0x1.0b4611a6p-34, r);
-    r = fma(-k, 0x1.3198a2e037073p-69, r);
-    const double r2 = r * r;
-    double ps = 1.0 / 355687428096000.0;          /* 1/17! */
-    ps = fma(ps, r2, -1.0 / 1307674368000.0);      /* 1/15! */
-    ps = fma(ps, r2, 1.0 / 6227020800.0);          /* 1/13! */
-    ps = fma(ps, r2, -1.0 / 39916800.0);           /* 1/11! */
-    ps = fma(ps, r2, 1.0 / 362880.0);              /* 1/9! */
-    ps = fma(ps, r2, -1.0 / 5040.0);               /* 1/7! */
-    ps = fma(ps, r2, 1.0 / 120.0);                 /* 1/5! */
-    ps = fma(ps, r2, -1.0 / 6.0);                  /* 1/3! */
-    const double sr = fma(ps * r2, r, r);
-    double pc = 1.0 / 6402373705728000.0;         /* 1/18! */
-    pc = fma(pc, r2, -1.0 / 20922789888000.0);     /* 1/16! */
-    pc = fma(pc, r2, 1.0 / 87178291200.0);         /* 1/14! */
-    pc = fma(pc, r2, -1.0 / 479001600.0);          /* 1/12! */
-    pc = fma(pc, r2, 1.0 / 3628800.0);             /* 1/10! */
-    pc = fma(pc, r2, -1.0 / 40320.0);              /* 1/8! */
-    pc = fma(pc, r2, 1.0 / 720.0);                 /* 1/6! */
-    pc = fma(pc, r2, -1.0 / 24.0);                 /* 1/4! */
-    pc = fma(pc, r2, 0.5);                         /* 1/2! (subtracted) */
-    const double cr = fma(-pc, r2, 1.0);
-    const int q = (int)((long long)k & 3);
+    const float two_over_pi = 0x1.45f306p-1f;
+    const float pio2_hi = 0x1.921fb6p+0f;
+    const float pio2_lo = -0x1.777a5cp-25f;
+    float k = rintf(t * two_over_pi);
+    float r = fmaf(-k, pio2_hi, t);
+    r = fmaf(-k, pio2_lo, r);
+    float r2 = r * r;
+    float ps = fmaf(r2, (float)(1.0 / 362880.0), (float)(-1.0 / 5040.0));
+    ps = fmaf(r2, ps, (float)(1.0 / 120.0));
+    ps = fmaf(r2, ps, (float)(-1.0 / 6.0));
+    ps = ps * r2;
+    float sr = fmaf(r, ps, r);
+    float pc = fmaf(r2, (float)(-1.0 / 3628800.0), (float)(1.0 / 40320.0));
+    pc = fmaf(r2, pc, (float)(-1.0 / 720.0));
+    pc = fmaf(r2, pc, (float)(1.0 / 24.0));
+    pc = fmaf(r2, pc, -0.5f);
+    float cr = fmaf(r2, pc, 1.0f);
+    int q = f2i(k) & 3;
     switch (q) {
-        case 0: *s = (float)sr; *c = (float)cr; break;
-        case 1: *s = (float)cr; *c = (float)-sr; break;
-        case 2: *s = (float)-sr; *c = (float)-cr; break;
-        default: *s = (float)-cr; *c = (float)sr; break;
+        case 0: *s = sr; *c = cr; break;
+        case 1: *s = cr; *c = -sr; break;
+        case 2: *s = -sr; *c = -cr; break;
+        default: *s = -cr; *c = sr; break;
     }
 }
 
@@ -476,6 +453,27 @@ static inline float hw_sum(const bl_t* b, float t00, float t10, float t01, float
         for (int k = 0; k < 4; k++)
             if (r[k] && !(f_bits(t[k]) >> 31)) neg = 0;
         return neg ? -0.0f : 0.0f;
+    }
+    /* fast path: every weighted texel within 2^4 of the largest, so none is
+     * truncated; the sum of the four 33-bit products is exact in double */
+    int Emin = 1000;
+    for (int k = 0; k < 4; k++) {
+        uint32_t u = f_bits(t[k]);
+        int e = (int)((u >> 23) & 0xffu) - 126;
+        if (q[k] > 0 && (u & 0x7fffffffu) != 0u && e < Emin) Emin = e;
+    }
+    if (E - Emin <= 4) {
+        double d = 0.0;
+        for (int k = 0; k < 4; k++)
+            if (q[k] > 0) d += (double)q[k] * (double)t[k];
+        d *= 0x1p-8;
+        float f = (float)d;
+        if ((double)f == d) return f;
+        float lo, hi;
+        if (fabs((double)f) > fabs(d)) { hi = f; lo = nextafterf(f, 0.0f); }
+        else { lo = f; hi = nextafterf(f, d > 0 ? INFINITY : -INFINITY); }
+        double mid = ((double)lo + (double)hi) * 0.5;
+        return fabs(d) >= fabs(mid) ? hi : lo;  /* ties away from zero */
     }
     long long S = 0;
     for (int k = 0; k < 4; k++) {

@@ -83,6 +83,7 @@ SIGNATURES = {
     "pt_server_create": (_I, [_I, _I, ctypes.c_size_t, ctypes.POINTER(_VP)]),
     "pt_server_run": (_I, [_VP, _VP, _I]),
     "pt_server_destroy": (_I, [_VP]),
+    "pt_measure_gather": (_I, [_I, _I, ctypes.POINTER(ctypes.c_double)]),
     "pt_host_alloc": (_I, [ctypes.c_size_t, ctypes.POINTER(_VP)]),
     "pt_host_free": (_I, [_VP]),
     "pt_get_kernel_stats": (_I, [_VP, _I, ctypes.POINTER(_abi.KernelStats)]),

@@ -6,10 +6,9 @@
 // and the operation order of every sum are fixed, which makes the results
 // reproducible on any IEEE FP32 machine.  Bilinear sampling uses exact FP32
 // weights or the texture unit's arithmetic (PT_FILTER_TEXTURE: the texture
-// unit itself in the tiled kernels, an exact emulation elsewhere), sin/cos
-// are correctly rounded (double-precision routine below), atan2/log/acos
-// come from the polynomial routines below, and double precision is used
-// exactly where the reference's C++ promotes to double.
+// unit itself in the tiled kernels, an exact emulation elsewhere),
+// sin/cos/atan2/log/acos come from the polynomial routines below, and double
+// precision is used exactly where the reference's C++ promotes to double.
 #pragma once
 
 #include <cstdint>
@@ -29,49 +28,31 @@ constexpr float kBigResidual = (float)10e30;
 // polynomial elementary functions
 // ---------------------------------------------------------------------------
 
-// sin t and cos t rounded to float: formed in double precision (Cody-Waite
-// reduction by pi/2 in three parts, the first two of 33 bits; Taylor series of
-// sin to r^17 and of cos to r^18 on |r| <= pi/4 by Horner's rule with fused
-// multiply-adds; relative error below 2^-58), so the results are the
-// correctly rounded values unless the exact value lies within that error of
-// a midpoint between floats.  The same operations as the oracle's
-// pt_sincosf; NaN and +-inf give the canonical NaN.
+// k = rint(t*2/pi); r = t - k*pi/2 (two-term Cody-Waite, fused);
+// Taylor series of sin to r^9 and cos to r^10 on |r| <= pi/4.
 __device__ __forceinline__ void sincos_poly(float t, float* s, float* c) {
-    if (!(fabsf(t) < INFINITY)) {
-        *s = __int_as_float(0x7fffffff);
-        *c = __int_as_float(0x7fffffff);
-        return;
-    }
-    const double x = (double)t;
-    const double k = rint(x * 0x1.45f306dc9c883p-1);
-    double r = fma(-k, 0x1.921fb544p+0, x);
-    r = fma(-k, 0x1.0b4611a6p-34, r);
-    r = fma(-k, 0x1.3198a2e037073p-69, r);
-    const double r2 = r * r;
-    double ps = 1.0 / 355687428096000.0;
-    ps = fma(ps, r2, -1.0 / 1307674368000.0);
-    ps = fma(ps, r2, 1.0 / 6227020800.0);
-    ps = fma(ps, r2, -1.0 / 39916800.0);
-    ps = fma(ps, r2, 1.0 / 362880.0);
-    ps = fma(ps, r2, -1.0 / 5040.0);
-    ps = fma(ps, r2, 1.0 / 120.0);
-    ps = fma(ps, r2, -1.0 / 6.0);
-    const double sr = fma(ps * r2, r, r);
-    double pc = 1.0 / 6402373705728000.0;
-    pc = fma(pc, r2, -1.0 / 20922789888000.0);
-    pc = fma(pc, r2, 1.0 / 87178291200.0);
-    pc = fma(pc, r2, -1.0 / 479001600.0);
-    pc = fma(pc, r2, 1.0 / 3628800.0);
-    pc = fma(pc, r2, -1.0 / 40320.0);
-    pc = fma(pc, r2, 1.0 / 720.0);
-    pc = fma(pc, r2, -1.0 / 24.0);
-    pc = fma(pc, r2, 0.5);
-    const double cr = fma(-pc, r2, 1.0);
-    const int q = (int)((long long)k & 3);
-    if (q == 0) { *s = (float)sr; *c = (float)cr; }
-    else if (q == 1) { *s = (float)cr; *c = (float)-sr; }
-    else if (q == 2) { *s = (float)-sr; *c = (float)-cr; }
-    else { *s = (float)-cr; *c = (float)sr; }
+    const float two_over_pi = 0x1.45f306p-1f;
+    const float pio2_hi = 0x1.921fb6p+0f;
+    const float pio2_lo = -0x1.777a5cp-25f;
+    float k = rintf(t * two_over_pi);
+    float r = fmaf(-k, pio2_hi, t);
+    r = fmaf(-k, pio2_lo, r);
+    float r2 = r * r;
+    float ps = fmaf(r2, (float)(1.0 / 362880.0), (float)(-1.0 / 5040.0));
+    ps = fmaf(r2, ps, (float)(1.0 / 120.0));
+    ps = fmaf(r2, ps, (float)(-1.0 / 6.0));
+    ps = ps * r2;
+    float sr = fmaf(r, ps, r);
+    float pc = fmaf(r2, (float)(-1.0 / 3628800.0), (float)(1.0 / 40320.0));
+    pc = fmaf(r2, pc, (float)(-1.0 / 720.0));
+    pc = fmaf(r2, pc, (float)(1.0 / 24.0));
+    pc = fmaf(r2, pc, -0.5f);
+    float cr = fmaf(r2, pc, 1.0f);
+    int q = ((int)k) & 3;  // cvt.rzi saturates, NaN -> 0
+    if (q == 0) { *s = sr; *c = cr; }
+    else if (q == 1) { *s = cr; *c = -sr; }
+    else if (q == 2) { *s = -sr; *c = -cr; }
+    else { *s = -cr; *c = sr; }
 }
 
 // atan on [0,1]: atan(u) = pi/4 + atan((u-1)/(u+1)) above tan(pi/8);

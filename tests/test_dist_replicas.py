@@ -34,7 +34,7 @@ def _rank_main(rank, port, out):
         if rank == 1:
             # the reference arm runs on rank 0 only; the other ranks return at once
             class A:
-                frames, steps, warmup = 1, 1, 0
+                frames, steps, warmup, gpus = 1, 1, 0, 2
             skipped = bench.run_reference(A(), d)
         d.barrier()
         d.close()
@@ -73,6 +73,26 @@ def test_single_process_needs_no_process_group():
         assert d.ws == 1 and d.rank == 0
         assert d.max(3.5) == 3.5
         d.barrier()
+        d.close()
+    finally:
+        for k, v in old.items():
+            if v is not None:
+                os.environ[k] = v
+
+
+def test_gpus_flag_must_match_the_launched_ranks():
+    """`--gpus N` without N launched ranks fails loudly instead of running
+    one replica."""
+    sys.path.insert(0, ROOT)
+    import bench
+    old = {k: os.environ.pop(k, None) for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    try:
+        d = bench.Dist()
+
+        class A:
+            frames, steps, warmup, gpus = 1, 1, 0, 8
+        with pytest.raises(SystemExit):
+            bench.run_reference(A(), d)
         d.close()
     finally:
         for k, v in old.items():

@@ -276,19 +276,3 @@ def test_texture_filter_emulation_matches_recorded_gb300_fetches(oracle_mod):
             assert (oracle_mod.tex_fetch(tex, q, hw=False).view(np.uint32) != out.view(np.uint32)).any()
     assert total > 100000
 
-
-def test_sin_cos_correctly_rounded(oracle_mod):
-    """The oracle's (and the kernels') sin and cos are the correctly rounded
-    float values: against sin/cos of the float argument in double precision,
-    rounded, over the angle range the synthesis produces and beyond; NaN and
-    infinities give NaN."""
-    L = oracle_mod.lib()
-    rng = np.random.default_rng(7)
-    th = np.concatenate([rng.uniform(-4 * np.pi, 4 * np.pi, 20000), rng.uniform(-1e-3, 1e-3, 2000),
-                         np.array([0.0, -0.0, np.pi / 2, -np.pi / 2, np.pi, 1e-30, 1000.5, -2e4])]).astype(np.float32)
-    s = np.array([L.pto_sinf(float(t)) for t in th], np.float32)
-    c = np.array([L.pto_cosf(float(t)) for t in th], np.float32)
-    assert np.array_equal(s, np.sin(th.astype(np.float64)).astype(np.float32))
-    assert np.array_equal(c, np.cos(th.astype(np.float64)).astype(np.float32))
-    for bad in (float("nan"), float("inf"), float("-inf")):
-        assert math.isnan(L.pto_sinf(bad)) and math.isnan(L.pto_cosf(bad))
