@@ -528,60 +528,188 @@ def run_ours(args, dist):
         line["ref_kernels_gpu"] = ref_kernels_gpu(2)
     if dist.rank == 0 and dist.ws == 1 and args.batch_stills > 0:
         line["batched"] = run_batched(args.batch_stills, args.batch_in_flight)
+    if dist.rank == 0 and dist.ws == 1 and args.serving_window > 0:
+        line["serving"] = run_serving(args.batch_in_flight, args.serving_window, args.serving_budget_gb)
     if dist.rank == 0:
         print(json.dumps(line))
     return 0
 
 
+def _input_pool():
+    """Worker processes (spawned: no CUDA state is inherited) that generate
+    the synthetic request inputs in parallel on the host cores."""
+    import concurrent.futures
+    import multiprocessing
+    return concurrent.futures.ProcessPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1)),
+                                                  mp_context=multiprocessing.get_context("spawn"))
+
+
+def _exemplar_job(size, seed):
+    return synthetic.make_exemplar(size, size, seed=seed)
+
+
+def _still_job(w, h, seed):
+    return synthetic.make_still(w, h, 3, seed=seed)
+
+
+def _clip_job(w, h, n, seed):
+    return synthetic.make_clip(w, h, 3, n, seed=seed)
+
+
+def _pinned(d):
+    """A copy of a dict of arrays in page-locked memory (where a client keeps
+    its request data)."""
+    from painttween_gb300 import host_array
+    out = {}
+    for key, v in d.items():
+        if isinstance(v, np.ndarray):
+            out[key] = host_array(v.shape, v.dtype)
+            out[key][...] = v
+        else:
+            out[key] = v
+    return out
+
+
 def batch_requests(n, seed=7):
     """n independent stills with sizes drawn uniformly from 128x128 to
-    1024x1024, each with an exemplar of 256..1024 px (8 exemplars of the
-    configuration-0 generator, handed to the requests in turn), synthesised
-    with the configuration-0 settings: patch radius 2, 3 levels, 4
-    iterations.  Inputs and results are in page-locked host memory."""
-    from painttween_gb300 import host_array
-
-    def pinned(d):  # the client keeps its request data in page-locked memory
-        out = {}
-        for key, v in d.items():
-            if isinstance(v, np.ndarray):
-                out[key] = host_array(v.shape, v.dtype)
-                out[key][...] = v
-            else:
-                out[key] = v
-        return out
+    1024x1024, each with its own exemplar of a size drawn uniformly from 256
+    to 1024 px (the configuration-0 generator), synthesised with the
+    configuration-0 settings: patch radius 2, 3 levels, 4 iterations.
+    Inputs are in page-locked host memory."""
     rng = np.random.default_rng(seed)
-    sizes = [256, 368, 480, 592, 704, 816, 912, 1024]
-    exs = [pinned(synthetic.make_exemplar(sz, sz, seed=100 + i)) for i, sz in enumerate(sizes)]
+    dims = [tuple(int(v) for v in rng.integers(128, 1025, size=2)) for _ in range(n)]
+    esz = [int(v) for v in rng.integers(256, 1025, size=n)]
+    with _input_pool() as pool:
+        exs = pool.map(_exemplar_job, esz, [100 + i for i in range(n)])
+        sts = pool.map(_still_job, [d[0] for d in dims], [d[1] for d in dims], [1000 + i for i in range(n)])
+        exs, sts = list(exs), list(sts)
     reqs = []
     for i in range(n):
-        w, h = (int(v) for v in rng.integers(128, 1025, size=2))
         p = synthetic.config("still256")["params"]
-        reqs.append(dict(params=p, style=exs[i % len(exs)],
-                         frames=[pinned(synthetic.make_still(w, h, 3, seed=1000 + i))]))
+        reqs.append(dict(params=p, style=_pinned(exs[i]), frames=[_pinned(sts[i])]))
     return reqs
 
 
+def _latencies(res):
+    arr = np.array([r["arrival_ms"] for r in res])
+    done = np.array([r["done_ms"] for r in res])
+    start = np.array([r["start_ms"] for r in res])
+    lat = done - arr
+    return {"requests": len(res), "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "service_p50_ms": float(np.percentile(done - start, 50)),
+            "service_p99_ms": float(np.percentile(done - start, 99)),
+            "requests_per_s": len(res) / (max(done.max() - arr.min(), 1e-6) / 1000.0),
+            "wall_s": float(done.max() - arr.min()) / 1000.0}
+
+
 def run_batched(n, in_flight):
-    """Batched vs plain on the same GPU: the same requests through a server
-    (pt_server) one at a time and `in_flight` at a time (all arriving at
-    once), each after a warm-up run of the same requests.  Latency is each
-    request's service time, from admission to its results written."""
+    """Batched vs plain on the same GPU: the same requests, all arriving at
+    once, through a server (pt_server) one at a time and `in_flight` at a
+    time, each after a warm-up run of the same requests.  Latency is from
+    arrival to the request's results written in host memory; the service
+    time (admission to results) is kept beside it.  The single-request
+    latency is each request's service time on the plain path."""
     from painttween_gb300.serving import Server
     reqs = batch_requests(n)
-    out = {"workload": "%d stills 128-1024 px, exemplars 256-1024 px, r2 / 3 levels / 4 iterations" % n,
-           "latency": "per-request service time (admission to results), ms"}
+    out = {"workload": "%d stills 128-1024 px, each with its own exemplar of 256-1024 px, r2 / 3 levels / 4 "
+                       "iterations, all arriving at once" % n,
+           "latency": "arrival to results in host memory, ms"}
     for name, k in (("plain", 1), ("batched", in_flight)):
-        srv = Server(max_in_flight=k)
-        srv.run(reqs, offsets=False, pinned=True)  # warm-up: the workers' contexts and memory caches
-        t0 = time.perf_counter()
-        res = srv.run(reqs, offsets=False, pinned=True)
-        wall = time.perf_counter() - t0
-        srv.close()
-        lat = np.array([r["done_ms"] - r["start_ms"] for r in res])
-        out[name] = {"in_flight": k, "requests_per_s": len(reqs) / wall, "p50_ms": float(np.percentile(lat, 50)),
-                     "p99_ms": float(np.percentile(lat, 99)), "wall_s": wall}
+        with Server(max_in_flight=k) as srv:
+            srv.run(reqs, offsets=False, pinned=True)  # warm-up: the workers' contexts and memory caches
+            res = srv.run(reqs, offsets=False, pinned=True)
+        out[name] = dict(_latencies(res), in_flight=k)
     out["speedup"] = out["batched"]["requests_per_s"] / out["plain"]["requests_per_s"]
+    out["p99_vs_single"] = out["batched"]["p99_ms"] / out["plain"]["service_p50_ms"]
+    return out
+
+
+def serving_requests(n, seed, clip_pool):
+    """n requests of the serving mix: 70 % stills of 128-1024 px (the
+    configuration-0 settings) and 30 % clips of 8-24 frames (the
+    configuration-1 settings: radius 2, 4 levels, 4 iterations, temporal
+    coherence 0.5), each with its own exemplar of 256-1024 px.  A clip is the
+    first frames of one of `clip_pool`'s 24-frame clips (512x512 to
+    1920x1080, the configuration-1 motion)."""
+    rng = np.random.default_rng(seed)
+    kinds = rng.random(n) < 0.7
+    esz = [int(v) for v in rng.integers(256, 1025, size=n)]
+    dims = [tuple(int(v) for v in rng.integers(128, 1025, size=2)) for _ in range(n)]
+    which = [int(v) for v in rng.integers(0, len(clip_pool), size=n)]
+    nfr = [int(v) for v in rng.integers(8, 25, size=n)]
+    stills = [i for i in range(n) if kinds[i]]
+    with _input_pool() as pool:
+        exs = list(pool.map(_exemplar_job, esz, [5000 + seed * 1000 + i for i in range(n)]))
+        sts = list(pool.map(_still_job, [dims[i][0] for i in stills], [dims[i][1] for i in stills],
+                            [7000 + seed * 1000 + i for i in stills]))
+    sts = dict(zip(stills, sts))
+    reqs = []
+    for i in range(n):
+        if kinds[i]:
+            p = synthetic.config("still256")["params"]
+            frames = [_pinned(sts[i])]
+        else:
+            p = synthetic.config("anim512")["params"]
+            frames = clip_pool[which[i]][:nfr[i]]
+        reqs.append(dict(params=p, style=_pinned(exs[i]), frames=frames, kind="still" if kinds[i] else "clip"))
+    return reqs
+
+
+def run_serving(in_flight, window_s, budget_gb, seed=11):
+    """The serving mix on one GPU.  (1) Capacity: a set of requests arriving
+    at once, through the plain path (one at a time) and the server
+    (`in_flight` at a time).  (2) Poisson arrivals over a window of
+    `window_s` seconds at 80 % of the server's capacity and at the nominal
+    100 requests/s, each run until its queue has drained; latency from
+    arrival, sustained requests/s over the run, and whether the queue stayed
+    bounded (the last quarter's latencies no more than twice the first
+    quarter's)."""
+    from painttween_gb300.serving import Server
+    sizes = [(512, 512), (960, 540), (1280, 720), (1920, 1080)]
+    with _input_pool() as pool:
+        clips = list(pool.map(_clip_job, [s[0] for s in sizes], [s[1] for s in sizes], [24] * len(sizes),
+                              [9000 + k for k in range(len(sizes))]))
+    clip_pool = [[_pinned(fr) for fr in c] for c in clips]
+    del clips
+    budget = int(budget_gb * 1e9)
+    out = {"mix": "70 % stills 128-1024 px (r2, 3 levels, 4 iterations), 30 % clips of 8-24 frames of "
+                  "512x512 / 960x540 / 1280x720 / 1920x1080 (r2, 4 levels, 4 iterations, temporal 0.5, "
+                  "forward + backward passes); each request with its own exemplar of 256-1024 px",
+           "budget_gb": budget_gb, "in_flight": in_flight,
+           "latency": "arrival to results in host memory, ms"}
+    cap_reqs = serving_requests(20, seed, clip_pool)
+    for name, k in (("plain", 1), ("server", in_flight)):
+        with Server(max_in_flight=k, hbm_budget=budget) as srv:
+            srv.run(cap_reqs[:6], offsets=False, pinned=True)  # warm-up
+            res = srv.run(cap_reqs, offsets=False, pinned=True)
+        out["capacity_" + name] = _latencies(res)
+    cap = out["capacity_server"]["requests_per_s"]
+    out["capacity_speedup"] = cap / out["capacity_plain"]["requests_per_s"]
+    rng = np.random.default_rng(seed + 1)
+    runs = []
+    # the nominal rate's window is cut to 50 arrivals, so that its backlog
+    # drains within the run
+    for rate, win in ((0.8 * cap, window_s), (100.0, min(window_s, 0.5))):
+        n = max(4, int(round(rate * win)))
+        reqs = serving_requests(n, seed + 2 + len(runs), clip_pool)
+        t = np.cumsum(rng.exponential(1000.0 / rate, size=n))
+        for r, a in zip(reqs, t):
+            r["arrival_ms"] = float(a)
+        with Server(max_in_flight=in_flight, hbm_budget=budget) as srv:
+            srv.run(cap_reqs[:6], offsets=False, pinned=True)  # warm-up
+            res = srv.run(reqs, offsets=False, pinned=True)
+        lat = np.array([r["latency_ms"] for r in res])
+        q = max(1, n // 4)
+        bounded = bool(np.mean(lat[-q:]) <= 2.0 * np.mean(lat[:q]))
+        st = _latencies(res)
+        still_lat = [r["latency_ms"] for r, rq in zip(res, reqs) if rq["kind"] == "still"]
+        st.update(arrival_rate=rate, window_s=float(t[-1] / 1000.0), bounded=bounded,
+                  still_p50_ms=float(np.percentile(still_lat, 50)) if still_lat else None,
+                  peak_context_gb=max(r["device_bytes"] for r in res) / 1e9)
+        runs.append(st)
+    out["poisson"] = runs
+    ok = [r["arrival_rate"] for r in runs if r["bounded"]]
+    out["max_bounded_rate"] = max(ok) if ok else None
     return out
 
 
@@ -597,6 +725,9 @@ def main():
     ap.add_argument("--no-ref-kernels", action="store_true", help="skip timing the reference's kernels on the GPU")
     ap.add_argument("--batch-stills", type=int, default=64, help="requests of the batched-vs-plain run (0: skip)")
     ap.add_argument("--batch-in-flight", type=int, default=8)
+    ap.add_argument("--serving-window", type=float, default=8.0,
+                    help="seconds of Poisson arrivals per rate of the serving run (0: skip)")
+    ap.add_argument("--serving-budget-gb", type=float, default=150.0)
     ap.add_argument("--filter", default="texture", choices=["texture", "exact"],
                     help="bilinear arithmetic: the texture unit's (the reference's) or exact FP32")
     ap.add_argument("--generic-kernels", action="store_true",

@@ -452,8 +452,11 @@ pt_status pt_host_free(void* p);
  * context and CUDA stream, so the kernels of requests in flight overlap on
  * the GPU (a small request alone leaves most of it idle).  Requests are
  * admitted in arrival order once their arrival time has passed and their
- * estimated device memory fits hbm_budget beside the requests in flight
- * (0: no budget); a request larger than the budget still runs, alone.  Each
+ * device memory fits hbm_budget beside the requests in flight (0: no
+ * budget): the running requests count with the memory their contexts
+ * actually hold once set up (pt_device_bytes; admission waits for that),
+ * the new one with an estimate from its sizes; a request larger than the
+ * budget still runs, alone.  Each
  * result equals pt_synthesize_frame / pt_synthesize_animation of that request
  * on a context of its own.  Returns the first failing request's status, after
  * all requests have run. */
@@ -483,6 +486,7 @@ typedef struct {
     double start_ms;          /* out: when its synthesis started */
     double done_ms;           /* out: when its results were written */
     pt_status status;         /* out */
+    size_t device_bytes;      /* out: device memory its worker context held once the request was set up */
 } pt_request;
 
 pt_status pt_serve(int device, pt_request* requests, int count, int max_in_flight, size_t hbm_budget);

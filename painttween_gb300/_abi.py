@@ -201,4 +201,4 @@ class Request(ctypes.Structure):
                 ("style_ids", ctypes.c_void_p), ("image_w", ctypes.c_int), ("image_h", ctypes.c_int),
                 ("frames", ctypes.c_int), ("inputs", ctypes.POINTER(FrameInputs)), ("out_rgba", ctypes.c_void_p),
                 ("out_offsets", ctypes.c_void_p), ("arrival_ms", ctypes.c_double), ("start_ms", ctypes.c_double),
-                ("done_ms", ctypes.c_double), ("status", ctypes.c_int)]
+                ("done_ms", ctypes.c_double), ("status", ctypes.c_int), ("device_bytes", ctypes.c_size_t)]

@@ -41,17 +41,32 @@ int level_count(int w, int h) {
     return (int)std::min(std::floor(std::log2((float)w)), std::floor(std::log2((float)h)));
 }
 
+// A layered float4 array (one layer per style) bound to a texture object
+// with the reference's sampling state (linear filter, clamp, unnormalised
+// coordinates).  Its extent is a capacity: a level of w x h texels occupies
+// the corner [0, w) x [0, h), its last column and row repeated once beyond
+// (where the capacity allows), and the kernels clamp coordinates to
+// [0, w-1] x [0, h-1] before a fetch that may leave the level.  That gives
+// the texels and weights of clamp addressing on an array of exactly w x h:
+// a clamped coordinate has fraction 0 at the edge, where the array's clamp
+// would blend the edge texel with itself, and the texel beyond the edge that
+// a fraction-0 fetch still addresses holds the edge's value.  Arrays are
+// therefore reused across exemplars of different sizes without cudaFreeArray,
+// which would wait for the whole device.
+struct TexArray {
+    cudaArray_t arr = nullptr;
+    cudaTextureObject_t tex = 0;
+    int cw = 0, ch = 0, layers = 0;
+    size_t bytes = 0;
+};
+
 struct ExLevel {  // one exemplar pyramid level, all styles (base and output planes)
     float4* base = nullptr;
     float4* out = nullptr;
     float4* bo = nullptr;   // base and output interleaved per texel, rebuilt when stale
     bool bo_stale = true;
-    // PT_FILTER_TEXTURE: base and output as layered arrays (one layer per
-    // style) bound to texture objects with the reference's sampling state
-    // (linear filter, clamp, unnormalised coordinates), refreshed when stale
-    cudaArray_t tarr[2] = {nullptr, nullptr};
-    cudaTextureObject_t tex[2] = {0, 0};
-    int tw = 0, th = 0;
+    // PT_FILTER_TEXTURE: base and output as textures, refreshed when stale
+    TexArray ta[2];
     bool tex_stale = true;
     float* orient = nullptr;
     float* dt = nullptr;
@@ -90,6 +105,7 @@ struct pt_ctx {
     std::map<void*, size_t> allocs;
     std::multimap<size_t, void*> cache;  // freed blocks by size
     size_t cached = 0;
+    std::vector<TexArray> tex_free;  // texture arrays not bound to a level (bytes counted in `cached`)
 
     pt_params params{};
     bool have_params = false;
@@ -236,15 +252,25 @@ static pt_status fail(pt_ctx* c, pt_status s, const char* fmt, ...) {
 // cudaFree runs, which would wait for the whole device and stall the other
 // contexts working beside this one.  The cache is released when an
 // allocation would exceed the budget or cudaMalloc fails.
+static void destroy_tex_array(TexArray& t) {
+    if (t.tex) cudaDestroyTextureObject(t.tex);
+    if (t.arr) cudaFreeArray(t.arr);
+    t = TexArray();
+}
+
 static void release_cache(pt_ctx* c) {
-    if (c->cache.empty()) return;
+    if (c->cache.empty() && c->tex_free.empty()) return;
     cudaStreamSynchronize(c->stream);
     for (auto& kv : c->cache) cudaFree(kv.second);
     c->cache.clear();
+    for (auto& t : c->tex_free) destroy_tex_array(t);
+    c->tex_free.clear();
     c->cached = 0;
 }
 // Block sizes are rounded up to classes of 1/8 of a power of two (at most
-// 12.5 % larger than asked), so blocks are reused across nearby sizes.
+// 12.5 % larger than asked); a request takes the smallest cached block that
+// fits if it is at most twice its size, so blocks are reused across requests
+// of different sizes.
 static size_t size_class(size_t bytes) {
     if (bytes <= 4096) return (bytes + 255) & ~(size_t)255;
     size_t top = 1;
@@ -256,8 +282,8 @@ static pt_status dalloc(pt_ctx* c, void** p, size_t bytes) {
     *p = nullptr;
     if (bytes == 0) bytes = 16;
     bytes = size_class(bytes);
-    auto it = c->cache.find(bytes);  // a cached block of this class
-    if (it != c->cache.end()) {
+    auto it = c->cache.lower_bound(bytes);  // the smallest cached block that fits, if at most twice the size
+    if (it != c->cache.end() && it->first <= 2 * bytes) {
         const size_t sz = it->first;
         *p = it->second;
         c->cache.erase(it);
@@ -283,7 +309,7 @@ static pt_status dalloc(pt_ctx* c, void** p, size_t bytes) {
         c->allocated += bytes;
         c->allocs[*p] = bytes;
     }
-    cudaError_t e = cudaMemsetAsync(*p, 0, c->allocs[*p], c->stream);
+    cudaError_t e = cudaMemsetAsync(*p, 0, bytes, c->stream);
     if (e != cudaSuccess) return fail(c, PT_ERR_CUDA, "cudaMemsetAsync: %s", cudaGetErrorString(e));
     return PT_OK;
 }
@@ -406,8 +432,8 @@ static Params make_params(pt_ctx* c, int level) {
         P.ex.ns = c->NS;
         P.ex.hw = p.filterMode == PT_FILTER_TEXTURE;
         if (P.ex.hw && !c->ex->tex_stale) {
-            P.ex.tbase = c->ex->tex[0];
-            P.ex.tout = c->ex->tex[1];
+            P.ex.tbase = c->ex->ta[0].tex;
+            P.ex.tout = c->ex->ta[1].tex;
         }
     }
     P.hwFilter = p.filterMode == PT_FILTER_TEXTURE;
@@ -422,49 +448,104 @@ static Params make_params(pt_ctx* c, int level) {
     return P;
 }
 
-static void free_textures(ExLevel* L) {
+// a level's texture arrays back to the context's free list
+static void free_textures(pt_ctx* c, ExLevel* L) {
     for (int k = 0; k < 2; k++) {
-        if (L->tex[k]) cudaDestroyTextureObject(L->tex[k]);
-        if (L->tarr[k]) cudaFreeArray(L->tarr[k]);
-        L->tex[k] = 0;
-        L->tarr[k] = nullptr;
+        if (L->ta[k].arr) {
+            c->allocated -= L->ta[k].bytes;
+            c->cached += L->ta[k].bytes;
+            c->tex_free.push_back(L->ta[k]);
+        }
+        L->ta[k] = TexArray();
     }
-    L->tw = L->th = 0;
     L->tex_stale = true;
 }
 
-// the layered textures of an exemplar level (PT_FILTER_TEXTURE), copied from
-// its planes after they were written
+// a free texture array of at least w x h texels and `layers` layers (the
+// smallest that fits), else a new one with its extent rounded up to 64
+static pt_status take_tex_array(pt_ctx* c, int w, int h, int layers, TexArray* out) {
+    int best = -1;
+    for (int i = 0; i < (int)c->tex_free.size(); i++) {
+        const TexArray& t = c->tex_free[i];
+        if (t.layers != layers || t.cw < w || t.ch < h) continue;
+        if (best < 0 || t.bytes < c->tex_free[best].bytes) best = i;
+    }
+    if (best >= 0 && c->tex_free[best].bytes <= 4 * (size_t)w * h * layers * sizeof(float4) + (1u << 20)) {
+        *out = c->tex_free[best];
+        c->tex_free.erase(c->tex_free.begin() + best);
+        c->cached -= out->bytes;
+        c->allocated += out->bytes;
+        return PT_OK;
+    }
+    TexArray t;
+    t.cw = (w + 1 + 63) / 64 * 64;  // room for the repeated edge column and row
+    t.ch = (h + 1 + 63) / 64 * 64;
+    t.layers = layers;
+    t.bytes = (size_t)t.cw * t.ch * layers * sizeof(float4);
+    if (c->budget && c->allocated + c->cached + t.bytes > c->budget) release_cache(c);
+    cudaChannelFormatDesc d = cudaCreateChannelDesc<float4>();
+    cudaError_t e = cudaMalloc3DArray(&t.arr, &d, make_cudaExtent(t.cw, t.ch, layers), cudaArrayLayered);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        release_cache(c);
+        e = cudaMalloc3DArray(&t.arr, &d, make_cudaExtent(t.cw, t.ch, layers), cudaArrayLayered);
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, PT_ERR_OOM, "cudaMalloc3DArray(%dx%dx%d) failed: %s", t.cw, t.ch, layers,
+                    cudaGetErrorString(e));
+    }
+    cudaResourceDesc rd;
+    memset(&rd, 0, sizeof rd);
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = t.arr;
+    cudaTextureDesc td;
+    memset(&td, 0, sizeof td);
+    td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 0;
+    e = cudaCreateTextureObject(&t.tex, &rd, &td, nullptr);
+    if (e != cudaSuccess) {
+        destroy_tex_array(t);
+        return fail(c, PT_ERR_CUDA, "cudaCreateTextureObject: %s", cudaGetErrorString(e));
+    }
+    c->allocated += t.bytes;
+    *out = t;
+    return PT_OK;
+}
+
+// one copy of a w x h x layers block of a pitched plane into an array
+static cudaError_t copy_to_array(const float4* src, int pitch_texels, int plane_rows, int sx, int sy, cudaArray_t dst,
+                                 int dx, int dy, int w, int h, int layers, cudaStream_t st) {
+    cudaMemcpy3DParms cp;
+    memset(&cp, 0, sizeof cp);
+    cp.srcPtr = make_cudaPitchedPtr((void*)src, (size_t)pitch_texels * sizeof(float4), pitch_texels, plane_rows);
+    cp.srcPos = make_cudaPos((size_t)sx * sizeof(float4), sy, 0);
+    cp.dstArray = dst;
+    cp.dstPos = make_cudaPos(dx, dy, 0);
+    cp.extent = make_cudaExtent(w, h, layers);
+    cp.kind = cudaMemcpyDeviceToDevice;
+    return cudaMemcpy3DAsync(&cp, st);
+}
+
+// the textures of an exemplar level (PT_FILTER_TEXTURE), copied from its
+// planes after they were written: the level into the array's corner, then
+// its last column, last row and corner texel once more beyond them
 static pt_status refresh_textures(pt_ctx* c, ExLevel* L) {
     if (!L->base) return PT_OK;
-    if (L->tarr[0] && (L->tw != L->w || L->th != L->h)) free_textures(L);
-    if (!L->tex_stale && L->tarr[0]) return PT_OK;
-    cudaChannelFormatDesc d = cudaCreateChannelDesc<float4>();
+    const int w = L->w, h = L->h, ns = c->NS;
+    if (L->ta[0].arr && (L->ta[0].cw < w + 1 || L->ta[0].ch < h + 1 || L->ta[0].layers != ns)) free_textures(c, L);
+    if (!L->tex_stale && L->ta[0].arr) return PT_OK;
     for (int k = 0; k < 2; k++) {
-        if (!L->tarr[k]) {
-            CU(cudaMalloc3DArray(&L->tarr[k], &d, make_cudaExtent(L->w, L->h, c->NS), cudaArrayLayered));
-            cudaResourceDesc rd;
-            memset(&rd, 0, sizeof rd);
-            rd.resType = cudaResourceTypeArray;
-            rd.res.array.array = L->tarr[k];
-            cudaTextureDesc td;
-            memset(&td, 0, sizeof td);
-            td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;
-            td.filterMode = cudaFilterModeLinear;
-            td.readMode = cudaReadModeElementType;
-            td.normalizedCoords = 0;
-            CU(cudaCreateTextureObject(&L->tex[k], &rd, &td, nullptr));
-        }
-        cudaMemcpy3DParms cp;
-        memset(&cp, 0, sizeof cp);
-        cp.srcPtr = make_cudaPitchedPtr((void*)(k ? L->out : L->base), (size_t)L->w * sizeof(float4), L->w, L->h);
-        cp.dstArray = L->tarr[k];
-        cp.extent = make_cudaExtent(L->w, L->h, c->NS);
-        cp.kind = cudaMemcpyDeviceToDevice;
-        CU(cudaMemcpy3DAsync(&cp, c->stream));
+        if (!L->ta[k].arr) TRY(take_tex_array(c, w + 1, h + 1, ns, &L->ta[k]));
+        const float4* src = k ? L->out : L->base;
+        cudaArray_t a = L->ta[k].arr;
+        CU(copy_to_array(src, w, h, 0, 0, a, 0, 0, w, h, ns, c->stream));
+        CU(copy_to_array(src, w, h, w - 1, 0, a, w, 0, 1, h, ns, c->stream));
+        CU(copy_to_array(src, w, h, 0, h - 1, a, 0, h, w, 1, ns, c->stream));
+        CU(copy_to_array(src, w, h, w - 1, h - 1, a, w, h, 1, 1, ns, c->stream));
     }
-    L->tw = L->w;
-    L->th = L->h;
     L->tex_stale = false;
     return PT_OK;
 }
@@ -838,8 +919,10 @@ pt_status pt_destroy(pt_ctx* c) {
     for (auto& e : c->ev_pool) cudaEventDestroy(e);
     for (auto& v : c->ev_pairs)
         for (auto& pr : v) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
-    free_textures(&c->up_ex);
-    for (auto& L : c->style_levels) free_textures(&L);
+    free_textures(c, &c->up_ex);
+    for (auto& L : c->style_levels) free_textures(c, &L);
+    for (auto& t : c->tex_free) destroy_tex_array(t);
+    c->tex_free.clear();
     for (auto& kv : c->allocs) cudaFree(kv.first);
     c->allocs.clear();
     for (auto& kv : c->cache) cudaFree(kv.second);
@@ -1668,7 +1751,7 @@ pt_status pt_set_style(pt_ctx* c, int style, int w, int h, const float* base, co
         for (auto& L : c->style_levels) {
             dfree_t(c, L.base); dfree_t(c, L.out); dfree_t(c, L.bo); dfree_t(c, L.orient); dfree_t(c, L.dt);
             dfree_t(c, L.ids);
-            free_textures(&L);
+            free_textures(c, &L);
         }
         c->style_levels.assign(nlev, ExLevel());
         for (int l = 0; l < nlev; l++) {

@@ -59,17 +59,26 @@ __device__ __forceinline__ void ld_texel(const float4* p, float4* b, float4* o) 
 // With HW (PT_FILTER_TEXTURE, textures bound) both colours come from the
 // texture unit: layered fetches of layer `li` (the clamped style layer) at the
 // texture coordinate u + 0.5, which is the reference's own sampling
-// (PYRAMID_FETCH_LAYER, texSynth_kernel.cu:600-601).
+// (PYRAMID_FETCH_LAYER, texSynth_kernel.cu:600-601).  The level sits in the
+// corner of a larger array with its edge texels repeated once beyond, so
+// outside the fast case the coordinate is clamped to [0, w-1] x [0, h-1]
+// first (NaN to 0): that fetches the texels, with the weights, that clamp
+// addressing on a w x h array would.
 template <bool PK, int HW>
 __device__ __forceinline__ void sample2(const ExView& E, int li, const float4* LBO, float u, float v, float4* base,
                                         float4* out, bool fast) {
     const int w = E.w, h = E.h;
-    float xs = u + 0.5f, ys = v + 0.5f;
     if (HW) {
+        if (!fast) {
+            u = fminf(fmaxf(u, 0.0f), (float)(w - 1));
+            v = fminf(fmaxf(v, 0.0f), (float)(h - 1));
+        }
+        const float xs = u + 0.5f, ys = v + 0.5f;
         *base = tex2DLayered<float4>(E.tbase, xs, ys, li);
         *out = tex2DLayered<float4>(E.tout, xs, ys, li);
         return;
     }
+    float xs = u + 0.5f, ys = v + 0.5f;
     float xb = xs - 0.5f, yb = ys - 0.5f;
     float fx = floorf(xb), fy = floorf(yb);
     float a = xb - fx, c = yb - fy;

@@ -2,9 +2,11 @@
 //
 // Worker threads each use a context of the server (its own device buffers,
 // memory cache and CUDA stream, kept between runs) and take requests in
-// arrival order.  A request is admitted once
-// its arrival time has passed and its estimated device memory fits the
-// budget beside the requests in flight, so several requests' kernels run on
+// arrival order.  A request is admitted once its arrival time has passed and
+// its device memory fits the budget beside the requests in flight: with a
+// budget, admission waits until the running requests' contexts are set up
+// and counts the memory those contexts actually hold, plus an estimate from
+// the new request's sizes.  Several requests' kernels so run on
 // the GPU at once: a small still alone fills only a few of the GPU's 152
 // SMs.  Everything here goes through the public C ABI; the contexts share
 // nothing, so each result is the one a request gets on a context of its own.
@@ -39,12 +41,14 @@ size_t estimate_bytes(const pt_request& r) {
            (size_t)r.style_w * r.style_h * per_texel;
 }
 
-pt_status run_request(pt_ctx* c, pt_request& r) {
 #define PT_TRY(expr)                   \
     do {                               \
         pt_status s_ = (expr);         \
         if (s_ != PT_OK) return s_;    \
     } while (0)
+
+// the request's buffers, exemplar pyramid and frame pyramids on the context
+pt_status setup_request(pt_ctx* c, pt_request& r) {
     if (r.frames < 1 || !r.inputs || r.image_w < 2 || r.image_h < 2) return PT_ERR_INVALID;
     PT_TRY(pt_initialize(c, r.image_w, r.image_h, r.style_w, r.style_h, 1));
     PT_TRY(pt_set_params(c, &r.params));
@@ -56,6 +60,11 @@ pt_status run_request(pt_ctx* c, pt_request& r) {
         PT_TRY(pt_set_frame(c, f, r.image_w, r.image_h, in.rgba, in.orient_tensor, in.dist_trans, in.ids, in.vel_fwd,
                             in.vel_bwd, in.scale));
     }
+    return PT_OK;
+}
+
+// its synthesis, results into the request's output arrays
+pt_status synthesize_request(pt_ctx* c, pt_request& r) {
     const int fl = PT_OUTPUT_LEVEL(&r.params);
     const size_t n = (size_t)(r.image_w >> fl) * (size_t)(r.image_h >> fl);
     if (r.frames == 1) {
@@ -68,16 +77,17 @@ pt_status run_request(pt_ctx* c, pt_request& r) {
     }
     PT_TRY(pt_clear_frames(c));
     return PT_OK;
-#undef PT_TRY
 }
+#undef PT_TRY
 
 struct Queue {
     std::mutex m;
     std::condition_variable cv;
     std::vector<int> order;  // request indices by arrival time
     size_t next = 0;         // next request of `order` to admit
-    size_t in_flight = 0;    // estimated bytes of the admitted, unfinished requests
+    size_t in_flight = 0;    // bytes of the admitted, unfinished requests
     int running = 0;
+    int setting_up = 0;      // admitted requests whose memory is still an estimate
 };
 
 }  // namespace
@@ -115,6 +125,7 @@ pt_status pt_server_run(pt_server* srv, pt_request* reqs, int count) {
     for (int i = 0; i < count; i++) {
         reqs[i].status = PT_ERR_STATE;  // not run
         reqs[i].start_ms = reqs[i].done_ms = 0.0;
+        reqs[i].device_bytes = 0;
     }
     Queue q;
     q.order.resize(count);
@@ -143,7 +154,9 @@ pt_status pt_server_run(pt_server* srv, pt_request* reqs, int count) {
                             idx = -1;
                             continue;
                         }
-                        if (hbm_budget && q.running > 0 && q.in_flight + est > hbm_budget) {  // no room yet
+                        // with a budget, the next admission waits until every running request's
+                        // memory is known, then needs room for its own estimate beside them
+                        if (hbm_budget && q.running > 0 && (q.setting_up > 0 || q.in_flight + est > hbm_budget)) {
                             q.cv.wait(lk);
                             idx = -1;
                             continue;
@@ -151,13 +164,26 @@ pt_status pt_server_run(pt_server* srv, pt_request* reqs, int count) {
                         q.next++;
                         q.in_flight += est;
                         q.running++;
+                        q.setting_up++;
                         break;
                     }
                 }
                 if (idx < 0) break;
                 pt_request& r = reqs[idx];
                 r.start_ms = ms_since(t0);
-                r.status = (created == PT_OK) ? run_request(c, r) : created;
+                r.status = (created == PT_OK) ? setup_request(c, r) : created;
+                r.device_bytes = c ? pt_device_bytes(c) : 0;
+                {
+                    // the budget from now on counts what the context actually holds
+                    std::lock_guard<std::mutex> lk(q.m);
+                    if (r.status == PT_OK) {
+                        q.in_flight = q.in_flight - est + r.device_bytes;
+                        est = r.device_bytes;
+                    }
+                    q.setting_up--;
+                }
+                q.cv.notify_all();
+                if (r.status == PT_OK) r.status = synthesize_request(c, r);
                 r.done_ms = ms_since(t0);
                 {
                     std::lock_guard<std::mutex> lk(q.m);

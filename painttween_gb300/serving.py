@@ -67,8 +67,9 @@ def _results(arr, outs, n, st):
     res = []
     for i in range(n):
         r = arr[i]
-        res.append(dict(rgba=outs[i][0], offsets=outs[i][1], start_ms=r.start_ms, done_ms=r.done_ms,
-                        latency_ms=r.done_ms - r.arrival_ms, status=r.status))
+        res.append(dict(rgba=outs[i][0], offsets=outs[i][1], arrival_ms=r.arrival_ms, start_ms=r.start_ms,
+                        done_ms=r.done_ms, latency_ms=r.done_ms - r.arrival_ms, status=r.status,
+                        device_bytes=r.device_bytes))
     if st != _abi.PT_OK:
         bad = [i for i in range(n) if arr[i].status != _abi.PT_OK]
         raise PaintTweenError(st, "%d of %d requests failed (first: %s)" % (len(bad), n, bad[:1]))

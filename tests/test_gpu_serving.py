@@ -79,6 +79,36 @@ def test_arrivals_and_budget_admission():
     spans = sorted((r["start_ms"], r["done_ms"]) for r in res)
     for (s0, d0), (s1, d1) in zip(spans, spans[1:]):
         assert s1 >= d0
+    # the memory each request's context held once set up is reported
+    assert all(r["device_bytes"] > 0 for r in res)
+
+
+def test_admission_counts_the_memory_contexts_hold():
+    """After set-up the budget counts what a context actually holds: a
+    budget a little above one request's memory lets no two of them run at
+    once, whatever the estimate from their sizes says."""
+    big = [_still(320, 320, 256, 51 + i) for i in range(3)]
+    alone = serve([big[0]], max_in_flight=1)[0]["device_bytes"]
+    res = serve(big, max_in_flight=3, hbm_budget=int(1.1 * alone))
+    spans = sorted((r["start_ms"], r["done_ms"]) for r in res)
+    for (s0, d0), (s1, d1) in zip(spans, spans[1:]):
+        assert s1 >= d0
+
+
+def test_reused_texture_arrays_match_the_oracle():
+    """A worker keeps its texture arrays: a small exemplar after a larger one
+    is fetched from the corner of the larger arrays, with the coordinates
+    clamped, and must give the oracle's clamp-addressing results bit for bit."""
+    from oracle import oracle as O
+    from painttween_gb300.serving import Server
+    small = _still(96, 80, 64, 61, levels=3, iterations=3)
+    small["params"].filterMode = _abi.FILTER_TEXTURE
+    big = _still(128, 96, 200, 62)
+    with Server(max_in_flight=1) as srv:
+        got = srv.run([dict(big, arrival_ms=0.0), dict(small, arrival_ms=1.0)])[1]
+    ref = O.OracleDriver(small["params"], [small["style"]], small["frames"], threads=8).render(0, 0)[0]
+    assert_offsets_equal(got["offsets"][0], ref[0], 1.0, "still after a larger exemplar")
+    assert np.abs(got["rgba"][0] - ref[2]).max() <= 1e-6
 
 
 def test_server_keeps_contexts_between_runs():
