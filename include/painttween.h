@@ -545,6 +545,15 @@ pt_status pt_get_kernel_stats(pt_ctx* ctx, int kernel, pt_kernel_stats* out);
 /* Blocks until the context's stream is idle. */
 pt_status pt_synchronize(pt_ctx* ctx);
 
+/* ---- file formats (host only) ---------------------------------------------
+ * Decodes the Huffman block of an OpenEXR PIZ chunk (the stage that
+ * OpenEXR's reader runs on the reference's PIZ-compressed RGBA temporaries,
+ * imageIO.h:131-133): `block` holds the u32 header (first and last symbol,
+ * table bytes, bit count, 0), the packed code-length table and the bits;
+ * writes exactly n_words 16-bit words.  PT_ERR_INVALID for a malformed or
+ * truncated block, or one that decodes to another count of words. */
+pt_status pt_piz_huffman_decode(const uint8_t* block, size_t block_bytes, uint16_t* out, size_t n_words);
+
 #ifdef __cplusplus
 }
 #endif

@@ -87,6 +87,7 @@ SIGNATURES = {
     "pt_host_alloc": (_I, [ctypes.c_size_t, ctypes.POINTER(_VP)]),
     "pt_host_free": (_I, [_VP]),
     "pt_get_kernel_stats": (_I, [_VP, _I, ctypes.POINTER(_abi.KernelStats)]),
+    "pt_piz_huffman_decode": (_I, [_VP, ctypes.c_size_t, _VP, ctypes.c_size_t]),
 }
 
 

@@ -515,13 +515,16 @@ static pt_status take_tex_array(pt_ctx* c, int w, int h, int layers, TexArray* o
     return PT_OK;
 }
 
-// one copy of a w x h x layers block of a pitched plane into an array
+// one copy of the w x h x layers block at (sx, sy) of layered planes
+// (pitch_texels x plane_rows texels per layer) into an array at (dx, dy):
+// the source pointer is offset to the block, whose rows and layers keep the
+// planes' strides
 static cudaError_t copy_to_array(const float4* src, int pitch_texels, int plane_rows, int sx, int sy, cudaArray_t dst,
                                  int dx, int dy, int w, int h, int layers, cudaStream_t st) {
     cudaMemcpy3DParms cp;
     memset(&cp, 0, sizeof cp);
-    cp.srcPtr = make_cudaPitchedPtr((void*)src, (size_t)pitch_texels * sizeof(float4), pitch_texels, plane_rows);
-    cp.srcPos = make_cudaPos((size_t)sx * sizeof(float4), sy, 0);
+    const size_t pitch = (size_t)pitch_texels * sizeof(float4);
+    cp.srcPtr = make_cudaPitchedPtr((void*)(src + (size_t)sy * pitch_texels + sx), pitch, pitch, plane_rows);
     cp.dstArray = dst;
     cp.dstPos = make_cudaPos(dx, dy, 0);
     cp.extent = make_cudaExtent(w, h, layers);

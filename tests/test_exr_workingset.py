@@ -16,10 +16,10 @@ import pytest
 from painttween_gb300 import _abi, exr, workingset
 
 
-@pytest.mark.parametrize("comp", [exr.NONE, exr.RLE, exr.ZIPS, exr.ZIP])
+@pytest.mark.parametrize("comp", [exr.NONE, exr.RLE, exr.ZIPS, exr.ZIP, exr.PIZ])
 def test_round_trip_every_compression(tmp_path, comp):
     rng = np.random.default_rng(comp)
-    h, w = 37, 19  # more lines than one ZIP chunk, odd sizes
+    h, w = 37, 19  # more lines than one ZIP / PIZ chunk, odd sizes
     chans = {"R": rng.random((h, w)).astype(np.float16), "G": np.zeros((h, w), np.float16),
              "layer.x": rng.normal(size=(h, w)).astype(np.float32), "n": rng.integers(0, 2**32, (h, w), np.uint32)}
     chans["G"][:, 3:9] = 1.5  # runs for RLE
@@ -59,10 +59,117 @@ def test_unsupported_compression_raises(tmp_path):
     exr.write(p, {"Y": np.zeros((4, 4), np.float32)}, exr.NONE)
     data = bytearray(open(p, "rb").read())
     i = data.index(b"compression\0compression\0") + len(b"compression\0compression\0") + 4
-    data[i] = exr.PIZ
+    data[i] = 5  # PXR24
     open(p, "wb").write(bytes(data))
     with pytest.raises(exr.ExrError):
         exr.read(p)
+
+
+# --- PIZ, against chunks assembled by hand from the format's layout ---------
+
+def _bits(*fields):
+    """Bytes of (value, bit count) fields, most significant bit first, the
+    last byte padded with zeros."""
+    s = "".join(format(v, "0%db" % n) for v, n in fields)
+    s += "0" * (-len(s) % 8)
+    return bytes(int(s[i:i + 8], 2) for i in range(0, len(s), 8))
+
+
+def _huf(im, iM, table, nbits, data):
+    return struct.pack("<5I", im, iM, len(table), nbits, 0) + table + data
+
+
+def _piz(lo, hi, bitmap, huf):
+    return struct.pack("<HH", lo, hi) + bytes(bitmap) + struct.pack("<i", len(huf)) + huf
+
+
+def test_piz_hand_built_two_equal_words():
+    """One HALF line of two words 0x0005: bit map byte 0 = bit 5; ranks
+    0 -> 0, 5 -> 1; no wavelet level (one line); Huffman symbols 1 and the
+    run symbol 2, both 1 bit long (codes 0 and 1); data "00"."""
+    huf = _huf(1, 2, bytes([0x04, 0x10]), 2, bytes([0x00]))
+    assert _bits((1, 6), (1, 6)) == bytes([0x04, 0x10])
+    chunk = _piz(0, 0, [0x20], huf)
+    out = exr._piz_decompress(chunk, [("Y", exr.HALF)], 2, 1)
+    assert out == bytes([5, 0, 5, 0])
+
+
+def test_piz_hand_built_run_code():
+    """Ten equal words 0x0007 sent as the word, the run symbol and 9 in 8
+    bits: "0" "1" "00001001"."""
+    huf = _huf(1, 2, _bits((1, 6), (1, 6)), 10, _bits((0, 1), (1, 1), (9, 8)))
+    chunk = _piz(0, 0, [0x80], huf)
+    out = exr._piz_decompress(chunk, [("Y", exr.HALF)], 10, 1)
+    assert out == bytes([7, 0]) * 10
+
+
+def test_piz_hand_built_wavelet_block():
+    """A 2x2 HALF block of words 1, 2 / 3, 4.  Ranks are the words (map
+    byte 0 = bits 1-4, largest rank 4 < 2^14: the 14-bit pair transform).
+    Encoding the block: rows (1, 2) -> (1, -1), (3, 4) -> (3, -1), then
+    columns (1, 3) -> (2, -2), (-1, -1) -> (-1, 0): words 2, 0xFFFF, 0xFFFE, 0.
+    Code lengths chosen by hand: 0, 2 and 0xFFFE 2 bits, 0xFFFF and the run
+    symbol 0x10000 3 bits; canonical codes 01, 10, 11, 000, 001.  The table
+    runs from symbol 0 to 0x10000: 2, 0, 2, 65531 zeros (251 long runs of
+    261 and one of 20), 2, 3, 3."""
+    table = [(2, 6), (0, 6), (2, 6)] + [(63, 6), (255, 8)] * 251 + [(63, 6), (14, 8)] + [(2, 6), (3, 6), (3, 6)]
+    data = [(0b10, 2), (0b000, 3), (0b11, 2), (0b01, 2)]
+    huf = _huf(0, 0x10000, _bits(*table), 9, _bits(*data))
+    assert _bits(*data) == bytes([0x86, 0x80])
+    chunk = _piz(0, 0, [0x1E], huf)
+    out = exr._piz_decompress(chunk, [("Y", exr.HALF)], 2, 2)
+    assert np.frombuffer(out, "<u2").tolist() == [1, 2, 3, 4]
+
+
+def test_piz_hand_built_float_channel():
+    """One FLOAT sample 1.0 (0x3F800000): words 0x0000, 0x3F80; map byte
+    2032 = bit 0 (0x3F80 = 16256); ranks 0, 1; lengths 1, 2 and 2 for the
+    run symbol: codes 1, 00, 01; data "1" "00"."""
+    huf = _huf(0, 2, _bits((1, 6), (2, 6), (2, 6)), 3, _bits((1, 1), (0, 2)))
+    chunk = _piz(2032, 2032, [0x01], huf)
+    out = exr._piz_decompress(chunk, [("Z", exr.FLOAT)], 1, 1)
+    assert struct.unpack("<f", out)[0] == 1.0
+
+
+def test_piz_pair_transforms():
+    """The 16-bit modular pair transform (largest rank >= 2^14), values
+    worked by hand, and both transforms invert on every word pair class."""
+    a, b = np.array([1, 40000]), np.array([3, 50000])
+    l, h = exr._enc16(a, b)
+    assert l.tolist() == [16386, 61384] and h.tolist() == [32766, 22768]
+    ra, rb = exr._dec16(l, h)
+    assert ra.tolist() == [1, 40000] and rb.tolist() == [3, 50000]
+    rng = np.random.default_rng(9)
+    x, y = rng.integers(0, 1 << 16, 5000), rng.integers(0, 1 << 16, 5000)
+    assert [v.tolist() for v in exr._dec16(*exr._enc16(x, y))] == [x.tolist(), y.tolist()]
+    x, y = rng.integers(0, 1 << 14, 5000), rng.integers(0, 1 << 14, 5000)
+    assert [v.tolist() for v in exr._dec14(*exr._enc14(x, y))] == [x.tolist(), y.tolist()]
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (3, 5), (32, 17), (7, 64), (32, 700)])
+def test_piz_round_trip_chunks(shape):
+    """The encoder's chunks decode back, odd sizes (odd rows and columns at
+    several wavelet levels), FLOAT / UINT channels (two word planes) and
+    more than 2^14 distinct words (the 16-bit transform)."""
+    rng = np.random.default_rng(shape[1])
+    h, w = shape
+    chans = [("A", exr.HALF), ("B", exr.FLOAT), ("C", exr.UINT)]
+    arrs = [rng.random((h, w)).astype(np.float16), rng.normal(size=(h, w)).astype(np.float32),
+            rng.integers(0, 2**32, (h, w), dtype=np.uint64).astype(np.uint32)]
+    raw = b"".join(a[r].tobytes() for r in range(h) for a in arrs)
+    assert exr._piz_decompress(exr._piz_compress(raw, chans, w, h), chans, w, h) == raw
+
+
+def test_piz_malformed_blocks_raise():
+    huf = _huf(1, 2, _bits((1, 6), (1, 6)), 10, _bits((0, 1), (1, 1), (9, 8)))
+    chunk = _piz(0, 0, [0x80], huf)
+    with pytest.raises(exr.ExrError):  # one word more than the run gives
+        exr._piz_decompress(chunk, [("Y", exr.HALF)], 11, 1)
+    with pytest.raises(exr.ExrError):  # truncated bits
+        exr._piz_decompress(chunk[:-1], [("Y", exr.HALF)], 10, 1)
+    bad = _huf(1, 2, _bits((1, 6), (1, 6)), 10, _bits((1, 1), (1, 1), (9, 8)))  # a run before any word
+    with pytest.raises(exr.ExrError):
+        exr._piz_decompress(_piz(0, 0, [0x80], bad), [("Y", exr.HALF)], 10, 1)
 
 
 def test_temporary_images_round_trip(tmp_path):
