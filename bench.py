@@ -621,6 +621,28 @@ def run_batched(n, in_flight):
         out[name] = dict(_latencies(res), in_flight=k)
     out["speedup"] = out["batched"]["requests_per_s"] / out["plain"]["requests_per_s"]
     out["p99_vs_single"] = out["batched"]["p99_ms"] / out["plain"]["service_p50_ms"]
+    # the GPU's own work in these requests: the summed durations of the
+    # patch-distance and canvas launches (per-launch CUDA events), request by
+    # request on one context -- a floor no overlap can go below
+    from painttween_gb300 import Synthesizer
+    s = Synthesizer(device=0)
+    busy_ms = 0.0
+    try:
+        for rq in reqs:
+            fr, st = rq["frames"][0], rq["style"]
+            h, w = fr["rgba"].shape[:2]
+            s.setup(rq["params"], w, h, st["w"], st["h"], 1)
+            s.set_style(0, st["base"], st["output"], st["orient_tensor"], st["dist_trans"], st["object_ids"])
+            s.set_frame_dict(0, fr)
+            s.set_profiling(_abi.PROFILE_TIMING)
+            s.synthesize_frame(0)
+            busy_ms += sum(s.kernel_stats(k)["total_ms"] for k in range(4))
+            s.set_profiling(0)
+    finally:
+        s.close()
+    out["gpu_kernel_s"] = busy_ms / 1000.0
+    out["floor_requests_per_s"] = n / (busy_ms / 1000.0)
+    out["batched"]["frac_of_floor"] = out["batched"]["requests_per_s"] / out["floor_requests_per_s"]
     return out
 
 
