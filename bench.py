@@ -621,9 +621,10 @@ def run_batched(n, in_flight):
         out[name] = dict(_latencies(res), in_flight=k)
     out["speedup"] = out["batched"]["requests_per_s"] / out["plain"]["requests_per_s"]
     out["p99_vs_single"] = out["batched"]["p99_ms"] / out["plain"]["service_p50_ms"]
-    # the GPU's own work in these requests: the summed durations of the
-    # patch-distance and canvas launches (per-launch CUDA events), request by
-    # request on one context -- a floor no overlap can go below
+    # the summed durations of the requests' patch-distance and canvas
+    # launches, request by request on one context (per-launch CUDA events):
+    # small requests' launches leave most SMs idle, so overlapping requests
+    # finishes faster than this serial kernel time
     from painttween_gb300 import Synthesizer
     s = Synthesizer(device=0)
     busy_ms = 0.0
@@ -640,9 +641,8 @@ def run_batched(n, in_flight):
             s.set_profiling(0)
     finally:
         s.close()
-    out["gpu_kernel_s"] = busy_ms / 1000.0
-    out["floor_requests_per_s"] = n / (busy_ms / 1000.0)
-    out["batched"]["frac_of_floor"] = out["batched"]["requests_per_s"] / out["floor_requests_per_s"]
+    out["serial_kernel_s"] = busy_ms / 1000.0
+    out["batched"]["wall_vs_serial_kernels"] = out["batched"]["wall_s"] / out["serial_kernel_s"]
     return out
 
 
