@@ -363,6 +363,7 @@ def run_ours(args, dist):
     s.setup(p, cfg["w"], cfg["h"], cfg["ew"], cfg["eh"], 1)
     if args.generic_kernels:
         s.set_tiled_kernels(False)  # same results, one-thread-per-pixel kernels (profiling them)
+    s.set_tma_staging(args.staging == "tma")
     s.set_style(0, ex["base"], ex["output"], ex["orient_tensor"], ex["dist_trans"], ex["object_ids"])
     for i, fr in enumerate(clip):
         s.set_frame_dict(i, fr)
@@ -480,6 +481,7 @@ def run_ours(args, dist):
                    "exemplar": "%dx%d" % (cfg["ew"], cfg["eh"]), "patch_radius": r, "levels": p.levels,
                    "iterations": p.iterations, "scheme": "FMBM_RM", "histogram": True,
                    "kernels": "generic" if args.generic_kernels else "tiled",
+                   "staging": args.staging,
                    "filter": args.filter,
                    "parallelism": "replicas" if dist.ws > 1 else "single",
                    "l2": "inputs larger than L2 (%.1f GB of resident frame pyramids per step)"
@@ -752,6 +754,8 @@ def main():
     ap.add_argument("--serving-budget-gb", type=float, default=150.0)
     ap.add_argument("--filter", default="texture", choices=["texture", "exact"],
                     help="bilinear arithmetic: the texture unit's (the reference's) or exact FP32")
+    ap.add_argument("--staging", default="tma", choices=["tma", "loads"],
+                    help="how the tiled kernels stage interior tiles: tensor copies or plain loads (same results)")
     ap.add_argument("--generic-kernels", action="store_true",
                     help="run the generic one-thread-per-pixel kernels instead of the tiled ones (profiling only)")
     args = ap.parse_args()

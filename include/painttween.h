@@ -533,6 +533,14 @@ pt_status pt_set_profiling(pt_ctx* ctx, int flags);
  * coherence term, one temporal direction), 0 = the generic kernels
  * everywhere.  Both compute identical results. */
 pt_status pt_set_tiled_kernels(pt_ctx* ctx, int on);
+/* Selects how the tiled kernels stage the pixel-side planes of a tile and
+ * its halo in shared memory: 1 (default) = tensor copies
+ * (cp.async.bulk.tensor, completed on an mbarrier) for every tile whose halo
+ * lies inside the level rectangle, plain loads with the clamp rules for the
+ * others; 0 = plain loads everywhere.  Both compute identical results.  A
+ * block that gives up waiting for its copies (a bounded wait) makes the next
+ * pt_synchronize / pt_synthesize_* return PT_ERR_CUDA. */
+pt_status pt_set_tma_staging(pt_ctx* ctx, int on);
 /* Selects whether the propagate/scatter loops of pt_synthesize_frame and
  * pt_synthesize_animation track which offsets each pass changed and skip the
  * evaluations whose inputs are unchanged since an earlier pass with the same

@@ -457,18 +457,100 @@ bool tiled_usable(pt_ctx* c) {
 
 // launches the tiled kernel of `kind` if one is instantiated for this
 // configuration; *done = false otherwise (the generic kernel is used)
+// cuTensorMapEncodeTiled, from the driver through the runtime (the library
+// links the runtime statically and not the driver)
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+    static const EncodeTiledFn fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+        return (EncodeTiledFn)p;
+    }();
+    return fn;
+}
+
+// The tensor map of a float4 plane (`pitch` texels per row) over a w x h
+// level: a FLOAT32 tensor of 4w x h elements whose boxes are tw x th texels
+// (4 tw elements: 16 tw bytes, a multiple of 16).  False when the plane
+// cannot be mapped (no encoder, an address not on 16 bytes, a level smaller
+// than a box); its tiles are then staged by plain loads.
+static bool plane_map(pt_ctx* c, const void* p, int pitch, int w, int h, int tw, int th, CUtensorMap* out) {
+    if (!p || ((uintptr_t)p & 15) || pitch < w || w < tw || h < th) return false;
+    const auto key = std::make_tuple(p, pitch, w, h, tw * 1024 + th);
+    auto it = c->tmaps.find(key);
+    if (it != c->tmaps.end()) {
+        *out = it->second;
+        return true;
+    }
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn) return false;
+    const cuuint64_t dims[2] = {4ull * (cuuint64_t)w, (cuuint64_t)h};
+    const cuuint64_t strides[1] = {(cuuint64_t)pitch * sizeof(float4)};
+    const cuuint32_t box[2] = {4u * (cuuint32_t)tw, (cuuint32_t)th};
+    const cuuint32_t es[2] = {1, 1};
+    CUtensorMap m;
+    if (fn(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(p), dims, strides, box, es,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    if (c->tmaps.size() >= 512) c->tmaps.clear();
+    c->tmaps.emplace(key, m);
+    *out = m;
+    return true;
+}
+
+// the tensor maps of the planes a tiled kernel of mode tm stages
+static void tile_maps(pt_ctx* c, const Params& P, int tm, TileMaps* M) {
+    memset(M, 0, sizeof(*M));
+    M->err = c->tma_err;
+    if (!c->use_tma || !c->tma_err) return;
+    const int tw = ptk::kTileW + 2 * P.r, th = ptk::kTileH + 2 * P.r;
+    const Arr<float4>& ib = P.img.base[P.img.cur];
+    bool ok = plane_map(c, ib.p, ib.w, P.lw, P.lh, tw, th, &M->base) &&
+              plane_map(c, P.canvas, P.W, P.lw, P.lh, tw, th, &M->canvas);
+    if (ok && tm) {
+        const AdvView& A = P.adv[tm == 1 ? 0 : 1];
+        ok = plane_map(c, A.base, P.W, P.lw, P.lh, tw, th, &M->pbase) &&
+             plane_map(c, A.out, P.W, P.lw, P.lh, tw, th, &M->pout) &&
+             plane_map(c, A.off.B, P.W, P.lw, P.lh, tw, th, &M->prec);
+    }
+    M->on = ok ? 1 : 0;
+}
+
 cudaError_t launch_tiled(pt_ctx* c, int kind, const Params& P, PatchPlanes work, int arg, uint32_t pass_id,
                          float* out, bool* done) {
     *done = false;
     if (!tiled_usable(c)) return cudaSuccess;
     int tm = temporal_mode(c);
+    if (P.r < 2 || P.r > 4) return cudaSuccess;
+    TileMaps M;
+    tile_maps(c, P, tm, &M);
     *done = true;
     switch (P.r) {
-        case 2: return pt::launch_tiled_2(kind, tm, P, work, arg, pass_id, out, c->stream);
-        case 3: return pt::launch_tiled_3(kind, tm, P, work, arg, pass_id, out, c->stream);
-        case 4: return pt::launch_tiled_4(kind, tm, P, work, arg, pass_id, out, c->stream);
-        default: *done = false; return cudaSuccess;
+        case 2: return pt::launch_tiled_2(kind, tm, P, M, work, arg, pass_id, out, c->stream);
+        case 3: return pt::launch_tiled_3(kind, tm, P, M, work, arg, pass_id, out, c->stream);
+        default: return pt::launch_tiled_4(kind, tm, P, M, work, arg, pass_id, out, c->stream);
     }
+}
+
+// the tensor-copy error flag: PT_ERR_CUDA (and the flag cleared) when a
+// tiled kernel's block gave up waiting for its staging copies
+pt_status check_tma(pt_ctx* c) {
+    if (!c->tma_err) return PT_OK;
+    int v = 0;
+    CU(cudaMemcpyAsync(&v, c->tma_err, sizeof v, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    if (!v) return PT_OK;
+    CU(cudaMemsetAsync(c->tma_err, 0, sizeof(int), c->stream));
+    return fail(c, PT_ERR_CUDA, "a tiled kernel's wait for its tensor copies ran out");
 }
 
 pt_status do_residual(pt_ctx* c, int level) {
@@ -624,7 +706,7 @@ pt_status pt_create(int device, size_t budget, pt_ctx** out) {
         return PT_ERR_CUDA;
     }
     pt_default_params(&c->params);
-    if (dalloc_t(c, &c->flag, 4) != PT_OK) {
+    if (dalloc_t(c, &c->flag, 4) != PT_OK || dalloc_t(c, &c->tma_err, 1) != PT_OK) {
         cudaStreamDestroy(c->stream);
         delete c;
         return PT_ERR_OOM;
@@ -682,7 +764,7 @@ pt_status pt_destroy(pt_ctx* c) {
 pt_status pt_synchronize(pt_ctx* c) {
     if (!c) return PT_ERR_INVALID;
     CU(cudaStreamSynchronize(c->stream));
-    return PT_OK;
+    return check_tma(c);
 }
 
 pt_status pt_set_params(pt_ctx* c, const pt_params* p) {

@@ -38,6 +38,7 @@ using ptk::ExView;
 using ptk::ImgView;
 using ptk::Params;
 using ptk::PatchPlanes;
+using ptk::TileMaps;
 
 
 namespace ptc {
@@ -204,6 +205,10 @@ struct pt_ctx {
     size_t cb_stage_bytes = 0;
     bool adv_written[2] = {false, false};  // advected F/B written since the last reset
     bool use_tiled = true;                 // tiled kernels where an instantiation exists
+    bool use_tma = true;                   // interior tiles staged by tensor copies
+    int* tma_err = nullptr;                // set by a block whose tensor-copy wait ran out
+    // tensor maps of staged planes: (plane, pitch, level w, level h, box) -> map
+    std::map<std::tuple<const void*, int, int, int, int>, CUtensorMap> tmaps;
 
     // change tracking of the driver's propagate/scatter loops
     bool use_incremental = true;
@@ -250,6 +255,7 @@ struct pt_ctx {
 
 inline PatchPlanes base_planes(pt_ctx* c) { return c->off[c->base_i]; }
 PT_HIDDEN pt_status base_for_partial_write(pt_ctx* c, int level, PatchPlanes* out);
+PT_HIDDEN pt_status check_tma(pt_ctx* c);
 PT_HIDDEN pt_status check_ready(pt_ctx* c, int level, bool need_ex = true, bool need_img = true);
 PT_HIDDEN pt_status copy_planes_full(pt_ctx* c, PatchPlanes dst, PatchPlanes src);
 PT_HIDDEN pt_status dalloc(pt_ctx* c, void** p, size_t bytes);

@@ -970,6 +970,7 @@ pt_status pt_synthesize_frame(pt_ctx* c, int frame, float* out_rgba, pt_patchxf*
     if (!c->initialized || !c->have_params) return fail(c, PT_ERR_STATE, "context not initialized");
     CU(cudaSetDevice(c->device));
     TRY(render(c, frame, frame));
+    TRY(check_tma(c));
     return fetch_final(c, frame, out_rgba, out_offsets);
 }
 
@@ -978,6 +979,7 @@ pt_status pt_synthesize_animation(pt_ctx* c, int first, int last, pt_frame_callb
     if (!c->initialized || !c->have_params) return fail(c, PT_ERR_STATE, "context not initialized");
     CU(cudaSetDevice(c->device));
     TRY(render(c, first, last));
+    TRY(check_tma(c));
     if (cb) {
         // each frame is handed to the callback from page-locked staging
         int lw = c->W >> c->out_level, lh = c->H >> c->out_level;

@@ -24,22 +24,23 @@
 
 namespace ptk {
 
-constexpr int kTileW = 32;
-constexpr int kTileH = 8;
 constexpr int kTileThreads = kTileW * kTileH;
 
 enum { TM_NONE = 0, TM_FWD = 1, TM_BWD = 2 };
 
+// The staged planes start on 128-byte boundaries (tensor copies write
+// there); a tile row is TW texels, as a tensor copy's box row is.
 template <int R, int TM>
 struct TileSmem {
     static constexpr int TW = kTileW + 2 * R;
     static constexpr int TH = kTileH + 2 * R;
     static constexpr int N = TW * TH;
-    float4 base[N];
-    float4 canvas[N];
-    float4 pbase[TM ? N : 1];
-    float4 pout[TM ? N : 1];
-    float phys[TM ? N : 1];
+    alignas(128) float4 base[N];
+    alignas(128) float4 canvas[N];
+    alignas(128) float4 pbase[TM ? N : 1];
+    alignas(128) float4 pout[TM ? N : 1];
+    alignas(128) float4 prec[TM ? N : 1];  // the advected records' B plane (.x: hysteresis, the validity)
+    unsigned long long bar;                // completion barrier of the tensor copies
 };
 
 // both colours of one exemplar texel: a 32-byte record of the interleaved
@@ -226,7 +227,7 @@ __device__ __forceinline__ float energy_taps(const Params& P, const TileSmem<R, 
                         float r = ssdp(sub4p(base, pbase), sub4p(tb, peb)) * P.tdIn;
                         r = fmaf(ssdp(sub4p(canvas, pout), sub4p(to, peo)), P.tdOut, r);
                         r = fmaf(ssdp(pout, to), P.tc, r);
-                        res = (T.phys[s] > 0) ? res + r : res;
+                        res = (T.prec[s].x > 0) ? res + r : res;
                     }
                 }
                 if (i == 0 && j == 0) {
@@ -279,26 +280,99 @@ __device__ __forceinline__ float energy_tiled(const Params& P, const TileSmem<R,
                                   EE ? exit_threshold(P, px, best) : kNoBest);
 }
 
+// Tensor copies into shared memory (cp.async.bulk.tensor) completing on an
+// mbarrier.  Every wait is bounded: kWaitLimit polls of mbarrier.try_wait,
+// each of which may suspend the thread for a short hardware time limit.
+constexpr int kWaitLimit = 1 << 20;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// box (x, y) of a 2-D tensor map into shared memory at dst, counted on bar
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+        "[%4];" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+// waits for the barrier's phase `parity` to complete; false if it did not
+// within the limit
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+#pragma unroll 1
+    for (int i = 0; i < kWaitLimit; i++) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
 // Stages the tile (and halo) of the pixel-side inputs and fills the
 // per-pixel state.  Returns false for threads whose pixel is outside the
-// level rectangle.
+// level rectangle.  A tile whose halo lies inside the level rectangle, where
+// the clamps are no-ops, is copied by tensor copies when the maps are on
+// (one thread issues them; the texture mode's flush of subnormal input
+// colours follows in shared memory); the others load texel by texel with
+// the clamp rules.  *abort is set (for the whole block) when the copies did
+// not complete within two bounded waits; the block must then return.
 template <int R, int TM>
-__device__ __forceinline__ bool stage_tile(const Params& P, TileSmem<R, TM>& T, PixT* px) {
-    constexpr int TW = TileSmem<R, TM>::TW, N = TileSmem<R, TM>::N;
+__device__ __forceinline__ bool stage_tile(const Params& P, const TileMaps& M, TileSmem<R, TM>& T, PixT* px,
+                                           bool* abort) {
+    constexpr int TW = TileSmem<R, TM>::TW, TH = TileSmem<R, TM>::TH, N = TileSmem<R, TM>::N;
     const int tid = threadIdx.x + threadIdx.y * kTileW;
     const int x0 = blockIdx.x * kTileW - R, y0 = blockIdx.y * kTileH - R;
-    const Arr<float4>& ib = P.img.base[P.img.cur];
-    for (int q = tid; q < N; q += kTileThreads) {
-        int gx = clampi(x0 + q % TW, 0, P.lw - 1);
-        int gy = clampi(y0 + q / TW, 0, P.lh - 1);
-        size_t k = (size_t)gy * P.W + gx;
-        T.base[q] = lin_texel_of(__ldg(ib.p + (size_t)gy * ib.w + gx), P.hwFilter);
-        T.canvas[q] = __ldg(P.canvas + k);
-        if (TM) {
-            const AdvView& A = P.adv[TM == TM_FWD ? 0 : 1];
-            T.pbase[q] = __ldg(A.base + k);
-            T.pout[q] = __ldg(A.out + k);
-            T.phys[q] = __ldg(&A.off.B[k].x);
+    *abort = false;
+    const bool interior = M.on && x0 >= 0 && y0 >= 0 && x0 + TW <= P.lw && y0 + TH <= P.lh;  // (block-uniform)
+    if (interior) {
+        const uint32_t bar = smem_addr(&T.bar);
+        if (tid == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        __syncthreads();
+        if (tid == 0) {
+            const uint32_t bytes = (uint32_t)(N * sizeof(float4)) * (TM ? 5u : 2u);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+            // x in FLOAT32 elements: 4 per texel, so x * 4 bytes is a multiple of 16
+            tma_load_2d(T.base, &M.base, 4 * x0, y0, bar);
+            tma_load_2d(T.canvas, &M.canvas, 4 * x0, y0, bar);
+            if (TM) {
+                tma_load_2d(T.pbase, &M.pbase, 4 * x0, y0, bar);
+                tma_load_2d(T.pout, &M.pout, 4 * x0, y0, bar);
+                tma_load_2d(T.prec, &M.prec, 4 * x0, y0, bar);
+            }
+        }
+        bool ok = mbar_wait(bar, 0);
+        if (!ok) ok = mbar_wait(bar, 0);  // the copies still in flight, once more
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0 && M.err) atomicExch(M.err, 1);
+            *abort = true;
+            return false;
+        }
+        if (P.hwFilter)
+            for (int q = tid; q < N; q += kTileThreads) T.base[q] = lin_texel_of(T.base[q], 1);
+    } else {
+        const Arr<float4>& ib = P.img.base[P.img.cur];
+        for (int q = tid; q < N; q += kTileThreads) {
+            int gx = clampi(x0 + q % TW, 0, P.lw - 1);
+            int gy = clampi(y0 + q / TW, 0, P.lh - 1);
+            size_t k = (size_t)gy * P.W + gx;
+            T.base[q] = lin_texel_of(__ldg(ib.p + (size_t)gy * ib.w + gx), P.hwFilter);
+            T.canvas[q] = __ldg(P.canvas + k);
+            if (TM) {
+                const AdvView& A = P.adv[TM == TM_FWD ? 0 : 1];
+                T.pbase[q] = __ldg(A.base + k);
+                T.pout[q] = __ldg(A.out + k);
+                T.prec[q] = __ldg(A.off.B + k);
+            }
         }
     }
     __syncthreads();
@@ -368,7 +442,8 @@ __device__ __forceinline__ bool block_idle(const Params& P, PatchPlanes work, bo
 
 // updateResidualCache_kernel, texSynth_kernel.cu:661-693
 template <int R, int TM, int HW>
-__global__ void __launch_bounds__(kTileThreads, 2) kt_residual(const Params P, float* out) {
+__global__ void __launch_bounds__(kTileThreads, 2) kt_residual(const Params P, const __grid_constant__ TileMaps M,
+                                                                    float* out) {
     __shared__ TileSmem<R, TM> T;
     // Change tracking: only pixels with a changed record in their patch
     // window get a new residual; the others keep theirs (the same inputs give
@@ -403,7 +478,8 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_residual(const Params P, f
         if (!__syncthreads_or(need)) return;
     }
     PixT px;
-    if (!stage_tile<R, TM>(P, T, &px)) return;
+    bool abort;
+    if (!stage_tile<R, TM>(P, M, T, &px, &abort)) return;
     if (!need) return;
     const size_t k = (size_t)px.y * P.W + px.x;
     if (image_culled(P, px.x, px.y)) { out[k] = 0.0f; return; }
@@ -583,7 +659,7 @@ __device__ __forceinline__ float tap_value(const Params& P, const TileSmem<R, TM
             float r = ssdp(sub4p(base, pbase), sub4p(tb, peb)) * P.tdIn;
             r = fmaf(ssdp(sub4p(canvas, pout), sub4p(to, peo)), P.tdOut, r);
             r = fmaf(ssdp(pout, to), P.tc, r);
-            res = (T.phys[s] > 0) ? res + r : res;
+            res = (T.prec[s].x > 0) ? res + r : res;
         }
     }
     if (j == 0 && i == 0) {
@@ -737,7 +813,8 @@ struct PropQueue {
 
 // propagate_kernel with lane cursors over the tile's candidates
 template <int R, int TM, int HW>
-__global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P, PatchPlanes work, int jump) {
+__global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P, const __grid_constant__ TileMaps M,
+                                                                       PatchPlanes work, int jump) {
     __shared__ TileSmem<R, TM> T;
     __shared__ PixShared S;
     __shared__ PropQueue Q;
@@ -767,7 +844,9 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P
     if (pid < kTileH) { Q.count[pid] = 0; Q.next[pid] = 0; }
     load_tap_table<R>(P, TT);
     PixT px;
-    const bool in = stage_tile<R, TM>(P, T, &px);  // (synchronises the block)
+    bool abort;
+    const bool in = stage_tile<R, TM>(P, M, T, &px, &abort);  // (synchronises the block)
+    if (abort) return;
     // phase 1: each pixel builds its candidates (the reference's order,
     // repeats and test_offset rejections resolved here) and queues them
     int n = 0;
@@ -920,7 +999,8 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P
 // scatter_kernel + averageOffset, texSynth_kernel.cu:841-952, each lane
 // running its own pixel's chain with a lane cursor
 template <int R, int TM, int HW>
-__global__ void __launch_bounds__(kTileThreads, 2) kt_scatter_q(const Params P, PatchPlanes work, int write_all,
+__global__ void __launch_bounds__(kTileThreads, 2) kt_scatter_q(const Params P, const __grid_constant__ TileMaps M,
+                                                                     PatchPlanes work, int write_all,
                                                                uint32_t pass_id) {
     __shared__ TileSmem<R, TM> T;
     // Change tracking: with the reference's generator a pixel's candidates
@@ -938,7 +1018,9 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter_q(const Params P, 
     __shared__ TapTable<R> TT;
     load_tap_table<R>(P, TT);
     PixT px;
-    const bool in = stage_tile<R, TM>(P, T, &px);  // (synchronises the block)
+    bool abort;
+    const bool in = stage_tile<R, TM>(P, M, T, &px, &abort);  // (synchronises the block)
+    if (abort) return;
     const int x = px.x, y = px.y;
     const size_t k = (size_t)y * P.W + x;
     bool own = false;
@@ -1089,7 +1171,8 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter_q(const Params P, 
 // the same operations on the same values, so the same bits.  With `fill`
 // every tap of every pixel is computed (the loop's first residual).
 template <int R, int TM, int HW>
-__global__ void __launch_bounds__(kTileThreads, 2) kt_residual_inc(const Params P, float* out) {
+__global__ void __launch_bounds__(kTileThreads, 2) kt_residual_inc(const Params P, const __grid_constant__ TileMaps M,
+                                                                        float* out) {
     constexpr int TW = TileSmem<R, TM>::TW, N = TileSmem<R, TM>::N, K = (2 * R + 1) * (2 * R + 1);
     __shared__ TileSmem<R, TM> T;
     __shared__ PixShared S;
@@ -1132,7 +1215,9 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_residual_inc(const Params 
     const bool need = in && (own || (m0 | m1));
     if (!__syncthreads_or(need)) return;
     PixT px;
-    stage_tile<R, TM>(P, T, &px);  // (synchronises the block)
+    bool abort;
+    stage_tile<R, TM>(P, M, T, &px, &abort);  // (synchronises the block)
+    if (abort) return;
     bool mine = false;
     int nt = 0;
     if (need) {
@@ -1241,17 +1326,17 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_residual_inc(const Params 
 }
 
 template <int R>
-cudaError_t launch_tiled_r(int kind, int tm, const Params& P, PatchPlanes work, int arg, uint32_t pass_id, float* out,
-                           cudaStream_t s) {
+cudaError_t launch_tiled_r(int kind, int tm, const Params& P, const TileMaps& M, PatchPlanes work, int arg,
+                           uint32_t pass_id, float* out, cudaStream_t s) {
     dim3 b(kTileW, kTileH), g((P.lw + kTileW - 1) / kTileW, (P.lh + kTileH - 1) / kTileH);
     // the texture-unit kernels fetch through the exemplar's textures, which
     // must be bound
     if (P.ex.hw && (!P.ex.tbase || !P.ex.tout)) return cudaErrorInvalidValue;
 #define PT_TILED_DISPATCH(TMV, HWV)                                                                   \
-    if (kind == 0) kt_propagate_q<R, TMV, HWV><<<g, b, 0, s>>>(P, work, arg);                        \
-    else if (kind == 1) kt_scatter_q<R, TMV, HWV><<<g, b, 0, s>>>(P, work, arg, pass_id);            \
-    else if (P.inc.on || P.inc.fill) kt_residual_inc<R, TMV, HWV><<<g, b, 0, s>>>(P, out);   \
-    else kt_residual<R, TMV, HWV><<<g, b, 0, s>>>(P, out);
+    if (kind == 0) kt_propagate_q<R, TMV, HWV><<<g, b, 0, s>>>(P, M, work, arg);                     \
+    else if (kind == 1) kt_scatter_q<R, TMV, HWV><<<g, b, 0, s>>>(P, M, work, arg, pass_id);         \
+    else if (P.inc.on || P.inc.fill) kt_residual_inc<R, TMV, HWV><<<g, b, 0, s>>>(P, M, out);        \
+    else kt_residual<R, TMV, HWV><<<g, b, 0, s>>>(P, M, out);
     if (P.ex.hw) {
         if (tm == TM_NONE) { PT_TILED_DISPATCH(TM_NONE, 1) }
         else if (tm == TM_FWD) { PT_TILED_DISPATCH(TM_FWD, 1) }

@@ -247,6 +247,12 @@ pt_status pt_set_tiled_kernels(pt_ctx* c, int on) {
     return PT_OK;
 }
 
+pt_status pt_set_tma_staging(pt_ctx* c, int on) {
+    if (!c) return PT_ERR_INVALID;
+    c->use_tma = on != 0;
+    return PT_OK;
+}
+
 pt_status pt_set_incremental(pt_ctx* c, int on) {
     if (!c) return PT_ERR_INVALID;
     c->use_incremental = on != 0;

@@ -2,8 +2,8 @@
 #include "pt_energy.cuh"
 
 namespace pt {
-cudaError_t launch_tiled_2(int kind, int tm, const Params& P, PatchPlanes work, int arg, uint32_t pass_id, float* out,
-                           cudaStream_t s) {
-    return ptk::launch_tiled_r<2>(kind, tm, P, work, arg, pass_id, out, s);
+cudaError_t launch_tiled_2(int kind, int tm, const Params& P, const TileMaps& M, PatchPlanes work, int arg,
+                           uint32_t pass_id, float* out, cudaStream_t s) {
+    return ptk::launch_tiled_r<2>(kind, tm, P, M, work, arg, pass_id, out, s);
 }
 }  // namespace pt

@@ -3,6 +3,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <cuda.h>  // CUtensorMap
 #include <cuda_runtime.h>
 
 #include "painttween.h"
@@ -10,6 +11,8 @@
 namespace ptk {
 
 constexpr int kMaxRadius = 15;  // taps per axis <= 31
+constexpr int kTileW = 32;      // pixel tile of the tiled kernels
+constexpr int kTileH = 8;
 
 // Offset field in three planes (SoA of the 36-byte PatchXF):
 //   A = (x, y, theta, layer as int bits), B = (hysteresis, scaleU, scaleV,
@@ -153,6 +156,20 @@ struct Params {
 struct ConvKernel {
     int r;
     float w[2 * kMaxRadius + 1];
+};
+
+// Tensor maps of the pixel-side planes a tiled kernel stages (each a float4
+// plane read as a FLOAT32 tensor of 4 * level width x level height, boxes of
+// one tile with its halo): the input colour, the canvas and, for temporal
+// passes, the advected colours and the advected records' B plane.  With
+// `on`, blocks whose tile and halo lie inside the level rectangle stage them
+// with tensor copies; the others (and every block without `on`) load them
+// with the clamp rules.  `err` is set when a block's wait for its copies
+// runs out.
+struct TileMaps {
+    CUtensorMap base, canvas, pbase, pout, prec;
+    int* err;
+    int on;
 };
 
 }  // namespace ptk

@@ -116,6 +116,9 @@ class TexSynth:
     def set_tiled_kernels(self, on):
         self._check(lib().pt_set_tiled_kernels(self.h, int(on)), "pt_set_tiled_kernels")
 
+    def set_tma_staging(self, on):
+        self._check(lib().pt_set_tma_staging(self.h, int(on)), "pt_set_tma_staging")
+
     def set_incremental(self, on):
         self._check(lib().pt_set_incremental(self.h, int(on)), "pt_set_incremental")
 

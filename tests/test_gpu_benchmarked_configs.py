@@ -1,14 +1,15 @@
 """The benchmarked configurations against the oracle, bit for bit.
 
 The other parity tests use small images; here the library runs the
-configurations the benchmark and the scaling runs use, cut in length only:
-four frames of the 512x512 animation (r2, 4 levels, 4 iterations, temporal
+configurations the benchmark and the scaling runs use, cut in length: four
+frames of the 512x512 animation (r2, 4 levels, 4 iterations, temporal
 coherence 0.5, FMBM_RM forward and backward), and two frames of the
-1920x1080 clip at full size and full settings (1024x1024 exemplar, r3, 5
-levels, 6 iterations, histogram term on, FMBM_RM forward and backward) --
-grids of thousands of blocks, the largest levels, the early exit, the
+1920x1080 clip at full size (1024x1024 exemplar, r3, 5 levels, histogram
+term on, FMBM_RM forward and backward) with 2 of its 6 iterations per level
+-- grids of thousands of blocks, the largest levels, the early exit, the
 change tracking and the tap queues at their real sizes.  The oracle runs on
-every host thread; these are the slowest tests of the suite.
+every host thread; these are the slowest tests of the suite (the 1080p cut
+at all 6 iterations takes the oracle about 11 minutes on 16 cores).
 """
 import os
 
@@ -49,4 +50,6 @@ def test_anim512_four_frame_cut_matches_oracle(gpu_lib):
 
 
 def test_clip1080p_two_frame_cut_matches_oracle(gpu_lib):
-    _both(synthetic.config("clip1080p"), 2, seed=2026)
+    cfg = synthetic.config("clip1080p")
+    cfg["params"].iterations = 2
+    _both(cfg, 2, seed=2026)

@@ -390,6 +390,38 @@ def test_tiled_and_generic_kernels_identical(r, fm):
         assert_offsets_equal(outs[0][f][1], ref[f][0], 1.0, "tiled vs oracle frame %d" % f)
 
 
+@pytest.mark.parametrize("fm", FILTER_MODES)
+@pytest.mark.parametrize("r", [2, 3, 4])
+def test_tensor_copy_staging_identical_to_plain_loads(r, fm):
+    """Tiles whose halo lies inside the level rectangle are staged by tensor
+    copies (pt_set_tma_staging, the default); plain loads everywhere give
+    the same bits, for every radius, temporal direction and filter mode.
+    Some input colours are subnormal: the texture mode flushes them to zero
+    in shared memory after the copies, as the loads do."""
+    p = config_params(r=r, levels=2, iterations=2, filter_mode=fm)
+    p.temporalCoherenceWeight = 0.5
+    p.hysteresisWeight = 0.25
+    p.distTransWeight = 0.5
+    W, H = 200, 120  # level 0 and 1 both have interior tiles
+    ex = synthetic.make_exemplar(96, 96, seed=70 + r)
+    clip = synthetic.make_clip(W, H, 3, 3, seed=80 + r)
+    for fr in clip:
+        fr["rgba"][30:50, 60:120, 0] = np.float32(1e-40)
+    outs = []
+    for tma in (True, False):
+        s = Synthesizer(device=0)
+        s.setup(p, W, H, 96, 96, 1)
+        s.set_tma_staging(tma)
+        s.set_style(0, ex["base"], ex["output"], ex["orient_tensor"], ex["dist_trans"], ex["object_ids"])
+        for i, fr in enumerate(clip):
+            s.set_frame_dict(i, fr)
+        outs.append(s.synthesize_animation(0, 2))
+        s.close()
+    for f in range(3):
+        assert_offsets_equal(outs[0][f][1], outs[1][f][1], 1.0, "tensor copies vs loads frame %d" % f)
+        assert_array_equal(outs[0][f][0], outs[1][f][0], "tensor copies vs loads output frame %d" % f)
+
+
 @pytest.mark.parametrize("radius", [1, 3, 7])
 def test_convolve_separable_matches_oracle(radius):
     """Separable Gaussian (convolutionRowsGPU + convolutionColumnsGPU) on a
