@@ -350,15 +350,6 @@ __device__ __forceinline__ bool stage_tile(const Params& P, const TileMaps& M, T
                 tma_load_2d(T.prec, &M.prec, 4 * x0, y0, bar);
             }
         }
-        bool ok = mbar_wait(bar, 0);
-        if (!ok) ok = mbar_wait(bar, 0);  // the copies still in flight, once more
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0 && M.err) atomicExch(M.err, 1);
-            *abort = true;
-            return false;
-        }
-        if (P.hwFilter)
-            for (int q = tid; q < N; q += kTileThreads) T.base[q] = lin_texel_of(T.base[q], 1);
     } else {
         const Arr<float4>& ib = P.img.base[P.img.cur];
         for (int q = tid; q < N; q += kTileThreads) {
@@ -375,46 +366,62 @@ __device__ __forceinline__ bool stage_tile(const Params& P, const TileMaps& M, T
             }
         }
     }
-    __syncthreads();
+    // the per-pixel state reads global memory only: with tensor copies it is
+    // computed while they are in flight
     const int x = blockIdx.x * kTileW + threadIdx.x, y = blockIdx.y * kTileH + threadIdx.y;
-    if (x >= P.lw || y >= P.lh) return false;
-    px->x = x;
-    px->y = y;
-    px->sidx = (threadIdx.y + R) * TW + threadIdx.x + R;
-    px->imin = max(-R, -x); px->imax = min(R, P.lw - 1 - x);
-    px->jmin = max(-R, -y); px->jmax = min(R, P.lh - 1 - y);
-    {
-        float sw = 0.0f;
+    const bool in = x < P.lw && y < P.lh;
+    if (in) {
+        px->x = x;
+        px->y = y;
+        px->sidx = (threadIdx.y + R) * TW + threadIdx.x + R;
+        px->imin = max(-R, -x); px->imax = min(R, P.lw - 1 - x);
+        px->jmin = max(-R, -y); px->jmax = min(R, P.lh - 1 - y);
+        {
+            float sw = 0.0f;
 #pragma unroll 1
-        for (int i = -R; i <= R; i++)
+            for (int i = -R; i <= R; i++)
 #pragma unroll
-            for (int j = -R; j <= R; j++) {
-                const bool valid = (i >= px->imin) && (i <= px->imax) && (j >= px->jmin) && (j <= px->jmax);
-                const float w = P.gauss[i + R] * P.gauss[j + R];
-                sw = valid ? sw + w : sw;
+                for (int j = -R; j <= R; j++) {
+                    const bool valid = (i >= px->imin) && (i <= px->imax) && (j >= px->jmin) && (j <= px->jmax);
+                    const float w = P.gauss[i + R] * P.gauss[j + R];
+                    sw = valid ? sw + w : sw;
+                }
+            px->sumW = sw;
+        }
+        const size_t k = (size_t)y * P.W + x;
+        px->hyst_on = false;
+        px->hyst = 0.0f;
+        if (P.hysteresisWeight != 0.0f) {
+            px->hyst_on = __ldg(&P.adv[0].off.B[k].x) > 0;
+            if (px->hyst_on) px->hyst = hysteresis_term(P, x, y);
+        }
+        px->temporal = false;
+        px->prev_fast = false;
+        if (TM) {
+            px->prev = load_patch(P.adv[TM == TM_FWD ? 0 : 1].off, k);
+            bool td = (P.tdIn > 0.f || P.tdOut > 0.f || P.tc > 0.f);
+            px->temporal = td && px->prev.hyst > 0;
+            if (px->temporal) {
+                float a = screen_to_exemplar_angle(P, x, y, px->prev.x, px->prev.y, px->prev.layer);
+                basis(a, P.scaleWU * px->prev.su, P.scaleWV * px->prev.sv, &px->pb0, &px->pb1);
+                px->prev_fast = footprint_inside<R>(px->prev.x, px->prev.y, px->pb0, px->pb1, P.ex.w, P.ex.h);
             }
-        px->sumW = sw;
-    }
-    const size_t k = (size_t)y * P.W + x;
-    px->hyst_on = false;
-    px->hyst = 0.0f;
-    if (P.hysteresisWeight != 0.0f) {
-        px->hyst_on = __ldg(&P.adv[0].off.B[k].x) > 0;
-        if (px->hyst_on) px->hyst = hysteresis_term(P, x, y);
-    }
-    px->temporal = false;
-    px->prev_fast = false;
-    if (TM) {
-        px->prev = load_patch(P.adv[TM == TM_FWD ? 0 : 1].off, k);
-        bool td = (P.tdIn > 0.f || P.tdOut > 0.f || P.tc > 0.f);
-        px->temporal = td && px->prev.hyst > 0;
-        if (px->temporal) {
-            float a = screen_to_exemplar_angle(P, x, y, px->prev.x, px->prev.y, px->prev.layer);
-            basis(a, P.scaleWU * px->prev.su, P.scaleWV * px->prev.sv, &px->pb0, &px->pb1);
-            px->prev_fast = footprint_inside<R>(px->prev.x, px->prev.y, px->pb0, px->pb1, P.ex.w, P.ex.h);
         }
     }
-    return true;
+    if (interior) {
+        const uint32_t bar = smem_addr(&T.bar);
+        bool ok = mbar_wait(bar, 0);
+        if (!ok) ok = mbar_wait(bar, 0);  // the copies still in flight, once more
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0 && M.err) atomicExch(M.err, 1);
+            *abort = true;
+            return false;
+        }
+        if (P.hwFilter)
+            for (int q = tid; q < N; q += kTileThreads) T.base[q] = lin_texel_of(T.base[q], 1);
+    }
+    __syncthreads();
+    return in;
 }
 
 // the four propagate sources of pixel (x, y), in the reference's order
