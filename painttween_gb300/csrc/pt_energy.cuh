@@ -631,40 +631,55 @@ __device__ __forceinline__ void lane_start(const Params& P, const LanePix& q, fl
     e->s0lo = q.sum0 >= 0.0f ? __fmul_rd(q.sum0, kBoundLo) : __fmul_rd(q.sum0, kBoundHi);
 }
 
-// calculateResidual's value at tap (i, j) of candidate e at pixel q, before
-// its Gaussian weight (texSynth_kernel.cu:537-659); fast / fastp are
-// warp-uniform
+// The exemplar samples of tap (i, j) of candidate e at pixel q (and, for a
+// temporal pixel, of its previous offset), with the sample position.
+struct TapSample {
+    float4 tb, to, peb, peo;
+    float tx, ty;
+};
+
 template <int R, int TM, int HW>
-__device__ __forceinline__ float tap_value(const Params& P, const TileSmem<R, TM>& T, const LanePix& q,
-                                           const LaneEval& e, int i, int j, bool fast, bool fastp) {
-    constexpr int TW = TileSmem<R, TM>::TW;
+__device__ __forceinline__ void tap_fetch(const Params& P, const LanePix& q, const LaneEval& e, int i, int j,
+                                          bool fast, bool fastp, TapSample* t) {
     const size_t lsz = (size_t)P.ex.w * P.ex.h;
     const int li = ex_layer(P.ex, e.layer);
     const size_t lo = (size_t)li * lsz;
     const float4* LBO = P.ex.bo + 2 * lo;
     const size_t lp = TM ? (size_t)q.prevlayer * lsz : 0;
     const float hw = (float)P.histW, hh = (float)P.histH;
-    const int s = q.sidx + j * TW + i;
-    const float4 base = T.base[s];
-    const float4 canvas = T.canvas[s];
     float tx = e.cx + fmaf((float)i, e.b0.x, (float)j * e.b1.x);
     float ty = e.cy + fmaf((float)i, e.b0.y, (float)j * e.b1.y);
     if (!fast) {
         if (tx >= hw) tx -= hw; else if (tx < 0) tx += hw;
         if (ty >= hh) ty -= hh; else if (ty < 0) ty += hh;
     }
-    float4 tb, to;
-    sample2<true, HW>(P.ex, li, LBO, tx, ty, &tb, &to, fast);
+    sample2<true, HW>(P.ex, li, LBO, tx, ty, &t->tb, &t->to, fast);
+    t->tx = tx;
+    t->ty = ty;
+    if (TM && q.temporal) {
+        float ptx = q.prevx + fmaf((float)i, q.pb0.x, (float)j * q.pb1.x);
+        float pty = q.prevy + fmaf((float)i, q.pb0.y, (float)j * q.pb1.y);
+        sample2<true, HW>(P.ex, TM ? q.prevlayer : 0, P.ex.bo + 2 * lp, ptx, pty, &t->peb, &t->peo, fastp);
+    }
+}
+
+// calculateResidual's value at tap (i, j) of candidate e at pixel q, before
+// its Gaussian weight (texSynth_kernel.cu:537-659), from the tap's samples
+template <int R, int TM, int HW>
+__device__ __forceinline__ float tap_finish(const Params& P, const TileSmem<R, TM>& T, const LanePix& q,
+                                            const LaneEval& e, int i, int j, const TapSample& t) {
+    constexpr int TW = TileSmem<R, TM>::TW;
+    const int s = q.sidx + j * TW + i;
+    const float4 base = T.base[s];
+    const float4 canvas = T.canvas[s];
+    const float4 tb = t.tb, to = t.to;
+    const float tx = t.tx, ty = t.ty;
     float res = ssd_ap(base, tb, P.alphaWeight) * P.inputAnalogyWeight;
     if (TM) {
         if (q.temporal) {
             const float4 pbase = T.pbase[s], pout = T.pout[s];
-            float ptx = q.prevx + fmaf((float)i, q.pb0.x, (float)j * q.pb1.x);
-            float pty = q.prevy + fmaf((float)i, q.pb0.y, (float)j * q.pb1.y);
-            float4 peb, peo;
-            sample2<true, HW>(P.ex, TM ? q.prevlayer : 0, P.ex.bo + 2 * lp, ptx, pty, &peb, &peo, fastp);
-            float r = ssdp(sub4p(base, pbase), sub4p(tb, peb)) * P.tdIn;
-            r = fmaf(ssdp(sub4p(canvas, pout), sub4p(to, peo)), P.tdOut, r);
+            float r = ssdp(sub4p(base, pbase), sub4p(tb, t.peb)) * P.tdIn;
+            r = fmaf(ssdp(sub4p(canvas, pout), sub4p(to, t.peo)), P.tdOut, r);
             r = fmaf(ssdp(pout, to), P.tc, r);
             res = (T.prec[s].x > 0) ? res + r : res;
         }
@@ -696,12 +711,26 @@ __device__ __forceinline__ float tap_value(const Params& P, const TileSmem<R, TM
     return res;
 }
 
+// calculateResidual's value at tap (i, j) of candidate e at pixel q, before
+// its Gaussian weight; fast / fastp are warp-uniform
+template <int R, int TM, int HW>
+__device__ __forceinline__ float tap_value(const Params& P, const TileSmem<R, TM>& T, const LanePix& q,
+                                           const LaneEval& e, int i, int j, bool fast, bool fastp) {
+    TapSample t;
+    tap_fetch<R, TM, HW>(P, q, e, i, j, fast, fastp, &t);
+    return tap_finish<R, TM, HW>(P, T, q, e, i, j, t);
+}
+
 // the taps of column e.col added to e.sum in the reference's order.  ROLL
 // keeps the column's taps in a loop (a smaller body: faster for scatter,
 // whose chain code competes for the instruction cache; propagate unrolls).
 // EE: a lane leaves the column as soon as its sum reaches e.thr2 (the sum
 // only grows, so stopping at any tap gives the decision of stopping at the
 // column's end), and the loads of its remaining taps are not issued.
+// With the texture unit and the column unrolled, each tap's fetches are
+// issued before the previous tap's sum and exit test (one tap ahead), so two
+// taps' fetch latencies overlap; a lane that exits has fetched one tap more
+// than it uses.
 template <int R, int TM, int HW, bool ROLL, bool EE>
 __device__ __forceinline__ float lane_column(const Params& P, const TileSmem<R, TM>& T, const LanePix& q,
                                              const LaneEval& e, bool fast, bool fastp) {
@@ -709,15 +738,31 @@ __device__ __forceinline__ float lane_column(const Params& P, const TileSmem<R, 
     const bool cvalid = (i >= q.imin) && (i <= q.imax);
     const float gi = P.gauss[i + R];
     float sum = e.sum;
+    if constexpr (HW && !ROLL) {
+        TapSample cur, nxt;
+        tap_fetch<R, TM, HW>(P, q, e, i, -R, fast, fastp, &cur);
+#pragma unroll
+        for (int j = -R; j <= R; j++) {
+            if (j < R) tap_fetch<R, TM, HW>(P, q, e, i, j + 1, fast, fastp, &nxt);
+            const bool valid = cvalid && (j >= q.jmin) && (j <= q.jmax);
+            const float res = tap_finish<R, TM, HW>(P, T, q, e, i, j, cur);
+            const float w = gi * P.gauss[j + R];
+            sum = valid ? fmaf(res, w, sum) : sum;
+            if (EE && sum >= e.thr2) break;
+            cur = nxt;
+        }
+        return sum;
+    } else {
 #pragma unroll(ROLL ? 1 : 2 * R + 1)
-    for (int j = -R; j <= R; j++) {
-        const bool valid = cvalid && (j >= q.jmin) && (j <= q.jmax);
-        const float res = tap_value<R, TM, HW>(P, T, q, e, i, j, fast, fastp);
-        const float w = gi * P.gauss[j + R];
-        sum = valid ? fmaf(res, w, sum) : sum;
-        if (EE && sum >= e.thr2) break;
+        for (int j = -R; j <= R; j++) {
+            const bool valid = cvalid && (j >= q.jmin) && (j <= q.jmax);
+            const float res = tap_value<R, TM, HW>(P, T, q, e, i, j, fast, fastp);
+            const float w = gi * P.gauss[j + R];
+            sum = valid ? fmaf(res, w, sum) : sum;
+            if (EE && sum >= e.thr2) break;
+        }
+        return sum;
     }
-    return sum;
 }
 
 // taps of the first `cols` columns inside the level rectangle
