@@ -727,10 +727,9 @@ __device__ __forceinline__ float tap_value(const Params& P, const TileSmem<R, TM
 // EE: a lane leaves the column as soon as its sum reaches e.thr2 (the sum
 // only grows, so stopping at any tap gives the decision of stopping at the
 // column's end), and the loads of its remaining taps are not issued.
-// With the texture unit and the column unrolled, each tap's fetches are
-// issued before the previous tap's sum and exit test (one tap ahead), so two
-// taps' fetch latencies overlap; a lane that exits has fetched one tap more
-// than it uses.
+// With the texture unit each tap's fetches are issued before the previous
+// tap's sum and exit test (one tap ahead), so two taps' fetch latencies
+// overlap; a lane that exits has fetched one tap more than it uses.
 template <int R, int TM, int HW, bool ROLL, bool EE>
 __device__ __forceinline__ float lane_column(const Params& P, const TileSmem<R, TM>& T, const LanePix& q,
                                              const LaneEval& e, bool fast, bool fastp) {
@@ -805,18 +804,41 @@ __device__ __forceinline__ bool lane_step(const Params& P, const TileSmem<R, TM>
     }
     if (EE && KB > 0 && !e.exact) {
         bool rejected = false;
+        if constexpr (HW) {  // (the next tap's fetches issued before this tap's test, as in lane_column)
+            TapSample cur, nxt;
+            int ij = TT.ij[e.col];
+            tap_fetch<R, TM, HW>(P, q, e, (ij & 15) - R, (ij >> 4) - R, fast, fastp, &cur);
 #pragma unroll(ROLL ? 1 : 2 * R + 1)
-        for (int k = 0; k < 2 * R + 1; k++) {
-            const int pos = e.col + k;
-            if (pos >= KB) break;
-            const int ij = TT.ij[pos];
-            const int i = (ij & 15) - R, j = (ij >> 4) - R;
-            const bool valid = (i >= q.imin) && (i <= q.imax) && (j >= q.jmin) && (j <= q.jmax);
-            const float res = tap_value<R, TM, HW>(P, T, q, e, i, j, fast, fastp);
-            e.sum = valid ? __fadd_rd(e.sum, __fmul_rd(res, TT.w[pos])) : e.sum;
-            if (__fadd_rd(__fmul_rd(e.sum, kBoundLo), e.s0lo) >= e.thr2) {
-                rejected = true;
-                break;
+            for (int k = 0; k < 2 * R + 1; k++) {
+                const int pos = e.col + k;
+                if (pos >= KB) break;
+                const int i = (ij & 15) - R, j = (ij >> 4) - R;
+                const int ijn = (pos + 1 < KB && k + 1 < 2 * R + 1) ? TT.ij[pos + 1] : -1;
+                if (ijn >= 0) tap_fetch<R, TM, HW>(P, q, e, (ijn & 15) - R, (ijn >> 4) - R, fast, fastp, &nxt);
+                const bool valid = (i >= q.imin) && (i <= q.imax) && (j >= q.jmin) && (j <= q.jmax);
+                const float res = tap_finish<R, TM, HW>(P, T, q, e, i, j, cur);
+                e.sum = valid ? __fadd_rd(e.sum, __fmul_rd(res, TT.w[pos])) : e.sum;
+                if (__fadd_rd(__fmul_rd(e.sum, kBoundLo), e.s0lo) >= e.thr2) {
+                    rejected = true;
+                    break;
+                }
+                cur = nxt;
+                ij = ijn;
+            }
+        } else {
+#pragma unroll(ROLL ? 1 : 2 * R + 1)
+            for (int k = 0; k < 2 * R + 1; k++) {
+                const int pos = e.col + k;
+                if (pos >= KB) break;
+                const int ij = TT.ij[pos];
+                const int i = (ij & 15) - R, j = (ij >> 4) - R;
+                const bool valid = (i >= q.imin) && (i <= q.imax) && (j >= q.jmin) && (j <= q.jmax);
+                const float res = tap_value<R, TM, HW>(P, T, q, e, i, j, fast, fastp);
+                e.sum = valid ? __fadd_rd(e.sum, __fmul_rd(res, TT.w[pos])) : e.sum;
+                if (__fadd_rd(__fmul_rd(e.sum, kBoundLo), e.s0lo) >= e.thr2) {
+                    rejected = true;
+                    break;
+                }
             }
         }
         e.col += 2 * R + 1;
