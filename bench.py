@@ -364,6 +364,7 @@ def run_ours(args, dist):
     if args.generic_kernels:
         s.set_tiled_kernels(False)  # same results, one-thread-per-pixel kernels (profiling them)
     s.set_tma_staging(args.staging == "tma")
+    s.set_propagate_lanes(args.propagate_lanes)
     s.set_style(0, ex["base"], ex["output"], ex["orient_tensor"], ex["dist_trans"], ex["object_ids"])
     for i, fr in enumerate(clip):
         s.set_frame_dict(i, fr)
@@ -482,6 +483,7 @@ def run_ours(args, dist):
                    "iterations": p.iterations, "scheme": "FMBM_RM", "histogram": True,
                    "kernels": "generic" if args.generic_kernels else "tiled",
                    "staging": args.staging,
+                   "propagate_warps_per_row": args.propagate_lanes or "autotuned",
                    "filter": args.filter,
                    "parallelism": "replicas" if dist.ws > 1 else "single",
                    "l2": "inputs larger than L2 (%.1f GB of resident frame pyramids per step)"
@@ -756,6 +758,8 @@ def main():
                     help="bilinear arithmetic: the texture unit's (the reference's) or exact FP32")
     ap.add_argument("--staging", default="tma", choices=["tma", "loads"],
                     help="how the tiled kernels stage interior tiles: tensor copies or plain loads (same results)")
+    ap.add_argument("--propagate-lanes", type=int, default=0, choices=[0, 1, 2],
+                    help="propagate's warps per tile row: 0 = autotuned per launch shape (same results)")
     ap.add_argument("--generic-kernels", action="store_true",
                     help="run the generic one-thread-per-pixel kernels instead of the tiled ones (profiling only)")
     args = ap.parse_args()

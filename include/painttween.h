@@ -541,6 +541,12 @@ pt_status pt_set_tiled_kernels(pt_ctx* ctx, int on);
  * block that gives up waiting for its copies (a bounded wait) makes the next
  * pt_synchronize / pt_synthesize_* return PT_ERR_CUDA. */
 pt_status pt_set_tma_staging(pt_ctx* ctx, int on);
+/* Warps per tile row of the tiled propagate kernel: 1 = one (a lane per
+ * pixel), 2 = two (the second warp only evaluates candidates from the row's
+ * queue: twice the lanes for the same candidates), 0 (default) = picked per
+ * launch shape (radius, temporal mode, filter mode, tile count) by an
+ * autotuner that times one launch of each.  All compute identical results. */
+pt_status pt_set_propagate_lanes(pt_ctx* ctx, int warps_per_row);
 /* Selects whether the propagate/scatter loops of pt_synthesize_frame and
  * pt_synthesize_animation track which offsets each pass changed and skip the
  * evaluations whose inputs are unchanged since an earlier pass with the same

@@ -77,6 +77,7 @@ SIGNATURES = {
     "pt_set_profiling": (_I, [_VP, _I]),
     "pt_set_tiled_kernels": (_I, [_VP, _I]),
     "pt_set_tma_staging": (_I, [_VP, _I]),
+    "pt_set_propagate_lanes": (_I, [_VP, _I]),
     "pt_set_incremental": (_I, [_VP, _I]),
     "pt_get_frame_result": (_I, [_VP, _I, _VP, _VP]),
     "pt_get_frame_residual": (_I, [_VP, _I, _VP]),

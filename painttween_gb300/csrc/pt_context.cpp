@@ -525,6 +525,50 @@ static void tile_maps(pt_ctx* c, const Params& P, int tm, TileMaps* M) {
     M->on = ok ? 1 : 0;
 }
 
+// Propagate's warps per tile row for this launch (0: one, 1: two) and the
+// variant being timed (-1: none).  Until both variants of a launch shape
+// have been timed, the coarse levels (no more tiles than SMs) take two.
+static int propagate_variant(pt_ctx* c, const Params& P, int tm, int* probe) {
+    *probe = -1;
+    if (c->prop_lanes) return c->prop_lanes - 1;
+    if (!c->sm_count) {
+        if (cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess) {
+            cudaGetLastError();
+            c->sm_count = 152;
+        }
+    }
+    const int blocks = ((P.lw + ptk::kTileW - 1) / ptk::kTileW) * ((P.lh + ptk::kTileH - 1) / ptk::kTileH);
+    const int fallback = blocks <= c->sm_count ? 1 : 0;
+    pt_ctx::Tune& t = c->tune[std::make_tuple(P.r, tm, P.ex.hw, blocks)];
+    if (t.choice >= 0) return t.choice;
+    if (t.probes < 2) {
+        for (int k = 0; k < 2; k++)
+            if (!t.ev[2 * t.probes + k] && cudaEventCreate(&t.ev[2 * t.probes + k]) != cudaSuccess) {
+                cudaGetLastError();
+                t.choice = fallback;  // no events: no timing
+                return fallback;
+            }
+        *probe = t.probes;
+        return t.probes++;
+    }
+    if (cudaEventQuery(t.ev[3]) == cudaSuccess && cudaEventQuery(t.ev[1]) == cudaSuccess) {
+        float a = 0.f, b = 0.f;
+        if (cudaEventElapsedTime(&a, t.ev[0], t.ev[1]) == cudaSuccess &&
+            cudaEventElapsedTime(&b, t.ev[2], t.ev[3]) == cudaSuccess)
+            t.choice = b < a ? 1 : 0;
+        else
+            t.choice = fallback;
+        cudaGetLastError();
+        for (auto& e : t.ev) {
+            if (e) cudaEventDestroy(e);
+            e = nullptr;
+        }
+        return t.choice;
+    }
+    cudaGetLastError();  // (cudaErrorNotReady)
+    return fallback;
+}
+
 cudaError_t launch_tiled(pt_ctx* c, int kind, const Params& P, PatchPlanes work, int arg, uint32_t pass_id,
                          float* out, bool* done) {
     *done = false;
@@ -533,12 +577,21 @@ cudaError_t launch_tiled(pt_ctx* c, int kind, const Params& P, PatchPlanes work,
     if (P.r < 2 || P.r > 4) return cudaSuccess;
     TileMaps M;
     tile_maps(c, P, tm, &M);
+    int probe = -1;
+    const int wide = kind == 0 ? propagate_variant(c, P, tm, &probe) : 0;
+    pt_ctx::Tune* t = probe >= 0 ? &c->tune[std::make_tuple(P.r, tm, P.ex.hw, ((P.lw + ptk::kTileW - 1) / ptk::kTileW) *
+                                                                                   ((P.lh + ptk::kTileH - 1) / ptk::kTileH))]
+                                 : nullptr;
+    if (t) cudaEventRecord(t->ev[2 * probe], c->stream);
     *done = true;
+    cudaError_t e;
     switch (P.r) {
-        case 2: return pt::launch_tiled_2(kind, tm, P, M, work, arg, pass_id, out, c->stream);
-        case 3: return pt::launch_tiled_3(kind, tm, P, M, work, arg, pass_id, out, c->stream);
-        default: return pt::launch_tiled_4(kind, tm, P, M, work, arg, pass_id, out, c->stream);
+        case 2: e = pt::launch_tiled_2(kind, tm, P, M, work, arg, pass_id, out, wide, c->stream); break;
+        case 3: e = pt::launch_tiled_3(kind, tm, P, M, work, arg, pass_id, out, wide, c->stream); break;
+        default: e = pt::launch_tiled_4(kind, tm, P, M, work, arg, pass_id, out, wide, c->stream); break;
     }
+    if (t) cudaEventRecord(t->ev[2 * probe + 1], c->stream);
+    return e;
 }
 
 // the tensor-copy error flag: PT_ERR_CUDA (and the flag cleared) when a
@@ -745,6 +798,9 @@ pt_status pt_destroy(pt_ctx* c) {
     for (auto& e : c->timers)
         if (e) cudaEventDestroy(e);
     for (auto& e : c->ev_pool) cudaEventDestroy(e);
+    for (auto& kv : c->tune)
+        for (auto& e : kv.second.ev)
+            if (e) cudaEventDestroy(e);
     for (auto& v : c->ev_pairs)
         for (auto& pr : v) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
     free_textures(c, &c->up_ex);

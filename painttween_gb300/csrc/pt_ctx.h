@@ -206,6 +206,18 @@ struct pt_ctx {
     bool adv_written[2] = {false, false};  // advected F/B written since the last reset
     bool use_tiled = true;                 // tiled kernels where an instantiation exists
     bool use_tma = true;                   // interior tiles staged by tensor copies
+    // propagate's warps per tile row: 0 = picked by the autotuner below, 1 or 2
+    int prop_lanes = 0;
+    int sm_count = 0;
+    // autotuner of propagate's warps per tile row, per (radius, temporal
+    // mode, filter mode, blocks): one launch of each variant is timed with
+    // events (the results are identical), and the faster one is kept
+    struct Tune {
+        int choice = -1;   // 0: one warp per row, 1: two; -1: not decided
+        int probes = 0;    // variants launched with events
+        cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    };
+    std::map<std::tuple<int, int, int, int>, Tune> tune;
     int* tma_err = nullptr;                // set by a block whose tensor-copy wait ran out
     // tensor maps of staged planes: (plane, pitch, level w, level h, box) -> map
     std::map<std::tuple<const void*, int, int, int, int>, CUtensorMap> tmaps;

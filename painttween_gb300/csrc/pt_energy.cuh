@@ -317,13 +317,14 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
 
 // Stages the tile (and halo) of the pixel-side inputs and fills the
 // per-pixel state.  Returns false for threads whose pixel is outside the
-// level rectangle.  A tile whose halo lies inside the level rectangle, where
+// level rectangle (and for the threads of a block of NT > kTileThreads
+// threads past the tile's pixels, which only evaluate candidates).  A tile whose halo lies inside the level rectangle, where
 // the clamps are no-ops, is copied by tensor copies when the maps are on
 // (one thread issues them; the texture mode's flush of subnormal input
 // colours follows in shared memory); the others load texel by texel with
 // the clamp rules.  *abort is set (for the whole block) when the copies did
 // not complete within two bounded waits; the block must then return.
-template <int R, int TM>
+template <int R, int TM, int NT = kTileThreads>
 __device__ __forceinline__ bool stage_tile(const Params& P, const TileMaps& M, TileSmem<R, TM>& T, PixT* px,
                                            bool* abort) {
     constexpr int TW = TileSmem<R, TM>::TW, TH = TileSmem<R, TM>::TH, N = TileSmem<R, TM>::N;
@@ -352,7 +353,7 @@ __device__ __forceinline__ bool stage_tile(const Params& P, const TileMaps& M, T
         }
     } else {
         const Arr<float4>& ib = P.img.base[P.img.cur];
-        for (int q = tid; q < N; q += kTileThreads) {
+        for (int q = tid; q < N; q += NT) {
             int gx = clampi(x0 + q % TW, 0, P.lw - 1);
             int gy = clampi(y0 + q / TW, 0, P.lh - 1);
             size_t k = (size_t)gy * P.W + gx;
@@ -369,7 +370,7 @@ __device__ __forceinline__ bool stage_tile(const Params& P, const TileMaps& M, T
     // the per-pixel state reads global memory only: with tensor copies it is
     // computed while they are in flight
     const int x = blockIdx.x * kTileW + threadIdx.x, y = blockIdx.y * kTileH + threadIdx.y;
-    const bool in = x < P.lw && y < P.lh;
+    const bool in = tid < kTileThreads && x < P.lw && y < P.lh;  // (threads past the tile's pixels only evaluate)
     if (in) {
         px->x = x;
         px->y = y;
@@ -418,7 +419,7 @@ __device__ __forceinline__ bool stage_tile(const Params& P, const TileMaps& M, T
             return false;
         }
         if (P.hwFilter)
-            for (int q = tid; q < N; q += kTileThreads) T.base[q] = lin_texel_of(T.base[q], 1);
+            for (int q = tid; q < N; q += NT) T.base[q] = lin_texel_of(T.base[q], 1);
     }
     __syncthreads();
     return in;
@@ -885,10 +886,15 @@ struct PropQueue {
     int count[kTileH], next[kTileH];  // per warp: its row's candidates (list[128 * warp ...])
 };
 
-// propagate_kernel with lane cursors over the tile's candidates
-template <int R, int TM, int HW>
-__global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P, const __grid_constant__ TileMaps M,
-                                                                       PatchPlanes work, int jump) {
+// propagate_kernel with lane cursors over the tile's candidates.  WIDE
+// warps per tile row: with WIDE = 2 the block has twice the tile's threads
+// and the second half only takes candidates from the rows' queues (the same
+// candidates and results, evaluated by twice the lanes: for the coarse
+// levels, whose few tiles leave most of the GPU idle).
+template <int R, int TM, int HW, int WIDE>
+__global__ void __launch_bounds__(kTileThreads * WIDE, WIDE == 1 ? 2 : 1)
+    kt_propagate_q(const Params P, const __grid_constant__ TileMaps M, PatchPlanes work, int jump) {
+    const int pid = threadIdx.x + threadIdx.y * kTileW;
     __shared__ TileSmem<R, TM> T;
     __shared__ PixShared S;
     __shared__ PropQueue Q;
@@ -900,7 +906,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P
     unsigned skip = 0;
     if (P.inc.on) {
         const int x = blockIdx.x * kTileW + threadIdx.x, y = blockIdx.y * kTileH + threadIdx.y;
-        const bool in = x < P.lw && y < P.lh;
+        const bool in = pid < kTileThreads && x < P.lw && y < P.lh;
         const size_t k = (size_t)y * P.W + x;
         bool need = in;
         if (in && P.inc.prev != INT_MIN && __ldg(P.inc.win + k) < P.inc.prev) {
@@ -914,12 +920,11 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P
         }
         if (block_idle(P, work, need, in, k)) return;
     }
-    const int pid = threadIdx.x + threadIdx.y * kTileW;
     if (pid < kTileH) { Q.count[pid] = 0; Q.next[pid] = 0; }
     load_tap_table<R>(P, TT);
     PixT px;
     bool abort;
-    const bool in = stage_tile<R, TM>(P, M, T, &px, &abort);  // (synchronises the block)
+    const bool in = stage_tile<R, TM, kTileThreads * WIDE>(P, M, T, &px, &abort);  // (synchronises the block)
     if (abort) return;
     // phase 1: each pixel builds its candidates (the reference's order,
     // repeats and test_offset rejections resolved here) and queues them
@@ -983,7 +988,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P
             put_pix<R>(S, pid, lane_pix<R>(P, px));
         }
     }
-    {
+    if (pid < kTileThreads) {  // (whole warps)
         // queue this pixel's n candidates
         const unsigned lane = lane_id();
         int incl = n;
@@ -1006,7 +1011,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_propagate_q(const Params P
         LaneEval e;
         bool act = false, more = true;
         int cur = 0;
-        const int warp = pid / kTileW;
+        const int warp = (pid / kTileW) % kTileH;  // the row whose queue this warp takes from
         const int count = Q.count[warp];
 #pragma unroll 1
         while (true) {
@@ -1401,13 +1406,14 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_residual_inc(const Params 
 
 template <int R>
 cudaError_t launch_tiled_r(int kind, int tm, const Params& P, const TileMaps& M, PatchPlanes work, int arg,
-                           uint32_t pass_id, float* out, cudaStream_t s) {
-    dim3 b(kTileW, kTileH), g((P.lw + kTileW - 1) / kTileW, (P.lh + kTileH - 1) / kTileH);
+                           uint32_t pass_id, float* out, int wide, cudaStream_t s) {
+    dim3 b(kTileW, kTileH), bw(kTileW, 2 * kTileH), g((P.lw + kTileW - 1) / kTileW, (P.lh + kTileH - 1) / kTileH);
     // the texture-unit kernels fetch through the exemplar's textures, which
     // must be bound
     if (P.ex.hw && (!P.ex.tbase || !P.ex.tout)) return cudaErrorInvalidValue;
 #define PT_TILED_DISPATCH(TMV, HWV)                                                                   \
-    if (kind == 0) kt_propagate_q<R, TMV, HWV><<<g, b, 0, s>>>(P, M, work, arg);                     \
+    if (kind == 0 && wide) kt_propagate_q<R, TMV, HWV, 2><<<g, bw, 0, s>>>(P, M, work, arg);          \
+    else if (kind == 0) kt_propagate_q<R, TMV, HWV, 1><<<g, b, 0, s>>>(P, M, work, arg);             \
     else if (kind == 1) kt_scatter_q<R, TMV, HWV><<<g, b, 0, s>>>(P, M, work, arg, pass_id);         \
     else if (P.inc.on || P.inc.fill) kt_residual_inc<R, TMV, HWV><<<g, b, 0, s>>>(P, M, out);        \
     else kt_residual<R, TMV, HWV><<<g, b, 0, s>>>(P, M, out);

@@ -247,6 +247,12 @@ pt_status pt_set_tiled_kernels(pt_ctx* c, int on) {
     return PT_OK;
 }
 
+pt_status pt_set_propagate_lanes(pt_ctx* c, int warps_per_row) {
+    if (!c || warps_per_row < 0 || warps_per_row > 2) return PT_ERR_INVALID;
+    c->prop_lanes = warps_per_row;
+    return PT_OK;
+}
+
 pt_status pt_set_tma_staging(pt_ctx* c, int on) {
     if (!c) return PT_ERR_INVALID;
     c->use_tma = on != 0;

@@ -83,11 +83,12 @@ cudaError_t launch_interleave_texels(const float4* base, const float4* out, floa
 // tiled patch-distance kernels for patch radius 2, 3, 4 (pt_tiled_r*.cu):
 // kind 0 = propagate (arg = jump), 1 = scatter (arg = write_all),
 // 2 = residual (into out); tm 0 = no temporal terms, 1 = forward, 2 = backward;
-// M: the tensor maps of the staged planes (M.on = 0: staged by plain loads)
+// M: the tensor maps of the staged planes (M.on = 0: staged by plain loads);
+// wide: propagate with two warps per tile row (same results)
 cudaError_t launch_tiled_2(int kind, int tm, const Params& P, const TileMaps& M, PatchPlanes work, int arg,
-                           uint32_t pass_id, float* out, cudaStream_t s);
+                           uint32_t pass_id, float* out, int wide, cudaStream_t s);
 cudaError_t launch_tiled_3(int kind, int tm, const Params& P, const TileMaps& M, PatchPlanes work, int arg,
-                           uint32_t pass_id, float* out, cudaStream_t s);
+                           uint32_t pass_id, float* out, int wide, cudaStream_t s);
 cudaError_t launch_tiled_4(int kind, int tm, const Params& P, const TileMaps& M, PatchPlanes work, int arg,
-                           uint32_t pass_id, float* out, cudaStream_t s);
+                           uint32_t pass_id, float* out, int wide, cudaStream_t s);
 }  // namespace pt

@@ -3,7 +3,7 @@
 
 namespace pt {
 cudaError_t launch_tiled_4(int kind, int tm, const Params& P, const TileMaps& M, PatchPlanes work, int arg,
-                           uint32_t pass_id, float* out, cudaStream_t s) {
-    return ptk::launch_tiled_r<4>(kind, tm, P, M, work, arg, pass_id, out, s);
+                           uint32_t pass_id, float* out, int wide, cudaStream_t s) {
+    return ptk::launch_tiled_r<4>(kind, tm, P, M, work, arg, pass_id, out, wide, s);
 }
 }  // namespace pt

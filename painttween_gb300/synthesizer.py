@@ -116,6 +116,9 @@ class TexSynth:
     def set_tiled_kernels(self, on):
         self._check(lib().pt_set_tiled_kernels(self.h, int(on)), "pt_set_tiled_kernels")
 
+    def set_propagate_lanes(self, warps_per_row):
+        self._check(lib().pt_set_propagate_lanes(self.h, int(warps_per_row)), "pt_set_propagate_lanes")
+
     def set_tma_staging(self, on):
         self._check(lib().pt_set_tma_staging(self.h, int(on)), "pt_set_tma_staging")
 

@@ -422,6 +422,37 @@ def test_tensor_copy_staging_identical_to_plain_loads(r, fm):
         assert_array_equal(outs[0][f][0], outs[1][f][0], "tensor copies vs loads output frame %d" % f)
 
 
+@pytest.mark.parametrize("fm", FILTER_MODES)
+@pytest.mark.parametrize("r", [2, 3, 4])
+def test_propagate_warps_per_row_identical(r, fm):
+    """Propagate with one warp per tile row, with two (the second only
+    evaluating queued candidates), and with the autotuner's choice per
+    launch shape give the same bits, and equal the oracle."""
+    p = config_params(r=r, levels=3, iterations=2, filter_mode=fm)
+    p.temporalCoherenceWeight = 0.5
+    p.hysteresisWeight = 0.25
+    W, H = 160, 96
+    ex = synthetic.make_exemplar(80, 80, seed=90 + r)
+    clip = synthetic.make_clip(W, H, 3, 3, seed=95 + r)
+    outs = []
+    for lanes in (1, 2, 0):
+        s = Synthesizer(device=0)
+        s.setup(p, W, H, 80, 80, 1)
+        s.set_propagate_lanes(lanes)
+        s.set_style(0, ex["base"], ex["output"], ex["orient_tensor"], ex["dist_trans"], ex["object_ids"])
+        for i, fr in enumerate(clip):
+            s.set_frame_dict(i, fr)
+        outs.append(s.synthesize_animation(0, 2))
+        s.close()
+    for o, name in ((outs[1], "two warps"), (outs[2], "autotuned")):
+        for f in range(3):
+            assert_offsets_equal(o[f][1], outs[0][f][1], 1.0, "%s vs one warp, frame %d" % (name, f))
+            assert_array_equal(o[f][0], outs[0][f][0], "%s vs one warp output, frame %d" % (name, f))
+    ref = O.OracleDriver(p, [ex], clip, threads=8).render(0, 2)
+    for f in range(3):
+        assert_offsets_equal(outs[1][f][1], ref[f][0], 1.0, "two warps vs oracle frame %d" % f)
+
+
 @pytest.mark.parametrize("radius", [1, 3, 7])
 def test_convolve_separable_matches_oracle(radius):
     """Separable Gaussian (convolutionRowsGPU + convolutionColumnsGPU) on a
