@@ -3,6 +3,8 @@
 // creation, parameters, initialisation and the step-wise image uploads.
 #include "pt_ctx.h"
 
+#include <mutex>
+
 // ---------------------------------------------------------------------------
 // errors and allocation
 // ---------------------------------------------------------------------------
@@ -526,20 +528,41 @@ static void tile_maps(pt_ctx* c, const Params& P, int tm, TileMaps* M) {
 }
 
 // Propagate's warps per tile row for this launch (0: one, 1: two) and the
-// variant being timed (-1: none).  Until both variants of a launch shape
-// have been timed, the coarse levels (no more tiles than SMs) take two.
-static int propagate_variant(pt_ctx* c, const Params& P, int tm, int* probe) {
-    *probe = -1;
-    if (c->prop_lanes) return c->prop_lanes - 1;
+// variant being timed (-1: none).  Launch shapes are keyed by radius,
+// temporal mode, filter mode and the tile count relative to the SM count,
+// in powers of two (up to a quarter, half, one, 2, 4, 8 SMs' worth, more):
+// the choice depends on how much of the GPU the tiles fill.  Decisions are shared by the contexts of a
+// device; until a shape's two variants have been timed, shapes with no
+// more tiles than SMs take two warps.
+static std::mutex g_tune_mutex;
+static std::map<std::tuple<int, int, int, int, int>, int> g_tune;  // (device, shape) -> choice
+
+static std::tuple<int, int, int, int> tune_key(pt_ctx* c, const Params& P, int tm, int* blocks) {
     if (!c->sm_count) {
         if (cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess) {
             cudaGetLastError();
             c->sm_count = 152;
         }
     }
-    const int blocks = ((P.lw + ptk::kTileW - 1) / ptk::kTileW) * ((P.lh + ptk::kTileH - 1) / ptk::kTileH);
+    *blocks = ((P.lw + ptk::kTileW - 1) / ptk::kTileW) * ((P.lh + ptk::kTileH - 1) / ptk::kTileH);
+    int cls = 0;
+    while (cls < 6 && 4 * (long long)*blocks > ((long long)c->sm_count << cls)) cls++;
+    return std::make_tuple(P.r, tm, P.ex.hw, cls);
+}
+
+static int propagate_variant(pt_ctx* c, const Params& P, int tm, int* probe) {
+    *probe = -1;
+    if (c->prop_lanes) return c->prop_lanes - 1;
+    int blocks = 0;
+    const auto key = tune_key(c, P, tm, &blocks);
+    const auto gkey = std::tuple_cat(std::make_tuple(c->device), key);
     const int fallback = blocks <= c->sm_count ? 1 : 0;
-    pt_ctx::Tune& t = c->tune[std::make_tuple(P.r, tm, P.ex.hw, blocks)];
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mutex);
+        auto it = g_tune.find(gkey);
+        if (it != g_tune.end()) return it->second;
+    }
+    pt_ctx::Tune& t = c->tune[key];
     if (t.choice >= 0) return t.choice;
     if (t.probes < 2) {
         for (int k = 0; k < 2; k++)
@@ -554,10 +577,13 @@ static int propagate_variant(pt_ctx* c, const Params& P, int tm, int* probe) {
     if (cudaEventQuery(t.ev[3]) == cudaSuccess && cudaEventQuery(t.ev[1]) == cudaSuccess) {
         float a = 0.f, b = 0.f;
         if (cudaEventElapsedTime(&a, t.ev[0], t.ev[1]) == cudaSuccess &&
-            cudaEventElapsedTime(&b, t.ev[2], t.ev[3]) == cudaSuccess)
+            cudaEventElapsedTime(&b, t.ev[2], t.ev[3]) == cudaSuccess) {
             t.choice = b < a ? 1 : 0;
-        else
+            std::lock_guard<std::mutex> lk(g_tune_mutex);
+            g_tune.emplace(gkey, t.choice);
+        } else {
             t.choice = fallback;
+        }
         cudaGetLastError();
         for (auto& e : t.ev) {
             if (e) cudaEventDestroy(e);
@@ -579,9 +605,8 @@ cudaError_t launch_tiled(pt_ctx* c, int kind, const Params& P, PatchPlanes work,
     tile_maps(c, P, tm, &M);
     int probe = -1;
     const int wide = kind == 0 ? propagate_variant(c, P, tm, &probe) : 0;
-    pt_ctx::Tune* t = probe >= 0 ? &c->tune[std::make_tuple(P.r, tm, P.ex.hw, ((P.lw + ptk::kTileW - 1) / ptk::kTileW) *
-                                                                                   ((P.lh + ptk::kTileH - 1) / ptk::kTileH))]
-                                 : nullptr;
+    int blocks = 0;
+    pt_ctx::Tune* t = probe >= 0 ? &c->tune[tune_key(c, P, tm, &blocks)] : nullptr;
     if (t) cudaEventRecord(t->ev[2 * probe], c->stream);
     *done = true;
     cudaError_t e;

@@ -209,9 +209,10 @@ struct pt_ctx {
     // propagate's warps per tile row: 0 = picked by the autotuner below, 1 or 2
     int prop_lanes = 0;
     int sm_count = 0;
-    // autotuner of propagate's warps per tile row, per (radius, temporal
-    // mode, filter mode, blocks): one launch of each variant is timed with
-    // events (the results are identical), and the faster one is kept
+    // autotuner of propagate's warps per tile row, per launch shape (radius,
+    // temporal mode, filter mode, tile-count class): one launch of each
+    // variant is timed with events (the results are identical), and the
+    // faster one is kept, for every context of the device
     struct Tune {
         int choice = -1;   // 0: one warp per row, 1: two; -1: not decided
         int probes = 0;    // variants launched with events
