@@ -15,7 +15,8 @@ and drives it in the reference's call sequence:
   WorkingBuffers::loadResidual reads the half .b channel).
 
 Only tests, __graft_entry__.smoke() and bench.py's CPU baseline may use this
-module, and only as the checker / the timed CPU baseline.
+module, and only to check the library's results or as the timed CPU
+baseline.
 """
 import ctypes
 import math

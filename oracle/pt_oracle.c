@@ -2,8 +2,9 @@
  * pt_oracle.c -- CPU oracle for PaintTween's offset-field synthesis.
  *
  * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
- * CPU-baseline leg of bench.py may load this library, and only as the checker
- * (or the timed CPU baseline); the product library never calls it.
+ * CPU-baseline leg of bench.py may load this library, and only to check the
+ * library's results (or as the timed CPU baseline); the product library
+ * never calls it.
  *
  * What it is: a scalar C restatement of the reference's hot path
  * (src/PaintTweenCUDA/texSynth_kernel.cu, texSynth_util.h, cudaImageBuffer.h,

@@ -81,7 +81,7 @@ int main(int argc, char** argv) {
     }
     std::vector<int32_t> hdr = read_array<int32_t>(in, 7);
     if (hdr[0] != 0x4C435450 || hdr[6] != (int32_t)sizeof(pt_params)) {
-        std::fprintf(stderr, "bad header (params size %d, this build %d)\n", hdr[6], (int)sizeof(pt_params));
+        std::fprintf(stderr, "bad header (params size %d, compiled %d)\n", hdr[6], (int)sizeof(pt_params));
         return 1;
     }
     const int w = hdr[1], h = hdr[2], ew = hdr[3], eh = hdr[4], frames = hdr[5];
