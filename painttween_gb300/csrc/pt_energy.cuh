@@ -513,13 +513,12 @@ constexpr unsigned kFull = 0xffffffffu;
 // (1 -/+ 2^-17): bounds of the rounding of a reference-order sum of <= 81 terms
 constexpr float kBoundLo = 1.0f - 1.0f / 131072.0f;
 constexpr float kBoundHi = 1.0f + 1.0f / 131072.0f;
-// Groups of 2R+1 taps of propagate's bound pass: none.  Propagate's
-// candidates come from coherent neighbours, so their energies are mostly
-// close to the best and a bound pass rarely rejects them before its end
-// (measured: 1 or 2 groups +45-53 %, the full pass +20 % propagate time);
-// scatter's random-search candidates are rejected after a few heavy taps
-// (full bound pass: -45 % scatter time).
-constexpr int kPropagateBoundGroups = 0;
+// Propagate takes no bound pass: its candidates come from coherent
+// neighbours, so their energies are mostly close to the best and a bound
+// pass rarely rejects them before its end (measured: 1 or 2 groups of 2R+1
+// taps +45-53 %, the full pass +20 % propagate time); scatter's
+// random-search candidates are rejected after a few heavy taps (full bound
+// pass: -45 % scatter time).
 
 // pixel side of an evaluation
 struct LanePix {
@@ -772,89 +771,21 @@ __device__ __forceinline__ unsigned lane_taps(const LanePix& q, int cols) {
     return last < q.imin ? 0u : (unsigned)((last - q.imin + 1) * (q.jmax - q.jmin + 1));
 }
 
-// One step of a lane: 2R+1 taps of its candidate; returns true when the
-// candidate is finished, with its energy in *r (kBigResidual where the tap
-// weights sum below kEpsilon, +inf where it was rejected early).
-//
-// With an exit threshold a candidate first takes a bound pass: its taps by
-// descending weight (TT), accumulating a lower bound of the weighted sum with
-// round-down products and sums.  The reference forms its sum in tap order
-// with round-to-nearest fmaf over at most 81 non-negative terms, which is at
-// least (1 - 2^-17) times the exact sum of those terms, plus its start sum
-// (the hysteresis term, <= 0) scaled by at most (1 + 2^-17).  So once
-// (1 - 2^-17) * bound + that start-sum share, rounded down, reaches
-// thr2 = best * sumW rounded up, the reference-order energy is >= best and
-// the strict "<" rejects the candidate.  The heavy central taps come first,
-// so a rejection needs a few taps instead of several columns.  A candidate
-// the bound pass does not reject (a winner or a near tie) then takes the
-// exact pass: its sum in the reference's tap order, as calculateResidual
-// forms it (texSynth_kernel.cu:537-659), exiting early on the exact sum.
-// BC bounds the bound pass to its first BC groups of 2R+1 taps (the exact
-// pass follows a candidate it has not rejected by then): candidates whose
-// energy is often close to the best (propagate's) pay the bound pass without
-// being rejected by it.
-template <int R, int TM, int HW, bool EE, bool ROLL, int BC>
-__device__ __forceinline__ bool lane_step(const Params& P, const TileSmem<R, TM>& T, const TapTable<R>& TT,
-                                          const LanePix& q, LaneEval& e, bool fast, bool fastp, float* r) {
-    constexpr int K = (2 * R + 1) * (2 * R + 1);
-    constexpr int KB = BC * (2 * R + 1) < K ? BC * (2 * R + 1) : K;  // taps of the bound pass at most
-    if (!e.exact && KB == 0) {
+// One step of a lane: the next column (2R+1 taps) of its candidate in the
+// reference's order; returns true when the candidate is finished, with its
+// energy in *r (kBigResidual where the tap weights sum below kEpsilon, +inf
+// where it was rejected early).  The sum is formed as calculateResidual forms
+// it (texSynth_kernel.cu:537-659), exiting early on it.  (Propagate's
+// candidates come from coherent neighbours and mostly tie with the best, so
+// it takes this exact pass alone; scatter's chains take a bound pass first,
+// lane_step_uni below.)
+template <int R, int TM, int HW, bool EE, bool ROLL>
+__device__ __forceinline__ bool lane_step(const Params& P, const TileSmem<R, TM>& T, const LanePix& q, LaneEval& e,
+                                          bool fast, bool fastp, float* r) {
+    if (!e.exact) {
         e.exact = true;
         e.col = -R;
         e.sum = q.sum0;
-    }
-    if (EE && KB > 0 && !e.exact) {
-        bool rejected = false;
-        if constexpr (HW) {  // (the next tap's fetches issued before this tap's test, as in lane_column)
-            TapSample cur, nxt;
-            int ij = TT.ij[e.col];
-            tap_fetch<R, TM, HW>(P, q, e, (ij & 15) - R, (ij >> 4) - R, fast, fastp, &cur);
-#pragma unroll(ROLL ? 1 : 2 * R + 1)
-            for (int k = 0; k < 2 * R + 1; k++) {
-                const int pos = e.col + k;
-                if (pos >= KB) break;
-                const int i = (ij & 15) - R, j = (ij >> 4) - R;
-                const int ijn = (pos + 1 < KB && k + 1 < 2 * R + 1) ? TT.ij[pos + 1] : -1;
-                if (ijn >= 0) tap_fetch<R, TM, HW>(P, q, e, (ijn & 15) - R, (ijn >> 4) - R, fast, fastp, &nxt);
-                const bool valid = (i >= q.imin) && (i <= q.imax) && (j >= q.jmin) && (j <= q.jmax);
-                const float res = tap_finish<R, TM, HW>(P, T, q, e, i, j, cur);
-                e.sum = valid ? __fadd_rd(e.sum, __fmul_rd(res, TT.w[pos])) : e.sum;
-                if (__fadd_rd(__fmul_rd(e.sum, kBoundLo), e.s0lo) >= e.thr2) {
-                    rejected = true;
-                    break;
-                }
-                cur = nxt;
-                ij = ijn;
-            }
-        } else {
-#pragma unroll(ROLL ? 1 : 2 * R + 1)
-            for (int k = 0; k < 2 * R + 1; k++) {
-                const int pos = e.col + k;
-                if (pos >= KB) break;
-                const int ij = TT.ij[pos];
-                const int i = (ij & 15) - R, j = (ij >> 4) - R;
-                const bool valid = (i >= q.imin) && (i <= q.imax) && (j >= q.jmin) && (j <= q.jmax);
-                const float res = tap_value<R, TM, HW>(P, T, q, e, i, j, fast, fastp);
-                e.sum = valid ? __fadd_rd(e.sum, __fmul_rd(res, TT.w[pos])) : e.sum;
-                if (__fadd_rd(__fmul_rd(e.sum, kBoundLo), e.s0lo) >= e.thr2) {
-                    rejected = true;
-                    break;
-                }
-            }
-        }
-        e.col += 2 * R + 1;
-        if (rejected) {
-            if (P.counters) count_taps(P, (unsigned)min(e.col, K), q.temporal);
-            *r = INFINITY;
-            return true;
-        }
-        if (e.col >= KB) {  // not rejected: the exact pass
-            if (P.counters) count_taps(P, (unsigned)KB, q.temporal);
-            e.exact = true;
-            e.col = -R;
-            e.sum = q.sum0;
-        }
-        return false;
     }
     e.sum = lane_column<R, TM, HW, ROLL, EE>(P, T, q, e, fast, fastp);
     e.col++;
@@ -862,6 +793,78 @@ __device__ __forceinline__ bool lane_step(const Params& P, const TileSmem<R, TM>
     if (!stop && e.col <= R) return false;
     if (P.counters) count_taps(P, lane_taps<R>(q, e.col + R), q.temporal);
     *r = (q.sumW < kEpsilon) ? kBigResidual : stop ? INFINITY : e.sum / q.sumW;
+    return true;
+}
+
+// One step of a lane of scatter's chains: with an exit threshold a
+// candidate first takes a bound pass, its taps by descending weight (TT),
+// accumulating a lower bound of the weighted sum with round-down products and
+// sums.  The reference forms its sum in tap order with round-to-nearest fmaf
+// over at most 81 non-negative terms, which is at least (1 - 2^-17) times the
+// exact sum of those terms, plus its start sum (the hysteresis term, <= 0)
+// scaled by at most (1 + 2^-17).  So once (1 - 2^-17) * bound + that
+// start-sum share, rounded down, reaches thr2 = best * sumW rounded up, the
+// reference-order energy is >= best and the strict "<" rejects the
+// candidate.  The heavy central taps come first, so a rejection needs a few
+// taps instead of several columns.  A candidate the bound pass does not
+// reject (a winner or a near tie) then takes the exact pass, lane_step's.
+// Both passes share one loop body: a step is up to 2R+1 taps, by descending
+// weight (bound pass: round-down products and sums, the bound test) or the
+// next column in the reference's order (exact pass: fmaf, the exact test),
+// chosen per lane by data, so the lanes of a warp in different passes issue
+// the same instructions instead of the two passes' code in turn.
+template <int R, int TM, int HW>
+__device__ __forceinline__ bool lane_step_uni(const Params& P, const TileSmem<R, TM>& T, const TapTable<R>& TT,
+                                              const LanePix& q, LaneEval& e, bool fast, bool fastp, float* r) {
+    constexpr int K = (2 * R + 1) * (2 * R + 1);
+    const bool bound = !e.exact;
+    bool hit = false;  // the pass's test reached its threshold
+    int done = 0;      // taps of this step
+#pragma unroll 1
+    for (int k = 0; k < 2 * R + 1; k++) {
+        const int pos = e.col + k;
+        if (bound && pos >= K) break;
+        int i, j;
+        float w;
+        if (bound) {
+            const int ij = TT.ij[pos];
+            i = (ij & 15) - R;
+            j = (ij >> 4) - R;
+            w = TT.w[pos];
+        } else {
+            i = e.col;
+            j = k - R;
+            w = P.gauss[i + R] * P.gauss[j + R];
+        }
+        const bool valid = (i >= q.imin) && (i <= q.imax) && (j >= q.jmin) && (j <= q.jmax);
+        const float res = tap_value<R, TM, HW>(P, T, q, e, i, j, fast, fastp);
+        const float sb = __fadd_rd(e.sum, __fmul_rd(res, w));
+        const float sx = fmaf(res, w, e.sum);
+        e.sum = valid ? (bound ? sb : sx) : e.sum;
+        done = k + 1;
+        hit = bound ? (__fadd_rd(__fmul_rd(e.sum, kBoundLo), e.s0lo) >= e.thr2) : (e.sum >= e.thr2);
+        if (hit) break;
+    }
+    if (bound) {
+        e.col += 2 * R + 1;
+        if (hit) {
+            if (P.counters) count_taps(P, (unsigned)min(e.col, K), q.temporal);
+            *r = INFINITY;
+            return true;
+        }
+        if (e.col >= K) {  // not rejected: the exact pass
+            if (P.counters) count_taps(P, (unsigned)K, q.temporal);
+            e.exact = true;
+            e.col = -R;
+            e.sum = q.sum0;
+        }
+        return false;
+    }
+    (void)done;
+    e.col++;
+    if (!hit && e.col <= R) return false;
+    if (P.counters) count_taps(P, lane_taps<R>(q, e.col + R), q.temporal);
+    *r = (q.sumW < kEpsilon) ? kBigResidual : hit ? INFINITY : e.sum / q.sumW;
     return true;
 }
 
@@ -898,7 +901,6 @@ __global__ void __launch_bounds__(kTileThreads * WIDE, WIDE == 1 ? 2 : 1)
     __shared__ TileSmem<R, TM> T;
     __shared__ PixShared S;
     __shared__ PropQueue Q;
-    __shared__ TapTable<R> TT;
     // Change tracking: a candidate whose source record and whose target's
     // patch window are unchanged since the previous pass with this jump was
     // rejected there against the same residual and is skipped (bit cdx of
@@ -921,7 +923,6 @@ __global__ void __launch_bounds__(kTileThreads * WIDE, WIDE == 1 ? 2 : 1)
         if (block_idle(P, work, need, in, k)) return;
     }
     if (pid < kTileH) { Q.count[pid] = 0; Q.next[pid] = 0; }
-    load_tap_table<R>(P, TT);
     PixT px;
     bool abort;
     const bool in = stage_tile<R, TM, kTileThreads * WIDE>(P, M, T, &px, &abort);  // (synchronises the block)
@@ -1037,7 +1038,7 @@ __global__ void __launch_bounds__(kTileThreads * WIDE, WIDE == 1 ? 2 : 1)
             const bool fastp = TM ? __all_sync(kFull, !act || !q.temporal || q.prev_fast) : true;
             if (act) {
                 float r;
-                if (lane_step<R, TM, HW, true, false, kPropagateBoundGroups>(P, T, TT, q, e, fast, fastp, &r)) {
+                if (lane_step<R, TM, HW, true, false>(P, T, q, e, fast, fastp, &r)) {
                     Q.ca[cur].x = r;
                     act = false;
                 }
@@ -1221,7 +1222,7 @@ __global__ void __launch_bounds__(kTileThreads, 2) kt_scatter_q(const Params P, 
         const bool fastp = TM ? __all_sync(kFull, !act || !q.temporal || q.prev_fast) : true;
         if (act) {
             float r;
-            if (lane_step<R, TM, HW, true, true, 2 * R + 1>(P, T, TT, q, e, fast, fastp, &r)) {
+            if (lane_step_uni<R, TM, HW>(P, T, TT, q, e, fast, fastp, &r)) {
                 if (r < best) {
                     best = r;
                     owx = e.cx; owy = e.cy; owt = cur_t; wkind = cur_avg ? 2 : 1;
