@@ -819,7 +819,6 @@ __device__ __forceinline__ bool lane_step_uni(const Params& P, const TileSmem<R,
     constexpr int K = (2 * R + 1) * (2 * R + 1);
     const bool bound = !e.exact;
     bool hit = false;  // the pass's test reached its threshold
-    int done = 0;      // taps of this step
 #pragma unroll 1
     for (int k = 0; k < 2 * R + 1; k++) {
         const int pos = e.col + k;
@@ -841,7 +840,6 @@ __device__ __forceinline__ bool lane_step_uni(const Params& P, const TileSmem<R,
         const float sb = __fadd_rd(e.sum, __fmul_rd(res, w));
         const float sx = fmaf(res, w, e.sum);
         e.sum = valid ? (bound ? sb : sx) : e.sum;
-        done = k + 1;
         hit = bound ? (__fadd_rd(__fmul_rd(e.sum, kBoundLo), e.s0lo) >= e.thr2) : (e.sum >= e.thr2);
         if (hit) break;
     }
@@ -860,7 +858,6 @@ __device__ __forceinline__ bool lane_step_uni(const Params& P, const TileSmem<R,
         }
         return false;
     }
-    (void)done;
     e.col++;
     if (!hit && e.col <= R) return false;
     if (P.counters) count_taps(P, lane_taps<R>(q, e.col + R), q.temporal);
